@@ -1,0 +1,383 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 patchy-Langevin step: particle-steps/s on the batched-replica workload.
+
+Workload (default): 512 independent replicas, N_r log-uniform in [1,024, 32,768] (about 4.7 M particles),
+4 tetrahedral patches, phi 0.15, kT_r ~ U[0.8, 1.2], depth_r ~ U[6, 10], range 1.2, cos 0.90, dt 0.005,
+FP32 state with FP64 reductions, cell list rebuilt every step, one CUDA-graph launch per step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mtcode|reference]
+
+One JSON line on rank 0.  ``value``: particle-steps/s of the device-resident step (all ranks);
+``e2e``: the same metric through the C ABI with host buffers (state upload, per-step temperature
+read-back as Condensate::run does, final state download) inside the timed region.  ``roofline``: the
+dominant kernel's algorithmic bytes / its CUDA-event time against the measured HBM copy bandwidth.
+``cpu_baseline``: the oracle (CPU restatement of the reference step) on a bounded sample, all host cores.
+Multi-GPU: replicas only -- each rank runs its own full replica set (weak scaling), no collective on the
+data path; the barrier and the max-over-ranks time use torch.distributed.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-steps/s on 1 GB300, batched FP32 vs plain FP64, force rel err <=1e-5"
+UNIT = "particle-steps/s"
+# algorithmic bytes per particle (FP32 rows of 48 B)
+BYTES_FORCE = 48 + 24 + 4 + 48 + 8 + 4          # own x,Q + p,L + id; write p,L,F~,T~ + bin + histogram
+BYTES_SCATTER = 8 + 4 + 48 + 48 + 4 + 24 + 48 + 24 + 4 + 24  # bin,start,row,row,id,disp -> row,p+L,id,disp
+BYTES_SCAN_PER_CELL = 16
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return rank, world, local
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def dist_max(world, value: float) -> float:
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else torch.device("cpu")
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def shard_replicas(n_replicas: int, rank: int, world: int) -> list:
+    """Replica indices a rank owns when a fixed set is split (contiguous blocks)."""
+    per = n_replicas // world
+    extra = n_replicas % world
+    start = rank * per + min(rank, extra)
+    return list(range(start, start + per + (1 if rank < extra else 0)))
+
+
+def make_workload(args, rank: int):
+    from mtcode_gb300 import workloads
+    if args.workload == "c4":
+        return workloads.patchy_c4(seed=args.seed + rank, n_replicas=args.replicas)
+    return workloads.WORKLOADS[args.workload](seed=args.seed + rank)
+
+
+# ---------------------------------------------------------------- CPU side (oracle port)
+def cpu_sample_rate(W, n_reps: int, steps: int, threads: int) -> dict:
+    """Oracle port of the reference step on a bounded sample: the first n_reps replicas, `steps` steps
+    each, one replica per host thread (the reference's own scale-out is one process per system)."""
+    from oracle import pyoracle as po
+    po.orc()
+    reps = W.replicas[:n_reps]
+    offs = np.concatenate([[0], np.cumsum([r.n for r in W.replicas])])
+
+    def one(r):
+        spec = reps[r]
+        sysm = po.System(spec)
+        a, b = offs[r], offs[r + 1]
+        st = dict(x=np.ascontiguousarray(W.x[a:b]), p=np.zeros((spec.n, 3)), Lb=np.zeros((spec.n, 3)),
+                  Q=np.ascontiguousarray(W.Q[a:b]))
+        st["Ft"], st["Tt"] = sysm.init_forces(st["x"], st["p"], st["Lb"], st["Q"])
+        t0 = time.perf_counter()
+        sysm.run(st, steps, noise_mode=2, seed=spec.seed, replica=r, draw0=1, check_skin=False)
+        return spec.n * steps, time.perf_counter() - t0
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        res = list(ex.map(one, range(len(reps))))
+    wall = time.perf_counter() - t0
+    ps = sum(r[0] for r in res)
+    cpu_s = sum(r[1] for r in res)
+    return {"value": ps / wall, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(reps)} of {len(W.replicas)} replicas ({ps // steps} particles) x {steps} steps, "
+                      f"one replica per thread, {cpu_s:.1f} s of CPU work"}
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the oracle port of the reference's CPU step (the reference's own build cannot travel
+    to the GPU host), all host threads, each step a bounded sample of the same workload."""
+    if rank != 0:
+        return
+    W = make_workload(args, 0)
+    threads = os.cpu_count() or 1
+    # each timed step advances a sample of 2 replicas per host thread by one step, in parallel
+    n_reps = min(len(W.replicas), 2 * threads)
+    steps = max(1, args.steps)
+    cpu_sample_rate(W, min(n_reps, threads), max(1, args.warmup), threads)  # untimed warm-up
+    t0 = time.perf_counter()
+    cb = cpu_sample_rate(W, n_reps, steps, threads)
+    elapsed = time.perf_counter() - t0
+    value = cb["value"]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": f"{args.workload}: {len(W.replicas)} patchy replicas, {W.n_total} particles",
+                       "sample": cb["sample"]},
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU side
+def run_gpu(args, rank, world, local):
+    import torch
+    from mtcode_gb300 import LangevinNVTRGPU
+
+    torch.cuda.set_device(local)
+    W = make_workload(args, rank)
+    n = W.n_total
+    z = np.zeros((n, 3))
+    s = LangevinNVTRGPU(W.replicas, precision=args.precision, device=local)
+    s.initialize(W.x, z, z, W.Q)
+    s.init_forces()
+    s.step(max(args.warmup, 3))
+    s.sync()
+    stream = torch.cuda.ExternalStream(s.stream, device=torch.device("cuda", local))
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+
+    # ---- device-resident timed region
+    dist_barrier(world)
+    torch.cuda.synchronize()
+    l0 = s.launches
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        s.step(args.steps)
+        ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.synchronize()
+    dist_barrier(world)
+    launches = s.launches - l0
+    ms = ev0.elapsed_time(ev1)
+    ms = dist_max(world, ms)
+    s.sync()
+    value = world * n * args.steps / (ms / 1e3)
+
+    # ---- per-kernel device times (instrumented steps, same stream) -> roofline of the dominant kernel
+    prof_steps = max(5, min(50, args.steps // 4))
+    prof = s.step_profile(prof_steps)
+    total_prof = sum(prof.values())
+    ncells = None
+    per_launch = {k: v / prof_steps for k, v in prof.items()}
+    dominant = max(per_launch, key=per_launch.get)
+    bytes_per = {"force": BYTES_FORCE * n, "scatter": BYTES_SCATTER * n}
+    pk = peaks()
+    alg = bytes_per.get(dominant)
+    achieved = alg / (per_launch[dominant] / 1e3) / 1e9 if alg else None
+    roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": (achieved / pk["hbm_gbs"]) if achieved else None, "traffic": None,
+                "peak_source": pk["source"],
+                "kernel_ms_per_step": {k: round(v, 5) for k, v in per_launch.items()},
+                "share": {k: round(v / total_prof, 4) for k, v in prof.items()},
+                "algorithmic_bytes_per_particle": {"force": BYTES_FORCE, "scatter": BYTES_SCATTER}}
+    if "scatter" in per_launch:
+        a2 = BYTES_SCATTER * n / (per_launch["scatter"] / 1e3) / 1e9
+        roofline["scatter_gbs"] = a2
+        roofline["scatter_frac"] = a2 / pk["hbm_gbs"]
+
+    # ---- end to end through the C ABI with host buffers
+    e2e = run_e2e(s, W, args, stream, ev0, ev1)
+    e2e["value"] = dist_max(world, -e2e["value"]) * -1 if world > 1 else e2e["value"]
+
+    # ---- plain FP64 single-system path on a sample of the same replicas
+    plain = run_plain_fp64(W, args, local) if args.plain_fp64 and rank == 0 else None
+
+    cpu = None
+    if rank == 0 and world == 1 and args.cpu_baseline:
+        threads = os.cpu_count() or 1
+        cpu = cpu_sample_rate(W, min(len(W.replicas), args.cpu_replicas), args.cpu_steps, threads)
+    s.close()
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "fp32" if args.precision == "fp32" else "f64",
+                "data": "synthetic (seeded)",
+                "config": {"workload": f"{args.workload}: {len(W.replicas)} patchy replicas, {n} particles per GPU",
+                           "replicas": len(W.replicas), "particles_per_gpu": n, "precision": args.precision,
+                           "l2": "inputs larger than L2 (state ~%d MB per GPU)" % (n * 250 // 2 ** 20),
+                           "parallelism": f"replicas x{world}"},
+                "gpu_launches": launches, "clocks": clk.summary(), "roofline": roofline, "e2e": e2e,
+                "cpu_baseline": cpu, "plain_fp64": plain}
+        print(json.dumps(line), flush=True)
+
+
+def run_e2e(s, W, args, stream, ev0, ev1) -> dict:
+    import torch
+    n = W.n_total
+    R = len(W.replicas)
+    state = s.get_state()
+    pinned = {k: torch.empty(v.shape, dtype=torch.float64, pin_memory=True).numpy() for k, v in state.items()}
+    for k in pinned:
+        pinned[k][...] = state[k]
+    temps = torch.empty((R, 6), dtype=torch.float64, pin_memory=True).numpy()
+    out = {k: torch.empty(v.shape, dtype=torch.float64, pin_memory=True).numpy() for k, v in state.items()}
+    k_e2e = max(10, args.steps // 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    s.initialize(pinned["x"], pinned["p"], pinned["Lb"], pinned["Q"], pinned["Ft"], pinned["Tt"])
+    for _ in range(k_e2e):
+        s.step(1)
+        temps[...] = s.measured_temperature()
+    st = s.get_state()
+    ev1.record(stream)
+    ev1.synchronize()
+    wall = time.perf_counter() - t0
+    h2d = n * (3 + 3 + 3 + 9 + 3 + 3) * 8
+    d2h_state = n * (3 + 3 + 3 + 9 + 3 + 3) * 8
+    return {"value": n * k_e2e / wall, "unit": UNIT, "h2d_bytes_per_step": h2d / k_e2e,
+            "d2h_bytes_per_step": R * 6 * 8 + d2h_state / k_e2e, "steps": k_e2e,
+            "what": "mtg_set_state (host FP64 state) + per step: mtg_step(1) + mtg_temperature (read-back) "
+                    "+ mtg_get_state at the end"}
+
+
+def run_plain_fp64(W, args, device) -> dict:
+    """The plain FP64 single-system path: one replica per handle, FP64, one after another."""
+    from mtcode_gb300 import LangevinNVTRGPU
+    import torch
+    offs = np.concatenate([[0], np.cumsum([r.n for r in W.replicas])])
+    reps = list(range(min(len(W.replicas), args.plain_replicas)))
+    steps = args.plain_steps
+    total_ps, total_s = 0, 0.0
+    for r in reps:
+        spec = W.replicas[r]
+        a, b = offs[r], offs[r + 1]
+        with LangevinNVTRGPU([spec], precision="fp64", device=device, track_displacement=False) as s:
+            z = np.zeros((spec.n, 3))
+            s.initialize(W.x[a:b], z, z, W.Q[a:b])
+            s.init_forces()
+            s.step(3)
+            s.sync()
+            stream = torch.cuda.ExternalStream(s.stream)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.step(steps)
+            e1.record(stream)
+            e1.synchronize()
+            total_s += e0.elapsed_time(e1) / 1e3
+            total_ps += spec.n * steps
+    return {"value": total_ps / total_s, "unit": UNIT, "dtype": "f64",
+            "sample": f"{len(reps)} replicas of the workload, each alone in its own FP64 handle, {steps} steps"}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["mtcode", "reference"], default="mtcode")
+    ap.add_argument("--workload", default="c4", choices=["c1", "c2", "c3", "c4"])
+    ap.add_argument("--replicas", type=int, default=512)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--cpu-replicas", type=int, default=128)
+    ap.add_argument("--cpu-steps", type=int, default=5)
+    ap.add_argument("--no-plain-fp64", dest="plain_fp64", action="store_false")
+    ap.add_argument("--plain-replicas", type=int, default=16)
+    ap.add_argument("--plain-steps", type=int, default=20)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,200 @@
+/*
+ * mtcode_gb300.h -- C ABI of the GB300 (sm_103a) rotational-Langevin step for patchy spheres.
+ *
+ * This is the drop-in boundary for the per-timestep hot path of osmanovicdino/mtcode: cell-list
+ * construction, the WCA-core + Kern-Frenkel patch force/torque loop, and the translational and
+ * rotational Langevin update.  The reference has no FFI of its own (every executable #includes the
+ * C++ sources); the entry points below are what its C++ classes forward to through the header-only
+ * adapter include/LangevinNVTRGPU.hpp.  Each entry point names the reference routine it replaces.
+ *
+ * Conventions (identical to the reference's row-major matrix<double> layout, DataStructures/matrix2.h:24-40):
+ *   x, p, F   n x 3 doubles, lab frame
+ *   Lb, T~    n x 3 doubles, BODY frame (angular momentum / carried torque)
+ *   Q         n x 9 doubles, lab -> body rotation; patch direction in the lab frame = Q^T n_body
+ *   noise     n x 6 doubles, mean 0, variance 1 (matrix2.cpp:1807-1821)
+ * Several independent replicas ("systems") live in one handle; host arrays for all replicas are
+ * concatenated replica after replica, each replica's rows in its own particle order.
+ *
+ * Errors: every call returns an mtg_status; nothing exits or reads stdin (the reference's error()
+ * and pausel(), Basic/basic.h:61-99, block on stdin).  Device-side conditions (non-finite state,
+ * a |pair force| above the reference's 1e4 pause threshold) are latched on the device and reported
+ * by the next synchronising call (mtg_sync, mtg_get_state, mtg_temperature, ...).
+ * Threading: one host thread per handle; calls are ordered on the handle's CUDA stream.
+ */
+#ifndef MTCODE_GB300_H
+#define MTCODE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MTG_API_VERSION 1
+
+typedef enum {
+    MTG_OK = 0,
+    MTG_ERR_ARG = 1,          /* invalid argument */
+    MTG_ERR_CUDA = 2,         /* CUDA runtime failure (mtg_last_error has the text) */
+    MTG_ERR_NOMEM = 3,        /* device allocation failed */
+    MTG_ERR_STATE = 4,        /* call order violated (e.g. a step before any state was set) */
+    MTG_ERR_NONFINITE = 5,    /* a position, force or torque became NaN/Inf on the device */
+    MTG_ERR_CAPACITY = 6,     /* a caller buffer is too small; the size needed is returned */
+    MTG_ERR_TIMEOUT = 7,      /* a bounded device-side wait expired */
+    MTG_ERR_NODEVICE = 8      /* no usable sm_103 device */
+} mtg_status;
+
+typedef enum { MTG_FP32 = 0, MTG_FP64 = 1 } mtg_precision;
+
+/* device-latched condition bits, read with mtg_flags() */
+#define MTG_FLAG_NONFINITE   0x1u   /* see MTG_ERR_NONFINITE */
+#define MTG_FLAG_FORCE_LIMIT 0x2u   /* some |pair force| > 1e4: where MD.cpp:1711-1749 would pausel() */
+
+typedef struct mtg_system mtg_system;
+
+/* Patch model in GeneralPatch form (MDBase/Potentials/ComboPatch/GeneralPatch.cpp:7-121).
+ * TetrahedralPatch(att, dis, thetam) (TetrahedralPatch.cpp:4-44) and BivalentPatch
+ * (BivalentPatch.cpp:4-34) are one-type special cases; mtg_model_tetrahedral / mtg_model_bivalent
+ * fill this struct for them.  Potentials are ordered type pair (k1 <= k2), then patch of k1, then
+ * patch of k2, exactly as GeneralPatch enumerates potential_bundle. */
+#define MTG_MAX_TYPES 4
+#define MTG_MAX_ORIENT 16
+#define MTG_MAX_POTS 64
+typedef struct {
+    int n_types;
+    int patches_per_type[MTG_MAX_TYPES];
+    int count_per_type[MTG_MAX_TYPES];    /* cumulative particle counts (GeneralPatch num_per_type) */
+    double orient[MTG_MAX_ORIENT][3];     /* body-frame patch unit vectors, types contiguous */
+    double params[MTG_MAX_POTS][3];       /* (att, dis, thetam) per potential (KernFrenkelOnePatch2) */
+} mtg_patch_model;
+
+/* One independent system: cube(box, pb, 3) + LangevinNVTR parameters + HSPotential + ComboPatch. */
+typedef struct {
+    int n;                 /* particles */
+    double box;            /* cube::l */
+    int periodic;          /* 1: periodic (all three axes); 0: reflecting walls */
+    double dt;             /* LangevinNVTR::setdt */
+    double kT;             /* setkT */
+    double gamma;          /* setgamma   (translational friction) */
+    double gammar;         /* setgammar  (rotational friction) */
+    double mass;           /* LangevinNVT::m (reference default 1) */
+    double inertia;        /* isotropic moment of inertia (reference default 0.25*2/5 = 0.1) */
+    double hs_eps;         /* HSPotential(eps, sigma): WCA core, potential.h:79-162 */
+    double hs_sigma;
+    double max_dist2;      /* LangevinNVTR::max_distance_check (reference default 2.4) */
+    uint64_t seed;         /* Philox key of this replica's noise stream */
+    mtg_patch_model model;
+} mtg_replica_desc;
+
+typedef struct {
+    int precision;                     /* mtg_precision */
+    int n_replicas;
+    const mtg_replica_desc *replicas;
+    int device;                        /* CUDA device ordinal */
+    int track_displacement;            /* 1: keep FP64 unwrapped-displacement accumulators */
+} mtg_config;
+
+/* Fill `m` with TetrahedralPatch(att, dis, thetam) / BivalentPatch(att, dis, thetam). */
+void mtg_model_tetrahedral(mtg_patch_model *m, double att, double dis, double thetam);
+void mtg_model_bivalent(mtg_patch_model *m, double att, double dis, double thetam);
+/* Reference defaults: dt 0.005, kT 1, gamma = gammar = 1, m 1, I 0.1, HS(1,1), max_dist2 2.4. */
+void mtg_replica_defaults(mtg_replica_desc *r);
+
+/* Create / destroy a handle.  Replaces constructing LangevinNVTR(cube&) + setdt/setkT/setgamma/
+ * setgammar (LangevinR.cpp:41-69, LangevinR.h:109-134) and binding a ComboPatch. */
+mtg_status mtg_create(const mtg_config *cfg, mtg_system **out);
+void mtg_destroy(mtg_system *h);
+
+/* Total particles over all replicas; particle offset of replica r. */
+int64_t mtg_num_particles(const mtg_system *h);
+int64_t mtg_replica_offset(const mtg_system *h, int replica);
+
+/* LangevinNVTR::initialize(x, p, Q, Lb) (LangevinR.cpp:309-325) for all replicas at once.
+ * Ft/Tt (the carried F~ lab / T~ body of Condensate::run) may be NULL: they are then zero and
+ * mtg_init_forces() should be called before the first step. */
+mtg_status mtg_set_state(mtg_system *h, const double *x, const double *p, const double *Lb, const double *Q,
+                         const double *Ft, const double *Tt);
+/* getdat/getmom/getangmom/getorientation (LangevinR.h:190-196) + the carried F~, T~; any may be NULL. */
+mtg_status mtg_get_state(mtg_system *h, double *x, double *p, double *Lb, double *Q, double *Ft, double *Tt);
+
+/* Condensate.cpp:312-334: F = calculateforces(HS) + calculate_forces_and_torques3D(ComboPatch),
+ * then create_forces_and_torques_sphere(F, T, one noise draw) -> carried F~, T~. */
+mtg_status mtg_init_forces(mtg_system *h);
+/* Same, with the noise of that draw supplied by the caller (total particles x 6, host memory):
+ * create_forces_and_torques_sphere(F, T, RT) with the caller's RT (LangevinR.cpp:580-592). */
+mtg_status mtg_init_forces_noise(mtg_system *h, const double *noise);
+
+/* nsteps of the Condensate::run loop body (Condensate.cpp:335-378) with counter-based Philox noise:
+ * advancemom_halfstep -> advance_pos -> rotate -> cell list -> forces+torques -> noise+friction
+ * (create_forces_and_torques_sphere) -> advancemom_halfstep.  The cell list is rebuilt every step
+ * and covers every pair within the force range exactly.  Asynchronous. */
+mtg_status mtg_step(mtg_system *h, int nsteps);
+/* Same, with the noise supplied by the caller instead of Philox: noise holds nsteps blocks of
+ * (total particles x 6) values, replaces generate_uniform_random_matrix (matrix2.cpp:1807-1821). */
+mtg_status mtg_step_noise(mtg_system *h, int nsteps, const double *noise);
+
+/* Forces at the current state without advancing it:
+ * F = MD::calculateforces(pairs, HSPotential) (MD.cpp:1684-1764) plus the patch forces, and
+ * T = the lab-frame torques of LangevinNVTR::calculate_forces_and_torques3D (LangevinR.cpp:911-1047).
+ * energy (nullable): per-particle potential energy, half of every pair energy (WCA + KF2). */
+mtg_status mtg_forces(mtg_system *h, double *F, double *T, double *energy);
+
+/* MD::calculatepairs_parallel(boxlist, rc) (MD.cpp:1100-1176) for one replica: every pair (i < j,
+ * local indices) with minimum-image distance < rc, sorted by (i, j).  The cell grid is rebuilt at
+ * side >= rc for this call.  If *npairs > cap on return, nothing beyond cap was written and the call
+ * returns MTG_ERR_CAPACITY. */
+mtg_status mtg_pairs(mtg_system *h, int replica, double rc, int32_t *pairs, int64_t cap, int64_t *npairs);
+
+/* LangevinNVTR::measured_temperature (LangevinR.cpp:170-193), per replica: 6 doubles
+ * (<p_k^2/2m>, <L_k^2/2I>, k = x,y,z).  out: n_replicas x 6. Synchronising. */
+mtg_status mtg_temperature(mtg_system *h, double *out);
+
+/* Per-replica FP64 observables at the current state, out: n_replicas x MTG_OBS_COUNT:
+ *  [0] KF2 patch energy, [1] WCA energy (+eps shifted, r < 1.12246 sigma), [2] virial sum r.f,
+ *  [3] bonded patch pairs (LangevinNVTR::calculate_bound_pairs criterion, LangevinR.cpp:1854-1998),
+ *  [4] pairs within the force range.  Synchronising. */
+#define MTG_OBS_COUNT 5
+mtg_status mtg_observables(mtg_system *h, double *out);
+
+/* FP64 unwrapped displacement accumulated since the last mtg_set_state (total particles x 3). */
+mtg_status mtg_get_displacement(mtg_system *h, double *disp);
+
+/* Number of noise draws consumed so far (mtg_init_forces and every step each consume one);
+ * set it to resume a run bit-reproducibly. */
+uint64_t mtg_get_draw(const mtg_system *h);
+mtg_status mtg_set_draw(mtg_system *h, uint64_t draw);
+
+/* Waits for the handle's stream and reports latched device conditions. */
+mtg_status mtg_sync(mtg_system *h);
+uint32_t mtg_flags(mtg_system *h);
+void mtg_clear_flags(mtg_system *h);
+
+/* The handle's cudaStream_t (as void*). */
+void *mtg_stream(mtg_system *h);
+
+/* Kernel launches issued on this handle so far (every entry point counts its own launches). */
+int64_t mtg_launch_count(const mtg_system *h);
+
+/* Instrumented steps: nsteps of mtg_step launched one kernel at a time (no graph) with CUDA events
+ * around every launch on the handle's stream.  kernel_ms[k] receives the summed device time of
+ * kernel k over the nsteps, for k = 0 scan_reduce, 1 scan_top, 2 scan_down, 3 scatter (reorder +
+ * first half-step), 4 force (force/torque + Langevin epilogue + next binning).  Synchronising. */
+#define MTG_PROFILE_KERNELS 5
+mtg_status mtg_step_profile(mtg_system *h, int nsteps, double *kernel_ms);
+
+/* Text of the last error on this handle (or of the last failed mtg_create when h is NULL). */
+const char *mtg_last_error(const mtg_system *h);
+const char *mtg_status_string(int status);
+int mtg_api_version(void);
+
+/* Host-side seeded synthetic inputs (no GPU use).
+ * mtg_random_positions: uniform in [0, box)^3 with non-overlap rejection at min_dist (minimum image
+ * when periodic); returns MTG_ERR_ARG if the packing cannot be reached in 1000*n attempts.
+ * mtg_random_rotations: uniform random rotations, the construction of LangevinR.cpp:239-267. */
+mtg_status mtg_random_positions(int n, double box, int periodic, double min_dist, uint64_t seed, double *x);
+void mtg_random_rotations(int n, uint64_t seed, double *Q);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MTCODE_GB300_H */

@@ -1,0 +1,322 @@
+// mtg_device.cuh -- device-side data layout and per-pair physics of the GB300 patchy-Langevin step.
+//
+// HBM layout (one handle, all replicas concatenated; "slot" = position in cell-sorted order):
+//   payload[slot]  12 reals  (x, y, z, Q0 | Q1..Q4 | Q5..Q8)          read by every neighbour
+//   motion[slot]   12 reals  (px, py, pz, Lx | Ly, Lz, F~x, F~y | F~z, T~x, T~y, T~z)
+//   ident[slot]    int32 global particle index (replica offset + reference particle index)
+//   disp_{x,y,z}   FP64 unwrapped displacement (SoA, optional)
+//   bin[slot]      int2 (global cell, rank inside the cell) of the particle's NEXT position
+//   cell_count / cell_start   per global cell (replica cell blocks are contiguous)
+// Every row is 48 B (FP32) or 96 B (FP64), so rows are 16-byte aligned and move as float4/double2.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mtg {
+
+constexpr int kMaxTypes = 4;
+constexpr int kMaxOrient = 16;
+constexpr int kMaxPots = 64;
+constexpr int kRow = 12;  // reals per payload / motion row
+
+// ------------------------------------------------------------------ per-replica constants
+template <class real>
+struct Replica {
+    int n;            // particles
+    int off;          // first slot / global particle index
+    int cell_off;     // first global cell
+    int nc;           // cells per side of the force grid
+    int periodic;
+    int model;        // index into the model table
+    uint32_t seed_lo, seed_hi;
+    real box, half_box, l2s;   // cube::l, l/2, (l/2)^2
+    real cell_scale;           // nc / box  (cube::assign_box: n * x / l)
+    real dt, half_dt, c1;      // dt, dt/2, dt/m
+    real fric_t, fric_r;       // -gamma/m, -gammar/I
+    real Rt, Rr;               // sqrt(2 gamma kT / dt), sqrt(2 gammar kT / dt)
+    real inertia;
+    real hs_limit, hs_4eps, hs_s6, hs_s12, hs_eps;  // HSPotential: 1.12246 sigma, 4 eps, sigma^6, sigma^12
+    real max_dist2;            // LangevinNVTR::max_distance_check
+    real rc2;                  // squared force range (max of HS range and patch range)
+    real patch_r2;             // squared range of any patch force: min(max_dist2, (1.4 dis_max)^2)
+    real bond_r;               // ComboPatch::max_check
+};
+
+// ------------------------------------------------------------------ patch model (GeneralPatch form)
+template <class real>
+struct Model {
+    int n_types;
+    int np[kMaxTypes];            // patches per type
+    int ncum[kMaxTypes];          // cumulative particle counts
+    int ooff[kMaxTypes];          // first orientation row of each type
+    int pstart[kMaxTypes][kMaxTypes];  // first potential of type pair (k1 <= k2)
+    real orient[kMaxOrient][3];
+    real att[kMaxPots], dis[kMaxPots], inv_dis[kMaxPots], rmax[kMaxPots], costm[kMaxPots], kfac[kMaxPots];
+    real mincos[kMaxTypes][kMaxTypes];  // smallest cos(thetam) of a type pair (early cone reject)
+};
+
+// ------------------------------------------------------------------ vector moves of 12-real rows
+template <class real> struct Row;
+template <> struct Row<float> {
+    float v[12];
+    __device__ __forceinline__ void load(const float *p) {
+        const float4 *q = reinterpret_cast<const float4 *>(p);
+        float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+        v[8] = c.x; v[9] = c.y; v[10] = c.z; v[11] = c.w;
+    }
+    __device__ __forceinline__ void store(float *p) const {
+        float4 *q = reinterpret_cast<float4 *>(p);
+        q[0] = make_float4(v[0], v[1], v[2], v[3]);
+        q[1] = make_float4(v[4], v[5], v[6], v[7]);
+        q[2] = make_float4(v[8], v[9], v[10], v[11]);
+    }
+};
+template <> struct Row<double> {
+    double v[12];
+    __device__ __forceinline__ void load(const double *p) {
+        const double2 *q = reinterpret_cast<const double2 *>(p);
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            double2 a = __ldg(q + k);
+            v[2 * k] = a.x; v[2 * k + 1] = a.y;
+        }
+    }
+    __device__ __forceinline__ void store(double *p) const {
+        double2 *q = reinterpret_cast<double2 *>(p);
+#pragma unroll
+        for (int k = 0; k < 6; k++) q[k] = make_double2(v[2 * k], v[2 * k + 1]);
+    }
+};
+
+// position only (first 16 bytes of a payload row for FP32, first 32 for FP64)
+__device__ __forceinline__ void load_pos(const float *p, float &x, float &y, float &z) {
+    float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+    x = a.x; y = a.y; z = a.z;
+}
+__device__ __forceinline__ void load_pos(const double *p, double &x, double &y, double &z) {
+    double2 a = __ldg(reinterpret_cast<const double2 *>(p));
+    x = a.x; y = a.y; z = __ldg(p + 2);
+}
+
+// ------------------------------------------------------------------ correctly rounded, uncontracted ops
+// The integrator uses explicit roundings so that the binning pass and the scatter pass compute the
+// identical next position, and so that the FP64 path rounds like the reference's x + c1 * p.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
+template <class real> __device__ __forceinline__ real rsqrt_(real a);
+template <> __device__ __forceinline__ float rsqrt_(float a) { return rsqrtf(a); }
+template <> __device__ __forceinline__ double rsqrt_(double a) { return 1.0 / sqrt(a); }
+
+// fasterfloor (Basic/basic.h:58)
+template <class real>
+__device__ __forceinline__ int fasterfloor(real x) { return x > real(0) ? (int)x : (int)x - 1; }
+
+// cube::assign_box (geometry.h:508-520) for one axis
+template <class real>
+__device__ __forceinline__ int axis_cell(real x, real scale, int nc) {
+    int m = fasterfloor<real>(mul_rn(x, scale));
+    m = m < 0 ? 0 : m;
+    return m > nc - 1 ? nc - 1 : m;
+}
+
+// cube::correct_position_and_momentum (geometry.h:403-446) for one coordinate.  The periodic wrap
+// repeats like the reference's while-loops but is bounded (a non-finite coordinate is left as is
+// and reported by the caller).
+template <class real>
+__device__ __forceinline__ void wrap_coord(real &x, real &p, real l, int periodic) {
+    if (periodic) {
+        if (x < real(0)) {
+            for (int it = 0; it < 8 && x < real(0); it++) x = add_rn(x, l);
+        } else if (x > l) {
+            for (int it = 0; it < 8 && x > l; it++) x = sub_rn(x, l);
+        }
+    } else {
+        if (x < real(0)) { x = -x; p = -p; }
+        else if (x > l) { x = sub_rn(l, sub_rn(x, l)); p = -p; }
+    }
+}
+
+// minimum image as cube::distance_vector (geometry.h:277-294): one correction when dx^2 > (l/2)^2
+template <class real>
+__device__ __forceinline__ real min_image(real dx, real l, real l2s, int periodic) {
+    if (periodic && dx * dx > l2s) dx = dx >= real(0) ? dx - l : dx + l;
+    return dx;
+}
+
+// ------------------------------------------------------------------ Philox4x32-10
+// Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3" (SC'11).
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// Six unit-variance uniform values for (particle, replica, draw):
+// xi = 3.464101615 u - 1.732050808, u = (w >> 8) 2^-24  (matrix2.cpp:1807-1821 shape, U[0,1) here).
+template <class real>
+__device__ __forceinline__ void philox_noise6(uint32_t local, uint32_t replica, uint64_t draw,
+                                              uint32_t seed_lo, uint32_t seed_hi, real xi[6]) {
+    uint2 key = make_uint2(seed_lo, seed_hi);
+    uint4 a = philox4x32_10(make_uint4(local, (uint32_t)draw, (uint32_t)(draw >> 32), 2u * replica), key);
+    uint4 b = philox4x32_10(make_uint4(local, (uint32_t)draw, (uint32_t)(draw >> 32), 2u * replica + 1u), key);
+    uint32_t w[6] = {a.x, a.y, a.z, a.w, b.x, b.y};
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        real u = real(w[k] >> 8) * real(1.0 / 16777216.0);
+        xi[k] = real(3.464101615) * u - real(1.732050808);
+    }
+}
+
+// ------------------------------------------------------------------ pair accumulators
+// FP32: per-particle sums are kept in 64-bit fixed point (2^-32 resolution).  Integer addition is
+// associative, so a particle's force does not depend on the order in which its neighbours are
+// visited -- and that order (the within-cell order of the counting sort) is not deterministic.
+// FP64: plain double sums.
+template <class real> struct Acc3;
+template <> struct Acc3<float> {
+    long long v[3];
+    __device__ __forceinline__ void zero() { v[0] = v[1] = v[2] = 0; }
+    __device__ __forceinline__ void add(float a, float b, float c) {
+        v[0] += __float2ll_rn(a * 4294967296.0f);
+        v[1] += __float2ll_rn(b * 4294967296.0f);
+        v[2] += __float2ll_rn(c * 4294967296.0f);
+    }
+    __device__ __forceinline__ float get(int k) const { return __ll2float_rn(v[k]) * 2.3283064365386963e-10f; }
+};
+template <> struct Acc3<double> {
+    double v[3];
+    __device__ __forceinline__ void zero() { v[0] = v[1] = v[2] = 0; }
+    __device__ __forceinline__ void add(double a, double b, double c) { v[0] += a; v[1] += b; v[2] += c; }
+    __device__ __forceinline__ double get(int k) const { return v[k]; }
+};
+
+// ------------------------------------------------------------------ physics of one pair
+
+// HSPotential::force (potential.h:106-118): magnitude, 0 beyond 1.12246 sigma
+template <class real>
+__device__ __forceinline__ real hs_force(const Replica<real> &R, real r) {
+    if (!(r < R.hs_limit)) return real(0);
+    real a = r * r * r;
+    a = a * a;
+    return R.hs_4eps * (real(12) * R.hs_s12 / (r * a * a) - real(6) * R.hs_s6 / (r * a));
+}
+
+// shifted WCA energy used for the energy observable
+template <class real>
+__device__ __forceinline__ real wca_energy(const Replica<real> &R, real r2) {
+    real s2 = R.hs_s6 / (r2 * r2 * r2);  // (sigma/r)^6
+    return R.hs_4eps * (s2 * s2 - s2) + R.hs_eps;
+}
+
+// Patch (KernFrenkelOnePatch2::force_and_torque, potentialtheta.h:517-750) for one in-cone potential.
+// u = (x_a - x_b)/r (a = lower reference index), n1/n2 = lab-frame patch vectors of a/b,
+// ci = -n1.u, cj = n2.u.  Adds the force on a to f, the torques on a/b to ta/tb, the energy to e.
+template <class real>
+__device__ __forceinline__ void kf2_pair(real att, real dis, real inv_dis, real kfac, const real u[3], real r,
+                                         const real n1[3], const real n2[3], real ci, real cj, real f[3], real ta[3],
+                                         real tb[3], real &e) {
+    if (ci > real(1)) ci = real(0.999999);
+    if (cj > real(1)) cj = real(0.999999);
+    real thi = acos(ci), thj = acos(cj);
+    real sai, cai, saj, caj;
+    sincos(kfac * thi, &sai, &cai);
+    sincos(kfac * thj, &saj, &caj);
+    real fang = cai * caj;
+    real fac = r * inv_dis;
+    real fac2 = fac * fac, fac4 = fac2 * fac2, fac8 = fac4 * fac4, fac10 = fac2 * fac8;
+    real ex = exp(real(-0.5) * fac10);
+    real pot = -att * ex;
+    real potf = real(-5) * att * fac8 * (fac * inv_dis) * ex;
+    // d1/d2 of the reference: zero when |c^2 - 1| < 1e-5, else -1/sqrt(1 - c^2)
+    real d1 = fabs(ci * ci - real(1)) < real(1e-5) ? real(0) : -rsqrt_<real>((real(1) - ci) * (real(1) + ci));
+    real d2 = fabs(cj * cj - real(1)) < real(1e-5) ? real(0) : -rsqrt_<real>((real(1) - cj) * (real(1) + cj));
+    real gi = -kfac * pot * sai * d1 * caj;
+    real gj = -kfac * pot * saj * d2 * cai;
+    real fp = fang * potf, gir = gi / r, gjr = gj / r;
+#pragma unroll
+    for (int k = 0; k < 3; k++) f[k] += fp * u[k] + gir * (n1[k] + ci * u[k]) - gjr * (n2[k] - cj * u[k]);
+    // torque on a: gi (n1 x u); torque on b: gj (u x n2)
+    ta[0] += gi * (n1[1] * u[2] - n1[2] * u[1]);
+    ta[1] += gi * (n1[2] * u[0] - n1[0] * u[2]);
+    ta[2] += gi * (n1[0] * u[1] - n1[1] * u[0]);
+    tb[0] += gj * (u[1] * n2[2] - u[2] * n2[1]);
+    tb[1] += gj * (u[2] * n2[0] - u[0] * n2[2]);
+    tb[2] += gj * (u[0] * n2[1] - u[1] * n2[0]);
+    e += pot * fang;
+}
+
+template <class real>
+__device__ __forceinline__ int type_of(const Model<real> &M, int local) {
+    int t = 0;
+#pragma unroll
+    for (int k = 0; k < kMaxTypes - 1; k++)
+        if (k < M.n_types - 1 && local >= M.ncum[k]) t = k + 1;
+    return t;
+}
+
+// All potentials of the canonical pair (a, b): Qa/Qb lab->body rows, u = (x_a - x_b)/r.
+// Returns the number of in-cone potentials; adds force on a, torques on a/b, energy, bonds.
+template <class real>
+__device__ __forceinline__ void patch_pair(const Model<real> &M, int ta_, int tb_, const real *Qa, const real *Qb,
+                                           const real u[3], real r, real bond_r, real f[3], real tqa[3],
+                                           real tqb[3], real &e, int &bonds) {
+    const int na = M.np[ta_], nb = M.np[tb_];
+    // body-frame images of u: c_i(patch) = -n_body . (Qa u), c_j = n_body . (Qb u)
+    real wa[3], wb[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        wa[k] = Qa[3 * k] * u[0] + Qa[3 * k + 1] * u[1] + Qa[3 * k + 2] * u[2];
+        wb[k] = Qb[3 * k] * u[0] + Qb[3 * k + 1] * u[1] + Qb[3 * k + 2] * u[2];
+    }
+    const real mc = M.mincos[ta_][tb_];
+    real ca[kMaxOrient], cb[kMaxOrient];
+    bool anya = false, anyb = false;
+    const int oa = M.ooff[ta_], ob = M.ooff[tb_];
+    for (int i = 0; i < na; i++) {
+        const real *nbv = M.orient[oa + i];
+        ca[i] = -(nbv[0] * wa[0] + nbv[1] * wa[1] + nbv[2] * wa[2]);
+        anya |= ca[i] > mc;
+    }
+    for (int j = 0; j < nb; j++) {
+        const real *nbv = M.orient[ob + j];
+        cb[j] = nbv[0] * wb[0] + nbv[1] * wb[1] + nbv[2] * wb[2];
+        anyb |= cb[j] > mc;
+    }
+    if (!(anya && anyb)) return;
+    const int ps = M.pstart[ta_][tb_];
+    for (int i = 0; i < na; i++) {
+        if (!(ca[i] > mc)) continue;
+        for (int j = 0; j < nb; j++) {
+            const int q = ps + i * nb + j;
+            const real cm = M.costm[q];
+            if (!(ca[i] > cm && cb[j] > cm)) continue;
+            if (r < bond_r) bonds++;
+            if (r > M.rmax[q]) continue;
+            // lab-frame patch vectors n = Q^T n_body
+            const real *b1 = M.orient[oa + i], *b2 = M.orient[ob + j];
+            real n1[3], n2[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                n1[k] = b1[0] * Qa[k] + b1[1] * Qa[3 + k] + b1[2] * Qa[6 + k];
+                n2[k] = b2[0] * Qb[k] + b2[1] * Qb[3 + k] + b2[2] * Qb[6 + k];
+            }
+            kf2_pair<real>(M.att[q], M.dis[q], M.inv_dis[q], M.kfac[q], u, r, n1, n2, ca[i], cb[j], f, tqa, tqb, e);
+        }
+    }
+}
+
+}  // namespace mtg

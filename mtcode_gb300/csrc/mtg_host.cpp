@@ -1,0 +1,96 @@
+// mtg_host.cpp -- host-side seeded synthetic inputs for the C ABI (no GPU use).
+#include <cmath>
+#include <cstdint>
+#include <vector>
+
+#include "../../include/mtcode_gb300.h"
+
+namespace {
+
+// splitmix64 (Steele, Lea, Flood, "Fast splittable pseudorandom number generators", OOPSLA 2014)
+struct SplitMix {
+    uint64_t s;
+    uint64_t next() {
+        uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    double uniform() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }  // [0,1)
+};
+
+}  // namespace
+
+extern "C" {
+
+// Random sequential addition with a cell hash: each candidate is tested against the accepted
+// particles of the 27 surrounding cells (side >= min_dist).
+mtg_status mtg_random_positions(int n, double box, int periodic, double min_dist, uint64_t seed, double *x) {
+    if (n < 0 || box <= 0 || min_dist < 0 || !x) return MTG_ERR_ARG;
+    SplitMix rng{seed ^ 0x5DEECE66Dull};
+    int nc = min_dist > 0 ? (int)std::floor(box / min_dist) : 1;
+    if (nc < 1) nc = 1;
+    if (nc > 512) nc = 512;
+    const double scale = nc / box;
+    std::vector<int> head((size_t)nc * nc * nc, -1), next((size_t)n, -1);
+    const double md2 = min_dist * min_dist;
+    int placed = 0;
+    int64_t attempts = 0, limit = 1000LL * (int64_t)(n > 0 ? n : 1);
+    while (placed < n) {
+        if (++attempts > limit) return MTG_ERR_ARG;
+        double c[3] = {rng.uniform() * box, rng.uniform() * box, rng.uniform() * box};
+        int ci[3];
+        for (int k = 0; k < 3; k++) {
+            ci[k] = (int)(c[k] * scale);
+            if (ci[k] >= nc) ci[k] = nc - 1;
+        }
+        bool ok = true;
+        const int lo = nc >= 3 ? -1 : 0, hi = nc >= 2 ? 1 : 0;
+        for (int dz = lo; dz <= hi && ok; dz++)
+            for (int dy = lo; dy <= hi && ok; dy++)
+                for (int dx = lo; dx <= hi && ok; dx++) {
+                    int a = ci[0] + dx, b = ci[1] + dy, e = ci[2] + dz;
+                    if (!periodic && (a < 0 || a >= nc || b < 0 || b >= nc || e < 0 || e >= nc)) continue;
+                    a = (a + nc) % nc; b = (b + nc) % nc; e = (e + nc) % nc;
+                    for (int j = head[(size_t)a + nc * ((size_t)b + (size_t)nc * e)]; j >= 0; j = next[j]) {
+                        double d2 = 0;
+                        for (int k = 0; k < 3; k++) {
+                            double d = c[k] - x[3 * (size_t)j + k];
+                            if (periodic) d -= box * std::nearbyint(d / box);
+                            d2 += d * d;
+                        }
+                        if (d2 < md2) { ok = false; break; }
+                    }
+                }
+        if (!ok) continue;
+        for (int k = 0; k < 3; k++) x[3 * (size_t)placed + k] = c[k];
+        size_t cell = (size_t)ci[0] + nc * ((size_t)ci[1] + (size_t)nc * ci[2]);
+        next[placed] = head[cell];
+        head[cell] = placed;
+        placed++;
+    }
+    return MTG_OK;
+}
+
+// Arvo, "Fast random rotation matrices" (Graphics Gems III, 1992): M = (2 v v^T - I) Rz(2 pi x1),
+// v = (cos(2 pi x2) sqrt(x3), sin(2 pi x2) sqrt(x3), sqrt(1 - x3)) -- the construction of
+// LangevinNVTR::initialize (LangevinR.cpp:239-267), driven by splitmix64 instead of rand().
+void mtg_random_rotations(int n, uint64_t seed, double *Q) {
+    SplitMix rng{seed ^ 0xA0761D6478BD642Full};
+    const double two_pi = 6.283185307179586476925286766559;
+    for (int i = 0; i < n; i++) {
+        double x1 = rng.uniform(), x2 = rng.uniform(), x3 = rng.uniform();
+        double v[3] = {std::cos(two_pi * x2) * std::sqrt(x3), std::sin(two_pi * x2) * std::sqrt(x3), std::sqrt(1. - x3)};
+        double c = std::cos(two_pi * x1), s = std::sin(two_pi * x1);
+        double Rz[3][3] = {{c, s, 0}, {-s, c, 0}, {0, 0, 1}};
+        double *q = Q + 9 * (size_t)i;
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) {
+                double acc = 0;
+                for (int k = 0; k < 3; k++) acc += (2 * v[a] * v[k] - (a == k ? 1.0 : 0.0)) * Rz[k][b];
+                q[3 * a + b] = acc;
+            }
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,596 @@
+// mtg_kernels.cuh -- sm_103a kernels of one rotational-Langevin step (all replicas in every launch).
+//
+// Step pipeline (slot order = cell-sorted order of the previous step):
+//   [bin]      next position of every particle -> global cell id + rank inside the cell
+//              (atomic histogram, warp-aggregated with __match_any_sync).  Fused into the force
+//              epilogue of the previous step; launched on its own only after a state upload.
+//   [scan]     exclusive scan of the cell histogram (warp-shuffle block scans, 3 phases)
+//   [scatter]  half-kick, drift + wrap, free-rotor rotation, written straight to the particle's new
+//              slot: the counting sort and the first half of the integrator are one pass
+//   [force]    one thread per particle: WCA core + KF2 patch force/torque over the 27 neighbour
+//              cells (9 contiguous row ranges of the sorted payload), then friction + Philox noise,
+//              the second half-kick, and the binning of the next step
+#pragma once
+
+#include "mtg_device.cuh"
+
+namespace mtg {
+namespace {  // internal linkage: every translation unit keeps its own kernels
+
+enum ForceMode : int { kModeStep = 0, kModeInit = 1, kModeForces = 2, kModeObs = 3 };
+
+template <class real>
+struct Buffers {
+    real *payload;
+    real *motion;
+    int *ident;
+    double *dx, *dy, *dz;  // unwrapped displacement (nullable)
+};
+
+template <class real>
+struct Tables {
+    const Replica<real> *reps;
+    const int *rep_slot;   // n_rep + 1 slot offsets (== particle offsets)
+    const Model<real> *models;
+    int nrep;
+    int ntot;
+    int ncells;
+};
+
+__device__ __forceinline__ int find_replica(const int *rep_slot, int nrep, int s) {
+    int lo = 0, hi = nrep;  // rep_slot[lo] <= s < rep_slot[hi]
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(rep_slot + mid) <= s) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// cell id of a position inside replica R (cube::assign_box with cells of the force grid)
+template <class real>
+__device__ __forceinline__ int cell_of(const Replica<real> &R, real x, real y, real z) {
+    int cx = axis_cell<real>(x, R.cell_scale, R.nc);
+    int cy = axis_cell<real>(y, R.cell_scale, R.nc);
+    int cz = axis_cell<real>(z, R.cell_scale, R.nc);
+    return R.cell_off + cx + R.nc * (cy + R.nc * cz);
+}
+
+// next position: p_h = p + (dt/2) F~ ; x' = x + (dt/m) p_h ; wrap (advancemom_halfstep, advance_pos)
+template <class real>
+__device__ __forceinline__ void drift_position(const Replica<real> &R, real x[3], real p[3], const real F[3]) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        p[k] = add_rn(p[k], mul_rn(R.half_dt, F[k]));
+        x[k] = add_rn(x[k], mul_rn(R.c1, p[k]));
+        wrap_coord<real>(x[k], p[k], R.box, R.periodic);
+    }
+}
+
+// warp-aggregated atomic increment of count[key]; returns this lane's rank
+__device__ __forceinline__ int aggregated_rank(int *count, int key) {
+    unsigned active = __activemask();
+    unsigned peers = __match_any_sync(active, key);
+    int leader = __ffs(peers) - 1;
+    int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count + key, __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
+// ------------------------------------------------------------------ bin (standalone)
+template <class real, bool MOVE>
+__global__ void __launch_bounds__(256) bin_kernel(Tables<real> tb, Buffers<real> in, int2 *bin, int *count,
+                                                  unsigned *flags) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
+        const int r = find_replica(tb.rep_slot, tb.nrep, s);
+        const Replica<real> R = tb.reps[r];
+        real x[3];
+        load_pos(in.payload + (size_t)s * kRow, x[0], x[1], x[2]);
+        if (MOVE) {
+            Row<real> m;
+            m.load(in.motion + (size_t)s * kRow);
+            real p[3] = {m.v[0], m.v[1], m.v[2]}, F[3] = {m.v[6], m.v[7], m.v[8]};
+            drift_position<real>(R, x, p, F);
+        }
+        if (!(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]))) {
+            atomicOr(flags, 1u);
+            x[0] = x[1] = x[2] = real(0);
+        }
+        int key = cell_of<real>(R, x[0], x[1], x[2]);
+        int rank = aggregated_rank(count, key);
+        bin[s] = make_int2(key, rank);
+    }
+}
+
+// ------------------------------------------------------------------ scan of the cell histogram
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;  // per thread -> 4096 cells per block
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int *warp_sums, int &total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < (blockDim.x >> 5) ? warp_sums[lane] : 0;
+        int winc = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, winc, o);
+            if (lane >= o) winc += t;
+        }
+        warp_sums[lane] = winc - w;
+        if (lane == 31) warp_sums[32] = winc;
+    }
+    __syncthreads();
+    int excl = inc - v + warp_sums[warp];
+    total = warp_sums[32];
+    __syncthreads();
+    return excl;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const int *count, int n, int *block_sums) {
+    __shared__ int ws[33];
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) s += (base + k < n) ? __ldg(count + base + k) : 0;
+    int total;
+    block_exclusive_scan(s, ws, total);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+// single block: exclusive scan of the block sums; also advances the noise draw counter
+__global__ void __launch_bounds__(kScanThreads) scan_top_kernel(int *block_sums, int nblocks, int *start, int n,
+                                                                unsigned long long *draw, int consume_draw) {
+    __shared__ int ws[33];
+    int carry = 0;
+    for (int b0 = 0; b0 < nblocks; b0 += kScanThreads) {
+        int i = b0 + threadIdx.x;
+        int v = i < nblocks ? block_sums[i] : 0;
+        int total;
+        int e = block_exclusive_scan(v, ws, total);
+        if (i < nblocks) block_sums[i] = e + carry;
+        carry += total;
+    }
+    if (threadIdx.x == 0) {
+        start[n] = carry;
+        if (consume_draw) {
+            draw[0] = draw[1];  // draw used by this step
+            draw[1] = draw[1] + 1ull;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_down_kernel(int *count, int n, const int *block_sums,
+                                                                 int *start) {
+    __shared__ int ws[33];
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        v[k] = (base + k < n) ? count[base + k] : 0;
+        s += v[k];
+    }
+    int total;
+    int e = block_exclusive_scan(s, ws, total) + block_sums[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        if (base + k < n) {
+            start[base + k] = e;
+            count[base + k] = 0;  // ready for the next histogram
+        }
+        e += v[k];
+    }
+}
+
+// ------------------------------------------------------------------ scatter (+ first half of the step)
+
+// LangevinNVTR::genfullmat (LangevinR.cpp:392-461) built as the product of its five Cayley
+// rotations: x(dt/2) y(dt/2) z(dt) y(dt/2) x(dt/2) of the free rotor, omega = L/I.
+template <class real>
+__device__ __forceinline__ void free_rotor(real dt, real inertia, const real L[3], real R[9]) {
+    real tx = dt * L[0] / inertia, ty = dt * L[1] / inertia, tz = dt * L[2] / inertia;
+    real hx = tx * real(0.25), hy = ty * real(0.25), hz = tz * real(0.5);
+    real dx_ = real(1) / (real(1) + hx * hx), dy_ = real(1) / (real(1) + hy * hy), dz_ = real(1) / (real(1) + hz * hz);
+    // sines enter with a minus sign: the rotations turn L forward by +omega dt
+    real cx = (real(1) - hx * hx) * dx_, sx = real(-2) * hx * dx_;
+    real cy = (real(1) - hy * hy) * dy_, sy = real(-2) * hy * dy_;
+    real cz = (real(1) - hz * hz) * dz_, sz = real(-2) * hz * dz_;
+    // M = Ax * Ay * Az * Ay * Ax with Ax = [[1,0,0],[0,c,s],[0,-s,c]], Ay = [[c,0,-s],[0,1,0],[s,0,c]],
+    // Az = [[c,s,0],[-s,c,0],[0,0,1]] (s as above); checked against genfullmat's closed form
+    real M[9] = {1, 0, 0, 0, cx, sx, 0, -sx, cx};
+    auto mul_y = [&](real c, real s) {
+        for (int r = 0; r < 3; r++) {
+            real a = M[3 * r], b = M[3 * r + 2];
+            M[3 * r] = a * c + b * s;
+            M[3 * r + 2] = -a * s + b * c;
+        }
+    };
+    auto mul_z = [&](real c, real s) {
+        for (int r = 0; r < 3; r++) {
+            real a = M[3 * r], b = M[3 * r + 1];
+            M[3 * r] = a * c - b * s;
+            M[3 * r + 1] = a * s + b * c;
+        }
+    };
+    auto mul_x = [&](real c, real s) {
+        for (int r = 0; r < 3; r++) {
+            real a = M[3 * r + 1], b = M[3 * r + 2];
+            M[3 * r + 1] = a * c - b * s;
+            M[3 * r + 2] = a * s + b * c;
+        }
+    };
+    mul_y(cy, sy);
+    mul_z(cz, sz);
+    mul_y(cy, sy);
+    mul_x(cx, sx);
+#pragma unroll
+    for (int k = 0; k < 9; k++) R[k] = M[k];
+}
+
+template <class real, bool MOVE>
+__global__ void __launch_bounds__(256) scatter_kernel(Tables<real> tb, Buffers<real> in, Buffers<real> out,
+                                                      const int2 *bin, const int *start, unsigned *flags) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
+        const int2 kb = bin[s];
+        const int d = __ldg(start + kb.x) + kb.y;
+        Row<real> P, M;
+        P.load(in.payload + (size_t)s * kRow);
+        M.load(in.motion + (size_t)s * kRow);
+        const int id = in.ident[s];
+        if (MOVE) {
+            const int r = find_replica(tb.rep_slot, tb.nrep, s);
+            const Replica<real> R = tb.reps[r];
+            real x[3] = {P.v[0], P.v[1], P.v[2]}, p[3] = {M.v[0], M.v[1], M.v[2]};
+            real F[3] = {M.v[6], M.v[7], M.v[8]};
+            real L[3] = {M.v[3], M.v[4], M.v[5]}, T[3] = {M.v[9], M.v[10], M.v[11]};
+            real step[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                real ph = add_rn(p[k], mul_rn(R.half_dt, F[k]));
+                step[k] = mul_rn(R.c1, ph);
+            }
+            drift_position<real>(R, x, p, F);  // identical arithmetic to the binning pass
+            if (!(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]))) atomicOr(flags, 1u);
+            if (in.dx) {
+                out.dx[d] = in.dx[s] + (double)step[0];
+                out.dy[d] = in.dy[s] + (double)step[1];
+                out.dz[d] = in.dz[s] + (double)step[2];
+            }
+#pragma unroll
+            for (int k = 0; k < 3; k++) L[k] = L[k] + R.half_dt * T[k];
+            real Rm[9];
+            free_rotor<real>(R.dt, R.inertia, L, Rm);
+            real Ln[3];
+#pragma unroll
+            for (int a = 0; a < 3; a++) Ln[a] = L[0] * Rm[3 * a] + L[1] * Rm[3 * a + 1] + L[2] * Rm[3 * a + 2];
+            // Q <- R^T Q (LangevinR.cpp:611-683)
+            real Q[9] = {P.v[3], P.v[4], P.v[5], P.v[6], P.v[7], P.v[8], P.v[9], P.v[10], P.v[11]};
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+#pragma unroll
+                for (int b = 0; b < 3; b++)
+                    P.v[3 + 3 * a + b] = Q[b] * Rm[a] + Q[3 + b] * Rm[3 + a] + Q[6 + b] * Rm[6 + a];
+            P.v[0] = x[0]; P.v[1] = x[1]; P.v[2] = x[2];
+            M.v[0] = p[0]; M.v[1] = p[1]; M.v[2] = p[2];
+            M.v[3] = Ln[0]; M.v[4] = Ln[1]; M.v[5] = Ln[2];
+        } else if (in.dx) {
+            out.dx[d] = in.dx[s];
+            out.dy[d] = in.dy[s];
+            out.dz[d] = in.dz[s];
+        }
+        P.store(out.payload + (size_t)d * kRow);
+        M.store(out.motion + (size_t)d * kRow);
+        out.ident[d] = id;
+    }
+}
+
+// ------------------------------------------------------------------ force + Langevin epilogue
+
+template <class real>
+struct ForceArgs {
+    Tables<real> tb;
+    Buffers<real> buf;      // current (cell-sorted) buffers; motion is updated in place
+    const int *start;       // cell starts of the current order
+    int2 *bin;              // next-step bins (modes step / init)
+    int *count;             // next-step histogram (modes step / init)
+    unsigned *flags;
+    const unsigned long long *draw;  // draw[0] = draw index of this pass
+    const double *ext_noise;         // ntot x 6 by global index, or null (Philox)
+    double *outF, *outT, *outE;      // mode forces: by global index
+    double *obs;                     // mode obs: n_rep x 5
+    int do_kick;                     // second half-kick (step) or not (init)
+};
+
+template <class real, int MODE>
+__global__ void __launch_bounds__(128) force_kernel(ForceArgs<real> a) {
+    const Tables<real> &tb = a.tb;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
+        const int r = find_replica(tb.rep_slot, tb.nrep, s);
+        const Replica<real> &R = tb.reps[r];
+        const Model<real> &Mo = tb.models[R.model];
+        Row<real> P;
+        P.load(a.buf.payload + (size_t)s * kRow);
+        const real xi = P.v[0], yi = P.v[1], zi = P.v[2];
+        const real *Qi = P.v + 3;
+        const int idi = a.buf.ident[s];
+        const int li = idi - R.off;
+        const int ti = type_of<real>(Mo, li);
+        const bool single_type = Mo.n_types == 1;
+
+        Acc3<real> F, T;
+        F.zero();
+        T.zero();
+        real ewca = real(0), epatch = real(0), vir = real(0);
+        int bonds = 0, npairs = 0;
+        bool big = false;
+
+        const int nc = R.nc;
+        const int cx = axis_cell<real>(xi, R.cell_scale, nc);
+        const int cy = axis_cell<real>(yi, R.cell_scale, nc);
+        const int cz = axis_cell<real>(zi, R.cell_scale, nc);
+        // stencil offsets per axis, de-duplicated for grids of 1 or 2 cells (geometry.h:523-608)
+        const int lo = nc >= 3 ? -1 : 0, hi = nc >= 2 ? 1 : 0;
+        const real range2 = MODE == kModeObs ? (R.rc2 > R.bond_r * R.bond_r ? R.rc2 : R.bond_r * R.bond_r) : R.rc2;
+
+        for (int dz = lo; dz <= hi; dz++) {
+            int zz = cz + dz;
+            if (zz < 0 || zz >= nc) {
+                if (!R.periodic) continue;
+                zz = zz < 0 ? zz + nc : zz - nc;
+            }
+            for (int dy = lo; dy <= hi; dy++) {
+                int yy = cy + dy;
+                if (yy < 0 || yy >= nc) {
+                    if (!R.periodic) continue;
+                    yy = yy < 0 ? yy + nc : yy - nc;
+                }
+                const int row = R.cell_off + nc * (yy + nc * zz);
+                // x-range [cx+lo, cx+hi] as at most two contiguous slot segments
+                int seg_a0, seg_a1, seg_b0 = 0, seg_b1 = 0;
+                if (nc < 3) {
+                    seg_a0 = __ldg(a.start + row);
+                    seg_a1 = __ldg(a.start + row + nc);
+                } else {
+                    int x0 = cx - 1, x1 = cx + 1;
+                    if (x0 < 0) {
+                        seg_a0 = __ldg(a.start + row);
+                        seg_a1 = __ldg(a.start + row + x1 + 1);
+                        if (R.periodic) {
+                            seg_b0 = __ldg(a.start + row + nc - 1);
+                            seg_b1 = __ldg(a.start + row + nc);
+                        }
+                    } else if (x1 >= nc) {
+                        seg_a0 = __ldg(a.start + row + x0);
+                        seg_a1 = __ldg(a.start + row + nc);
+                        if (R.periodic) {
+                            seg_b0 = __ldg(a.start + row);
+                            seg_b1 = __ldg(a.start + row + 1);
+                        }
+                    } else {
+                        seg_a0 = __ldg(a.start + row + x0);
+                        seg_a1 = __ldg(a.start + row + x1 + 1);
+                    }
+                }
+                for (int seg = 0; seg < 2; seg++) {
+                    const int j0 = seg ? seg_b0 : seg_a0, j1 = seg ? seg_b1 : seg_a1;
+                    for (int j = j0; j < j1; j++) {
+                        if (j == s) continue;
+                        const real *pj = a.buf.payload + (size_t)j * kRow;
+                        real xj, yj, zj;
+                        load_pos(pj, xj, yj, zj);
+                        real dx = min_image<real>(xi - xj, R.box, R.l2s, R.periodic);
+                        real dy2 = min_image<real>(yi - yj, R.box, R.l2s, R.periodic);
+                        real dz2 = min_image<real>(zi - zj, R.box, R.l2s, R.periodic);
+                        real r2 = dx * dx + dy2 * dy2 + dz2 * dz2;
+                        if (!(r2 < range2)) continue;
+                        const real rr = sqrt(r2);
+                        if (r2 < R.rc2) npairs++;
+                        // WCA core: same vector for both orientations of the pair
+                        real fi[3] = {0, 0, 0};
+                        if (rr < R.hs_limit) {
+                            real fh = hs_force<real>(R, rr);
+                            big |= fabs(fh) > real(1e4);
+                            real s_ = fh / rr;
+                            fi[0] = s_ * dx; fi[1] = s_ * dy2; fi[2] = s_ * dz2;
+                            ewca += real(0.5) * wca_energy<real>(R, r2);
+                        }
+                        real ti_[3] = {0, 0, 0};
+                        if (r2 < R.patch_r2 || MODE == kModeObs) {
+                            const int idj = __ldg(a.buf.ident + j);
+                            const int tj = single_type ? 0 : type_of<real>(Mo, idj - R.off);
+                            if (Mo.np[ti] > 0 && Mo.np[tj] > 0) {
+                                Row<real> Pj;
+                                Pj.load(pj);
+                                const bool i_first = idi < idj;  // canonical order of the reference (p1 < p2)
+                                real u[3];
+                                const real inv = real(1) / rr;
+                                const real sg = i_first ? real(1) : real(-1);
+                                u[0] = sg * dx * inv; u[1] = sg * dy2 * inv; u[2] = sg * dz2 * inv;
+                                real f[3] = {0, 0, 0}, tqa[3] = {0, 0, 0}, tqb[3] = {0, 0, 0}, e = 0;
+                                int nb = 0;
+                                const bool force_ok = r2 < R.max_dist2;
+                                if (force_ok || MODE == kModeObs) {
+                                    if (i_first)
+                                        patch_pair<real>(Mo, ti, tj, Qi, Pj.v + 3, u, rr, R.bond_r, f, tqa, tqb, e, nb);
+                                    else
+                                        patch_pair<real>(Mo, tj, ti, Pj.v + 3, Qi, u, rr, R.bond_r, f, tqa, tqb, e, nb);
+                                }
+                                if (!force_ok) { f[0] = f[1] = f[2] = 0; tqa[0] = tqa[1] = tqa[2] = 0; tqb[0] = tqb[1] = tqb[2] = 0; e = 0; }
+                                bonds += nb;
+                                epatch += real(0.5) * e;
+#pragma unroll
+                                for (int k = 0; k < 3; k++) {
+                                    fi[k] += sg * f[k];
+                                    ti_[k] = i_first ? tqa[k] : tqb[k];
+                                }
+                            }
+                        }
+                        F.add(fi[0], fi[1], fi[2]);
+                        T.add(ti_[0], ti_[1], ti_[2]);
+                        vir += real(0.5) * (dx * fi[0] + dy2 * fi[1] + dz2 * fi[2]);
+                    }
+                }
+            }
+        }
+        if (big) atomicOr(a.flags, 2u);
+
+        if (MODE == kModeForces) {
+            a.outF[3 * (size_t)idi + 0] = F.get(0);
+            a.outF[3 * (size_t)idi + 1] = F.get(1);
+            a.outF[3 * (size_t)idi + 2] = F.get(2);
+            a.outT[3 * (size_t)idi + 0] = T.get(0);
+            a.outT[3 * (size_t)idi + 1] = T.get(1);
+            a.outT[3 * (size_t)idi + 2] = T.get(2);
+            if (a.outE) a.outE[idi] = (double)ewca + (double)epatch;
+            continue;
+        }
+        if (MODE == kModeObs) {
+            // warp-shuffle reduction when the whole warp is in one replica, else per-lane atomics
+            double v[5] = {0, 0, 0, 0, 0};
+            v[2] = (double)vir;
+            v[4] = 0.5 * (double)npairs;
+            v[3] = 0.5 * (double)bonds;
+            v[0] = (double)epatch;
+            v[1] = (double)ewca;
+            double *o = a.obs + 5 * (size_t)r;
+#pragma unroll
+            for (int k = 0; k < 5; k++) atomicAdd(o + k, v[k]);
+            continue;
+        }
+
+        // ---- create_forces_and_torques_sphere (LangevinR.cpp:474-578) + advancemom_halfstep
+        Row<real> Mv;
+        Mv.load(a.buf.motion + (size_t)s * kRow);
+        real p[3] = {Mv.v[0], Mv.v[1], Mv.v[2]}, L[3] = {Mv.v[3], Mv.v[4], Mv.v[5]};
+        real xi6[6];
+        if (a.ext_noise) {
+#pragma unroll
+            for (int k = 0; k < 6; k++) xi6[k] = (real)a.ext_noise[6 * (size_t)idi + k];
+        } else {
+            philox_noise6<real>((uint32_t)li, (uint32_t)r, a.draw[0], R.seed_lo, R.seed_hi, xi6);
+        }
+        real pb[3], fb[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) pb[k] = Qi[3 * k] * p[0] + Qi[3 * k + 1] * p[1] + Qi[3 * k + 2] * p[2];
+#pragma unroll
+        for (int k = 0; k < 3; k++) fb[k] = R.fric_t * pb[k] + R.Rt * xi6[k];
+        real Ft[3], Tt[3], Fl[3] = {F.get(0), F.get(1), F.get(2)}, Tl[3] = {T.get(0), T.get(1), T.get(2)};
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            Ft[k] = Fl[k] + fb[0] * Qi[k] + fb[1] * Qi[3 + k] + fb[2] * Qi[6 + k];
+            Tt[k] = R.fric_r * L[k] + R.Rr * xi6[3 + k] + Tl[0] * Qi[3 * k] + Tl[1] * Qi[3 * k + 1] + Tl[2] * Qi[3 * k + 2];
+        }
+        if (a.do_kick) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                p[k] = add_rn(p[k], mul_rn(R.half_dt, Ft[k]));
+                L[k] = L[k] + R.half_dt * Tt[k];
+            }
+        }
+        if (!(isfinite(Ft[0]) && isfinite(Ft[1]) && isfinite(Ft[2]) && isfinite(Tt[0]) && isfinite(Tt[1]) &&
+              isfinite(Tt[2]) && isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2])))
+            atomicOr(a.flags, 1u);
+        Mv.v[0] = p[0]; Mv.v[1] = p[1]; Mv.v[2] = p[2];
+        Mv.v[3] = L[0]; Mv.v[4] = L[1]; Mv.v[5] = L[2];
+        Mv.v[6] = Ft[0]; Mv.v[7] = Ft[1]; Mv.v[8] = Ft[2];
+        Mv.v[9] = Tt[0]; Mv.v[10] = Tt[1]; Mv.v[11] = Tt[2];
+        Mv.store(a.buf.motion + (size_t)s * kRow);
+
+        // ---- bin the next step's position (same arithmetic as the scatter pass)
+        real xn[3] = {xi, yi, zi}, pn[3] = {p[0], p[1], p[2]};
+        drift_position<real>(R, xn, pn, Ft);
+        if (!(isfinite(xn[0]) && isfinite(xn[1]) && isfinite(xn[2]))) {
+            atomicOr(a.flags, 1u);
+            xn[0] = xn[1] = xn[2] = real(0);
+        }
+        const int key = cell_of<real>(R, xn[0], xn[1], xn[2]);
+        const int rank = aggregated_rank(a.count, key);
+        a.bin[s] = make_int2(key, rank);
+    }
+}
+
+// ------------------------------------------------------------------ state in / out, reductions
+
+// host-order doubles (ntot rows) -> rows in slot order == global index order
+template <class real>
+__global__ void load_state_kernel(int ntot, const double *x, const double *p, const double *Lb, const double *Q,
+                                  const double *Ft, const double *Tt, Buffers<real> out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ntot; i += gridDim.x * blockDim.x) {
+        Row<real> P, M;
+        P.v[0] = (real)x[3 * (size_t)i]; P.v[1] = (real)x[3 * (size_t)i + 1]; P.v[2] = (real)x[3 * (size_t)i + 2];
+        for (int k = 0; k < 9; k++) P.v[3 + k] = (real)Q[9 * (size_t)i + k];
+        for (int k = 0; k < 3; k++) {
+            M.v[k] = (real)p[3 * (size_t)i + k];
+            M.v[3 + k] = (real)Lb[3 * (size_t)i + k];
+            M.v[6 + k] = Ft ? (real)Ft[3 * (size_t)i + k] : real(0);
+            M.v[9 + k] = Tt ? (real)Tt[3 * (size_t)i + k] : real(0);
+        }
+        P.store(out.payload + (size_t)i * kRow);
+        M.store(out.motion + (size_t)i * kRow);
+        out.ident[i] = i;
+        if (out.dx) { out.dx[i] = 0; out.dy[i] = 0; out.dz[i] = 0; }
+    }
+}
+
+// slot order -> host order doubles; which: bit0 x, bit1 p, bit2 Lb, bit3 Q, bit4 Ft, bit5 Tt, bit6 disp
+template <class real>
+__global__ void store_state_kernel(int ntot, Buffers<real> in, double *x, double *p, double *Lb, double *Q, double *Ft,
+                                   double *Tt, double *disp) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ntot; s += gridDim.x * blockDim.x) {
+        Row<real> P, M;
+        P.load(in.payload + (size_t)s * kRow);
+        M.load(in.motion + (size_t)s * kRow);
+        const size_t i = (size_t)in.ident[s];
+        for (int k = 0; k < 3; k++) {
+            if (x) x[3 * i + k] = (double)P.v[k];
+            if (p) p[3 * i + k] = (double)M.v[k];
+            if (Lb) Lb[3 * i + k] = (double)M.v[3 + k];
+            if (Ft) Ft[3 * i + k] = (double)M.v[6 + k];
+            if (Tt) Tt[3 * i + k] = (double)M.v[9 + k];
+        }
+        if (Q)
+            for (int k = 0; k < 9; k++) Q[9 * i + k] = (double)P.v[3 + k];
+        if (disp && in.dx) {
+            disp[3 * i] = in.dx[s];
+            disp[3 * i + 1] = in.dy[s];
+            disp[3 * i + 2] = in.dz[s];
+        }
+    }
+}
+
+// LangevinNVTR::measured_temperature sums (LangevinR.cpp:170-193): per replica sum p_k^2, sum L_k^2
+template <class real>
+__global__ void __launch_bounds__(256) temperature_kernel(Tables<real> tb, Buffers<real> in, double *out) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
+        const int r = find_replica(tb.rep_slot, tb.nrep, s);
+        Row<real> M;
+        M.load(in.motion + (size_t)s * kRow);
+        double v[6];
+        for (int k = 0; k < 6; k++) v[k] = (double)M.v[k] * (double)M.v[k];
+        unsigned active = __activemask();
+        unsigned peers = __match_any_sync(active, r);
+        const int lane = threadIdx.x & 31;
+        if (peers == 0xffffffffu) {
+            for (int k = 0; k < 6; k++)
+                for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+            if (lane == 0)
+                for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)r + k, v[k]);
+        } else {
+            for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)r + k, v[k]);
+        }
+    }
+}
+
+}  // namespace
+}  // namespace mtg

@@ -1,0 +1,653 @@
+// mtg_sys.cuh -- one handle's device buffers and the launch sequence of every C-ABI operation,
+// templated on the arithmetic type (float: the batched path; double: the plain FP64 path).
+//
+// A step is five kernels (scan x3, scatter, force) captured once into a CUDA graph per buffer
+// parity and replayed.
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mtg_kernels.cuh"
+#include "mtg_pairs.cuh"
+#include "mtg_sys_base.h"
+
+namespace mtg_impl {
+
+// the reference's `pi` is a long double holding pi rounded to double (Basic/basic.h:31)
+const long double kPiL = (long double)3.1415926535897932384626433832795028841971693993751;
+
+inline int n_pots_of(const mtg_patch_model &m) {
+    int npots = 0;
+    for (int a = 0; a < m.n_types; a++)
+        for (int b = a; b < m.n_types; b++) npots += m.patches_per_type[a] * m.patches_per_type[b];
+    return npots;
+}
+
+template <class real>
+mtg::Model<real> make_model(const mtg_patch_model &m) {
+    mtg::Model<real> M;
+    std::memset(&M, 0, sizeof(M));
+    M.n_types = m.n_types;
+    int oo = 0;
+    for (int k = 0; k < m.n_types; k++) {
+        M.np[k] = m.patches_per_type[k];
+        M.ncum[k] = m.count_per_type[k];
+        M.ooff[k] = oo;
+        oo += m.patches_per_type[k];
+    }
+    for (int i = 0; i < oo; i++)
+        for (int c = 0; c < 3; c++) M.orient[i][c] = (real)m.orient[i][c];
+    int ps = 0;
+    for (int a = 0; a < m.n_types; a++)
+        for (int b = a; b < m.n_types; b++) {
+            M.pstart[a][b] = ps;
+            double mc = 2.0;
+            for (int q = ps; q < ps + m.patches_per_type[a] * m.patches_per_type[b]; q++) {
+                double att = m.params[q][0], dis = m.params[q][1], th = m.params[q][2];
+                M.att[q] = (real)att;
+                M.dis[q] = (real)dis;
+                M.inv_dis[q] = (real)(1.0 / dis);
+                M.rmax[q] = (real)(1.4 * dis);
+                M.costm[q] = (real)std::cos(th);
+                M.kfac[q] = (real)(double)(kPiL / (2.0L * (long double)th));
+                mc = std::min(mc, std::cos(th));
+            }
+            M.mincos[a][b] = M.mincos[b][a] = (real)mc;
+            ps += m.patches_per_type[a] * m.patches_per_type[b];
+        }
+    return M;
+}
+
+struct ReplicaGeometry {
+    double rc;        // force range
+    double patch_r;   // patch force range
+    double bond_r;    // ComboPatch::max_check
+};
+
+inline ReplicaGeometry geometry_of(const mtg_replica_desc &d) {
+    ReplicaGeometry g;
+    double hs = 1.12246 * d.hs_sigma;
+    double dmax = 0;
+    bool patches = false;
+    for (int k = 0; k < d.model.n_types; k++) patches |= d.model.patches_per_type[k] > 0;
+    int np = n_pots_of(d.model);
+    for (int q = 0; q < np; q++) dmax = std::max(dmax, 1.4 * d.model.params[q][1]);
+    g.patch_r = patches ? std::min(std::sqrt(d.max_dist2), dmax) : 0.0;
+    g.rc = std::max(hs, g.patch_r);
+    g.bond_r = std::max(1.0, dmax);
+    return g;
+}
+
+template <class real>
+mtg::Replica<real> make_replica(const mtg_replica_desc &d, int off, int cell_off, int nc, int model) {
+    mtg::Replica<real> R;
+    std::memset(&R, 0, sizeof(R));
+    ReplicaGeometry g = geometry_of(d);
+    R.n = d.n;
+    R.off = off;
+    R.cell_off = cell_off;
+    R.nc = nc;
+    R.periodic = d.periodic ? 1 : 0;
+    R.model = model;
+    R.seed_lo = (uint32_t)d.seed;
+    R.seed_hi = (uint32_t)(d.seed >> 32);
+    R.box = (real)d.box;
+    R.half_box = (real)(d.box * 0.5);
+    R.l2s = (real)((d.box / 2.) * (d.box / 2.));
+    R.cell_scale = (real)((double)nc / d.box);
+    R.dt = (real)d.dt;
+    R.half_dt = (real)(d.dt / 2.);
+    R.c1 = (real)(d.dt / d.mass);
+    R.fric_t = (real)(-d.gamma / d.mass);
+    R.fric_r = (real)(-d.gammar / d.inertia);
+    R.Rt = (real)std::sqrt(2 * d.gamma * d.kT / d.dt);
+    R.Rr = (real)std::sqrt(2 * d.gammar * d.kT / d.dt);
+    R.inertia = (real)d.inertia;
+    double s6 = std::pow(d.hs_sigma, 6);
+    R.hs_limit = (real)(1.12246 * d.hs_sigma);
+    R.hs_4eps = (real)(4 * d.hs_eps);
+    R.hs_s6 = (real)s6;
+    R.hs_s12 = (real)(s6 * s6);
+    R.hs_eps = (real)d.hs_eps;
+    R.max_dist2 = (real)d.max_dist2;
+    R.rc2 = (real)(g.rc * g.rc);
+    R.patch_r2 = (real)(g.patch_r * g.patch_r);
+    R.bond_r = (real)g.bond_r;
+    return R;
+}
+
+// cells per side so that side >= range (with room for rounding of the cell assignment)
+inline int cells_per_side(double box, double range) {
+    int nc = (int)std::floor(box / (range * 1.0001));
+    return std::max(1, nc);
+}
+
+inline int grid_for(int64_t n, int block, int per_sm, int sms) {
+    int64_t need = (n + block - 1) / block;
+    int64_t cap = (int64_t)per_sm * sms;
+    return (int)std::max<int64_t>(1, std::min(need, cap));
+}
+
+template <class real>
+struct Sys : SysBase {
+    int device = 0;
+    int sms = 0;
+    cudaStream_t st = nullptr;
+    int nrep = 0;
+    int ntot_ = 0;
+    bool track_disp = true;
+    std::vector<mtg_replica_desc> desc;
+    std::vector<mtg::Replica<real>> reps, reps_obs;
+    std::vector<mtg::Model<real>> models;
+    std::vector<int> rep_slot;
+    int ncells = 0, ncells_obs = 0, ncells_alloc = 0;
+
+    mtg::Replica<real> *d_reps = nullptr, *d_reps_obs = nullptr;
+    mtg::Model<real> *d_models = nullptr;
+    int *d_rep_slot = nullptr;
+    mtg::Buffers<real> buf[2] = {};
+    int cur = 0;
+    int2 *d_bin = nullptr;
+    int *d_count = nullptr, *d_start = nullptr, *d_block = nullptr;
+    unsigned *d_flags = nullptr;
+    unsigned long long *d_draw = nullptr;
+    double *d_stage = nullptr;   // 24 x ntot doubles: host-order state in / out
+    double *d_noise = nullptr;   // ntot x 6 (external noise)
+    double *d_obs = nullptr;     // nrep x 6
+    unsigned *h_flags = nullptr; // pinned
+    uint64_t draw = 0;
+    bool have_state = false, cells_valid = false, bins_valid = false, forces_ready = false;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int64_t nlaunch = 0;
+    // occupancy-derived grid caps
+    int occ_force = 1, occ_stream = 1;
+
+    Sys(const mtg_config &cfg) {
+        device = cfg.device;
+        MTG_CUDA(cudaSetDevice(device));
+        cudaDeviceProp prop;
+        MTG_CUDA(cudaGetDeviceProperties(&prop, device));
+        sms = prop.multiProcessorCount;
+        MTG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        nrep = cfg.n_replicas;
+        track_disp = cfg.track_displacement != 0;
+        desc.assign(cfg.replicas, cfg.replicas + nrep);
+        int64_t off = 0, coff = 0, coff_obs = 0;
+        rep_slot.push_back(0);
+        for (int r = 0; r < nrep; r++) {
+            const mtg_replica_desc &d = desc[r];
+            ReplicaGeometry g = geometry_of(d);
+            int nc = cells_per_side(d.box, g.rc);
+            int nco = cells_per_side(d.box, std::max(g.rc, g.bond_r));
+            models.push_back(make_model<real>(d.model));
+            reps.push_back(make_replica<real>(d, (int)off, (int)coff, nc, r));
+            reps_obs.push_back(make_replica<real>(d, (int)off, (int)coff_obs, nco, r));
+            off += d.n;
+            coff += (int64_t)nc * nc * nc;
+            coff_obs += (int64_t)nco * nco * nco;
+            if (off > 0x7fffffff || coff > 0x7fffffff) throw Fail{MTG_ERR_ARG, "too many particles or cells"};
+            rep_slot.push_back((int)off);
+        }
+        ntot_ = (int)off;
+        ncells = (int)coff;
+        ncells_obs = (int)coff_obs;
+        ncells_alloc = std::max(ncells, ncells_obs);
+        size_t n = (size_t)std::max(ntot_, 1);
+        MTG_CUDA(cudaMalloc(&d_reps, sizeof(mtg::Replica<real>) * nrep));
+        MTG_CUDA(cudaMalloc(&d_reps_obs, sizeof(mtg::Replica<real>) * nrep));
+        MTG_CUDA(cudaMalloc(&d_models, sizeof(mtg::Model<real>) * nrep));
+        MTG_CUDA(cudaMalloc(&d_rep_slot, sizeof(int) * (nrep + 1)));
+        MTG_CUDA(cudaMemcpy(d_reps, reps.data(), sizeof(mtg::Replica<real>) * nrep, cudaMemcpyHostToDevice));
+        MTG_CUDA(cudaMemcpy(d_reps_obs, reps_obs.data(), sizeof(mtg::Replica<real>) * nrep, cudaMemcpyHostToDevice));
+        MTG_CUDA(cudaMemcpy(d_models, models.data(), sizeof(mtg::Model<real>) * nrep, cudaMemcpyHostToDevice));
+        MTG_CUDA(cudaMemcpy(d_rep_slot, rep_slot.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice));
+        for (int b = 0; b < 2; b++) {
+            MTG_CUDA(cudaMalloc(&buf[b].payload, sizeof(real) * mtg::kRow * n));
+            MTG_CUDA(cudaMalloc(&buf[b].motion, sizeof(real) * mtg::kRow * n));
+            MTG_CUDA(cudaMalloc(&buf[b].ident, sizeof(int) * n));
+            if (track_disp) {
+                MTG_CUDA(cudaMalloc(&buf[b].dx, sizeof(double) * n));
+                MTG_CUDA(cudaMalloc(&buf[b].dy, sizeof(double) * n));
+                MTG_CUDA(cudaMalloc(&buf[b].dz, sizeof(double) * n));
+            }
+        }
+        MTG_CUDA(cudaMalloc(&d_bin, sizeof(int2) * n));
+        MTG_CUDA(cudaMalloc(&d_count, sizeof(int) * (ncells_alloc + 1)));
+        MTG_CUDA(cudaMalloc(&d_start, sizeof(int) * (ncells_alloc + 1)));
+        int nblk = (ncells_alloc + mtg::kScanTile - 1) / mtg::kScanTile + 1;
+        MTG_CUDA(cudaMalloc(&d_block, sizeof(int) * nblk));
+        MTG_CUDA(cudaMalloc(&d_flags, sizeof(unsigned)));
+        MTG_CUDA(cudaMalloc(&d_draw, sizeof(unsigned long long) * 2));
+        MTG_CUDA(cudaMalloc(&d_stage, sizeof(double) * 24 * n));
+        MTG_CUDA(cudaMalloc(&d_obs, sizeof(double) * 6 * std::max(nrep, 1)));
+        MTG_CUDA(cudaMallocHost(&h_flags, sizeof(unsigned)));
+        MTG_CUDA(cudaMemsetAsync(d_count, 0, sizeof(int) * (ncells_alloc + 1), st));
+        MTG_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(unsigned), st));
+        MTG_CUDA(cudaMemsetAsync(d_draw, 0, sizeof(unsigned long long) * 2, st));
+        int occ = 0;
+        MTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mtg::force_kernel<real, mtg::kModeStep>, 128, 0));
+        occ_force = std::max(occ, 1);
+        MTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mtg::scatter_kernel<real, true>, 256, 0));
+        occ_stream = std::max(occ, 1);
+        MTG_CUDA(cudaStreamSynchronize(st));
+    }
+
+    ~Sys() override {
+        cudaSetDevice(device);
+        if (st) cudaStreamSynchronize(st);
+        for (int b = 0; b < 2; b++) {
+            if (graph[b]) cudaGraphExecDestroy(graph[b]);
+            cudaFree(buf[b].payload); cudaFree(buf[b].motion); cudaFree(buf[b].ident);
+            cudaFree(buf[b].dx); cudaFree(buf[b].dy); cudaFree(buf[b].dz);
+        }
+        cudaFree(d_reps); cudaFree(d_reps_obs); cudaFree(d_models); cudaFree(d_rep_slot);
+        cudaFree(d_bin); cudaFree(d_count); cudaFree(d_start); cudaFree(d_block);
+        cudaFree(d_flags); cudaFree(d_draw); cudaFree(d_stage); cudaFree(d_noise); cudaFree(d_obs);
+        if (h_flags) cudaFreeHost(h_flags);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    mtg::Tables<real> tables(bool obs = false) const {
+        mtg::Tables<real> t;
+        t.reps = obs ? d_reps_obs : d_reps;
+        t.rep_slot = d_rep_slot;
+        t.models = d_models;
+        t.nrep = nrep;
+        t.ntot = ntot_;
+        t.ncells = obs ? ncells_obs : ncells;
+        return t;
+    }
+
+    int64_t ntot() const override { return ntot_; }
+    int64_t offset(int r) const override { return rep_slot[r]; }
+    cudaStream_t stream() const override { return st; }
+    int64_t launches() const override { return nlaunch; }
+
+    void check_launch() { MTG_CUDA(cudaGetLastError()); }
+
+    // counting sort of the current buffer by cell (no motion), result in the other buffer
+    void rebuild_cells(bool obs) {
+        mtg::Tables<real> tb = tables(obs);
+        int nc = obs ? ncells_obs : ncells;
+        MTG_CUDA(cudaMemsetAsync(d_count, 0, sizeof(int) * (ncells_alloc + 1), st));
+        const int g = grid_for(ntot_, 256, occ_stream, sms);
+        mtg::bin_kernel<real, false><<<g, 256, 0, st>>>(tb, buf[cur], d_bin, d_count, d_flags);
+        check_launch();
+        scan(nc, false);
+        mtg::scatter_kernel<real, false><<<g, 256, 0, st>>>(tb, buf[cur], buf[cur ^ 1], d_bin, d_start, d_flags);
+        check_launch();
+        cur ^= 1;
+        nlaunch += 5;
+        cells_valid = !obs;
+        bins_valid = false;
+    }
+
+    void scan(int n, bool consume_draw) {
+        int nblk = (n + mtg::kScanTile - 1) / mtg::kScanTile;
+        if (nblk < 1) nblk = 1;
+        mtg::scan_reduce_kernel<<<nblk, mtg::kScanThreads, 0, st>>>(d_count, n, d_block);
+        mtg::scan_top_kernel<<<1, mtg::kScanThreads, 0, st>>>(d_block, nblk, d_start, n, d_draw, consume_draw ? 1 : 0);
+        mtg::scan_down_kernel<<<nblk, mtg::kScanThreads, 0, st>>>(d_count, n, d_block, d_start);
+        check_launch();
+    }
+
+    mtg::ForceArgs<real> force_args(int b, int do_kick) {
+        mtg::ForceArgs<real> a;
+        std::memset(&a, 0, sizeof(a));
+        a.tb = tables();
+        a.buf = buf[b];
+        a.start = d_start;
+        a.bin = d_bin;
+        a.count = d_count;
+        a.flags = d_flags;
+        a.draw = d_draw;
+        a.do_kick = do_kick;
+        return a;
+    }
+
+    // one step from buffer b: scan (+draw), scatter b -> b^1, force on b^1
+    void enqueue_step(int b, const double *ext_noise) {
+        mtg::Tables<real> tb = tables();
+        scan(ncells, true);
+        const int g = grid_for(ntot_, 256, occ_stream, sms);
+        mtg::scatter_kernel<real, true><<<g, 256, 0, st>>>(tb, buf[b], buf[b ^ 1], d_bin, d_start, d_flags);
+        mtg::ForceArgs<real> a = force_args(b ^ 1, 1);
+        a.ext_noise = ext_noise;
+        const int gf = grid_for(ntot_, 128, occ_force, sms);
+        mtg::force_kernel<real, mtg::kModeStep><<<gf, 128, 0, st>>>(a);
+        check_launch();
+    }
+
+    void set_state(const double *x, const double *p, const double *Lb, const double *Q, const double *Ft,
+                   const double *Tt) override {
+        MTG_REQUIRE(x && p && Lb && Q, "mtg_set_state: x, p, Lb and Q are required");
+        size_t n = (size_t)ntot_;
+        double *sx = d_stage, *sp = sx + 3 * n, *sl = sp + 3 * n, *sq = sl + 3 * n, *sf = sq + 9 * n, *stt = sf + 3 * n;
+        MTG_CUDA(cudaMemcpyAsync(sx, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+        MTG_CUDA(cudaMemcpyAsync(sp, p, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+        MTG_CUDA(cudaMemcpyAsync(sl, Lb, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+        MTG_CUDA(cudaMemcpyAsync(sq, Q, sizeof(double) * 9 * n, cudaMemcpyHostToDevice, st));
+        if (Ft) MTG_CUDA(cudaMemcpyAsync(sf, Ft, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+        if (Tt) MTG_CUDA(cudaMemcpyAsync(stt, Tt, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+        const int g = grid_for(ntot_, 256, occ_stream, sms);
+        mtg::load_state_kernel<real><<<g, 256, 0, st>>>(ntot_, sx, sp, sl, sq, Ft ? sf : nullptr, Tt ? stt : nullptr,
+                                                        buf[cur]);
+        check_launch();
+        nlaunch += 1;
+        have_state = true;
+        cells_valid = bins_valid = false;
+        forces_ready = Ft && Tt;
+    }
+
+    mtg_status get_state(double *x, double *p, double *Lb, double *Q, double *Ft, double *Tt) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_get_state: no state has been set"};
+        size_t n = (size_t)ntot_;
+        double *sx = d_stage, *sp = sx + 3 * n, *sl = sp + 3 * n, *sq = sl + 3 * n, *sf = sq + 9 * n, *stt = sf + 3 * n;
+        const int g = grid_for(ntot_, 256, occ_stream, sms);
+        mtg::store_state_kernel<real><<<g, 256, 0, st>>>(ntot_, buf[cur], x ? sx : nullptr, p ? sp : nullptr,
+                                                         Lb ? sl : nullptr, Q ? sq : nullptr, Ft ? sf : nullptr,
+                                                         Tt ? stt : nullptr, nullptr);
+        check_launch();
+        nlaunch += 1;
+        if (x) MTG_CUDA(cudaMemcpyAsync(x, sx, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        if (p) MTG_CUDA(cudaMemcpyAsync(p, sp, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        if (Lb) MTG_CUDA(cudaMemcpyAsync(Lb, sl, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        if (Q) MTG_CUDA(cudaMemcpyAsync(Q, sq, sizeof(double) * 9 * n, cudaMemcpyDeviceToHost, st));
+        if (Ft) MTG_CUDA(cudaMemcpyAsync(Ft, sf, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        if (Tt) MTG_CUDA(cudaMemcpyAsync(Tt, stt, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+        return (flags() & MTG_FLAG_NONFINITE) ? MTG_ERR_NONFINITE : MTG_OK;
+    }
+
+    void displacement(double *disp) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_get_displacement: no state has been set"};
+        if (!track_disp) throw Fail{MTG_ERR_STATE, "mtg_get_displacement: handle created without displacement tracking"};
+        size_t n = (size_t)ntot_;
+        const int g = grid_for(ntot_, 256, occ_stream, sms);
+        mtg::store_state_kernel<real><<<g, 256, 0, st>>>(ntot_, buf[cur], nullptr, nullptr, nullptr, nullptr, nullptr,
+                                                         nullptr, d_stage);
+        check_launch();
+        nlaunch += 1;
+        MTG_CUDA(cudaMemcpyAsync(disp, d_stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+    }
+
+    void tick_draw() {
+        // draw[0] <- draw[1]++ for a pass that does not run the scan
+        unsigned long long h[2] = {draw, draw + 1};
+        MTG_CUDA(cudaMemcpyAsync(d_draw, h, sizeof(h), cudaMemcpyHostToDevice, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+        draw += 1;
+    }
+
+    const double *upload_noise(const double *noise) {
+        size_t n = (size_t)ntot_;
+        if (!d_noise) MTG_CUDA(cudaMalloc(&d_noise, sizeof(double) * 6 * std::max<size_t>(n, 1)));
+        MTG_CUDA(cudaMemcpyAsync(d_noise, noise, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, st));
+        return d_noise;
+    }
+
+    void init_forces(const double *noise) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_init_forces: no state has been set"};
+        rebuild_cells(false);
+        tick_draw();
+        mtg::ForceArgs<real> a = force_args(cur, 0);
+        if (noise) a.ext_noise = upload_noise(noise);
+        const int gf = grid_for(ntot_, 128, occ_force, sms);
+        mtg::force_kernel<real, mtg::kModeInit><<<gf, 128, 0, st>>>(a);
+        check_launch();
+        nlaunch += 1;
+        cells_valid = true;
+        bins_valid = true;
+        forces_ready = true;
+    }
+
+    void build_graph(int b) {
+        cudaGraph_t g;
+        MTG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        enqueue_step(b, nullptr);
+        MTG_CUDA(cudaStreamEndCapture(st, &g));
+        MTG_CUDA(cudaGraphInstantiate(&graph[b], g, 0));
+        MTG_CUDA(cudaGraphDestroy(g));
+    }
+
+    void step(int nsteps, const double *noise) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_step: no state has been set"};
+        MTG_REQUIRE(nsteps >= 0, "mtg_step: nsteps must be >= 0");
+        if (!forces_ready) init_forces(nullptr);
+        if (!bins_valid) {
+            MTG_CUDA(cudaMemsetAsync(d_count, 0, sizeof(int) * (ncells_alloc + 1), st));
+            const int g = grid_for(ntot_, 256, occ_stream, sms);
+            mtg::bin_kernel<real, true><<<g, 256, 0, st>>>(tables(), buf[cur], d_bin, d_count, d_flags);
+            check_launch();
+            nlaunch += 1;
+            bins_valid = true;
+        }
+        // the device draw counter follows the host one
+        unsigned long long h[2] = {draw, draw};
+        MTG_CUDA(cudaMemcpyAsync(d_draw, h, sizeof(h), cudaMemcpyHostToDevice, st));
+        size_t n = (size_t)ntot_;
+        if (noise) {
+            for (int s = 0; s < nsteps; s++) {
+                enqueue_step(cur, upload_noise(noise + (size_t)s * 6 * n));
+                cur ^= 1;
+                nlaunch += 5;
+                draw += 1;
+            }
+            MTG_CUDA(cudaStreamSynchronize(st));
+        } else {
+            for (int s = 0; s < nsteps; s++) {
+                if (!graph[cur]) build_graph(cur);
+                MTG_CUDA(cudaGraphLaunch(graph[cur], st));
+                cur ^= 1;
+                nlaunch += 5;
+                draw += 1;
+            }
+        }
+        cells_valid = true;
+        bins_valid = true;
+    }
+
+    void step_profile(int nsteps, double *kernel_ms) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_step_profile: no state has been set"};
+        MTG_REQUIRE(nsteps >= 1 && kernel_ms, "mtg_step_profile: nsteps >= 1 and an output are required");
+        step(0, nullptr);  // initial forces / bins, as mtg_step would
+        unsigned long long h[2] = {draw, draw};
+        MTG_CUDA(cudaMemcpyAsync(d_draw, h, sizeof(h), cudaMemcpyHostToDevice, st));
+        cudaEvent_t ev[6];
+        for (auto &e : ev) MTG_CUDA(cudaEventCreate(&e));
+        double acc[5] = {0, 0, 0, 0, 0};
+        mtg::Tables<real> tb = tables();
+        const int g = grid_for(ntot_, 256, occ_stream, sms);
+        const int gf = grid_for(ntot_, 128, occ_force, sms);
+        int nblk = std::max(1, (ncells + mtg::kScanTile - 1) / mtg::kScanTile);
+        for (int s = 0; s < nsteps; s++) {
+            const int b = cur;
+            MTG_CUDA(cudaEventRecord(ev[0], st));
+            mtg::scan_reduce_kernel<<<nblk, mtg::kScanThreads, 0, st>>>(d_count, ncells, d_block);
+            MTG_CUDA(cudaEventRecord(ev[1], st));
+            mtg::scan_top_kernel<<<1, mtg::kScanThreads, 0, st>>>(d_block, nblk, d_start, ncells, d_draw, 1);
+            MTG_CUDA(cudaEventRecord(ev[2], st));
+            mtg::scan_down_kernel<<<nblk, mtg::kScanThreads, 0, st>>>(d_count, ncells, d_block, d_start);
+            MTG_CUDA(cudaEventRecord(ev[3], st));
+            mtg::scatter_kernel<real, true><<<g, 256, 0, st>>>(tb, buf[b], buf[b ^ 1], d_bin, d_start, d_flags);
+            MTG_CUDA(cudaEventRecord(ev[4], st));
+            mtg::ForceArgs<real> a = force_args(b ^ 1, 1);
+            mtg::force_kernel<real, mtg::kModeStep><<<gf, 128, 0, st>>>(a);
+            MTG_CUDA(cudaEventRecord(ev[5], st));
+            check_launch();
+            MTG_CUDA(cudaEventSynchronize(ev[5]));
+            for (int k = 0; k < 5; k++) {
+                float ms = 0;
+                MTG_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+                acc[k] += ms;
+            }
+            cur ^= 1;
+            nlaunch += 5;
+            draw += 1;
+        }
+        for (auto &e : ev) cudaEventDestroy(e);
+        for (int k = 0; k < 5; k++) kernel_ms[k] = acc[k];
+        cells_valid = true;
+        bins_valid = true;
+    }
+
+    void forces(double *F, double *T, double *E) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_forces: no state has been set"};
+        MTG_REQUIRE(F && T, "mtg_forces: F and T are required");
+        if (!cells_valid) rebuild_cells(false);
+        size_t n = (size_t)ntot_;
+        double *sF = d_stage, *sT = sF + 3 * n, *sE = sT + 3 * n;
+        mtg::ForceArgs<real> a = force_args(cur, 0);
+        a.outF = sF;
+        a.outT = sT;
+        a.outE = E ? sE : nullptr;
+        const int gf = grid_for(ntot_, 128, occ_force, sms);
+        mtg::force_kernel<real, mtg::kModeForces><<<gf, 128, 0, st>>>(a);
+        check_launch();
+        nlaunch += 1;
+        MTG_CUDA(cudaMemcpyAsync(F, sF, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaMemcpyAsync(T, sT, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        if (E) MTG_CUDA(cudaMemcpyAsync(E, sE, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+    }
+
+    void temperature(double *out) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_temperature: no state has been set"};
+        MTG_CUDA(cudaMemsetAsync(d_obs, 0, sizeof(double) * 6 * nrep, st));
+        const int g = grid_for(ntot_, 256, occ_stream, sms);
+        mtg::temperature_kernel<real><<<g, 256, 0, st>>>(tables(), buf[cur], d_obs);
+        check_launch();
+        nlaunch += 1;
+        MTG_CUDA(cudaMemcpyAsync(out, d_obs, sizeof(double) * 6 * nrep, cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+        for (int r = 0; r < nrep; r++) {
+            double n = (double)desc[r].n;
+            for (int k = 0; k < 3; k++) {
+                out[6 * r + k] = out[6 * r + k] / (2. * desc[r].mass) / n;
+                out[6 * r + 3 + k] = out[6 * r + 3 + k] / (2. * desc[r].inertia) / n;
+            }
+        }
+    }
+
+    void observables(double *out) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_observables: no state has been set"};
+        // the bond criterion reaches ComboPatch::max_check, beyond the force range: own cell grid
+        rebuild_cells(true);
+        MTG_CUDA(cudaMemsetAsync(d_obs, 0, sizeof(double) * 6 * nrep, st));
+        mtg::ForceArgs<real> a = force_args(cur, 0);
+        a.tb = tables(true);
+        a.obs = d_obs;
+        std::vector<double> h(6 * (size_t)nrep);
+        const int gf = grid_for(ntot_, 128, occ_force, sms);
+        mtg::force_kernel<real, mtg::kModeObs><<<gf, 128, 0, st>>>(a);
+        check_launch();
+        nlaunch += 1;
+        MTG_CUDA(cudaMemcpyAsync(h.data(), d_obs, sizeof(double) * 6 * nrep, cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+        for (int r = 0; r < nrep; r++)
+            for (int k = 0; k < MTG_OBS_COUNT; k++) out[MTG_OBS_COUNT * r + k] = h[5 * (size_t)r + k];
+        cells_valid = false;  // the buffer is now ordered by the observable grid
+        bins_valid = false;
+    }
+
+    mtg_status pairs(int replica, double rc, int32_t *out, int64_t cap, int64_t *npairs) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_pairs: no state has been set"};
+        MTG_REQUIRE(replica >= 0 && replica < nrep, "mtg_pairs: replica out of range");
+        MTG_REQUIRE(rc > 0 && npairs, "mtg_pairs: rc must be positive and npairs non-null");
+        const mtg_replica_desc &d = desc[replica];
+        int nc = std::max(1, (int)std::floor(d.box / (rc * (1 + 1e-12))));
+        int ncell = nc * nc * nc;
+        int n = d.n;
+        int off = rep_slot[replica];
+        // device scratch: bins, counts, starts, members, per-particle pair counts, offsets, pairs
+        int2 *pbin = nullptr;
+        int *pcount = nullptr, *pstart = nullptr, *pmem = nullptr, *pcnt = nullptr, *poff = nullptr, *pblock = nullptr;
+        int32_t *pout = nullptr;
+        mtg_status result = MTG_OK;
+        auto cleanup = [&]() {
+            cudaFree(pbin); cudaFree(pcount); cudaFree(pstart); cudaFree(pmem); cudaFree(pcnt); cudaFree(poff);
+            cudaFree(pblock); cudaFree(pout);
+        };
+        try {
+            size_t nn = (size_t)std::max(n, 1);
+            MTG_CUDA(cudaMalloc(&pbin, sizeof(int2) * nn));
+            MTG_CUDA(cudaMalloc(&pcount, sizeof(int) * (ncell + 1)));
+            MTG_CUDA(cudaMalloc(&pstart, sizeof(int) * (ncell + 1)));
+            MTG_CUDA(cudaMalloc(&pmem, sizeof(int) * nn));
+            MTG_CUDA(cudaMalloc(&pcnt, sizeof(int) * nn));
+            MTG_CUDA(cudaMalloc(&poff, sizeof(int) * (nn + 1)));
+            int nblk = (ncell + mtg::kScanTile - 1) / mtg::kScanTile + 1;
+            MTG_CUDA(cudaMalloc(&pblock, sizeof(int) * nblk));
+            MTG_CUDA(cudaMemsetAsync(pcount, 0, sizeof(int) * (ncell + 1), st));
+            mtg::PairGrid grid{off, n, nc, d.box, (double)nc / d.box, d.periodic ? 1 : 0, rc};
+            const int g = grid_for(n, 256, occ_stream, sms);
+            mtg::pair_bin_kernel<real><<<g, 256, 0, st>>>(grid, buf[cur], pbin, pcount);
+            int nb = (ncell + mtg::kScanTile - 1) / mtg::kScanTile;
+            if (nb < 1) nb = 1;
+            mtg::scan_reduce_kernel<<<nb, mtg::kScanThreads, 0, st>>>(pcount, ncell, pblock);
+            mtg::scan_top_kernel<<<1, mtg::kScanThreads, 0, st>>>(pblock, nb, pstart, ncell, d_draw, 0);
+            mtg::scan_down_kernel<<<nb, mtg::kScanThreads, 0, st>>>(pcount, ncell, pblock, pstart);
+            mtg::pair_fill_kernel<<<g, 256, 0, st>>>(grid, pbin, pstart, pmem);
+            mtg::pair_count_kernel<real><<<g, 256, 0, st>>>(grid, buf[cur], pstart, pmem, pcnt);
+            check_launch();
+            std::vector<int> hc(n + 1, 0), ho(n + 1, 0);
+            MTG_CUDA(cudaMemcpyAsync(hc.data(), pcnt, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+            MTG_CUDA(cudaStreamSynchronize(st));
+            int64_t total = 0;
+            for (int i = 0; i < n; i++) {
+                ho[i] = (int)total;
+                total += hc[i];
+            }
+            ho[n] = (int)total;
+            *npairs = total;
+            if (total > cap || !out) {
+                cleanup();
+                return total > cap ? MTG_ERR_CAPACITY : MTG_OK;
+            }
+            MTG_CUDA(cudaMalloc(&pout, sizeof(int32_t) * 2 * std::max<int64_t>(total, 1)));
+            MTG_CUDA(cudaMemcpyAsync(poff, ho.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st));
+            mtg::pair_write_kernel<real><<<g, 256, 0, st>>>(grid, buf[cur], pstart, pmem, poff, pout);
+            check_launch();
+            std::vector<int32_t> hp(2 * (size_t)total);
+            MTG_CUDA(cudaMemcpyAsync(hp.data(), pout, sizeof(int32_t) * 2 * total, cudaMemcpyDeviceToHost, st));
+            MTG_CUDA(cudaStreamSynchronize(st));
+            nlaunch += 7;
+            // each particle's segment holds its partners j > i; sort them
+            for (int i = 0; i < n; i++) {
+                std::vector<int32_t> seg;
+                for (int q = ho[i]; q < ho[i + 1]; q++) seg.push_back(hp[2 * (size_t)q + 1]);
+                std::sort(seg.begin(), seg.end());
+                for (int q = ho[i]; q < ho[i + 1]; q++) {
+                    out[2 * (size_t)q] = i;
+                    out[2 * (size_t)q + 1] = seg[q - ho[i]];
+                }
+            }
+        } catch (...) {
+            cleanup();
+            throw;
+        }
+        cleanup();
+        return result;
+    }
+
+    void set_draw(uint64_t d) override { draw = d; }
+    uint64_t get_draw() const override { return draw; }
+
+    uint32_t flags() override {
+        MTG_CUDA(cudaMemcpyAsync(h_flags, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+        return *h_flags;
+    }
+    void clear_flags() override {
+        MTG_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(unsigned), st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+    }
+};
+
+
+}  // namespace mtg_impl

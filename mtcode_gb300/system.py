@@ -1,0 +1,276 @@
+"""Host-side mirror of the reference's LangevinNVTR + ComboPatch interface over the C ABI.
+
+``LangevinNVTRGPU`` keeps the reference's method names (``initialize``, ``getdat``, ``getmom``,
+``getangmom``, ``getorientation``, ``calculatepairs_parallel``, ``calculate_forces_and_torques3D``,
+``measured_temperature``) and adds the fused ``step(nsteps)`` that replaces the body of
+``Condensate::run`` (Condensate/Condensate.cpp:335-378).  Arrays are row-major float64 exactly like the
+reference's ``matrix<double>`` (x, p, Lb: n x 3; Q: n x 9; pairs: P x 2).  Every call goes to the CUDA
+library; errors raise ``MtgError`` instead of the reference's stdin-blocking ``error()``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import MtgError, dptr
+
+TETRA = np.array([[math.sqrt(8 / 9), 0.0, -1 / 3],
+                  [-math.sqrt(2 / 9), math.sqrt(2 / 3), -1 / 3],
+                  [-math.sqrt(2 / 9), -math.sqrt(2 / 3), -1 / 3],
+                  [0.0, 0.0, 1.0]])
+
+
+@dataclass
+class PatchModelSpec:
+    """GeneralPatch-shaped model (GeneralPatch.cpp:7-121).  ``count_per_type`` is cumulative."""
+    patches_per_type: list
+    count_per_type: list
+    orient: np.ndarray           # (sum patches) x 3 body-frame unit vectors
+    params: np.ndarray           # n_pots x 3: (att, dis, thetam)
+
+    @staticmethod
+    def tetrahedral(n: int, att: float, dis: float, thetam: float) -> "PatchModelSpec":
+        """TetrahedralPatch(att, dis, thetam) (TetrahedralPatch.cpp:4-44)."""
+        return PatchModelSpec([4], [n], TETRA.copy(), np.tile([att, dis, thetam], (16, 1)).astype(float))
+
+    @staticmethod
+    def bivalent(n: int, att: float, dis: float, thetam: float) -> "PatchModelSpec":
+        """BivalentPatch(att, dis, thetam) (BivalentPatch.cpp:4-34): patches at -x and +x."""
+        return PatchModelSpec([2], [n], np.array([[-1.0, 0, 0], [1.0, 0, 0]]),
+                              np.tile([att, dis, thetam], (4, 1)).astype(float))
+
+    @property
+    def n_pots(self) -> int:
+        k = self.patches_per_type
+        return sum(k[a] * k[b] for a in range(len(k)) for b in range(a, len(k)))
+
+    def to_c(self) -> _lib.PatchModel:
+        m = _lib.PatchModel()
+        m.n_types = len(self.patches_per_type)
+        for k, (npt, cnt) in enumerate(zip(self.patches_per_type, self.count_per_type)):
+            m.patches_per_type[k] = int(npt)
+            m.count_per_type[k] = int(cnt)
+        for i, v in enumerate(np.asarray(self.orient, float).reshape(-1, 3)):
+            for c in range(3):
+                m.orient[i][c] = float(v[c])
+        for q, v in enumerate(np.asarray(self.params, float).reshape(-1, 3)):
+            for c in range(3):
+                m.params[q][c] = float(v[c])
+        return m
+
+
+@dataclass
+class ReplicaSpec:
+    """One independent system: cube(box) + LangevinNVTR parameters + HSPotential + ComboPatch."""
+    n: int
+    box: float
+    model: PatchModelSpec
+    periodic: bool = True
+    dt: float = 0.005
+    kT: float = 1.0
+    gamma: float = 1.0
+    gammar: float = 1.0
+    mass: float = 1.0
+    inertia: float = 0.25 * 2.0 / 5.0
+    hs_eps: float = 1.0
+    hs_sigma: float = 1.0
+    max_dist2: float = 2.4
+    seed: int = 0
+
+    def to_c(self) -> _lib.ReplicaDesc:
+        d = _lib.ReplicaDesc()
+        d.n, d.box, d.periodic = int(self.n), float(self.box), int(bool(self.periodic))
+        d.dt, d.kT, d.gamma, d.gammar = float(self.dt), float(self.kT), float(self.gamma), float(self.gammar)
+        d.mass, d.inertia = float(self.mass), float(self.inertia)
+        d.hs_eps, d.hs_sigma, d.max_dist2 = float(self.hs_eps), float(self.hs_sigma), float(self.max_dist2)
+        d.seed = int(self.seed) & 0xFFFFFFFFFFFFFFFF
+        d.model = self.model.to_c()
+        return d
+
+
+def _check(h, status: int) -> None:
+    if status != 0:
+        msg = _lib.lib().mtg_last_error(h)
+        raise MtgError(status, (msg or b"").decode())
+
+
+class LangevinNVTRGPU:
+    """All replicas of one GPU handle (one CUDA stream)."""
+
+    def __init__(self, replicas: list, precision: str = "fp32", device: int = 0, track_displacement: bool = True):
+        L = _lib.lib()
+        self.replicas = list(replicas)
+        self._descs = (_lib.ReplicaDesc * len(self.replicas))(*[r.to_c() for r in self.replicas])
+        cfg = _lib.Config()
+        cfg.precision = _lib.MTG_FP64 if precision == "fp64" else _lib.MTG_FP32
+        cfg.n_replicas = len(self.replicas)
+        cfg.replicas = C.cast(self._descs, C.POINTER(_lib.ReplicaDesc))
+        cfg.device = int(device)
+        cfg.track_displacement = int(bool(track_displacement))
+        h = C.c_void_p()
+        st = L.mtg_create(C.byref(cfg), C.byref(h))
+        if st != 0:
+            raise MtgError(st, (L.mtg_last_error(None) or b"").decode())
+        self._h = h
+        self.precision = precision
+        self.n = int(L.mtg_num_particles(h))
+        self.offsets = np.array([L.mtg_replica_offset(h, r) for r in range(len(self.replicas))] + [self.n])
+
+    # ------------------------------------------------------------------ lifetime
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.lib().mtg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ------------------------------------------------------------------ state
+    def initialize(self, x, p, Lb, Q, Ft=None, Tt=None) -> None:
+        """LangevinNVTR::initialize(positions, momenta, orientations, angular_momenta) for all replicas."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None for a in (x, p, Lb, Q, Ft, Tt)]
+        for a, w in zip(arrs, (3, 3, 3, 9, 3, 3)):
+            if a is not None and a.size != self.n * w:
+                raise ValueError(f"state array of size {a.size}, expected {self.n * w}")
+        self._hold = arrs  # host memory must outlive the (staged) copies
+        _check(self._h, _lib.lib().mtg_set_state(self._h, *[dptr(a) for a in arrs]))
+
+    def get_state(self) -> dict:
+        out = {k: np.empty((self.n, w)) for k, w in (("x", 3), ("p", 3), ("Lb", 3), ("Q", 9), ("Ft", 3), ("Tt", 3))}
+        _check(self._h, _lib.lib().mtg_get_state(self._h, *[dptr(out[k]) for k in ("x", "p", "Lb", "Q", "Ft", "Tt")]))
+        return out
+
+    def getdat(self) -> np.ndarray:
+        x = np.empty((self.n, 3))
+        _check(self._h, _lib.lib().mtg_get_state(self._h, dptr(x), None, None, None, None, None))
+        return x
+
+    def getmom(self) -> np.ndarray:
+        p = np.empty((self.n, 3))
+        _check(self._h, _lib.lib().mtg_get_state(self._h, None, dptr(p), None, None, None, None))
+        return p
+
+    def getangmom(self) -> np.ndarray:
+        L = np.empty((self.n, 3))
+        _check(self._h, _lib.lib().mtg_get_state(self._h, None, None, dptr(L), None, None, None))
+        return L
+
+    def getorientation(self) -> np.ndarray:
+        Q = np.empty((self.n, 9))
+        _check(self._h, _lib.lib().mtg_get_state(self._h, None, None, None, dptr(Q), None, None))
+        return Q
+
+    # ------------------------------------------------------------------ the hot path
+    def init_forces(self, noise: np.ndarray | None = None) -> None:
+        """Condensate.cpp:312-334: F~, T~ from forces + one noise draw (Philox, or ``noise`` n x 6)."""
+        if noise is None:
+            _check(self._h, _lib.lib().mtg_init_forces(self._h))
+        else:
+            noise = np.ascontiguousarray(noise, dtype=np.float64)
+            if noise.size != self.n * 6:
+                raise ValueError("noise must hold n x 6 values")
+            _check(self._h, _lib.lib().mtg_init_forces_noise(self._h, dptr(noise)))
+
+    def step_profile(self, nsteps: int) -> dict:
+        """Per-kernel device milliseconds summed over ``nsteps`` instrumented steps."""
+        out = np.zeros(_lib.MTG_PROFILE_KERNELS)
+        _check(self._h, _lib.lib().mtg_step_profile(self._h, int(nsteps), dptr(out)))
+        return dict(zip(_lib.PROFILE_KERNEL_NAMES, out.tolist()))
+
+    def step(self, nsteps: int = 1, noise: np.ndarray | None = None) -> None:
+        """nsteps of the Condensate::run loop body; ``noise`` (nsteps x n x 6) replaces Philox."""
+        if noise is None:
+            _check(self._h, _lib.lib().mtg_step(self._h, int(nsteps)))
+        else:
+            noise = np.ascontiguousarray(noise, dtype=np.float64)
+            if noise.size != nsteps * self.n * 6:
+                raise ValueError("noise must hold nsteps x n x 6 values")
+            _check(self._h, _lib.lib().mtg_step_noise(self._h, int(nsteps), dptr(noise)))
+
+    def calculate_forces_and_torques3D(self, with_energy: bool = False):
+        """MD::calculateforces(HSPotential) + LangevinNVTR::calculate_forces_and_torques3D: F, T (lab)."""
+        F = np.empty((self.n, 3))
+        T = np.empty((self.n, 3))
+        E = np.empty(self.n) if with_energy else None
+        _check(self._h, _lib.lib().mtg_forces(self._h, dptr(F), dptr(T), dptr(E)))
+        return (F, T, E) if with_energy else (F, T)
+
+    def calculatepairs_parallel(self, rc: float, replica: int = 0) -> np.ndarray:
+        """MD::calculatepairs_parallel: sorted (i < j) pairs of one replica within rc."""
+        L = _lib.lib()
+        npairs = C.c_int64(0)
+        st = L.mtg_pairs(self._h, int(replica), float(rc), None, 0, C.byref(npairs))
+        if st not in (0, 6):
+            _check(self._h, st)
+        out = np.empty((max(npairs.value, 1), 2), dtype=np.int32)
+        _check(self._h, L.mtg_pairs(self._h, int(replica), float(rc), out.ctypes.data_as(_lib._I32),
+                                    out.shape[0], C.byref(npairs)))
+        return out[: npairs.value]
+
+    def measured_temperature(self) -> np.ndarray:
+        """LangevinNVTR::measured_temperature per replica: (<p^2/2m> xyz, <L^2/2I> xyz)."""
+        out = np.empty((len(self.replicas), 6))
+        _check(self._h, _lib.lib().mtg_temperature(self._h, dptr(out)))
+        return out
+
+    def observables(self) -> np.ndarray:
+        """Per replica: patch energy, WCA energy, virial, bonded patch pairs, pairs in range."""
+        out = np.empty((len(self.replicas), _lib.MTG_OBS_COUNT))
+        _check(self._h, _lib.lib().mtg_observables(self._h, dptr(out)))
+        return out
+
+    def displacement(self) -> np.ndarray:
+        d = np.empty((self.n, 3))
+        _check(self._h, _lib.lib().mtg_get_displacement(self._h, dptr(d)))
+        return d
+
+    def sync(self) -> None:
+        _check(self._h, _lib.lib().mtg_sync(self._h))
+
+    @property
+    def flags(self) -> int:
+        return int(_lib.lib().mtg_flags(self._h))
+
+    @property
+    def draw(self) -> int:
+        return int(_lib.lib().mtg_get_draw(self._h))
+
+    @draw.setter
+    def draw(self, value: int) -> None:
+        _check(self._h, _lib.lib().mtg_set_draw(self._h, int(value)))
+
+    @property
+    def launches(self) -> int:
+        return int(_lib.lib().mtg_launch_count(self._h))
+
+    @property
+    def stream(self) -> int:
+        return int(_lib.lib().mtg_stream(self._h) or 0)
+
+
+def random_positions(n: int, box: float, periodic: bool = True, min_dist: float = 0.9, seed: int = 0) -> np.ndarray:
+    x = np.empty((n, 3))
+    st = _lib.lib().mtg_random_positions(int(n), float(box), int(bool(periodic)), float(min_dist),
+                                         int(seed) & 0xFFFFFFFFFFFFFFFF, dptr(x))
+    if st != 0:
+        raise MtgError(st, f"could not place {n} particles at min_dist {min_dist} in a box of {box}")
+    return x
+
+
+def random_rotations(n: int, seed: int = 0) -> np.ndarray:
+    Q = np.empty((n, 9))
+    _lib.lib().mtg_random_rotations(int(n), int(seed) & 0xFFFFFFFFFFFFFFFF, dptr(Q))
+    return Q

@@ -1,0 +1,120 @@
+/*
+ * oracle.h -- CPU restatement (FP64) of the mtcode rotational-Langevin step for patchy spheres.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA path: only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm may load it.  The product
+ * (mtcode_gb300/) never calls into it and has no CPU fallback.
+ *
+ * Parity pinning: every routine here is compared, bit for bit on x86-64, against the reference's own
+ * routines compiled from the reference sources (oracle/ref_driver.cpp -> oracle/_ref/libmtref.so) on
+ * the golden inputs committed under tests/golden/ (see tests/test_oracle_golden.py).
+ *
+ * Conventions follow the reference (units sigma = epsilon = m = 1):
+ *   x, p, Lb, F, T : row-major n x 3 doubles (Lb and the carried torque are BODY frame)
+ *   Q              : row-major n x 9 doubles, lab -> body rotation (patch in lab frame = Q^T n_body)
+ *   pairs          : row-major np x 2 ints
+ */
+#ifndef MTG_ORACLE_H
+#define MTG_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_MAX_TYPES 8
+#define ORC_MAX_ORIENT 64
+#define ORC_MAX_POTS 2048
+
+/* GeneralPatch-shaped patch model (MDBase/Potentials/ComboPatch/GeneralPatch.cpp:7-121).
+ * TetrahedralPatch (TetrahedralPatch.cpp:4-44) is one type with the four tetrahedral vectors and 16
+ * identical potentials; BivalentPatch (BivalentPatch.cpp:4-34) is one type with -x/+x and 4 potentials.
+ * Potentials are enumerated type pair (k1 <= k2), then patch of k1, then patch of k2. */
+typedef struct {
+    int n_types;
+    int patches_per_type[ORC_MAX_TYPES];
+    int num_per_type[ORC_MAX_TYPES];      /* cumulative particle counts (particle i has type k if i < num_per_type[k]) */
+    double orient[ORC_MAX_ORIENT][3];     /* body-frame patch unit vectors, types contiguous */
+    int n_pots;
+    double att[ORC_MAX_POTS];             /* KernFrenkelOnePatch2::att */
+    double dis[ORC_MAX_POTS];             /* KernFrenkelOnePatch2::dis */
+    double thetam[ORC_MAX_POTS];          /* KernFrenkelOnePatch2::thetam */
+} orc_model;
+
+typedef struct {
+    int n;
+    double box;          /* cube::l */
+    int periodic;        /* cube::periodic */
+    double dt, kT, gamma, gammar, mass, inertia;
+    double hs_eps, hs_sigma;   /* HSPotential(eps, sigma) */
+    double max_dist2;          /* LangevinNVTR::max_distance_check (squared distance) */
+    const orc_model *model;
+} orc_params;
+
+/* geometry.h:508-520 */
+int orc_assign_box(const double *xrow, int n, double box);
+/* geometry.h:523-608: sorted, de-duplicated 27-cell stencil of cell c; returns its length */
+int orc_neighbor_cells(int c, int n, int *out);
+/* MD.cpp:1035-1098 + 715-869 (serial order). Returns the number of pairs (may exceed cap: then
+ * only the first cap pairs are written). */
+long orc_pairs(const orc_params *P, const double *x, int ncell, double rc, int *pairs, long cap);
+
+/* MD.cpp:1684-1764 with HSPotential::force (potential.h:106-118). F is overwritten. */
+void orc_hs_forces(const orc_params *P, const double *x, const int *pairs, long np, double *F);
+/* LangevinR.cpp:911-1047 with KernFrenkelOnePatch2::force_and_torque (potentialtheta.h:517-750).
+ * Adds into F and T (lab frame). */
+void orc_patch_forces(const orc_params *P, const double *x, const double *Q, const int *pairs, long np,
+                      double *F, double *T);
+/* one KernFrenkelOnePatch2::force_and_torque evaluation, exposed for unit tests */
+void orc_kf2_force_torque(const double nb1[3], const double nb2[3], double att, double dis, double thetam,
+                          const double un[3], double rij, const double *Qi, const double *Qj, double out9[9]);
+
+/* LangevinR.cpp:474-592: F <- F + Q^T(-(gamma/m) Q p + Rt xi[0:3]);  T <- -(gammar/I) Lb + Rr xi[3:6] + Q T */
+void orc_langevin_forces(const orc_params *P, const double *p, const double *Lb, const double *Q,
+                         const double *noise, double *F, double *T);
+/* LangevinR.cpp:327-347 */
+void orc_halfkick(int n, double dt, double *p, double *Lb, const double *F, const double *T);
+/* Langevin.cpp:205-222 then geometry.h:403-446 */
+void orc_drift(const orc_params *P, double *x, double *p);
+/* LangevinR.cpp:392-461 (genfullmat) and 594-695 (rotate) */
+void orc_rotation_matrix(double dt, double inertia, const double L[3], double R[9]);
+void orc_rotate(const orc_params *P, double *Lb, double *Q);
+/* LangevinR.cpp:170-193: per-axis <p^2/2m>, <L^2/2I> */
+void orc_temperature(const orc_params *P, const double *p, const double *Lb, double out6[6]);
+
+/* Philox4x32-10 (Salmon et al., SC'11 "Parallel random numbers: as easy as 1, 2, 3"). */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* The noise draw the CUDA path uses: for particle i (local index), replica r, draw d:
+ *   ctr = {i, d_lo, d_hi, 2r + blk}, key = {seed_lo, seed_hi}, 8 words -> the first 6 give
+ *   xi = 3.464101615 * u - 1.732050808 with u = (w >> 8) * 2^-24   (matrix2.cpp:1807-1821 shape) */
+void orc_philox_noise(int n, uint64_t seed, uint32_t replica, uint64_t draw, double *noise);
+
+/* Energy and bookkeeping observables over all pairs within range:
+ *   out[0] = KF2 patch energy (potentialtheta.h:448-515 form),
+ *   out[1] = WCA energy 4e[(s/r)^12-(s/r)^6]+e for r < 1.12246 s (HSPotential force range),
+ *   out[2] = virial sum r_ij . f_ij (central + patch forces),
+ *   out[3] = number of bonded patch pairs (LangevinR.cpp:1854-1998 criterion, max_check = max 1.4 dis). */
+void orc_observables(const orc_params *P, const double *x, const double *Q, const int *pairs, long np,
+                     double out[4]);
+
+/* Full forces as the driver computes them: F = HS forces + patch forces; T = patch torques (lab). */
+void orc_forces(const orc_params *P, const double *x, const double *Q, int ncell, double rc,
+                double *F, double *T);
+
+/* Condensate.cpp:312-334: initial F~, T~ from the current state and one noise draw. */
+void orc_init_forces(const orc_params *P, const double *x, const double *p, const double *Lb, const double *Q,
+                     int ncell, double rc, const double *noise, double *Ft, double *Tt);
+
+/* Condensate.cpp:335-378 loop body, nsteps times, pairs rebuilt every `rebuild` steps at (ncell, rc)
+ * from the positions at the start of the step.  noise_mode: 0 = xi = 0, 1 = external array
+ * (nsteps x n x 6), 2 = Philox(seed, replica, draw0 + step).  With check_skin, returns -1 if a pair
+ * came within the force range without being in the (stale) pair list -- the skin was too small. */
+int orc_run(const orc_params *P, double *x, double *p, double *Lb, double *Q, double *Ft, double *Tt,
+            int nsteps, int ncell, double rc, int rebuild, int noise_mode, const double *noise,
+            uint64_t seed, uint32_t replica, uint64_t draw0, int check_skin);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

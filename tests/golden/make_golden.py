@@ -1,0 +1,236 @@
+"""Generates the golden fixtures in this directory by running the REFERENCE's own routines
+(osmanovicdino/mtcode, compiled by oracle/build_ref.sh into oracle/_ref/libmtref.so) on seeded inputs.
+
+    python tests/golden/make_golden.py [--reference /root/reference]
+
+Inputs are rounded to float32-representable doubles so that the FP32 GPU path, the FP64 GPU path,
+the oracle and the reference all start from bit-identical coordinates.  Force cases are re-seeded
+until no pair sits within 1e-6 of a branch threshold of the patch potential (cone edge, radial cut,
+|c^2-1| = 1e-5): an FP32 evaluation may legitimately fall on the other side of such a threshold.
+"""
+from __future__ import annotations
+
+import argparse
+import math
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle import pyoracle as po  # noqa: E402
+from mtcode_gb300.system import PatchModelSpec, ReplicaSpec, random_positions, random_rotations  # noqa: E402
+from mtcode_gb300.workloads import box_for, crowded_model, tubulin_model  # noqa: E402
+
+HERE = Path(__file__).resolve().parent
+D = po._d
+
+
+def f32(a):
+    return np.ascontiguousarray(np.asarray(a, np.float32).astype(np.float64))
+
+
+def ref_pairs(spec, x, ncell, rc, parallel=False):
+    R = po.ref()
+    cap = 64 * len(x) + 64
+    out = np.empty((cap, 2), dtype=np.intc)
+    fn = R.ref_pairs_parallel if parallel else R.ref_pairs
+    n = fn(spec.n, spec.box, int(spec.periodic), D(x), ncell, rc, out.ctypes.data_as(po._I), cap)
+    assert n <= cap
+    p = np.sort(out[:n], axis=1)
+    return p[np.lexsort((p[:, 1], p[:, 0]))]
+
+
+def ref_forces(spec, x, Q, rc):
+    R = po.ref()
+    args = po.ref_model_args(spec.model)
+    F = np.empty((spec.n, 3))
+    T = np.empty((spec.n, 3))
+    ncell = max(1, int(math.floor(spec.box / rc)))
+    kind, att, dis, th, nt, ppt, npt, orient, params = args
+    R.ref_forces(spec.n, spec.box, int(spec.periodic), D(x), D(Q), ncell, rc, spec.hs_eps, spec.hs_sigma, kind, att,
+                 dis, th, nt, ppt.ctypes.data_as(po._I), npt.ctypes.data_as(po._I), D(orient), D(params), D(F), D(T))
+    return F, T
+
+
+def ref_run(spec, st, nsteps, rc, rebuild, noise=None, init=True, noise0=None):
+    R = po.ref()
+    kind, att, dis, th, nt, ppt, npt, orient, params = po.ref_model_args(spec.model)
+    ncell = max(1, int(math.floor(spec.box / rc)))
+    temps = np.empty((nsteps, 6))
+    R.ref_run(spec.n, spec.box, int(spec.periodic), D(st["x"]), D(st["p"]), D(st["Lb"]), D(st["Q"]), D(st["Ft"]),
+              D(st["Tt"]), spec.dt, spec.kT, spec.gamma, spec.gammar, spec.hs_eps, spec.hs_sigma, kind, att, dis, th,
+              nt, ppt.ctypes.data_as(po._I), npt.ctypes.data_as(po._I), D(orient), D(params), ncell, rc, rebuild,
+              nsteps, D(noise), int(init), D(noise0), D(temps))
+    return temps
+
+
+def threshold_margin(spec, x, Q, rc):
+    """Smallest distance of any in-range pair quantity to a branch threshold of the force routine."""
+    sysm = po.System(spec)
+    pr = sysm.pairs(x, rc)
+    if len(pr) == 0:
+        return 1.0
+    d = x[pr[:, 0]] - x[pr[:, 1]]
+    if spec.periodic:
+        d = np.where(d * d > (spec.box / 2) ** 2, d - np.sign(d) * spec.box, d)
+    r2 = (d * d).sum(1)
+    r = np.sqrt(r2)
+    m = spec.model
+    margins = [np.abs(r2 - spec.max_dist2).min(), np.abs(r - 1.12246 * spec.hs_sigma).min()]
+    ppt = list(m.patches_per_type)
+    cum = np.asarray(m.count_per_type)
+    types = np.searchsorted(cum, np.arange(spec.n), side="right")
+    ooff = np.concatenate([[0], np.cumsum(ppt)])
+    params = np.asarray(m.params).reshape(-1, 3)
+    orient = np.asarray(m.orient).reshape(-1, 3)
+    Qm = Q.reshape(-1, 3, 3)
+    u = d / r[:, None]
+    ps = 0
+    for a in range(len(ppt)):
+        for b in range(a, len(ppt)):
+            sel = (types[pr[:, 0]] == a) & (types[pr[:, 1]] == b) & (r2 < spec.max_dist2)
+            for i in range(ppt[a]):
+                for j in range(ppt[b]):
+                    q = ps + i * ppt[b] + j
+                    att, dis, th = params[q]
+                    n1 = np.einsum("k,pkc->pc", orient[ooff[a] + i], Qm[pr[sel, 0]])
+                    n2 = np.einsum("k,pkc->pc", orient[ooff[b] + j], Qm[pr[sel, 1]])
+                    ci = -(n1 * u[sel]).sum(1)
+                    cj = (n2 * u[sel]).sum(1)
+                    cm = math.cos(th)
+                    live = (ci > cm - 1e-3) & (cj > cm - 1e-3)
+                    if live.any():
+                        margins.append(np.abs(ci[live] - cm).min())
+                        margins.append(np.abs(cj[live] - cm).min())
+                        margins.append(np.abs(np.abs(ci[live] ** 2 - 1) - 1e-5).min())
+                        margins.append(np.abs(np.abs(cj[live] ** 2 - 1) - 1e-5).min())
+                        margins.append(np.abs(r[sel][live] - 1.4 * dis).min())
+            ps += ppt[a] * ppt[b]
+    return float(min(margins))
+
+
+def make_system(kind, n, phi, seed, periodic=True, min_dist=0.9, kT=1.0):
+    box = box_for(n, phi)
+    if kind == "tetra":
+        model = PatchModelSpec.tetrahedral(n, 8.0, 1.2, math.acos(0.90))
+    elif kind == "tubulin":
+        model = tubulin_model(n)
+    elif kind == "crowded":
+        model = crowded_model(n // 4, n)
+    elif kind == "bivalent":
+        model = PatchModelSpec.bivalent(n, 8.0, 1.2, math.acos(0.90))
+    else:
+        raise ValueError(kind)
+    spec = ReplicaSpec(n=n, box=box, model=model, periodic=periodic, kT=kT, seed=seed)
+    x = f32(random_positions(n, box, periodic, min_dist, 1000 + seed))
+    Q = f32(random_rotations(n, 2000 + seed))
+    return spec, x, Q
+
+
+def spec_record(spec):
+    m = spec.model
+    return dict(n=spec.n, box=spec.box, periodic=int(spec.periodic), dt=spec.dt, kT=spec.kT, gamma=spec.gamma,
+                gammar=spec.gammar, mass=spec.mass, inertia=spec.inertia, hs_eps=spec.hs_eps, hs_sigma=spec.hs_sigma,
+                max_dist2=spec.max_dist2, seed=spec.seed, patches_per_type=np.asarray(m.patches_per_type),
+                count_per_type=np.asarray(m.count_per_type), orient=np.asarray(m.orient, float),
+                params=np.asarray(m.params, float))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    args = ap.parse_args()
+    po.build_oracle()
+    po.build_ref(args.reference)
+    assert po.ref() is not None, "reference shim not built"
+
+    # ---- A. pair sets (MD::calculatepairs and calculatepairs_parallel)
+    pair_cases = [("tetra", 1000, 0.10, 1, True, 1.68), ("tetra", 1000, 0.30, 2, True, 1.5),
+                  ("tetra", 600, 0.10, 3, False, 1.68), ("tetra", 800, 0.10, 4, True, 3.5),
+                  ("tetra", 10, 0.10, 5, True, 1.68), ("tetra", 3, 0.05, 6, True, 1.2),
+                  ("tetra", 40, 0.15, 7, False, 1.68)]
+    for k, (kind, n, phi, seed, per, rc) in enumerate(pair_cases):
+        spec, x, Q = make_system(kind, n, phi, seed, per)
+        ncell = max(1, int(math.floor(spec.box / rc)))
+        p1 = ref_pairs(spec, x, ncell, rc)
+        p2 = ref_pairs(spec, x, ncell, rc, parallel=True)
+        assert np.array_equal(p1, p2)
+        np.savez_compressed(HERE / f"pairs_{k}.npz", x=x, rc=rc, ncell=ncell, pairs=p1, **spec_record(spec))
+        print(f"pairs_{k}: n={n} L={spec.box:.3f} ncell={ncell} periodic={per} pairs={len(p1)}")
+
+    # ---- B. forces and torques (calculateforces(HS) + calculate_forces_and_torques3D(ComboPatch))
+    force_cases = [("tetra", 800, 0.30), ("tubulin", 800, 0.30), ("crowded", 800, 0.30), ("bivalent", 600, 0.30),
+                   ("tetra", 200, 0.10)]
+    for k, (kind, n, phi) in enumerate(force_cases):
+        for seed in range(50):
+            spec, x, Q = make_system(kind, n, phi, 10 * k + seed, True, min_dist=0.95)
+            rc = po.System(spec).force_range * 1.05
+            if threshold_margin(spec, x, Q, rc) > 1e-6:
+                break
+        F, T = ref_forces(spec, x, Q, rc)
+        np.savez_compressed(HERE / f"forces_{k}.npz", x=x, Q=Q, rc=rc, F=F, T=T, **spec_record(spec))
+        print(f"forces_{k}: {kind} n={n} |F|max={np.abs(F).max():.3g} |T|max={np.abs(T).max():.3g} "
+              f"patch-torqued particles={(np.abs(T).sum(1) > 0).sum()}")
+
+    # ---- C. 100-step trajectories: noise off (kT = 0) and shared pre-generated noise
+    traj_cases = [("tetra", 256, 0.30, 0.0, "off"), ("tetra", 256, 0.30, 1.0, "shared"),
+                  ("tubulin", 256, 0.30, 1.0, "shared"), ("crowded", 256, 0.30, 1.0, "shared")]
+    for k, (kind, n, phi, kT, mode) in enumerate(traj_cases):
+        spec, x, Q = make_system(kind, n, phi, 100 + k, True, min_dist=0.95, kT=kT)
+        st0 = dict(x=x.copy(), p=np.zeros((n, 3)), Lb=np.zeros((n, 3)), Q=Q.copy(), Ft=np.zeros((n, 3)),
+                   Tt=np.zeros((n, 3)))
+        nsteps = 100
+        noise = po.philox_noise(n * (nsteps + 1), 77 + k, 0, 0).reshape(nsteps + 1, n, 6) if mode == "shared" else None
+        st = {kk: v.copy() for kk, v in st0.items()}
+        rc = 1.68
+        temps = ref_run(spec, st, nsteps, rc, 1, None if noise is None else np.ascontiguousarray(noise[1:]), True,
+                        None if noise is None else np.ascontiguousarray(noise[0]))
+        np.savez_compressed(HERE / f"traj_{k}.npz", x0=st0["x"], Q0=st0["Q"], nsteps=nsteps, noise_seed=77 + k,
+                            noise_mode=mode, rc=rc, temps=temps, **{"final_" + kk: v for kk, v in st.items()},
+                            **spec_record(spec))
+        print(f"traj_{k}: {kind} kT={kT} noise={mode} <p^2/2>={temps[-1, :3].mean():.4f}")
+
+    # ---- D. two-particle torque cases (kT = 0), after Code/BugReports/TorqueBug.md
+    rng = np.random.default_rng(5)
+    cases = []
+    for k in range(6):
+        spec = ReplicaSpec(n=2, box=10.0, model=PatchModelSpec.tetrahedral(2, 8.0, 1.2, math.acos(0.90)), kT=0.0)
+        x = np.array([[5.0, 5.0, 5.0], [5.0 + 1.05 + 0.05 * k, 5.0, 5.0]])
+        # rotate each body so that one patch points (almost) at the other particle
+        Qs = []
+        for a, target in ((0, np.array([1.0, 0, 0])), (1, np.array([-1.0, 0, 0]))):
+            v = target + 0.2 * rng.normal(size=3)
+            v /= np.linalg.norm(v)
+            nb = po.System(spec).spec.model.orient[k % 4]
+            # lab patch = Q^T nb; pick Q = R(nb -> v)^T so that Q^T nb = v
+            ax = np.cross(nb, v)
+            s, c = np.linalg.norm(ax), float(nb @ v)
+            K = np.array([[0, -ax[2], ax[1]], [ax[2], 0, -ax[0]], [-ax[1], ax[0], 0]]) / (s if s > 0 else 1)
+            Rm = np.eye(3) + s * K + (1 - c) * K @ K
+            Qs.append(Rm.T.reshape(9))
+        Q = f32(np.array(Qs))
+        x = f32(x)
+        st = dict(x=x.copy(), p=np.zeros((2, 3)), Lb=np.zeros((2, 3)), Q=Q.copy(), Ft=np.zeros((2, 3)),
+                  Tt=np.zeros((2, 3)))
+        x0, Q0 = x.copy(), Q.copy()
+        ref_run(spec, st, 200, 3.0, 1)
+        np.savez_compressed(HERE / f"torque_{k}.npz", x0=x0, Q0=Q0, nsteps=200, rc=3.0,
+                            **{"final_" + kk: v for kk, v in st.items()}, **spec_record(spec))
+        cases.append(np.abs(st["Lb"]).max())
+    print("torque cases: max |L| after 200 steps", np.round(cases, 4))
+
+    # ---- E. free-rotor rotation matrices (genfullmat)
+    Ls = rng.normal(size=(64, 3)) * np.array([[0.1], [1.0], [10.0], [50.0]]).repeat(16, 0)
+    Rs = np.empty((64, 9))
+    for i, L in enumerate(Ls):
+        L = np.ascontiguousarray(L)
+        po.ref().ref_rotation_matrix(0.005, D(L), D(Rs[i]))
+    np.savez_compressed(HERE / "rotation.npz", L=Ls, R=Rs, dt=0.005, inertia=0.1)
+    print("rotation.npz written")
+
+
+if __name__ == "__main__":
+    main()
