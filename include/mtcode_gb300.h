@@ -92,6 +92,8 @@ typedef struct {
     const mtg_replica_desc *replicas;
     int device;                        /* CUDA device ordinal */
     int track_displacement;            /* 1: keep FP64 unwrapped-displacement accumulators */
+    int force_kernel;                  /* FP32 only: 0 = tiled shared-memory kernel (default),
+                                          1 = one thread per particle (the form the FP64 path uses) */
 } mtg_config;
 
 /* Fill `m` with TetrahedralPatch(att, dis, thetam) / BivalentPatch(att, dis, thetam). */

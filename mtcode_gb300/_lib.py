@@ -65,6 +65,7 @@ class Config(C.Structure):
         ("replicas", C.POINTER(ReplicaDesc)),
         ("device", C.c_int),
         ("track_displacement", C.c_int),
+        ("force_kernel", C.c_int),
     ]
 
 

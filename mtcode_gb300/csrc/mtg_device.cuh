@@ -1,13 +1,15 @@
 // mtg_device.cuh -- device-side data layout and per-pair physics of the GB300 patchy-Langevin step.
 //
 // HBM layout (one handle, all replicas concatenated; "slot" = position in cell-sorted order):
-//   payload[slot]  12 reals  (x, y, z, Q0 | Q1..Q4 | Q5..Q8)          read by every neighbour
+//   pos[slot]      4 reals   (x, y, z, Q8)       the only array neighbour scans read (16 B in FP32)
+//   rota[slot]     4 reals   (Q0, Q1, Q2, Q3)    read for in-range pairs only
+//   rotb[slot]     4 reals   (Q4, Q5, Q6, Q7)
 //   motion[slot]   12 reals  (px, py, pz, Lx | Ly, Lz, F~x, F~y | F~z, T~x, T~y, T~z)
 //   ident[slot]    int32 global particle index (replica offset + reference particle index)
 //   disp_{x,y,z}   FP64 unwrapped displacement (SoA, optional)
 //   bin[slot]      int2 (global cell, rank inside the cell) of the particle's NEXT position
 //   cell_count / cell_start   per global cell (replica cell blocks are contiguous)
-// Every row is 48 B (FP32) or 96 B (FP64), so rows are 16-byte aligned and move as float4/double2.
+// Every element is 16 B (FP32) or 32 B (FP64) aligned, so rows move as float4/double2 vectors.
 #pragma once
 
 #include <cstdint>
@@ -18,7 +20,7 @@ namespace mtg {
 constexpr int kMaxTypes = 4;
 constexpr int kMaxOrient = 16;
 constexpr int kMaxPots = 64;
-constexpr int kRow = 12;  // reals per payload / motion row
+constexpr int kRow = 12;  // reals per motion row
 
 // ------------------------------------------------------------------ per-replica constants
 template <class real>
@@ -91,7 +93,24 @@ template <> struct Row<double> {
     }
 };
 
-// position only (first 16 bytes of a payload row for FP32, first 32 for FP64)
+// four consecutive reals (one 16-byte vector in FP32, two in FP64)
+__device__ __forceinline__ void load4(const float *p, float v[4]) {
+    float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+__device__ __forceinline__ void load4(const double *p, double v[4]) {
+    double2 a = __ldg(reinterpret_cast<const double2 *>(p)), b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+__device__ __forceinline__ void store4(float *p, float a, float b, float c, float d) {
+    *reinterpret_cast<float4 *>(p) = make_float4(a, b, c, d);
+}
+__device__ __forceinline__ void store4(double *p, double a, double b, double c, double d) {
+    reinterpret_cast<double2 *>(p)[0] = make_double2(a, b);
+    reinterpret_cast<double2 *>(p)[1] = make_double2(c, d);
+}
+
+// position of a slot (pos array: x, y, z, Q8)
 __device__ __forceinline__ void load_pos(const float *p, float &x, float &y, float &z) {
     float4 a = __ldg(reinterpret_cast<const float4 *>(p));
     x = a.x; y = a.y; z = a.z;
@@ -100,6 +119,26 @@ __device__ __forceinline__ void load_pos(const double *p, double &x, double &y, 
     double2 a = __ldg(reinterpret_cast<const double2 *>(p));
     x = a.x; y = a.y; z = __ldg(p + 2);
 }
+
+// position + orientation of one slot in logical order v = (x, y, z, Q0..Q8)
+template <class real>
+struct Payload {
+    real v[12];
+    __device__ __forceinline__ void load(const real *pos, const real *rota, const real *rotb, size_t s) {
+        real a[4], b[4], c[4];
+        load4(pos + 4 * s, a);
+        load4(rota + 4 * s, b);
+        load4(rotb + 4 * s, c);
+        v[0] = a[0]; v[1] = a[1]; v[2] = a[2]; v[11] = a[3];
+        v[3] = b[0]; v[4] = b[1]; v[5] = b[2]; v[6] = b[3];
+        v[7] = c[0]; v[8] = c[1]; v[9] = c[2]; v[10] = c[3];
+    }
+    __device__ __forceinline__ void store(real *pos, real *rota, real *rotb, size_t d) const {
+        store4(pos + 4 * d, v[0], v[1], v[2], v[11]);
+        store4(rota + 4 * d, v[3], v[4], v[5], v[6]);
+        store4(rotb + 4 * d, v[7], v[8], v[9], v[10]);
+    }
+};
 
 // ------------------------------------------------------------------ correctly rounded, uncontracted ops
 // The integrator uses explicit roundings so that the binning pass and the scatter pass compute the
@@ -206,13 +245,13 @@ template <> struct Acc3<double> {
 
 // ------------------------------------------------------------------ physics of one pair
 
-// HSPotential::force (potential.h:106-118): magnitude, 0 beyond 1.12246 sigma
+// HSPotential::force (potential.h:106-118) divided by r: 4 eps (12 s^12/r^14 - 6 s^6/r^8), written in
+// terms of r^2 so no power of a rounded square root enters; the caller applies the r < 1.12246 sigma cut.
 template <class real>
-__device__ __forceinline__ real hs_force(const Replica<real> &R, real r) {
-    if (!(r < R.hs_limit)) return real(0);
-    real a = r * r * r;
-    a = a * a;
-    return R.hs_4eps * (real(12) * R.hs_s12 / (r * a * a) - real(6) * R.hs_s6 / (r * a));
+__device__ __forceinline__ real hs_force_over_r(const Replica<real> &R, real r2) {
+    real inv2 = real(1) / r2;
+    real s6 = R.hs_s6 * inv2 * inv2 * inv2;  // (sigma/r)^6
+    return R.hs_4eps * inv2 * (real(12) * s6 * s6 - real(6) * s6);
 }
 
 // shifted WCA energy used for the energy observable

@@ -8,7 +8,7 @@
 //   [scatter]  half-kick, drift + wrap, free-rotor rotation, written straight to the particle's new
 //              slot: the counting sort and the first half of the integrator are one pass
 //   [force]    one thread per particle: WCA core + KF2 patch force/torque over the 27 neighbour
-//              cells (9 contiguous row ranges of the sorted payload), then friction + Philox noise,
+//              cells (9 contiguous row ranges of the sorted positions), then friction + Philox noise,
 //              the second half-kick, and the binning of the next step
 #pragma once
 
@@ -21,7 +21,7 @@ enum ForceMode : int { kModeStep = 0, kModeInit = 1, kModeForces = 2, kModeObs =
 
 template <class real>
 struct Buffers {
-    real *payload;
+    real *pos, *rota, *rotb;  // 4 reals per slot each: (x, y, z, Q8), (Q0..Q3), (Q4..Q7)
     real *motion;
     int *ident;
     double *dx, *dy, *dz;  // unwrapped displacement (nullable)
@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(256) bin_kernel(Tables<real> tb, Buffers<real>
         const int r = find_replica(tb.rep_slot, tb.nrep, s);
         const Replica<real> R = tb.reps[r];
         real x[3];
-        load_pos(in.payload + (size_t)s * kRow, x[0], x[1], x[2]);
+        load_pos(in.pos + 4 * (size_t)s, x[0], x[1], x[2]);
         if (MOVE) {
             Row<real> m;
             m.load(in.motion + (size_t)s * kRow);
@@ -244,8 +244,9 @@ __global__ void __launch_bounds__(256) scatter_kernel(Tables<real> tb, Buffers<r
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
         const int2 kb = bin[s];
         const int d = __ldg(start + kb.x) + kb.y;
-        Row<real> P, M;
-        P.load(in.payload + (size_t)s * kRow);
+        Payload<real> P;
+        Row<real> M;
+        P.load(in.pos, in.rota, in.rotb, s);
         M.load(in.motion + (size_t)s * kRow);
         const int id = in.ident[s];
         if (MOVE) {
@@ -289,7 +290,7 @@ __global__ void __launch_bounds__(256) scatter_kernel(Tables<real> tb, Buffers<r
             out.dy[d] = in.dy[s];
             out.dz[d] = in.dz[s];
         }
-        P.store(out.payload + (size_t)d * kRow);
+        P.store(out.pos, out.rota, out.rotb, d);
         M.store(out.motion + (size_t)d * kRow);
         out.ident[d] = id;
     }
@@ -312,15 +313,18 @@ struct ForceArgs {
     int do_kick;                     // second half-kick (step) or not (init)
 };
 
+// One particle by one thread: the straightforward form of the force loop.  Used by the FP64 path,
+// the observable pass, replicas with fewer than three cells per side, and the FP32 tile kernel's
+// fallback for crowded tiles.
 template <class real, int MODE>
-__global__ void __launch_bounds__(128) force_kernel(ForceArgs<real> a) {
+__device__ __noinline__ void simple_particle(const ForceArgs<real> &a, int s) {
     const Tables<real> &tb = a.tb;
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
+    {
         const int r = find_replica(tb.rep_slot, tb.nrep, s);
         const Replica<real> &R = tb.reps[r];
         const Model<real> &Mo = tb.models[R.model];
-        Row<real> P;
-        P.load(a.buf.payload + (size_t)s * kRow);
+        Payload<real> P;
+        P.load(a.buf.pos, a.buf.rota, a.buf.rotb, s);
         const real xi = P.v[0], yi = P.v[1], zi = P.v[2];
         const real *Qi = P.v + 3;
         const int idi = a.buf.ident[s];
@@ -386,9 +390,8 @@ __global__ void __launch_bounds__(128) force_kernel(ForceArgs<real> a) {
                     const int j0 = seg ? seg_b0 : seg_a0, j1 = seg ? seg_b1 : seg_a1;
                     for (int j = j0; j < j1; j++) {
                         if (j == s) continue;
-                        const real *pj = a.buf.payload + (size_t)j * kRow;
                         real xj, yj, zj;
-                        load_pos(pj, xj, yj, zj);
+                        load_pos(a.buf.pos + 4 * (size_t)j, xj, yj, zj);
                         real dx = min_image<real>(xi - xj, R.box, R.l2s, R.periodic);
                         real dy2 = min_image<real>(yi - yj, R.box, R.l2s, R.periodic);
                         real dz2 = min_image<real>(zi - zj, R.box, R.l2s, R.periodic);
@@ -399,9 +402,8 @@ __global__ void __launch_bounds__(128) force_kernel(ForceArgs<real> a) {
                         // WCA core: same vector for both orientations of the pair
                         real fi[3] = {0, 0, 0};
                         if (rr < R.hs_limit) {
-                            real fh = hs_force<real>(R, rr);
-                            big |= fabs(fh) > real(1e4);
-                            real s_ = fh / rr;
+                            real s_ = hs_force_over_r<real>(R, r2);
+                            big |= fabs(s_ * rr) > real(1e4);
                             fi[0] = s_ * dx; fi[1] = s_ * dy2; fi[2] = s_ * dz2;
                             ewca += real(0.5) * wca_energy<real>(R, r2);
                         }
@@ -410,8 +412,8 @@ __global__ void __launch_bounds__(128) force_kernel(ForceArgs<real> a) {
                             const int idj = __ldg(a.buf.ident + j);
                             const int tj = single_type ? 0 : type_of<real>(Mo, idj - R.off);
                             if (Mo.np[ti] > 0 && Mo.np[tj] > 0) {
-                                Row<real> Pj;
-                                Pj.load(pj);
+                                Payload<real> Pj;
+                                Pj.load(a.buf.pos, a.buf.rota, a.buf.rotb, j);
                                 const bool i_first = idi < idj;  // canonical order of the reference (p1 < p2)
                                 real u[3];
                                 const real inv = real(1) / rr;
@@ -453,7 +455,7 @@ __global__ void __launch_bounds__(128) force_kernel(ForceArgs<real> a) {
             a.outT[3 * (size_t)idi + 1] = T.get(1);
             a.outT[3 * (size_t)idi + 2] = T.get(2);
             if (a.outE) a.outE[idi] = (double)ewca + (double)epatch;
-            continue;
+            return;
         }
         if (MODE == kModeObs) {
             // warp-shuffle reduction when the whole warp is in one replica, else per-lane atomics
@@ -466,7 +468,7 @@ __global__ void __launch_bounds__(128) force_kernel(ForceArgs<real> a) {
             double *o = a.obs + 5 * (size_t)r;
 #pragma unroll
             for (int k = 0; k < 5; k++) atomicAdd(o + k, v[k]);
-            continue;
+            return;
         }
 
         // ---- create_forces_and_torques_sphere (LangevinR.cpp:474-578) + advancemom_halfstep
@@ -520,6 +522,12 @@ __global__ void __launch_bounds__(128) force_kernel(ForceArgs<real> a) {
     }
 }
 
+template <class real, int MODE>
+__global__ void __launch_bounds__(128) force_kernel(ForceArgs<real> a) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < a.tb.ntot; s += gridDim.x * blockDim.x)
+        simple_particle<real, MODE>(a, s);
+}
+
 // ------------------------------------------------------------------ state in / out, reductions
 
 // host-order doubles (ntot rows) -> rows in slot order == global index order
@@ -527,7 +535,8 @@ template <class real>
 __global__ void load_state_kernel(int ntot, const double *x, const double *p, const double *Lb, const double *Q,
                                   const double *Ft, const double *Tt, Buffers<real> out) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ntot; i += gridDim.x * blockDim.x) {
-        Row<real> P, M;
+        Payload<real> P;
+        Row<real> M;
         P.v[0] = (real)x[3 * (size_t)i]; P.v[1] = (real)x[3 * (size_t)i + 1]; P.v[2] = (real)x[3 * (size_t)i + 2];
         for (int k = 0; k < 9; k++) P.v[3 + k] = (real)Q[9 * (size_t)i + k];
         for (int k = 0; k < 3; k++) {
@@ -536,7 +545,7 @@ __global__ void load_state_kernel(int ntot, const double *x, const double *p, co
             M.v[6 + k] = Ft ? (real)Ft[3 * (size_t)i + k] : real(0);
             M.v[9 + k] = Tt ? (real)Tt[3 * (size_t)i + k] : real(0);
         }
-        P.store(out.payload + (size_t)i * kRow);
+        P.store(out.pos, out.rota, out.rotb, i);
         M.store(out.motion + (size_t)i * kRow);
         out.ident[i] = i;
         if (out.dx) { out.dx[i] = 0; out.dy[i] = 0; out.dz[i] = 0; }
@@ -548,8 +557,9 @@ template <class real>
 __global__ void store_state_kernel(int ntot, Buffers<real> in, double *x, double *p, double *Lb, double *Q, double *Ft,
                                    double *Tt, double *disp) {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ntot; s += gridDim.x * blockDim.x) {
-        Row<real> P, M;
-        P.load(in.payload + (size_t)s * kRow);
+        Payload<real> P;
+        Row<real> M;
+        P.load(in.pos, in.rota, in.rotb, s);
         M.load(in.motion + (size_t)s * kRow);
         const size_t i = (size_t)in.ident[s];
         for (int k = 0; k < 3; k++) {

@@ -46,9 +46,9 @@ __device__ __forceinline__ bool distance_less_than(const double xi[3], const dou
 }
 
 template <class real>
-__device__ __forceinline__ void load_pos_d(const real *payload, int s, double x[3]) {
+__device__ __forceinline__ void load_pos_d(const real *pos, int s, double x[3]) {
     real a, b, c;
-    load_pos(payload + (size_t)s * kRow, a, b, c);
+    load_pos(pos + 4 * (size_t)s, a, b, c);
     x[0] = (double)a; x[1] = (double)b; x[2] = (double)c;
 }
 
@@ -56,7 +56,7 @@ template <class real>
 __global__ void pair_bin_kernel(PairGrid g, Buffers<real> in, int2 *bin, int *count) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
         double x[3];
-        load_pos_d<real>(in.payload, g.off + i, x);
+        load_pos_d<real>(in.pos, g.off + i, x);
         int key = pair_axis_cell(x[0], g.nc, g.box) + g.nc * (pair_axis_cell(x[1], g.nc, g.box) +
                                                               g.nc * pair_axis_cell(x[2], g.nc, g.box));
         int rank = atomicAdd(count + key, 1);
@@ -76,7 +76,7 @@ template <class real, class Fn>
 __device__ __forceinline__ void pair_visit(const PairGrid &g, const Buffers<real> &in, const int *start,
                                            const int *members, int s, int li, Fn f) {
     double xi[3];
-    load_pos_d<real>(in.payload, s, xi);
+    load_pos_d<real>(in.pos, s, xi);
     const int cx = pair_axis_cell(xi[0], g.nc, g.box), cy = pair_axis_cell(xi[1], g.nc, g.box),
               cz = pair_axis_cell(xi[2], g.nc, g.box);
     const int lo = g.nc >= 3 ? -1 : 0, hi = g.nc >= 2 ? 1 : 0;  // de-duplicated stencil (geometry.h:596-606)
@@ -90,7 +90,7 @@ __device__ __forceinline__ void pair_visit(const PairGrid &g, const Buffers<real
                     const int lj = in.ident[t] - g.off;
                     if (lj <= li) continue;
                     double xj[3];
-                    load_pos_d<real>(in.payload, t, xj);
+                    load_pos_d<real>(in.pos, t, xj);
                     // the reference tests (lower index, higher index) in that order
                     if (distance_less_than(xi, xj, g.box, g.periodic, g.rc)) f(lj);
                 }

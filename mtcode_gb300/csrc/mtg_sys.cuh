@@ -9,11 +9,13 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "mtg_kernels.cuh"
 #include "mtg_pairs.cuh"
 #include "mtg_sys_base.h"
+#include "mtg_tile.cuh"
 
 namespace mtg_impl {
 
@@ -132,6 +134,42 @@ inline int grid_for(int64_t n, int block, int per_sm, int sms) {
     return (int)std::max<int64_t>(1, std::min(need, cap));
 }
 
+// Tile plan of one replica for the FP32 tile kernel: whole x-rows or chunks of 32/16/8 cells, times
+// T x T rows (T = 4, 2, 1), chosen from the mean cell occupancy so that a tile holds about one
+// CTA's worth of particles (<= 256) and its staged halo fits the shared buffer with room to spare.
+inline void plan_tiles(int rep, int nc, double per_cell, std::vector<int4> &out) {
+    if (nc < 3 || nc > 1023) {
+        out.push_back(make_int4(rep, 0, 1 << 21, 0));
+        return;
+    }
+    struct Cand { bool whole; int tx, T; double home, staged; };
+    std::vector<Cand> cands;
+    for (int T : {4, 2, 1}) {
+        if (nc <= mtg::kTileXMax) cands.push_back({true, nc, T, nc * T * T * per_cell, nc * (T + 2.0) * (T + 2.0) * per_cell});
+        for (int tx : {32, 16, 8})
+            if (tx + 2 <= nc) cands.push_back({false, tx, T, tx * T * T * per_cell, (tx + 2.0) * (T + 2.0) * (T + 2.0) * per_cell});
+    }
+    const Cand *best = nullptr;
+    for (const Cand &c : cands) {
+        if (c.staged > 0.6 * mtg::kStageCap || c.home > 280) continue;
+        if (!best || c.home > best->home * 1.05 ||
+            (c.home > best->home * 0.95 && c.staged / c.home < best->staged / best->home))
+            best = &c;
+    }
+    if (!best)
+        for (const Cand &c : cands)
+            if (!best || c.staged < best->staged) best = &c;
+    const int T = best->T, tx = best->whole ? nc : best->tx;
+    for (int z0 = 0; z0 < nc; z0 += T)
+        for (int y0 = 0; y0 < nc; y0 += T)
+            for (int x0 = 0; x0 < nc; x0 += tx) {
+                const int ty = std::min(T, nc - y0), tz = std::min(T, nc - z0);
+                const int sx = best->whole ? nc : std::min(tx, nc - x0) + 2;
+                out.push_back(make_int4(rep, x0 | (y0 << 10) | (z0 << 20),
+                                        sx | (ty << 10) | (tz << 15) | ((best->whole ? 1 : 0) << 20), 0));
+            }
+}
+
 template <class real>
 struct Sys : SysBase {
     int device = 0;
@@ -163,6 +201,11 @@ struct Sys : SysBase {
     bool have_state = false, cells_valid = false, bins_valid = false, forces_ready = false;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int64_t nlaunch = 0;
+    // FP32 tile kernel
+    bool use_tiles = false;
+    int4 *d_tiles = nullptr;
+    int ntiles = 0, occ_tile = 1;
+    size_t tile_smem = 0;
     // occupancy-derived grid caps
     int occ_force = 1, occ_stream = 1;
 
@@ -206,7 +249,9 @@ struct Sys : SysBase {
         MTG_CUDA(cudaMemcpy(d_models, models.data(), sizeof(mtg::Model<real>) * nrep, cudaMemcpyHostToDevice));
         MTG_CUDA(cudaMemcpy(d_rep_slot, rep_slot.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice));
         for (int b = 0; b < 2; b++) {
-            MTG_CUDA(cudaMalloc(&buf[b].payload, sizeof(real) * mtg::kRow * n));
+            MTG_CUDA(cudaMalloc(&buf[b].pos, sizeof(real) * 4 * n));
+            MTG_CUDA(cudaMalloc(&buf[b].rota, sizeof(real) * 4 * n));
+            MTG_CUDA(cudaMalloc(&buf[b].rotb, sizeof(real) * 4 * n));
             MTG_CUDA(cudaMalloc(&buf[b].motion, sizeof(real) * mtg::kRow * n));
             MTG_CUDA(cudaMalloc(&buf[b].ident, sizeof(int) * n));
             if (track_disp) {
@@ -233,6 +278,27 @@ struct Sys : SysBase {
         occ_force = std::max(occ, 1);
         MTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mtg::scatter_kernel<real, true>, 256, 0));
         occ_stream = std::max(occ, 1);
+        if constexpr (std::is_same<real, float>::value) {
+            use_tiles = cfg.force_kernel != 1;
+            if (use_tiles) {
+                std::vector<int4> tiles;
+                for (int r = 0; r < nrep; r++)
+                    plan_tiles(r, reps[r].nc, (double)desc[r].n / ((double)reps[r].nc * reps[r].nc * reps[r].nc), tiles);
+                ntiles = (int)tiles.size();
+                MTG_CUDA(cudaMalloc(&d_tiles, sizeof(int4) * ntiles));
+                MTG_CUDA(cudaMemcpy(d_tiles, tiles.data(), sizeof(int4) * ntiles, cudaMemcpyHostToDevice));
+                tile_smem = sizeof(mtg::TileShared);
+                MTG_CUDA(cudaFuncSetAttribute(mtg::tile_force_kernel<mtg::kModeStep>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem));
+                MTG_CUDA(cudaFuncSetAttribute(mtg::tile_force_kernel<mtg::kModeInit>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem));
+                MTG_CUDA(cudaFuncSetAttribute(mtg::tile_force_kernel<mtg::kModeForces>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem));
+                MTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mtg::tile_force_kernel<mtg::kModeStep>,
+                                                                       mtg::kTileThreads, tile_smem));
+                occ_tile = std::max(occ, 1);
+            }
+        }
         MTG_CUDA(cudaStreamSynchronize(st));
     }
 
@@ -241,12 +307,13 @@ struct Sys : SysBase {
         if (st) cudaStreamSynchronize(st);
         for (int b = 0; b < 2; b++) {
             if (graph[b]) cudaGraphExecDestroy(graph[b]);
-            cudaFree(buf[b].payload); cudaFree(buf[b].motion); cudaFree(buf[b].ident);
+            cudaFree(buf[b].pos); cudaFree(buf[b].rota); cudaFree(buf[b].rotb); cudaFree(buf[b].motion); cudaFree(buf[b].ident);
             cudaFree(buf[b].dx); cudaFree(buf[b].dy); cudaFree(buf[b].dz);
         }
         cudaFree(d_reps); cudaFree(d_reps_obs); cudaFree(d_models); cudaFree(d_rep_slot);
         cudaFree(d_bin); cudaFree(d_count); cudaFree(d_start); cudaFree(d_block);
         cudaFree(d_flags); cudaFree(d_draw); cudaFree(d_stage); cudaFree(d_noise); cudaFree(d_obs);
+        cudaFree(d_tiles);
         if (h_flags) cudaFreeHost(h_flags);
         if (st) cudaStreamDestroy(st);
     }
@@ -309,6 +376,20 @@ struct Sys : SysBase {
         return a;
     }
 
+    // force pass in the given mode: the FP32 tile kernel where it applies, else the per-particle kernel
+    template <int MODE>
+    void launch_force(const mtg::ForceArgs<real> &a) {
+        if constexpr (std::is_same<real, float>::value) {
+            if (use_tiles && MODE != mtg::kModeObs && !a.outE) {
+                const int g = std::max(1, std::min(ntiles, occ_tile * sms));
+                mtg::tile_force_kernel<MODE><<<g, mtg::kTileThreads, tile_smem, st>>>(a, d_tiles, ntiles);
+                return;
+            }
+        }
+        const int gf = grid_for(ntot_, 128, occ_force, sms);
+        mtg::force_kernel<real, MODE><<<gf, 128, 0, st>>>(a);
+    }
+
     // one step from buffer b: scan (+draw), scatter b -> b^1, force on b^1
     void enqueue_step(int b, const double *ext_noise) {
         mtg::Tables<real> tb = tables();
@@ -317,8 +398,7 @@ struct Sys : SysBase {
         mtg::scatter_kernel<real, true><<<g, 256, 0, st>>>(tb, buf[b], buf[b ^ 1], d_bin, d_start, d_flags);
         mtg::ForceArgs<real> a = force_args(b ^ 1, 1);
         a.ext_noise = ext_noise;
-        const int gf = grid_for(ntot_, 128, occ_force, sms);
-        mtg::force_kernel<real, mtg::kModeStep><<<gf, 128, 0, st>>>(a);
+        launch_force<mtg::kModeStep>(a);
         check_launch();
     }
 
@@ -397,8 +477,7 @@ struct Sys : SysBase {
         tick_draw();
         mtg::ForceArgs<real> a = force_args(cur, 0);
         if (noise) a.ext_noise = upload_noise(noise);
-        const int gf = grid_for(ntot_, 128, occ_force, sms);
-        mtg::force_kernel<real, mtg::kModeInit><<<gf, 128, 0, st>>>(a);
+        launch_force<mtg::kModeInit>(a);
         check_launch();
         nlaunch += 1;
         cells_valid = true;
@@ -477,7 +556,7 @@ struct Sys : SysBase {
             mtg::scatter_kernel<real, true><<<g, 256, 0, st>>>(tb, buf[b], buf[b ^ 1], d_bin, d_start, d_flags);
             MTG_CUDA(cudaEventRecord(ev[4], st));
             mtg::ForceArgs<real> a = force_args(b ^ 1, 1);
-            mtg::force_kernel<real, mtg::kModeStep><<<gf, 128, 0, st>>>(a);
+            launch_force<mtg::kModeStep>(a);
             MTG_CUDA(cudaEventRecord(ev[5], st));
             check_launch();
             MTG_CUDA(cudaEventSynchronize(ev[5]));
@@ -506,8 +585,7 @@ struct Sys : SysBase {
         a.outF = sF;
         a.outT = sT;
         a.outE = E ? sE : nullptr;
-        const int gf = grid_for(ntot_, 128, occ_force, sms);
-        mtg::force_kernel<real, mtg::kModeForces><<<gf, 128, 0, st>>>(a);
+        launch_force<mtg::kModeForces>(a);
         check_launch();
         nlaunch += 1;
         MTG_CUDA(cudaMemcpyAsync(F, sF, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
@@ -543,8 +621,7 @@ struct Sys : SysBase {
         a.tb = tables(true);
         a.obs = d_obs;
         std::vector<double> h(6 * (size_t)nrep);
-        const int gf = grid_for(ntot_, 128, occ_force, sms);
-        mtg::force_kernel<real, mtg::kModeObs><<<gf, 128, 0, st>>>(a);
+        launch_force<mtg::kModeObs>(a);
         check_launch();
         nlaunch += 1;
         MTG_CUDA(cudaMemcpyAsync(h.data(), d_obs, sizeof(double) * 6 * nrep, cudaMemcpyDeviceToHost, st));

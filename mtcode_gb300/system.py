@@ -101,7 +101,8 @@ def _check(h, status: int) -> None:
 class LangevinNVTRGPU:
     """All replicas of one GPU handle (one CUDA stream)."""
 
-    def __init__(self, replicas: list, precision: str = "fp32", device: int = 0, track_displacement: bool = True):
+    def __init__(self, replicas: list, precision: str = "fp32", device: int = 0, track_displacement: bool = True,
+                 force_kernel: str = "tiled"):
         L = _lib.lib()
         self.replicas = list(replicas)
         self._descs = (_lib.ReplicaDesc * len(self.replicas))(*[r.to_c() for r in self.replicas])
@@ -111,6 +112,7 @@ class LangevinNVTRGPU:
         cfg.replicas = C.cast(self._descs, C.POINTER(_lib.ReplicaDesc))
         cfg.device = int(device)
         cfg.track_displacement = int(bool(track_displacement))
+        cfg.force_kernel = 1 if force_kernel == "per_particle" else 0
         h = C.c_void_p()
         st = L.mtg_create(C.byref(cfg), C.byref(h))
         if st != 0:

@@ -49,3 +49,17 @@ def norm_rel_err(a, b) -> float:
     a = np.asarray(a).ravel()
     b = np.asarray(b).ravel()
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def force_errors(a, b) -> dict:
+    """Error of a per-particle vector field a against the reference b (both n x 3):
+    rms   ||a - b||_2 / ||b||_2 over all particles -- the force relative error of the tests;
+    max   max_i |a_i - b_i| / rms_i |b_i|  -- the worst particle, in units of the RMS force.
+    (A per-particle relative error |a_i - b_i| / |b_i| is ill-conditioned where pair forces of tens of
+    eps/sigma cancel to a small net force, so it is reported only against the RMS scale.)"""
+    a = np.asarray(a).reshape(len(b), -1)
+    b = np.asarray(b).reshape(len(b), -1)
+    d = np.linalg.norm(a - b, axis=1)
+    nb = np.linalg.norm(b, axis=1)
+    scale = max(float(np.sqrt((nb ** 2).mean())), 1e-300)
+    return {"rms": float(np.linalg.norm(d) / max(np.linalg.norm(nb), 1e-300)), "max": float(d.max() / scale)}

@@ -63,7 +63,7 @@ def test_create_without_device_fails_cleanly():
     L.mtg_replica_defaults(C.byref(reps[0]))
     reps[0].n, reps[0].box = 10, 10.0
     L.mtg_model_tetrahedral(C.byref(reps[0].model), 8.0, 1.2, 0.45)
-    cfg = _lib.Config(0, 1, C.cast(reps, C.POINTER(_lib.ReplicaDesc)), 0, 1)
+    cfg = _lib.Config(0, 1, C.cast(reps, C.POINTER(_lib.ReplicaDesc)), 0, 1, 0)
     h = C.c_void_p()
     st = L.mtg_create(C.byref(cfg), C.byref(h))
     assert st == 8 and not h.value

@@ -1,0 +1,121 @@
+"""GPU tests of the batched path: many uneven replicas in one handle.
+
+  forces of every replica of a batch vs the oracle (both FP32 force kernels, and FP64);
+  a replica advanced inside a batch equals the same replica advanced alone (noise off);
+  FP32 steps are bit-for-bit reproducible run to run (fixed-point force sums + counter-based noise);
+  at the full batched size, Newton's third law holds exactly (the fixed-point pair sums cancel).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from mtcode_gb300 import LangevinNVTRGPU
+from mtcode_gb300 import workloads
+from oracle import pyoracle as po
+from tests._util import force_errors
+
+pytestmark = pytest.mark.gpu
+
+
+def small_batch(seed=3, n_replicas=12, phi=0.15, kT=None):
+    W = workloads.patchy_c4(seed=seed, n_replicas=n_replicas, n_min=200, n_max=6000, phi=phi)
+    if kT is not None:
+        for r in W.replicas:
+            r.kT = kT
+    W.x = W.x.astype(np.float32).astype(np.float64)
+    W.Q = W.Q.astype(np.float32).astype(np.float64)
+    return W
+
+
+def offsets(W):
+    return np.concatenate([[0], np.cumsum([r.n for r in W.replicas])])
+
+
+@pytest.mark.parametrize("precision,kernel", [("fp32", "tiled"), ("fp32", "per_particle"), ("fp64", "tiled")])
+def test_batched_forces_vs_oracle(precision, kernel):
+    W = small_batch(phi=0.3)
+    z = W.zeros3()
+    with LangevinNVTRGPU(W.replicas, precision=precision, force_kernel=kernel) as s:
+        s.initialize(W.x, z, z, W.Q)
+        F, T = s.calculate_forces_and_torques3D()
+    off = offsets(W)
+    for r, spec in enumerate(W.replicas):
+        a, b = off[r], off[r + 1]
+        Fo, To = po.System(spec).forces(W.x[a:b], W.Q[a:b])
+        rms_tol = 1e-12 if precision == "fp64" else 1e-5
+        assert force_errors(F[a:b], Fo)["rms"] <= rms_tol, r
+        assert force_errors(T[a:b], To)["rms"] <= rms_tol, r
+
+
+def test_tiled_and_per_particle_kernels_agree():
+    W = small_batch(seed=5, phi=0.25)
+    z = W.zeros3()
+    out = {}
+    for kernel in ("tiled", "per_particle"):
+        with LangevinNVTRGPU(W.replicas, force_kernel=kernel) as s:
+            s.initialize(W.x, z, z, W.Q)
+            out[kernel] = s.calculate_forces_and_torques3D()
+    assert force_errors(out["tiled"][0], out["per_particle"][0])["rms"] <= 1e-6
+    assert force_errors(out["tiled"][1], out["per_particle"][1])["rms"] <= 1e-6
+
+
+@pytest.mark.parametrize("kernel", ["tiled", "per_particle"])
+def test_replica_in_batch_equals_replica_alone(kernel):
+    W = small_batch(seed=7, n_replicas=6, kT=0.0)
+    z = W.zeros3()
+    with LangevinNVTRGPU(W.replicas, force_kernel=kernel) as s:
+        s.initialize(W.x, z, z, W.Q)
+        s.init_forces()
+        s.step(25)
+        batch = s.get_state()
+    off = offsets(W)
+    for r in (0, 3, 5):
+        a, b = off[r], off[r + 1]
+        zz = np.zeros((b - a, 3))
+        with LangevinNVTRGPU([W.replicas[r]], force_kernel=kernel) as s1:
+            s1.initialize(W.x[a:b], zz, zz, W.Q[a:b])
+            s1.init_forces()
+            s1.step(25)
+            alone = s1.get_state()
+        for key in ("x", "p", "Lb", "Q"):
+            assert np.array_equal(batch[key][a:b], alone[key]), (r, key)
+
+
+def test_fp32_steps_are_bitwise_reproducible():
+    W = small_batch(seed=11, n_replicas=8)
+    z = W.zeros3()
+    finals = []
+    for _ in range(2):
+        with LangevinNVTRGPU(W.replicas) as s:
+            s.initialize(W.x, z, z, W.Q)
+            s.init_forces()
+            s.step(40)
+            finals.append(s.get_state())
+    for key in finals[0]:
+        assert np.array_equal(finals[0][key], finals[1][key]), key
+
+
+def test_full_size_batch_newton_third_law_and_finiteness():
+    """The benchmark workload (512 replicas, ~5 M particles): per replica the fixed-point pair sums
+    cancel exactly, so the total force is zero to the fixed-point resolution after the float round."""
+    W = workloads.patchy_c4(seed=0)
+    z = W.zeros3()
+    with LangevinNVTRGPU(W.replicas) as s:
+        s.initialize(W.x, z, z, W.Q)
+        F, T = s.calculate_forces_and_torques3D()
+        s.init_forces()
+        s.step(20)
+        st = s.get_state()
+        assert s.flags & 1 == 0
+    off = offsets(W)
+    sums = np.array([F[off[r]:off[r + 1]].sum(0) for r in range(len(W.replicas))])
+    # each particle's force is one float rounding of an exact integer sum: |sum| <= n * ulp(|F|max)
+    for r in range(len(W.replicas)):
+        Fr = F[off[r]:off[r + 1]]
+        bound = len(Fr) * np.spacing(np.float32(np.abs(Fr).max())) + 1e-6
+        assert np.abs(sums[r]).max() <= bound, r
+    assert np.isfinite(st["x"]).all() and np.isfinite(st["p"]).all() and np.isfinite(st["Lb"]).all()
+    for r, spec in enumerate(W.replicas):
+        xr = st["x"][off[r]:off[r + 1]]
+        assert (xr >= 0).all() and (xr <= spec.box).all()
