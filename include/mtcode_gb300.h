@@ -49,6 +49,9 @@ typedef enum { MTG_FP32 = 0, MTG_FP64 = 1 } mtg_precision;
 /* device-latched condition bits, read with mtg_flags() */
 #define MTG_FLAG_NONFINITE   0x1u   /* see MTG_ERR_NONFINITE */
 #define MTG_FLAG_FORCE_LIMIT 0x2u   /* some |pair force| > 1e4: where MD.cpp:1711-1749 would pausel() */
+#define MTG_FLAG_TIMEOUT     0x4u   /* a bounded device wait expired (see MTG_ERR_TIMEOUT) */
+#define MTG_FLAG_OVERFLOW    0x8u   /* a tile's pair list overflowed: handled by the per-particle path */
+#define MTG_FLAG_BINNING     0x10u  /* the cell histogram disagreed with the particle count: step skipped */
 
 typedef struct mtg_system mtg_system;
 

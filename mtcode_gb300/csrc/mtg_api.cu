@@ -262,7 +262,10 @@ mtg_status mtg_set_draw(mtg_system *h, uint64_t d) {
 mtg_status mtg_sync(mtg_system *h) {
     MTG_GUARD(h, {
         MTG_CUDA(cudaStreamSynchronize(h->impl->stream()));
-        if (h->impl->flags() & MTG_FLAG_NONFINITE) return MTG_ERR_NONFINITE;
+        const uint32_t f = h->impl->flags();
+        if (f & MTG_FLAG_TIMEOUT) throw Fail{MTG_ERR_TIMEOUT, "a bounded device wait expired"};
+        if (f & MTG_FLAG_BINNING) throw Fail{MTG_ERR_STATE, "cell binning incomplete: a step was skipped"};
+        if (f & MTG_FLAG_NONFINITE) return MTG_ERR_NONFINITE;
     });
     return MTG_OK;
 }

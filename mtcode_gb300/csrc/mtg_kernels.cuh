@@ -241,9 +241,18 @@ __device__ __forceinline__ void free_rotor(real dt, real inertia, const real L[3
 template <class real, bool MOVE>
 __global__ void __launch_bounds__(256) scatter_kernel(Tables<real> tb, Buffers<real> in, Buffers<real> out,
                                                       const int2 *bin, const int *start, unsigned *flags) {
+    // every particle must have been binned exactly once; otherwise nothing is moved (latched error)
+    if (__ldg(start + tb.ncells) != tb.ntot) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(flags, 16u);
+        return;
+    }
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
         const int2 kb = bin[s];
         const int d = __ldg(start + kb.x) + kb.y;
+        if (kb.x < 0 || kb.x >= tb.ncells || d < 0 || d >= tb.ntot) {
+            atomicOr(flags, 16u);
+            continue;
+        }
         Payload<real> P;
         Row<real> M;
         P.load(in.pos, in.rota, in.rotb, s);

@@ -135,8 +135,9 @@ inline int grid_for(int64_t n, int block, int per_sm, int sms) {
 }
 
 // Tile plan of one replica for the FP32 tile kernel: whole x-rows or chunks of 32/16/8 cells, times
-// T x T rows (T = 4, 2, 1), chosen from the mean cell occupancy so that a tile holds about one
-// CTA's worth of particles (<= 256) and its staged halo fits the shared buffer with room to spare.
+// T x T rows (T = 4, 2, 1).  Warps take 32-particle units of a tile, so larger tiles only lower the
+// halo share; the choice is the largest tile whose expected staged count (tile + one-cell halo, from
+// the mean cell occupancy) is at most half the staging buffer, leaving room for density fluctuations.
 inline void plan_tiles(int rep, int nc, double per_cell, std::vector<int4> &out) {
     if (nc < 3 || nc > 1023) {
         out.push_back(make_int4(rep, 0, 1 << 21, 0));
@@ -151,7 +152,7 @@ inline void plan_tiles(int rep, int nc, double per_cell, std::vector<int4> &out)
     }
     const Cand *best = nullptr;
     for (const Cand &c : cands) {
-        if (c.staged > 0.6 * mtg::kStageCap || c.home > 280) continue;
+        if (c.staged > 0.5 * mtg::kStageCap) continue;
         if (!best || c.home > best->home * 1.05 ||
             (c.home > best->home * 0.95 && c.staged / c.home < best->staged / best->home))
             best = &c;
@@ -381,7 +382,7 @@ struct Sys : SysBase {
     void launch_force(const mtg::ForceArgs<real> &a) {
         if constexpr (std::is_same<real, float>::value) {
             if (use_tiles && MODE != mtg::kModeObs && !a.outE) {
-                const int g = std::max(1, std::min(ntiles, occ_tile * sms));
+                const int g = std::max(1, std::min(ntiles, occ_tile * sms));  // persistent: one CTA per SM
                 mtg::tile_force_kernel<MODE><<<g, mtg::kTileThreads, tile_smem, st>>>(a, d_tiles, ntiles);
                 return;
             }

@@ -19,32 +19,57 @@
 namespace mtg {
 namespace {  // internal linkage
 
-constexpr int kTileThreads = 256;
+constexpr int kTileThreads = 512;  // one persistent CTA per SM: 15 consumer warps + 1 producer warp
+constexpr int kTileWarps = kTileThreads / 32;
+constexpr int kConsumerWarps = kTileWarps - 1;
+constexpr int kStageBufs = 3;      // ring of staging buffers: the producer runs up to two tiles ahead
 constexpr int kTileYZMax = 4;
 constexpr int kTileXMax = 32;
 constexpr int kStageCells = (kTileXMax + 2) * (kTileYZMax + 2) * (kTileYZMax + 2);  // 1224
-constexpr int kStageCap = 1536;   // staged particles per tile
-constexpr int kPairCap = 2560;    // in-range pairs per chunk of home particles
-constexpr int kTaskCap = 1024;    // in-cone patch potentials per chunk
+constexpr int kStageCap = 2048;    // staged particles per buffer
+constexpr int kWarpPairCap = 640;  // in-range pairs per 32 home particles
+constexpr int kWarpTaskCap = 256;  // in-cone patch potentials per 32 home particles
 constexpr unsigned kWaitSpins = 1u << 20;
 
 // tile descriptor: x = replica, y = x0 | y0 << 10 | z0 << 20, z = sx | ty << 10 | tz << 15 | whole << 20 | simple << 21
 // sx = staged cells per row (nc for whole rows, tx + 2 for a chunk), tx = sx - 2 for chunks.
-struct TileShared {
+
+enum StageMode : int { kStaged = 0, kSlots = 1 };
+
+// one staging buffer: a tile's positions (TMA-copied) and cell table, or -- for tiny replicas and tiles
+// too crowded to stage -- just the slot ranges of its particles
+struct StageBuf {
+    float4 pos[kStageCap];
+    int slot[kStageCap];             // global slot of every staged particle
+    int cell_sm[kStageCells + 1];    // offset of every staged cell in pos[]
+    int row_start[kTileYZMax * kTileYZMax + 1];  // home particles before each home row
+    int seg_s0[kTileYZMax * kTileYZMax], seg_n[kTileYZMax * kTileYZMax + 1];  // kSlots: slot runs
     unsigned long long bar;
-    int nstage, npairs, ntasks, nhome, abort_flag, overflow;
-    int row_start[kTileYZMax * kTileYZMax + 1];  // prefix of home particles over home rows
-    int cell_sm[kStageCells + 1];
-    int cell_slot[kStageCells];
-    float4 stage[kStageCap];
-    unsigned long long acc[kTileThreads][6];
-    int h_slot[kTileThreads], h_id[kTileThreads];
-    short h_k[kTileThreads], h_cell[kTileThreads];
-    int pair_slot[kPairCap];
-    short pair_k[kPairCap];
-    unsigned char pair_home[kPairCap];
-    unsigned task[kTaskCap];
-    int scan_ws[33];
+    int4 desc;
+    int mode, total, nhome, nseg;
+    // units of the CTA-wide stream this buffer holds, published as ONE 64-bit word so a reader never
+    // sees half of an update: bits 0-31 first unit, bits 32-62 unit count, bit 63 mbarrier parity
+    unsigned long long range;
+    int nunits;                      // unit count of the tile held (producer's copy)
+    int done;                        // units of this tile finished by the consumers
+};
+
+// per-warp scratch: the compacted pair and task lists of 32 home particles and their sums
+struct WarpScratch {
+    unsigned long long acc[32][6];
+    int h_k[32], h_slot[32], h_id[32];
+    short pair_k[kWarpPairCap];
+    unsigned char pair_h[kWarpPairCap];
+    unsigned task[kWarpTaskCap];
+    int npairs, ntasks;
+};
+
+struct TileShared {
+    StageBuf buf[kStageBufs];
+    WarpScratch w[kConsumerWarps];
+    int claim;                       // next unit of the CTA-wide stream
+    int final_units;                 // -1 until the producer has published its last tile
+    int overflow;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
@@ -100,21 +125,6 @@ __device__ __forceinline__ void acc_add(unsigned long long *a, float v) {
 }
 __device__ __forceinline__ float acc_get(unsigned long long a) {
     return __ll2float_rn((long long)a) * 2.3283064365386963e-10f;
-}
-
-// global cell of staged cell (sx_, sy, sz) in tile g, or -1 when it lies outside a walled box
-__device__ __forceinline__ int staged_global_cell(const TileGeom &g, const Replica<float> &R, int sx_, int sy, int sz) {
-    const int nc = R.nc;
-    int gx = g.whole ? sx_ : g.x0 - 1 + sx_;
-    int gy = g.y0 - 1 + sy, gz = g.z0 - 1 + sz;
-    if (R.periodic) {
-        gx = (gx + nc) % nc;
-        gy = (gy + nc) % nc;
-        gz = (gz + nc) % nc;
-    } else if (gx < 0 || gx >= nc || gy < 0 || gy >= nc || gz < 0 || gz >= nc) {
-        return -1;
-    }
-    return R.cell_off + gx + nc * (gy + nc * gz);
 }
 
 // the Langevin epilogue shared with the simple kernel (create_forces_and_torques_sphere + half-kick +
@@ -177,14 +187,16 @@ __device__ __forceinline__ void load_q(const ForceArgs<float> &a, int slot, floa
     Q[4] = c[0]; Q[5] = c[1]; Q[6] = c[2]; Q[7] = c[3]; Q[8] = q8;
 }
 
-// one in-cone patch potential q of pair p (phase 3, or immediately when the task list is full)
+// one in-cone patch potential q of pair p of warp scratch W (phase 3, or at once when the task list
+// is full): Kern-Frenkel force on the home particle and torque on it, into W's fixed-point sums
 __device__ __noinline__ void eval_task(const ForceArgs<float> &a, const Replica<float> &R, const Model<float> &M,
-                                       TileShared &sh, int p, int q) {
-    const int h = sh.pair_home[p];
-    const int kk = sh.pair_k[p], j = sh.pair_slot[p];
-    const int ki = sh.h_k[h], si = sh.h_slot[h], idi = sh.h_id[h];
+                                       const StageBuf &B, WarpScratch &W, int p, int q) {
+    const int h = W.pair_h[p];
+    const int kk = W.pair_k[p];
+    const int ki = W.h_k[h], si = W.h_slot[h], idi = W.h_id[h];
+    const int j = B.slot[kk];
     const int idj = __ldg(a.buf.ident + j);
-    const float4 pi = sh.stage[ki], pj = sh.stage[kk];
+    const float4 pi = B.pos[ki], pj = B.pos[kk];
     float d[3] = {min_image<float>(pi.x - pj.x, R.box, R.l2s, R.periodic),
                   min_image<float>(pi.y - pj.y, R.box, R.l2s, R.periodic),
                   min_image<float>(pi.z - pj.z, R.box, R.l2s, R.periodic)};
@@ -214,7 +226,7 @@ __device__ __noinline__ void eval_task(const ForceArgs<float> &a, const Replica<
     const float cj = n2[0] * u[0] + n2[1] * u[1] + n2[2] * u[2];
     float f[3] = {0, 0, 0}, tqa[3] = {0, 0, 0}, tqb[3] = {0, 0, 0}, e = 0;
     kf2_pair<float>(M.att[q], M.dis[q], M.inv_dis[q], M.kfac[q], u, rr, n1, n2, ci, cj, f, tqa, tqb, e);
-    unsigned long long *acc = sh.acc[h];
+    unsigned long long *acc = W.acc[h];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         acc_add(acc + k, sg * f[k]);
@@ -224,17 +236,17 @@ __device__ __noinline__ void eval_task(const ForceArgs<float> &a, const Replica<
 
 // phase 2 body: WCA core + cone tests of pair p; in-cone potentials become tasks
 __device__ __forceinline__ void eval_pair(const ForceArgs<float> &a, const Replica<float> &R, const Model<float> &M,
-                                          TileShared &sh, int p, bool &big) {
-    const int h = sh.pair_home[p];
-    const int kk = sh.pair_k[p], j = sh.pair_slot[p];
-    const int ki = sh.h_k[h];
-    const float4 pi = sh.stage[ki], pj = sh.stage[kk];
+                                          const StageBuf &B, WarpScratch &W, int p, bool &big) {
+    const int h = W.pair_h[p];
+    const int kk = W.pair_k[p];
+    const int ki = W.h_k[h];
+    const float4 pi = B.pos[ki], pj = B.pos[kk];
     float d[3] = {min_image<float>(pi.x - pj.x, R.box, R.l2s, R.periodic),
                   min_image<float>(pi.y - pj.y, R.box, R.l2s, R.periodic),
                   min_image<float>(pi.z - pj.z, R.box, R.l2s, R.periodic)};
     const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
     const float rr = sqrtf(r2);
-    unsigned long long *acc = sh.acc[h];
+    unsigned long long *acc = W.acc[h];
     if (rr < R.hs_limit) {
         const float s_ = hs_force_over_r<float>(R, r2);
         big |= fabsf(s_ * rr) > 1e4f;
@@ -243,7 +255,8 @@ __device__ __forceinline__ void eval_pair(const ForceArgs<float> &a, const Repli
         acc_add(acc + 2, s_ * d[2]);
     }
     if (!(r2 < R.patch_r2)) return;
-    const int idi = sh.h_id[h];
+    const int j = B.slot[kk];
+    const int idi = W.h_id[h];
     const int idj = __ldg(a.buf.ident + j);
     const bool single = M.n_types == 1;
     const int ti = single ? 0 : type_of<float>(M, idi - R.off);
@@ -253,7 +266,7 @@ __device__ __forceinline__ void eval_pair(const ForceArgs<float> &a, const Repli
     const float sg = i_first ? 1.f : -1.f, inv = 1.f / rr;
     const float u[3] = {sg * d[0] * inv, sg * d[1] * inv, sg * d[2] * inv};
     float Qi[9], Qj[9];
-    load_q(a, sh.h_slot[h], pi.w, Qi);
+    load_q(a, W.h_slot[h], pi.w, Qi);
     load_q(a, j, pj.w, Qj);
     const float *Qa = i_first ? Qi : Qj, *Qb = i_first ? Qj : Qi;
     const int ta = i_first ? ti : tj, tb = i_first ? tj : ti;
@@ -283,249 +296,402 @@ __device__ __forceinline__ void eval_pair(const ForceArgs<float> &a, const Repli
             const float *w = M.orient[ob + jb];
             const float cb = w[0] * wb[0] + w[1] * wb[1] + w[2] * wb[2];
             if (!(ca > M.costm[q] && cb > M.costm[q]) || rr > M.rmax[q]) continue;
-            const int t = atomicAdd(&sh.ntasks, 1);
-            if (t < kTaskCap) sh.task[t] = ((unsigned)p << 8) | (unsigned)q;
-            else eval_task(a, R, M, sh, p, q);
+            const int t = atomicAdd(&W.ntasks, 1);
+            if (t < kWarpTaskCap) W.task[t] = ((unsigned)p << 8) | (unsigned)q;
+            else eval_task(a, R, M, B, W, p, q);
         }
     }
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(kTileThreads) tile_force_kernel(ForceArgs<float> a, const int4 *tiles, int ntiles) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    TileShared &sh = *reinterpret_cast<TileShared *>(smem_raw);
-    const int tid = threadIdx.x;
-    if (tid == 0) {
-        mbar_init(&sh.bar, 1);
-        fence_proxy_async();
-        sh.overflow = 0;
+// staged-cell wrap: the coordinates here are at most one cell outside [0, nc)
+__device__ __forceinline__ int wrap1(int v, int nc) { return v < 0 ? v + nc : (v >= nc ? v - nc : v); }
+
+// global cell of staged cell (sx_, sy, sz) of tile g, or -1 outside a walled box
+__device__ __forceinline__ int staged_cell(const TileGeom &g, const Replica<float> &R, int sx_, int sy, int sz) {
+    const int nc = R.nc;
+    int gx = g.whole ? sx_ : g.x0 - 1 + sx_;
+    int gy = g.y0 - 1 + sy, gz = g.z0 - 1 + sz;
+    if (R.periodic) {
+        gx = wrap1(gx, nc);
+        gy = wrap1(gy, nc);
+        gz = wrap1(gz, nc);
+    } else if (gx < 0 || gx >= nc || gy < 0 || gy >= nc || gz < 0 || gz >= nc) {
+        return -1;
     }
-    __syncthreads();
-    unsigned phase = 0;
+    return R.cell_off + gx + nc * (gy + nc * gz);
+}
 
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const TileGeom g = decode_tile(tiles[tile]);
-        const Replica<float> &R = a.tb.reps[g.rep];
-        const Model<float> &M = a.tb.models[R.model];
+__device__ __forceinline__ int ld_volatile(const int *p) { return *(const volatile int *)p; }
 
-        if (g.simple) {
-            // replicas with fewer than three cells per side: every particle by the per-thread path
-            for (int s = R.off + tid; s < R.off + R.n; s += kTileThreads) simple_particle<float, MODE>(a, s);
-            __syncthreads();
-            continue;
+// Producer warp: build buffer B's table for `tile` and start its bulk copies.  Returns the number of
+// 32-particle units of the tile.
+__device__ int produce_tile(const ForceArgs<float> &a, const int4 *tiles, int tile, StageBuf &B, int lane) {
+    const int4 desc = tiles[tile];
+    const TileGeom g = decode_tile(desc);
+    const Replica<float> &R = a.tb.reps[g.rep];
+    int nhome = 0, mode = kStaged, total = 0;
+    if (g.simple) {
+        mode = kSlots;
+        if (lane == 0) {
+            B.seg_s0[0] = R.off;
+            B.seg_n[0] = 0;
+            B.seg_n[1] = R.n;
+            B.nseg = 1;
         }
-        const int nrows_y = g.ty + 2, nrows_z = g.tz + 2;
-        const int ncells_staged = g.sx * nrows_y * nrows_z;
-
-        // ---- staged cell table: counts, block-wide exclusive scan -> shared offsets
-        constexpr int kItems = (kStageCells + kTileThreads - 1) / kTileThreads;
-        int cnt[kItems], gc[kItems];
-        int local = 0;
+        nhome = R.n;
+    } else {
+        const int nry = g.ty + 2, nrz = g.tz + 2;
+        const int ncs = g.sx * nry * nrz;
+        // cell counts in lane-strided rounds of 32 cells, four rounds in flight, warp-shuffle scan
+        int base = 0;
+        for (int c0 = 0; c0 < ncs; c0 += 128) {
+            int gs[4], cnt[4];
 #pragma unroll
-        for (int it = 0; it < kItems; it++) {
-            const int c = tid * kItems + it;
-            cnt[it] = 0;
-            gc[it] = -1;
-            if (c < ncells_staged) {
-                const int sx_ = c % g.sx, sy = (c / g.sx) % nrows_y, sz = c / (g.sx * nrows_y);
-                gc[it] = staged_global_cell(g, R, sx_, sy, sz);
-                if (gc[it] >= 0) cnt[it] = __ldg(a.start + gc[it] + 1) - __ldg(a.start + gc[it]);
-            }
-            local += cnt[it];
-        }
-        int total;
-        int off = block_exclusive_scan(local, sh.scan_ws, total);
-#pragma unroll
-        for (int it = 0; it < kItems; it++) {
-            const int c = tid * kItems + it;
-            if (c < ncells_staged) {
-                sh.cell_sm[c] = off;
-                sh.cell_slot[c] = gc[it] >= 0 ? __ldg(a.start + gc[it]) : 0;
-            }
-            off += cnt[it];
-        }
-        if (tid == 0) {
-            sh.cell_sm[ncells_staged] = total;
-            sh.nstage = total;
-        }
-        __syncthreads();
-
-        if (total > kStageCap) {
-            // too crowded to stage: the per-thread path over the home rows (slots are contiguous per row)
-            const int hx0 = g.whole ? 0 : 1, hx1 = g.whole ? g.sx : g.sx - 1;
-            for (int rz = 1; rz <= g.tz; rz++)
-                for (int ry = 1; ry <= g.ty; ry++) {
-                    const int base = (rz * nrows_y + ry) * g.sx;
-                    const int s0 = sh.cell_slot[base + hx0];
-                    const int s1 = sh.cell_slot[base + hx1 - 1] + (sh.cell_sm[base + hx1] - sh.cell_sm[base + hx1 - 1]);
-                    for (int s = s0 + tid; s < s1; s += kTileThreads) simple_particle<float, MODE>(a, s);
+            for (int q = 0; q < 4; q++) {
+                const int c = c0 + 32 * q + lane;
+                gs[q] = 0;
+                cnt[q] = 0;
+                if (c < ncs) {
+                    const int gcell = staged_cell(g, R, c % g.sx, (c / g.sx) % nry, c / (g.sx * nry));
+                    if (gcell >= 0) {
+                        gs[q] = __ldg(a.start + gcell);
+                        cnt[q] = __ldg(a.start + gcell + 1) - gs[q];
+                    }
                 }
-            __syncthreads();
-            continue;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int c = c0 + 32 * q + lane;
+                int inc = cnt[q];
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (lane >= o) inc += t;
+                }
+                const int off = base + inc - cnt[q];
+                if (c < ncs) {
+                    B.cell_sm[c] = off;
+                    for (int k = 0; k < cnt[q] && off + k < kStageCap; k++) B.slot[off + k] = gs[q] + k;
+                }
+                base += __shfl_sync(0xffffffffu, inc, 31);
+            }
         }
-
-        // ---- TMA bulk copies of the staged positions (one per contiguous piece of a staged row)
-        if (tid == 0) {
-            fence_proxy_async();
-            mbar_arrive_expect_tx(&sh.bar, (unsigned)total * 16u);
+        total = base;
+        if (lane == 0) B.cell_sm[ncs] = total;
+        __syncwarp();
+        const int hx0 = g.whole ? 0 : 1, hx1 = g.whole ? g.sx : g.sx - 1;
+        const int nrows = g.ty * g.tz;
+        if (total <= kStageCap) {
+            if (lane == 0) {
+                int acc = 0;
+                for (int r = 0; r < nrows; r++) {
+                    const int rb = ((1 + r / g.ty) * nry + (1 + r % g.ty)) * g.sx;
+                    B.row_start[r] = acc;
+                    acc += B.cell_sm[rb + hx1] - B.cell_sm[rb + hx0];
+                }
+                B.row_start[nrows] = acc;
+            }
+            __syncwarp();
+            nhome = B.row_start[nrows];
+            if (nhome == 0) {
+                mode = kSlots;  // nothing to compute: no copies either
+                if (lane == 0) {
+                    B.seg_n[0] = 0;
+                    B.nseg = 0;
+                }
+            }
+        } else {
+            // too crowded to stage: the home rows as slot runs (consecutive cells, contiguous slots)
+            mode = kSlots;
+            int n = 0, s0 = 0;
+            if (lane < nrows) {
+                const int ry = 1 + lane % g.ty, rz = 1 + lane / g.ty;
+                const int c0 = staged_cell(g, R, hx0, ry, rz), c1 = staged_cell(g, R, hx1 - 1, ry, rz);
+                s0 = __ldg(a.start + c0);
+                n = __ldg(a.start + c1 + 1) - s0;
+            }
+            int inc = n;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += t;
+            }
+            if (lane < nrows) {
+                B.seg_s0[lane] = s0;
+                B.seg_n[lane] = inc - n;
+            }
+            if (lane == nrows - 1) B.seg_n[nrows] = inc;
+            if (lane == 0) B.nseg = nrows;
+            nhome = __shfl_sync(0xffffffffu, inc, nrows - 1);
         }
-        __syncthreads();
-        if (tid < nrows_y * nrows_z) {
-            fence_proxy_async();  // this thread's earlier generic reads of the buffer precede the copies
-            const int base = tid * g.sx;
+    }
+    const int units = (nhome + 31) / 32;
+    if (lane == 0) {
+        B.desc = desc;
+        B.mode = mode;
+        B.total = total;
+        B.nhome = nhome;
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive_expect_tx(&B.bar, mode == kStaged ? (unsigned)total * 16u : 0u);
+    if (mode == kStaged) {
+        const int nry = g.ty + 2, nrows_all = nry * (g.tz + 2);
+        fence_proxy_async();
+        for (int row = lane; row < nrows_all; row += 32) {
+            const int sy = row % nry, sz = row / nry, rb = row * g.sx;
             int c = 0;
             while (c < g.sx) {
-                // extend the piece while the global cells stay consecutive
-                const int g0 = sh.cell_slot[base + c];
+                const int gc0 = staged_cell(g, R, c, sy, sz);
                 int e = c + 1;
-                const int gcell0 = staged_global_cell(g, R, c, tid % nrows_y, tid / nrows_y);
-                if (gcell0 < 0) { c = e; continue; }
-                while (e < g.sx) {
-                    const int gce = staged_global_cell(g, R, e, tid % nrows_y, tid / nrows_y);
-                    if (gce != gcell0 + (e - c)) break;
-                    e++;
-                }
-                const int bytes = (sh.cell_sm[base + e] - sh.cell_sm[base + c]) * 16;
-                if (bytes > 0)
-                    bulk_copy_g2s(&sh.stage[sh.cell_sm[base + c]], a.buf.pos + 4 * (size_t)g0, (unsigned)bytes, &sh.bar);
+                if (gc0 >= 0)
+                    while (e < g.sx && staged_cell(g, R, e, sy, sz) == gc0 + (e - c)) e++;
+                const int bytes = (B.cell_sm[rb + e] - B.cell_sm[rb + c]) * 16;
+                if (gc0 >= 0 && bytes > 0)
+                    bulk_copy_g2s(&B.pos[B.cell_sm[rb + c]], a.buf.pos + 4 * (size_t)B.slot[B.cell_sm[rb + c]],
+                                  (unsigned)bytes, &B.bar);
                 c = e;
             }
         }
-        // bounded wait for the copies
-        bool done = false;
-        for (unsigned it = 0; it < kWaitSpins && !done; it++) done = mbar_try_wait(&sh.bar, phase);
-        if (__syncthreads_or(!done)) {
-            if (tid == 0) atomicOr(a.flags, 4u);
-            for (unsigned it = 0; it < kWaitSpins && !done; it++) done = mbar_try_wait(&sh.bar, phase);
-            return;
-        }
-        phase ^= 1u;
+    }
+    return units;
+}
 
-        // ---- home particles: the inner rows, contiguous in shared memory per row
-        const int hx0 = g.whole ? 0 : 1, hx1 = g.whole ? g.sx : g.sx - 1;
-        if (tid == 0) {
-            int acc_rows = 0;
-            for (int r = 0; r < g.ty * g.tz; r++) {
-                const int ry = 1 + r % g.ty, rz = 1 + r / g.ty;
-                const int base = (rz * nrows_y + ry) * g.sx;
-                sh.row_start[r] = acc_rows;
-                acc_rows += sh.cell_sm[base + hx1] - sh.cell_sm[base + hx0];
-            }
-            sh.row_start[g.ty * g.tz] = acc_rows;
-            sh.nhome = acc_rows;
+// Consumer warp: unit u (32 home particles) of a staged tile -- phases 1-4
+template <int MODE>
+__device__ void consume_staged_unit(const ForceArgs<float> &a, const StageBuf &B, WarpScratch &W, int u, int lane,
+                                    bool &big, int &overflow) {
+    const TileGeom g = decode_tile(B.desc);
+    const Replica<float> &R = a.tb.reps[g.rep];
+    const Model<float> &M = a.tb.models[R.model];
+    const int nry = g.ty + 2;
+    const int hx0 = g.whole ? 0 : 1, hx1 = g.whole ? g.sx : g.sx - 1;
+    const int hidx = 32 * u + lane;
+    const bool active = hidx < B.nhome;
+    int myk = 0, mycell = 0;
+    if (active) {
+        int r = 0;
+        while (B.row_start[r + 1] <= hidx) r++;
+        const int rb = ((1 + r / g.ty) * nry + (1 + r % g.ty)) * g.sx;
+        myk = B.cell_sm[rb + hx0] + (hidx - B.row_start[r]);
+        int lo = hx0, hi = hx1;  // cell_sm[rb+lo] <= myk < cell_sm[rb+hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (B.cell_sm[rb + mid] <= myk) lo = mid;
+            else hi = mid;
         }
-        __syncthreads();
-        const int nhome = sh.nhome;
-        bool big = false;
-
-        for (int c0 = 0; c0 < nhome; c0 += kTileThreads) {
-            const int nchunk = min(kTileThreads, nhome - c0);
-            // -- locate this thread's home particle
-            int myk = -1, mycell = -1;
-            if (tid < nchunk) {
-                const int hidx = c0 + tid;
-                int r = 0;
-                while (sh.row_start[r + 1] <= hidx) r++;
-                const int ry = 1 + r % g.ty, rz = 1 + r / g.ty;
-                const int base = (rz * nrows_y + ry) * g.sx;
-                myk = sh.cell_sm[base + hx0] + (hidx - sh.row_start[r]);
-                int lo = hx0, hi = hx1;  // cell_sm[base+lo] <= myk < cell_sm[base+hi]
-                while (hi - lo > 1) {
-                    const int mid = (lo + hi) >> 1;
-                    if (sh.cell_sm[base + mid] <= myk) lo = mid;
-                    else hi = mid;
-                }
-                mycell = base + lo;
-                const int slot = sh.cell_slot[mycell] + (myk - sh.cell_sm[mycell]);
-                sh.h_k[tid] = (short)myk;
-                sh.h_cell[tid] = (short)mycell;
-                sh.h_slot[tid] = slot;
-                sh.h_id[tid] = __ldg(a.buf.ident + slot);
+        mycell = rb + lo;
+        const int slot = B.slot[myk];
+        W.h_k[lane] = myk;
+        W.h_slot[lane] = slot;
+        W.h_id[lane] = __ldg(a.buf.ident + slot);
+    }
 #pragma unroll
-                for (int k = 0; k < 6; k++) sh.acc[tid][k] = 0ull;
-            }
-            if (tid == 0) {
-                sh.npairs = 0;
-                sh.ntasks = 0;
-            }
-            __syncthreads();
+    for (int k = 0; k < 6; k++) W.acc[lane][k] = 0ull;
+    if (lane == 0) {
+        W.npairs = 0;
+        W.ntasks = 0;
+    }
+    __syncwarp();
 
-            // -- phase 1: candidate scan in shared memory
-            if (tid < nchunk) {
-                const float4 pi = sh.stage[myk];
-                const int lx = mycell % g.sx, ly = (mycell / g.sx) % nrows_y, lz = mycell / (g.sx * nrows_y);
-                for (int dz = -1; dz <= 1; dz++)
-                    for (int dy = -1; dy <= 1; dy++) {
-                        const int rowb = ((lz + dz) * nrows_y + (ly + dy)) * g.sx;
-                        for (int dx = -1; dx <= 1; dx++) {
-                            int cx = lx + dx;
-                            if (g.whole) {
-                                if (cx < 0 || cx >= g.sx) {
-                                    if (!R.periodic) continue;
-                                    cx = cx < 0 ? cx + g.sx : cx - g.sx;
-                                }
-                            }
-                            const int cell = rowb + cx;
-                            const int k0 = sh.cell_sm[cell], k1 = sh.cell_sm[cell + 1];
-                            for (int kk = k0; kk < k1; kk++) {
-                                if (kk == myk) continue;
-                                const float4 pj = sh.stage[kk];
-                                const float dx_ = min_image<float>(pi.x - pj.x, R.box, R.l2s, R.periodic);
-                                const float dy_ = min_image<float>(pi.y - pj.y, R.box, R.l2s, R.periodic);
-                                const float dz_ = min_image<float>(pi.z - pj.z, R.box, R.l2s, R.periodic);
-                                if (dx_ * dx_ + dy_ * dy_ + dz_ * dz_ < R.rc2) {
-                                    const int p = atomicAdd(&sh.npairs, 1);
-                                    if (p < kPairCap) {
-                                        sh.pair_k[p] = (short)kk;
-                                        sh.pair_slot[p] = sh.cell_slot[cell] + (kk - k0);
-                                        sh.pair_home[p] = (unsigned char)tid;
-                                    }
-                                }
+    // -- phase 1: candidate scan in shared memory
+    if (active) {
+        const float4 pi = B.pos[myk];
+        const int lx = mycell % g.sx, ly = (mycell / g.sx) % nry, lz = mycell / (g.sx * nry);
+        for (int dz = -1; dz <= 1; dz++)
+            for (int dy = -1; dy <= 1; dy++) {
+                const int rowb = ((lz + dz) * nry + (ly + dy)) * g.sx;
+                for (int dx = -1; dx <= 1; dx++) {
+                    int cx = lx + dx;
+                    if (g.whole && (cx < 0 || cx >= g.sx)) {
+                        if (!R.periodic) continue;
+                        cx = cx < 0 ? cx + g.sx : cx - g.sx;
+                    }
+                    const int k0 = B.cell_sm[rowb + cx], k1 = B.cell_sm[rowb + cx + 1];
+                    for (int kk = k0; kk < k1; kk++) {
+                        if (kk == myk) continue;
+                        const float4 pj = B.pos[kk];
+                        const float dx_ = min_image<float>(pi.x - pj.x, R.box, R.l2s, R.periodic);
+                        const float dy_ = min_image<float>(pi.y - pj.y, R.box, R.l2s, R.periodic);
+                        const float dz_ = min_image<float>(pi.z - pj.z, R.box, R.l2s, R.periodic);
+                        if (dx_ * dx_ + dy_ * dy_ + dz_ * dz_ < R.rc2) {
+                            const int p = atomicAdd(&W.npairs, 1);
+                            if (p < kWarpPairCap) {
+                                W.pair_k[p] = (short)kk;
+                                W.pair_h[p] = (unsigned char)lane;
                             }
                         }
                     }
-            }
-            __syncthreads();
-            if (sh.npairs > kPairCap) {
-                // more pairs than the list holds: this chunk goes through the per-thread path instead
-                if (tid < nchunk) simple_particle<float, MODE>(a, sh.h_slot[tid]);
-                if (tid == 0) sh.overflow = 1;
-                __syncthreads();
-                continue;
-            }
-            const int npairs = sh.npairs;
-
-            // -- phase 2: pairs spread over all threads
-            for (int p = tid; p < npairs; p += kTileThreads) eval_pair(a, R, M, sh, p, big);
-            __syncthreads();
-            // -- phase 3: in-cone patch potentials spread over all threads
-            const int ntasks = min(sh.ntasks, kTaskCap);
-            for (int t = tid; t < ntasks; t += kTileThreads) eval_task(a, R, M, sh, (int)(sh.task[t] >> 8), (int)(sh.task[t] & 255u));
-            __syncthreads();
-
-            // -- phase 4: epilogue per home particle
-            if (tid < nchunk) {
-                const int s = sh.h_slot[tid];
-                const float F[3] = {acc_get(sh.acc[tid][0]), acc_get(sh.acc[tid][1]), acc_get(sh.acc[tid][2])};
-                const float T[3] = {acc_get(sh.acc[tid][3]), acc_get(sh.acc[tid][4]), acc_get(sh.acc[tid][5])};
-                if (MODE == kModeForces) {
-                    const int id = sh.h_id[tid];
-                    for (int k = 0; k < 3; k++) {
-                        a.outF[3 * (size_t)id + k] = F[k];
-                        a.outT[3 * (size_t)id + k] = T[k];
-                    }
-                } else {
-                    const float4 pi = sh.stage[myk];
-                    float Qi[9];
-                    load_q(a, s, pi.w, Qi);
-                    langevin_epilogue(a, R, g.rep, s, sh.h_id[tid], F, T, Qi, pi.x, pi.y, pi.z);
                 }
             }
-            __syncthreads();
+    }
+    __syncwarp();
+    if (W.npairs > kWarpPairCap) {
+        // more pairs than the warp's list holds: these 32 particles take the per-thread path
+        if (active) simple_particle<float, MODE>(a, W.h_slot[lane]);
+        overflow = 1;
+        __syncwarp();
+        return;
+    }
+    // -- phase 2: the warp's pairs spread over its lanes
+    const int npairs = W.npairs;
+    for (int p = lane; p < npairs; p += 32) eval_pair(a, R, M, B, W, p, big);
+    __syncwarp();
+    // -- phase 3: in-cone patch potentials spread over the lanes
+    const int ntasks = min(W.ntasks, kWarpTaskCap);
+    for (int t = lane; t < ntasks; t += 32) eval_task(a, R, M, B, W, (int)(W.task[t] >> 8), (int)(W.task[t] & 255u));
+    __syncwarp();
+    // -- phase 4: epilogue per home particle
+    if (active) {
+        const int s = W.h_slot[lane];
+        const float F[3] = {acc_get(W.acc[lane][0]), acc_get(W.acc[lane][1]), acc_get(W.acc[lane][2])};
+        const float T[3] = {acc_get(W.acc[lane][3]), acc_get(W.acc[lane][4]), acc_get(W.acc[lane][5])};
+        if (MODE == kModeForces) {
+            const int id = W.h_id[lane];
+            for (int k = 0; k < 3; k++) {
+                a.outF[3 * (size_t)id + k] = F[k];
+                a.outT[3 * (size_t)id + k] = T[k];
+            }
+        } else {
+            const float4 pi = B.pos[myk];
+            float Qi[9];
+            load_q(a, s, pi.w, Qi);
+            langevin_epilogue(a, R, g.rep, s, W.h_id[lane], F, T, Qi, pi.x, pi.y, pi.z);
+        }
+    }
+    __syncwarp();
+}
+
+// Persistent warp-specialised force kernel.  The last warp of each CTA stages tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ... into a ring of three buffers and publishes their 32-particle units
+// as consecutive ranges of one CTA-wide unit stream; the other warps claim units from the stream in
+// order.  A buffer is restaged only after every unit of its previous tile is done, and claims are
+// monotone, so every mbarrier wait below has an unambiguous parity.  All waits are bounded.
+template <int MODE>
+__global__ void __launch_bounds__(kTileThreads, 1) tile_force_kernel(ForceArgs<float> a, const int4 *tiles, int ntiles) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    TileShared &sh = *reinterpret_cast<TileShared *>(smem_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) {
+        for (int b = 0; b < kStageBufs; b++) {
+            mbar_init(&sh.buf[b].bar, 1);
+            sh.buf[b].range = 0ull;
+            sh.buf[b].nunits = 0;
+            sh.buf[b].done = 0;
+        }
+        fence_proxy_async();
+        sh.claim = 0;
+        sh.final_units = -1;
+        sh.overflow = 0;
+    }
+    __syncthreads();
+
+    if (warp == kTileWarps - 1) {
+        // ---------------- producer
+        int cum = 0;
+        for (int k = 0;; k++) {
+            const int tile = blockIdx.x + k * gridDim.x;
+            if (tile >= ntiles) break;
+            StageBuf &B = sh.buf[k % kStageBufs];
+            if (k >= kStageBufs) {
+                // wait until the consumers are done with the tile this buffer held
+                const int need = B.nunits;
+                bool ok = false;
+                for (unsigned it = 0; it < (kWaitSpins << 4) && !ok; it++) {
+                    ok = ld_volatile(&B.done) >= need;
+                    if (!ok) __nanosleep(64);
+                }
+                if (!ok) {
+                    if (lane == 0) atomicOr(a.flags, 4u);
+                    break;
+                }
+                __threadfence_block();
+            }
+            const int units = produce_tile(a, tiles, tile, B, lane);
+            if (lane == 0) {
+                B.done = 0;
+                B.nunits = units;
+                __threadfence_block();
+                const unsigned long long parity = (unsigned long long)((k / kStageBufs) & 1);
+                *(volatile unsigned long long *)&B.range =
+                    (unsigned long long)(unsigned)cum | ((unsigned long long)(unsigned)units << 32) | (parity << 63);
+            }
+            cum += units;
+            __syncwarp();
+        }
+        if (lane == 0) *(volatile int *)&sh.final_units = cum;
+        // drain: the last use of every buffer has completed (its copies landed) before this CTA exits
+        const int nk = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+        for (int b = 0; b < kStageBufs && b < nk; b++) {
+            const int klast = b + ((nk - 1 - b) / kStageBufs) * kStageBufs;
+            bool ok = false;
+            for (unsigned it = 0; it < kWaitSpins && !ok; it++) ok = mbar_try_wait(&sh.buf[b].bar, (unsigned)(klast / kStageBufs) & 1u);
+            if (!ok && lane == 0) atomicOr(a.flags, 4u);
+        }
+    } else {
+        // ---------------- consumers
+        WarpScratch &W = sh.w[warp];
+        bool big = false;
+        int overflow = 0;
+        for (;;) {
+            int U = 0;
+            if (lane == 0) U = atomicAdd(&sh.claim, 1);
+            U = __shfl_sync(0xffffffffu, U, 0);
+            // find the buffer that holds unit U (published by the producer in order)
+            int b = -1, ubegin = 0;
+            unsigned parity = 0;
+            bool stop = false;
+            for (unsigned it = 0; it < (kWaitSpins << 4); it++) {
+                for (int q = 0; q < kStageBufs; q++) {
+                    const unsigned long long rw = *(const volatile unsigned long long *)&sh.buf[q].range;
+                    const int beg = (int)(unsigned)(rw & 0xffffffffull);
+                    const int cnt = (int)(unsigned)((rw >> 32) & 0x7fffffffull);
+                    if (beg <= U && U < beg + cnt) {
+                        b = q;
+                        ubegin = beg;
+                        parity = (unsigned)(rw >> 63);
+                    }
+                }
+                if (b >= 0) break;
+                const int fin = ld_volatile(&sh.final_units);
+                if (fin >= 0 && U >= fin) {
+                    stop = true;
+                    break;
+                }
+                __nanosleep(64);
+            }
+            if (stop) break;
+            if (b < 0) {
+                if (lane == 0) atomicOr(a.flags, 4u);
+                break;
+            }
+            StageBuf &B = sh.buf[b];
+            bool ready = false;
+            for (unsigned it = 0; it < kWaitSpins && !ready; it++) ready = mbar_try_wait(&B.bar, parity);
+            ready = __all_sync(0xffffffffu, ready);
+            if (!ready) {
+                if (lane == 0) atomicOr(a.flags, 4u);
+                break;
+            }
+            const int u = U - ubegin;
+            if (B.mode == kStaged) {
+                consume_staged_unit<MODE>(a, B, W, u, lane, big, overflow);
+            } else {
+                const int hidx = 32 * u + lane;
+                if (hidx < B.nhome) {
+                    int r = 0;
+                    while (B.seg_n[r + 1] <= hidx) r++;
+                    simple_particle<float, MODE>(a, B.seg_s0[r] + (hidx - B.seg_n[r]));
+                }
+            }
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence_block();
+                atomicAdd(&B.done, 1);
+            }
         }
         if (big) atomicOr(a.flags, 2u);
+        if (overflow && lane == 0) atomicOr(a.flags, 8u);
     }
-    if (tid == 0 && sh.overflow) atomicOr(a.flags, 8u);
 }
 
 }  // namespace
