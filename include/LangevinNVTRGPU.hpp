@@ -1,0 +1,166 @@
+// LangevinNVTRGPU.hpp -- header-only C++ adapter that gives the reference's LangevinNVTR interface
+// (MDBase/Rotational/LangevinR.h:59-270) to the GB300 C ABI (mtcode_gb300.h).
+//
+// A maintainer of osmanovicdino/mtcode replaces the step loop of Condensate::run
+// (Condensate/Condensate.cpp:335-378) by
+//
+//     LangevinNVTRGPU<matrix<double>> gpu(geo_l, /*periodic*/ true, N, model);
+//     gpu.setdt(dt); gpu.setkT(kT); gpu.setgamma(g); gpu.setgammar(gr);
+//     gpu.initialize(pos, mom, orient, angmom);        // LangevinNVTR::initialize(x, p, Q, L)
+//     gpu.init_forces();                               // the F, T, RT before the loop (:312-334)
+//     for (i ...) { gpu.measured_temperature(meas); gpu.step(1); if (i % every == 0) gpu.getdat(pos); ... }
+//
+// The matrix type only needs operator()(i, j), getNsafe() and getncols(), so the same header works
+// with the reference's matrix<T> (DataStructures/matrix2.h) and with any other row-major container.
+// Every failure throws std::runtime_error with the library's message (the reference's error()
+// would block on stdin, Basic/basic.h:61-71).
+#ifndef MTCODE_GB300_LANGEVINNVTRGPU_HPP
+#define MTCODE_GB300_LANGEVINNVTRGPU_HPP
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "mtcode_gb300.h"
+
+// Names here avoid the reference's object-like macros (Basic/basic.h defines check, min, mathematica,
+// convert, ...), so this header can follow the reference's own includes.
+namespace mtg_adapter {
+
+inline void require_ok(mtg_system *h, mtg_status st, const char *what) {
+    if (st != MTG_OK)
+        throw std::runtime_error(std::string(what) + ": " + mtg_status_string(st) + " -- " + mtg_last_error(h));
+}
+
+template <class M>
+void to_rows(M &m, int n, int c, std::vector<double> &out) {
+    out.resize((size_t)n * c);
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < c; k++) out[(size_t)c * i + k] = m(i, k);
+}
+
+template <class M>
+void from_rows(const std::vector<double> &in, int n, int c, M &m) {
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < c; k++) m(i, k) = in[(size_t)c * i + k];
+}
+
+}  // namespace mtg_adapter
+
+template <class Matrix>
+class LangevinNVTRGPU {
+  public:
+    // cube(l, pb, 3) + the ComboPatch in GeneralPatch form (mtg_model_tetrahedral / _bivalent or a
+    // filled mtg_patch_model); precision MTG_FP32 (batched path) or MTG_FP64 (plain path)
+    LangevinNVTRGPU(double box, bool periodic, int n, const mtg_patch_model &model, int precision = MTG_FP32,
+                    int device = 0)
+        : precision_(precision), device_(device) {
+        mtg_replica_defaults(&desc_);
+        desc_.n = n;
+        desc_.box = box;
+        desc_.periodic = periodic ? 1 : 0;
+        desc_.model = model;
+        if (desc_.model.n_types == 1 && desc_.model.count_per_type[0] == 0) desc_.model.count_per_type[0] = n;
+    }
+    ~LangevinNVTRGPU() { mtg_destroy(h_); }
+    LangevinNVTRGPU(const LangevinNVTRGPU &) = delete;
+    LangevinNVTRGPU &operator=(const LangevinNVTRGPU &) = delete;
+
+    // LangevinNVTR setters (LangevinR.h:109-134, LangevinR.cpp:130-144); effective at initialize()
+    void setdt(double v) { desc_.dt = v; }
+    void setkT(double v) { desc_.kT = v; }
+    void setgamma(double v) { desc_.gamma = v; }
+    void setgammar(double v) { desc_.gammar = v; }
+    void setm(double v) { desc_.mass = v; }
+    void setinertia(double v) { desc_.inertia = v; }
+    void setmaxdistance(double v) { desc_.max_dist2 = v; }    // LangevinR.h:136-138
+    void sethardcore(double eps, double sigma) { desc_.hs_eps = eps; desc_.hs_sigma = sigma; }  // HSPotential(eps, sigma)
+    void setseed(uint64_t s) { desc_.seed = s; }
+
+    // LangevinNVTR::initialize(positions, momenta, orientations, angular_momenta) (LangevinR.cpp:309-325)
+    void initialize(Matrix &x, Matrix &p, Matrix &Q, Matrix &L) {
+        if (!h_) create();
+        const int n = desc_.n;
+        mtg_adapter::to_rows(x, n, 3, bx_);
+        mtg_adapter::to_rows(p, n, 3, bp_);
+        mtg_adapter::to_rows(Q, n, 9, bq_);
+        mtg_adapter::to_rows(L, n, 3, bl_);
+        mtg_adapter::require_ok(h_, mtg_set_state(h_, bx_.data(), bp_.data(), bl_.data(), bq_.data(), nullptr, nullptr),
+                           "initialize");
+    }
+
+    // F, T, RT and create_forces_and_torques_sphere before the loop (Condensate.cpp:312-334)
+    void init_forces() { mtg_adapter::require_ok(h_, mtg_init_forces(h_), "init_forces"); }
+
+    // nsteps of the loop body (Condensate.cpp:335-378); asynchronous
+    void step(int nsteps = 1) { mtg_adapter::require_ok(h_, mtg_step(h_, nsteps), "step"); }
+
+    // MD::calculateforces(pairs, HSPotential) + calculate_forces_and_torques3D(pairs, ComboPatch, F, T)
+    void calculate_forces_and_torques3D(Matrix &F, Matrix &T) {
+        const int n = desc_.n;
+        std::vector<double> f((size_t)n * 3), t((size_t)n * 3);
+        mtg_adapter::require_ok(h_, mtg_forces(h_, f.data(), t.data(), nullptr), "calculate_forces_and_torques3D");
+        mtg_adapter::from_rows(f, n, 3, F);
+        mtg_adapter::from_rows(t, n, 3, T);
+    }
+
+    // MD::calculatepairs_parallel(boxes, rc) -> pairs (i < j), P x 2, into any resizable int matrix
+    template <class IntMatrix>
+    void calculatepairs_parallel(double rc, IntMatrix &pairs_out) {
+        int64_t np = 0;
+        mtg_status st = mtg_pairs(h_, 0, rc, nullptr, 0, &np);
+        if (st != MTG_OK && st != MTG_ERR_CAPACITY) mtg_adapter::require_ok(h_, st, "calculatepairs_parallel");
+        std::vector<int32_t> buf((size_t)(np > 0 ? np : 1) * 2);
+        mtg_adapter::require_ok(h_, mtg_pairs(h_, 0, rc, buf.data(), np, &np), "calculatepairs_parallel");
+        pairs_out.resize(np, 2);
+        for (int64_t i = 0; i < np; i++) {
+            pairs_out(i, 0) = buf[2 * i];
+            pairs_out(i, 1) = buf[2 * i + 1];
+        }
+    }
+
+    // LangevinNVTR::measured_temperature(vector1<double>&) (LangevinR.cpp:170-193); any vec with operator[]
+    template <class Vec>
+    void measured_temperature(Vec &ret) {
+        double t[6];
+        mtg_adapter::require_ok(h_, mtg_temperature(h_, t), "measured_temperature");
+        for (int k = 0; k < 6; k++) ret[k] = t[k];
+    }
+
+    // getdat / getmom / getorientation / getangmom (LangevinR.h:190-196), into caller matrices
+    void getdat(Matrix &x) { get(0, x); }
+    void getmom(Matrix &p) { get(1, p); }
+    void getorientation(Matrix &Q) { get(3, Q); }
+    void getangmom(Matrix &L) { get(2, L); }
+
+    mtg_system *handle() { return h_; }
+
+  private:
+    void create() {
+        mtg_config cfg{};
+        cfg.precision = precision_;
+        cfg.n_replicas = 1;
+        cfg.replicas = &desc_;
+        cfg.device = device_;
+        cfg.track_displacement = 1;
+        cfg.force_kernel = 0;
+        mtg_status st = mtg_create(&cfg, &h_);
+        if (st != MTG_OK) throw std::runtime_error(std::string("mtg_create: ") + mtg_last_error(nullptr));
+    }
+    void get(int which, Matrix &m) {
+        const int n = desc_.n, w = which == 3 ? 9 : 3;
+        std::vector<double> b((size_t)n * w);
+        double *ptr[4] = {nullptr, nullptr, nullptr, nullptr};
+        ptr[which] = b.data();
+        mtg_adapter::require_ok(h_, mtg_get_state(h_, ptr[0], ptr[1], ptr[2], ptr[3], nullptr, nullptr), "get_state");
+        mtg_adapter::from_rows(b, n, w, m);
+    }
+
+    mtg_replica_desc desc_;
+    int precision_, device_;
+    mtg_system *h_ = nullptr;
+    std::vector<double> bx_, bp_, bq_, bl_;
+};
+
+#endif  // MTCODE_GB300_LANGEVINNVTRGPU_HPP

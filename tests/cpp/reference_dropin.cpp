@@ -1,0 +1,58 @@
+// reference_dropin.cpp -- compile check: the adapter instantiated with the REFERENCE's own types
+// (matrix<double>, matrix<int>, vector1<double>, TetrahedralPatch), exactly as Condensate::run would
+// use it.  Built by tests/test_adapter.py only where the reference sources are present.
+#include <stdlib.h>
+#include <iostream>
+#include <fstream>
+#include <vector>
+#include <algorithm>
+#include <sstream>
+#include <string>
+#include <iomanip>
+#include <random>
+#include <chrono>
+#include <unistd.h>
+#include <execinfo.h>
+#include <signal.h>
+#include <sys/stat.h>
+typedef int omp_int_t;
+inline omp_int_t omp_get_thread_num() { return 0; }
+inline omp_int_t omp_get_max_threads() { return 1; }
+inline omp_int_t omp_get_num_threads() { return 1; }
+using namespace std;
+#include "Basic/basic.h"
+#include "DataStructures/vector1.h"
+#include "DataStructures/matrix2.h"
+#include "DataStructures/matrix2.cpp"
+#include "MDBase/MD.h"
+#include "MDBase/Langevin.h"
+#include "Condensate/Condensate.h"
+
+#include "LangevinNVTRGPU.hpp"
+
+// Condensate::run's loop with the step on the GPU; the reference's TetrahedralPatch parameters feed
+// the GeneralPatch-form model of the C ABI
+void run_on_gpu(double l, int N, matrix<double> &dat, int runtime, TetrahedralPatch &pots) {
+    mtg_patch_model model;
+    mtg_model_tetrahedral(&model, pots.str, pots.dis, pots.ang);
+    LangevinNVTRGPU<matrix<double>> obj(l, true, N, model);
+    obj.setdt(0.005);
+    obj.setkT(1.0);
+    matrix<double> mom(N, 3), ang(N, 3), orient(N, 9);
+    for (int i = 0; i < N; i++) orient(i, 0) = orient(i, 4) = orient(i, 8) = 1.0;
+    obj.initialize(dat, mom, orient, ang);
+    matrix<double> F(N, 3), T(N, 3);
+    obj.calculate_forces_and_torques3D(F, T);
+    matrix<int> pairs;
+    obj.calculatepairs_parallel(3.5, pairs);
+    obj.init_forces();
+    vector1<double> meas(6);
+    for (int i = 0; i < runtime; i++) {
+        obj.measured_temperature(meas);
+        obj.step(1);
+    }
+    obj.getdat(dat);
+    obj.getorientation(orient);
+}
+
+int main() { return 0; }
