@@ -192,6 +192,26 @@ const char *mtg_last_error(const mtg_system *h);
 const char *mtg_status_string(int status);
 int mtg_api_version(void);
 
+/* Neighbour-pair build that allocates no device memory.  It has no counterpart in the reference.
+ * It is for callers that cannot allocate device memory when they need the pair list: code that runs
+ * inside another framework's memory pool or allocator hooks, or a host application that reserves the
+ * device memory up front and forbids allocations inside its step loop.  Inputs and outputs are the
+ * caller's DEVICE buffers: x_dev (n x 3 doubles, row-major), pairs_dev (room for cap pairs of two
+ * int32, i < j, unordered) and npairs_dev (one int64: the number of pairs within rc, which may exceed
+ * cap; only the first cap are written).  Work is queued on `stream` (a cudaStream_t, NULL for the
+ * default stream); results are ready when the stream is.  The inclusion test is the reference's
+ * cube::distance_less_than, so the set equals mtg_pairs on the same coordinates.
+ * Scratch lives in one fixed array inside the library (a file-scope device array, held by every GPU
+ * that loads the library until the process exits), which limits a call to
+ * n <= MTG_NOALLOC_MAX_PARTICLES and (floor(box / rc))^3 <= MTG_NOALLOC_MAX_CELLS; larger calls return
+ * MTG_ERR_ARG without touching the device.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) and should come before any stream capture.  Every call shares the one
+ * array: calls that overlap on the GPU (different streams, or host threads sharing a device) race. */
+#define MTG_NOALLOC_MAX_PARTICLES 65536
+#define MTG_NOALLOC_MAX_CELLS 65536
+mtg_status mtg_pairs_noalloc(const double *x_dev, int n, double box, int periodic, double rc, int32_t *pairs_dev,
+                             int64_t cap, int64_t *npairs_dev, void *stream);
+
 /* Host-side seeded synthetic inputs (no GPU use).
  * mtg_random_positions: uniform in [0, box)^3 with non-overlap rejection at min_dist (minimum image
  * when periodic); returns MTG_ERR_ARG if the packing cannot be reached in 1000*n attempts.

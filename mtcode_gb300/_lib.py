@@ -17,6 +17,8 @@ MTG_MAX_ORIENT = 16
 MTG_MAX_POTS = 64
 MTG_OBS_COUNT = 5
 MTG_PROFILE_KERNELS = 5
+MTG_NOALLOC_MAX_PARTICLES = 65536
+MTG_NOALLOC_MAX_CELLS = 65536
 PROFILE_KERNEL_NAMES = ("scan_reduce", "scan_top", "scan_down", "scatter", "force")
 MTG_FP32 = 0
 MTG_FP64 = 1
@@ -104,6 +106,8 @@ SIGNATURES = [
     ("mtg_last_error", C.c_char_p, [_H]),
     ("mtg_status_string", C.c_char_p, [C.c_int]),
     ("mtg_api_version", C.c_int, []),
+    ("mtg_pairs_noalloc", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_double, C.c_void_p, C.c_int64,
+                                     C.c_void_p, C.c_void_p]),
     ("mtg_random_positions", C.c_int, [C.c_int, C.c_double, C.c_int, C.c_double, C.c_uint64, _D]),
     ("mtg_random_rotations", None, [C.c_int, C.c_uint64, _D]),
 ]

@@ -22,7 +22,7 @@ BUILD = PKG / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", str(ROOT / "include")]
-CU_SOURCES = ["mtg_api.cu", "mtg_sys_f32.cu", "mtg_sys_f64.cu"]
+CU_SOURCES = ["mtg_api.cu", "mtg_sys_f32.cu", "mtg_sys_f64.cu", "mtg_noalloc.cu"]
 CPP_SOURCES = ["mtg_host.cpp"]
 
 
