@@ -1,0 +1,51 @@
+"""Run a seeded workload for a number of steps and report the time per step.
+
+    python -m mtcode_gb300.run --workload c4 --replicas 48 --steps 4 [--precision fp32] [--profile]
+
+Used for quick timing and as the target of profiler captures (it launches the same kernels as the
+benchmark, on a workload of the chosen size).
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+import numpy as np
+
+from . import LangevinNVTRGPU, workloads
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--workload", default="c4", choices=sorted(workloads.WORKLOADS))
+    ap.add_argument("--replicas", type=int, default=512, help="replicas of the c4 workload")
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
+    ap.add_argument("--kernel", choices=["tiled", "per_particle"], default="tiled")
+    ap.add_argument("--profile", action="store_true", help="also print per-kernel device times")
+    args = ap.parse_args()
+    if args.workload == "c4":
+        W = workloads.patchy_c4(seed=args.seed, n_replicas=args.replicas)
+    else:
+        W = workloads.WORKLOADS[args.workload](seed=args.seed)
+    n = W.n_total
+    z = np.zeros((n, 3))
+    with LangevinNVTRGPU(W.replicas, precision=args.precision, force_kernel=args.kernel) as s:
+        s.initialize(W.x, z, z, W.Q)
+        s.init_forces()
+        s.sync()
+        t0 = time.perf_counter()
+        s.step(args.steps)
+        s.sync()
+        dt = time.perf_counter() - t0
+        line = f"{W.name}: {len(W.replicas)} replicas, {n} particles, {args.steps} steps, {1e3 * dt / args.steps:.3f} ms/step, " \
+               f"{n * args.steps / dt:.3e} particle-steps/s"
+        if args.profile:
+            prof = s.step_profile(max(1, args.steps))
+            line += " | " + " ".join(f"{k}={v / max(1, args.steps):.3f}ms" for k, v in prof.items())
+        print(line, flush=True)
+
+
+if __name__ == "__main__":
+    main()
