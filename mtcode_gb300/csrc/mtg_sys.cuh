@@ -134,7 +134,7 @@ inline int grid_for(int64_t n, int block, int per_sm, int sms) {
     return (int)std::max<int64_t>(1, std::min(need, cap));
 }
 
-// Tile plan of one replica for the FP32 tile kernel: whole x-rows or chunks of 32/16/8 cells, times
+// Tile plan of one replica for the FP32 tile kernel: whole x-rows or chunks of 30/16/8 cells, times
 // T x T rows (T = 4, 2, 1).  Warps take 32-particle units of a tile, so larger tiles only lower the
 // halo share; the choice is the largest tile whose expected staged count (tile + one-cell halo, from
 // the mean cell occupancy) is at most half the staging buffer, leaving room for density fluctuations.
@@ -147,7 +147,7 @@ inline void plan_tiles(int rep, int nc, double per_cell, std::vector<int4> &out)
     std::vector<Cand> cands;
     for (int T : {4, 2, 1}) {
         if (nc <= mtg::kTileXMax) cands.push_back({true, nc, T, nc * T * T * per_cell, nc * (T + 2.0) * (T + 2.0) * per_cell});
-        for (int tx : {32, 16, 8})
+        for (int tx : {30, 16, 8})  // a staged row (tx + 2 cells) spans at most one warp's lanes
             if (tx + 2 <= nc) cands.push_back({false, tx, T, tx * T * T * per_cell, (tx + 2.0) * (T + 2.0) * (T + 2.0) * per_cell});
     }
     const Cand *best = nullptr;

@@ -4,8 +4,8 @@
 //   stage   the positions of the tile and its one-cell halo (16 B per particle) are copied into shared
 //           memory by cp.async.bulk (TMA bulk copies, one per contiguous row piece) on an mbarrier;
 //           the wait is bounded and latches MTG_FLAG_TIMEOUT instead of hanging
-//   phase 1 one thread per home particle scans its 27 cells in shared memory and appends every pair
-//           within the force range to a shared pair list           (cheap, the only divergent loop)
+//   phase 1 one lane per home particle scans its 27 cells in shared memory; in-range pairs are
+//           appended to the warp's pair list by ballot (warp-uniform loops, no atomics)
 //   phase 2 all threads take pairs evenly: WCA core, body-frame cone tests; every in-cone patch
 //           potential is appended to a shared task list
 //   phase 3 all threads take tasks evenly: Kern-Frenkel force/torque (the transcendental part)
@@ -37,11 +37,12 @@ constexpr unsigned kWaitSpins = 1u << 20;
 enum StageMode : int { kStaged = 0, kSlots = 1 };
 
 // one staging buffer: a tile's positions (TMA-copied) and cell table, or -- for tiny replicas and tiles
-// too crowded to stage -- just the slot ranges of its particles
+// too crowded to stage -- just the slot ranges of its particles.  A staged particle k of staged cell c
+// has global slot cell_lo[c] + (k - cell_sm[c]).
 struct StageBuf {
     float4 pos[kStageCap];
-    int slot[kStageCap];             // global slot of every staged particle
-    int cell_sm[kStageCells + 1];    // offset of every staged cell in pos[]
+    int cell_sm[kStageCells + 1];    // offset of every staged cell in pos[] (+ the total)
+    int cell_lo[kStageCells];        // global slot of the first particle of every staged cell
     int row_start[kTileYZMax * kTileYZMax + 1];  // home particles before each home row
     int seg_s0[kTileYZMax * kTileYZMax], seg_n[kTileYZMax * kTileYZMax + 1];  // kSlots: slot runs
     unsigned long long bar;
@@ -54,14 +55,22 @@ struct StageBuf {
     int done;                        // units of this tile finished by the consumers
 };
 
+// pair-list entry: staged particle k (bits 0-10), its staged cell (bits 11-21), home lane (22-26)
+__device__ __forceinline__ unsigned pair_entry(int k, int cell, int lane) {
+    return (unsigned)k | ((unsigned)cell << 11) | ((unsigned)lane << 22);
+}
+__device__ __forceinline__ int pair_k(unsigned e) { return (int)(e & 2047u); }
+__device__ __forceinline__ int pair_cell(unsigned e) { return (int)((e >> 11) & 2047u); }
+__device__ __forceinline__ int pair_h(unsigned e) { return (int)(e >> 22); }
+
 // per-warp scratch: the compacted pair and task lists of 32 home particles and their sums
 struct WarpScratch {
     unsigned long long acc[32][6];
+    float4 h_qa[32], h_qb[32];       // home orientation rows (Q0..Q3, Q4..Q7); Q8 is pos.w
     int h_k[32], h_slot[32], h_id[32];
-    short pair_k[kWarpPairCap];
-    unsigned char pair_h[kWarpPairCap];
+    unsigned pair[kWarpPairCap];
     unsigned task[kWarpTaskCap];
-    int npairs, ntasks;
+    int ntasks;
 };
 
 struct TileShared {
@@ -187,14 +196,20 @@ __device__ __forceinline__ void load_q(const ForceArgs<float> &a, int slot, floa
     Q[4] = c[0]; Q[5] = c[1]; Q[6] = c[2]; Q[7] = c[3]; Q[8] = q8;
 }
 
+__device__ __forceinline__ void home_q(const WarpScratch &W, int h, float q8, float Q[9]) {
+    const float4 b = W.h_qa[h], c = W.h_qb[h];
+    Q[0] = b.x; Q[1] = b.y; Q[2] = b.z; Q[3] = b.w;
+    Q[4] = c.x; Q[5] = c.y; Q[6] = c.z; Q[7] = c.w; Q[8] = q8;
+}
+
 // one in-cone patch potential q of pair p of warp scratch W (phase 3, or at once when the task list
 // is full): Kern-Frenkel force on the home particle and torque on it, into W's fixed-point sums
 __device__ __noinline__ void eval_task(const ForceArgs<float> &a, const Replica<float> &R, const Model<float> &M,
                                        const StageBuf &B, WarpScratch &W, int p, int q) {
-    const int h = W.pair_h[p];
-    const int kk = W.pair_k[p];
-    const int ki = W.h_k[h], si = W.h_slot[h], idi = W.h_id[h];
-    const int j = B.slot[kk];
+    const unsigned e = W.pair[p];
+    const int h = pair_h(e), kk = pair_k(e), cj = pair_cell(e);
+    const int ki = W.h_k[h], idi = W.h_id[h];
+    const int j = B.cell_lo[cj] + (kk - B.cell_sm[cj]);
     const int idj = __ldg(a.buf.ident + j);
     const float4 pi = B.pos[ki], pj = B.pos[kk];
     float d[3] = {min_image<float>(pi.x - pj.x, R.box, R.l2s, R.periodic),
@@ -206,7 +221,7 @@ __device__ __noinline__ void eval_task(const ForceArgs<float> &a, const Replica<
     const float sg = i_first ? 1.f : -1.f, inv = 1.f / rr;
     const float u[3] = {sg * d[0] * inv, sg * d[1] * inv, sg * d[2] * inv};
     float Qi[9], Qj[9];
-    load_q(a, si, pi.w, Qi);
+    home_q(W, h, pi.w, Qi);
     load_q(a, j, pj.w, Qj);
     const float *Qa = i_first ? Qi : Qj, *Qb = i_first ? Qj : Qi;
     const int ta = type_of<float>(M, (i_first ? idi : idj) - R.off);
@@ -222,10 +237,10 @@ __device__ __noinline__ void eval_task(const ForceArgs<float> &a, const Replica<
         n2[k] = b2[0] * Qb[k] + b2[1] * Qb[3 + k] + b2[2] * Qb[6 + k];
     }
     // the cone test already passed in the body frame; the lab-frame cosines feed the force
-    const float ci = -(n1[0] * u[0] + n1[1] * u[1] + n1[2] * u[2]);
-    const float cj = n2[0] * u[0] + n2[1] * u[1] + n2[2] * u[2];
-    float f[3] = {0, 0, 0}, tqa[3] = {0, 0, 0}, tqb[3] = {0, 0, 0}, e = 0;
-    kf2_pair<float>(M.att[q], M.dis[q], M.inv_dis[q], M.kfac[q], u, rr, n1, n2, ci, cj, f, tqa, tqb, e);
+    const float cos1 = -(n1[0] * u[0] + n1[1] * u[1] + n1[2] * u[2]);
+    const float cos2 = n2[0] * u[0] + n2[1] * u[1] + n2[2] * u[2];
+    float f[3] = {0, 0, 0}, tqa[3] = {0, 0, 0}, tqb[3] = {0, 0, 0}, en = 0;
+    kf2_pair<float>(M.att[q], M.dis[q], M.inv_dis[q], M.kfac[q], u, rr, n1, n2, cos1, cos2, f, tqa, tqb, en);
     unsigned long long *acc = W.acc[h];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
@@ -237,8 +252,8 @@ __device__ __noinline__ void eval_task(const ForceArgs<float> &a, const Replica<
 // phase 2 body: WCA core + cone tests of pair p; in-cone potentials become tasks
 __device__ __forceinline__ void eval_pair(const ForceArgs<float> &a, const Replica<float> &R, const Model<float> &M,
                                           const StageBuf &B, WarpScratch &W, int p, bool &big) {
-    const int h = W.pair_h[p];
-    const int kk = W.pair_k[p];
+    const unsigned e = W.pair[p];
+    const int h = pair_h(e), kk = pair_k(e);
     const int ki = W.h_k[h];
     const float4 pi = B.pos[ki], pj = B.pos[kk];
     float d[3] = {min_image<float>(pi.x - pj.x, R.box, R.l2s, R.periodic),
@@ -255,7 +270,8 @@ __device__ __forceinline__ void eval_pair(const ForceArgs<float> &a, const Repli
         acc_add(acc + 2, s_ * d[2]);
     }
     if (!(r2 < R.patch_r2)) return;
-    const int j = B.slot[kk];
+    const int cj = pair_cell(e);
+    const int j = B.cell_lo[cj] + (kk - B.cell_sm[cj]);
     const int idi = W.h_id[h];
     const int idj = __ldg(a.buf.ident + j);
     const bool single = M.n_types == 1;
@@ -266,7 +282,7 @@ __device__ __forceinline__ void eval_pair(const ForceArgs<float> &a, const Repli
     const float sg = i_first ? 1.f : -1.f, inv = 1.f / rr;
     const float u[3] = {sg * d[0] * inv, sg * d[1] * inv, sg * d[2] * inv};
     float Qi[9], Qj[9];
-    load_q(a, W.h_slot[h], pi.w, Qi);
+    home_q(W, h, pi.w, Qi);
     load_q(a, j, pj.w, Qj);
     const float *Qa = i_first ? Qi : Qj, *Qb = i_first ? Qj : Qi;
     const int ta = i_first ? ti : tj, tb = i_first ? tj : ti;
@@ -323,13 +339,30 @@ __device__ __forceinline__ int staged_cell(const TileGeom &g, const Replica<floa
 
 __device__ __forceinline__ int ld_volatile(const int *p) { return *(const volatile int *)p; }
 
+__device__ __forceinline__ int warp_inclusive_scan(int v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
 // Producer warp: build buffer B's table for `tile` and start its bulk copies.  Returns the number of
 // 32-particle units of the tile.
+//   1  lanes over the flattened staged cells (row-major, x fastest): count and first global slot of
+//      every cell, eight cells per lane in flight
+//   2  one exclusive scan over the flattened counts (a chunk per lane + a warp scan) -> cell_sm
+//   3  lanes over the staged rows: each row is one contiguous run of global slots (consecutive x
+//      cells are consecutive in the sorted order) plus, for a chunk at the box edge, one wrapped
+//      cell; every lane issues its rows' bulk copies.  Copies are issued only when the whole tile
+//      fits, so the bytes the barrier expects are exactly the bytes copied.
 __device__ int produce_tile(const ForceArgs<float> &a, const int4 *tiles, int tile, StageBuf &B, int lane) {
     const int4 desc = tiles[tile];
     const TileGeom g = decode_tile(desc);
     const Replica<float> &R = a.tb.reps[g.rep];
     int nhome = 0, mode = kStaged, total = 0;
+    unsigned issued = 0;  // bytes of bulk copies this lane issued
     if (g.simple) {
         mode = kSlots;
         if (lane == 0) {
@@ -340,89 +373,114 @@ __device__ int produce_tile(const ForceArgs<float> &a, const int4 *tiles, int ti
         }
         nhome = R.n;
     } else {
-        const int nry = g.ty + 2, nrz = g.tz + 2;
-        const int ncs = g.sx * nry * nrz;
-        // cell counts in lane-strided rounds of 32 cells, four rounds in flight, warp-shuffle scan
-        int base = 0;
-        for (int c0 = 0; c0 < ncs; c0 += 128) {
-            int gs[4], cnt[4];
+        const int nc = R.nc, sx = g.sx;
+        const int nry = g.ty + 2, nrz = g.tz + 2, nrows = nry * nrz, ncell = nrows * sx;
+        const float inv_sx = 1.f / (float)sx;
+        // -- 1: counts and global starts
+        constexpr int kBatch = 8;
+        for (int i0 = 0; i0 < ncell; i0 += 32 * kBatch) {
+            int lo[kBatch], hi[kBatch];
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int c = c0 + 32 * q + lane;
-                gs[q] = 0;
-                cnt[q] = 0;
-                if (c < ncs) {
-                    const int gcell = staged_cell(g, R, c % g.sx, (c / g.sx) % nry, c / (g.sx * nry));
-                    if (gcell >= 0) {
-                        gs[q] = __ldg(a.start + gcell);
-                        cnt[q] = __ldg(a.start + gcell + 1) - gs[q];
+            for (int q = 0; q < kBatch; q++) {
+                const int i = i0 + 32 * q + lane;
+                lo[q] = hi[q] = 0;
+                if (i < ncell) {
+                    // i / sx exactly: (i + 0.5) / sx is at least 0.5 / sx away from an integer
+                    const int r = __float2int_rz(((float)i + 0.5f) * inv_sx);
+                    const int c = i - r * sx;
+                    const int gc = staged_cell(g, R, c, r % nry, r / nry);
+                    if (gc >= 0) {
+                        lo[q] = __ldg(a.start + gc);
+                        hi[q] = __ldg(a.start + gc + 1);
                     }
                 }
             }
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int c = c0 + 32 * q + lane;
-                int inc = cnt[q];
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int t = __shfl_up_sync(0xffffffffu, inc, o);
-                    if (lane >= o) inc += t;
+            for (int q = 0; q < kBatch; q++) {
+                const int i = i0 + 32 * q + lane;
+                if (i < ncell) {
+                    B.cell_sm[i] = hi[q] - lo[q];
+                    B.cell_lo[i] = lo[q];
                 }
-                const int off = base + inc - cnt[q];
-                if (c < ncs) {
-                    B.cell_sm[c] = off;
-                    for (int k = 0; k < cnt[q] && off + k < kStageCap; k++) B.slot[off + k] = gs[q] + k;
-                }
-                base += __shfl_sync(0xffffffffu, inc, 31);
             }
         }
-        total = base;
-        if (lane == 0) B.cell_sm[ncs] = total;
         __syncwarp();
-        const int hx0 = g.whole ? 0 : 1, hx1 = g.whole ? g.sx : g.sx - 1;
-        const int nrows = g.ty * g.tz;
+        // -- 2: exclusive scan of the counts
+        const int per = (ncell + 31) >> 5;
+        const int j0 = min(lane * per, ncell), j1 = min(j0 + per, ncell);
+        int sum = 0;
+        for (int j = j0; j < j1; j++) sum += B.cell_sm[j];
+        const int inc = warp_inclusive_scan(sum, lane);
+        int run = inc - sum;
+        for (int j = j0; j < j1; j++) {
+            const int cnt = B.cell_sm[j];
+            B.cell_sm[j] = run;
+            run += cnt;
+        }
+        total = __shfl_sync(0xffffffffu, inc, 31);
+        if (lane == 0) B.cell_sm[ncell] = total;
+        __syncwarp();
+        const int hx0 = g.whole ? 0 : 1, hx1 = g.whole ? sx : sx - 1;
+        const int nhrows = g.ty * g.tz;
         if (total <= kStageCap) {
-            if (lane == 0) {
-                int acc = 0;
-                for (int r = 0; r < nrows; r++) {
-                    const int rb = ((1 + r / g.ty) * nry + (1 + r % g.ty)) * g.sx;
-                    B.row_start[r] = acc;
-                    acc += B.cell_sm[rb + hx1] - B.cell_sm[rb + hx0];
-                }
-                B.row_start[nrows] = acc;
+            // -- 3: copies, lanes over rows.  The unwrapped run is staged cells [ru0, ru1); a chunk that
+            // starts at x = 0 has its wrapped cell first, one that ends at the box's far side last.
+            int ru0 = 0, ru1 = sx;
+            if (!g.whole) {
+                if (g.x0 == 0) ru0 = 1;
+                else if (g.x0 - 1 + sx > nc) ru1 = sx - 1;
             }
-            __syncwarp();
-            nhome = B.row_start[nrows];
-            if (nhome == 0) {
-                mode = kSlots;  // nothing to compute: no copies either
-                if (lane == 0) {
-                    B.seg_n[0] = 0;
-                    B.nseg = 0;
+            const int wc = ru0 == 1 ? 0 : (ru1 < sx ? sx - 1 : -1);
+            bool fenced = false;
+            for (int r = lane; r < nrows; r += 32) {
+                const int rb = r * sx;
+                const int k0 = B.cell_sm[rb + ru0], k1 = B.cell_sm[rb + ru1];
+                if (k1 > k0) {
+                    if (!fenced) { fence_proxy_async(); fenced = true; }
+                    bulk_copy_g2s(&B.pos[k0], a.buf.pos + 4 * (size_t)B.cell_lo[rb + ru0], (unsigned)(k1 - k0) * 16u,
+                                  &B.bar);
+                    issued += (unsigned)(k1 - k0) * 16u;
+                }
+                if (wc >= 0) {
+                    const int w0 = B.cell_sm[rb + wc], w1 = B.cell_sm[rb + wc + 1];
+                    if (w1 > w0) {
+                        if (!fenced) { fence_proxy_async(); fenced = true; }
+                        bulk_copy_g2s(&B.pos[w0], a.buf.pos + 4 * (size_t)B.cell_lo[rb + wc], (unsigned)(w1 - w0) * 16u,
+                                      &B.bar);
+                        issued += (unsigned)(w1 - w0) * 16u;
+                    }
                 }
             }
+            // home particles before each home row
+            int hn = 0;
+            if (lane < nhrows) {
+                const int rb = ((1 + lane / g.ty) * nry + (1 + lane % g.ty)) * sx;
+                hn = B.cell_sm[rb + hx1] - B.cell_sm[rb + hx0];
+            }
+            const int hinc = warp_inclusive_scan(hn, lane);
+            if (lane < nhrows) B.row_start[lane] = hinc - hn;
+            nhome = __shfl_sync(0xffffffffu, hinc, 31);
+            if (lane == 0) B.row_start[nhrows] = nhome;
         } else {
-            // too crowded to stage: the home rows as slot runs (consecutive cells, contiguous slots)
+            // too crowded to stage: the home rows as slot runs, nothing copied
             mode = kSlots;
             int n = 0, s0 = 0;
-            if (lane < nrows) {
+            if (lane < nhrows) {
                 const int ry = 1 + lane % g.ty, rz = 1 + lane / g.ty;
-                const int c0 = staged_cell(g, R, hx0, ry, rz), c1 = staged_cell(g, R, hx1 - 1, ry, rz);
+                const int gy = g.y0 - 1 + ry, gz = g.z0 - 1 + rz;  // home rows are inside the box
+                const int c0 = R.cell_off + (g.whole ? 0 : g.x0) + nc * (gy + nc * gz);
+                const int c1 = c0 + (hx1 - hx0) - 1;
                 s0 = __ldg(a.start + c0);
                 n = __ldg(a.start + c1 + 1) - s0;
             }
-            int inc = n;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int t = __shfl_up_sync(0xffffffffu, inc, o);
-                if (lane >= o) inc += t;
-            }
-            if (lane < nrows) {
+            const int hinc = warp_inclusive_scan(n, lane);
+            if (lane < nhrows) {
                 B.seg_s0[lane] = s0;
-                B.seg_n[lane] = inc - n;
+                B.seg_n[lane] = hinc - n;
             }
-            if (lane == nrows - 1) B.seg_n[nrows] = inc;
-            if (lane == 0) B.nseg = nrows;
-            nhome = __shfl_sync(0xffffffffu, inc, nrows - 1);
+            if (lane == nhrows - 1) B.seg_n[nhrows] = hinc;
+            if (lane == 0) B.nseg = nhrows;
+            nhome = __shfl_sync(0xffffffffu, hinc, 31);
         }
     }
     const int units = (nhome + 31) / 32;
@@ -432,27 +490,11 @@ __device__ int produce_tile(const ForceArgs<float> &a, const int4 *tiles, int ti
         B.total = total;
         B.nhome = nhome;
     }
+    issued = __reduce_add_sync(0xffffffffu, issued);
     __syncwarp();
-    if (lane == 0) mbar_arrive_expect_tx(&B.bar, mode == kStaged ? (unsigned)total * 16u : 0u);
-    if (mode == kStaged) {
-        const int nry = g.ty + 2, nrows_all = nry * (g.tz + 2);
-        fence_proxy_async();
-        for (int row = lane; row < nrows_all; row += 32) {
-            const int sy = row % nry, sz = row / nry, rb = row * g.sx;
-            int c = 0;
-            while (c < g.sx) {
-                const int gc0 = staged_cell(g, R, c, sy, sz);
-                int e = c + 1;
-                if (gc0 >= 0)
-                    while (e < g.sx && staged_cell(g, R, e, sy, sz) == gc0 + (e - c)) e++;
-                const int bytes = (B.cell_sm[rb + e] - B.cell_sm[rb + c]) * 16;
-                if (gc0 >= 0 && bytes > 0)
-                    bulk_copy_g2s(&B.pos[B.cell_sm[rb + c]], a.buf.pos + 4 * (size_t)B.slot[B.cell_sm[rb + c]],
-                                  (unsigned)bytes, &B.bar);
-                c = e;
-            }
-        }
-    }
+    // the single arrival expects exactly the bytes issued (zero when nothing was copied), so the
+    // phase always completes
+    if (lane == 0) mbar_arrive_expect_tx(&B.bar, issued);
     return units;
 }
 
@@ -480,52 +522,89 @@ __device__ void consume_staged_unit(const ForceArgs<float> &a, const StageBuf &B
             else hi = mid;
         }
         mycell = rb + lo;
-        const int slot = B.slot[myk];
+        const int slot = B.cell_lo[mycell] + (myk - B.cell_sm[mycell]);
         W.h_k[lane] = myk;
         W.h_slot[lane] = slot;
         W.h_id[lane] = __ldg(a.buf.ident + slot);
+        W.h_qa[lane] = __ldg(reinterpret_cast<const float4 *>(a.buf.rota) + slot);
+        W.h_qb[lane] = __ldg(reinterpret_cast<const float4 *>(a.buf.rotb) + slot);
     }
 #pragma unroll
     for (int k = 0; k < 6; k++) W.acc[lane][k] = 0ull;
-    if (lane == 0) {
-        W.npairs = 0;
-        W.ntasks = 0;
-    }
+    if (lane == 0) W.ntasks = 0;
     __syncwarp();
 
-    // -- phase 1: candidate scan in shared memory
-    if (active) {
-        const float4 pi = B.pos[myk];
+    // -- phase 1: candidate scan in shared memory.  A neighbour cell reached across a periodic face
+    // holds unshifted coordinates; its image shift s (0 or +-L per axis, known from the staged cell's
+    // unwrapped coordinate) gives the separation (x_i - x_j) - s, which is exactly what the minimum-image
+    // rule computes for every pair within the force range.  The three cells of a row are at most two
+    // contiguous segments (split only where an image shift changes).  The loops are warp-uniform (each
+    // row runs to the longest lane's candidate count), so in-range candidates are appended with one
+    // ballot per candidate round and no shared-memory atomics.
+    int npairs = 0;  // warp-uniform
+    {
+        const float4 pi = active ? B.pos[myk] : make_float4(0.f, 0.f, 0.f, 0.f);
         const int lx = mycell % g.sx, ly = (mycell / g.sx) % nry, lz = mycell / (g.sx * nry);
-        for (int dz = -1; dz <= 1; dz++)
+        const int nc = R.nc;
+        const float L = R.box;
+        const unsigned lt_mask = (1u << lane) - 1u;
+        for (int dz = -1; dz <= 1; dz++) {
+            const int gz = g.z0 - 1 + lz + dz;
+            const float shz = gz < 0 ? -L : (gz >= nc ? L : 0.f);
             for (int dy = -1; dy <= 1; dy++) {
+                const int gy = g.y0 - 1 + ly + dy;
+                const float shy = gy < 0 ? -L : (gy >= nc ? L : 0.f);
                 const int rowb = ((lz + dz) * nry + (ly + dy)) * g.sx;
-                for (int dx = -1; dx <= 1; dx++) {
-                    int cx = lx + dx;
-                    if (g.whole && (cx < 0 || cx >= g.sx)) {
-                        if (!R.periodic) continue;
-                        cx = cx < 0 ? cx + g.sx : cx - g.sx;
-                    }
-                    const int k0 = B.cell_sm[rowb + cx], k1 = B.cell_sm[rowb + cx + 1];
-                    for (int kk = k0; kk < k1; kk++) {
-                        if (kk == myk) continue;
-                        const float4 pj = B.pos[kk];
-                        const float dx_ = min_image<float>(pi.x - pj.x, R.box, R.l2s, R.periodic);
-                        const float dy_ = min_image<float>(pi.y - pj.y, R.box, R.l2s, R.periodic);
-                        const float dz_ = min_image<float>(pi.z - pj.z, R.box, R.l2s, R.periodic);
-                        if (dx_ * dx_ + dy_ * dy_ + dz_ * dz_ < R.rc2) {
-                            const int p = atomicAdd(&W.npairs, 1);
-                            if (p < kWarpPairCap) {
-                                W.pair_k[p] = (short)kk;
-                                W.pair_h[p] = (unsigned char)lane;
-                            }
-                        }
+                // segments of this row: [c0, c1) unshifted in x, plus one wrapped cell cw (shift shw)
+                int c0 = lx - 1, c1 = lx + 2, cw = -1;
+                float shw = 0.f;
+                if (g.whole) {
+                    if (c0 < 0) { c0 = 0; cw = R.periodic ? nc - 1 : -1; shw = -L; }
+                    if (c1 > g.sx) { c1 = g.sx; cw = R.periodic ? 0 : -1; shw = L; }
+                } else {
+                    const int gx0 = g.x0 - 1 + c0, gx1 = g.x0 - 1 + (c1 - 1);
+                    if (gx0 < 0) { cw = c0; shw = -L; c0 += 1; }
+                    else if (gx1 >= nc) { cw = c1 - 1; shw = L; c1 -= 1; }
+                }
+                int ka = 0, lena = 0, kb = 0, len = 0, b1 = 0, b2 = 0;
+                if (active) {
+                    ka = B.cell_sm[rowb + c0];
+                    lena = B.cell_sm[rowb + c1] - ka;
+                    b1 = c0 + 1 < c1 ? B.cell_sm[rowb + c0 + 1] : 1 << 30;  // cell boundaries inside [c0, c1)
+                    b2 = c0 + 2 < c1 ? B.cell_sm[rowb + c0 + 2] : 1 << 30;
+                    len = lena;
+                    if (cw >= 0) {
+                        kb = B.cell_sm[rowb + cw];
+                        len += B.cell_sm[rowb + cw + 1] - kb;
                     }
                 }
+                const int maxlen = __reduce_max_sync(0xffffffffu, len);
+                for (int t = 0; t < maxlen; t++) {
+                    bool hit = false;
+                    int kk = 0, cell = 0;
+                    if (t < len) {
+                        const bool sega = t < lena;
+                        kk = sega ? ka + t : kb + (t - lena);
+                        cell = sega ? rowb + c0 + (kk >= b1) + (kk >= b2) : rowb + cw;
+                        const float shx = sega ? 0.f : shw;
+                        const float4 pj = B.pos[kk];
+                        const float ddx = (pi.x - pj.x) - shx;
+                        const float ddy = (pi.y - pj.y) - shy;
+                        const float ddz = (pi.z - pj.z) - shz;
+                        hit = kk != myk && ddx * ddx + ddy * ddy + ddz * ddz < R.rc2;
+                    }
+                    const unsigned m = __ballot_sync(0xffffffffu, hit);
+                    if (hit) {
+                        const int p = npairs + __popc(m & lt_mask);
+                        if (p < kWarpPairCap) W.pair[p] = pair_entry(kk, cell, lane);
+                    }
+                    npairs += __popc(m);
+                }
             }
+        }
     }
     __syncwarp();
-    if (W.npairs > kWarpPairCap) {
+    if (npairs > kWarpPairCap) {
         // more pairs than the warp's list holds: these 32 particles take the per-thread path
         if (active) simple_particle<float, MODE>(a, W.h_slot[lane]);
         overflow = 1;
@@ -533,7 +612,6 @@ __device__ void consume_staged_unit(const ForceArgs<float> &a, const StageBuf &B
         return;
     }
     // -- phase 2: the warp's pairs spread over its lanes
-    const int npairs = W.npairs;
     for (int p = lane; p < npairs; p += 32) eval_pair(a, R, M, B, W, p, big);
     __syncwarp();
     // -- phase 3: in-cone patch potentials spread over the lanes
@@ -593,7 +671,15 @@ __global__ void __launch_bounds__(kTileThreads, 1) tile_force_kernel(ForceArgs<f
             if (tile >= ntiles) break;
             StageBuf &B = sh.buf[k % kStageBufs];
             if (k >= kStageBufs) {
-                // wait until the consumers are done with the tile this buffer held
+                // the previous use's copies have landed (also when no consumer waited on them) ...
+                bool landed = false;
+                const unsigned prev = (unsigned)((k - kStageBufs) / kStageBufs) & 1u;
+                for (unsigned it = 0; it < kWaitSpins && !landed; it++) landed = mbar_try_wait(&B.bar, prev);
+                if (!landed) {
+                    if (lane == 0) atomicOr(a.flags, 4u);
+                    break;
+                }
+                // ... and the consumers are done with the tile this buffer held
                 const int need = B.nunits;
                 bool ok = false;
                 for (unsigned it = 0; it < (kWaitSpins << 4) && !ok; it++) {
