@@ -132,8 +132,8 @@ void mtg_replica_defaults(mtg_replica_desc *r) {
 }
 
 mtg_status mtg_create(const mtg_config *cfg, mtg_system **out) {
-    if (!cfg || !out || cfg->n_replicas < 1 || !cfg->replicas) {
-        g_create_error = "mtg_create: null config/output or no replicas";
+    if (!cfg || !out || cfg->n_replicas < 1 || cfg->n_replicas >= (1 << 30) || !cfg->replicas) {
+        g_create_error = "mtg_create: null config/output, or replica count outside [1, 2^30)";
         return MTG_ERR_ARG;
     }
     *out = nullptr;

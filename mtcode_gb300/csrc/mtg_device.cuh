@@ -56,6 +56,7 @@ struct Model {
     real orient[kMaxOrient][3];
     real att[kMaxPots], dis[kMaxPots], inv_dis[kMaxPots], rmax[kMaxPots], costm[kMaxPots], kfac[kMaxPots];
     real mincos[kMaxTypes][kMaxTypes];  // smallest cos(thetam) of a type pair (early cone reject)
+    real mincos_any[kMaxTypes];         // smallest cos(thetam) of a type with any type
 };
 
 // ------------------------------------------------------------------ vector moves of 12-real rows

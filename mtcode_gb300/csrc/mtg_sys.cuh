@@ -61,6 +61,10 @@ mtg::Model<real> make_model(const mtg_patch_model &m) {
             M.mincos[a][b] = M.mincos[b][a] = (real)mc;
             ps += m.patches_per_type[a] * m.patches_per_type[b];
         }
+    for (int a = 0; a < m.n_types; a++) {
+        M.mincos_any[a] = (real)2;
+        for (int b = 0; b < m.n_types; b++) M.mincos_any[a] = std::min(M.mincos_any[a], M.mincos[a][b]);
+    }
     return M;
 }
 
@@ -138,9 +142,10 @@ inline int grid_for(int64_t n, int block, int per_sm, int sms) {
 // T x T rows (T = 4, 2, 1).  Warps take 32-particle units of a tile, so larger tiles only lower the
 // halo share; the choice is the largest tile whose expected staged count (tile + one-cell halo, from
 // the mean cell occupancy) is at most half the staging buffer, leaving room for density fluctuations.
-inline void plan_tiles(int rep, int nc, double per_cell, std::vector<int4> &out) {
+inline void plan_tiles(int rep, int nc, int periodic, int cell_off, double per_cell, std::vector<int4> &out) {
+    const int rep_word = rep | ((periodic ? 1 : 0) << 30);
     if (nc < 3 || nc > 1023) {
-        out.push_back(make_int4(rep, 0, 1 << 21, 0));
+        out.push_back(make_int4(rep_word, 0, 1 << 21, cell_off));
         return;
     }
     struct Cand { bool whole; int tx, T; double home, staged; };
@@ -166,8 +171,9 @@ inline void plan_tiles(int rep, int nc, double per_cell, std::vector<int4> &out)
             for (int x0 = 0; x0 < nc; x0 += tx) {
                 const int ty = std::min(T, nc - y0), tz = std::min(T, nc - z0);
                 const int sx = best->whole ? nc : std::min(tx, nc - x0) + 2;
-                out.push_back(make_int4(rep, x0 | (y0 << 10) | (z0 << 20),
-                                        sx | (ty << 10) | (tz << 15) | ((best->whole ? 1 : 0) << 20), 0));
+                out.push_back(make_int4(rep_word, x0 | (y0 << 10) | (z0 << 20),
+                                        sx | (ty << 10) | (tz << 15) | ((best->whole ? 1 : 0) << 20) | (nc << 22),
+                                        cell_off));
             }
 }
 
@@ -284,7 +290,7 @@ struct Sys : SysBase {
             if (use_tiles) {
                 std::vector<int4> tiles;
                 for (int r = 0; r < nrep; r++)
-                    plan_tiles(r, reps[r].nc, (double)desc[r].n / ((double)reps[r].nc * reps[r].nc * reps[r].nc), tiles);
+                    plan_tiles(r, reps[r].nc, reps[r].periodic, reps[r].cell_off, (double)desc[r].n / ((double)reps[r].nc * reps[r].nc * reps[r].nc), tiles);
                 ntiles = (int)tiles.size();
                 MTG_CUDA(cudaMalloc(&d_tiles, sizeof(int4) * ntiles));
                 MTG_CUDA(cudaMemcpy(d_tiles, tiles.data(), sizeof(int4) * ntiles, cudaMemcpyHostToDevice));

@@ -6,10 +6,10 @@
 //           the wait is bounded and latches MTG_FLAG_TIMEOUT instead of hanging
 //   phase 1 one lane per home particle scans its 27 cells in shared memory; in-range pairs are
 //           appended to the warp's pair list by ballot (warp-uniform loops, no atomics)
-//   phase 2 all threads take pairs evenly: WCA core, body-frame cone tests; every in-cone patch
-//           potential is appended to a shared task list
-//   phase 3 all threads take tasks evenly: Kern-Frenkel force/torque (the transcendental part)
-//   phase 4 one thread per home particle: friction + Philox noise, half-kick, next-step binning
+//   phase 2 all lanes take pairs evenly: WCA core and the home particle's cone test (2a); the pairs
+//           that pass are compacted and take the neighbour's orientation, the body-frame cone tests
+//           and the Kern-Frenkel force/torque of the in-cone patch potentials (2b)
+//   phase 3 one lane per home particle: friction + Philox noise, half-kick, next-step binning
 // Forces and torques are summed in 64-bit fixed point in shared memory (integer atomics commute), so
 // the result does not depend on the order in which lanes or CTAs visit pairs.
 #pragma once
@@ -25,13 +25,15 @@ constexpr int kConsumerWarps = kTileWarps - 1;
 constexpr int kStageBufs = 3;      // ring of staging buffers: the producer runs up to two tiles ahead
 constexpr int kTileYZMax = 4;
 constexpr int kTileXMax = 32;
-constexpr int kStageCells = (kTileXMax + 2) * (kTileYZMax + 2) * (kTileYZMax + 2);  // 1224
+constexpr int kStageRows = (kTileYZMax + 2) * (kTileYZMax + 2);                   // 36
+constexpr int kStageCells = (kTileXMax + 2) * kStageRows;                           // 1224
+constexpr int kStartRowsCap = (kTileXMax + 2) * kStageRows;  // prefetched start[] entries of a tile
 constexpr int kStageCap = 2048;    // staged particles per buffer
 constexpr int kWarpPairCap = 640;  // in-range pairs per 32 home particles
-constexpr int kWarpTaskCap = 256;  // in-cone patch potentials per 32 home particles
 constexpr unsigned kWaitSpins = 1u << 20;
 
-// tile descriptor: x = replica, y = x0 | y0 << 10 | z0 << 20, z = sx | ty << 10 | tz << 15 | whole << 20 | simple << 21
+// tile descriptor: x = replica | periodic << 30, y = x0 | y0 << 10 | z0 << 20,
+// z = sx | ty << 10 | tz << 15 | whole << 20 | simple << 21 | nc << 22, w = the replica's first cell.
 // sx = staged cells per row (nc for whole rows, tx + 2 for a chunk), tx = sx - 2 for chunks.
 
 enum StageMode : int { kStaged = 0, kSlots = 1 };
@@ -69,13 +71,14 @@ struct WarpScratch {
     float4 h_qa[32], h_qb[32];       // home orientation rows (Q0..Q3, Q4..Q7); Q8 is pos.w
     int h_k[32], h_slot[32], h_id[32];
     unsigned pair[kWarpPairCap];
-    unsigned task[kWarpTaskCap];
-    int ntasks;
 };
 
 struct TileShared {
     StageBuf buf[kStageBufs];
     WarpScratch w[kConsumerWarps];
+    // start[] entries of the next tiles, copied ahead by the producer (cp.async): per staged row the
+    // starts of its sx cells, then the end of its unwrapped run, then the end of its wrapped cell
+    int start_rows[2][kStartRowsCap];
     int claim;                       // next unit of the CTA-wide stream
     int final_units;                 // -1 until the producer has published its last tile
     int overflow;
@@ -111,13 +114,22 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsign
         : "memory");
 }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 struct TileGeom {
-    int rep, x0, y0, z0, sx, ty, tz, whole, simple;
+    int rep, x0, y0, z0, sx, ty, tz, whole, simple, nc, periodic, cell_off;
 };
 __device__ __forceinline__ TileGeom decode_tile(int4 t) {
     TileGeom g;
-    g.rep = t.x;
+    g.rep = t.x & 0x3fffffff;
+    g.periodic = (t.x >> 30) & 1;
+    g.nc = (t.z >> 22) & 1023;
+    g.cell_off = t.w;
     g.x0 = t.y & 1023;
     g.y0 = (t.y >> 10) & 1023;
     g.z0 = (t.y >> 20) & 1023;
@@ -202,34 +214,13 @@ __device__ __forceinline__ void home_q(const WarpScratch &W, int h, float q8, fl
     Q[4] = c.x; Q[5] = c.y; Q[6] = c.z; Q[7] = c.w; Q[8] = q8;
 }
 
-// one in-cone patch potential q of pair p of warp scratch W (phase 3, or at once when the task list
-// is full): Kern-Frenkel force on the home particle and torque on it, into W's fixed-point sums
-__device__ __noinline__ void eval_task(const ForceArgs<float> &a, const Replica<float> &R, const Model<float> &M,
-                                       const StageBuf &B, WarpScratch &W, int p, int q) {
-    const unsigned e = W.pair[p];
-    const int h = pair_h(e), kk = pair_k(e), cj = pair_cell(e);
-    const int ki = W.h_k[h], idi = W.h_id[h];
-    const int j = B.cell_lo[cj] + (kk - B.cell_sm[cj]);
-    const int idj = __ldg(a.buf.ident + j);
-    const float4 pi = B.pos[ki], pj = B.pos[kk];
-    float d[3] = {min_image<float>(pi.x - pj.x, R.box, R.l2s, R.periodic),
-                  min_image<float>(pi.y - pj.y, R.box, R.l2s, R.periodic),
-                  min_image<float>(pi.z - pj.z, R.box, R.l2s, R.periodic)};
-    const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-    const float rr = sqrtf(r2);
-    const bool i_first = idi < idj;
-    const float sg = i_first ? 1.f : -1.f, inv = 1.f / rr;
-    const float u[3] = {sg * d[0] * inv, sg * d[1] * inv, sg * d[2] * inv};
-    float Qi[9], Qj[9];
-    home_q(W, h, pi.w, Qi);
-    load_q(a, j, pj.w, Qj);
-    const float *Qa = i_first ? Qi : Qj, *Qb = i_first ? Qj : Qi;
-    const int ta = type_of<float>(M, (i_first ? idi : idj) - R.off);
-    const int tb = type_of<float>(M, (i_first ? idj : idi) - R.off);
-    const int nb = M.np[tb];
-    const int rel = q - M.pstart[ta][tb];
-    const int ia = rel / nb, ib = rel - ia * nb;
-    const float *b1 = M.orient[M.ooff[ta] + ia], *b2 = M.orient[M.ooff[tb] + ib];
+// Kern-Frenkel force and torques of patch potential q between patch rows oa (of the pair's first
+// particle a) and ob (of b); u = (x_a - x_b) / r.  Adds the force on the home particle (a when i_first)
+// and the torque on it to f and t.
+__device__ __forceinline__ void kf2_potential(const Model<float> &M, int q, int oa, int ob, const float *Qa,
+                                              const float *Qb, const float u[3], float rr, bool i_first, float f[3],
+                                              float t[3]) {
+    const float *b1 = M.orient[oa], *b2 = M.orient[ob];
     float n1[3], n2[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
@@ -239,51 +230,91 @@ __device__ __noinline__ void eval_task(const ForceArgs<float> &a, const Replica<
     // the cone test already passed in the body frame; the lab-frame cosines feed the force
     const float cos1 = -(n1[0] * u[0] + n1[1] * u[1] + n1[2] * u[2]);
     const float cos2 = n2[0] * u[0] + n2[1] * u[1] + n2[2] * u[2];
-    float f[3] = {0, 0, 0}, tqa[3] = {0, 0, 0}, tqb[3] = {0, 0, 0}, en = 0;
-    kf2_pair<float>(M.att[q], M.dis[q], M.inv_dis[q], M.kfac[q], u, rr, n1, n2, cos1, cos2, f, tqa, tqb, en);
-    unsigned long long *acc = W.acc[h];
+    float fk[3] = {0, 0, 0}, tqa[3] = {0, 0, 0}, tqb[3] = {0, 0, 0}, en = 0;
+    kf2_pair<float>(M.att[q], M.dis[q], M.inv_dis[q], M.kfac[q], u, rr, n1, n2, cos1, cos2, fk, tqa, tqb, en);
+    const float sg = i_first ? 1.f : -1.f;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        acc_add(acc + k, sg * f[k]);
-        acc_add(acc + 3 + k, i_first ? tqa[k] : tqb[k]);
+        f[k] += sg * fk[k];
+        t[k] += i_first ? tqa[k] : tqb[k];
     }
 }
 
-// phase 2 body: WCA core + cone tests of pair p; in-cone potentials become tasks
-__device__ __forceinline__ void eval_pair(const ForceArgs<float> &a, const Replica<float> &R, const Model<float> &M,
-                                          const StageBuf &B, WarpScratch &W, int p, bool &big) {
-    const unsigned e = W.pair[p];
-    const int h = pair_h(e), kk = pair_k(e);
-    const int ki = W.h_k[h];
-    const float4 pi = B.pos[ki], pj = B.pos[kk];
-    float d[3] = {min_image<float>(pi.x - pj.x, R.box, R.l2s, R.periodic),
-                  min_image<float>(pi.y - pj.y, R.box, R.l2s, R.periodic),
-                  min_image<float>(pi.z - pj.z, R.box, R.l2s, R.periodic)};
+// separation x_home - x_neighbour of pair entry e (minimum image)
+__device__ __forceinline__ void pair_sep(const Replica<float> &R, const StageBuf &B, const WarpScratch &W, unsigned e,
+                                         float4 &pi, float4 &pj, float d[3]) {
+    pi = B.pos[W.h_k[pair_h(e)]];
+    pj = B.pos[pair_k(e)];
+    d[0] = min_image<float>(pi.x - pj.x, R.box, R.l2s, R.periodic);
+    d[1] = min_image<float>(pi.y - pj.y, R.box, R.l2s, R.periodic);
+    d[2] = min_image<float>(pi.z - pj.z, R.box, R.l2s, R.periodic);
+}
+
+// phase 2a body: WCA core of pair entry e, then the home particle's own cone test from data in shared
+// memory.  Its cosines are -(n . Qi (d / r)) in either order of the pair (the ones phase 2b tests up to
+// rounding, hence the 1e-5 margin), so a pair none of whose home patches is within the widest cone of
+// the home type has no patch potential.  Returns whether the pair goes on to phase 2b.
+__device__ __forceinline__ bool pair_core(const Replica<float> &R, const Model<float> &M, const StageBuf &B,
+                                          WarpScratch &W, unsigned e, bool &big) {
+    const int h = pair_h(e);
+    float4 pi, pj;
+    float d[3];
+    pair_sep(R, B, W, e, pi, pj, d);
     const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
     const float rr = sqrtf(r2);
-    unsigned long long *acc = W.acc[h];
     if (rr < R.hs_limit) {
         const float s_ = hs_force_over_r<float>(R, r2);
         big |= fabsf(s_ * rr) > 1e4f;
+        unsigned long long *acc = W.acc[h];
         acc_add(acc + 0, s_ * d[0]);
         acc_add(acc + 1, s_ * d[1]);
         acc_add(acc + 2, s_ * d[2]);
     }
-    if (!(r2 < R.patch_r2)) return;
-    const int cj = pair_cell(e);
+    if (!(r2 < R.patch_r2)) return false;
+    const int ti = M.n_types == 1 ? 0 : type_of<float>(M, W.h_id[h] - R.off);
+    const int nph = M.np[ti];
+    if (nph == 0) return false;
+    const float inv = 1.f / rr;
+    float Qi[9];
+    home_q(W, h, pi.w, Qi);
+    float w[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) w[k] = Qi[3 * k] * (d[0] * inv) + Qi[3 * k + 1] * (d[1] * inv) + Qi[3 * k + 2] * (d[2] * inv);
+    const float mca = M.mincos_any[ti] - 1e-5f;
+    const int oh = M.ooff[ti];
+    bool any = false;
+    for (int ia = 0; ia < nph; ia++) {
+        const float *v = M.orient[oh + ia];
+        any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > mca;
+    }
+    return any;
+}
+
+// phase 2b body: body-frame cone tests and Kern-Frenkel potentials of pair entry e.  The first
+// in-cone potential of the pair is evaluated after the cone loops, where the lanes of the warp that
+// have one meet again; a pair rarely has a second (then it is evaluated in the loop).
+__device__ __forceinline__ void pair_patches(const ForceArgs<float> &a, const Replica<float> &R, const Model<float> &M,
+                                             const StageBuf &B, WarpScratch &W, unsigned e) {
+    const int h = pair_h(e), kk = pair_k(e), cj = pair_cell(e);
+    float4 pi, pj;
+    float d[3];
+    pair_sep(R, B, W, e, pi, pj, d);
+    const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    const float rr = sqrtf(r2);
     const int j = B.cell_lo[cj] + (kk - B.cell_sm[cj]);
     const int idi = W.h_id[h];
     const int idj = __ldg(a.buf.ident + j);
+    float Qj[9];
+    load_q(a, j, pj.w, Qj);
     const bool single = M.n_types == 1;
     const int ti = single ? 0 : type_of<float>(M, idi - R.off);
     const int tj = single ? 0 : type_of<float>(M, idj - R.off);
-    if (M.np[ti] == 0 || M.np[tj] == 0) return;
+    if (M.np[tj] == 0) return;
     const bool i_first = idi < idj;
     const float sg = i_first ? 1.f : -1.f, inv = 1.f / rr;
     const float u[3] = {sg * d[0] * inv, sg * d[1] * inv, sg * d[2] * inv};
-    float Qi[9], Qj[9];
+    float Qi[9];
     home_q(W, h, pi.w, Qi);
-    load_q(a, j, pj.w, Qj);
     const float *Qa = i_first ? Qi : Qj, *Qb = i_first ? Qj : Qi;
     const int ta = i_first ? ti : tj, tb = i_first ? tj : ti;
     float wa[3], wb[3];
@@ -302,6 +333,8 @@ __device__ __forceinline__ void eval_pair(const ForceArgs<float> &a, const Repli
         if (cb > mc) maskb |= 1u << jb;
     }
     if (!maskb) return;
+    float f[3] = {0.f, 0.f, 0.f}, t[3] = {0.f, 0.f, 0.f};
+    int q1 = -1, ra = 0, rb = 0;
     for (int ia = 0; ia < na; ia++) {
         const float *v = M.orient[oa + ia];
         const float ca = -(v[0] * wa[0] + v[1] * wa[1] + v[2] * wa[2]);
@@ -312,32 +345,104 @@ __device__ __forceinline__ void eval_pair(const ForceArgs<float> &a, const Repli
             const float *w = M.orient[ob + jb];
             const float cb = w[0] * wb[0] + w[1] * wb[1] + w[2] * wb[2];
             if (!(ca > M.costm[q] && cb > M.costm[q]) || rr > M.rmax[q]) continue;
-            const int t = atomicAdd(&W.ntasks, 1);
-            if (t < kWarpTaskCap) W.task[t] = ((unsigned)p << 8) | (unsigned)q;
-            else eval_task(a, R, M, B, W, p, q);
+            if (q1 < 0) {
+                q1 = q;
+                ra = oa + ia;
+                rb = ob + jb;
+            } else {
+                kf2_potential(M, q, oa + ia, ob + jb, Qa, Qb, u, rr, i_first, f, t);
+            }
         }
+    }
+    if (q1 < 0) return;
+    kf2_potential(M, q1, ra, rb, Qa, Qb, u, rr, i_first, f, t);
+    unsigned long long *acc = W.acc[h];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        acc_add(acc + k, f[k]);
+        acc_add(acc + 3 + k, t[k]);
     }
 }
 
 // staged-cell wrap: the coordinates here are at most one cell outside [0, nc)
 __device__ __forceinline__ int wrap1(int v, int nc) { return v < 0 ? v + nc : (v >= nc ? v - nc : v); }
 
-// global cell of staged cell (sx_, sy, sz) of tile g, or -1 outside a walled box
-__device__ __forceinline__ int staged_cell(const TileGeom &g, const Replica<float> &R, int sx_, int sy, int sz) {
-    const int nc = R.nc;
-    int gx = g.whole ? sx_ : g.x0 - 1 + sx_;
-    int gy = g.y0 - 1 + sy, gz = g.z0 - 1 + sz;
-    if (R.periodic) {
-        gx = wrap1(gx, nc);
-        gy = wrap1(gy, nc);
-        gz = wrap1(gz, nc);
-    } else if (gx < 0 || gx >= nc || gy < 0 || gy >= nc || gz < 0 || gz >= nc) {
-        return -1;
+__device__ __forceinline__ int ld_volatile(const int *p) { return *(const volatile int *)p; }
+
+// x layout of a tile's staged rows, the same for every row: this lane's cell (c = lane) and its global
+// x, the unwrapped run [ru0, ru1) of consecutive global cells, and the wrapped cell wc (-1 if none)
+struct RowLayout {
+    int c, gx, ru0, ru1, wc, gx_end, gx_w;
+    bool in_row, xok;
+};
+__device__ __forceinline__ RowLayout row_layout(const TileGeom &g, int lane) {
+    RowLayout L;
+    const int nc = g.nc, sx = g.sx;
+    L.c = lane;
+    L.in_row = lane < sx;
+    L.gx = g.whole ? lane : g.x0 - 1 + lane;
+    L.xok = L.in_row;
+    if (L.gx < 0 || L.gx >= nc) {
+        if (g.periodic) L.gx = L.gx < 0 ? L.gx + nc : L.gx - nc;
+        else L.xok = false;
     }
-    return R.cell_off + gx + nc * (gy + nc * gz);
+    // a chunk that starts at x = 0 has its wrapped (or, walled, missing) cell first, one that ends at
+    // the box's far side last; a chunk is at most nc - 2 cells wide, so only one end can wrap
+    L.ru0 = 0;
+    L.ru1 = sx;
+    if (!g.whole) {
+        if (g.x0 == 0) L.ru0 = 1;
+        else if (g.x0 - 1 + sx > nc) L.ru1 = sx - 1;
+    }
+    L.wc = L.ru0 == 1 ? 0 : (L.ru1 < sx ? sx - 1 : -1);
+    L.gx_end = g.whole ? L.ru1 - 1 : g.x0 - 1 + (L.ru1 - 1);  // last cell of the run (inside the box)
+    L.gx_w = L.wc == 0 ? nc - 1 : 0;                          // the wrapped cell's global x
+    return L;
 }
 
-__device__ __forceinline__ int ld_volatile(const int *p) { return *(const volatile int *)p; }
+// global index of staged plane sz's first cell, or -1 outside a walled box
+__device__ __forceinline__ int plane_base(const TileGeom &g, int sz) {
+    int gz = g.z0 - 1 + sz;
+    if (gz < 0 || gz >= g.nc) {
+        if (!g.periodic) return -1;
+        gz = wrap1(gz, g.nc);
+    }
+    return g.cell_off + g.nc * g.nc * gz;
+}
+// global index of staged row sy's first cell (x = 0) in plane zb, or -1 outside a walled box
+__device__ __forceinline__ int row_base(const TileGeom &g, int zb, int sy) {
+    int gy = g.y0 - 1 + sy;
+    if (gy < 0 || gy >= g.nc) {
+        if (!g.periodic) return -1;
+        gy = wrap1(gy, g.nc);
+    }
+    return zb < 0 ? -1 : zb + g.nc * gy;
+}
+
+// Issue (cp.async, 4 B each) the copies of the start[] entries tile `desc` needs into P; the caller
+// commits them as one group.  Row r of P (stride sx + 2): start of each of its sx cells, then
+// start[last run cell + 1], then start[wrapped cell + 1].
+__device__ void prefetch_starts(const ForceArgs<float> &a, const int4 desc, int *P, int lane) {
+    const TileGeom g = decode_tile(desc);
+    if (g.simple) return;
+    const int sx = g.sx, nry = g.ty + 2, nrz = g.tz + 2, stride = sx + 2;
+    const RowLayout L = row_layout(g, lane);
+    const bool wrapped = L.wc >= 0 && g.periodic;
+    for (int sz = 0; sz < nrz; sz++) {
+        const int zb = plane_base(g, sz);
+#pragma unroll
+        for (int sy = 0; sy < kTileYZMax + 2; sy++) {
+            if (sy >= nry) break;
+            const int rowg = row_base(g, zb, sy);
+            if (rowg >= 0) {
+                int *Pr = P + (sz * nry + sy) * stride;
+                if (L.xok) cp_async4(Pr + L.c, a.start + rowg + L.gx);
+                if (lane == 0) cp_async4(Pr + sx, a.start + rowg + L.gx_end + 1);
+                if (lane == 1 && wrapped) cp_async4(Pr + sx + 1, a.start + rowg + L.gx_w + 1);
+            }
+        }
+    }
+}
 
 __device__ __forceinline__ int warp_inclusive_scan(int v, int lane) {
 #pragma unroll
@@ -357,13 +462,12 @@ __device__ __forceinline__ int warp_inclusive_scan(int v, int lane) {
 //      cells are consecutive in the sorted order) plus, for a chunk at the box edge, one wrapped
 //      cell; every lane issues its rows' bulk copies.  Copies are issued only when the whole tile
 //      fits, so the bytes the barrier expects are exactly the bytes copied.
-__device__ int produce_tile(const ForceArgs<float> &a, const int4 *tiles, int tile, StageBuf &B, int lane) {
-    const int4 desc = tiles[tile];
+__device__ int produce_tile(const ForceArgs<float> &a, const int4 desc, StageBuf &B, const int *P, int lane) {
     const TileGeom g = decode_tile(desc);
-    const Replica<float> &R = a.tb.reps[g.rep];
     int nhome = 0, mode = kStaged, total = 0;
     unsigned issued = 0;  // bytes of bulk copies this lane issued
     if (g.simple) {
+        const Replica<float> &R = a.tb.reps[g.rep];
         mode = kSlots;
         if (lane == 0) {
             B.seg_s0[0] = R.off;
@@ -373,34 +477,28 @@ __device__ int produce_tile(const ForceArgs<float> &a, const int4 *tiles, int ti
         }
         nhome = R.n;
     } else {
-        const int nc = R.nc, sx = g.sx;
+        const int nc = g.nc, sx = g.sx;
         const int nry = g.ty + 2, nrz = g.tz + 2, nrows = nry * nrz, ncell = nrows * sx;
-        const float inv_sx = 1.f / (float)sx;
-        // -- 1: counts and global starts
-        constexpr int kBatch = 8;
-        for (int i0 = 0; i0 < ncell; i0 += 32 * kBatch) {
-            int lo[kBatch], hi[kBatch];
+        // -- 1: counts and global starts of the staged cells from the prefetched start[] rows
+        const RowLayout L = row_layout(g, lane);
+        const int stride = sx + 2;
+        // the entry after this lane's start: the next cell's, the run's end or the wrapped cell's end
+        const int nxt_off = L.c == L.wc ? sx + 1 : (L.c == L.ru1 - 1 ? sx : L.c + 1);
+        if (L.in_row) {
+            for (int sz = 0; sz < nrz; sz++) {
+                const int zb = plane_base(g, sz);
 #pragma unroll
-            for (int q = 0; q < kBatch; q++) {
-                const int i = i0 + 32 * q + lane;
-                lo[q] = hi[q] = 0;
-                if (i < ncell) {
-                    // i / sx exactly: (i + 0.5) / sx is at least 0.5 / sx away from an integer
-                    const int r = __float2int_rz(((float)i + 0.5f) * inv_sx);
-                    const int c = i - r * sx;
-                    const int gc = staged_cell(g, R, c, r % nry, r / nry);
-                    if (gc >= 0) {
-                        lo[q] = __ldg(a.start + gc);
-                        hi[q] = __ldg(a.start + gc + 1);
+                for (int sy = 0; sy < kTileYZMax + 2; sy++) {
+                    if (sy >= nry) break;
+                    const int r = sz * nry + sy;
+                    int lo = 0, cnt = 0;
+                    if (L.xok && row_base(g, zb, sy) >= 0) {
+                        const int *Pr = P + r * stride;
+                        lo = Pr[L.c];
+                        cnt = Pr[nxt_off] - lo;
                     }
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < kBatch; q++) {
-                const int i = i0 + 32 * q + lane;
-                if (i < ncell) {
-                    B.cell_sm[i] = hi[q] - lo[q];
-                    B.cell_lo[i] = lo[q];
+                    B.cell_sm[r * sx + L.c] = cnt;
+                    B.cell_lo[r * sx + L.c] = lo;
                 }
             }
         }
@@ -423,14 +521,8 @@ __device__ int produce_tile(const ForceArgs<float> &a, const int4 *tiles, int ti
         const int hx0 = g.whole ? 0 : 1, hx1 = g.whole ? sx : sx - 1;
         const int nhrows = g.ty * g.tz;
         if (total <= kStageCap) {
-            // -- 3: copies, lanes over rows.  The unwrapped run is staged cells [ru0, ru1); a chunk that
-            // starts at x = 0 has its wrapped cell first, one that ends at the box's far side last.
-            int ru0 = 0, ru1 = sx;
-            if (!g.whole) {
-                if (g.x0 == 0) ru0 = 1;
-                else if (g.x0 - 1 + sx > nc) ru1 = sx - 1;
-            }
-            const int wc = ru0 == 1 ? 0 : (ru1 < sx ? sx - 1 : -1);
+            // -- 3: copies, lanes over rows: the unwrapped run [ru0, ru1) and the wrapped cell wc
+            const int ru0 = L.ru0, ru1 = L.ru1, wc = L.wc;
             bool fenced = false;
             for (int r = lane; r < nrows; r += 32) {
                 const int rb = r * sx;
@@ -468,7 +560,7 @@ __device__ int produce_tile(const ForceArgs<float> &a, const int4 *tiles, int ti
             if (lane < nhrows) {
                 const int ry = 1 + lane % g.ty, rz = 1 + lane / g.ty;
                 const int gy = g.y0 - 1 + ry, gz = g.z0 - 1 + rz;  // home rows are inside the box
-                const int c0 = R.cell_off + (g.whole ? 0 : g.x0) + nc * (gy + nc * gz);
+                const int c0 = g.cell_off + (g.whole ? 0 : g.x0) + nc * (gy + nc * gz);
                 const int c1 = c0 + (hx1 - hx0) - 1;
                 s0 = __ldg(a.start + c0);
                 n = __ldg(a.start + c1 + 1) - s0;
@@ -531,7 +623,6 @@ __device__ void consume_staged_unit(const ForceArgs<float> &a, const StageBuf &B
     }
 #pragma unroll
     for (int k = 0; k < 6; k++) W.acc[lane][k] = 0ull;
-    if (lane == 0) W.ntasks = 0;
     __syncwarp();
 
     // -- phase 1: candidate scan in shared memory.  A neighbour cell reached across a periodic face
@@ -611,14 +702,30 @@ __device__ void consume_staged_unit(const ForceArgs<float> &a, const StageBuf &B
         __syncwarp();
         return;
     }
-    // -- phase 2: the warp's pairs spread over its lanes
-    for (int p = lane; p < npairs; p += 32) eval_pair(a, R, M, B, W, p, big);
+    // -- phase 2a: the warp's pairs spread over its lanes: WCA core and the home cone test.  Pairs that
+    // may have a patch potential are compacted in place (an entry is written only after every lane of
+    // its round has read its own), so phase 2b runs its global loads on dense rounds.
+    int ncand = 0;  // warp-uniform
+    {
+        const unsigned lt_mask = (1u << lane) - 1u;
+        for (int p0 = 0; p0 < npairs; p0 += 32) {
+            const int p = p0 + lane;
+            unsigned e = 0;
+            bool keep = false;
+            if (p < npairs) {
+                e = W.pair[p];
+                keep = pair_core(R, M, B, W, e, big);
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            if (keep) W.pair[ncand + __popc(m & lt_mask)] = e;
+            ncand += __popc(m);
+        }
+    }
     __syncwarp();
-    // -- phase 3: in-cone patch potentials spread over the lanes
-    const int ntasks = min(W.ntasks, kWarpTaskCap);
-    for (int t = lane; t < ntasks; t += 32) eval_task(a, R, M, B, W, (int)(W.task[t] >> 8), (int)(W.task[t] & 255u));
+    // -- phase 2b: cone tests and Kern-Frenkel potentials of the remaining pairs
+    for (int p = lane; p < ncand; p += 32) pair_patches(a, R, M, B, W, W.pair[p]);
     __syncwarp();
-    // -- phase 4: epilogue per home particle
+    // -- phase 3: epilogue per home particle
     if (active) {
         const int s = W.h_slot[lane];
         const float F[3] = {acc_get(W.acc[lane][0]), acc_get(W.acc[lane][1]), acc_get(W.acc[lane][2])};
@@ -632,7 +739,7 @@ __device__ void consume_staged_unit(const ForceArgs<float> &a, const StageBuf &B
         } else {
             const float4 pi = B.pos[myk];
             float Qi[9];
-            load_q(a, s, pi.w, Qi);
+            home_q(W, lane, pi.w, Qi);
             langevin_epilogue(a, R, g.rep, s, W.h_id[lane], F, T, Qi, pi.x, pi.y, pi.z);
         }
     }
@@ -665,10 +772,22 @@ __global__ void __launch_bounds__(kTileThreads, 1) tile_force_kernel(ForceArgs<f
 
     if (warp == kTileWarps - 1) {
         // ---------------- producer
+        // the start[] entries of tile k are copied (cp.async) during tile k - 1, its descriptor is
+        // loaded during tile k - 2
         int cum = 0;
+        const int G = (int)gridDim.x;
+        int4 cur = (int)blockIdx.x < ntiles ? tiles[blockIdx.x] : make_int4(0, 0, 0, 0);
+        int4 nxt = (int)blockIdx.x + G < ntiles ? tiles[blockIdx.x + G] : make_int4(0, 0, 0, 0);
+        if ((int)blockIdx.x < ntiles) prefetch_starts(a, cur, sh.start_rows[0], lane);
+        cp_async_commit();
         for (int k = 0;; k++) {
-            const int tile = blockIdx.x + k * gridDim.x;
+            const int tile = blockIdx.x + k * G;
             if (tile >= ntiles) break;
+            const int4 desc = cur;
+            if (tile + G < ntiles) prefetch_starts(a, nxt, sh.start_rows[(k + 1) & 1], lane);
+            cp_async_commit();
+            cur = nxt;
+            if (tile + 2 * G < ntiles) nxt = tiles[tile + 2 * G];
             StageBuf &B = sh.buf[k % kStageBufs];
             if (k >= kStageBufs) {
                 // the previous use's copies have landed (also when no consumer waited on them) ...
@@ -692,7 +811,9 @@ __global__ void __launch_bounds__(kTileThreads, 1) tile_force_kernel(ForceArgs<f
                 }
                 __threadfence_block();
             }
-            const int units = produce_tile(a, tiles, tile, B, lane);
+            cp_async_wait_prev();  // this tile's start[] entries have landed (this lane's copies) ...
+            __syncwarp();          // ... and every lane's
+            const int units = produce_tile(a, desc, B, sh.start_rows[k & 1], lane);
             if (lane == 0) {
                 B.done = 0;
                 B.nunits = units;
@@ -705,6 +826,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) tile_force_kernel(ForceArgs<f
             __syncwarp();
         }
         if (lane == 0) *(volatile int *)&sh.final_units = cum;
+        cp_async_wait_all();
         // drain: the last use of every buffer has completed (its copies landed) before this CTA exits
         const int nk = (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
         for (int b = 0; b < kStageBufs && b < nk; b++) {
