@@ -670,26 +670,32 @@ __device__ void consume_staged_unit(const ForceArgs<float> &a, const StageBuf &B
                     }
                 }
                 const int maxlen = __reduce_max_sync(0xffffffffu, len);
-                for (int t = 0; t < maxlen; t++) {
-                    bool hit = false;
-                    int kk = 0, cell = 0;
-                    if (t < len) {
-                        const bool sega = t < lena;
-                        kk = sega ? ka + t : kb + (t - lena);
-                        cell = sega ? rowb + c0 + (kk >= b1) + (kk >= b2) : rowb + cw;
-                        const float shx = sega ? 0.f : shw;
-                        const float4 pj = B.pos[kk];
-                        const float ddx = (pi.x - pj.x) - shx;
-                        const float ddy = (pi.y - pj.y) - shy;
-                        const float ddz = (pi.z - pj.z) - shz;
-                        hit = kk != myk && ddx * ddx + ddy * ddy + ddz * ddz < R.rc2;
+                // four candidates per lane per round: their loads are issued together
+                for (int t0 = 0; t0 < maxlen; t0 += 4) {
+                    float4 pj[4];
+                    int kq[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int t = t0 + u;
+                        kq[u] = t < lena ? ka + t : kb + (t - lena);
+                        pj[u] = B.pos[t < len ? kq[u] : myk];
                     }
-                    const unsigned m = __ballot_sync(0xffffffffu, hit);
-                    if (hit) {
-                        const int p = npairs + __popc(m & lt_mask);
-                        if (p < kWarpPairCap) W.pair[p] = pair_entry(kk, cell, lane);
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int t = t0 + u;
+                        const float shx = t < lena ? 0.f : shw;
+                        const float ddx = (pi.x - pj[u].x) - shx;
+                        const float ddy = (pi.y - pj[u].y) - shy;
+                        const float ddz = (pi.z - pj[u].z) - shz;
+                        const bool hit = t < len && kq[u] != myk && ddx * ddx + ddy * ddy + ddz * ddz < R.rc2;
+                        const unsigned m = __ballot_sync(0xffffffffu, hit);
+                        if (hit) {
+                            const int p = npairs + __popc(m & lt_mask);
+                            const int cell = t < lena ? rowb + c0 + (kq[u] >= b1) + (kq[u] >= b2) : rowb + cw;
+                            if (p < kWarpPairCap) W.pair[p] = pair_entry(kq[u], cell, lane);
+                        }
+                        npairs += __popc(m);
                     }
-                    npairs += __popc(m);
                 }
             }
         }
