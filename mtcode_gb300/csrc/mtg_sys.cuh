@@ -269,7 +269,9 @@ struct Sys : SysBase {
         }
         MTG_CUDA(cudaMalloc(&d_bin, sizeof(int2) * n));
         MTG_CUDA(cudaMalloc(&d_count, sizeof(int) * (ncells_alloc + 1)));
-        MTG_CUDA(cudaMalloc(&d_start, sizeof(int) * (ncells_alloc + 1)));
+        // + 8: the tile kernel copies cell starts in aligned 16-byte chunks, up to 3 entries past the end
+        MTG_CUDA(cudaMalloc(&d_start, sizeof(int) * (ncells_alloc + 8)));
+        MTG_CUDA(cudaMemset(d_start, 0, sizeof(int) * (ncells_alloc + 8)));
         int nblk = (ncells_alloc + mtg::kScanTile - 1) / mtg::kScanTile + 1;
         MTG_CUDA(cudaMalloc(&d_block, sizeof(int) * nblk));
         MTG_CUDA(cudaMalloc(&d_flags, sizeof(unsigned)));

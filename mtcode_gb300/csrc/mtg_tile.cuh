@@ -27,7 +27,8 @@ constexpr int kTileYZMax = 4;
 constexpr int kTileXMax = 32;
 constexpr int kStageRows = (kTileYZMax + 2) * (kTileYZMax + 2);                   // 36
 constexpr int kStageCells = (kTileXMax + 2) * kStageRows;                           // 1224
-constexpr int kStartRowsCap = (kTileXMax + 2) * kStageRows;  // prefetched start[] entries of a tile
+constexpr int kStartRowInts = 48;  // prefetched start[] entries of one staged row: run 40 + wrapped cell 8
+constexpr int kStartRunInts = 40;
 constexpr int kStageCap = 2048;    // staged particles per buffer
 constexpr int kWarpPairCap = 640;  // in-range pairs per 32 home particles
 constexpr unsigned kWaitSpins = 1u << 20;
@@ -76,9 +77,9 @@ struct WarpScratch {
 struct TileShared {
     StageBuf buf[kStageBufs];
     WarpScratch w[kConsumerWarps];
-    // start[] entries of the next tiles, copied ahead by the producer (cp.async): per staged row the
-    // starts of its sx cells, then the end of its unwrapped run, then the end of its wrapped cell
-    int start_rows[2][kStartRowsCap];
+    // start[] entries of the next tiles, copied ahead by the producer (cp.async, 16-byte chunks): per
+    // staged row the aligned chunks holding its run's starts and end, then those of its wrapped cell
+    __align__(16) int start_rows[2][kStageRows * kStartRowInts];
     int claim;                       // next unit of the CTA-wide stream
     int final_units;                 // -1 until the producer has published its last tile
     int overflow;
@@ -114,8 +115,8 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsign
         : "memory");
 }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
@@ -419,27 +420,40 @@ __device__ __forceinline__ int row_base(const TileGeom &g, int zb, int sy) {
     return zb < 0 ? -1 : zb + g.nc * gy;
 }
 
-// Issue (cp.async, 4 B each) the copies of the start[] entries tile `desc` needs into P; the caller
-// commits them as one group.  Row r of P (stride sx + 2): start of each of its sx cells, then
-// start[last run cell + 1], then start[wrapped cell + 1].
+// staged row r of a tile with nry rows per plane: (sy, sz) without a divide (r < 36, nry <= 6: the
+// quotient (r + 0.5) / nry is at least 1 / 12 away from an integer)
+__device__ __forceinline__ void row_yz(int r, int nry, float inv_nry, int &sy, int &sz) {
+    sz = __float2int_rz(((float)r + 0.5f) * inv_nry);
+    sy = r - sz * nry;
+}
+
+// Issue the copies of the start[] entries tile `desc` needs into P (cp.async, aligned 16-byte chunks,
+// lanes over rows); the caller commits them as one group.  Row r of P (kStartRowInts entries): from
+// entry 0 the chunks holding start[first run cell .. last run cell + 1] (the first at entry
+// first & 3), from entry kStartRunInts the chunks holding start[wrapped cell], start[wrapped cell + 1]
+// (the first at entry kStartRunInts + (wrapped cell & 3)).
 __device__ void prefetch_starts(const ForceArgs<float> &a, const int4 desc, int *P, int lane) {
     const TileGeom g = decode_tile(desc);
     if (g.simple) return;
-    const int sx = g.sx, nry = g.ty + 2, nrz = g.tz + 2, stride = sx + 2;
-    const RowLayout L = row_layout(g, lane);
+    const int nry = g.ty + 2, nrows = nry * (g.tz + 2);
+    const float inv_nry = 1.f / (float)nry;
+    const RowLayout L = row_layout(g, lane);  // the lane-independent parts (runs) are what is used here
+    const int run_x0 = g.whole ? L.ru0 : g.x0 - 1 + L.ru0;
+    const int nrun = L.ru1 - L.ru0;
     const bool wrapped = L.wc >= 0 && g.periodic;
-    for (int sz = 0; sz < nrz; sz++) {
-        const int zb = plane_base(g, sz);
-#pragma unroll
-        for (int sy = 0; sy < kTileYZMax + 2; sy++) {
-            if (sy >= nry) break;
-            const int rowg = row_base(g, zb, sy);
-            if (rowg >= 0) {
-                int *Pr = P + (sz * nry + sy) * stride;
-                if (L.xok) cp_async4(Pr + L.c, a.start + rowg + L.gx);
-                if (lane == 0) cp_async4(Pr + sx, a.start + rowg + L.gx_end + 1);
-                if (lane == 1 && wrapped) cp_async4(Pr + sx + 1, a.start + rowg + L.gx_w + 1);
-            }
+    for (int r = lane; r < nrows; r += 32) {
+        int sy, sz;
+        row_yz(r, nry, inv_nry, sy, sz);
+        const int rowg = row_base(g, plane_base(g, sz), sy);
+        if (rowg < 0) continue;
+        int *Pr = P + r * kStartRowInts;
+        const int f = rowg + run_x0;
+        const int c0 = f & ~3, c1 = (f + nrun + 1 + 3) & ~3;  // at most 10 chunks
+        for (int c = c0; c < c1; c += 4) cp_async16(Pr + (c - c0), a.start + c);
+        if (wrapped) {
+            const int gw = rowg + L.gx_w;
+            const int w0 = gw & ~3, w1 = (gw + 2 + 3) & ~3;  // at most 2 chunks
+            for (int c = w0; c < w1; c += 4) cp_async16(Pr + kStartRunInts + (c - w0), a.start + c);
         }
     }
 }
@@ -481,9 +495,7 @@ __device__ int produce_tile(const ForceArgs<float> &a, const int4 desc, StageBuf
         const int nry = g.ty + 2, nrz = g.tz + 2, nrows = nry * nrz, ncell = nrows * sx;
         // -- 1: counts and global starts of the staged cells from the prefetched start[] rows
         const RowLayout L = row_layout(g, lane);
-        const int stride = sx + 2;
-        // the entry after this lane's start: the next cell's, the run's end or the wrapped cell's end
-        const int nxt_off = L.c == L.wc ? sx + 1 : (L.c == L.ru1 - 1 ? sx : L.c + 1);
+        const int run_x0 = g.whole ? L.ru0 : g.x0 - 1 + L.ru0;
         if (L.in_row) {
             for (int sz = 0; sz < nrz; sz++) {
                 const int zb = plane_base(g, sz);
@@ -492,10 +504,13 @@ __device__ int produce_tile(const ForceArgs<float> &a, const int4 desc, StageBuf
                     if (sy >= nry) break;
                     const int r = sz * nry + sy;
                     int lo = 0, cnt = 0;
-                    if (L.xok && row_base(g, zb, sy) >= 0) {
-                        const int *Pr = P + r * stride;
-                        lo = Pr[L.c];
-                        cnt = Pr[nxt_off] - lo;
+                    const int rowg = row_base(g, zb, sy);
+                    if (L.xok && rowg >= 0) {
+                        const int *Pr = P + r * kStartRowInts;
+                        const int e = L.c == L.wc ? kStartRunInts + ((rowg + L.gx_w) & 3)
+                                                  : ((rowg + run_x0) & 3) + (L.c - L.ru0);
+                        lo = Pr[e];
+                        cnt = Pr[e + 1] - lo;
                     }
                     B.cell_sm[r * sx + L.c] = cnt;
                     B.cell_lo[r * sx + L.c] = lo;
