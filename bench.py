@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 patchy-Langevin step: particle-steps/s on the batched-replica workload.
 
-Workload (default): 512 independent replicas, N_r log-uniform in [1,024, 32,768] (about 4.7 M particles),
+Workload (default): 512 independent replicas, N_r log-uniform in [1,024, 32,768] (5,158,422 particles with seed 0),
 4 tetrahedral patches, phi 0.15, kT_r ~ U[0.8, 1.2], depth_r ~ U[6, 10], range 1.2, cos 0.90, dt 0.005,
 FP32 state with FP64 reductions, cell list rebuilt every step, one CUDA-graph launch per step.
 
