@@ -144,6 +144,14 @@ mtg_status mtg_step_noise(mtg_system *h, int nsteps, const double *noise);
  * energy (nullable): per-particle potential energy, half of every pair energy (WCA + KF2). */
 mtg_status mtg_forces(mtg_system *h, double *F, double *T, double *energy);
 
+/* Fixed bonds with HarmonicPotential(k, r0) (MDBase/Potentials/potential.h:265-297): from now on every
+ * force pass adds MD::calculateforces(bonds, pot) (MD.cpp:1684-1764), f = -k (r - r0) along the
+ * minimum-image separation, to the central forces -- the bonded term of the polymer drivers
+ * (mainActivePolymer.cpp:390-402).  bonds: nbonds x 2 host-order (global) particle indices, both ends
+ * in one replica; nbonds = 0 removes them.  mtg_forces' energy then includes 0.5 k (r - r0)^2 per bond
+ * (half to each end); mtg_observables does not.  Call mtg_init_forces after changing bonds mid-run. */
+mtg_status mtg_set_bonds(mtg_system *h, const int32_t *bonds, int64_t nbonds, double k, double r0);
+
 /* MD::calculatepairs_parallel(boxlist, rc) (MD.cpp:1100-1176) for one replica: every pair (i < j,
  * local indices) with minimum-image distance < rc, sorted by (i, j).  The cell grid is rebuilt at
  * side >= rc for this call.  If *npairs > cap on return, nothing beyond cap was written and the call
@@ -218,6 +226,11 @@ mtg_status mtg_pairs_noalloc(const double *x_dev, int n, double box, int periodi
  * mtg_random_rotations: uniform random rotations, the construction of LangevinR.cpp:239-267. */
 mtg_status mtg_random_positions(int n, double box, int periodic, double min_dist, uint64_t seed, double *x);
 void mtg_random_rotations(int n, uint64_t seed, double *Q);
+/* mtg_random_chains: n_chains self-avoiding random-walk chains of `beads` beads (bond length step,
+ * every bead at least min_dist from all others, minimum image), chain c's bead b at row c*beads + b of
+ * x: the random-walk start of the bonded-polymer workloads.  MTG_ERR_ARG if a chain cannot be placed. */
+mtg_status mtg_random_chains(int n_chains, int beads, double box, int periodic, double step, double min_dist,
+                             uint64_t seed, double *x);
 
 #ifdef __cplusplus
 }

@@ -92,6 +92,7 @@ SIGNATURES = [
     ("mtg_step", C.c_int, [_H, C.c_int]),
     ("mtg_step_noise", C.c_int, [_H, C.c_int, _D]),
     ("mtg_forces", C.c_int, [_H, _D, _D, _D]),
+    ("mtg_set_bonds", C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_int64, C.c_double, C.c_double]),
     ("mtg_pairs", C.c_int, [_H, C.c_int, C.c_double, _I32, C.c_int64, C.POINTER(C.c_int64)]),
     ("mtg_temperature", C.c_int, [_H, _D]),
     ("mtg_observables", C.c_int, [_H, _D]),
@@ -110,6 +111,7 @@ SIGNATURES = [
                                      C.c_void_p, C.c_void_p]),
     ("mtg_random_positions", C.c_int, [C.c_int, C.c_double, C.c_int, C.c_double, C.c_uint64, _D]),
     ("mtg_random_rotations", None, [C.c_int, C.c_uint64, _D]),
+    ("mtg_random_chains", C.c_int, [C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double, C.c_uint64, _D]),
 ]
 
 _lib = None

@@ -61,7 +61,9 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         obj = BUILD / (src + ".o")
         objs.append(obj)
         if force or _stale(obj, [CSRC / src] + headers):
-            jobs.append([nvcc(), *NVCC_FLAGS, "-x", "c++", "-c", str(CSRC / src), "-o", str(obj)])
+            # no FMA contraction: seeded host inputs come out bit-identical on every host architecture
+            jobs.append([nvcc(), *NVCC_FLAGS, "-Xcompiler", "-ffp-contract=off", "-x", "c++", "-c", str(CSRC / src),
+                         "-o", str(obj)])
     if jobs:
         with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
             for _ in ex.map(_run, jobs):

@@ -201,6 +201,11 @@ mtg_status mtg_init_forces_noise(mtg_system *h, const double *noise) {
     return MTG_OK;
 }
 
+mtg_status mtg_set_bonds(mtg_system *h, const int32_t *bonds, int64_t nbonds, double k, double r0) {
+    MTG_GUARD(h, h->impl->set_bonds(bonds, nbonds, k, r0));
+    return MTG_OK;
+}
+
 mtg_status mtg_step_profile(mtg_system *h, int nsteps, double *kernel_ms) {
     MTG_GUARD(h, h->impl->step_profile(nsteps, kernel_ms));
     return MTG_OK;

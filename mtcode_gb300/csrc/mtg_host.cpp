@@ -1,6 +1,7 @@
 // mtg_host.cpp -- host-side seeded synthetic inputs for the C ABI (no GPU use).
 #include <cmath>
 #include <cstdint>
+#include <climits>
 #include <vector>
 
 #include "../../include/mtcode_gb300.h"
@@ -68,6 +69,109 @@ mtg_status mtg_random_positions(int n, double box, int periodic, double min_dist
         next[placed] = head[cell];
         head[cell] = placed;
         placed++;
+    }
+    return MTG_OK;
+}
+
+// Self-avoiding random-walk chains: chain c's bead b goes to row c * beads + b.  The first bead of a chain
+// is uniform in the box; each next one is `step` away from its predecessor along a direction drawn
+// uniformly on the sphere (rejection from the cube, no trig, so the same bits on every host).  Every
+// bead keeps min_dist from all earlier beads (minimum image); walls reject, periodic faces wrap.  A
+// chain that gets stuck is removed and restarted.
+mtg_status mtg_random_chains(int n_chains, int beads, double box, int periodic, double step, double min_dist,
+                             uint64_t seed, double *x) {
+    if (n_chains < 0 || beads < 1 || box <= 0 || step <= 0 || min_dist < 0 || min_dist >= step || !x)
+        return MTG_ERR_ARG;
+    const int64_t n = (int64_t)n_chains * beads;
+    if (n > INT32_MAX) return MTG_ERR_ARG;
+    SplitMix rng{seed ^ 0x2545F4914F6CDD1Dull};
+    int nc = min_dist > 0 ? (int)std::floor(box / min_dist) : 1;
+    if (nc < 1) nc = 1;
+    if (nc > 1024) nc = 1024;
+    const double scale = nc / box;
+    std::vector<int> head((size_t)nc * nc * nc, -1), next((size_t)(n > 0 ? n : 1), -1), cell_of((size_t)(n > 0 ? n : 1));
+    const double md2 = min_dist * min_dist;
+    auto cell_index = [&](const double c[3]) {
+        int ci[3];
+        for (int k = 0; k < 3; k++) {
+            ci[k] = (int)(c[k] * scale);
+            if (ci[k] >= nc) ci[k] = nc - 1;
+            if (ci[k] < 0) ci[k] = 0;
+        }
+        return ci[0] + nc * (ci[1] + nc * ci[2]);
+    };
+    auto is_free = [&](const double c[3]) {
+        const int cc = cell_index(c);
+        const int ci[3] = {cc % nc, (cc / nc) % nc, cc / (nc * nc)};
+        const int lo = nc >= 3 ? -1 : 0, hi = nc >= 2 ? 1 : 0;
+        for (int dz = lo; dz <= hi; dz++)
+            for (int dy = lo; dy <= hi; dy++)
+                for (int dx = lo; dx <= hi; dx++) {
+                    int a = ci[0] + dx, b = ci[1] + dy, e = ci[2] + dz;
+                    if (!periodic && (a < 0 || a >= nc || b < 0 || b >= nc || e < 0 || e >= nc)) continue;
+                    a = (a + nc) % nc; b = (b + nc) % nc; e = (e + nc) % nc;
+                    for (int j = head[(size_t)a + nc * ((size_t)b + (size_t)nc * e)]; j >= 0; j = next[j]) {
+                        double d2 = 0;
+                        for (int k = 0; k < 3; k++) {
+                            double d = c[k] - x[3 * (size_t)j + k];
+                            if (periodic) d -= box * std::nearbyint(d / box);
+                            d2 += d * d;
+                        }
+                        if (d2 < md2) return false;
+                    }
+                }
+        return true;
+    };
+    auto place = [&](int i, const double c[3]) {
+        for (int k = 0; k < 3; k++) x[3 * (size_t)i + k] = c[k];
+        const int cc = cell_index(c);
+        cell_of[i] = cc;
+        next[i] = head[cc];
+        head[cc] = i;
+    };
+    for (int ch = 0; ch < n_chains; ch++) {
+        const int i0 = ch * beads;
+        bool done = false;
+        for (int restart = 0; restart < 1000 && !done; restart++) {
+            int placed = 0;
+            for (int tries = 0; tries < 10000 && placed == 0; tries++) {
+                double c[3] = {rng.uniform() * box, rng.uniform() * box, rng.uniform() * box};
+                if (is_free(c)) { place(i0, c); placed = 1; }
+            }
+            if (!placed) return MTG_ERR_ARG;
+            while (placed < beads) {
+                bool ok = false;
+                for (int tries = 0; tries < 200 && !ok; tries++) {
+                    double v[3], r2 = 0;
+                    do {
+                        r2 = 0;
+                        for (int k = 0; k < 3; k++) { v[k] = 2.0 * rng.uniform() - 1.0; r2 += v[k] * v[k]; }
+                    } while (r2 > 1.0 || r2 < 1e-6);
+                    const double inv = step / std::sqrt(r2);
+                    double c[3];
+                    bool inside = true;
+                    for (int k = 0; k < 3; k++) {
+                        c[k] = x[3 * (size_t)(i0 + placed - 1) + k] + v[k] * inv;
+                        if (periodic) {
+                            if (c[k] < 0) c[k] += box;
+                            else if (c[k] >= box) c[k] -= box;
+                        } else if (c[k] < 0 || c[k] >= box) {
+                            inside = false;
+                        }
+                    }
+                    if (inside && is_free(c)) { place(i0 + placed, c); ok = true; }
+                }
+                if (!ok) break;
+                placed++;
+            }
+            if (placed == beads) {
+                done = true;
+            } else {
+                // stuck: unlink this chain's beads (the most recent insertions head their cells)
+                for (int i = i0 + placed - 1; i >= i0; i--) head[cell_of[i]] = next[i];
+            }
+        }
+        if (!done) return MTG_ERR_ARG;
     }
     return MTG_OK;
 }

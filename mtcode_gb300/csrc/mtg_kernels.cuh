@@ -25,6 +25,8 @@ struct Buffers {
     real *motion;
     int *ident;
     double *dx, *dy, *dz;  // unwrapped displacement (nullable)
+    int *slot_of;          // global index -> slot of the buffer in use (shared by both buffers; nullable,
+                           // kept only when bonds are set)
 };
 
 template <class real>
@@ -302,6 +304,7 @@ __global__ void __launch_bounds__(256) scatter_kernel(Tables<real> tb, Buffers<r
         P.store(out.pos, out.rota, out.rotb, d);
         M.store(out.motion + (size_t)d * kRow);
         out.ident[d] = id;
+        if (out.slot_of) out.slot_of[id] = d;
     }
 }
 
@@ -320,7 +323,37 @@ struct ForceArgs {
     double *outF, *outT, *outE;      // mode forces: by global index
     double *obs;                     // mode obs: n_rep x 5
     int do_kick;                     // second half-kick (step) or not (init)
+    // fixed bonds, by global index (CSR: partners of i are bond_partner[bond_start[i] .. bond_start[i+1]));
+    // null when the system has none.  HarmonicPotential(bond_k, bond_r0).
+    const int *bond_start, *bond_partner;
+    real bond_k, bond_r0;
 };
+
+// Harmonic bonds of particle idi at (xi, yi, zi): HarmonicPotential::force (potential.h:274-276),
+// f = -k (r - r0), along the minimum-image separation, as MD::calculateforces applies it to a bond list
+// (MD.cpp:1684-1764).  Each bond is evaluated from both of its ends: x_j - x_i is exactly -(x_i - x_j),
+// so the two forces are equal and opposite bit for bit and nothing is scattered.  Adds the force on idi
+// to f, half of each bond's energy 0.5 k (r - r0)^2 to e.
+template <class real>
+__device__ __forceinline__ void bond_forces(const ForceArgs<real> &a, const Replica<real> &R, int idi, real xi, real yi,
+                                            real zi, real f[3], real &e, bool &big) {
+    const int b0 = __ldg(a.bond_start + idi), b1 = __ldg(a.bond_start + idi + 1);
+    for (int b = b0; b < b1; b++) {
+        const int j = __ldg(a.buf.slot_of + __ldg(a.bond_partner + b));
+        real xj, yj, zj;
+        load_pos(a.buf.pos + 4 * (size_t)j, xj, yj, zj);
+        const real dx = min_image<real>(xi - xj, R.box, R.l2s, R.periodic);
+        const real dy = min_image<real>(yi - yj, R.box, R.l2s, R.periodic);
+        const real dz = min_image<real>(zi - zj, R.box, R.l2s, R.periodic);
+        const real r = sqrt(dx * dx + dy * dy + dz * dz);
+        const real f1 = -a.bond_k * (r - a.bond_r0);
+        big |= fabs(f1) > real(1e4);
+        f[0] += f1 * dx / r;
+        f[1] += f1 * dy / r;
+        f[2] += f1 * dz / r;
+        e += real(0.25) * a.bond_k * (r - a.bond_r0) * (r - a.bond_r0);
+    }
+}
 
 // One particle by one thread: the straightforward form of the force loop.  Used by the FP64 path,
 // the observable pass, replicas with fewer than three cells per side, and the FP32 tile kernel's
@@ -454,6 +487,12 @@ __device__ __noinline__ void simple_particle(const ForceArgs<real> &a, int s) {
                 }
             }
         }
+        real ebond = real(0);
+        if (a.bond_start && MODE != kModeObs) {
+            real fb[3] = {real(0), real(0), real(0)};
+            bond_forces<real>(a, R, idi, xi, yi, zi, fb, ebond, big);
+            F.add(fb[0], fb[1], fb[2]);
+        }
         if (big) atomicOr(a.flags, 2u);
 
         if (MODE == kModeForces) {
@@ -463,7 +502,7 @@ __device__ __noinline__ void simple_particle(const ForceArgs<real> &a, int s) {
             a.outT[3 * (size_t)idi + 0] = T.get(0);
             a.outT[3 * (size_t)idi + 1] = T.get(1);
             a.outT[3 * (size_t)idi + 2] = T.get(2);
-            if (a.outE) a.outE[idi] = (double)ewca + (double)epatch;
+            if (a.outE) a.outE[idi] = (double)ewca + (double)epatch + (double)ebond;
             return;
         }
         if (MODE == kModeObs) {
@@ -557,8 +596,14 @@ __global__ void load_state_kernel(int ntot, const double *x, const double *p, co
         P.store(out.pos, out.rota, out.rotb, i);
         M.store(out.motion + (size_t)i * kRow);
         out.ident[i] = i;
+        if (out.slot_of) out.slot_of[i] = i;
         if (out.dx) { out.dx[i] = 0; out.dy[i] = 0; out.dz[i] = 0; }
     }
+}
+
+// id -> slot map of a buffer (when bonds are set on a system that already holds a state)
+__global__ void slot_map_kernel(int ntot, const int *ident, int *slot_of) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ntot; s += gridDim.x * blockDim.x) slot_of[ident[s]] = s;
 }
 
 // slot order -> host order doubles; which: bit0 x, bit1 p, bit2 Lb, bit3 Q, bit4 Ft, bit5 Tt, bit6 disp

@@ -207,6 +207,10 @@ struct Sys : SysBase {
     uint64_t draw = 0;
     bool have_state = false, cells_valid = false, bins_valid = false, forces_ready = false;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    // fixed bonds (CSR by global index) and the id -> slot map the bond pass needs
+    int *d_bond_start = nullptr, *d_bond_partner = nullptr, *d_slot_of = nullptr;
+    int64_t nbonds = 0;
+    double bond_k = 0, bond_r0 = 0;
     int64_t nlaunch = 0;
     // FP32 tile kernel
     bool use_tiles = false;
@@ -323,6 +327,7 @@ struct Sys : SysBase {
         cudaFree(d_bin); cudaFree(d_count); cudaFree(d_start); cudaFree(d_block);
         cudaFree(d_flags); cudaFree(d_draw); cudaFree(d_stage); cudaFree(d_noise); cudaFree(d_obs);
         cudaFree(d_tiles);
+        cudaFree(d_bond_start); cudaFree(d_bond_partner); cudaFree(d_slot_of);
         if (h_flags) cudaFreeHost(h_flags);
         if (st) cudaStreamDestroy(st);
     }
@@ -382,6 +387,12 @@ struct Sys : SysBase {
         a.flags = d_flags;
         a.draw = d_draw;
         a.do_kick = do_kick;
+        if (nbonds > 0) {
+            a.bond_start = d_bond_start;
+            a.bond_partner = d_bond_partner;
+            a.bond_k = (real)bond_k;
+            a.bond_r0 = (real)bond_r0;
+        }
         return a;
     }
 
@@ -501,6 +512,62 @@ struct Sys : SysBase {
         MTG_CUDA(cudaStreamEndCapture(st, &g));
         MTG_CUDA(cudaGraphInstantiate(&graph[b], g, 0));
         MTG_CUDA(cudaGraphDestroy(g));
+    }
+
+    // MD::calculateforces(bond list, HarmonicPotential(k, r0)) added to every force pass from now on
+    void set_bonds(const int32_t *bonds, int64_t nb, double k, double r0) override {
+        MTG_REQUIRE(nb >= 0 && (nb == 0 || bonds), "mtg_set_bonds: nbonds must be >= 0 and bonds non-null");
+        MTG_REQUIRE(std::isfinite(k) && std::isfinite(r0) && r0 >= 0, "mtg_set_bonds: k and r0 must be finite, r0 >= 0");
+        MTG_REQUIRE(nb <= (int64_t)INT32_MAX / 2, "mtg_set_bonds: too many bonds");
+        // every bond joins two different particles of one replica (host-order global indices)
+        std::vector<int> deg((size_t)ntot_ + 1, 0);
+        auto replica_of = [&](int i) {
+            return (int)(std::upper_bound(rep_slot.begin(), rep_slot.end(), i) - rep_slot.begin()) - 1;
+        };
+        for (int64_t q = 0; q < nb; q++) {
+            const int a = bonds[2 * q], b = bonds[2 * q + 1];
+            MTG_REQUIRE(a >= 0 && a < ntot_ && b >= 0 && b < ntot_ && a != b,
+                        "mtg_set_bonds: bond " + std::to_string(q) + " joins " + std::to_string(a) + " and " +
+                            std::to_string(b) + " (the indices must differ and lie in [0, " + std::to_string(ntot_) + "))");
+            MTG_REQUIRE(replica_of(a) == replica_of(b),
+                        "mtg_set_bonds: bond " + std::to_string(q) + " joins particles of two replicas");
+            deg[(size_t)a + 1]++;
+            deg[(size_t)b + 1]++;
+        }
+        for (int i = 0; i < ntot_; i++) deg[(size_t)i + 1] += deg[i];
+        std::vector<int> partner((size_t)std::max<int64_t>(1, 2 * nb)), fill(deg.begin(), deg.end() - 1);
+        for (int64_t q = 0; q < nb; q++) {
+            const int a = bonds[2 * q], b = bonds[2 * q + 1];
+            partner[(size_t)fill[a]++] = b;
+            partner[(size_t)fill[b]++] = a;
+        }
+        MTG_CUDA(cudaStreamSynchronize(st));
+        cudaFree(d_bond_start); cudaFree(d_bond_partner);
+        d_bond_start = d_bond_partner = nullptr;
+        nbonds = 0;
+        for (int b = 0; b < 2; b++) {
+            if (graph[b]) cudaGraphExecDestroy(graph[b]);
+            graph[b] = nullptr;  // captured with the previous force arguments
+        }
+        if (nb == 0) return;
+        MTG_CUDA(cudaMalloc(&d_bond_start, sizeof(int) * ((size_t)ntot_ + 1)));
+        MTG_CUDA(cudaMalloc(&d_bond_partner, sizeof(int) * partner.size()));
+        MTG_CUDA(cudaMemcpy(d_bond_start, deg.data(), sizeof(int) * deg.size(), cudaMemcpyHostToDevice));
+        MTG_CUDA(cudaMemcpy(d_bond_partner, partner.data(), sizeof(int) * partner.size(), cudaMemcpyHostToDevice));
+        if (!d_slot_of) {
+            MTG_CUDA(cudaMalloc(&d_slot_of, sizeof(int) * (size_t)ntot_));
+            buf[0].slot_of = buf[1].slot_of = d_slot_of;
+            if (have_state) {
+                const int g = grid_for(ntot_, 256, occ_stream, sms);
+                mtg::slot_map_kernel<<<g, 256, 0, st>>>(ntot_, buf[cur].ident, d_slot_of);
+                check_launch();
+                nlaunch += 1;
+            }
+        }
+        nbonds = nb;
+        bond_k = k;
+        bond_r0 = r0;
+        MTG_CUDA(cudaStreamSynchronize(st));
     }
 
     void step(int nsteps, const double *noise) override {

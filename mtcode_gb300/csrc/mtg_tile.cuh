@@ -749,8 +749,13 @@ __device__ void consume_staged_unit(const ForceArgs<float> &a, const StageBuf &B
     // -- phase 3: epilogue per home particle
     if (active) {
         const int s = W.h_slot[lane];
-        const float F[3] = {acc_get(W.acc[lane][0]), acc_get(W.acc[lane][1]), acc_get(W.acc[lane][2])};
+        float F[3] = {acc_get(W.acc[lane][0]), acc_get(W.acc[lane][1]), acc_get(W.acc[lane][2])};
         const float T[3] = {acc_get(W.acc[lane][3]), acc_get(W.acc[lane][4]), acc_get(W.acc[lane][5])};
+        if (a.bond_start) {
+            const float4 ph = B.pos[myk];
+            float eb = 0.f;
+            bond_forces<float>(a, R, W.h_id[lane], ph.x, ph.y, ph.z, F, eb, big);
+        }
         if (MODE == kModeForces) {
             const int id = W.h_id[lane];
             for (int k = 0; k < 3; k++) {

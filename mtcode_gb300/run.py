@@ -18,7 +18,7 @@ from . import LangevinNVTRGPU, workloads
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--workload", default="c4", choices=sorted(workloads.WORKLOADS))
-    ap.add_argument("--replicas", type=int, default=512, help="replicas of the c4 workload")
+    ap.add_argument("--replicas", type=int, default=512, help="replicas of the c4 / c5 workloads (c5: 64 by default)")
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
@@ -27,12 +27,16 @@ def main() -> None:
     args = ap.parse_args()
     if args.workload == "c4":
         W = workloads.patchy_c4(seed=args.seed, n_replicas=args.replicas)
+    elif args.workload == "c5":
+        W = workloads.polymer_c5(seed=args.seed, n_replicas=min(args.replicas, 64))
     else:
         W = workloads.WORKLOADS[args.workload](seed=args.seed)
     n = W.n_total
     z = np.zeros((n, 3))
     with LangevinNVTRGPU(W.replicas, precision=args.precision, force_kernel=args.kernel) as s:
         s.initialize(W.x, z, z, W.Q)
+        if W.bonds is not None:
+            s.set_bonds(W.bonds, W.bond_k, W.bond_r0)
         s.init_forces()
         s.sync()
         t0 = time.perf_counter()

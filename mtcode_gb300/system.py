@@ -202,6 +202,14 @@ class LangevinNVTRGPU:
                 raise ValueError("noise must hold nsteps x n x 6 values")
             _check(self._h, _lib.lib().mtg_step_noise(self._h, int(nsteps), dptr(noise)))
 
+    def set_bonds(self, bonds, k: float, r0: float) -> None:
+        """Fixed bonds with HarmonicPotential(k, r0), added to every force pass (MD::calculateforces over
+        the bond list, MD.cpp:1684-1764).  ``bonds``: n_b x 2 host-order (global) particle indices, both
+        ends in one replica; an empty list removes them."""
+        b = np.ascontiguousarray(np.asarray(bonds, dtype=np.int32).reshape(-1, 2))
+        _check(self._h, _lib.lib().mtg_set_bonds(self._h, b.ctypes.data_as(_lib._I32) if len(b) else None, len(b),
+                                                 float(k), float(r0)))
+
     def calculate_forces_and_torques3D(self, with_energy: bool = False):
         """MD::calculateforces(HSPotential) + LangevinNVTR::calculate_forces_and_torques3D: F, T (lab)."""
         F = np.empty((self.n, 3))
@@ -269,6 +277,18 @@ def random_positions(n: int, box: float, periodic: bool = True, min_dist: float 
                                          int(seed) & 0xFFFFFFFFFFFFFFFF, dptr(x))
     if st != 0:
         raise MtgError(st, f"could not place {n} particles at min_dist {min_dist} in a box of {box}")
+    return x
+
+
+def random_chains(n_chains: int, beads: int, box: float, periodic: bool = True, step: float = 1.0,
+                  min_dist: float = 0.9, seed: int = 0) -> np.ndarray:
+    """Self-avoiding random-walk chains (bond length ``step``, every bead >= ``min_dist`` from all
+    others); chain c's bead b is row c * beads + b."""
+    x = np.empty((n_chains * beads, 3))
+    st = _lib.lib().mtg_random_chains(int(n_chains), int(beads), float(box), int(bool(periodic)), float(step),
+                                      float(min_dist), int(seed) & 0xFFFFFFFFFFFFFFFF, dptr(x))
+    if st != 0:
+        raise MtgError(st, f"could not place {n_chains} chains of {beads} beads in a box of {box}")
     return x
 
 

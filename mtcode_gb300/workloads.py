@@ -10,6 +10,11 @@ and zero angular momenta.  No public dataset is involved; everything is generate
   patchy_c3   N=1,048,576 = 262,144 tetrahedral (depth 7) + 786,432 WCA crowders, phi 0.25
   patchy_c4   512 replicas, N_r log-uniform in [1,024, 32,768], phi 0.15, kT_r ~ U[0.8, 1.2],
               depth_r ~ U[6, 10], range 1.2, cos 0.90, own Philox seed per replica
+  polymer_c5  64 replicas x 2,621 chains x 100 beads (262,100 per replica), phi 0.10, harmonic bonds
+              k = 100, r0 = 1, WCA core between all beads, every 10th bead carries -x/+x patches
+              (depth 8, range 1.2, cos 0.90), self-avoiding random-walk start (step 1, 0.9 sigma), dt 0.002.
+              Patchy beads are numbered first (GeneralPatch types are contiguous index ranges) and the
+              bond list is renumbered with them.
 """
 from __future__ import annotations
 
@@ -18,7 +23,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .system import PatchModelSpec, ReplicaSpec, random_positions, random_rotations
+from .system import PatchModelSpec, ReplicaSpec, random_chains, random_positions, random_rotations
 
 
 @dataclass
@@ -27,6 +32,9 @@ class Workload:
     replicas: list           # ReplicaSpec per replica
     x: np.ndarray            # concatenated initial positions (n_total x 3)
     Q: np.ndarray            # concatenated initial orientations (n_total x 9)
+    bonds: np.ndarray | None = None   # fixed bonds (n_b x 2 global indices), HarmonicPotential(bond_k, bond_r0)
+    bond_k: float = 0.0
+    bond_r0: float = 0.0
 
     @property
     def n_total(self) -> int:
@@ -111,4 +119,47 @@ def patchy_c4(seed: int = 0, n_replicas: int = 512, n_min: int = 1024, n_max: in
     return Workload("patchy_c4", reps, x, Q)
 
 
-WORKLOADS = {"c1": patchy_c1, "c2": patchy_c2, "c3": patchy_c3, "c4": patchy_c4}
+def bead_model(n_patchy: int, n: int, depth: float = 8.0, dis: float = 1.2, cos_max: float = 0.90) -> PatchModelSpec:
+    """Two GeneralPatch types: beads 0 .. n_patchy-1 carry the BivalentPatch pair -x/+x, the rest none."""
+    th = math.acos(cos_max)
+    return PatchModelSpec([2, 0], [n_patchy, n], np.array([[-1.0, 0, 0], [1.0, 0, 0]]),
+                          np.tile([depth, dis, th], (4, 1)).astype(float))
+
+
+def chain_replica(n_chains: int, beads: int, box: float, every: int, seed: int, periodic: bool = True):
+    """Random-walk chains with every `every`-th bead patchy, renumbered patchy-first.
+    Returns (x, bonds, n_patchy) in the new numbering."""
+    xc = random_chains(n_chains, beads, box, periodic, 1.0, 0.9, seed)
+    n = n_chains * beads
+    idx = np.arange(n)
+    patchy = (idx % beads) % every == 0
+    order = np.concatenate([idx[patchy], idx[~patchy]])
+    new_of_old = np.empty(n, dtype=np.int64)
+    new_of_old[order] = idx
+    first = (idx % beads) != beads - 1
+    bonds = np.stack([new_of_old[idx[first]], new_of_old[idx[first] + 1]], axis=1).astype(np.int32)
+    return np.ascontiguousarray(xc[order]), bonds, int(patchy.sum())
+
+
+def polymer_c5(seed: int = 0, n_replicas: int = 64, n_chains: int = 2621, beads: int = 100, phi: float = 0.10,
+               every: int = 10, k: float = 100.0, r0: float = 1.0, dt: float = 0.002, kT: float = 1.0) -> Workload:
+    from concurrent.futures import ThreadPoolExecutor
+    n = n_chains * beads
+    box = box_for(n, phi)
+    reps = []
+
+    def one(r):
+        return chain_replica(n_chains, beads, box, every, seed * 1000003 + 2 * r)
+
+    with ThreadPoolExecutor(max_workers=16) as ex:
+        parts = list(ex.map(one, range(n_replicas)))
+    xs, qs, bs = [], [], []
+    for r, (x, b, n_patchy) in enumerate(parts):
+        reps.append(ReplicaSpec(n=n, box=box, model=bead_model(n_patchy, n), kT=kT, dt=dt, seed=(seed << 20) + r))
+        xs.append(x)
+        qs.append(random_rotations(n, seed * 1000003 + 2 * r + 1))
+        bs.append(b + r * n)
+    return Workload("polymer_c5", reps, np.concatenate(xs), np.concatenate(qs), np.concatenate(bs), k, r0)
+
+
+WORKLOADS = {"c1": patchy_c1, "c2": patchy_c2, "c3": patchy_c3, "c4": patchy_c4, "c5": polymer_c5}

@@ -185,6 +185,35 @@ void orc_hs_forces(const orc_params *P, const double *x, const int *pairs, long 
     }
 }
 
+void orc_bond_forces(const orc_params *P, const double *x, const int *bonds, long nb, double k, double r0, double *F)
+{
+    memset(F, 0, sizeof(double) * 3 * (size_t)P->n);
+    for (long q = 0; q < nb; q++) {
+        int p1 = bonds[2 * q], p2 = bonds[2 * q + 1];
+        double un[3];
+        double dis = orc_distance_vector(P, x, p1, p2, un);
+        double f1 = -k * (sqrt(dis) - r0);
+        for (int j = 0; j < 3; j++) {
+            double fac = f1 * un[j] / sqrt(dis);
+            F[3 * p1 + j] += fac;
+            F[3 * p2 + j] += -fac;
+        }
+    }
+}
+
+void orc_central_forces(const orc_params *P, const double *x, const int *pairs, long np, double *F)
+{
+    if (P->nbonds <= 0 || !P->bonds) {
+        orc_hs_forces(P, x, pairs, np, F);
+        return;
+    }
+    double *F2 = (double *)malloc(sizeof(double) * 3 * (size_t)(P->n > 0 ? P->n : 1));
+    orc_bond_forces(P, x, P->bonds, P->nbonds, P->bond_k, P->bond_r0, F);
+    orc_hs_forces(P, x, pairs, np, F2);
+    for (size_t i = 0; i < 3 * (size_t)P->n; i++) F[i] += F2[i];
+    free(F2);
+}
+
 /* ---------------------------------------------------------------- patch force (KernFrenkelOnePatch2) */
 
 void orc_kf2_force_torque(const double nb1[3], const double nb2[3], double att, double dis, double thetam,
@@ -539,7 +568,7 @@ void orc_forces(const orc_params *P, const double *x, const double *Q, int ncell
 {
     int *pairs;
     long np = orc_pairs_alloc(P, x, ncell, rc, &pairs);
-    orc_hs_forces(P, x, pairs, np, F);
+    orc_central_forces(P, x, pairs, np, F);
     memset(T, 0, sizeof(double) * 3 * (size_t)P->n);
     orc_patch_forces(P, x, Q, pairs, np, F, T);
     free(pairs);
@@ -583,7 +612,7 @@ int orc_run(const orc_params *P, double *x, double *p, double *Lb, double *Q, do
         orc_halfkick(n, P->dt, p, Lb, Ft, Tt);
         orc_drift(P, x, p);
         orc_rotate(P, Lb, Q);
-        orc_hs_forces(P, x, pairs, np, Ft);
+        orc_central_forces(P, x, pairs, np, Ft);
         memset(Tt, 0, sizeof(double) * 3 * (size_t)n);
         orc_patch_forces(P, x, Q, pairs, np, Ft, Tt);
         if (check_skin) {   /* every pair within the force range must be in the list */

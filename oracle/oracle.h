@@ -50,6 +50,11 @@ typedef struct {
     double hs_eps, hs_sigma;   /* HSPotential(eps, sigma) */
     double max_dist2;          /* LangevinNVTR::max_distance_check (squared distance) */
     const orc_model *model;
+    /* fixed bond list (nbonds x 2 particle indices) with HarmonicPotential(bond_k, bond_r0)
+     * (MDBase/Potentials/potential.h:265-297); nbonds = 0 for none */
+    const int *bonds;
+    long nbonds;
+    double bond_k, bond_r0;
 } orc_params;
 
 /* geometry.h:508-520 */
@@ -62,6 +67,12 @@ long orc_pairs(const orc_params *P, const double *x, int ncell, double rc, int *
 
 /* MD.cpp:1684-1764 with HSPotential::force (potential.h:106-118). F is overwritten. */
 void orc_hs_forces(const orc_params *P, const double *x, const int *pairs, long np, double *F);
+/* MD.cpp:1684-1764 over the bond list with HarmonicPotential::force (potential.h:274-276):
+ * f = -k (r - r0) along x_p1 - x_p2.  F is overwritten. */
+void orc_bond_forces(const orc_params *P, const double *x, const int *bonds, long nb, double k, double r0, double *F);
+/* The central forces a bonded driver sums (mainActivePolymer.cpp:390-402 pattern): F = bond forces,
+ * then F += HS forces over the pairs (the HS part alone when P has no bonds).  F is overwritten. */
+void orc_central_forces(const orc_params *P, const double *x, const int *pairs, long np, double *F);
 /* LangevinR.cpp:911-1047 with KernFrenkelOnePatch2::force_and_torque (potentialtheta.h:517-750).
  * Adds into F and T (lab frame). */
 void orc_patch_forces(const orc_params *P, const double *x, const double *Q, const int *pairs, long np,
@@ -98,7 +109,8 @@ void orc_philox_noise(int n, uint64_t seed, uint32_t replica, uint64_t draw, dou
 void orc_observables(const orc_params *P, const double *x, const double *Q, const int *pairs, long np,
                      double out[4]);
 
-/* Full forces as the driver computes them: F = HS forces + patch forces; T = patch torques (lab). */
+/* Full forces as the driver computes them: F = (bond forces +) HS forces + patch forces;
+ * T = patch torques (lab). */
 void orc_forces(const orc_params *P, const double *x, const double *Q, int ncell, double rc,
                 double *F, double *T);
 

@@ -53,7 +53,8 @@ class OrcParams(C.Structure):
     _fields_ = [("n", C.c_int), ("box", C.c_double), ("periodic", C.c_int), ("dt", C.c_double),
                 ("kT", C.c_double), ("gamma", C.c_double), ("gammar", C.c_double), ("mass", C.c_double),
                 ("inertia", C.c_double), ("hs_eps", C.c_double), ("hs_sigma", C.c_double),
-                ("max_dist2", C.c_double), ("model", C.POINTER(OrcModel))]
+                ("max_dist2", C.c_double), ("model", C.POINTER(OrcModel)), ("bonds", C.POINTER(C.c_int)),
+                ("nbonds", C.c_long), ("bond_k", C.c_double), ("bond_r0", C.c_double)]
 
 
 _D = C.POINTER(C.c_double)
@@ -88,6 +89,8 @@ def orc() -> C.CDLL:
         L.orc_temperature.argtypes = [P, _D, _D, _D]
         L.orc_rotation_matrix.argtypes = [C.c_double, C.c_double, _D, _D]
         L.orc_hs_forces.argtypes = [P, _D, _I, C.c_long, _D]
+        L.orc_bond_forces.argtypes = [P, _D, _I, C.c_long, C.c_double, C.c_double, _D]
+        L.orc_central_forces.argtypes = [P, _D, _I, C.c_long, _D]
         L.orc_patch_forces.argtypes = [P, _D, _D, _I, C.c_long, _D, _D]
         L.orc_observables.argtypes = [P, _D, _D, _I, C.c_long, _D]
         L.orc_neighbor_cells.restype = C.c_int
@@ -122,6 +125,25 @@ class System:
         p.max_dist2 = float(spec.max_dist2)
         p.model = C.pointer(self.model)
         self.params = p
+        self.set_bonds(None)
+
+    def set_bonds(self, bonds, k: float = 0.0, r0: float = 0.0) -> None:
+        """Fixed bond list (n_b x 2 local particle indices) with HarmonicPotential(k, r0)."""
+        p = self.params
+        if bonds is None or len(bonds) == 0:
+            self._bonds = None
+            p.bonds, p.nbonds, p.bond_k, p.bond_r0 = None, 0, 0.0, 0.0
+            return
+        self._bonds = np.ascontiguousarray(bonds, dtype=np.intc).reshape(-1, 2)
+        p.bonds = self._bonds.ctypes.data_as(_I)
+        p.nbonds, p.bond_k, p.bond_r0 = len(self._bonds), float(k), float(r0)
+
+    def bond_forces(self, x, bonds, k: float, r0: float) -> np.ndarray:
+        b = np.ascontiguousarray(bonds, dtype=np.intc).reshape(-1, 2)
+        F = np.empty((self.spec.n, 3))
+        orc().orc_bond_forces(C.byref(self.params), _d(np.ascontiguousarray(x, float)), b.ctypes.data_as(_I),
+                              len(b), float(k), float(r0), _d(F))
+        return F
 
     @property
     def force_range(self) -> float:
@@ -221,6 +243,10 @@ def ref() -> C.CDLL | None:
                               C.c_double, C.c_int, _I, _I, _D, _D, C.c_int, C.c_double, C.c_int, C.c_int, _D,
                               C.c_int, _D, _D]
         L.ref_rotation_matrix.argtypes = [C.c_double, _D, _D]
+        L.ref_bond_forces.argtypes = [C.c_int, C.c_double, C.c_int, _D, _I, C.c_long, C.c_double, C.c_double, _D]
+        L.ref_forces_bonded.argtypes = [C.c_int, C.c_double, C.c_int, _D, _D, C.c_int, C.c_double, C.c_double,
+                                        C.c_double, C.c_int, _I, _I, _D, _D, _I, C.c_long, C.c_double, C.c_double,
+                                        _D, _D]
         _ref = L
     return _ref
 

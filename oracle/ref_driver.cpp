@@ -172,6 +172,58 @@ void ref_forces(int n, double box, int periodic, const double *x, const double *
     delete b;
 }
 
+// F = MD::calculateforces(bond list, HarmonicPotential(k, r0))  (MD.cpp:1684-1764, potential.h:265-297),
+// the bonded term of the polymer drivers (mainActivePolymer.cpp:390).
+void ref_bond_forces(int n, double box, int periodic, const double *x, const int *bonds, long nb, double k, double r0,
+                     double *F)
+{
+    vector<double> zeros3(3 * (size_t)n, 0.0), zeros9(9 * (size_t)n, 0.0);
+    LangevinNVTR *b = make_system(n, box, periodic, x, zeros3.data(), zeros3.data(), zeros9.data(), 0.005, 1, 1, 1);
+    matrix<int> bp((int)nb, 2);
+    for (long i = 0; i < nb; i++) {
+        bp(i, 0) = bonds[2 * i];
+        bp(i, 1) = bonds[2 * i + 1];
+    }
+    HarmonicPotential pot(k, r0);
+    matrix<double> Fm = b->calculateforces(bp, pot);
+    from_mat(Fm, F, n, 3);
+    delete b;
+}
+
+// The force pass of a bonded patchy system, summed as the polymer drivers do (mainActivePolymer.cpp:
+// 390-402): F = calculateforces(bonds, HarmonicPotential(k, r0)); F += calculateforces(pairs,
+// HSPotential); T = 0; calculate_forces_and_torques3D(pairs, ComboPatch, F, T).
+void ref_forces_bonded(int n, double box, int periodic, const double *x, const double *Q, int ncell, double rc,
+                       double hs_eps, double hs_sigma, int n_types, const int *ppt, const int *npt, const double *orient,
+                       const double *params, const int *bonds, long nb, double k, double r0, double *F, double *T)
+{
+    vector<double> zeros3(3 * (size_t)n, 0.0);
+    LangevinNVTR *b = make_system(n, box, periodic, x, zeros3.data(), zeros3.data(), Q, 0.005, 1, 1, 1);
+    RefModelDesc d = {2, 0.0, 0.0, 0.0, n_types, ppt, npt, orient, params};
+    ComboPatch *pots = make_model(d);
+    int ccc;
+    matrix<int> boxes = b->getgeo().generate_boxes_relationships(ncell, ccc);
+    matrix<int> *pairs = b->calculatepairs(boxes, rc);
+    matrix<int> bp((int)nb, 2);
+    for (long i = 0; i < nb; i++) {
+        bp(i, 0) = bonds[2 * i];
+        bp(i, 1) = bonds[2 * i + 1];
+    }
+    HarmonicPotential bond(k, r0);
+    HSPotential wsa(hs_eps, hs_sigma);
+    matrix<double> Fm = b->calculateforces(bp, bond);
+    matrix<double> F2 = b->calculateforces(*pairs, wsa);
+    Fm += F2;
+    matrix<double> Tm(n, 3);
+    Tm.reset_parallel(0.0);
+    b->calculate_forces_and_torques3D(*pairs, *pots, Fm, Tm);
+    from_mat(Fm, F, n, 3);
+    from_mat(Tm, T, n, 3);
+    delete pairs;
+    delete pots;
+    delete b;
+}
+
 // Condensate::run loop body (Condensate.cpp:335-378), nsteps times.  Pairs are rebuilt from the
 // positions at the start of a step every `rebuild` steps (the driver uses 20 at rc 3.5).
 // noise: nsteps x n x 6 values used in place of generate_uniform_random_matrix, or NULL for zeros.

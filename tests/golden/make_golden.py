@@ -22,7 +22,7 @@ sys.path.insert(0, str(ROOT))
 
 from oracle import pyoracle as po  # noqa: E402
 from mtcode_gb300.system import PatchModelSpec, ReplicaSpec, random_positions, random_rotations  # noqa: E402
-from mtcode_gb300.workloads import box_for, crowded_model, tubulin_model  # noqa: E402
+from mtcode_gb300.workloads import bead_model, box_for, chain_replica, crowded_model, tubulin_model  # noqa: E402
 
 HERE = Path(__file__).resolve().parent
 D = po._d
@@ -53,6 +53,51 @@ def ref_forces(spec, x, Q, rc):
     R.ref_forces(spec.n, spec.box, int(spec.periodic), D(x), D(Q), ncell, rc, spec.hs_eps, spec.hs_sigma, kind, att,
                  dis, th, nt, ppt.ctypes.data_as(po._I), npt.ctypes.data_as(po._I), D(orient), D(params), D(F), D(T))
     return F, T
+
+
+def ref_forces_bonded(spec, x, Q, rc, bonds, k, r0):
+    R = po.ref()
+    _, _, _, _, nt, ppt, npt, orient, params = po.ref_model_args(spec.model)
+    F = np.empty((spec.n, 3))
+    T = np.empty((spec.n, 3))
+    ncell = max(1, int(math.floor(spec.box / rc)))
+    b = np.ascontiguousarray(bonds, dtype=np.intc)
+    R.ref_forces_bonded(spec.n, spec.box, int(spec.periodic), D(x), D(Q), ncell, rc, spec.hs_eps, spec.hs_sigma, nt,
+                        ppt.ctypes.data_as(po._I), npt.ctypes.data_as(po._I), D(orient), D(params),
+                        b.ctypes.data_as(po._I), len(b), k, r0, D(F), D(T))
+    return F, T
+
+
+def ref_bond_forces(spec, x, bonds, k, r0):
+    F = np.empty((spec.n, 3))
+    b = np.ascontiguousarray(bonds, dtype=np.intc)
+    po.ref().ref_bond_forces(spec.n, spec.box, int(spec.periodic), D(x), b.ctypes.data_as(po._I), len(b), k, r0, D(F))
+    return F
+
+
+def bonded_cases():
+    """F. bonded bead systems: harmonic bonds + WCA + patches on every `every`-th bead (patchy first)."""
+    cases = [(20, 30, 0.35, 2, True), (24, 25, 0.35, 2, False)]
+    for k, (nch, beads, phi, every, per) in enumerate(cases):
+        n = nch * beads
+        box = box_for(n, phi)
+        for seed in range(50):
+            x, bonds, n_patchy = chain_replica(nch, beads, box, every, 300 + 10 * k + seed, per)
+            # stretch and compress the bonds: +-0.06 per coordinate keeps every bead > 0.78 sigma apart
+            x = x + np.random.default_rng(500 + 10 * k + seed).uniform(-0.06, 0.06, x.shape)
+            x = f32(np.mod(x, box) if per else np.clip(x, 0.0, np.nextafter(box, 0)))
+            spec = ReplicaSpec(n=n, box=box, model=bead_model(n_patchy, n), periodic=per, kT=1.0, dt=0.002,
+                               seed=seed)
+            Q = f32(random_rotations(n, 400 + 10 * k + seed))
+            rc = po.System(spec).force_range * 1.05
+            if threshold_margin(spec, x, Q, rc) > 1e-6:
+                break
+        F, T = ref_forces_bonded(spec, x, Q, rc, bonds, 100.0, 1.0)
+        Fb = ref_bond_forces(spec, x, bonds, 100.0, 1.0)
+        np.savez_compressed(HERE / f"bonded_{k}.npz", x=x, Q=Q, rc=rc, bonds=bonds, bond_k=100.0, bond_r0=1.0, F=F,
+                            T=T, F_bond=Fb, **spec_record(spec))
+        print(f"bonded_{k}: n={n} patchy={n_patchy} bonds={len(bonds)} periodic={per} |F|max={np.abs(F).max():.3g} "
+              f"|F_bond|max={np.abs(Fb).max():.3g} torqued={(np.abs(T).sum(1) > 0).sum()}")
 
 
 def ref_run(spec, st, nsteps, rc, rebuild, noise=None, init=True, noise0=None):
@@ -142,10 +187,14 @@ def spec_record(spec):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--only", choices=["bonded"], help="regenerate one group of fixtures only")
     args = ap.parse_args()
     po.build_oracle()
     po.build_ref(args.reference)
     assert po.ref() is not None, "reference shim not built"
+    if args.only == "bonded":
+        bonded_cases()
+        return
 
     # ---- A. pair sets (MD::calculatepairs and calculatepairs_parallel)
     pair_cases = [("tetra", 1000, 0.10, 1, True, 1.68), ("tetra", 1000, 0.30, 2, True, 1.5),
@@ -230,6 +279,8 @@ def main():
         po.ref().ref_rotation_matrix(0.005, D(L), D(Rs[i]))
     np.savez_compressed(HERE / "rotation.npz", L=Ls, R=Rs, dt=0.005, inertia=0.1)
     print("rotation.npz written")
+
+    bonded_cases()
 
 
 if __name__ == "__main__":

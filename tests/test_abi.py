@@ -101,3 +101,23 @@ def test_random_rotations_are_proper():
 def test_overpacked_start_is_rejected():
     with pytest.raises(Exception):
         random_positions(2000, 5.0, True, 0.9, 1)
+
+
+def test_random_chains_are_self_avoiding_and_seeded():
+    """mtg_random_chains (host helper, no GPU): bond length exactly `step`, every pair of beads at least
+    min_dist apart (minimum image), in the box, and the same output for the same seed."""
+    from mtcode_gb300.system import random_chains
+    box = 12.0
+    x = random_chains(10, 40, box, True, 1.0, 0.9, 5)
+    assert np.array_equal(x, random_chains(10, 40, box, True, 1.0, 0.9, 5))
+    assert (x >= 0).all() and (x < box).all()
+    d = x[:, None, :] - x[None, :, :]
+    d -= box * np.round(d / box)
+    r = np.sqrt((d * d).sum(-1))
+    np.fill_diagonal(r, np.inf)
+    assert r.min() >= 0.9
+    idx = np.arange(len(x) - 1)
+    bond = idx[idx % 40 != 39]
+    assert np.allclose(r[bond, bond + 1], 1.0, rtol=0, atol=1e-12)
+    xw = random_chains(6, 30, box, False, 1.0, 0.9, 6)
+    assert (xw >= 0).all() and (xw < box).all()

@@ -118,3 +118,35 @@ def test_oracle_vs_reference_live():
         assert close(F, Fr) and close(T, Tr)
         nc = max(1, int(math.floor(spec.box / 1.7)))
         assert np.array_equal(sorted_pairs(sysm.pairs(x, 1.7, nc)), ref_pairs(spec, x, nc, 1.7))
+
+
+@pytest.mark.parametrize("k", range(2))
+def test_bonded_forces_match_reference(k):
+    """Harmonic bonds (MD::calculateforces with HarmonicPotential) alone, and the bonded driver's sum
+    bond + HS + patch forces, against the reference's own routines."""
+    d = load(f"bonded_{k}.npz")
+    sysm = po.System(spec_from(d))
+    bk, br = float(d["bond_k"]), float(d["bond_r0"])
+    assert close(sysm.bond_forces(d["x"], d["bonds"], bk, br), d["F_bond"])
+    sysm.set_bonds(d["bonds"], bk, br)
+    F, T = sysm.forces(d["x"], d["Q"], float(d["rc"]))
+    assert close(F, d["F"])
+    assert close(T, d["T"])
+
+
+@pytest.mark.skipif(po.ref() is None, reason="the reference shim is only built where the reference sources exist")
+def test_bond_forces_live_vs_reference():
+    """Fresh chains (not in the fixtures): the oracle's bond forces equal the reference's bit for bit."""
+    from mtcode_gb300.workloads import bead_model, box_for, chain_replica
+    n_ch, beads = 30, 40
+    box = box_for(n_ch * beads, 0.2)
+    x, bonds, n_patchy = chain_replica(n_ch, beads, box, 4, 9)
+    x = x + np.random.default_rng(3).uniform(-0.05, 0.05, x.shape)
+    from mtcode_gb300.system import ReplicaSpec
+    spec = ReplicaSpec(n=n_ch * beads, box=box, model=bead_model(n_patchy, n_ch * beads))
+    F = po.System(spec).bond_forces(x, bonds, 37.0, 1.1)
+    Fr = np.empty_like(F)
+    b = np.ascontiguousarray(bonds, dtype=np.intc)
+    po.ref().ref_bond_forces(spec.n, spec.box, 1, po._d(np.ascontiguousarray(x)), b.ctypes.data_as(po._I), len(b),
+                             37.0, 1.1, po._d(Fr))
+    assert np.array_equal(F, Fr)
