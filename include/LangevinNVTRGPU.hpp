@@ -105,6 +105,20 @@ class LangevinNVTRGPU {
         mtg_adapter::from_rows(t, n, 3, T);
     }
 
+    // the bonded term of the polymer drivers: F += MD::calculateforces(bonds, HarmonicPotential(k, r0))
+    // (mainActivePolymer.cpp:390-402) on every force pass; bonds is any B x 2 int matrix (e.g. matrix<int>)
+    template <class IntMatrix>
+    void setbonds(IntMatrix &bonds, double k, double r0) {
+        if (!h_) create();
+        const int nb = bonds.getNsafe();
+        std::vector<int32_t> b((size_t)nb * 2);
+        for (int i = 0; i < nb; i++) {
+            b[2 * (size_t)i] = bonds(i, 0);
+            b[2 * (size_t)i + 1] = bonds(i, 1);
+        }
+        mtg_adapter::require_ok(h_, mtg_set_bonds(h_, nb ? b.data() : nullptr, nb, k, r0), "setbonds");
+    }
+
     // MD::calculatepairs_parallel(boxes, rc) -> pairs (i < j), P x 2, into any resizable int matrix
     template <class IntMatrix>
     void calculatepairs_parallel(double rc, IntMatrix &pairs_out) {

@@ -45,6 +45,13 @@ void run_on_gpu(double l, int N, matrix<double> &dat, int runtime, TetrahedralPa
     obj.calculate_forces_and_torques3D(F, T);
     matrix<int> pairs;
     obj.calculatepairs_parallel(3.5, pairs);
+    // the bonded drivers' bond list is the reference's own matrix<int> (mainActivePolymer.cpp:390)
+    matrix<int> bp2(N - 1, 2);
+    for (int i = 0; i + 1 < N; i++) {
+        bp2(i, 0) = i;
+        bp2(i, 1) = i + 1;
+    }
+    obj.setbonds(bp2, 100.0, 1.0);
     obj.init_forces();
     vector1<double> meas(6);
     for (int i = 0; i < runtime; i++) {
