@@ -254,6 +254,10 @@ class LangevinNVTRGPU:
     def flags(self) -> int:
         return int(_lib.lib().mtg_flags(self._h))
 
+    def clear_flags(self) -> None:
+        """Clear the device-latched condition bits (mtg_clear_flags)."""
+        _lib.lib().mtg_clear_flags(self._h)
+
     @property
     def draw(self) -> int:
         return int(_lib.lib().mtg_get_draw(self._h))
