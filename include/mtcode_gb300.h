@@ -232,6 +232,19 @@ void mtg_random_rotations(int n, uint64_t seed, double *Q);
 mtg_status mtg_random_chains(int n_chains, int beads, double box, int periodic, double step, double min_dist,
                              uint64_t seed, double *x);
 
+/* Frame files in the reference's format (no GPU use).
+ * mtg_csv_write: rows x cols row-major doubles as matrix::operator<<= writes them (matrix2.cpp:898-912):
+ *   ',' between values, '\n' after each row, each value as an ostream prints a double (%g).
+ * mtg_csv_read: importcsv (matrix2.cpp:1597-1640): rows from lines, atof per ','-cell, short rows padded
+ *   with 0.  *rows / *cols receive the shape; with a null a only the shape is read; MTG_ERR_CAPACITY if
+ *   rows * cols > cap.
+ * mtg_frame_name: Condensate::run's frame names (Condensate.cpp:296-300, 383-405), e.g. kind "pos" or
+ *   "orientation": kind + strbase + "_i=" + frame zero-padded to the digits of ceil(runtime/every)
+ *   + ".csv".  Writes at most cap bytes (snprintf) and returns the full length, -1 on bad arguments. */
+mtg_status mtg_csv_write(const char *path, const double *a, int64_t rows, int cols);
+mtg_status mtg_csv_read(const char *path, double *a, int64_t cap, int64_t *rows, int *cols);
+int mtg_frame_name(char *out, int cap, const char *kind, const char *strbase, int frame, int runtime, int every);
+
 #ifdef __cplusplus
 }
 #endif

@@ -112,6 +112,9 @@ SIGNATURES = [
     ("mtg_random_positions", C.c_int, [C.c_int, C.c_double, C.c_int, C.c_double, C.c_uint64, _D]),
     ("mtg_random_rotations", None, [C.c_int, C.c_uint64, _D]),
     ("mtg_random_chains", C.c_int, [C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double, C.c_uint64, _D]),
+    ("mtg_csv_write", C.c_int, [C.c_char_p, _D, C.c_int64, C.c_int]),
+    ("mtg_csv_read", C.c_int, [C.c_char_p, _D, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
+    ("mtg_frame_name", C.c_int, [C.c_char_p, C.c_int, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int]),
 ]
 
 _lib = None

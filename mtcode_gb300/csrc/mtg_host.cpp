@@ -1,8 +1,13 @@
 // mtg_host.cpp -- host-side seeded synthetic inputs for the C ABI (no GPU use).
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
 #include <cstdint>
 #include <climits>
 #include <vector>
+#include <algorithm>
 
 #include "../../include/mtcode_gb300.h"
 
@@ -174,6 +179,78 @@ mtg_status mtg_random_chains(int n_chains, int beads, double box, int periodic, 
         if (!done) return MTG_ERR_ARG;
     }
     return MTG_OK;
+}
+
+// Frame files in the reference's format: one row per line, values separated by ',', each value as
+// std::ostream prints a double by default (six significant digits, %g), i.e. matrix::operator<<=
+// (DataStructures/matrix2.cpp:898-912) as Condensate::run writes pos / orientation frames
+// (Condensate/Condensate.cpp:378-418).
+mtg_status mtg_csv_write(const char *path, const double *a, int64_t rows, int cols) {
+    if (!path || (rows > 0 && !a) || rows < 0 || cols < 1) return MTG_ERR_ARG;
+    FILE *f = std::fopen(path, "w");
+    if (!f) return MTG_ERR_ARG;
+    char buf[64];
+    for (int64_t i = 0; i < rows; i++)
+        for (int j = 0; j < cols; j++) {
+            int n = std::snprintf(buf, sizeof(buf), "%g", a[(size_t)i * cols + j]);
+            buf[n++] = j == cols - 1 ? '\n' : ',';
+            if (std::fwrite(buf, 1, (size_t)n, f) != (size_t)n) {
+                std::fclose(f);
+                return MTG_ERR_ARG;
+            }
+        }
+    return std::fclose(f) == 0 ? MTG_OK : MTG_ERR_ARG;
+}
+
+// importcsv (DataStructures/matrix2.cpp:1597-1640): every line is a row, cells split at ',' and read
+// with atof; the column count is the longest row's and shorter rows are padded with 0.  With a null
+// `a` (or too small a capacity) only the shape is returned, and MTG_ERR_CAPACITY when it does not fit.
+mtg_status mtg_csv_read(const char *path, double *a, int64_t cap, int64_t *rows, int *cols) {
+    if (!path || !rows || !cols) return MTG_ERR_ARG;
+    FILE *f = std::fopen(path, "r");
+    if (!f) return MTG_ERR_ARG;
+    std::vector<std::vector<double>> data;
+    std::string line;
+    int c;
+    bool more = true;
+    while (more) {
+        line.clear();
+        while ((c = std::fgetc(f)) != EOF && c != '\n') line.push_back((char)c);
+        if (c == EOF) {
+            more = false;
+            if (line.empty()) break;  // getline yields no line after a final newline
+        }
+        std::vector<double> row;
+        size_t start = 0;
+        while (start < line.size()) {  // getline(cell, ','): no empty cell after a trailing ','
+            size_t end = line.find(',', start);
+            if (end == std::string::npos) end = line.size();
+            row.push_back(std::atof(line.substr(start, end - start).c_str()));
+            start = end + 1;
+        }
+        data.push_back(std::move(row));
+    }
+    std::fclose(f);
+    int nz = 0;
+    for (auto &r : data) nz = std::max(nz, (int)r.size());
+    *rows = (int64_t)data.size();
+    *cols = nz;
+    if (!a || cap < (int64_t)data.size() * nz) return a ? MTG_ERR_CAPACITY : MTG_OK;
+    for (size_t i = 0; i < data.size(); i++)
+        for (int j = 0; j < nz; j++) a[i * nz + j] = j < (int)data[i].size() ? data[i][j] : 0.0;
+    return MTG_OK;
+}
+
+// Condensate::run's frame file name: kind + strbase + "_i=" + the frame number zero-padded to the
+// digits of ceil(runtime / every) + ".csv" (Condensate.cpp:296-300, 383-405).  Returns the length.
+int mtg_frame_name(char *out, int cap, const char *kind, const char *strbase, int frame, int runtime, int every) {
+    if (!kind || every < 1 || runtime < 0 || frame < 0) return -1;
+    int tf = (int)std::ceil((double)runtime / (double)every), digits = 0;
+    do {
+        ++digits;
+        tf /= 10;
+    } while (tf);
+    return std::snprintf(out, out ? (size_t)cap : 0, "%s%s_i=%0*d.csv", kind, strbase ? strbase : "", digits, frame);
 }
 
 // Arvo, "Fast random rotation matrices" (Graphics Gems III, 1992): M = (2 v v^T - I) Rz(2 pi x1),

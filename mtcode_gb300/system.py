@@ -254,6 +254,22 @@ class LangevinNVTRGPU:
     def flags(self) -> int:
         return int(_lib.lib().mtg_flags(self._h))
 
+    def write_frame(self, directory, frame: int, runtime: int, every: int, strbase: str = "",
+                    replica: int | None = None) -> tuple:
+        """The pos / orientation frame files Condensate::run writes every `every` steps
+        (Condensate.cpp:378-418), for the whole handle or one replica.  Returns the two paths."""
+        from pathlib import Path
+        st = self.get_state()
+        x, Q = st["x"], st["Q"]
+        if replica is not None:
+            off = int(_lib.lib().mtg_replica_offset(self._h, int(replica)))
+            n = self.replicas[replica].n
+            x, Q = x[off:off + n], Q[off:off + n]
+        paths = tuple(Path(directory) / frame_name(kind, frame, runtime, every, strbase) for kind in ("pos", "orientation"))
+        write_csv(paths[0], x)
+        write_csv(paths[1], Q)
+        return paths
+
     def clear_flags(self) -> None:
         """Clear the device-latched condition bits (mtg_clear_flags)."""
         _lib.lib().mtg_clear_flags(self._h)
@@ -294,6 +310,40 @@ def random_chains(n_chains: int, beads: int, box: float, periodic: bool = True, 
     if st != 0:
         raise MtgError(st, f"could not place {n_chains} chains of {beads} beads in a box of {box}")
     return x
+
+
+def frame_name(kind: str, frame: int, runtime: int, every: int, strbase: str = "") -> str:
+    """Condensate::run's frame file name, e.g. frame_name("pos", 7, 1000, 10) == "pos_i=007.csv"."""
+    L = _lib.lib()
+    n = L.mtg_frame_name(None, 0, kind.encode(), strbase.encode(), int(frame), int(runtime), int(every))
+    if n < 0:
+        raise ValueError("frame_name: every >= 1, runtime >= 0 and frame >= 0 are required")
+    buf = C.create_string_buffer(n + 1)
+    L.mtg_frame_name(buf, n + 1, kind.encode(), strbase.encode(), int(frame), int(runtime), int(every))
+    return buf.value.decode()
+
+
+def write_csv(path, a) -> None:
+    """A matrix as the reference writes it (matrix::operator<<=: ',' separated, %g values)."""
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(len(a), -1))
+    st = _lib.lib().mtg_csv_write(str(path).encode(), dptr(a), a.shape[0], a.shape[1])
+    if st != 0:
+        raise MtgError(st, f"could not write {path}")
+
+
+def read_csv(path) -> np.ndarray:
+    """importcsv: rows from lines, atof per ','-cell, short rows padded with 0."""
+    L = _lib.lib()
+    rows, cols = C.c_int64(0), C.c_int(0)
+    st = L.mtg_csv_read(str(path).encode(), None, 0, C.byref(rows), C.byref(cols))
+    if st != 0:
+        raise MtgError(st, f"could not read {path}")
+    out = np.zeros((rows.value, cols.value))
+    if out.size:
+        st = L.mtg_csv_read(str(path).encode(), dptr(out), out.size, C.byref(rows), C.byref(cols))
+        if st != 0:
+            raise MtgError(st, f"could not read {path}")
+    return out
 
 
 def random_rotations(n: int, seed: int = 0) -> np.ndarray:

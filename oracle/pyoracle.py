@@ -244,6 +244,9 @@ def ref() -> C.CDLL | None:
                               C.c_int, _D, _D]
         L.ref_rotation_matrix.argtypes = [C.c_double, _D, _D]
         L.ref_bond_forces.argtypes = [C.c_int, C.c_double, C.c_int, _D, _I, C.c_long, C.c_double, C.c_double, _D]
+        L.ref_write_csv.argtypes = [C.c_char_p, _D, C.c_int, C.c_int]
+        L.ref_import_csv.restype = C.c_long
+        L.ref_import_csv.argtypes = [C.c_char_p, _D, C.c_long, C.POINTER(C.c_int)]
         L.ref_forces_bonded.argtypes = [C.c_int, C.c_double, C.c_int, _D, _D, C.c_int, C.c_double, C.c_double,
                                         C.c_double, C.c_int, _I, _I, _D, _D, _I, C.c_long, C.c_double, C.c_double,
                                         _D, _D]

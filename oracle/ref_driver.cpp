@@ -224,6 +224,30 @@ void ref_forces_bonded(int n, double box, int periodic, const double *x, const d
     delete b;
 }
 
+// The frame writer and reader of Condensate::run: ofstream << = matrix (matrix2.cpp:898-912) and
+// importcsv (matrix2.cpp:1597-1640).
+void ref_write_csv(const char *path, const double *a, int rows, int cols)
+{
+    matrix<double> m(rows, cols);
+    for (int i = 0; i < rows; i++)
+        for (int j = 0; j < cols; j++) m(i, j) = a[(size_t)i * cols + j];
+    ofstream f(path);
+    f <<= m;
+    f.close();
+}
+
+long ref_import_csv(const char *path, double *out, long cap, int *cols)
+{
+    bool err = false;
+    matrix<double> m = importcsv(string(path), 0.0, err);
+    if (err) return -1;
+    long nr = m.getNsafe();
+    *cols = m.getncols();
+    for (long i = 0; i < nr && (i + 1) * (long)*cols <= cap; i++)
+        for (int j = 0; j < *cols; j++) out[i * *cols + j] = m(i, j);
+    return nr;
+}
+
 // Condensate::run loop body (Condensate.cpp:335-378), nsteps times.  Pairs are rebuilt from the
 // positions at the start of a step every `rebuild` steps (the driver uses 20 at rc 3.5).
 // noise: nsteps x n x 6 values used in place of generate_uniform_random_matrix, or NULL for zeros.

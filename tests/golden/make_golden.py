@@ -100,6 +100,35 @@ def bonded_cases():
               f"|F_bond|max={np.abs(Fb).max():.3g} torqued={(np.abs(T).sum(1) > 0).sum()}")
 
 
+# awkward inputs for importcsv: short rows, empty cells, a trailing ',', no final newline.  (An empty
+# line is not among them: importcsv reads past the row there -- a[i].size() - 1 wraps around -- and
+# crashes; mtg_csv_read gives such a row zeros.)
+CSV_CASES = ["1,2,3\n4,5\n6\n", "1.5,,-2\n3e2,4,\n", "7,8,9", "-0,1e-300,nan,inf\n5\n"]
+
+
+def frame_cases():
+    """G. frame files: the reference's writer (matrix operator<<=) and reader (importcsv)."""
+    import tempfile
+    rng = np.random.default_rng(11)
+    a = rng.normal(size=(40, 9)) * 10.0 ** rng.integers(-9, 9, (40, 1))
+    a = np.ascontiguousarray(np.concatenate([a, [[0.0, -0.0, 1e-300, 1e300, 123456789.0, 1 / 3, -2.5, 7.0, 1e-5]]]))
+    tmp = Path(tempfile.mkdtemp())
+    po.ref().ref_write_csv(str(tmp / "w.csv").encode(), D(a), a.shape[0], a.shape[1])
+    written = (tmp / "w.csv").read_bytes()
+    parsed = []
+    for k, text in enumerate(CSV_CASES):
+        (tmp / f"r{k}.csv").write_text(text)
+        out = np.empty(256)
+        cols = po.C.c_int(0)
+        nr = po.ref().ref_import_csv(str(tmp / f"r{k}.csv").encode(), D(out), 256, po.C.byref(cols))
+        parsed.append(out[: nr * cols.value].reshape(nr, cols.value).copy())
+    np.savez_compressed(HERE / "frames.npz", data=a, written=np.frombuffer(written, dtype=np.uint8),
+                        **{f"csv_{k}": np.frombuffer(t.encode(), dtype=np.uint8) for k, t in enumerate(CSV_CASES)},
+                        **{f"parsed_{k}": p for k, p in enumerate(parsed)})
+    print(f"frames.npz: writer {len(written)} bytes, {len(CSV_CASES)} importcsv cases "
+          f"shapes {[p.shape for p in parsed]}")
+
+
 def ref_run(spec, st, nsteps, rc, rebuild, noise=None, init=True, noise0=None):
     R = po.ref()
     kind, att, dis, th, nt, ppt, npt, orient, params = po.ref_model_args(spec.model)
@@ -187,13 +216,16 @@ def spec_record(spec):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
-    ap.add_argument("--only", choices=["bonded"], help="regenerate one group of fixtures only")
+    ap.add_argument("--only", choices=["bonded", "frames"], help="regenerate one group of fixtures only")
     args = ap.parse_args()
     po.build_oracle()
     po.build_ref(args.reference)
     assert po.ref() is not None, "reference shim not built"
     if args.only == "bonded":
         bonded_cases()
+        return
+    if args.only == "frames":
+        frame_cases()
         return
 
     # ---- A. pair sets (MD::calculatepairs and calculatepairs_parallel)
@@ -281,6 +313,7 @@ def main():
     print("rotation.npz written")
 
     bonded_cases()
+    frame_cases()
 
 
 if __name__ == "__main__":
