@@ -169,6 +169,18 @@ mtg_status mtg_temperature(mtg_system *h, double *out);
 #define MTG_OBS_COUNT 5
 mtg_status mtg_observables(mtg_system *h, double *out);
 
+/* calcg1(data, geo, rmax, dr) (MDBase/Analysis/PairCorrelation.cpp:9-153) for one replica at the
+ * current state: counts of unordered pair distances (cube::distance, geometry.h:107-121, FP64) in bins
+ * floor(r / dr) < nbins = floor(rmax / dr).  *nbins receives the bin count; hist (cap >= nbins
+ * entries, or null to ask for the count) the counts.  rmax must not exceed the box side.  Synchronising. */
+mtg_status mtg_gr(mtg_system *h, int replica, double rmax, double dr, int64_t *hist, int cap, int *nbins);
+
+/* distance_graph(pos, boxes, geo, cut, index_test) (MDBase/Analysis/AnalyzeGrowth.cpp:136-171) for one
+ * replica: labels[i] (local index i) = the smallest local index of i's connected component in the graph
+ * of pairs closer than cut, the labels ConnectedComponentsParallel_Old (Bindings/GraphAlgorithms.cpp:
+ * 672-800) converges to.  Synchronising. */
+mtg_status mtg_clusters(mtg_system *h, int replica, double cut, int32_t *labels);
+
 /* FP64 unwrapped displacement accumulated since the last mtg_set_state (total particles x 3). */
 mtg_status mtg_get_displacement(mtg_system *h, double *disp);
 

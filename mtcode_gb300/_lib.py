@@ -93,6 +93,8 @@ SIGNATURES = [
     ("mtg_step_noise", C.c_int, [_H, C.c_int, _D]),
     ("mtg_forces", C.c_int, [_H, _D, _D, _D]),
     ("mtg_set_bonds", C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_int64, C.c_double, C.c_double]),
+    ("mtg_gr", C.c_int, [_H, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_int64), C.c_int, C.POINTER(C.c_int)]),
+    ("mtg_clusters", C.c_int, [_H, C.c_int, C.c_double, _I32]),
     ("mtg_pairs", C.c_int, [_H, C.c_int, C.c_double, _I32, C.c_int64, C.POINTER(C.c_int64)]),
     ("mtg_temperature", C.c_int, [_H, _D]),
     ("mtg_observables", C.c_int, [_H, _D]),

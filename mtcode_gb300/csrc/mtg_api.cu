@@ -206,6 +206,16 @@ mtg_status mtg_set_bonds(mtg_system *h, const int32_t *bonds, int64_t nbonds, do
     return MTG_OK;
 }
 
+mtg_status mtg_gr(mtg_system *h, int replica, double rmax, double dr, int64_t *hist, int cap, int *nbins) {
+    MTG_GUARD(h, h->impl->gr(replica, rmax, dr, hist, cap, nbins));
+    return MTG_OK;
+}
+
+mtg_status mtg_clusters(mtg_system *h, int replica, double cut, int32_t *labels) {
+    MTG_GUARD(h, h->impl->clusters(replica, cut, labels));
+    return MTG_OK;
+}
+
 mtg_status mtg_step_profile(mtg_system *h, int nsteps, double *kernel_ms) {
     MTG_GUARD(h, h->impl->step_profile(nsteps, kernel_ms));
     return MTG_OK;

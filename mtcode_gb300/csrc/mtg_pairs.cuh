@@ -123,5 +123,115 @@ __global__ void pair_write_kernel(PairGrid g, Buffers<real> in, const int *start
     }
 }
 
+// ------------------------------------------------------------------ analysis passes on the pair grid
+
+// cube::distance (geometry.h:107-121) with explicit FP64 roundings: dx = x_i - x_j, one image correction
+// dx - SIGN(l, dx) when |dx| > l / 2, sqrt of the summed squares (symmetric in i, j bit for bit)
+__device__ __forceinline__ double cube_distance(const double xi[3], const double xj[3], double box, int periodic) {
+    const double half = __dmul_rn(box, 0.5);
+    double temp = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        double dx = __dsub_rn(xi[k], xj[k]);
+        if (periodic && fabs(dx) > half) dx = dx >= 0.0 ? __dsub_rn(dx, box) : __dadd_rn(dx, box);
+        temp = __dadd_rn(temp, __dmul_rn(dx, dx));
+    }
+    return __dsqrt_rn(temp);
+}
+
+// calcg1 (MDBase/Analysis/PairCorrelation.cpp:9-153): every unordered pair of the stencil once, bin
+// floor(r / dr) when below nbins.  Counts go to a block histogram in shared memory (nbins <= smem_bins)
+// or straight to global memory.
+template <class real>
+__global__ void pair_hist_kernel(PairGrid g, Buffers<real> in, const int *start, const int *members, double dr,
+                                 int nbins, int smem_bins, unsigned long long *hist) {
+    extern __shared__ unsigned long long hs[];
+    const bool local = nbins <= smem_bins;
+    if (local)
+        for (int b = threadIdx.x; b < nbins; b += blockDim.x) hs[b] = 0ull;
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
+        const int s = g.off + i;
+        const int li = in.ident[s] - g.off;
+        double xi[3];
+        load_pos_d<real>(in.pos, s, xi);
+        const int cx = pair_axis_cell(xi[0], g.nc, g.box), cy = pair_axis_cell(xi[1], g.nc, g.box),
+                  cz = pair_axis_cell(xi[2], g.nc, g.box);
+        const int lo = g.nc >= 3 ? -1 : 0, hi = g.nc >= 2 ? 1 : 0;
+        for (int dz = lo; dz <= hi; dz++)
+            for (int dy = lo; dy <= hi; dy++)
+                for (int dx = lo; dx <= hi; dx++) {
+                    int a = (cx + dx + g.nc) % g.nc, b = (cy + dy + g.nc) % g.nc, c = (cz + dz + g.nc) % g.nc;
+                    int cell = a + g.nc * (b + g.nc * c);
+                    for (int q = start[cell]; q < start[cell + 1]; q++) {
+                        const int t = members[q];
+                        if (in.ident[t] - g.off <= li) continue;
+                        double xj[3];
+                        load_pos_d<real>(in.pos, t, xj);
+                        const double r = cube_distance(xi, xj, g.box, g.periodic);
+                        const double f = floor(__ddiv_rn(r, dr));
+                        if (f < (double)nbins) {
+                            const int bin = (int)f;
+                            if (local) atomicAdd(hs + bin, 1ull);
+                            else atomicAdd(hist + bin, 1ull);
+                        }
+                    }
+                }
+    }
+    __syncthreads();
+    if (local)
+        for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+            if (hs[b]) atomicAdd(hist + b, hs[b]);
+}
+
+// Connected components of the pairs closer than g.rc (distance_graph, AnalyzeGrowth.cpp:136-171) by
+// union-find over local indices: a root is only ever hooked under a smaller root (compare-and-swap on
+// the root's entry), so parent[i] <= i, every walk ends, and a component's final root is its smallest
+// index -- the label ConnectedComponentsParallel_Old (GraphAlgorithms.cpp:672-800) converges to.
+__device__ __forceinline__ int uf_find(const int *parent, int a, int limit, bool &ok) {
+    for (int it = 0; it < limit; it++) {
+        const int p = *(const volatile int *)(parent + a);
+        if (p == a) return a;
+        a = p;
+    }
+    ok = false;
+    return a;
+}
+
+__global__ void uf_init_kernel(int n, int *parent) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) parent[i] = i;
+}
+
+template <class real>
+__global__ void uf_hook_kernel(PairGrid g, Buffers<real> in, const int *start, const int *members, int *parent,
+                               unsigned *flags) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
+        const int s = g.off + i;
+        const int li = in.ident[s] - g.off;
+        bool ok = true;
+        pair_visit<real>(g, in, start, members, s, li, [&](int lj) {
+            int u = li, v = lj;
+            for (int it = 0; it <= g.n && ok; it++) {
+                u = uf_find(parent, u, g.n + 1, ok);
+                v = uf_find(parent, v, g.n + 1, ok);
+                if (u == v) break;
+                if (u < v) { const int t = u; u = v; v = t; }
+                const int old = atomicCAS(parent + u, u, v);
+                if (old == u) break;
+                u = old;
+            }
+        });
+        if (!ok) atomicOr(flags, 4u);
+    }
+}
+
+__global__ void uf_label_kernel(int n, const int *parent, int32_t *labels, unsigned *flags) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        bool ok = true;
+        labels[i] = uf_find(parent, i, n + 1, ok);
+        if (!ok) atomicOr(flags, 4u);
+    }
+}
+
 }  // namespace
 }  // namespace mtg

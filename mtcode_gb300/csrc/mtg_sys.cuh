@@ -6,6 +6,7 @@
 #pragma once
 
 #include <algorithm>
+#include <memory>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -786,6 +787,96 @@ struct Sys : SysBase {
         }
         cleanup();
         return result;
+    }
+
+    // one replica binned on a grid of side >= rc (the analysis passes); frees its device arrays
+    struct ReplicaCells {
+        mtg::PairGrid grid{};
+        int ncell = 0;
+        int2 *bin = nullptr;
+        int *count = nullptr, *start = nullptr, *mem = nullptr, *block = nullptr;
+        ~ReplicaCells() { cudaFree(bin); cudaFree(count); cudaFree(start); cudaFree(mem); cudaFree(block); }
+    };
+
+    void bin_replica(int replica, double rc, ReplicaCells &c) {
+        const mtg_replica_desc &d = desc[replica];
+        const int nc = std::max(1, (int)std::floor(d.box / (rc * (1 + 1e-12))));
+        c.ncell = nc * nc * nc;
+        const int n = d.n;
+        size_t nn = (size_t)std::max(n, 1);
+        MTG_CUDA(cudaMalloc(&c.bin, sizeof(int2) * nn));
+        MTG_CUDA(cudaMalloc(&c.count, sizeof(int) * (c.ncell + 1)));
+        MTG_CUDA(cudaMalloc(&c.start, sizeof(int) * (c.ncell + 1)));
+        MTG_CUDA(cudaMalloc(&c.mem, sizeof(int) * nn));
+        const int nb = std::max(1, (c.ncell + mtg::kScanTile - 1) / mtg::kScanTile);
+        MTG_CUDA(cudaMalloc(&c.block, sizeof(int) * (nb + 1)));
+        MTG_CUDA(cudaMemsetAsync(c.count, 0, sizeof(int) * (c.ncell + 1), st));
+        c.grid = mtg::PairGrid{rep_slot[replica], n, nc, d.box, (double)nc / d.box, d.periodic ? 1 : 0, rc};
+        const int g = grid_for(n, 256, occ_stream, sms);
+        mtg::pair_bin_kernel<real><<<g, 256, 0, st>>>(c.grid, buf[cur], c.bin, c.count);
+        mtg::scan_reduce_kernel<<<nb, mtg::kScanThreads, 0, st>>>(c.count, c.ncell, c.block);
+        mtg::scan_top_kernel<<<1, mtg::kScanThreads, 0, st>>>(c.block, nb, c.start, c.ncell, d_draw, 0);
+        mtg::scan_down_kernel<<<nb, mtg::kScanThreads, 0, st>>>(c.count, c.ncell, c.block, c.start);
+        mtg::pair_fill_kernel<<<g, 256, 0, st>>>(c.grid, c.bin, c.start, c.mem);
+        check_launch();
+        nlaunch += 5;
+    }
+
+    // calcg1 (Analysis/PairCorrelation.cpp:9-153) for one replica
+    void gr(int replica, double rmax, double dr, int64_t *hist, int cap, int *nbins) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_gr: no state has been set"};
+        MTG_REQUIRE(replica >= 0 && replica < nrep, "mtg_gr: replica out of range");
+        MTG_REQUIRE(nbins && std::isfinite(rmax) && std::isfinite(dr) && rmax > 0 && dr > 0,
+                    "mtg_gr: rmax and dr must be positive and nbins non-null");
+        MTG_REQUIRE(rmax <= desc[replica].box, "mtg_gr: rmax must not exceed the box side (calcg1 needs a cell)");
+        const double nbd = std::floor(rmax / dr);
+        MTG_REQUIRE(nbd <= 1e8, "mtg_gr: more than 1e8 bins");
+        const int nb = (int)nbd;
+        *nbins = nb;
+        if (!hist || nb == 0) return;
+        MTG_REQUIRE(cap >= nb, "mtg_gr: hist holds fewer than floor(rmax / dr) bins");
+        ReplicaCells c;
+        bin_replica(replica, rmax, c);
+        unsigned long long *dh = nullptr;
+        MTG_CUDA(cudaMalloc(&dh, sizeof(unsigned long long) * nb));
+        std::unique_ptr<void, void (*)(void *)> guard(dh, [](void *q) { cudaFree(q); });
+        MTG_CUDA(cudaMemsetAsync(dh, 0, sizeof(unsigned long long) * nb, st));
+        const int smem_bins = 4096;  // 32 KB of block histogram
+        const int g = grid_for(desc[replica].n, 256, 1, sms);
+        mtg::pair_hist_kernel<real><<<g, 256, nb <= smem_bins ? sizeof(unsigned long long) * nb : 0, st>>>(
+            c.grid, buf[cur], c.start, c.mem, dr, nb, smem_bins, dh);
+        check_launch();
+        nlaunch += 1;
+        std::vector<unsigned long long> h((size_t)nb);
+        MTG_CUDA(cudaMemcpyAsync(h.data(), dh, sizeof(unsigned long long) * nb, cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+        for (int b = 0; b < nb; b++) hist[b] = (int64_t)h[(size_t)b];
+    }
+
+    // distance_graph (Analysis/AnalyzeGrowth.cpp:136-171) for one replica: smallest local index of each
+    // particle's connected component, pairs closer than cut
+    void clusters(int replica, double cut, int32_t *labels) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_clusters: no state has been set"};
+        MTG_REQUIRE(replica >= 0 && replica < nrep, "mtg_clusters: replica out of range");
+        MTG_REQUIRE(labels && std::isfinite(cut) && cut > 0, "mtg_clusters: cut must be positive and labels non-null");
+        const int n = desc[replica].n;
+        ReplicaCells c;
+        bin_replica(replica, cut, c);
+        int *parent = nullptr;
+        int32_t *dl = nullptr;
+        MTG_CUDA(cudaMalloc(&parent, sizeof(int) * (size_t)n));
+        std::unique_ptr<void, void (*)(void *)> g1(parent, [](void *q) { cudaFree(q); });
+        MTG_CUDA(cudaMalloc(&dl, sizeof(int32_t) * (size_t)n));
+        std::unique_ptr<void, void (*)(void *)> g2(dl, [](void *q) { cudaFree(q); });
+        const int g = grid_for(n, 256, occ_stream, sms);
+        mtg::uf_init_kernel<<<g, 256, 0, st>>>(n, parent);
+        mtg::uf_hook_kernel<real><<<g, 256, 0, st>>>(c.grid, buf[cur], c.start, c.mem, parent, d_flags);
+        mtg::uf_label_kernel<<<g, 256, 0, st>>>(n, parent, dl, d_flags);
+        check_launch();
+        nlaunch += 3;
+        MTG_CUDA(cudaMemcpyAsync(labels, dl, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+        if (flags() & MTG_FLAG_TIMEOUT) throw Fail{MTG_ERR_TIMEOUT, "mtg_clusters: a union-find walk exceeded its bound"};
     }
 
     void set_draw(uint64_t d) override { draw = d; }

@@ -254,6 +254,24 @@ class LangevinNVTRGPU:
     def flags(self) -> int:
         return int(_lib.lib().mtg_flags(self._h))
 
+    def gr(self, rmax: float, dr: float, replica: int = 0) -> np.ndarray:
+        """calcg1: counts of unordered pair distances of one replica in bins of dr below floor(rmax/dr)*dr."""
+        L = _lib.lib()
+        nb = C.c_int(0)
+        _check(self._h, L.mtg_gr(self._h, int(replica), float(rmax), float(dr), None, 0, C.byref(nb)))
+        out = np.zeros(nb.value, dtype=np.int64)
+        if nb.value:
+            _check(self._h, L.mtg_gr(self._h, int(replica), float(rmax), float(dr),
+                                     out.ctypes.data_as(C.POINTER(C.c_int64)), nb.value, C.byref(nb)))
+        return out
+
+    def clusters(self, cut: float, replica: int = 0) -> np.ndarray:
+        """distance_graph: per particle of one replica, the smallest local index of its connected
+        component in the graph of pairs closer than cut."""
+        out = np.empty(self.replicas[replica].n, dtype=np.int32)
+        _check(self._h, _lib.lib().mtg_clusters(self._h, int(replica), float(cut), out.ctypes.data_as(_lib._I32)))
+        return out
+
     def write_frame(self, directory, frame: int, runtime: int, every: int, strbase: str = "",
                     replica: int | None = None) -> tuple:
         """The pos / orientation frame files Condensate::run writes every `every` steps

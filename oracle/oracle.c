@@ -564,6 +564,53 @@ static long orc_pairs_alloc(const orc_params *P, const double *x, int ncell, dou
     return np;
 }
 
+/* cube::distance (geometry.h:107-121) */
+static double orc_distance(const orc_params *P, const double *x, int i, int j)
+{
+    double temp = 0.0;
+    for (int k = 0; k < 3; k++) {
+        double dx = x[3 * i + k] - x[3 * j + k];
+        if (P->periodic && fabs(dx) > P->box * 0.5) dx = dx - (dx >= 0.0 ? P->box : -P->box);
+        temp += dx * dx;
+    }
+    return sqrt(temp);
+}
+
+int orc_gr(const orc_params *P, const double *x, double max, double dx, long *hist, int cap)
+{
+    int gs = (int)floor(max / dx);
+    for (int b = 0; b < gs && b < cap; b++) hist[b] = 0;
+    /* every unordered pair once; only distances below gs * dx <= max land in a bin */
+    for (int i = 0; i < P->n; i++)
+        for (int j = i + 1; j < P->n; j++) {
+            int in = (int)floor(orc_distance(P, x, i, j) / dx);
+            if (in < gs && in < cap) hist[in] += 1;
+        }
+    return gs;
+}
+
+static int orc_find(int *parent, int a)
+{
+    while (parent[a] != a) a = parent[a];
+    return a;
+}
+
+void orc_clusters(const orc_params *P, const double *x, double cut, int *labels)
+{
+    int *pairs;
+    int ncell = (int)floor(P->box / cut);
+    if (ncell < 1) ncell = 1;
+    long np = orc_pairs_alloc(P, x, ncell, cut, &pairs);
+    for (int i = 0; i < P->n; i++) labels[i] = i;
+    for (long q = 0; q < np; q++) {  /* union by smaller root: a component's root is its smallest index */
+        int a = orc_find(labels, pairs[2 * q]), b = orc_find(labels, pairs[2 * q + 1]);
+        if (a < b) labels[b] = a;
+        else if (b < a) labels[a] = b;
+    }
+    for (int i = 0; i < P->n; i++) labels[i] = orc_find(labels, i);
+    free(pairs);
+}
+
 void orc_forces(const orc_params *P, const double *x, const double *Q, int ncell, double rc, double *F, double *T)
 {
     int *pairs;

@@ -109,6 +109,16 @@ void orc_philox_noise(int n, uint64_t seed, uint32_t replica, uint64_t draw, dou
 void orc_observables(const orc_params *P, const double *x, const double *Q, const int *pairs, long np,
                      double out[4]);
 
+/* calcg1(data, geo, max, dx) (MDBase/Analysis/PairCorrelation.cpp:9-153): histogram of the distances
+ * of all unordered pairs, cube::distance (geometry.h:107-121), bin floor(r / dx) for the
+ * floor(max / dx) bins.  Returns the bin count (hist receives at most cap bins). */
+int orc_gr(const orc_params *P, const double *x, double max, double dx, long *hist, int cap);
+/* distance_graph(pos, boxes, geo, cut, index_test) (MDBase/Analysis/AnalyzeGrowth.cpp:136-171):
+ * connected components of the graph of pairs closer than cut (the calculatepairs_parallel set);
+ * ConnectedComponentsParallel_Old (Bindings/GraphAlgorithms.cpp:672-800) converges to the smallest
+ * particle index of each component, which labels[i] receives. */
+void orc_clusters(const orc_params *P, const double *x, double cut, int *labels);
+
 /* Full forces as the driver computes them: F = (bond forces +) HS forces + patch forces;
  * T = patch torques (lab). */
 void orc_forces(const orc_params *P, const double *x, const double *Q, int ncell, double rc,

@@ -91,6 +91,9 @@ def orc() -> C.CDLL:
         L.orc_hs_forces.argtypes = [P, _D, _I, C.c_long, _D]
         L.orc_bond_forces.argtypes = [P, _D, _I, C.c_long, C.c_double, C.c_double, _D]
         L.orc_central_forces.argtypes = [P, _D, _I, C.c_long, _D]
+        L.orc_gr.restype = C.c_int
+        L.orc_gr.argtypes = [P, _D, C.c_double, C.c_double, C.POINTER(C.c_long), C.c_int]
+        L.orc_clusters.argtypes = [P, _D, C.c_double, _I]
         L.orc_patch_forces.argtypes = [P, _D, _D, _I, C.c_long, _D, _D]
         L.orc_observables.argtypes = [P, _D, _D, _I, C.c_long, _D]
         L.orc_neighbor_cells.restype = C.c_int
@@ -137,6 +140,20 @@ class System:
         self._bonds = np.ascontiguousarray(bonds, dtype=np.intc).reshape(-1, 2)
         p.bonds = self._bonds.ctypes.data_as(_I)
         p.nbonds, p.bond_k, p.bond_r0 = len(self._bonds), float(k), float(r0)
+
+    def gr(self, x, rmax: float, dr: float) -> np.ndarray:
+        """calcg1: counts of unordered pair distances in bins of dr below floor(rmax / dr) * dr."""
+        nb = int(math.floor(rmax / dr))
+        out = np.zeros(max(nb, 1), dtype=np.int64)
+        orc().orc_gr(C.byref(self.params), _d(np.ascontiguousarray(x, float)), float(rmax), float(dr),
+                     out.ctypes.data_as(C.POINTER(C.c_long)), len(out))
+        return out[:nb]
+
+    def clusters(self, x, cut: float) -> np.ndarray:
+        """distance_graph: per particle the smallest index of its connected component (pairs closer than cut)."""
+        out = np.empty(self.spec.n, dtype=np.intc)
+        orc().orc_clusters(C.byref(self.params), _d(np.ascontiguousarray(x, float)), float(cut), out.ctypes.data_as(_I))
+        return out
 
     def bond_forces(self, x, bonds, k: float, r0: float) -> np.ndarray:
         b = np.ascontiguousarray(bonds, dtype=np.intc).reshape(-1, 2)
@@ -244,6 +261,10 @@ def ref() -> C.CDLL | None:
                               C.c_int, _D, _D]
         L.ref_rotation_matrix.argtypes = [C.c_double, _D, _D]
         L.ref_bond_forces.argtypes = [C.c_int, C.c_double, C.c_int, _D, _I, C.c_long, C.c_double, C.c_double, _D]
+        L.ref_calcg1.restype = C.c_long
+        L.ref_calcg1.argtypes = [C.c_int, C.c_double, C.c_int, _D, C.c_double, C.c_double, C.POINTER(C.c_long),
+                                 C.c_long]
+        L.ref_distance_graph.argtypes = [C.c_int, C.c_double, C.c_int, _D, C.c_double, _I]
         L.ref_write_csv.argtypes = [C.c_char_p, _D, C.c_int, C.c_int]
         L.ref_import_csv.restype = C.c_long
         L.ref_import_csv.argtypes = [C.c_char_p, _D, C.c_long, C.POINTER(C.c_int)]

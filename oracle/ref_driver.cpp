@@ -248,6 +248,32 @@ long ref_import_csv(const char *path, double *out, long cap, int *cols)
     return nr;
 }
 
+// calcg1 (MDBase/Analysis/PairCorrelation.cpp:9-153): returns the bin count, hist receives <= cap bins
+long ref_calcg1(int n, double box, int periodic, const double *x, double max, double dx, long *hist, long cap)
+{
+    vector1<bool> pb(3, periodic != 0);
+    cube geo(box, pb, 3);
+    matrix<double> X = to_mat(x, n, 3);
+    vector1<int> g = calcg1(X, geo, max, dx);
+    long m = g.getsize();
+    for (long i = 0; i < m && i < cap; i++) hist[i] = g[i];
+    return m;
+}
+
+// distance_graph (MDBase/Analysis/AnalyzeGrowth.cpp:136-171) on cells of side >= cut, every pair kept
+void ref_distance_graph(int n, double box, int periodic, const double *x, double cut, int *labels)
+{
+    vector1<bool> pb(3, periodic != 0);
+    cube geo(box, pb, 3);
+    matrix<double> X = to_mat(x, n, 3);
+    int ccc;
+    int num = (int)floor(box / cut);
+    matrix<int> boxes = geo.generate_boxes_relationships(num, ccc);
+    index_test all;
+    vector1<int> lab = distance_graph(X, boxes, geo, cut, &all);
+    for (int i = 0; i < n; i++) labels[i] = lab[i];
+}
+
 // Condensate::run loop body (Condensate.cpp:335-378), nsteps times.  Pairs are rebuilt from the
 // positions at the start of a step every `rebuild` steps (the driver uses 20 at rc 3.5).
 // noise: nsteps x n x 6 values used in place of generate_uniform_random_matrix, or NULL for zeros.

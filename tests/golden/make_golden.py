@@ -129,6 +129,22 @@ def frame_cases():
           f"shapes {[p.shape for p in parsed]}")
 
 
+def analysis_cases():
+    """H. analysis: calcg1 histograms and distance_graph component labels from the reference."""
+    cases = [(2000, 0.30, True, 4.0, 0.05, 1.25), (900, 0.20, False, 3.0, 0.02, 1.1), (400, 0.05, True, 5.0, 0.1, 1.6)]
+    for k, (n, phi, per, rmax, dr, cut) in enumerate(cases):
+        spec, x, _ = make_system("tetra", n, phi, 700 + k, per)
+        h = np.zeros(100000, dtype=np.int64)
+        m = po.ref().ref_calcg1(n, spec.box, int(per), D(x), rmax, dr, h.ctypes.data_as(po.C.POINTER(po.C.c_long)),
+                                len(h))
+        labels = np.empty(n, dtype=np.intc)
+        po.ref().ref_distance_graph(n, spec.box, int(per), D(x), cut, labels.ctypes.data_as(po._I))
+        np.savez_compressed(HERE / f"analysis_{k}.npz", x=x, rmax=rmax, dr=dr, hist=h[:m].copy(), cut=cut,
+                            labels=labels, **spec_record(spec))
+        print(f"analysis_{k}: n={n} periodic={per} bins={m} pairs<rmax={h[:m].sum()} "
+              f"components={len(np.unique(labels))} largest={np.bincount(labels).max()}")
+
+
 def ref_run(spec, st, nsteps, rc, rebuild, noise=None, init=True, noise0=None):
     R = po.ref()
     kind, att, dis, th, nt, ppt, npt, orient, params = po.ref_model_args(spec.model)
@@ -216,7 +232,7 @@ def spec_record(spec):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
-    ap.add_argument("--only", choices=["bonded", "frames"], help="regenerate one group of fixtures only")
+    ap.add_argument("--only", choices=["bonded", "frames", "analysis"], help="regenerate one group of fixtures only")
     args = ap.parse_args()
     po.build_oracle()
     po.build_ref(args.reference)
@@ -226,6 +242,9 @@ def main():
         return
     if args.only == "frames":
         frame_cases()
+        return
+    if args.only == "analysis":
+        analysis_cases()
         return
 
     # ---- A. pair sets (MD::calculatepairs and calculatepairs_parallel)
@@ -314,6 +333,7 @@ def main():
 
     bonded_cases()
     frame_cases()
+    analysis_cases()
 
 
 if __name__ == "__main__":

@@ -150,3 +150,12 @@ def test_bond_forces_live_vs_reference():
     po.ref().ref_bond_forces(spec.n, spec.box, 1, po._d(np.ascontiguousarray(x)), b.ctypes.data_as(po._I), len(b),
                              37.0, 1.1, po._d(Fr))
     assert np.array_equal(F, Fr)
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_analysis_matches_reference(k):
+    """calcg1 histogram and distance_graph labels: integer results, equal to the reference's."""
+    d = load(f"analysis_{k}.npz")
+    sysm = po.System(spec_from(d))
+    assert np.array_equal(sysm.gr(d["x"], float(d["rmax"]), float(d["dr"])), d["hist"])
+    assert np.array_equal(sysm.clusters(d["x"], float(d["cut"])), d["labels"])
