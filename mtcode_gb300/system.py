@@ -268,7 +268,8 @@ class LangevinNVTRGPU:
     def clusters(self, cut: float, replica: int = 0) -> np.ndarray:
         """distance_graph: per particle of one replica, the smallest local index of its connected
         component in the graph of pairs closer than cut."""
-        out = np.empty(self.replicas[replica].n, dtype=np.int32)
+        n = self.replicas[replica].n if 0 <= replica < len(self.replicas) else 1  # the library rejects the rest
+        out = np.empty(n, dtype=np.int32)
         _check(self._h, _lib.lib().mtg_clusters(self._h, int(replica), float(cut), out.ctypes.data_as(_lib._I32)))
         return out
 

@@ -70,7 +70,7 @@ def test_frames_from_a_running_system(tmp_path):
         s.step(20)
         pos_path, ori_path = s.write_frame(tmp_path, 2, 100, 10, replica=1)
         st = s.get_state()
-    assert pos_path.name == "pos_i=002.csv" and ori_path.name == "orientation_i=002.csv"
+    assert pos_path.name == "pos_i=02.csv" and ori_path.name == "orientation_i=02.csv"  # ceil(100/10): 2 digits
     xr, Qr = read_csv(pos_path), read_csv(ori_path)
     assert np.allclose(xr, st["x"][n:], rtol=5e-6, atol=1e-12)
     assert np.allclose(Qr, st["Q"][n:], rtol=5e-6, atol=1e-6)
