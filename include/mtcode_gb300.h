@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define MTG_API_VERSION 1
+#define MTG_API_VERSION 2
 
 typedef enum {
     MTG_OK = 0,
@@ -97,6 +97,12 @@ typedef struct {
     int track_displacement;            /* 1: keep FP64 unwrapped-displacement accumulators */
     int force_kernel;                  /* FP32 only: 0 = tiled shared-memory kernel (default),
                                           1 = one thread per particle (the form the FP64 path uses) */
+    double neighbor_skin;              /* 0 (default): the cell list is rebuilt every step.  > 0: Verlet
+                                          skin (sigma): cells and per-particle candidate lists are built at
+                                          force range + skin and reused until some particle has moved more
+                                          than skin / 2 since the build -- the reference's pair reuse
+                                          (Condensate.cpp:344-350) with an exactness check instead of a
+                                          fixed 20-step schedule.  The force set is the same either way. */
 } mtg_config;
 
 /* Fill `m` with TetrahedralPatch(att, dis, thetam) / BivalentPatch(att, dis, thetam). */
@@ -203,9 +209,15 @@ int64_t mtg_launch_count(const mtg_system *h);
 /* Instrumented steps: nsteps of mtg_step launched one kernel at a time (no graph) with CUDA events
  * around every launch on the handle's stream.  kernel_ms[k] receives the summed device time of
  * kernel k over the nsteps, for k = 0 scan_reduce, 1 scan_top, 2 scan_down, 3 scatter (reorder +
- * first half-step), 4 force (force/torque + Langevin epilogue + next binning).  Synchronising. */
+ * first half-step), 4 force (force/torque + Langevin epilogue + next binning).  With a neighbour skin:
+ * 0 = rebuild decision + binning + scan_reduce, 1 scan_top, 2 scan_down, 3 scatter + copy-back (rebuild
+ * steps) + in-place first half-step (other steps), 4 force.  Synchronising. */
 #define MTG_PROFILE_KERNELS 5
 mtg_status mtg_step_profile(mtg_system *h, int nsteps, double *kernel_ms);
+
+/* With a neighbour skin: list rebuilds since mtg_create (each initial force pass and each step that
+ * rebuilt); 0 without a skin.  Synchronising. */
+int64_t mtg_neighbor_rebuilds(mtg_system *h);
 
 /* Text of the last error on this handle (or of the last failed mtg_create when h is NULL). */
 const char *mtg_last_error(const mtg_system *h);

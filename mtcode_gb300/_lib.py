@@ -68,6 +68,7 @@ class Config(C.Structure):
         ("device", C.c_int),
         ("track_displacement", C.c_int),
         ("force_kernel", C.c_int),
+        ("neighbor_skin", C.c_double),
     ]
 
 
@@ -93,6 +94,7 @@ SIGNATURES = [
     ("mtg_step_noise", C.c_int, [_H, C.c_int, _D]),
     ("mtg_forces", C.c_int, [_H, _D, _D, _D]),
     ("mtg_set_bonds", C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_int64, C.c_double, C.c_double]),
+    ("mtg_neighbor_rebuilds", C.c_int64, [_H]),
     ("mtg_gr", C.c_int, [_H, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_int64), C.c_int, C.POINTER(C.c_int)]),
     ("mtg_clusters", C.c_int, [_H, C.c_int, C.c_double, _I32]),
     ("mtg_pairs", C.c_int, [_H, C.c_int, C.c_double, _I32, C.c_int64, C.POINTER(C.c_int64)]),

@@ -159,6 +159,8 @@ mtg_status mtg_create(const mtg_config *cfg, mtg_system **out) {
             if (d.model.n_types == 1 && d.model.count_per_type[0] == 0) d.model.count_per_type[0] = d.n;
             check_model(d.model, d.n);
         }
+        MTG_REQUIRE(std::isfinite(cfg->neighbor_skin) && cfg->neighbor_skin >= 0 && cfg->neighbor_skin <= 10,
+                    "mtg_create: neighbor_skin must lie in [0, 10] sigma");
         mtg_config c = *cfg;
         c.replicas = reps.data();
         std::unique_ptr<mtg_system> h(new mtg_system);
@@ -204,6 +206,17 @@ mtg_status mtg_init_forces_noise(mtg_system *h, const double *noise) {
 mtg_status mtg_set_bonds(mtg_system *h, const int32_t *bonds, int64_t nbonds, double k, double r0) {
     MTG_GUARD(h, h->impl->set_bonds(bonds, nbonds, k, r0));
     return MTG_OK;
+}
+
+int64_t mtg_neighbor_rebuilds(mtg_system *h) {
+    if (!h) return 0;
+    try {
+        cudaSetDevice(h->device);
+        return h->impl->rebuilds();
+    } catch (const Fail &f) {
+        h->err = f.msg;
+        return 0;
+    }
 }
 
 mtg_status mtg_gr(mtg_system *h, int replica, double rmax, double dr, int64_t *hist, int cap, int *nbins) {

@@ -42,6 +42,8 @@ struct Replica {
     real max_dist2;            // LangevinNVTR::max_distance_check
     real rc2;                  // squared force range (max of HS range and patch range)
     real patch_r2;             // squared range of any patch force: min(max_dist2, (1.4 dis_max)^2)
+    real rc2_list;             // skin lists: squared list range (force range + skin, padded for rounding)
+    real half_skin2;           // skin lists: (skin / 2)^2, the displacement that forces a rebuild
     real bond_r;               // ComboPatch::max_check
 };
 

@@ -27,7 +27,16 @@ struct Buffers {
     double *dx, *dy, *dz;  // unwrapped displacement (nullable)
     int *slot_of;          // global index -> slot of the buffer in use (shared by both buffers; nullable,
                            // kept only when bonds are set)
+    real *xref;            // skin lists: position of each slot at the last list build (4 reals), shared
+    int *home_cell;        // skin lists: cell of each slot at the last list build, shared
 };
+
+// Skin-list state (int[4], device): [0] this step rebuilds, [1] a particle will have moved more than half
+// the skin by the next step, [2] rebuild requested by the host, [3] rebuilds so far
+constexpr int kListCap = 32;  // candidates kept per particle; a longer list marks the particle overflowed
+
+// a kernel on a skin-list step runs when the step's rebuild flag equals `want` (always without a gate)
+__device__ __forceinline__ bool gated_off(const int *gate, int want) { return gate && *gate != want; }
 
 template <class real>
 struct Tables {
@@ -84,7 +93,8 @@ __device__ __forceinline__ int aggregated_rank(int *count, int key) {
 // ------------------------------------------------------------------ bin (standalone)
 template <class real, bool MOVE>
 __global__ void __launch_bounds__(256) bin_kernel(Tables<real> tb, Buffers<real> in, int2 *bin, int *count,
-                                                  unsigned *flags) {
+                                                  unsigned *flags, const int *gate = nullptr) {
+    if (gated_off(gate, 1)) return;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
         const int r = find_replica(tb.rep_slot, tb.nrep, s);
         const Replica<real> R = tb.reps[r];
@@ -139,7 +149,9 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_sums, int &
     return excl;
 }
 
-__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const int *count, int n, int *block_sums) {
+__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const int *count, int n, int *block_sums,
+                                                                   const int *gate = nullptr) {
+    if (gated_off(gate, 1)) return;
     __shared__ int ws[33];
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     int s = 0;
@@ -152,7 +164,9 @@ __global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const int *co
 
 // single block: exclusive scan of the block sums; also advances the noise draw counter
 __global__ void __launch_bounds__(kScanThreads) scan_top_kernel(int *block_sums, int nblocks, int *start, int n,
-                                                                unsigned long long *draw, int consume_draw) {
+                                                                unsigned long long *draw, int consume_draw,
+                                                                const int *gate = nullptr) {
+    if (gated_off(gate, 1)) return;
     __shared__ int ws[33];
     int carry = 0;
     for (int b0 = 0; b0 < nblocks; b0 += kScanThreads) {
@@ -173,7 +187,8 @@ __global__ void __launch_bounds__(kScanThreads) scan_top_kernel(int *block_sums,
 }
 
 __global__ void __launch_bounds__(kScanThreads) scan_down_kernel(int *count, int n, const int *block_sums,
-                                                                 int *start) {
+                                                                 int *start, const int *gate = nullptr) {
+    if (gated_off(gate, 1)) return;
     __shared__ int ws[33];
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     int v[kScanItems];
@@ -240,9 +255,46 @@ __device__ __forceinline__ void free_rotor(real dt, real inertia, const real L[3
     for (int k = 0; k < 9; k++) R[k] = M[k];
 }
 
+// First half of the step for one particle (advancemom_halfstep, advance_pos, rotate: LangevinR.cpp:327-347,
+// Langevin.cpp:205-222, LangevinR.cpp:594-695): half-kick with the carried F~/T~, drift + wrap/reflect,
+// free-rotor rotation.  step receives the unwrapped drift (c1 * p_half) for the displacement sums.
+template <class real>
+__device__ __forceinline__ void advance_particle(const Replica<real> &R, Payload<real> &P, Row<real> &M, real step[3],
+                                                 unsigned *flags) {
+    real x[3] = {P.v[0], P.v[1], P.v[2]}, p[3] = {M.v[0], M.v[1], M.v[2]};
+    real F[3] = {M.v[6], M.v[7], M.v[8]};
+    real L[3] = {M.v[3], M.v[4], M.v[5]}, T[3] = {M.v[9], M.v[10], M.v[11]};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        real ph = add_rn(p[k], mul_rn(R.half_dt, F[k]));
+        step[k] = mul_rn(R.c1, ph);
+    }
+    drift_position<real>(R, x, p, F);  // identical arithmetic to the binning pass
+    if (!(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]))) atomicOr(flags, 1u);
+#pragma unroll
+    for (int k = 0; k < 3; k++) L[k] = L[k] + R.half_dt * T[k];
+    real Rm[9];
+    free_rotor<real>(R.dt, R.inertia, L, Rm);
+    real Ln[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) Ln[a] = L[0] * Rm[3 * a] + L[1] * Rm[3 * a + 1] + L[2] * Rm[3 * a + 2];
+    // Q <- R^T Q (LangevinR.cpp:611-683)
+    real Q[9] = {P.v[3], P.v[4], P.v[5], P.v[6], P.v[7], P.v[8], P.v[9], P.v[10], P.v[11]};
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++)
+            P.v[3 + 3 * a + b] = Q[b] * Rm[a] + Q[3 + b] * Rm[3 + a] + Q[6 + b] * Rm[6 + a];
+    P.v[0] = x[0]; P.v[1] = x[1]; P.v[2] = x[2];
+    M.v[0] = p[0]; M.v[1] = p[1]; M.v[2] = p[2];
+    M.v[3] = Ln[0]; M.v[4] = Ln[1]; M.v[5] = Ln[2];
+}
+
 template <class real, bool MOVE>
 __global__ void __launch_bounds__(256) scatter_kernel(Tables<real> tb, Buffers<real> in, Buffers<real> out,
-                                                      const int2 *bin, const int *start, unsigned *flags) {
+                                                      const int2 *bin, const int *start, unsigned *flags,
+                                                      const int *gate = nullptr) {
+    if (gated_off(gate, 1)) return;
     // every particle must have been binned exactly once; otherwise nothing is moved (latched error)
     if (__ldg(start + tb.ncells) != tb.ntot) {
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(flags, 16u);
@@ -263,39 +315,13 @@ __global__ void __launch_bounds__(256) scatter_kernel(Tables<real> tb, Buffers<r
         if (MOVE) {
             const int r = find_replica(tb.rep_slot, tb.nrep, s);
             const Replica<real> R = tb.reps[r];
-            real x[3] = {P.v[0], P.v[1], P.v[2]}, p[3] = {M.v[0], M.v[1], M.v[2]};
-            real F[3] = {M.v[6], M.v[7], M.v[8]};
-            real L[3] = {M.v[3], M.v[4], M.v[5]}, T[3] = {M.v[9], M.v[10], M.v[11]};
             real step[3];
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                real ph = add_rn(p[k], mul_rn(R.half_dt, F[k]));
-                step[k] = mul_rn(R.c1, ph);
-            }
-            drift_position<real>(R, x, p, F);  // identical arithmetic to the binning pass
-            if (!(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]))) atomicOr(flags, 1u);
+            advance_particle<real>(R, P, M, step, flags);
             if (in.dx) {
                 out.dx[d] = in.dx[s] + (double)step[0];
                 out.dy[d] = in.dy[s] + (double)step[1];
                 out.dz[d] = in.dz[s] + (double)step[2];
             }
-#pragma unroll
-            for (int k = 0; k < 3; k++) L[k] = L[k] + R.half_dt * T[k];
-            real Rm[9];
-            free_rotor<real>(R.dt, R.inertia, L, Rm);
-            real Ln[3];
-#pragma unroll
-            for (int a = 0; a < 3; a++) Ln[a] = L[0] * Rm[3 * a] + L[1] * Rm[3 * a + 1] + L[2] * Rm[3 * a + 2];
-            // Q <- R^T Q (LangevinR.cpp:611-683)
-            real Q[9] = {P.v[3], P.v[4], P.v[5], P.v[6], P.v[7], P.v[8], P.v[9], P.v[10], P.v[11]};
-#pragma unroll
-            for (int a = 0; a < 3; a++)
-#pragma unroll
-                for (int b = 0; b < 3; b++)
-                    P.v[3 + 3 * a + b] = Q[b] * Rm[a] + Q[3 + b] * Rm[3 + a] + Q[6 + b] * Rm[6 + a];
-            P.v[0] = x[0]; P.v[1] = x[1]; P.v[2] = x[2];
-            M.v[0] = p[0]; M.v[1] = p[1]; M.v[2] = p[2];
-            M.v[3] = Ln[0]; M.v[4] = Ln[1]; M.v[5] = Ln[2];
         } else if (in.dx) {
             out.dx[d] = in.dx[s];
             out.dy[d] = in.dy[s];
@@ -305,6 +331,80 @@ __global__ void __launch_bounds__(256) scatter_kernel(Tables<real> tb, Buffers<r
         M.store(out.motion + (size_t)d * kRow);
         out.ident[d] = id;
         if (out.slot_of) out.slot_of[id] = d;
+        if (out.xref) {
+            out.xref[4 * (size_t)d] = P.v[0];
+            out.xref[4 * (size_t)d + 1] = P.v[1];
+            out.xref[4 * (size_t)d + 2] = P.v[2];
+            out.home_cell[d] = kb.x;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ skin-list steps
+
+// decides whether this step rebuilds the lists, and takes the step's noise draw (draw[0] <- draw[1]++)
+__global__ void skin_decide_kernel(int *skin, unsigned long long *draw) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const int rebuild = (skin[1] | skin[2]) ? 1 : 0;
+        skin[0] = rebuild;
+        skin[1] = 0;
+        skin[2] = 0;
+        skin[3] += rebuild;
+        draw[0] = draw[1];
+        draw[1] = draw[1] + 1ull;
+    }
+}
+
+__global__ void skin_set_kernel(int *skin, int now, int next, int forced) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        if (now >= 0) skin[0] = now;
+        if (next >= 0) skin[1] = next;
+        if (forced >= 0) skin[2] = forced;
+    }
+}
+
+// the first half of the step in place (no re-sort) on steps that keep their lists
+template <class real>
+__global__ void __launch_bounds__(256) integrate_kernel(Tables<real> tb, Buffers<real> b, unsigned *flags,
+                                                        const int *gate) {
+    if (gated_off(gate, 0)) return;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
+        Payload<real> P;
+        Row<real> M;
+        P.load(b.pos, b.rota, b.rotb, s);
+        M.load(b.motion + (size_t)s * kRow);
+        const int r = find_replica(tb.rep_slot, tb.nrep, s);
+        const Replica<real> R = tb.reps[r];
+        real step[3];
+        advance_particle<real>(R, P, M, step, flags);
+        if (b.dx) {
+            b.dx[s] += (double)step[0];
+            b.dy[s] += (double)step[1];
+            b.dz[s] += (double)step[2];
+        }
+        P.store(b.pos, b.rota, b.rotb, s);
+        M.store(b.motion + (size_t)s * kRow);
+    }
+}
+
+// after a rebuild's scatter into the spare buffer, the sorted state goes back to the buffer in use
+template <class real>
+__global__ void __launch_bounds__(256) copy_back_kernel(int ntot, Buffers<real> from, Buffers<real> to,
+                                                        const int *gate) {
+    if (gated_off(gate, 1)) return;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ntot; s += gridDim.x * blockDim.x) {
+        Payload<real> P;
+        Row<real> M;
+        P.load(from.pos, from.rota, from.rotb, s);
+        M.load(from.motion + (size_t)s * kRow);
+        P.store(to.pos, to.rota, to.rotb, s);
+        M.store(to.motion + (size_t)s * kRow);
+        to.ident[s] = from.ident[s];
+        if (from.dx) {
+            to.dx[s] = from.dx[s];
+            to.dy[s] = from.dy[s];
+            to.dz[s] = from.dz[s];
+        }
     }
 }
 
@@ -327,7 +427,25 @@ struct ForceArgs {
     // null when the system has none.  HarmonicPotential(bond_k, bond_r0).
     const int *bond_start, *bond_partner;
     real bond_k, bond_r0;
+    // skin lists (null without): rebuild flag of this step, the next step's flag, candidate lists
+    // (list[t * ntot + slot], kListCap per slot) and their lengths by slot
+    const int *skin;
+    int *skin_next;
+    unsigned *list;
+    int *list_n;
 };
+
+// skin lists: flags the next step for a rebuild when slot s's next position (xn) is more than half the
+// skin away from where it was at the last build (minimum image)
+template <class real>
+__device__ __forceinline__ void skin_check(const ForceArgs<real> &a, const Replica<real> &R, int s, const real xn[3]) {
+    real xr, yr, zr;
+    load_pos(a.buf.xref + 4 * (size_t)s, xr, yr, zr);
+    const real dx = min_image<real>(xn[0] - xr, R.box, R.l2s, R.periodic);
+    const real dy = min_image<real>(xn[1] - yr, R.box, R.l2s, R.periodic);
+    const real dz = min_image<real>(xn[2] - zr, R.box, R.l2s, R.periodic);
+    if (!(dx * dx + dy * dy + dz * dz <= R.half_skin2)) *a.skin_next = 1;
+}
 
 // Harmonic bonds of particle idi at (xi, yi, zi): HarmonicPotential::force (potential.h:274-276),
 // f = -k (r - r0), along the minimum-image separation, as MD::calculateforces applies it to a bond list
@@ -382,9 +500,23 @@ __device__ __noinline__ void simple_particle(const ForceArgs<real> &a, int s) {
         bool big = false;
 
         const int nc = R.nc;
-        const int cx = axis_cell<real>(xi, R.cell_scale, nc);
-        const int cy = axis_cell<real>(yi, R.cell_scale, nc);
-        const int cz = axis_cell<real>(zi, R.cell_scale, nc);
+        int cx, cy, cz;
+        if (a.skin && MODE != kModeObs) {
+            // skin lists: the cell the slot was sorted into at the last build; particles have moved less
+            // than half the skin since, so its stencil still holds every partner within the force range
+            int key = a.buf.home_cell[s] - R.cell_off;
+            if (key < 0 || key >= nc * nc * nc) {  // never after a rebuild on this grid; keep in range anyway
+                atomicOr(a.flags, 16u);
+                key = 0;
+            }
+            cx = key % nc;
+            cy = (key / nc) % nc;
+            cz = key / (nc * nc);
+        } else {
+            cx = axis_cell<real>(xi, R.cell_scale, nc);
+            cy = axis_cell<real>(yi, R.cell_scale, nc);
+            cz = axis_cell<real>(zi, R.cell_scale, nc);
+        }
         // stencil offsets per axis, de-duplicated for grids of 1 or 2 cells (geometry.h:523-608)
         const int lo = nc >= 3 ? -1 : 0, hi = nc >= 2 ? 1 : 0;
         const real range2 = MODE == kModeObs ? (R.rc2 > R.bond_r * R.bond_r ? R.rc2 : R.bond_r * R.bond_r) : R.rc2;
@@ -557,16 +689,21 @@ __device__ __noinline__ void simple_particle(const ForceArgs<real> &a, int s) {
         Mv.v[9] = Tt[0]; Mv.v[10] = Tt[1]; Mv.v[11] = Tt[2];
         Mv.store(a.buf.motion + (size_t)s * kRow);
 
-        // ---- bin the next step's position (same arithmetic as the scatter pass)
+        // ---- bin the next step's position (same arithmetic as the scatter pass), or with skin lists
+        // check how far it will be from where the lists were built
         real xn[3] = {xi, yi, zi}, pn[3] = {p[0], p[1], p[2]};
         drift_position<real>(R, xn, pn, Ft);
         if (!(isfinite(xn[0]) && isfinite(xn[1]) && isfinite(xn[2]))) {
             atomicOr(a.flags, 1u);
             xn[0] = xn[1] = xn[2] = real(0);
         }
-        const int key = cell_of<real>(R, xn[0], xn[1], xn[2]);
-        const int rank = aggregated_rank(a.count, key);
-        a.bin[s] = make_int2(key, rank);
+        if (a.skin) {
+            skin_check<real>(a, R, s, xn);
+        } else {
+            const int key = cell_of<real>(R, xn[0], xn[1], xn[2]);
+            const int rank = aggregated_rank(a.count, key);
+            a.bin[s] = make_int2(key, rank);
+        }
     }
 }
 

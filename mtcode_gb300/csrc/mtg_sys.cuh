@@ -89,8 +89,13 @@ inline ReplicaGeometry geometry_of(const mtg_replica_desc &d) {
     return g;
 }
 
+// skin lists: the list (and cell) range, force range + skin, padded by 1e-3 sigma so that an FP32
+// rounding of the displacement test can never lose a pair
+inline double list_range(double rc, double skin) { return skin > 0 ? rc + skin + 1e-3 : rc; }
+
 template <class real>
-mtg::Replica<real> make_replica(const mtg_replica_desc &d, int off, int cell_off, int nc, int model) {
+mtg::Replica<real> make_replica(const mtg_replica_desc &d, int off, int cell_off, int nc, int model,
+                                double skin = 0.0) {
     mtg::Replica<real> R;
     std::memset(&R, 0, sizeof(R));
     ReplicaGeometry g = geometry_of(d);
@@ -124,6 +129,9 @@ mtg::Replica<real> make_replica(const mtg_replica_desc &d, int off, int cell_off
     R.rc2 = (real)(g.rc * g.rc);
     R.patch_r2 = (real)(g.patch_r * g.patch_r);
     R.bond_r = (real)g.bond_r;
+    const double rl = list_range(g.rc, skin);
+    R.rc2_list = (real)(rl * rl);
+    R.half_skin2 = (real)(0.25 * skin * skin);
     return R;
 }
 
@@ -217,6 +225,11 @@ struct Sys : SysBase {
     bool use_tiles = false;
     int4 *d_tiles = nullptr;
     int ntiles = 0, occ_tile = 1;
+    // skin lists (null without a skin): state flags, candidate lists and lengths, build positions / cells
+    double skin = 0;
+    int *d_skin = nullptr, *d_list_n = nullptr, *d_home_cell = nullptr;
+    unsigned *d_list = nullptr;
+    real *d_xref = nullptr;
     size_t tile_smem = 0;
     // occupancy-derived grid caps
     int occ_force = 1, occ_stream = 1;
@@ -230,16 +243,17 @@ struct Sys : SysBase {
         MTG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         nrep = cfg.n_replicas;
         track_disp = cfg.track_displacement != 0;
+        skin = cfg.neighbor_skin;
         desc.assign(cfg.replicas, cfg.replicas + nrep);
         int64_t off = 0, coff = 0, coff_obs = 0;
         rep_slot.push_back(0);
         for (int r = 0; r < nrep; r++) {
             const mtg_replica_desc &d = desc[r];
             ReplicaGeometry g = geometry_of(d);
-            int nc = cells_per_side(d.box, g.rc);
+            int nc = cells_per_side(d.box, list_range(g.rc, skin));
             int nco = cells_per_side(d.box, std::max(g.rc, g.bond_r));
             models.push_back(make_model<real>(d.model));
-            reps.push_back(make_replica<real>(d, (int)off, (int)coff, nc, r));
+            reps.push_back(make_replica<real>(d, (int)off, (int)coff, nc, r, skin));
             reps_obs.push_back(make_replica<real>(d, (int)off, (int)coff_obs, nco, r));
             off += d.n;
             coff += (int64_t)nc * nc * nc;
@@ -270,6 +284,19 @@ struct Sys : SysBase {
                 MTG_CUDA(cudaMalloc(&buf[b].dx, sizeof(double) * n));
                 MTG_CUDA(cudaMalloc(&buf[b].dy, sizeof(double) * n));
                 MTG_CUDA(cudaMalloc(&buf[b].dz, sizeof(double) * n));
+            }
+        }
+        if (skin > 0) {
+            MTG_CUDA(cudaMalloc(&d_skin, sizeof(int) * 4));
+            MTG_CUDA(cudaMemset(d_skin, 0, sizeof(int) * 4));
+            MTG_CUDA(cudaMalloc(&d_list, sizeof(unsigned) * mtg::kListCap * n));
+            MTG_CUDA(cudaMalloc(&d_list_n, sizeof(int) * n));
+            MTG_CUDA(cudaMemset(d_list_n, 0, sizeof(int) * n));
+            MTG_CUDA(cudaMalloc(&d_home_cell, sizeof(int) * n));
+            MTG_CUDA(cudaMalloc(&d_xref, sizeof(real) * 4 * n));
+            for (int b = 0; b < 2; b++) {
+                buf[b].xref = d_xref;
+                buf[b].home_cell = d_home_cell;
             }
         }
         MTG_CUDA(cudaMalloc(&d_bin, sizeof(int2) * n));
@@ -329,6 +356,7 @@ struct Sys : SysBase {
         cudaFree(d_flags); cudaFree(d_draw); cudaFree(d_stage); cudaFree(d_noise); cudaFree(d_obs);
         cudaFree(d_tiles);
         cudaFree(d_bond_start); cudaFree(d_bond_partner); cudaFree(d_slot_of);
+        cudaFree(d_skin); cudaFree(d_list); cudaFree(d_list_n); cudaFree(d_home_cell); cudaFree(d_xref);
         if (h_flags) cudaFreeHost(h_flags);
         if (st) cudaStreamDestroy(st);
     }
@@ -388,6 +416,12 @@ struct Sys : SysBase {
         a.flags = d_flags;
         a.draw = d_draw;
         a.do_kick = do_kick;
+        if (skin > 0) {
+            a.skin = d_skin;
+            a.skin_next = d_skin + 1;
+            a.list = d_list;
+            a.list_n = d_list_n;
+        }
         if (nbonds > 0) {
             a.bond_start = d_bond_start;
             a.bond_partner = d_bond_partner;
@@ -411,8 +445,56 @@ struct Sys : SysBase {
         mtg::force_kernel<real, MODE><<<gf, 128, 0, st>>>(a);
     }
 
+    // a skin-list step on buffer b (which stays the buffer in use): the decision, then either the
+    // rebuild (binning, scan, scatter b -> b^1, copy back) or the in-place first half-step, then the force
+    // pass in build or list mode -- one launch sequence, the unused branch's kernels return at once
+    void enqueue_skin_step(int b, const double *ext_noise) {
+        mtg::Tables<real> tb = tables();
+        const int g = grid_for(ntot_, 256, occ_stream, sms);
+        mtg::skin_decide_kernel<<<1, 32, 0, st>>>(d_skin, d_draw);
+        mtg::bin_kernel<real, true><<<g, 256, 0, st>>>(tb, buf[b], d_bin, d_count, d_flags, d_skin);
+        int nblk = std::max(1, (ncells + mtg::kScanTile - 1) / mtg::kScanTile);
+        mtg::scan_reduce_kernel<<<nblk, mtg::kScanThreads, 0, st>>>(d_count, ncells, d_block, d_skin);
+        mtg::scan_top_kernel<<<1, mtg::kScanThreads, 0, st>>>(d_block, nblk, d_start, ncells, d_draw, 0, d_skin);
+        mtg::scan_down_kernel<<<nblk, mtg::kScanThreads, 0, st>>>(d_count, ncells, d_block, d_start, d_skin);
+        mtg::scatter_kernel<real, true><<<g, 256, 0, st>>>(tb, buf[b], buf[b ^ 1], d_bin, d_start, d_flags, d_skin);
+        mtg::copy_back_kernel<real><<<g, 256, 0, st>>>(ntot_, buf[b ^ 1], buf[b], d_skin);
+        mtg::integrate_kernel<real><<<g, 256, 0, st>>>(tb, buf[b], d_flags, d_skin);
+        mtg::ForceArgs<real> a = force_args(b, 1);
+        a.ext_noise = ext_noise;
+        launch_force<mtg::kModeStep>(a);
+        check_launch();
+    }
+
+    void count_rebuild() {
+        int h[4];
+        MTG_CUDA(cudaMemcpyAsync(h, d_skin, sizeof(h), cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+        h[3] += 1;
+        MTG_CUDA(cudaMemcpyAsync(d_skin + 3, h + 3, sizeof(int), cudaMemcpyHostToDevice, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+    }
+
+    void set_skin(int now, int next, int forced) {
+        mtg::skin_set_kernel<<<1, 32, 0, st>>>(d_skin, now, next, forced);
+        check_launch();
+        nlaunch += 1;
+    }
+
+    int64_t rebuilds() override {
+        if (skin <= 0) return 0;
+        int h[4];
+        MTG_CUDA(cudaMemcpyAsync(h, d_skin, sizeof(h), cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+        return h[3];
+    }
+
     // one step from buffer b: scan (+draw), scatter b -> b^1, force on b^1
     void enqueue_step(int b, const double *ext_noise) {
+        if (skin > 0) {
+            enqueue_skin_step(b, ext_noise);
+            return;
+        }
         mtg::Tables<real> tb = tables();
         scan(ncells, true);
         const int g = grid_for(ntot_, 256, occ_stream, sms);
@@ -496,6 +578,10 @@ struct Sys : SysBase {
         if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_init_forces: no state has been set"};
         rebuild_cells(false);
         tick_draw();
+        if (skin > 0) {
+            set_skin(1, 0, 0);  // this pass builds the lists (a rebuild)
+            count_rebuild();
+        }
         mtg::ForceArgs<real> a = force_args(cur, 0);
         if (noise) a.ext_noise = upload_noise(noise);
         launch_force<mtg::kModeInit>(a);
@@ -575,7 +661,9 @@ struct Sys : SysBase {
         if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_step: no state has been set"};
         MTG_REQUIRE(nsteps >= 0, "mtg_step: nsteps must be >= 0");
         if (!forces_ready) init_forces(nullptr);
-        if (!bins_valid) {
+        if (skin > 0) {
+            if (!cells_valid) set_skin(-1, -1, 1);  // the buffer was re-sorted by another grid: rebuild first
+        } else if (!bins_valid) {
             MTG_CUDA(cudaMemsetAsync(d_count, 0, sizeof(int) * (ncells_alloc + 1), st));
             const int g = grid_for(ntot_, 256, occ_stream, sms);
             mtg::bin_kernel<real, true><<<g, 256, 0, st>>>(tables(), buf[cur], d_bin, d_count, d_flags);
@@ -590,8 +678,8 @@ struct Sys : SysBase {
         if (noise) {
             for (int s = 0; s < nsteps; s++) {
                 enqueue_step(cur, upload_noise(noise + (size_t)s * 6 * n));
-                cur ^= 1;
-                nlaunch += 5;
+                if (skin <= 0) cur ^= 1;  // a skin step leaves the state in the buffer it started in
+                nlaunch += skin > 0 ? 9 : 5;
                 draw += 1;
             }
             MTG_CUDA(cudaStreamSynchronize(st));
@@ -599,8 +687,8 @@ struct Sys : SysBase {
             for (int s = 0; s < nsteps; s++) {
                 if (!graph[cur]) build_graph(cur);
                 MTG_CUDA(cudaGraphLaunch(graph[cur], st));
-                cur ^= 1;
-                nlaunch += 5;
+                if (skin <= 0) cur ^= 1;
+                nlaunch += skin > 0 ? 9 : 5;
                 draw += 1;
             }
         }
@@ -621,7 +709,35 @@ struct Sys : SysBase {
         const int g = grid_for(ntot_, 256, occ_stream, sms);
         const int gf = grid_for(ntot_, 128, occ_force, sms);
         int nblk = std::max(1, (ncells + mtg::kScanTile - 1) / mtg::kScanTile);
-        for (int s = 0; s < nsteps; s++) {
+        for (int s = 0; s < nsteps && skin > 0; s++) {
+            const int b = cur;
+            MTG_CUDA(cudaEventRecord(ev[0], st));
+            mtg::skin_decide_kernel<<<1, 32, 0, st>>>(d_skin, d_draw);
+            mtg::bin_kernel<real, true><<<g, 256, 0, st>>>(tb, buf[b], d_bin, d_count, d_flags, d_skin);
+            mtg::scan_reduce_kernel<<<nblk, mtg::kScanThreads, 0, st>>>(d_count, ncells, d_block, d_skin);
+            MTG_CUDA(cudaEventRecord(ev[1], st));
+            mtg::scan_top_kernel<<<1, mtg::kScanThreads, 0, st>>>(d_block, nblk, d_start, ncells, d_draw, 0, d_skin);
+            MTG_CUDA(cudaEventRecord(ev[2], st));
+            mtg::scan_down_kernel<<<nblk, mtg::kScanThreads, 0, st>>>(d_count, ncells, d_block, d_start, d_skin);
+            MTG_CUDA(cudaEventRecord(ev[3], st));
+            mtg::scatter_kernel<real, true><<<g, 256, 0, st>>>(tb, buf[b], buf[b ^ 1], d_bin, d_start, d_flags, d_skin);
+            mtg::copy_back_kernel<real><<<g, 256, 0, st>>>(ntot_, buf[b ^ 1], buf[b], d_skin);
+            mtg::integrate_kernel<real><<<g, 256, 0, st>>>(tb, buf[b], d_flags, d_skin);
+            MTG_CUDA(cudaEventRecord(ev[4], st));
+            mtg::ForceArgs<real> a = force_args(b, 1);
+            launch_force<mtg::kModeStep>(a);
+            MTG_CUDA(cudaEventRecord(ev[5], st));
+            check_launch();
+            MTG_CUDA(cudaEventSynchronize(ev[5]));
+            for (int k = 0; k < 5; k++) {
+                float ms = 0;
+                MTG_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+                acc[k] += ms;
+            }
+            nlaunch += 9;
+            draw += 1;
+        }
+        for (int s = 0; s < nsteps && skin <= 0; s++) {
             const int b = cur;
             MTG_CUDA(cudaEventRecord(ev[0], st));
             mtg::scan_reduce_kernel<<<nblk, mtg::kScanThreads, 0, st>>>(d_count, ncells, d_block);
@@ -655,7 +771,18 @@ struct Sys : SysBase {
     void forces(double *F, double *T, double *E) override {
         if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_forces: no state has been set"};
         MTG_REQUIRE(F && T, "mtg_forces: F and T are required");
-        if (!cells_valid) rebuild_cells(false);
+        if (skin > 0) {
+            // the lists are valid for the current positions as long as the sort they were built on is
+            if (!cells_valid) {
+                rebuild_cells(false);
+                set_skin(1, -1, -1);
+                count_rebuild();
+            } else {
+                set_skin(0, -1, -1);
+            }
+        } else if (!cells_valid) {
+            rebuild_cells(false);
+        }
         size_t n = (size_t)ntot_;
         double *sF = d_stage, *sT = sF + 3 * n, *sE = sT + 3 * n;
         mtg::ForceArgs<real> a = force_args(cur, 0);

@@ -41,6 +41,7 @@ struct SysBase {
     virtual void set_bonds(const int32_t *, int64_t, double, double) = 0;
     virtual void gr(int, double, double, int64_t *, int, int *) = 0;
     virtual void clusters(int, double, int32_t *) = 0;
+    virtual int64_t rebuilds() = 0;
     virtual mtg_status pairs(int, double, int32_t *, int64_t, int64_t *) = 0;
     virtual void temperature(double *) = 0;
     virtual void observables(double *) = 0;

@@ -196,9 +196,13 @@ __device__ __forceinline__ void langevin_epilogue(const ForceArgs<float> &a, con
         atomicOr(a.flags, 1u);
         xn[0] = xn[1] = xn[2] = 0.f;
     }
-    const int key = cell_of<float>(R, xn[0], xn[1], xn[2]);
-    const int rank = aggregated_rank(a.count, key);
-    a.bin[s] = make_int2(key, rank);
+    if (a.skin) {
+        skin_check<float>(a, R, s, xn);
+    } else {
+        const int key = cell_of<float>(R, xn[0], xn[1], xn[2]);
+        const int rank = aggregated_rank(a.count, key);
+        a.bin[s] = make_int2(key, rank);
+    }
 }
 
 __device__ __forceinline__ void load_q(const ForceArgs<float> &a, int slot, float q8, float Q[9]) {
@@ -605,49 +609,26 @@ __device__ int produce_tile(const ForceArgs<float> &a, const int4 desc, StageBuf
     return units;
 }
 
-// Consumer warp: unit u (32 home particles) of a staged tile -- phases 1-4
-template <int MODE>
-__device__ void consume_staged_unit(const ForceArgs<float> &a, const StageBuf &B, WarpScratch &W, int u, int lane,
-                                    bool &big, int &overflow) {
-    const TileGeom g = decode_tile(B.desc);
-    const Replica<float> &R = a.tb.reps[g.rep];
-    const Model<float> &M = a.tb.models[R.model];
-    const int nry = g.ty + 2;
-    const int hx0 = g.whole ? 0 : 1, hx1 = g.whole ? g.sx : g.sx - 1;
-    const int hidx = 32 * u + lane;
-    const bool active = hidx < B.nhome;
-    int myk = 0, mycell = 0;
-    if (active) {
-        int r = 0;
-        while (B.row_start[r + 1] <= hidx) r++;
-        const int rb = ((1 + r / g.ty) * nry + (1 + r % g.ty)) * g.sx;
-        myk = B.cell_sm[rb + hx0] + (hidx - B.row_start[r]);
-        int lo = hx0, hi = hx1;  // cell_sm[rb+lo] <= myk < cell_sm[rb+hi]
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (B.cell_sm[rb + mid] <= myk) lo = mid;
-            else hi = mid;
-        }
-        mycell = rb + lo;
-        const int slot = B.cell_lo[mycell] + (myk - B.cell_sm[mycell]);
-        W.h_k[lane] = myk;
-        W.h_slot[lane] = slot;
-        W.h_id[lane] = __ldg(a.buf.ident + slot);
-        W.h_qa[lane] = __ldg(reinterpret_cast<const float4 *>(a.buf.rota) + slot);
-        W.h_qb[lane] = __ldg(reinterpret_cast<const float4 *>(a.buf.rotb) + slot);
-    }
-#pragma unroll
-    for (int k = 0; k < 6; k++) W.acc[lane][k] = 0ull;
-    __syncwarp();
+enum ScanKind : int { kScanExact = 0, kScanBuild = 1, kScanStale = 2 };
 
-    // -- phase 1: candidate scan in shared memory.  A neighbour cell reached across a periodic face
-    // holds unshifted coordinates; its image shift s (0 or +-L per axis, known from the staged cell's
-    // unwrapped coordinate) gives the separation (x_i - x_j) - s, which is exactly what the minimum-image
-    // rule computes for every pair within the force range.  The three cells of a row are at most two
-    // contiguous segments (split only where an image shift changes).  The loops are warp-uniform (each
-    // row runs to the longest lane's candidate count), so in-range candidates are appended with one
-    // ballot per candidate round and no shared-memory atomics.
+// Phase 1: candidate scan in shared memory, one lane per home particle.  A neighbour cell reached across
+// a periodic face holds unshifted coordinates; its image shift s (0 or +-L per axis, known from the
+// staged cell's unwrapped coordinate) gives the separation (x_i - x_j) - s, which is exactly what the
+// minimum-image rule computes for every pair within the force range.  The three cells of a row are at
+// most two contiguous segments (split only where an image shift changes).  The loops are warp-uniform
+// (each row runs to the longest lane's candidate count), so in-range candidates are appended with one
+// ballot per candidate round and no shared-memory atomics.  Returns the warp's pair count.
+//   kScanExact  cells sorted this step, pairs within the force range
+//   kScanBuild  skin lists, rebuild step: also stores every candidate within the list range as the
+//               home's list (staged particle | staged cell << 11) and its length
+//   kScanStale  skin lists, cells sorted at the last build and particles moved since: minimum image
+template <int KIND>
+__device__ __forceinline__ int scan_cells(const ForceArgs<float> &a, const Replica<float> &R, const TileGeom &g,
+                                          const StageBuf &B, WarpScratch &W, bool active, int myk, int mycell, int slot,
+                                          int lane) {
+    const int nry = g.ty + 2;
     int npairs = 0;  // warp-uniform
+    int lc = 0;      // KIND == kScanBuild: candidates of this lane's home within the list range
     {
         const float4 pi = active ? B.pos[myk] : make_float4(0.f, 0.f, 0.f, 0.f);
         const int lx = mycell % g.sx, ly = (mycell / g.sx) % nry, lz = mycell / (g.sx * nry);
@@ -698,15 +679,29 @@ __device__ void consume_staged_unit(const ForceArgs<float> &a, const StageBuf &B
 #pragma unroll
                     for (int u = 0; u < 4; u++) {
                         const int t = t0 + u;
-                        const float shx = t < lena ? 0.f : shw;
-                        const float ddx = (pi.x - pj[u].x) - shx;
-                        const float ddy = (pi.y - pj[u].y) - shy;
-                        const float ddz = (pi.z - pj[u].z) - shz;
-                        const bool hit = t < len && kq[u] != myk && ddx * ddx + ddy * ddy + ddz * ddz < R.rc2;
+                        float ddx, ddy, ddz;
+                        if (KIND == kScanStale) {
+                            // positions have moved since the cells were built: plain minimum image
+                            ddx = min_image<float>(pi.x - pj[u].x, R.box, R.l2s, R.periodic);
+                            ddy = min_image<float>(pi.y - pj[u].y, R.box, R.l2s, R.periodic);
+                            ddz = min_image<float>(pi.z - pj[u].z, R.box, R.l2s, R.periodic);
+                        } else {
+                            const float shx = t < lena ? 0.f : shw;
+                            ddx = (pi.x - pj[u].x) - shx;
+                            ddy = (pi.y - pj[u].y) - shy;
+                            ddz = (pi.z - pj[u].z) - shz;
+                        }
+                        const float r2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                        const bool cand = t < len && kq[u] != myk;
+                        const bool hit = cand && r2 < R.rc2;
+                        const int cell = t < lena ? rowb + c0 + (kq[u] >= b1) + (kq[u] >= b2) : rowb + cw;
+                        if (KIND == kScanBuild && cand && r2 < R.rc2_list) {
+                            if (lc < kListCap) a.list[(size_t)lc * a.tb.ntot + slot] = (unsigned)kq[u] | ((unsigned)cell << 11);
+                            lc++;
+                        }
                         const unsigned m = __ballot_sync(0xffffffffu, hit);
                         if (hit) {
                             const int p = npairs + __popc(m & lt_mask);
-                            const int cell = t < lena ? rowb + c0 + (kq[u] >= b1) + (kq[u] >= b2) : rowb + cw;
                             if (p < kWarpPairCap) W.pair[p] = pair_entry(kq[u], cell, lane);
                         }
                         npairs += __popc(m);
@@ -714,6 +709,91 @@ __device__ void consume_staged_unit(const ForceArgs<float> &a, const StageBuf &B
                 }
             }
         }
+    }
+    if (KIND == kScanBuild && active) a.list_n[slot] = lc;
+    return npairs;
+}
+
+// Phase 1 on a step that keeps its skin lists: each lane's home tests its stored candidates (the staged
+// indices are those of the last build: the cells, hence the staging, are unchanged until the next one).
+__device__ __forceinline__ int scan_list(const ForceArgs<float> &a, const Replica<float> &R, const StageBuf &B,
+                                         WarpScratch &W, bool active, int myk, int slot, int cnt, int lane) {
+    const float4 pi = active ? B.pos[myk] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const int maxlen = __reduce_max_sync(0xffffffffu, cnt);
+    int npairs = 0;
+    for (int t0 = 0; t0 < maxlen; t0 += 4) {
+        unsigned e[4];
+        float4 pj[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) e[u] = t0 + u < cnt ? __ldg(a.list + (size_t)(t0 + u) * a.tb.ntot + slot) : 0u;
+#pragma unroll
+        for (int u = 0; u < 4; u++) pj[u] = B.pos[t0 + u < cnt ? (int)(e[u] & 2047u) : myk];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const float ddx = min_image<float>(pi.x - pj[u].x, R.box, R.l2s, R.periodic);
+            const float ddy = min_image<float>(pi.y - pj[u].y, R.box, R.l2s, R.periodic);
+            const float ddz = min_image<float>(pi.z - pj[u].z, R.box, R.l2s, R.periodic);
+            const bool hit = t0 + u < cnt && ddx * ddx + ddy * ddy + ddz * ddz < R.rc2;
+            const unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (hit) {
+                const int p = npairs + __popc(m & lt_mask);
+                if (p < kWarpPairCap) W.pair[p] = pair_entry((int)(e[u] & 2047u), (int)(e[u] >> 11), lane);
+            }
+            npairs += __popc(m);
+        }
+    }
+    return npairs;
+}
+
+// Consumer warp: unit u (32 home particles) of a staged tile -- phases 1-4
+template <int MODE>
+__device__ void consume_staged_unit(const ForceArgs<float> &a, const StageBuf &B, WarpScratch &W, int u, int lane,
+                                    bool &big, int &overflow) {
+    const TileGeom g = decode_tile(B.desc);
+    const Replica<float> &R = a.tb.reps[g.rep];
+    const Model<float> &M = a.tb.models[R.model];
+    const int nry = g.ty + 2;
+    const int hx0 = g.whole ? 0 : 1, hx1 = g.whole ? g.sx : g.sx - 1;
+    const int hidx = 32 * u + lane;
+    const bool active = hidx < B.nhome;
+    int myk = 0, mycell = 0;
+    if (active) {
+        int r = 0;
+        while (B.row_start[r + 1] <= hidx) r++;
+        const int rb = ((1 + r / g.ty) * nry + (1 + r % g.ty)) * g.sx;
+        myk = B.cell_sm[rb + hx0] + (hidx - B.row_start[r]);
+        int lo = hx0, hi = hx1;  // cell_sm[rb+lo] <= myk < cell_sm[rb+hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (B.cell_sm[rb + mid] <= myk) lo = mid;
+            else hi = mid;
+        }
+        mycell = rb + lo;
+        const int slot = B.cell_lo[mycell] + (myk - B.cell_sm[mycell]);
+        W.h_k[lane] = myk;
+        W.h_slot[lane] = slot;
+        W.h_id[lane] = __ldg(a.buf.ident + slot);
+        W.h_qa[lane] = __ldg(reinterpret_cast<const float4 *>(a.buf.rota) + slot);
+        W.h_qb[lane] = __ldg(reinterpret_cast<const float4 *>(a.buf.rotb) + slot);
+    }
+#pragma unroll
+    for (int k = 0; k < 6; k++) W.acc[lane][k] = 0ull;
+    __syncwarp();
+
+    // -- phase 1: the warp's pair list (scan_cells / scan_list)
+    const int slot = active ? W.h_slot[lane] : 0;
+    int npairs;
+    if (!a.skin) {
+        npairs = scan_cells<kScanExact>(a, R, g, B, W, active, myk, mycell, slot, lane);
+    } else if (*a.skin) {
+        npairs = scan_cells<kScanBuild>(a, R, g, B, W, active, myk, mycell, slot, lane);
+    } else {
+        const int cnt = active ? __ldg(a.list_n + slot) : 0;
+        if (__any_sync(0xffffffffu, cnt > kListCap))  // a home had more candidates than its list holds
+            npairs = scan_cells<kScanStale>(a, R, g, B, W, active, myk, mycell, slot, lane);
+        else
+            npairs = scan_list(a, R, B, W, active, myk, slot, cnt, lane);
     }
     __syncwarp();
     if (npairs > kWarpPairCap) {

@@ -24,6 +24,7 @@ def main() -> None:
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
     ap.add_argument("--kernel", choices=["tiled", "per_particle"], default="tiled")
     ap.add_argument("--profile", action="store_true", help="also print per-kernel device times")
+    ap.add_argument("--skin", type=float, default=0.0, help="neighbour skin (sigma); 0 rebuilds cells every step")
     args = ap.parse_args()
     if args.workload == "c4":
         W = workloads.patchy_c4(seed=args.seed, n_replicas=args.replicas)
@@ -33,7 +34,7 @@ def main() -> None:
         W = workloads.WORKLOADS[args.workload](seed=args.seed)
     n = W.n_total
     z = np.zeros((n, 3))
-    with LangevinNVTRGPU(W.replicas, precision=args.precision, force_kernel=args.kernel) as s:
+    with LangevinNVTRGPU(W.replicas, precision=args.precision, force_kernel=args.kernel, neighbor_skin=args.skin) as s:
         s.initialize(W.x, z, z, W.Q)
         if W.bonds is not None:
             s.set_bonds(W.bonds, W.bond_k, W.bond_r0)
@@ -45,6 +46,8 @@ def main() -> None:
         dt = time.perf_counter() - t0
         line = f"{W.name}: {len(W.replicas)} replicas, {n} particles, {args.steps} steps, {1e3 * dt / args.steps:.3f} ms/step, " \
                f"{n * args.steps / dt:.3e} particle-steps/s"
+        if args.skin > 0:
+            line += f", {s.rebuilds} list builds"
         if args.profile:
             prof = s.step_profile(max(1, args.steps))
             line += " | " + " ".join(f"{k}={v / max(1, args.steps):.3f}ms" for k, v in prof.items())

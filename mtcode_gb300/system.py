@@ -102,7 +102,9 @@ class LangevinNVTRGPU:
     """All replicas of one GPU handle (one CUDA stream)."""
 
     def __init__(self, replicas: list, precision: str = "fp32", device: int = 0, track_displacement: bool = True,
-                 force_kernel: str = "tiled"):
+                 force_kernel: str = "tiled", neighbor_skin: float = 0.0):
+        """``neighbor_skin`` > 0 (sigma): cells and candidate lists at force range + skin, reused until a
+        particle has moved more than half the skin (the same force set as a rebuild every step)."""
         L = _lib.lib()
         self.replicas = list(replicas)
         self._descs = (_lib.ReplicaDesc * len(self.replicas))(*[r.to_c() for r in self.replicas])
@@ -113,6 +115,7 @@ class LangevinNVTRGPU:
         cfg.device = int(device)
         cfg.track_displacement = int(bool(track_displacement))
         cfg.force_kernel = 1 if force_kernel == "per_particle" else 0
+        cfg.neighbor_skin = float(neighbor_skin)
         h = C.c_void_p()
         st = L.mtg_create(C.byref(cfg), C.byref(h))
         if st != 0:
@@ -288,6 +291,11 @@ class LangevinNVTRGPU:
         write_csv(paths[0], x)
         write_csv(paths[1], Q)
         return paths
+
+    @property
+    def rebuilds(self) -> int:
+        """Neighbour-list rebuilds so far (0 without a skin)."""
+        return int(_lib.lib().mtg_neighbor_rebuilds(self._h))
 
     def clear_flags(self) -> None:
         """Clear the device-latched condition bits (mtg_clear_flags)."""
