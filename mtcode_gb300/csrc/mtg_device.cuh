@@ -229,15 +229,33 @@ __device__ __forceinline__ void philox_noise6(uint32_t local, uint32_t replica, 
 // visited -- and that order (the within-cell order of the counting sort) is not deterministic.
 // FP64: plain double sums.
 template <class real> struct Acc3;
+// 64-bit fixed point with 32 fraction bits, converted with 32-bit instructions only (64-bit integer <->
+// float conversions run on GB300's narrow FP64 pipe).  to_fixed(v) equals round-to-nearest-even of
+// v * 2^32 for |v| < 2^31: the floor part is exact and v - floor(v) is exact, so one rounding of the
+// fraction * 2^32 (< 2^32) is the rounding of the whole.  from_fixed rounds the fraction to 24 bits first,
+// so it can differ from a correctly rounded conversion by one unit in the last place; it is a fixed
+// function of the sum, which is what order independence needs.
+__device__ __forceinline__ long long to_fixed(float v) {
+    const float h = floorf(v);
+    const int hi = __float2int_rz(h);
+    const unsigned lo = __float2uint_rn((v - h) * 4294967296.0f);
+    return (long long)(((unsigned long long)(long long)hi << 32) + (unsigned long long)lo);
+}
+__device__ __forceinline__ float from_fixed(long long a) {
+    const int hi = (int)(a >> 32);
+    const unsigned lo = (unsigned)(unsigned long long)a;
+    return fmaf(__uint2float_rn(lo), 2.3283064365386963e-10f, __int2float_rn(hi));
+}
+
 template <> struct Acc3<float> {
     long long v[3];
     __device__ __forceinline__ void zero() { v[0] = v[1] = v[2] = 0; }
     __device__ __forceinline__ void add(float a, float b, float c) {
-        v[0] += __float2ll_rn(a * 4294967296.0f);
-        v[1] += __float2ll_rn(b * 4294967296.0f);
-        v[2] += __float2ll_rn(c * 4294967296.0f);
+        v[0] += to_fixed(a);
+        v[1] += to_fixed(b);
+        v[2] += to_fixed(c);
     }
-    __device__ __forceinline__ float get(int k) const { return __ll2float_rn(v[k]) * 2.3283064365386963e-10f; }
+    __device__ __forceinline__ float get(int k) const { return from_fixed(v[k]); }
 };
 template <> struct Acc3<double> {
     double v[3];

@@ -143,11 +143,9 @@ __device__ __forceinline__ TileGeom decode_tile(int4 t) {
 }
 
 __device__ __forceinline__ void acc_add(unsigned long long *a, float v) {
-    atomicAdd(a, (unsigned long long)__float2ll_rn(v * 4294967296.0f));
+    atomicAdd(a, (unsigned long long)to_fixed(v));
 }
-__device__ __forceinline__ float acc_get(unsigned long long a) {
-    return __ll2float_rn((long long)a) * 2.3283064365386963e-10f;
-}
+__device__ __forceinline__ float acc_get(unsigned long long a) { return from_fixed((long long)a); }
 
 // the Langevin epilogue shared with the simple kernel (create_forces_and_torques_sphere + half-kick +
 // binning of the next step); F, T are the lab-frame force and torque of slot s
