@@ -335,8 +335,8 @@ __global__ void __launch_bounds__(256) scatter_kernel(Tables<real> tb, Buffers<r
             out.xref[4 * (size_t)d] = P.v[0];
             out.xref[4 * (size_t)d + 1] = P.v[1];
             out.xref[4 * (size_t)d + 2] = P.v[2];
-            out.home_cell[d] = kb.x;
         }
+        if (out.home_cell) out.home_cell[d] = kb.x;
     }
 }
 
@@ -522,13 +522,14 @@ __device__ __noinline__ void simple_particle(const ForceArgs<real> &a, int s) {
         const real range2 = MODE == kModeObs ? (R.rc2 > R.bond_r * R.bond_r ? R.rc2 : R.bond_r * R.bond_r) : R.rc2;
 
         for (int dz = lo; dz <= hi; dz++) {
-            int zz = cz + dz;
+            // fewer than three cells per side: every cell of the side is a neighbour, walls or not
+            int zz = nc < 3 ? dz : cz + dz;
             if (zz < 0 || zz >= nc) {
                 if (!R.periodic) continue;
                 zz = zz < 0 ? zz + nc : zz - nc;
             }
             for (int dy = lo; dy <= hi; dy++) {
-                int yy = cy + dy;
+                int yy = nc < 3 ? dy : cy + dy;
                 if (yy < 0 || yy >= nc) {
                     if (!R.periodic) continue;
                     yy = yy < 0 ? yy + nc : yy - nc;

@@ -1,0 +1,242 @@
+// mtg_pipe.cuh -- the FP32 force pass as a pair pipeline: three high-occupancy kernels, no shared-memory
+// tiles.
+//
+//   pairfind   one thread per particle (slot s): every candidate t > s of the 27 cells around s's cell
+//              within the range (the force range, or with a neighbour skin the list range) is one
+//              unordered pair (s, t), appended through a per-block buffer to a list in HBM
+//   pairforce  one thread per pair: WCA core (HSPotential, MD::calculateforces) and the Kern-Frenkel
+//              patch potentials (calculate_forces_and_torques3D) of the pair in the reference's canonical
+//              order (lower particle index first), added to BOTH particles as 64-bit fixed-point sums
+//              (integer atomics commute: the sums do not depend on the order of the pairs)
+//   epilogue   one thread per particle: read and clear the sums, bonds, friction + Philox noise,
+//              half-kick, next-step binning (or the skin displacement check)
+//
+// With a neighbour skin the pair list is built only on rebuild steps (slots do not move in between) and
+// the force kernel drops the pairs beyond the force range each step.
+#pragma once
+
+#include <cooperative_groups.h>
+
+#include "mtg_tile.cuh"
+
+namespace mtg {
+namespace {  // internal linkage
+
+constexpr int kPipeThreads = 256;
+constexpr int kPairBlockCap = 2048;    // pairs a pairfind block buffers in shared memory
+constexpr int kPairsPerParticle = 16;  // capacity of the pair list (unordered pairs per particle)
+
+__device__ __forceinline__ void block_pair_append(int2 *buf, int *nb, int2 p, int2 *pairs,
+                                                  unsigned long long *npairs, long long cap, unsigned *flags) {
+    // warp-aggregated: the lanes that found a pair in this iteration take consecutive buffer entries
+    cooperative_groups::coalesced_group g = cooperative_groups::coalesced_threads();
+    int q = 0;
+    if (g.thread_rank() == 0) q = atomicAdd(nb, (int)g.size());
+    q = g.shfl(q, 0) + (int)g.thread_rank();
+    if (q < kPairBlockCap) {
+        buf[q] = p;
+    } else {  // the block buffer is full: straight to the list
+        const unsigned long long w = atomicAdd(npairs, 1ull);
+        if ((long long)w < cap) pairs[w] = p;
+        else atomicOr(flags, 8u);
+    }
+}
+
+// range2_list: use the replica's list range (skin lists) instead of its force range
+__global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float> a, int2 *pairs,
+                                                                unsigned long long *npairs, long long cap,
+                                                                int range_list, const int *gate) {
+    if (gated_off(gate, 1)) return;
+    __shared__ int2 buf[kPairBlockCap];
+    __shared__ int nb;
+    __shared__ unsigned long long base;
+    if (threadIdx.x == 0) nb = 0;
+    __syncthreads();
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < a.tb.ntot) {
+        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, s);
+        const Replica<float> &R = a.tb.reps[r];
+        const float range2 = range_list ? R.rc2_list : R.rc2;
+        const int nc = R.nc;
+        int key = a.buf.home_cell[s] - R.cell_off;
+        if (key < 0 || key >= nc * nc * nc) {
+            atomicOr(a.flags, 16u);
+            key = 0;
+        }
+        const int cx = key % nc, cy = (key / nc) % nc, cz = key / (nc * nc);
+        float xi, yi, zi;
+        load_pos(a.buf.pos + 4 * (size_t)s, xi, yi, zi);
+        const int lo = nc >= 3 ? -1 : 0, hi = nc >= 2 ? 1 : 0;  // de-duplicated stencil (geometry.h:596-606)
+        for (int dz = lo; dz <= hi; dz++) {
+            // fewer than three cells per side: every cell of the side is a neighbour, walls or not
+            int zz = nc < 3 ? dz : cz + dz;
+            if (zz < 0 || zz >= nc) {
+                if (!R.periodic) continue;
+                zz = zz < 0 ? zz + nc : zz - nc;
+            }
+            for (int dy = lo; dy <= hi; dy++) {
+                int yy = nc < 3 ? dy : cy + dy;
+                if (yy < 0 || yy >= nc) {
+                    if (!R.periodic) continue;
+                    yy = yy < 0 ? yy + nc : yy - nc;
+                }
+                const int row = R.cell_off + nc * (yy + nc * zz);
+                // the x-range [cx-1, cx+1] as at most two contiguous slot segments
+                int a0, a1, b0 = 0, b1 = 0;
+                if (nc < 3) {
+                    a0 = __ldg(a.start + row);
+                    a1 = __ldg(a.start + row + nc);
+                } else if (cx == 0) {
+                    a0 = __ldg(a.start + row);
+                    a1 = __ldg(a.start + row + 2);
+                    if (R.periodic) {
+                        b0 = __ldg(a.start + row + nc - 1);
+                        b1 = __ldg(a.start + row + nc);
+                    }
+                } else if (cx == nc - 1) {
+                    a0 = __ldg(a.start + row + nc - 2);
+                    a1 = __ldg(a.start + row + nc);
+                    if (R.periodic) {
+                        b0 = __ldg(a.start + row);
+                        b1 = __ldg(a.start + row + 1);
+                    }
+                } else {
+                    a0 = __ldg(a.start + row + cx - 1);
+                    a1 = __ldg(a.start + row + cx + 2);
+                }
+                for (int seg = 0; seg < 2; seg++) {
+                    int t0 = seg ? b0 : a0;
+                    const int t1 = seg ? b1 : a1;
+                    if (t0 <= s) t0 = s + 1;  // each unordered pair once: from its lower slot
+                    for (int t = t0; t < t1; t++) {
+                        float xj, yj, zj;
+                        load_pos(a.buf.pos + 4 * (size_t)t, xj, yj, zj);
+                        const float dx = min_image<float>(xi - xj, R.box, R.l2s, R.periodic);
+                        const float dy2 = min_image<float>(yi - yj, R.box, R.l2s, R.periodic);
+                        const float dz2 = min_image<float>(zi - zj, R.box, R.l2s, R.periodic);
+                        if (dx * dx + dy2 * dy2 + dz2 * dz2 < range2)
+                            block_pair_append(buf, &nb, make_int2(s, t), pairs, npairs, cap, a.flags);
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    const int n = nb < kPairBlockCap ? nb : kPairBlockCap;
+    if (threadIdx.x == 0) base = n ? atomicAdd(npairs, (unsigned long long)n) : 0ull;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        if ((long long)(base + i) < cap) pairs[base + i] = buf[i];
+        else atomicOr(a.flags, 8u);
+    }
+}
+
+__global__ void pair_reset_kernel(unsigned long long *npairs, const int *gate) {
+    if (gated_off(gate, 1)) return;
+    if (threadIdx.x == 0 && blockIdx.x == 0) *npairs = 0ull;
+}
+
+__device__ __forceinline__ void fixed_add(long long *acc, float v) {
+    if (v != 0.f) atomicAdd(reinterpret_cast<unsigned long long *>(acc), (unsigned long long)to_fixed(v));
+}
+
+// forces and torques of the listed pairs into acc (6 fixed-point sums per slot: F lab, T lab)
+__global__ void __launch_bounds__(kPipeThreads) pairforce_kernel(ForceArgs<float> a, const int2 *pairs,
+                                                                 const unsigned long long *npairs, long long cap,
+                                                                 long long *acc) {
+    const long long n = (long long)*npairs < cap ? (long long)*npairs : cap;
+    bool big = false;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int2 pr = pairs[q];
+        const int sa = pr.x, sb = pr.y;
+        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, sa);
+        const Replica<float> &R = a.tb.reps[r];
+        float xa[4], xb[4];
+        load4(a.buf.pos + 4 * (size_t)sa, xa);
+        load4(a.buf.pos + 4 * (size_t)sb, xb);
+        const float d[3] = {min_image<float>(xa[0] - xb[0], R.box, R.l2s, R.periodic),
+                            min_image<float>(xa[1] - xb[1], R.box, R.l2s, R.periodic),
+                            min_image<float>(xa[2] - xb[2], R.box, R.l2s, R.periodic)};
+        const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if (!(r2 < R.rc2)) continue;  // skin lists hold pairs up to the list range
+        const float rr = sqrtf(r2);
+        float fa[3] = {0.f, 0.f, 0.f}, ta[3] = {0.f, 0.f, 0.f}, tb[3] = {0.f, 0.f, 0.f};
+        if (rr < R.hs_limit) {
+            const float s_ = hs_force_over_r<float>(R, r2);
+            big |= fabsf(s_ * rr) > 1e4f;
+            fa[0] = s_ * d[0];
+            fa[1] = s_ * d[1];
+            fa[2] = s_ * d[2];
+        }
+        if (r2 < R.patch_r2) {
+            const Model<float> &M = a.tb.models[R.model];
+            const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
+            const bool single = M.n_types == 1;
+            const int tya = single ? 0 : type_of<float>(M, ida - R.off);
+            const int tyb = single ? 0 : type_of<float>(M, idb - R.off);
+            if (M.np[tya] > 0 && M.np[tyb] > 0) {
+                float Qa[9], Qb[9];
+                load_q(a, sa, xa[3], Qa);
+                load_q(a, sb, xb[3], Qb);
+                const bool a_first = ida < idb;  // canonical order of the reference (p1 < p2)
+                const float sg = a_first ? 1.f : -1.f, inv = 1.f / rr;
+                const float u[3] = {sg * d[0] * inv, sg * d[1] * inv, sg * d[2] * inv};
+                float f[3] = {0.f, 0.f, 0.f}, t1[3] = {0.f, 0.f, 0.f}, t2[3] = {0.f, 0.f, 0.f}, e = 0.f;
+                int nbond = 0;
+                if (a_first) patch_pair<float>(M, tya, tyb, Qa, Qb, u, rr, R.bond_r, f, t1, t2, e, nbond);
+                else patch_pair<float>(M, tyb, tya, Qb, Qa, u, rr, R.bond_r, f, t1, t2, e, nbond);
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    fa[k] += sg * f[k];
+                    ta[k] = a_first ? t1[k] : t2[k];
+                    tb[k] = a_first ? t2[k] : t1[k];
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            fixed_add(acc + 6 * (size_t)sa + k, fa[k]);
+            fixed_add(acc + 6 * (size_t)sb + k, -fa[k]);
+            fixed_add(acc + 6 * (size_t)sa + 3 + k, ta[k]);
+            fixed_add(acc + 6 * (size_t)sb + 3 + k, tb[k]);
+        }
+    }
+    if (big) atomicOr(a.flags, 2u);
+}
+
+// per particle: the summed force and torque (cleared for the next pass), bonds, then the mode's output
+template <int MODE>
+__global__ void __launch_bounds__(kPipeThreads) pair_epilogue_kernel(ForceArgs<float> a, long long *acc) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < a.tb.ntot; s += gridDim.x * blockDim.x) {
+        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, s);
+        const Replica<float> &R = a.tb.reps[r];
+        long long *as = acc + 6 * (size_t)s;
+        float F[3] = {from_fixed(as[0]), from_fixed(as[1]), from_fixed(as[2])};
+        const float T[3] = {from_fixed(as[3]), from_fixed(as[4]), from_fixed(as[5])};
+#pragma unroll
+        for (int k = 0; k < 6; k++) as[k] = 0;
+        const int id = a.buf.ident[s];
+        float xi[4];
+        load4(a.buf.pos + 4 * (size_t)s, xi);
+        if (a.bond_start) {
+            float eb = 0.f;
+            bool big = false;
+            bond_forces<float>(a, R, id, xi[0], xi[1], xi[2], F, eb, big);
+            if (big) atomicOr(a.flags, 2u);
+        }
+        if (MODE == kModeForces) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                a.outF[3 * (size_t)id + k] = F[k];
+                a.outT[3 * (size_t)id + k] = T[k];
+            }
+        } else {
+            float Qi[9];
+            load_q(a, s, xi[3], Qi);
+            langevin_epilogue(a, R, r, s, id, F, T, Qi, xi[0], xi[1], xi[2]);
+        }
+    }
+}
+
+}  // namespace
+}  // namespace mtg

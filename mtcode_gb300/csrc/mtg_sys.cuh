@@ -17,6 +17,7 @@
 #include "mtg_pairs.cuh"
 #include "mtg_sys_base.h"
 #include "mtg_tile.cuh"
+#include "mtg_pipe.cuh"
 
 namespace mtg_impl {
 
@@ -225,6 +226,12 @@ struct Sys : SysBase {
     bool use_tiles = false;
     int4 *d_tiles = nullptr;
     int ntiles = 0, occ_tile = 1;
+    // FP32 pair pipeline (force_kernel 2): pair list, its length, fixed-point force/torque sums per slot
+    bool use_pipe = false;
+    int2 *d_pairs = nullptr;
+    unsigned long long *d_npairs = nullptr;
+    long long *d_acc = nullptr;
+    long long pair_cap = 0;
     // skin lists (null without a skin): state flags, candidate lists and lengths, build positions / cells
     double skin = 0;
     int *d_skin = nullptr, *d_list_n = nullptr, *d_home_cell = nullptr;
@@ -320,7 +327,21 @@ struct Sys : SysBase {
         MTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mtg::scatter_kernel<real, true>, 256, 0));
         occ_stream = std::max(occ, 1);
         if constexpr (std::is_same<real, float>::value) {
-            use_tiles = cfg.force_kernel != 1;
+            use_pipe = cfg.force_kernel == 2;
+            use_tiles = cfg.force_kernel == 0;
+            if (use_pipe) {
+                pair_cap = (long long)mtg::kPairsPerParticle * (long long)n;
+                MTG_CUDA(cudaMalloc(&d_pairs, sizeof(int2) * (size_t)pair_cap));
+                MTG_CUDA(cudaMalloc(&d_npairs, sizeof(unsigned long long)));
+                MTG_CUDA(cudaMemset(d_npairs, 0, sizeof(unsigned long long)));
+                MTG_CUDA(cudaMalloc(&d_acc, sizeof(long long) * 6 * n));
+                MTG_CUDA(cudaMemset(d_acc, 0, sizeof(long long) * 6 * n));
+                if (!d_home_cell) {
+                    MTG_CUDA(cudaMalloc(&d_home_cell, sizeof(int) * n));
+                    MTG_CUDA(cudaMemset(d_home_cell, 0, sizeof(int) * n));
+                    buf[0].home_cell = buf[1].home_cell = d_home_cell;
+                }
+            }
             if (use_tiles) {
                 std::vector<int4> tiles;
                 for (int r = 0; r < nrep; r++)
@@ -357,6 +378,7 @@ struct Sys : SysBase {
         cudaFree(d_tiles);
         cudaFree(d_bond_start); cudaFree(d_bond_partner); cudaFree(d_slot_of);
         cudaFree(d_skin); cudaFree(d_list); cudaFree(d_list_n); cudaFree(d_home_cell); cudaFree(d_xref);
+        cudaFree(d_pairs); cudaFree(d_npairs); cudaFree(d_acc);
         if (h_flags) cudaFreeHost(h_flags);
         if (st) cudaStreamDestroy(st);
     }
@@ -435,6 +457,19 @@ struct Sys : SysBase {
     template <int MODE>
     void launch_force(const mtg::ForceArgs<real> &a) {
         if constexpr (std::is_same<real, float>::value) {
+            if (use_pipe && MODE != mtg::kModeObs && !a.outE) {
+                // with a skin the list is rebuilt only on rebuild steps (the gate); the force and epilogue
+                // passes run every time
+                const int *gate = skin > 0 ? d_skin : nullptr;
+                mtg::pair_reset_kernel<<<1, 32, 0, st>>>(d_npairs, gate);
+                const int gb = (ntot_ + mtg::kPipeThreads - 1) / mtg::kPipeThreads;
+                mtg::pairfind_kernel<<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap,
+                                                                                  skin > 0 ? 1 : 0, gate);
+                mtg::pairforce_kernel<<<sms * 16, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap, d_acc);
+                mtg::pair_epilogue_kernel<MODE><<<grid_for(ntot_, mtg::kPipeThreads, 8, sms), mtg::kPipeThreads, 0, st>>>(
+                    a, d_acc);
+                return;
+            }
             if (use_tiles && MODE != mtg::kModeObs && !a.outE) {
                 const int g = std::max(1, std::min(ntiles, occ_tile * sms));  // persistent: one CTA per SM
                 mtg::tile_force_kernel<MODE><<<g, mtg::kTileThreads, tile_smem, st>>>(a, d_tiles, ntiles);

@@ -114,7 +114,7 @@ class LangevinNVTRGPU:
         cfg.replicas = C.cast(self._descs, C.POINTER(_lib.ReplicaDesc))
         cfg.device = int(device)
         cfg.track_displacement = int(bool(track_displacement))
-        cfg.force_kernel = 1 if force_kernel == "per_particle" else 0
+        cfg.force_kernel = {"tiled": 0, "per_particle": 1, "pairs": 2}[force_kernel]
         cfg.neighbor_skin = float(neighbor_skin)
         h = C.c_void_p()
         st = L.mtg_create(C.byref(cfg), C.byref(h))

@@ -32,7 +32,8 @@ def offsets(W):
     return np.concatenate([[0], np.cumsum([r.n for r in W.replicas])])
 
 
-@pytest.mark.parametrize("precision,kernel", [("fp32", "tiled"), ("fp32", "per_particle"), ("fp64", "tiled")])
+@pytest.mark.parametrize("precision,kernel", [("fp32", "tiled"), ("fp32", "per_particle"), ("fp32", "pairs"),
+                                              ("fp64", "tiled")])
 def test_batched_forces_vs_oracle(precision, kernel):
     W = small_batch(phi=0.3)
     z = W.zeros3()
@@ -52,15 +53,16 @@ def test_tiled_and_per_particle_kernels_agree():
     W = small_batch(seed=5, phi=0.25)
     z = W.zeros3()
     out = {}
-    for kernel in ("tiled", "per_particle"):
+    for kernel in ("tiled", "per_particle", "pairs"):
         with LangevinNVTRGPU(W.replicas, force_kernel=kernel) as s:
             s.initialize(W.x, z, z, W.Q)
             out[kernel] = s.calculate_forces_and_torques3D()
-    assert force_errors(out["tiled"][0], out["per_particle"][0])["rms"] <= 1e-6
-    assert force_errors(out["tiled"][1], out["per_particle"][1])["rms"] <= 1e-6
+    for other in ("per_particle", "pairs"):
+        assert force_errors(out["tiled"][0], out[other][0])["rms"] <= 1e-6
+        assert force_errors(out["tiled"][1], out[other][1])["rms"] <= 1e-6
 
 
-@pytest.mark.parametrize("kernel", ["tiled", "per_particle"])
+@pytest.mark.parametrize("kernel", ["tiled", "per_particle", "pairs"])
 def test_replica_in_batch_equals_replica_alone(kernel):
     W = small_batch(seed=7, n_replicas=6, kT=0.0)
     z = W.zeros3()
@@ -82,12 +84,13 @@ def test_replica_in_batch_equals_replica_alone(kernel):
             assert np.array_equal(batch[key][a:b], alone[key]), (r, key)
 
 
-def test_fp32_steps_are_bitwise_reproducible():
+@pytest.mark.parametrize("kernel", ["tiled", "pairs"])
+def test_fp32_steps_are_bitwise_reproducible(kernel):
     W = small_batch(seed=11, n_replicas=8)
     z = W.zeros3()
     finals = []
     for _ in range(2):
-        with LangevinNVTRGPU(W.replicas) as s:
+        with LangevinNVTRGPU(W.replicas, force_kernel=kernel) as s:
             s.initialize(W.x, z, z, W.Q)
             s.init_forces()
             s.step(40)
@@ -96,12 +99,13 @@ def test_fp32_steps_are_bitwise_reproducible():
         assert np.array_equal(finals[0][key], finals[1][key]), key
 
 
-def test_full_size_batch_newton_third_law_and_finiteness():
+@pytest.mark.parametrize("kernel", ["tiled", "pairs"])
+def test_full_size_batch_newton_third_law_and_finiteness(kernel):
     """The benchmark workload (512 replicas, ~5 M particles): per replica the fixed-point pair sums
     cancel exactly, so the total force is zero to the fixed-point resolution after the float round."""
     W = workloads.patchy_c4(seed=0)
     z = W.zeros3()
-    with LangevinNVTRGPU(W.replicas) as s:
+    with LangevinNVTRGPU(W.replicas, force_kernel=kernel) as s:
         s.initialize(W.x, z, z, W.Q)
         F, T = s.calculate_forces_and_torques3D()
         s.init_forces()

@@ -24,11 +24,11 @@ def tetra(n, phi, **kw):
     return ReplicaSpec(n=n, box=box_for(n, phi), model=PatchModelSpec.tetrahedral(n, 8.0, 1.2, math.acos(0.9)), **kw)
 
 
-def run(specs, x, Q, steps, precision="fp32", skin=0.0, chunks=1, bonds=None, observe=False):
+def run(specs, x, Q, steps, precision="fp32", skin=0.0, chunks=1, bonds=None, observe=False, kernel="tiled"):
     n = len(x)
     z = np.zeros((n, 3))
     out = []
-    with LangevinNVTRGPU(specs, precision=precision, neighbor_skin=skin) as s:
+    with LangevinNVTRGPU(specs, precision=precision, neighbor_skin=skin, force_kernel=kernel) as s:
         s.initialize(x, z, z, Q)
         if bonds is not None:
             s.set_bonds(bonds, 100.0, 1.0)
@@ -42,18 +42,20 @@ def run(specs, x, Q, steps, precision="fp32", skin=0.0, chunks=1, bonds=None, ob
     return out, rebuilds
 
 
+@pytest.mark.parametrize("kernel", ["tiled", "pairs"])
 @pytest.mark.parametrize("skin", [0.3, 0.6])
-def test_fp32_trajectory_is_bit_identical_with_a_skin(skin):
+def test_fp32_trajectory_is_bit_identical_with_a_skin(skin, kernel):
     W = patchy_c4(seed=3, n_replicas=6)
-    exact, _ = run(W.replicas, W.x, W.Q, 40, chunks=3)
-    listed, rebuilds = run(W.replicas, W.x, W.Q, 40, skin=skin, chunks=3)
+    exact, _ = run(W.replicas, W.x, W.Q, 40, chunks=3, kernel=kernel)
+    listed, rebuilds = run(W.replicas, W.x, W.Q, 40, skin=skin, chunks=3, kernel=kernel)
     for a, b in zip(exact, listed):
         for key in ("x", "p", "Lb", "Q", "Ft", "Tt"):
             assert np.array_equal(a[key], b[key]), key
     assert 1 < rebuilds < 121, rebuilds  # lists were reused, and rebuilt
 
 
-def test_fp32_bonded_crowded_and_walled_systems_with_a_skin():
+@pytest.mark.parametrize("kernel", ["tiled", "pairs"])
+def test_fp32_bonded_crowded_and_walled_systems_with_a_skin(kernel):
     sp1, x1, Q1, b1 = None, None, None, None
     n = 40 * 30
     box = box_for(n, 0.25)
@@ -65,8 +67,8 @@ def test_fp32_bonded_crowded_and_walled_systems_with_a_skin():
                         random_positions(1500, sp3.box, False, 0.95, 19)])
     Q = random_rotations(len(x), 20)
     specs = [sp1, sp2, sp3]
-    exact, _ = run(specs, x, Q, 60, chunks=2, bonds=bonds, observe=True)
-    listed, rebuilds = run(specs, x, Q, 60, skin=0.4, chunks=2, bonds=bonds, observe=True)
+    exact, _ = run(specs, x, Q, 60, chunks=2, bonds=bonds, observe=True, kernel=kernel)
+    listed, rebuilds = run(specs, x, Q, 60, skin=0.4, chunks=2, bonds=bonds, observe=True, kernel=kernel)
     for a, b in zip(exact, listed):
         for key in ("x", "p", "Lb", "Q", "Ft", "Tt"):
             assert np.array_equal(a[key], b[key]), key
@@ -85,13 +87,14 @@ def test_fp64_trajectory_with_a_skin():
     assert rebuilds >= 1
 
 
-def test_forces_with_a_skin_match_the_oracle_between_rebuilds():
+@pytest.mark.parametrize("kernel", ["tiled", "pairs"])
+def test_forces_with_a_skin_match_the_oracle_between_rebuilds(kernel):
     spec = tetra(3000, 0.3, seed=8)
     x = random_positions(spec.n, spec.box, True, 0.95, 9)
     Q = random_rotations(spec.n, 10)
     z = np.zeros((spec.n, 3))
     sysm = po.System(spec)
-    with LangevinNVTRGPU([spec], precision="fp32", neighbor_skin=0.5) as s:
+    with LangevinNVTRGPU([spec], precision="fp32", neighbor_skin=0.5, force_kernel=kernel) as s:
         s.initialize(x, z, z, Q)
         s.init_forces()
         for _ in range(4):
