@@ -26,6 +26,13 @@ constexpr int kPipeThreads = 256;
 constexpr int kPairBlockCap = 2048;    // pairs a pairfind block buffers in shared memory
 constexpr int kPairsPerParticle = 16;  // capacity of the pair list (unordered pairs per particle)
 
+// |d|^2 with explicit roundings (no contraction), so that pairfind and pairforce decide a pair at the
+// cutoff identically; with the image shift applied as (x_i - x_j) - s the separation is bit for bit the
+// minimum image's
+__device__ __forceinline__ float sep_r2(float dx, float dy, float dz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
 __device__ __forceinline__ void block_pair_append(int2 *buf, int *nb, int2 p, int2 *pairs,
                                                   unsigned long long *npairs, long long cap, unsigned *flags) {
     // warp-aggregated: the lanes that found a pair in this iteration take consecutive buffer entries
@@ -64,25 +71,33 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
             key = 0;
         }
         const int cx = key % nc, cy = (key / nc) % nc, cz = key / (nc * nc);
-        float xi, yi, zi;
-        load_pos(a.buf.pos + 4 * (size_t)s, xi, yi, zi);
+        const float4 pi = __ldg(reinterpret_cast<const float4 *>(a.buf.pos) + s);
+        const float L = R.box;
         const int lo = nc >= 3 ? -1 : 0, hi = nc >= 2 ? 1 : 0;  // de-duplicated stencil (geometry.h:596-606)
         for (int dz = lo; dz <= hi; dz++) {
             // fewer than three cells per side: every cell of the side is a neighbour, walls or not
             int zz = nc < 3 ? dz : cz + dz;
+            // pairfind runs right after a sort, so every particle lies in its cell: a neighbour cell
+            // reached across a periodic face holds coordinates one box length away (image shift)
+            float shz = 0.f;
             if (zz < 0 || zz >= nc) {
                 if (!R.periodic) continue;
+                shz = zz < 0 ? -L : L;
                 zz = zz < 0 ? zz + nc : zz - nc;
             }
             for (int dy = lo; dy <= hi; dy++) {
                 int yy = nc < 3 ? dy : cy + dy;
+                float shy = 0.f;
                 if (yy < 0 || yy >= nc) {
                     if (!R.periodic) continue;
+                    shy = yy < 0 ? -L : L;
                     yy = yy < 0 ? yy + nc : yy - nc;
                 }
+
                 const int row = R.cell_off + nc * (yy + nc * zz);
                 // the x-range [cx-1, cx+1] as at most two contiguous slot segments
                 int a0, a1, b0 = 0, b1 = 0;
+                float shb = 0.f;  // image shift of the wrapped cell
                 if (nc < 3) {
                     a0 = __ldg(a.start + row);
                     a1 = __ldg(a.start + row + nc);
@@ -92,6 +107,7 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
                     if (R.periodic) {
                         b0 = __ldg(a.start + row + nc - 1);
                         b1 = __ldg(a.start + row + nc);
+                        shb = -L;
                     }
                 } else if (cx == nc - 1) {
                     a0 = __ldg(a.start + row + nc - 2);
@@ -99,6 +115,7 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
                     if (R.periodic) {
                         b0 = __ldg(a.start + row);
                         b1 = __ldg(a.start + row + 1);
+                        shb = L;
                     }
                 } else {
                     a0 = __ldg(a.start + row + cx - 1);
@@ -108,13 +125,16 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
                     int t0 = seg ? b0 : a0;
                     const int t1 = seg ? b1 : a1;
                     if (t0 <= s) t0 = s + 1;  // each unordered pair once: from its lower slot
+                    const float shx = seg ? shb : 0.f;
                     for (int t = t0; t < t1; t++) {
-                        float xj, yj, zj;
-                        load_pos(a.buf.pos + 4 * (size_t)t, xj, yj, zj);
-                        const float dx = min_image<float>(xi - xj, R.box, R.l2s, R.periodic);
-                        const float dy2 = min_image<float>(yi - yj, R.box, R.l2s, R.periodic);
-                        const float dz2 = min_image<float>(zi - zj, R.box, R.l2s, R.periodic);
-                        if (dx * dx + dy2 * dy2 + dz2 * dz2 < range2)
+                        const float4 pj = __ldg(reinterpret_cast<const float4 *>(a.buf.pos) + t);
+                        float dx = (pi.x - pj.x) - shx, dy2 = (pi.y - pj.y) - shy, dz2 = (pi.z - pj.z) - shz;
+                        if (nc < 3) {  // tiny grids: no cell geometry to lean on
+                            dx = min_image<float>(pi.x - pj.x, R.box, R.l2s, R.periodic);
+                            dy2 = min_image<float>(pi.y - pj.y, R.box, R.l2s, R.periodic);
+                            dz2 = min_image<float>(pi.z - pj.z, R.box, R.l2s, R.periodic);
+                        }
+                        if (sep_r2(dx, dy2, dz2) < range2)
                             block_pair_append(buf, &nb, make_int2(s, t), pairs, npairs, cap, a.flags);
                     }
                 }
@@ -141,7 +161,7 @@ __device__ __forceinline__ void fixed_add(long long *acc, float v) {
 }
 
 // forces and torques of the listed pairs into acc (6 fixed-point sums per slot: F lab, T lab)
-__global__ void __launch_bounds__(kPipeThreads) pairforce_kernel(ForceArgs<float> a, const int2 *pairs,
+__global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<float> a, const int2 *pairs,
                                                                  const unsigned long long *npairs, long long cap,
                                                                  long long *acc) {
     const long long n = (long long)*npairs < cap ? (long long)*npairs : cap;
@@ -157,7 +177,7 @@ __global__ void __launch_bounds__(kPipeThreads) pairforce_kernel(ForceArgs<float
         const float d[3] = {min_image<float>(xa[0] - xb[0], R.box, R.l2s, R.periodic),
                             min_image<float>(xa[1] - xb[1], R.box, R.l2s, R.periodic),
                             min_image<float>(xa[2] - xb[2], R.box, R.l2s, R.periodic)};
-        const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        const float r2 = sep_r2(d[0], d[1], d[2]);
         if (!(r2 < R.rc2)) continue;  // skin lists hold pairs up to the list range
         const float rr = sqrtf(r2);
         float fa[3] = {0.f, 0.f, 0.f}, ta[3] = {0.f, 0.f, 0.f}, tb[3] = {0.f, 0.f, 0.f};
@@ -170,13 +190,33 @@ __global__ void __launch_bounds__(kPipeThreads) pairforce_kernel(ForceArgs<float
         }
         if (r2 < R.patch_r2) {
             const Model<float> &M = a.tb.models[R.model];
-            const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
+            const int ida = __ldg(a.buf.ident + sa);
             const bool single = M.n_types == 1;
             const int tya = single ? 0 : type_of<float>(M, ida - R.off);
-            const int tyb = single ? 0 : type_of<float>(M, idb - R.off);
-            if (M.np[tya] > 0 && M.np[tyb] > 0) {
-                float Qa[9], Qb[9];
+            float Qa[9];
+            bool any = M.np[tya] > 0;
+            if (any) {
+                // particle a's own cone test first: its cosines are -(n . Qa (d / r)) in either order of
+                // the pair (the ones patch_pair tests, up to rounding: the 1e-5 margin); most pairs have
+                // no patch of a in any cone and need neither b's orientation nor its type
                 load_q(a, sa, xa[3], Qa);
+                const float inv = 1.f / rr;
+                float w[3];
+#pragma unroll
+                for (int k = 0; k < 3; k++)
+                    w[k] = Qa[3 * k] * (d[0] * inv) + Qa[3 * k + 1] * (d[1] * inv) + Qa[3 * k + 2] * (d[2] * inv);
+                const float mca = M.mincos_any[tya] - 1e-5f;
+                const int oa = M.ooff[tya];
+                any = false;
+                for (int ia = 0; ia < M.np[tya]; ia++) {
+                    const float *v = M.orient[oa + ia];
+                    any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > mca;
+                }
+            }
+            const int idb = any ? __ldg(a.buf.ident + sb) : 0;
+            const int tyb = single || !any ? 0 : type_of<float>(M, idb - R.off);
+            if (any && M.np[tyb] > 0) {
+                float Qb[9];
                 load_q(a, sb, xb[3], Qb);
                 const bool a_first = ida < idb;  // canonical order of the reference (p1 < p2)
                 const float sg = a_first ? 1.f : -1.f, inv = 1.f / rr;
@@ -207,14 +247,19 @@ __global__ void __launch_bounds__(kPipeThreads) pairforce_kernel(ForceArgs<float
 // per particle: the summed force and torque (cleared for the next pass), bonds, then the mode's output
 template <int MODE>
 __global__ void __launch_bounds__(kPipeThreads) pair_epilogue_kernel(ForceArgs<float> a, long long *acc) {
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < a.tb.ntot; s += gridDim.x * blockDim.x) {
+    {
+        const int s = blockIdx.x * blockDim.x + threadIdx.x;  // one particle per thread: many loads in flight
+        if (s >= a.tb.ntot) return;
         const int r = find_replica(a.tb.rep_slot, a.tb.nrep, s);
         const Replica<float> &R = a.tb.reps[r];
-        long long *as = acc + 6 * (size_t)s;
-        float F[3] = {from_fixed(as[0]), from_fixed(as[1]), from_fixed(as[2])};
-        const float T[3] = {from_fixed(as[3]), from_fixed(as[4]), from_fixed(as[5])};
-#pragma unroll
-        for (int k = 0; k < 6; k++) as[k] = 0;
+        longlong2 *as = reinterpret_cast<longlong2 *>(acc + 6 * (size_t)s);  // 48 B per slot: 16-byte aligned
+        const longlong2 s0 = as[0], s1 = as[1], s2 = as[2];
+        float F[3] = {from_fixed(s0.x), from_fixed(s0.y), from_fixed(s1.x)};
+        const float T[3] = {from_fixed(s1.y), from_fixed(s2.x), from_fixed(s2.y)};
+        const longlong2 zero = make_longlong2(0, 0);
+        as[0] = zero;
+        as[1] = zero;
+        as[2] = zero;
         const int id = a.buf.ident[s];
         float xi[4];
         load4(a.buf.pos + 4 * (size_t)s, xi);

@@ -466,8 +466,7 @@ struct Sys : SysBase {
                 mtg::pairfind_kernel<<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap,
                                                                                   skin > 0 ? 1 : 0, gate);
                 mtg::pairforce_kernel<<<sms * 16, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap, d_acc);
-                mtg::pair_epilogue_kernel<MODE><<<grid_for(ntot_, mtg::kPipeThreads, 8, sms), mtg::kPipeThreads, 0, st>>>(
-                    a, d_acc);
+                mtg::pair_epilogue_kernel<MODE><<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_acc);
                 return;
             }
             if (use_tiles && MODE != mtg::kModeObs && !a.outE) {
