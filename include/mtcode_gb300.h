@@ -95,10 +95,10 @@ typedef struct {
     const mtg_replica_desc *replicas;
     int device;                        /* CUDA device ordinal */
     int track_displacement;            /* 1: keep FP64 unwrapped-displacement accumulators */
-    int force_kernel;                  /* FP32 only: 0 = tiled shared-memory kernel (default),
-                                          1 = one thread per particle (the form the FP64 path uses),
-                                          2 = pair pipeline (pair list, one thread per pair, fixed-point
-                                              atomics on both particles, per-particle epilogue) */
+    int force_kernel;                  /* FP32 only: 0 = pair pipeline (default: pair list, one thread per
+                                              pair, fixed-point atomics on both particles, per-particle
+                                              epilogue), 1 = one thread per particle (the form the FP64
+                                              path uses), 2 = tiled shared-memory kernel */
     double neighbor_skin;              /* 0 (default): the cell list is rebuilt every step.  > 0: Verlet
                                           skin (sigma): cells and per-particle candidate lists are built at
                                           force range + skin and reused until some particle has moved more

@@ -327,8 +327,8 @@ struct Sys : SysBase {
         MTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mtg::scatter_kernel<real, true>, 256, 0));
         occ_stream = std::max(occ, 1);
         if constexpr (std::is_same<real, float>::value) {
-            use_pipe = cfg.force_kernel == 2;
-            use_tiles = cfg.force_kernel == 0;
+            use_pipe = cfg.force_kernel == 0;
+            use_tiles = cfg.force_kernel == 2;
             if (use_pipe) {
                 pair_cap = (long long)mtg::kPairsPerParticle * (long long)n;
                 MTG_CUDA(cudaMalloc(&d_pairs, sizeof(int2) * (size_t)pair_cap));

@@ -22,7 +22,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
-    ap.add_argument("--kernel", choices=["tiled", "per_particle", "pairs"], default="tiled")
+    ap.add_argument("--kernel", choices=["pairs", "tiled", "per_particle"], default="pairs")
     ap.add_argument("--profile", action="store_true", help="also print per-kernel device times")
     ap.add_argument("--skin", type=float, default=0.0, help="neighbour skin (sigma); 0 rebuilds cells every step")
     args = ap.parse_args()

@@ -102,7 +102,7 @@ class LangevinNVTRGPU:
     """All replicas of one GPU handle (one CUDA stream)."""
 
     def __init__(self, replicas: list, precision: str = "fp32", device: int = 0, track_displacement: bool = True,
-                 force_kernel: str = "tiled", neighbor_skin: float = 0.0):
+                 force_kernel: str = "pairs", neighbor_skin: float = 0.0):
         """``neighbor_skin`` > 0 (sigma): cells and candidate lists at force range + skin, reused until a
         particle has moved more than half the skin (the same force set as a rebuild every step)."""
         L = _lib.lib()
@@ -114,7 +114,7 @@ class LangevinNVTRGPU:
         cfg.replicas = C.cast(self._descs, C.POINTER(_lib.ReplicaDesc))
         cfg.device = int(device)
         cfg.track_displacement = int(bool(track_displacement))
-        cfg.force_kernel = {"tiled": 0, "per_particle": 1, "pairs": 2}[force_kernel]
+        cfg.force_kernel = {"pairs": 0, "per_particle": 1, "tiled": 2}[force_kernel]
         cfg.neighbor_skin = float(neighbor_skin)
         h = C.c_void_p()
         st = L.mtg_create(C.byref(cfg), C.byref(h))

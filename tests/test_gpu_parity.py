@@ -26,12 +26,12 @@ from oracle import pyoracle as po
 from tests._util import force_errors, load, sorted_pairs, spec_from
 
 pytestmark = pytest.mark.gpu
-PRECISIONS = ["fp32", "fp64", "fp32-pairs"]  # fp32-pairs: the FP32 pair-pipeline force kernel
+PRECISIONS = ["fp32", "fp64", "fp32-tiled"]  # fp32: the default pair pipeline; fp32-tiled: the tile kernel
 
 
 def make(spec, x, Q, precision, p=None, Lb=None, Ft=None, Tt=None):
     n = spec.n
-    s = (LangevinNVTRGPU([spec], precision="fp32", force_kernel="pairs") if precision == "fp32-pairs"
+    s = (LangevinNVTRGPU([spec], precision="fp32", force_kernel="tiled") if precision == "fp32-tiled"
          else LangevinNVTRGPU([spec], precision=precision))
     z = np.zeros((n, 3))
     s.initialize(x, z if p is None else p, z if Lb is None else Lb, Q, Ft, Tt)
