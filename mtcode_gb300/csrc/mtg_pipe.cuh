@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
     __syncthreads();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < a.tb.ntot) {
-        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, s);
+        const int r = __ldg(a.tb.rep_of + s);
         const Replica<float> &R = a.tb.reps[r];
         const float range2 = range_list ? R.rc2_list : R.rc2;
         const int nc = R.nc;
@@ -73,70 +73,76 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
         const int cx = key % nc, cy = (key / nc) % nc, cz = key / (nc * nc);
         const float4 pi = __ldg(reinterpret_cast<const float4 *>(a.buf.pos) + s);
         const float L = R.box;
-        const int lo = nc >= 3 ? -1 : 0, hi = nc >= 2 ? 1 : 0;  // de-duplicated stencil (geometry.h:596-606)
-        for (int dz = lo; dz <= hi; dz++) {
-            // fewer than three cells per side: every cell of the side is a neighbour, walls or not
-            int zz = nc < 3 ? dz : cz + dz;
+        // Each unordered pair once.  With three or more cells per side: the forward half of the stencil
+        // (rows (dy, dz) = (0, 0) [cells x, x + 1], (1, 0), (-1..1, 1) [cells x - 1 .. x + 1]) -- an offset
+        // and its negative are distinct cells, so exactly one of the two particles' scans holds the
+        // other -- and in the own cell only the later slots.  Smaller grids: every cell, later slots.
+        const bool small = nc < 3;
+        const int nrows = small ? 9 : 5;
+        for (int rr = 0; rr < nrows; rr++) {
+            int dy, dz;
+            if (small) {
+                dy = rr % 3;
+                dz = rr / 3;
+                if (dy >= nc || dz >= nc) continue;
+            } else {
+                dy = rr == 0 ? 0 : (rr == 1 ? 1 : rr - 3);
+                dz = rr <= 1 ? 0 : 1;
+            }
             // pairfind runs right after a sort, so every particle lies in its cell: a neighbour cell
             // reached across a periodic face holds coordinates one box length away (image shift)
-            float shz = 0.f;
-            if (zz < 0 || zz >= nc) {
+            int zz = small ? dz : cz + dz, yy = small ? dy : cy + dy;
+            float shz = 0.f, shy = 0.f;
+            if (zz >= nc) {
                 if (!R.periodic) continue;
-                shz = zz < 0 ? -L : L;
-                zz = zz < 0 ? zz + nc : zz - nc;
+                shz = L;
+                zz -= nc;
             }
-            for (int dy = lo; dy <= hi; dy++) {
-                int yy = nc < 3 ? dy : cy + dy;
-                float shy = 0.f;
-                if (yy < 0 || yy >= nc) {
-                    if (!R.periodic) continue;
-                    shy = yy < 0 ? -L : L;
-                    yy = yy < 0 ? yy + nc : yy - nc;
-                }
-
-                const int row = R.cell_off + nc * (yy + nc * zz);
-                // the x-range [cx-1, cx+1] as at most two contiguous slot segments
-                int a0, a1, b0 = 0, b1 = 0;
-                float shb = 0.f;  // image shift of the wrapped cell
-                if (nc < 3) {
-                    a0 = __ldg(a.start + row);
-                    a1 = __ldg(a.start + row + nc);
-                } else if (cx == 0) {
-                    a0 = __ldg(a.start + row);
-                    a1 = __ldg(a.start + row + 2);
-                    if (R.periodic) {
+            if (yy < 0 || yy >= nc) {
+                if (!R.periodic) continue;
+                shy = yy < 0 ? -L : L;
+                yy = yy < 0 ? yy + nc : yy - nc;
+            }
+            const int row = R.cell_off + nc * (yy + nc * zz);
+            // x cells of this row as at most two contiguous slot segments: [a0, a1) unshifted and one
+            // wrapped cell [b0, b1) (image shift shb)
+            int a0, a1, b0 = 0, b1 = 0;
+            float shb = 0.f;
+            if (small) {
+                a0 = __ldg(a.start + row);
+                a1 = __ldg(a.start + row + nc);
+            } else {
+                const int x0 = rr == 0 ? cx : cx - 1, x1 = cx + 1;  // the own row starts at the own cell
+                a0 = __ldg(a.start + row + (x0 < 0 ? 0 : x0));
+                a1 = __ldg(a.start + row + (x1 >= nc ? nc : x1 + 1));
+                if (R.periodic) {
+                    if (x0 < 0) {
                         b0 = __ldg(a.start + row + nc - 1);
                         b1 = __ldg(a.start + row + nc);
                         shb = -L;
-                    }
-                } else if (cx == nc - 1) {
-                    a0 = __ldg(a.start + row + nc - 2);
-                    a1 = __ldg(a.start + row + nc);
-                    if (R.periodic) {
+                    } else if (x1 >= nc) {
                         b0 = __ldg(a.start + row);
                         b1 = __ldg(a.start + row + 1);
                         shb = L;
                     }
-                } else {
-                    a0 = __ldg(a.start + row + cx - 1);
-                    a1 = __ldg(a.start + row + cx + 2);
                 }
-                for (int seg = 0; seg < 2; seg++) {
-                    int t0 = seg ? b0 : a0;
-                    const int t1 = seg ? b1 : a1;
-                    if (t0 <= s) t0 = s + 1;  // each unordered pair once: from its lower slot
-                    const float shx = seg ? shb : 0.f;
-                    for (int t = t0; t < t1; t++) {
-                        const float4 pj = __ldg(reinterpret_cast<const float4 *>(a.buf.pos) + t);
-                        float dx = (pi.x - pj.x) - shx, dy2 = (pi.y - pj.y) - shy, dz2 = (pi.z - pj.z) - shz;
-                        if (nc < 3) {  // tiny grids: no cell geometry to lean on
-                            dx = min_image<float>(pi.x - pj.x, R.box, R.l2s, R.periodic);
-                            dy2 = min_image<float>(pi.y - pj.y, R.box, R.l2s, R.periodic);
-                            dz2 = min_image<float>(pi.z - pj.z, R.box, R.l2s, R.periodic);
-                        }
-                        if (sep_r2(dx, dy2, dz2) < range2)
-                            block_pair_append(buf, &nb, make_int2(s, t), pairs, npairs, cap, a.flags);
+            }
+            const bool own = small || rr == 0;  // rows that hold slots at or below s
+            for (int seg = 0; seg < 2; seg++) {
+                int t0 = seg ? b0 : a0;
+                const int t1 = seg ? b1 : a1;
+                if (own && t0 <= s) t0 = s + 1;
+                const float shx = seg ? shb : 0.f;
+                for (int t = t0; t < t1; t++) {
+                    const float4 pj = __ldg(reinterpret_cast<const float4 *>(a.buf.pos) + t);
+                    float dx = (pi.x - pj.x) - shx, dy2 = (pi.y - pj.y) - shy, dz2 = (pi.z - pj.z) - shz;
+                    if (small) {  // tiny grids: no cell geometry to lean on
+                        dx = min_image<float>(pi.x - pj.x, R.box, R.l2s, R.periodic);
+                        dy2 = min_image<float>(pi.y - pj.y, R.box, R.l2s, R.periodic);
+                        dz2 = min_image<float>(pi.z - pj.z, R.box, R.l2s, R.periodic);
                     }
+                    if (sep_r2(dx, dy2, dz2) < range2)
+                        block_pair_append(buf, &nb, make_int2(s, t), pairs, npairs, cap, a.flags);
                 }
             }
         }
@@ -169,7 +175,7 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
         const int2 pr = pairs[q];
         const int sa = pr.x, sb = pr.y;
-        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, sa);
+        const int r = __ldg(a.tb.rep_of + sa);
         const Replica<float> &R = a.tb.reps[r];
         float xa[4], xb[4];
         load4(a.buf.pos + 4 * (size_t)sa, xa);
@@ -250,7 +256,7 @@ __global__ void __launch_bounds__(kPipeThreads) pair_epilogue_kernel(ForceArgs<f
     {
         const int s = blockIdx.x * blockDim.x + threadIdx.x;  // one particle per thread: many loads in flight
         if (s >= a.tb.ntot) return;
-        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, s);
+        const int r = __ldg(a.tb.rep_of + s);
         const Replica<float> &R = a.tb.reps[r];
         longlong2 *as = reinterpret_cast<longlong2 *>(acc + 6 * (size_t)s);  // 48 B per slot: 16-byte aligned
         const longlong2 s0 = as[0], s1 = as[1], s2 = as[2];
