@@ -127,11 +127,13 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
                     }
                 }
             }
-            const bool own = small || rr == 0;  // rows that hold slots at or below s
+            const bool own = small || rr == 0;  // segments [a0, a1) that hold s's own cell
             for (int seg = 0; seg < 2; seg++) {
                 int t0 = seg ? b0 : a0;
                 const int t1 = seg ? b1 : a1;
-                if (own && t0 <= s) t0 = s + 1;
+                // only the own cell filters by slot; the wrapped cell of the own row is a forward
+                // neighbour whose slots may lie below s
+                if (own && seg == 0 && t0 <= s) t0 = s + 1;
                 const float shx = seg ? shb : 0.f;
                 for (int t = t0; t < t1; t++) {
                     const float4 pj = __ldg(reinterpret_cast<const float4 *>(a.buf.pos) + t);
