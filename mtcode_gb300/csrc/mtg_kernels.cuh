@@ -42,7 +42,6 @@ template <class real>
 struct Tables {
     const Replica<real> *reps;
     const int *rep_slot;   // n_rep + 1 slot offsets (== particle offsets)
-    const int *rep_of;     // replica of every slot (slot ranges never change)
     const Model<real> *models;
     int nrep;
     int ntot;

@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
     __syncthreads();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < a.tb.ntot) {
-        const int r = __ldg(a.tb.rep_of + s);
+        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, s);
         const Replica<float> &R = a.tb.reps[r];
         const float range2 = range_list ? R.rc2_list : R.rc2;
         const int nc = R.nc;
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
         const int2 pr = pairs[q];
         const int sa = pr.x, sb = pr.y;
-        const int r = __ldg(a.tb.rep_of + sa);
+        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, sa);
         const Replica<float> &R = a.tb.reps[r];
         float xa[4], xb[4];
         load4(a.buf.pos + 4 * (size_t)sa, xa);
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(kPipeThreads) pair_epilogue_kernel(ForceArgs<f
     {
         const int s = blockIdx.x * blockDim.x + threadIdx.x;  // one particle per thread: many loads in flight
         if (s >= a.tb.ntot) return;
-        const int r = __ldg(a.tb.rep_of + s);
+        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, s);
         const Replica<float> &R = a.tb.reps[r];
         longlong2 *as = reinterpret_cast<longlong2 *>(acc + 6 * (size_t)s);  // 48 B per slot: 16-byte aligned
         const longlong2 s0 = as[0], s1 = as[1], s2 = as[2];

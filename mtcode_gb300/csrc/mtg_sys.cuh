@@ -203,7 +203,7 @@ struct Sys : SysBase {
 
     mtg::Replica<real> *d_reps = nullptr, *d_reps_obs = nullptr;
     mtg::Model<real> *d_models = nullptr;
-    int *d_rep_slot = nullptr, *d_rep_of = nullptr;
+    int *d_rep_slot = nullptr;
     mtg::Buffers<real> buf[2] = {};
     int cur = 0;
     int2 *d_bin = nullptr;
@@ -281,13 +281,7 @@ struct Sys : SysBase {
         MTG_CUDA(cudaMemcpy(d_reps_obs, reps_obs.data(), sizeof(mtg::Replica<real>) * nrep, cudaMemcpyHostToDevice));
         MTG_CUDA(cudaMemcpy(d_models, models.data(), sizeof(mtg::Model<real>) * nrep, cudaMemcpyHostToDevice));
         MTG_CUDA(cudaMemcpy(d_rep_slot, rep_slot.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice));
-        {
-            std::vector<int> ro((size_t)std::max(ntot_, 1), 0);
-            for (int r = 0; r < nrep; r++)
-                for (int i = rep_slot[r]; i < rep_slot[r + 1]; i++) ro[(size_t)i] = r;
-            MTG_CUDA(cudaMalloc(&d_rep_of, sizeof(int) * ro.size()));
-            MTG_CUDA(cudaMemcpy(d_rep_of, ro.data(), sizeof(int) * ro.size(), cudaMemcpyHostToDevice));
-        }
+
         for (int b = 0; b < 2; b++) {
             MTG_CUDA(cudaMalloc(&buf[b].pos, sizeof(real) * 4 * n));
             MTG_CUDA(cudaMalloc(&buf[b].rota, sizeof(real) * 4 * n));
@@ -379,7 +373,7 @@ struct Sys : SysBase {
             cudaFree(buf[b].pos); cudaFree(buf[b].rota); cudaFree(buf[b].rotb); cudaFree(buf[b].motion); cudaFree(buf[b].ident);
             cudaFree(buf[b].dx); cudaFree(buf[b].dy); cudaFree(buf[b].dz);
         }
-        cudaFree(d_reps); cudaFree(d_reps_obs); cudaFree(d_models); cudaFree(d_rep_slot); cudaFree(d_rep_of);
+        cudaFree(d_reps); cudaFree(d_reps_obs); cudaFree(d_models); cudaFree(d_rep_slot);
         cudaFree(d_bin); cudaFree(d_count); cudaFree(d_start); cudaFree(d_block);
         cudaFree(d_flags); cudaFree(d_draw); cudaFree(d_stage); cudaFree(d_noise); cudaFree(d_obs);
         cudaFree(d_tiles);
@@ -394,7 +388,6 @@ struct Sys : SysBase {
         mtg::Tables<real> t;
         t.reps = obs ? d_reps_obs : d_reps;
         t.rep_slot = d_rep_slot;
-        t.rep_of = d_rep_of;
         t.models = d_models;
         t.nrep = nrep;
         t.ntot = ntot_;
