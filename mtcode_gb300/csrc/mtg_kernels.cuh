@@ -41,21 +41,15 @@ __device__ __forceinline__ bool gated_off(const int *gate, int want) { return ga
 template <class real>
 struct Tables {
     const Replica<real> *reps;
-    const int *rep_slot;   // n_rep + 1 slot offsets (== particle offsets), then the bucket table (find_replica)
+    const int *rep_slot;   // n_rep + 1 slot offsets (== particle offsets)
     const Model<real> *models;
     int nrep;
     int ntot;
     int ncells;
 };
 
-// Replica of slot s.  rep_slot[nrep + 1 + b] is the replica of slot b * kBucket (replica indices grow
-// with the slot), so the replica of s lies between the entries of its bucket and the next: a few
-// steps of binary search over data that stays in L1, instead of log2(nrep).
-constexpr int kBucketShift = 12;
 __device__ __forceinline__ int find_replica(const int *rep_slot, int nrep, int s) {
-    const int *bucket = rep_slot + nrep + 1;
-    int lo = __ldg(bucket + (s >> kBucketShift)), hi = __ldg(bucket + (s >> kBucketShift) + 1) + 1;
-    if (hi > nrep) hi = nrep;  // rep_slot[lo] <= s < rep_slot[hi]
+    int lo = 0, hi = nrep;  // rep_slot[lo] <= s < rep_slot[hi]
     while (hi - lo > 1) {
         int mid = (lo + hi) >> 1;
         if (__ldg(rep_slot + mid) <= s) lo = mid;

@@ -276,22 +276,11 @@ struct Sys : SysBase {
         MTG_CUDA(cudaMalloc(&d_reps, sizeof(mtg::Replica<real>) * nrep));
         MTG_CUDA(cudaMalloc(&d_reps_obs, sizeof(mtg::Replica<real>) * nrep));
         MTG_CUDA(cudaMalloc(&d_models, sizeof(mtg::Model<real>) * nrep));
-        // slot offsets, then the replica of every kBucket-th slot (find_replica's bucket table)
-        std::vector<int> rs_ext(rep_slot.begin(), rep_slot.end());
-        {
-            const int nb = (ntot_ >> mtg::kBucketShift) + 2;
-            int r = 0;
-            for (int b = 0; b < nb; b++) {
-                const long long s0 = (long long)b << mtg::kBucketShift;
-                while (r < nrep - 1 && rep_slot[r + 1] <= s0) r++;
-                rs_ext.push_back(r);
-            }
-        }
-        MTG_CUDA(cudaMalloc(&d_rep_slot, sizeof(int) * rs_ext.size()));
+        MTG_CUDA(cudaMalloc(&d_rep_slot, sizeof(int) * (nrep + 1)));
         MTG_CUDA(cudaMemcpy(d_reps, reps.data(), sizeof(mtg::Replica<real>) * nrep, cudaMemcpyHostToDevice));
         MTG_CUDA(cudaMemcpy(d_reps_obs, reps_obs.data(), sizeof(mtg::Replica<real>) * nrep, cudaMemcpyHostToDevice));
         MTG_CUDA(cudaMemcpy(d_models, models.data(), sizeof(mtg::Model<real>) * nrep, cudaMemcpyHostToDevice));
-        MTG_CUDA(cudaMemcpy(d_rep_slot, rs_ext.data(), sizeof(int) * rs_ext.size(), cudaMemcpyHostToDevice));
+        MTG_CUDA(cudaMemcpy(d_rep_slot, rep_slot.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice));
 
         for (int b = 0; b < 2; b++) {
             MTG_CUDA(cudaMalloc(&buf[b].pos, sizeof(real) * 4 * n));
