@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define MTG_API_VERSION 2
+#define MTG_API_VERSION 3
 
 typedef enum {
     MTG_OK = 0,
@@ -52,6 +52,9 @@ typedef enum { MTG_FP32 = 0, MTG_FP64 = 1 } mtg_precision;
 #define MTG_FLAG_TIMEOUT     0x4u   /* a bounded device wait expired (see MTG_ERR_TIMEOUT) */
 #define MTG_FLAG_OVERFLOW    0x8u   /* a tile's pair list overflowed: handled by the per-particle path */
 #define MTG_FLAG_BINNING     0x10u  /* the cell histogram disagreed with the particle count: step skipped */
+#define MTG_FLAG_BIND        0x20u  /* single-bond mode: the candidate list, a patch's candidate partners (8)
+                                       or a patch cluster (128 patches) outgrew its capacity, or a cluster
+                                       reached one of the reference's error() paths */
 
 typedef struct mtg_system mtg_system;
 
@@ -225,6 +228,74 @@ int64_t mtg_neighbor_rebuilds(mtg_system *h);
 const char *mtg_last_error(const mtg_system *h);
 const char *mtg_status_string(int status);
 int mtg_api_version(void);
+
+/* ---------------------------------------------------------------- single-bond-per-patch mode
+ * Condensate::run_singlebond (Condensate/Condensate.cpp:422-618): every patch holds at most one bond.  Each
+ * force pass runs LangevinNVTR::calculate_forces_and_torques3D_onlyone_nonlets (MDBase/Rotational/
+ * LangevinRforce.cpp:2874-4030): candidate patch pairs that pass the distance and cone tests become edges,
+ * bonds whose partner is no longer a candidate break, and each connected cluster of patches is resolved by
+ * the binding model (one bond per patch); only bound pairs then exert the Kern-Frenkel force and torque,
+ * on top of the WCA core (and any harmonic bonds).  The candidate list (LangevinNVTR::calculate_patch_list,
+ * LangevinR.cpp:1702-1852) is rebuilt every patch_every steps.  Patches are numbered per replica as
+ * GeneralPatch numbers them (GeneralPatch.cpp:285-320; TetrahedralPatch: 4 i + k).
+ * Binding decisions draw counter-based Philox numbers keyed by (replica seed, draw index, cluster's
+ * smallest patch, decision number), the same draw index as the step's noise. */
+
+/* Binding model in table form (MDBase/Bindings).  species_rule: the species of a patch index --
+ *   0 one species (BindingModelSingle), 1 index < div1 ? 1 : 2 (BindingModelBinary),
+ *   2 SortingFunctionUniform (1 below div1, 2 below div2, else 3), 3 SortingFunctionNonUniform
+ *   (as 2, but past div2 only every np-th patch, (index - div2) % np == np - 1, is species 3, the rest 1)
+ *   (BindingModelTernary.h:6-30).
+ * drate rows: species pairs 11, 12, 13, 22, 23, 33 (doubr**): [before * 2 + 0] = rate to unbound,
+ *   [before * 2 + 1] = rate to bound, before = the pair was bound to each other.
+ * trate rows: sorted species triples 111, 112, 113, 122, 123, 133, 222, 223, 233, 333 (tripr***):
+ *   [state * 4 + k], state 0..3 = bound 12 / 23 / 13 / none, k = to 12 / 23 / 13 / none.
+ * A BindingModelTernary's tables are its own rate vectors; mtg_binding_single and
+ * mtg_binding_binary_equilibrium fill the table form of the other two models. */
+typedef struct {
+    int species_rule;
+    int div1, div2, np;
+    double drate[6][4];
+    double trate[10][16];
+} mtg_binding_model;
+
+/* BindingModelSingle(on_rate, off_rate) (Bindings/BindingModelSingle.cpp). */
+void mtg_binding_single(mtg_binding_model *m, double on_rate, double off_rate);
+/* BindingModelBinary(div) + setup_equilibrium() (Bindings/BindingModelBinary.cpp); its 122 and 222 triplets
+ * take the rate to none-bound from tripr111, as the reference's triplet does. */
+void mtg_binding_binary_equilibrium(mtg_binding_model *m, int div);
+
+typedef struct {
+    mtg_binding_model model;
+    double max_ang;     /* ComboPatch::max_ang of the candidate cone test; NAN: GeneralPatch's value,
+                           min(0.6, cos thetam) over the potentials (TetrahedralPatch / BivalentPatch keep
+                           0.6, combopatch.h:15) */
+    double list_cut;    /* candidates come from particle pairs closer than min(list_cut, max_check + 1);
+                           run_singlebond builds its pair list at 2.5 sigma */
+    int patch_every;    /* candidate list rebuilt every patch_every steps (run_singlebond: 10) */
+} mtg_single_bond;
+
+/* max_ang NAN, list_cut 2.5, patch_every 10, model = BindingModelSingle(1, 0). */
+void mtg_single_bond_defaults(mtg_single_bond *sb);
+
+/* Switch a handle to single-bond mode (sb non-null) or back to the full Kern-Frenkel force (sb null).
+ * Needs the pair pipeline or the per-particle force kernel and no neighbour skin.  The bond state starts
+ * all unbound; mtg_init_forces (or the first step) then runs the initial force pass of run_singlebond,
+ * which also decides the first bonds. */
+mtg_status mtg_set_single_bond(mtg_system *h, const mtg_single_bond *sb);
+/* Patches over all replicas, and the first patch of a replica (bond-state arrays are concatenated
+ * replica after replica, each replica's patches in its own numbering). */
+int64_t mtg_num_patches(const mtg_system *h);
+int64_t mtg_patch_offset(const mtg_system *h, int replica);
+/* BinaryBindStore (Bindings/BinaryBindStore.h): boundto (replica-local patch index of the partner) and
+ * isbound (0 / 1) of every patch.  Setting it marks the candidate list for a rebuild at the next pass. */
+mtg_status mtg_set_bind_state(mtg_system *h, const int32_t *boundto, const uint8_t *isbound);
+mtg_status mtg_get_bind_state(mtg_system *h, int32_t *boundto, uint8_t *isbound);
+/* One calculate_forces_and_torques3D_onlyone_nonlets pass at the current state, as run_singlebond's first
+ * call makes it: candidate list rebuilt, bonds decided (consuming one draw index), then F = WCA core
+ * (+ harmonic bonds) + bound-pair forces and T = bound-pair torques (lab), either nullable.  The state
+ * does not move.  Synchronising. */
+mtg_status mtg_bind_update(mtg_system *h, double *F, double *T);
 
 /* Neighbour-pair build that allocates no device memory.  It has no counterpart in the reference.
  * It is for callers that cannot allocate device memory when they need the pair list: code that runs

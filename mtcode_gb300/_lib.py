@@ -24,6 +24,7 @@ MTG_FP32 = 0
 MTG_FP64 = 1
 MTG_FLAG_NONFINITE = 0x1
 MTG_FLAG_FORCE_LIMIT = 0x2
+MTG_FLAG_BIND = 0x20
 
 STATUS = {
     0: "MTG_OK", 1: "MTG_ERR_ARG", 2: "MTG_ERR_CUDA", 3: "MTG_ERR_NOMEM", 4: "MTG_ERR_STATE",
@@ -72,8 +73,30 @@ class Config(C.Structure):
     ]
 
 
+class BindingModel(C.Structure):
+    """mtg_binding_model: species rule, doublet rows (11, 12, 13, 22, 23, 33), triplet rows (111 ... 333)."""
+    _fields_ = [
+        ("species_rule", C.c_int),
+        ("div1", C.c_int),
+        ("div2", C.c_int),
+        ("np", C.c_int),
+        ("drate", (C.c_double * 4) * 6),
+        ("trate", (C.c_double * 16) * 10),
+    ]
+
+
+class SingleBond(C.Structure):
+    _fields_ = [
+        ("model", BindingModel),
+        ("max_ang", C.c_double),
+        ("list_cut", C.c_double),
+        ("patch_every", C.c_int),
+    ]
+
+
 _D = C.POINTER(C.c_double)
 _I32 = C.POINTER(C.c_int32)
+_U8 = C.POINTER(C.c_uint8)
 _H = C.c_void_p
 
 # (name, restype, argtypes) for every entry point of include/mtcode_gb300.h
@@ -119,6 +142,15 @@ SIGNATURES = [
     ("mtg_csv_write", C.c_int, [C.c_char_p, _D, C.c_int64, C.c_int]),
     ("mtg_csv_read", C.c_int, [C.c_char_p, _D, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
     ("mtg_frame_name", C.c_int, [C.c_char_p, C.c_int, C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int]),
+    ("mtg_binding_single", None, [C.POINTER(BindingModel), C.c_double, C.c_double]),
+    ("mtg_binding_binary_equilibrium", None, [C.POINTER(BindingModel), C.c_int]),
+    ("mtg_single_bond_defaults", None, [C.POINTER(SingleBond)]),
+    ("mtg_set_single_bond", C.c_int, [_H, C.POINTER(SingleBond)]),
+    ("mtg_num_patches", C.c_int64, [_H]),
+    ("mtg_patch_offset", C.c_int64, [_H, C.c_int]),
+    ("mtg_set_bind_state", C.c_int, [_H, _I32, _U8]),
+    ("mtg_get_bind_state", C.c_int, [_H, _I32, _U8]),
+    ("mtg_bind_update", C.c_int, [_H, _D, _D]),
 ]
 
 _lib = None

@@ -293,7 +293,39 @@ mtg_status mtg_sync(mtg_system *h) {
         const uint32_t f = h->impl->flags();
         if (f & MTG_FLAG_TIMEOUT) throw Fail{MTG_ERR_TIMEOUT, "a bounded device wait expired"};
         if (f & MTG_FLAG_BINNING) throw Fail{MTG_ERR_STATE, "cell binning incomplete: a step was skipped"};
+        if (f & MTG_FLAG_BIND)
+            throw Fail{MTG_ERR_CAPACITY, "single-bond mode: a candidate list, candidate partners of a patch (8) or "
+                                         "a patch cluster (128) exceeded its capacity"};
         if (f & MTG_FLAG_NONFINITE) return MTG_ERR_NONFINITE;
+    });
+    return MTG_OK;
+}
+
+mtg_status mtg_set_single_bond(mtg_system *h, const mtg_single_bond *sb) {
+    MTG_GUARD(h, h->impl->set_single_bond(sb));
+    return MTG_OK;
+}
+
+int64_t mtg_num_patches(const mtg_system *h) { return h ? h->impl->num_patches() : 0; }
+
+int64_t mtg_patch_offset(const mtg_system *h, int replica) { return h ? h->impl->patch_offset(replica) : 0; }
+
+mtg_status mtg_set_bind_state(mtg_system *h, const int32_t *boundto, const uint8_t *isbound) {
+    MTG_GUARD(h, h->impl->set_bind_state(boundto, isbound));
+    return MTG_OK;
+}
+
+mtg_status mtg_get_bind_state(mtg_system *h, int32_t *boundto, uint8_t *isbound) {
+    MTG_GUARD(h, h->impl->get_bind_state(boundto, isbound));
+    return MTG_OK;
+}
+
+mtg_status mtg_bind_update(mtg_system *h, double *F, double *T) {
+    MTG_GUARD(h, {
+        h->impl->bind_update(F, T);
+        if (h->impl->flags() & MTG_FLAG_BIND)
+            throw Fail{MTG_ERR_CAPACITY, "single-bond mode: a candidate list, candidate partners of a patch (8) or "
+                                         "a patch cluster (128) exceeded its capacity"};
     });
     return MTG_OK;
 }

@@ -253,6 +253,58 @@ int mtg_frame_name(char *out, int cap, const char *kind, const char *strbase, in
     return std::snprintf(out, out ? (size_t)cap : 0, "%s%s_i=%0*d.csv", kind, strbase ? strbase : "", digits, frame);
 }
 
+// BindingModelSingle(on_rate, off_rate) (Bindings/BindingModelSingle.cpp) in table form: a doublet goes to
+// unbound with weight off_rate and to bound with on_rate, whatever it was before; a triplet bound on one edge
+// keeps it with on_rate and moves to each other state with off_rate / 3 + 0.001, an unbound triplet binds each
+// edge with on_rate / 3 and stays unbound with off_rate.
+void mtg_binding_single(mtg_binding_model *m, double on_rate, double off_rate) {
+    if (!m) return;
+    std::memset(m, 0, sizeof(*m));
+    m->species_rule = 0;
+    m->np = 1;
+    m->drate[0][0] = off_rate;
+    m->drate[0][1] = on_rate;
+    m->drate[0][2] = off_rate;
+    m->drate[0][3] = on_rate;
+    const double x = (off_rate / 3.) + 0.001;
+    double *t = m->trate[0];
+    for (int st = 0; st < 3; st++)
+        for (int k = 0; k < 4; k++) t[4 * st + k] = k == st ? on_rate : x;
+    t[12] = on_rate / 3.;
+    t[13] = on_rate / 3.;
+    t[14] = on_rate / 3.;
+    t[15] = off_rate;
+}
+
+// BindingModelBinary(div) + setup_equilibrium() (Bindings/BindingModelBinary.cpp): every species pair binds
+// a doublet for certain; every species triple uses the same triplet table, and the 122 / 222 triplets take
+// their rate to none-bound from the 111 table, as the reference's triplet does.
+void mtg_binding_binary_equilibrium(mtg_binding_model *m, int div) {
+    if (!m) return;
+    std::memset(m, 0, sizeof(*m));
+    m->species_rule = 1;
+    m->div1 = div;
+    m->np = 1;
+    static const double r2[4] = {0.0, 1.0, 0.0, 1.0};
+    static const double t3[16] = {0.998, 0.001, 0.001, 0.000, 0.001, 0.998, 0.001, 0.000,
+                                  0.001, 0.001, 0.998, 0.000, 0.33, 0.33, 0.33, 0.01};
+    const int pair_rows[3] = {0, 1, 3};        // 11, 12, 22
+    const int triple_rows[4] = {0, 1, 3, 6};   // 111, 112, 122, 222
+    for (int r : pair_rows) std::memcpy(m->drate[r], r2, sizeof(r2));
+    for (int r : triple_rows) std::memcpy(m->trate[r], t3, sizeof(t3));
+    for (int r : {3, 6})
+        for (int st = 0; st < 4; st++) m->trate[r][4 * st + 3] = m->trate[0][4 * st + 3];
+}
+
+void mtg_single_bond_defaults(mtg_single_bond *sb) {
+    if (!sb) return;
+    std::memset(sb, 0, sizeof(*sb));
+    mtg_binding_single(&sb->model, 1.0, 0.0);
+    sb->max_ang = std::nan("");
+    sb->list_cut = 2.5;
+    sb->patch_every = 10;
+}
+
 // Arvo, "Fast random rotation matrices" (Graphics Gems III, 1992): M = (2 v v^T - I) Rz(2 pi x1),
 // v = (cos(2 pi x2) sqrt(x3), sin(2 pi x2) sqrt(x3), sqrt(1 - x3)) -- the construction of
 // LangevinNVTR::initialize (LangevinR.cpp:239-267), driven by splitmix64 instead of rand().

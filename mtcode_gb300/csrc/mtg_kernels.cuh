@@ -410,6 +410,42 @@ __global__ void __launch_bounds__(256) copy_back_kernel(int ntot, Buffers<real> 
 
 // ------------------------------------------------------------------ force + Langevin epilogue
 
+// per replica: patch numbering (GeneralPatch, GeneralPatch.cpp:285-320) and the FP64 constants of the tests
+struct BindRep {
+    int patch_off, npatch;
+    int pbase[kMaxTypes + 1];     // first local patch of each type; pbase[n_types] = patches of the replica
+    int reach;                    // candidate stencil half-width in force-grid cells
+    int periodic;
+    uint32_t seed_lo, seed_hi;
+    double box, l2s;              // cube::l, (l/2)^2
+    double orient[kMaxOrient][3]; // body-frame patch vectors
+    double ctm[kMaxPots];         // cos(thetam) of each potential
+    double disp[kMaxPots];        // interaction_distance = 1.4 dis (potentialtheta.h:416)
+    double mk2;                   // ComboPatch::max_check^2
+    double max_dis;               // max_check + 1 (calculate_patch_list)
+    double list_cut2;             // squared pair-list cut the candidates come from (run_singlebond: 2.5 sigma)
+    double max_ang;               // ComboPatch::max_ang
+};
+
+// ------------------------------------------------------------------ patch numbering
+template <class real>
+__device__ __forceinline__ int patch_of(const BindRep &B, const Model<real> &M, int li, int t, int c) {
+    return B.patch_off + B.pbase[t] + (li - (t ? M.ncum[t - 1] : 0)) * M.np[t] + c;
+}
+
+// GeneralPatch::which_particle: local particle, type and patch number of local patch lp
+template <class real>
+__device__ __forceinline__ void patch_owner(const BindRep &B, const Model<real> &M, int lp, int &li, int &t, int &c) {
+    t = 0;
+#pragma unroll
+    for (int k = 1; k < kMaxTypes; k++)
+        if (k < M.n_types && lp >= B.pbase[k]) t = k;
+    const int rel = lp - B.pbase[t], np = M.np[t] > 0 ? M.np[t] : 1;
+    li = (t ? M.ncum[t - 1] : 0) + rel / np;
+    c = rel % np;
+}
+
+
 template <class real>
 struct ForceArgs {
     Tables<real> tb;
@@ -433,6 +469,10 @@ struct ForceArgs {
     int *skin_next;
     unsigned *list;
     int *list_n;
+    // single-bond-per-patch mode (null otherwise): patch numbering per replica, bond state by global patch
+    const BindRep *bind_reps;
+    const unsigned char *bind_on;
+    const int *bind_to;
 };
 
 // skin lists: flags the next step for a rebuild when slot s's next position (xn) is more than half the
@@ -470,6 +510,57 @@ __device__ __forceinline__ void bond_forces(const ForceArgs<real> &a, const Repl
         f[1] += f1 * dy / r;
         f[2] += f1 * dz / r;
         e += real(0.25) * a.bond_k * (r - a.bond_r0) * (r - a.bond_r0);
+    }
+}
+
+// ------------------------------------------------------------------ bound-pair forces (force epilogue)
+// KernFrenkelOnePatch2::force_and_torque of every bound patch of particle idi (LangevinRforce.cpp:3940-4030):
+// each pair is evaluated in its canonical order (lower particle index first) from both of its ends, so the
+// two ends see equal and opposite forces bit for bit.  Adds the force and the lab torque on idi, and half of
+// each pair's energy.
+template <class real>
+__device__ __forceinline__ void bound_patch_forces(const ForceArgs<real> &a, const Replica<real> &R,
+                                                   const Model<real> &M, int r, int idi, const real Pi[12], real f[3],
+                                                   real t[3], real &e) {
+    const BindRep &B = a.bind_reps[r];
+    const int li = idi - R.off, ti = type_of<real>(M, li), na = M.np[ti];
+    for (int ka = 0; ka < na; ka++) {
+        const int wp = patch_of<real>(B, M, li, ti, ka);
+        if (!a.bind_on[wp]) continue;
+        const int wq = a.bind_to[wp];
+        int lj, tj, kb;
+        patch_owner<real>(B, M, wq - B.patch_off, lj, tj, kb);
+        const int sj = a.buf.slot_of[R.off + lj];
+        Payload<real> Pj;
+        Pj.load(a.buf.pos, a.buf.rota, a.buf.rotb, sj);
+        const bool i_first = li < lj;
+        const real *P1 = i_first ? Pi : Pj.v, *P2 = i_first ? Pj.v : Pi;
+        const int t1 = i_first ? ti : tj, t2 = i_first ? tj : ti, c1 = i_first ? ka : kb, c2 = i_first ? kb : ka;
+        const real dx = min_image<real>(P1[0] - P2[0], R.box, R.l2s, R.periodic);
+        const real dy = min_image<real>(P1[1] - P2[1], R.box, R.l2s, R.periodic);
+        const real dz = min_image<real>(P1[2] - P2[2], R.box, R.l2s, R.periodic);
+        const real rr = sqrt(dx * dx + dy * dy + dz * dz);
+        const int q = M.pstart[t1][t2] + c1 * M.np[t2] + c2;
+        if (rr > M.rmax[q]) continue;   // interaction_distance (potentialtheta.h:522)
+        const real u[3] = {dx / rr, dy / rr, dz / rr};
+        const real *b1 = M.orient[M.ooff[t1] + c1], *b2 = M.orient[M.ooff[t2] + c2];
+        real n1[3], n2[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            n1[k] = b1[0] * P1[3 + k] + b1[1] * P1[6 + k] + b1[2] * P1[9 + k];
+            n2[k] = b2[0] * P2[3 + k] + b2[1] * P2[6 + k] + b2[2] * P2[9 + k];
+        }
+        const real ci = -(n1[0] * u[0] + n1[1] * u[1] + n1[2] * u[2]);
+        const real cj = n2[0] * u[0] + n2[1] * u[1] + n2[2] * u[2];
+        if (!(ci > M.costm[q] && cj > M.costm[q])) continue;
+        real fa[3] = {0, 0, 0}, ta[3] = {0, 0, 0}, tb[3] = {0, 0, 0}, ee = 0;
+        kf2_pair<real>(M.att[q], M.dis[q], M.inv_dis[q], M.kfac[q], u, rr, n1, n2, ci, cj, fa, ta, tb, ee);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            f[k] += i_first ? fa[k] : -fa[k];
+            t[k] += i_first ? ta[k] : tb[k];
+        }
+        e += real(0.5) * ee;
     }
 }
 
@@ -625,6 +716,12 @@ __device__ __noinline__ void simple_particle(const ForceArgs<real> &a, int s) {
             real fb[3] = {real(0), real(0), real(0)};
             bond_forces<real>(a, R, idi, xi, yi, zi, fb, ebond, big);
             F.add(fb[0], fb[1], fb[2]);
+        }
+        if (a.bind_on && MODE != kModeObs) {
+            real fb[3] = {real(0), real(0), real(0)}, tb[3] = {real(0), real(0), real(0)};
+            bound_patch_forces<real>(a, R, Mo, r, idi, P.v, fb, tb, epatch);
+            F.add(fb[0], fb[1], fb[2]);
+            T.add(tb[0], tb[1], tb[2]);
         }
         if (big) atomicOr(a.flags, 2u);
 

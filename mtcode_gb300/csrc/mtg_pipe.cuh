@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(kPipeThreads) pair_epilogue_kernel(ForceArgs<f
         longlong2 *as = reinterpret_cast<longlong2 *>(acc + 6 * (size_t)s);  // 48 B per slot: 16-byte aligned
         const longlong2 s0 = as[0], s1 = as[1], s2 = as[2];
         float F[3] = {from_fixed(s0.x), from_fixed(s0.y), from_fixed(s1.x)};
-        const float T[3] = {from_fixed(s1.y), from_fixed(s2.x), from_fixed(s2.y)};
+        float T[3] = {from_fixed(s1.y), from_fixed(s2.x), from_fixed(s2.y)};
         const longlong2 zero = make_longlong2(0, 0);
         as[0] = zero;
         as[1] = zero;
@@ -276,6 +276,12 @@ __global__ void __launch_bounds__(kPipeThreads) pair_epilogue_kernel(ForceArgs<f
             bool big = false;
             bond_forces<float>(a, R, id, xi[0], xi[1], xi[2], F, eb, big);
             if (big) atomicOr(a.flags, 2u);
+        }
+        if (a.bind_on) {
+            Payload<float> P;
+            P.load(a.buf.pos, a.buf.rota, a.buf.rotb, s);
+            float eb = 0.f;
+            bound_patch_forces<float>(a, R, a.tb.models[R.model], r, id, P.v, F, T, eb);
         }
         if (MODE == kModeForces) {
 #pragma unroll

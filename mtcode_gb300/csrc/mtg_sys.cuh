@@ -18,6 +18,7 @@
 #include "mtg_sys_base.h"
 #include "mtg_tile.cuh"
 #include "mtg_pipe.cuh"
+#include "mtg_bind.cuh"
 
 namespace mtg_impl {
 
@@ -240,6 +241,20 @@ struct Sys : SysBase {
     size_t tile_smem = 0;
     // occupancy-derived grid caps
     int occ_force = 1, occ_stream = 1;
+    // single-bond-per-patch mode (Condensate::run_singlebond): patch numbering, binding model, candidate
+    // list, per-update adjacency, bond state (global patch indices), large-cluster queue and scratch
+    bool single_bond = false;
+    int ptot = 0, patch_every = 10, scratch_threads = 0;
+    std::vector<int> patch_slot;
+    std::vector<mtg::Replica<real>> reps_full;   // replica constants with the full patch force
+    mtg::BindRep *d_brep = nullptr;
+    mtg::BindModel *d_bmodel = nullptr;
+    int *d_patch_slot = nullptr, *d_boundto = nullptr, *d_large = nullptr, *d_scratch = nullptr;
+    int4 *d_plist = nullptr;
+    long long plist_cap = 0;
+    unsigned long long *d_bctr = nullptr, *d_deg = nullptr;
+    int2 *d_adj = nullptr;
+    unsigned char *d_isbound = nullptr;
 
     Sys(const mtg_config &cfg) {
         device = cfg.device;
@@ -380,6 +395,7 @@ struct Sys : SysBase {
         cudaFree(d_bond_start); cudaFree(d_bond_partner); cudaFree(d_slot_of);
         cudaFree(d_skin); cudaFree(d_list); cudaFree(d_list_n); cudaFree(d_home_cell); cudaFree(d_xref);
         cudaFree(d_pairs); cudaFree(d_npairs); cudaFree(d_acc);
+        free_bind();
         if (h_flags) cudaFreeHost(h_flags);
         if (st) cudaStreamDestroy(st);
     }
@@ -451,7 +467,269 @@ struct Sys : SysBase {
             a.bond_k = (real)bond_k;
             a.bond_r0 = (real)bond_r0;
         }
+        if (single_bond) {
+            a.bind_reps = d_brep;
+            a.bind_on = d_isbound;
+            a.bind_to = d_boundto;
+        }
         return a;
+    }
+
+    // ---------------------------------------------------------------- single-bond-per-patch mode
+    static constexpr int kBindLaunches = 5;   // begin, candidates, edges, decide, large
+
+    mtg::BindState bind_state() const {
+        mtg::BindState S;
+        std::memset(&S, 0, sizeof(S));
+        S.reps = d_brep;
+        S.model = d_bmodel;
+        S.patch_slot = d_patch_slot;
+        S.nrep = nrep;
+        S.ptot = ptot;
+        S.patch_every = patch_every;
+        S.plist = d_plist;
+        S.plist_cap = plist_cap;
+        S.ctr = d_bctr;
+        S.deg = d_deg;
+        S.adj = d_adj;
+        S.boundto = d_boundto;
+        S.isbound = d_isbound;
+        S.large = d_large;
+        S.scratch = d_scratch;
+        S.scratch_threads = scratch_threads;
+        S.flags = d_flags;
+        S.draw = d_draw;
+        return S;
+    }
+
+    // this update's stamp and, when due (or forced), the candidate list from buffer b, whose cells the
+    // current cell starts describe
+    void enqueue_bind_begin(int b, int force, int advance) {
+        const mtg::BindState S = bind_state();
+        mtg::bind_begin_kernel<<<1, 32, 0, st>>>(S, force, advance);
+        const int g = std::max(1, (ntot_ + 255) / 256);
+        mtg::bind_candidates_kernel<real><<<g, 256, 0, st>>>(force_args(b, 0), S);
+    }
+
+    // edges, clusters and bond decisions on buffer b (positions reached through slot_of)
+    void enqueue_bind_decide(int b) {
+        const mtg::BindState S = bind_state();
+        const mtg::ForceArgs<real> a = force_args(b, 0);
+        mtg::bind_edge_kernel<real><<<sms * 8, 256, 0, st>>>(a, S);
+        mtg::bind_decide_kernel<<<std::max(1, (ptot + 255) / 256), 256, 0, st>>>(S);
+        mtg::bind_large_kernel<real><<<scratch_threads / mtg::kLargeThreads, mtg::kLargeThreads, 0, st>>>(a, S);
+    }
+
+    void free_bind() {
+        cudaFree(d_brep); cudaFree(d_bmodel); cudaFree(d_patch_slot); cudaFree(d_boundto); cudaFree(d_large);
+        cudaFree(d_scratch); cudaFree(d_plist); cudaFree(d_bctr); cudaFree(d_deg); cudaFree(d_adj);
+        cudaFree(d_isbound);
+        d_brep = nullptr; d_bmodel = nullptr; d_patch_slot = d_boundto = d_large = d_scratch = nullptr;
+        d_plist = nullptr; d_bctr = d_deg = nullptr; d_adj = nullptr; d_isbound = nullptr;
+    }
+
+    void drop_graphs() {
+        for (int b = 0; b < 2; b++) {
+            if (graph[b]) cudaGraphExecDestroy(graph[b]);
+            graph[b] = nullptr;
+        }
+    }
+
+    void ensure_slot_of() {
+        if (d_slot_of) return;
+        MTG_CUDA(cudaMalloc(&d_slot_of, sizeof(int) * (size_t)std::max(ntot_, 1)));
+        buf[0].slot_of = buf[1].slot_of = d_slot_of;
+        if (have_state) {
+            const int g = grid_for(ntot_, 256, occ_stream, sms);
+            mtg::slot_map_kernel<<<g, 256, 0, st>>>(ntot_, buf[cur].ident, d_slot_of);
+            check_launch();
+            nlaunch += 1;
+        }
+    }
+
+    void set_single_bond(const mtg_single_bond *sb) override {
+        MTG_CUDA(cudaStreamSynchronize(st));
+        if (!sb) {
+            if (!single_bond) return;
+            drop_graphs();
+            free_bind();
+            single_bond = false;
+            reps = reps_full;
+            MTG_CUDA(cudaMemcpy(d_reps, reps.data(), sizeof(mtg::Replica<real>) * nrep, cudaMemcpyHostToDevice));
+            forces_ready = false;
+            return;
+        }
+        MTG_REQUIRE(skin <= 0, "mtg_set_single_bond: not available with a neighbour skin");
+        MTG_REQUIRE(!use_tiles, "mtg_set_single_bond: needs the pair pipeline or the per-particle force kernel");
+        const mtg_binding_model &bm = sb->model;
+        MTG_REQUIRE(bm.species_rule >= 0 && bm.species_rule <= 3, "mtg_set_single_bond: species_rule must be 0..3");
+        MTG_REQUIRE(bm.species_rule != 3 || bm.np >= 1, "mtg_set_single_bond: SortingFunctionNonUniform needs np >= 1");
+        for (int r = 0; r < 6; r++)
+            for (int k = 0; k < 4; k++) MTG_REQUIRE(std::isfinite(bm.drate[r][k]), "mtg_set_single_bond: rates must be finite");
+        for (int r = 0; r < 10; r++)
+            for (int k = 0; k < 16; k++) MTG_REQUIRE(std::isfinite(bm.trate[r][k]), "mtg_set_single_bond: rates must be finite");
+        MTG_REQUIRE(sb->patch_every >= 1, "mtg_set_single_bond: patch_every must be >= 1");
+        MTG_REQUIRE(std::isfinite(sb->list_cut) && sb->list_cut > 0, "mtg_set_single_bond: list_cut must be positive");
+        MTG_REQUIRE(std::isnan(sb->max_ang) || std::isfinite(sb->max_ang), "mtg_set_single_bond: max_ang must be finite or NAN");
+        // patch numbering (GeneralPatch total_patches_per_type) and the FP64 constants of every replica
+        std::vector<mtg::BindRep> br((size_t)nrep);
+        std::vector<int> pslot(1, 0);
+        int64_t poff = 0;
+        for (int r = 0; r < nrep; r++) {
+            const mtg_replica_desc &d = desc[r];
+            const mtg_patch_model &m = d.model;
+            mtg::BindRep &B = br[(size_t)r];
+            std::memset(&B, 0, sizeof(B));
+            int base = 0;
+            for (int k = 0; k < m.n_types; k++) {
+                B.pbase[k] = base;
+                base += m.patches_per_type[k] * (m.count_per_type[k] - (k ? m.count_per_type[k - 1] : 0));
+            }
+            for (int k = m.n_types; k <= mtg::kMaxTypes; k++) B.pbase[k] = base;
+            B.patch_off = (int)poff;
+            B.npatch = base;
+            B.periodic = d.periodic ? 1 : 0;
+            B.seed_lo = (uint32_t)d.seed;
+            B.seed_hi = (uint32_t)(d.seed >> 32);
+            B.box = d.box;
+            B.l2s = (d.box / 2.) * (d.box / 2.);
+            int no = 0;
+            for (int k = 0; k < m.n_types; k++) no += m.patches_per_type[k];
+            for (int i = 0; i < no; i++)
+                for (int c = 0; c < 3; c++) B.orient[i][c] = m.orient[i][c];
+            double mc = 1.0, ma = 0.6;   // ComboPatch defaults (combopatch.h:15)
+            const int npots = n_pots_of(m);
+            for (int q = 0; q < npots; q++) {
+                B.ctm[q] = std::cos(m.params[q][2]);
+                B.disp[q] = 1.4 * m.params[q][1];
+                mc = std::max(mc, B.disp[q]);
+                ma = std::min(ma, B.ctm[q]);
+            }
+            B.mk2 = mc * mc;
+            B.max_dis = mc + 1.;
+            B.list_cut2 = sb->list_cut * sb->list_cut;
+            B.max_ang = std::isnan(sb->max_ang) ? ma : sb->max_ang;
+            const double side = d.box / reps[r].nc, range = std::min(sb->list_cut, mc + 1.);
+            B.reach = std::max(1, (int)std::ceil(range / side));
+            MTG_REQUIRE(B.reach <= 2 || reps[r].nc <= 4,
+                        "mtg_set_single_bond: the candidate range spans more than two force-grid cells");
+            poff += base;
+            MTG_REQUIRE(poff < (int64_t)INT32_MAX, "mtg_set_single_bond: too many patches");
+            pslot.push_back((int)poff);
+        }
+        mtg::BindModel hm;
+        std::memset(&hm, 0, sizeof(hm));
+        hm.rule = bm.species_rule;
+        hm.div1 = bm.div1;
+        hm.div2 = bm.div2;
+        hm.np = bm.np >= 1 ? bm.np : 1;
+        std::memcpy(hm.drate, bm.drate, sizeof(hm.drate));
+        std::memcpy(hm.trate, bm.trate, sizeof(hm.trate));
+
+        drop_graphs();
+        free_bind();
+        ptot = (int)poff;
+        patch_every = sb->patch_every;
+        patch_slot = pslot;
+        const size_t np = (size_t)std::max(ptot, 1);
+        plist_cap = std::min<long long>((1LL << 29) - 1, 64LL * std::max(ntot_, 1) + 1024);
+        scratch_threads = std::max(1, sms) * 8;
+        scratch_threads = (scratch_threads + mtg::kLargeThreads - 1) / mtg::kLargeThreads * mtg::kLargeThreads;
+        MTG_CUDA(cudaMalloc(&d_brep, sizeof(mtg::BindRep) * nrep));
+        MTG_CUDA(cudaMalloc(&d_bmodel, sizeof(mtg::BindModel)));
+        MTG_CUDA(cudaMalloc(&d_patch_slot, sizeof(int) * (nrep + 1)));
+        MTG_CUDA(cudaMalloc(&d_plist, sizeof(int4) * (size_t)plist_cap));
+        MTG_CUDA(cudaMalloc(&d_bctr, sizeof(unsigned long long) * 8));
+        MTG_CUDA(cudaMalloc(&d_deg, sizeof(unsigned long long) * np));
+        MTG_CUDA(cudaMalloc(&d_adj, sizeof(int2) * mtg::kAdjCap * np));
+        MTG_CUDA(cudaMalloc(&d_boundto, sizeof(int) * np));
+        MTG_CUDA(cudaMalloc(&d_isbound, np));
+        MTG_CUDA(cudaMalloc(&d_large, sizeof(int) * np));
+        MTG_CUDA(cudaMalloc(&d_scratch, sizeof(int) * (size_t)mtg::kScratchInts * scratch_threads));
+        MTG_CUDA(cudaMemcpy(d_brep, br.data(), sizeof(mtg::BindRep) * nrep, cudaMemcpyHostToDevice));
+        MTG_CUDA(cudaMemcpy(d_bmodel, &hm, sizeof(hm), cudaMemcpyHostToDevice));
+        MTG_CUDA(cudaMemcpy(d_patch_slot, pslot.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice));
+        MTG_CUDA(cudaMemset(d_bctr, 0, sizeof(unsigned long long) * 8));
+        MTG_CUDA(cudaMemset(d_deg, 0, sizeof(unsigned long long) * np));
+        MTG_CUDA(cudaMemset(d_boundto, 0, sizeof(int) * np));
+        MTG_CUDA(cudaMemset(d_isbound, 0, np));
+        ensure_slot_of();
+        // the force pass keeps the WCA core only: no pair reaches the patch term, and the pair range
+        // shrinks to the WCA range (padded so that no rounding of r^2 against r drops a core pair)
+        if (!single_bond) reps_full = reps;
+        reps = reps_full;
+        for (int r = 0; r < nrep; r++) {
+            const double hs = 1.12246 * desc[r].hs_sigma * (1 + 1e-6);
+            reps[r].patch_r2 = (real)0;
+            reps[r].rc2 = (real)(hs * hs);
+        }
+        MTG_CUDA(cudaMemcpy(d_reps, reps.data(), sizeof(mtg::Replica<real>) * nrep, cudaMemcpyHostToDevice));
+        single_bond = true;
+        forces_ready = false;
+        MTG_CUDA(cudaStreamSynchronize(st));
+    }
+
+    int64_t num_patches() const override { return single_bond ? ptot : 0; }
+    int64_t patch_offset(int r) const override {
+        return single_bond && r >= 0 && r <= nrep ? patch_slot[(size_t)r] : -1;
+    }
+
+    void set_bind_state(const int32_t *bt, const uint8_t *ib) override {
+        MTG_REQUIRE(single_bond, "mtg_set_bind_state: the handle is not in single-bond mode");
+        MTG_REQUIRE(bt && ib, "mtg_set_bind_state: boundto and isbound are required");
+        std::vector<int> g((size_t)std::max(ptot, 1));
+        std::vector<unsigned char> b((size_t)std::max(ptot, 1));
+        for (int r = 0; r < nrep; r++) {
+            const int o = patch_slot[(size_t)r], n = patch_slot[(size_t)r + 1] - o;
+            for (int i = 0; i < n; i++) {
+                const int v = bt[o + i];
+                MTG_REQUIRE(v >= 0 && v < n, "mtg_set_bind_state: boundto[" + std::to_string(o + i) + "] = " +
+                                                 std::to_string(v) + " is not a patch of its replica");
+                g[(size_t)(o + i)] = o + v;
+                b[(size_t)(o + i)] = ib[o + i] ? 1 : 0;
+            }
+        }
+        MTG_CUDA(cudaMemcpyAsync(d_boundto, g.data(), sizeof(int) * (size_t)ptot, cudaMemcpyHostToDevice, st));
+        MTG_CUDA(cudaMemcpyAsync(d_isbound, b.data(), (size_t)ptot, cudaMemcpyHostToDevice, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+    }
+
+    void get_bind_state(int32_t *bt, uint8_t *ib) override {
+        MTG_REQUIRE(single_bond, "mtg_get_bind_state: the handle is not in single-bond mode");
+        std::vector<int> g((size_t)std::max(ptot, 1));
+        std::vector<unsigned char> b((size_t)std::max(ptot, 1));
+        MTG_CUDA(cudaMemcpyAsync(g.data(), d_boundto, sizeof(int) * (size_t)ptot, cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaMemcpyAsync(b.data(), d_isbound, (size_t)ptot, cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+        for (int r = 0; r < nrep; r++) {
+            const int o = patch_slot[(size_t)r], n = patch_slot[(size_t)r + 1] - o;
+            for (int i = 0; i < n; i++) {
+                if (bt) bt[o + i] = g[(size_t)(o + i)] - o;
+                if (ib) ib[o + i] = b[(size_t)(o + i)];
+            }
+        }
+    }
+
+    void bind_update(double *F, double *T) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_bind_update: no state has been set"};
+        MTG_REQUIRE(single_bond, "mtg_bind_update: the handle is not in single-bond mode");
+        if (!cells_valid) rebuild_cells(false);
+        tick_draw();
+        enqueue_bind_begin(cur, 1, 0);
+        enqueue_bind_decide(cur);
+        check_launch();
+        nlaunch += kBindLaunches;
+        size_t n = (size_t)ntot_;
+        double *sF = d_stage, *sT = sF + 3 * n;
+        mtg::ForceArgs<real> a = force_args(cur, 0);
+        a.outF = sF;
+        a.outT = sT;
+        launch_force<mtg::kModeForces>(a);
+        check_launch();
+        nlaunch += 1;
+        if (F) MTG_CUDA(cudaMemcpyAsync(F, sF, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        if (T) MTG_CUDA(cudaMemcpyAsync(T, sT, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
     }
 
     // force pass in the given mode: the FP32 tile kernel where it applies, else the per-particle kernel
@@ -531,9 +809,11 @@ struct Sys : SysBase {
             return;
         }
         mtg::Tables<real> tb = tables();
+        if (single_bond) enqueue_bind_begin(b, 0, 1);   // candidates from the positions at the step's start
         scan(ncells, true);
         const int g = grid_for(ntot_, 256, occ_stream, sms);
         mtg::scatter_kernel<real, true><<<g, 256, 0, st>>>(tb, buf[b], buf[b ^ 1], d_bin, d_start, d_flags);
+        if (single_bond) enqueue_bind_decide(b ^ 1);
         mtg::ForceArgs<real> a = force_args(b ^ 1, 1);
         a.ext_noise = ext_noise;
         launch_force<mtg::kModeStep>(a);
@@ -617,6 +897,11 @@ struct Sys : SysBase {
             set_skin(1, 0, 0);  // this pass builds the lists (a rebuild)
             count_rebuild();
         }
+        if (single_bond) {   // run_singlebond's first onlyone_nonlets call (Condensate.cpp:455-460)
+            enqueue_bind_begin(cur, 1, 0);
+            enqueue_bind_decide(cur);
+            nlaunch += kBindLaunches;
+        }
         mtg::ForceArgs<real> a = force_args(cur, 0);
         if (noise) a.ext_noise = upload_noise(noise);
         launch_force<mtg::kModeInit>(a);
@@ -696,6 +981,7 @@ struct Sys : SysBase {
         if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_step: no state has been set"};
         MTG_REQUIRE(nsteps >= 0, "mtg_step: nsteps must be >= 0");
         if (!forces_ready) init_forces(nullptr);
+        if (single_bond && !cells_valid) rebuild_cells(false);   // the candidate pass reads the force grid
         if (skin > 0) {
             if (!cells_valid) set_skin(-1, -1, 1);  // the buffer was re-sorted by another grid: rebuild first
         } else if (!bins_valid) {
@@ -714,7 +1000,7 @@ struct Sys : SysBase {
             for (int s = 0; s < nsteps; s++) {
                 enqueue_step(cur, upload_noise(noise + (size_t)s * 6 * n));
                 if (skin <= 0) cur ^= 1;  // a skin step leaves the state in the buffer it started in
-                nlaunch += skin > 0 ? 9 : 5;
+                nlaunch += (skin > 0 ? 9 : 5) + (single_bond ? kBindLaunches : 0);
                 draw += 1;
             }
             MTG_CUDA(cudaStreamSynchronize(st));
@@ -723,7 +1009,7 @@ struct Sys : SysBase {
                 if (!graph[cur]) build_graph(cur);
                 MTG_CUDA(cudaGraphLaunch(graph[cur], st));
                 if (skin <= 0) cur ^= 1;
-                nlaunch += skin > 0 ? 9 : 5;
+                nlaunch += (skin > 0 ? 9 : 5) + (single_bond ? kBindLaunches : 0);
                 draw += 1;
             }
         }

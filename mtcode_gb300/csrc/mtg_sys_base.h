@@ -54,6 +54,12 @@ struct SysBase {
     virtual int64_t launches() const = 0;
     virtual int64_t ntot() const = 0;
     virtual int64_t offset(int r) const = 0;
+    virtual void set_single_bond(const mtg_single_bond *) = 0;
+    virtual int64_t num_patches() const = 0;
+    virtual int64_t patch_offset(int r) const = 0;
+    virtual void set_bind_state(const int32_t *, const uint8_t *) = 0;
+    virtual void get_bind_state(int32_t *, uint8_t *) = 0;
+    virtual void bind_update(double *, double *) = 0;
 };
 
 

@@ -213,6 +213,55 @@ class LangevinNVTRGPU:
         _check(self._h, _lib.lib().mtg_set_bonds(self._h, b.ctypes.data_as(_lib._I32) if len(b) else None, len(b),
                                                  float(k), float(r0)))
 
+    # ------------------------------------------------------------------ single-bond-per-patch mode
+    def set_single_bond(self, model: "_lib.BindingModel | None", max_ang: float | None = None, list_cut: float = 2.5,
+                        patch_every: int = 10) -> None:
+        """Condensate::run_singlebond's force pass (one bond per patch, binding model ``model``); None switches
+        back to the full Kern-Frenkel force.  ``max_ang`` None: GeneralPatch's min(0.6, cos thetam)."""
+        L = _lib.lib()
+        if model is None:
+            _check(self._h, L.mtg_set_single_bond(self._h, None))
+            return
+        sb = _lib.SingleBond()
+        L.mtg_single_bond_defaults(C.byref(sb))
+        sb.model = model
+        sb.max_ang = float("nan") if max_ang is None else float(max_ang)
+        sb.list_cut = float(list_cut)
+        sb.patch_every = int(patch_every)
+        _check(self._h, L.mtg_set_single_bond(self._h, C.byref(sb)))
+
+    @property
+    def num_patches(self) -> int:
+        return int(_lib.lib().mtg_num_patches(self._h))
+
+    def patch_offset(self, replica: int) -> int:
+        return int(_lib.lib().mtg_patch_offset(self._h, int(replica)))
+
+    def set_bind_state(self, boundto, isbound) -> None:
+        """BinaryBindStore of every patch: boundto (replica-local partner patch), isbound (0 / 1)."""
+        bt = np.ascontiguousarray(boundto, dtype=np.int32)
+        ib = np.ascontiguousarray(isbound, dtype=np.uint8)
+        if bt.size != self.num_patches or ib.size != self.num_patches:
+            raise ValueError("boundto and isbound need one entry per patch")
+        _check(self._h, _lib.lib().mtg_set_bind_state(self._h, bt.ctypes.data_as(_lib._I32),
+                                                      ib.ctypes.data_as(_lib._U8)))
+
+    def get_bind_state(self) -> tuple:
+        n = max(self.num_patches, 1)
+        bt = np.empty(n, dtype=np.int32)
+        ib = np.empty(n, dtype=np.uint8)
+        _check(self._h, _lib.lib().mtg_get_bind_state(self._h, bt.ctypes.data_as(_lib._I32),
+                                                      ib.ctypes.data_as(_lib._U8)))
+        return bt[: self.num_patches], ib[: self.num_patches]
+
+    def bind_update(self):
+        """One calculate_forces_and_torques3D_onlyone_nonlets pass at the current state (bonds decided,
+        one draw index consumed): F (WCA core + bonds + bound pairs) and T (bound pairs, lab)."""
+        F = np.empty((self.n, 3))
+        T = np.empty((self.n, 3))
+        _check(self._h, _lib.lib().mtg_bind_update(self._h, dptr(F), dptr(T)))
+        return F, T
+
     def calculate_forces_and_torques3D(self, with_energy: bool = False):
         """MD::calculateforces(HSPotential) + LangevinNVTR::calculate_forces_and_torques3D: F, T (lab)."""
         F = np.empty((self.n, 3))
@@ -377,3 +426,33 @@ def random_rotations(n: int, seed: int = 0) -> np.ndarray:
     Q = np.empty((n, 9))
     _lib.lib().mtg_random_rotations(int(n), int(seed) & 0xFFFFFFFFFFFFFFFF, dptr(Q))
     return Q
+
+
+def binding_single(on_rate: float, off_rate: float) -> "_lib.BindingModel":
+    """BindingModelSingle(on_rate, off_rate) in table form (mtg_binding_single)."""
+    m = _lib.BindingModel()
+    _lib.lib().mtg_binding_single(C.byref(m), float(on_rate), float(off_rate))
+    return m
+
+
+def binding_binary_equilibrium(div: int) -> "_lib.BindingModel":
+    """BindingModelBinary(div) + setup_equilibrium() in table form."""
+    m = _lib.BindingModel()
+    _lib.lib().mtg_binding_binary_equilibrium(C.byref(m), int(div))
+    return m
+
+
+def binding_tables(rule: int, drate, trate, div1: int = 0, div2: int = 0, np_: int = 1) -> "_lib.BindingModel":
+    """A binding model from its rate tables (e.g. a BindingModelTernary's doubr** / tripr*** vectors):
+    rule 0 one species, 1 binary (patch < div1), 2 SortingFunctionUniform, 3 SortingFunctionNonUniform."""
+    m = _lib.BindingModel()
+    m.species_rule, m.div1, m.div2, m.np = int(rule), int(div1), int(div2), int(np_)
+    d = np.asarray(drate, float).reshape(6, 4)
+    t = np.asarray(trate, float).reshape(10, 16)
+    for r in range(6):
+        for k in range(4):
+            m.drate[r][k] = float(d[r, k])
+    for r in range(10):
+        for k in range(16):
+            m.trate[r][k] = float(t[r, k])
+    return m

@@ -680,3 +680,617 @@ int orc_run(const orc_params *P, double *x, double *p, double *Lb, double *Q, do
     free(xi);
     return status;
 }
+
+/* ================================================================ single-bond-per-patch mode
+ * Condensate::run_singlebond (Condensate/Condensate.cpp:422-618): every patch holds at most one bond,
+ * decided each step by LangevinNVTR::calculate_forces_and_torques3D_onlyone_nonlets
+ * (MDBase/Rotational/LangevinRforce.cpp:2874-3500) from a candidate patch-pair list
+ * (LangevinNVTR::calculate_patch_list, LangevinR.cpp:1702-1852) and a binding model
+ * (MDBase/Bindings/BindingModel{Single,Binary,Ternary}). */
+
+/* ComboPatch::max_check: 1 (combopatch.h:15) raised to every potential's interaction_distance = 1.4 dis
+ * (potentialtheta.h:416; GeneralPatch.cpp:97, TetrahedralPatch.cpp:42) */
+double orc_max_check(const orc_model *M)
+{
+    double mc = 1.0;
+    for (int q = 0; q < M->n_pots; q++)
+        if (1.4 * M->dis[q] > mc) mc = 1.4 * M->dis[q];
+    return mc;
+}
+
+/* first patch index of type k (GeneralPatch total_patches_per_type, GeneralPatch.cpp:285-295) */
+static int orc_patch_base(const orc_model *M, int k)
+{
+    int s = 0;
+    for (int a = 0; a < k; a++) s += M->patches_per_type[a] * (M->num_per_type[a] - (a ? M->num_per_type[a - 1] : 0));
+    return s;
+}
+
+int orc_total_patches(const orc_model *M, int n)
+{
+    (void)n;
+    return orc_patch_base(M, M->n_types);
+}
+
+/* GeneralPatch::which_patch (GeneralPatch.cpp:297-320) for particle i, type k, patch c */
+static int orc_patch_index(const orc_model *M, int i, int k, int c)
+{
+    return orc_patch_base(M, k) + (i - (k ? M->num_per_type[k - 1] : 0)) * M->patches_per_type[k] + c;
+}
+
+/* GeneralPatch::which_particle (GeneralPatch.cpp:431-448): particle and its patch number of patch wp */
+static void orc_patch_owner(const orc_model *M, int wp, int *particle, int *type, int *patch)
+{
+    for (int k = 0; k < M->n_types; k++) {
+        int b0 = orc_patch_base(M, k), b1 = orc_patch_base(M, k + 1);
+        if (wp >= b0 && wp < b1) {
+            *type = k;
+            *particle = (k ? M->num_per_type[k - 1] : 0) + (wp - b0) / M->patches_per_type[k];
+            *patch = (wp - b0) % M->patches_per_type[k];
+            return;
+        }
+    }
+    *type = -1; *particle = -1; *patch = -1;
+}
+
+/* lab-frame patch vector Q^T n_b in the reference's operation order (LangevinRforce.cpp:2980-2985) */
+static void orc_lab_patch(const double nb[3], const double *q, double n[3])
+{
+    n[0] = nb[0] * q[0] + nb[1] * q[3] + nb[2] * q[6];
+    n[1] = nb[0] * q[1] + nb[1] * q[4] + nb[2] * q[7];
+    n[2] = nb[0] * q[2] + nb[1] * q[5] + nb[2] * q[8];
+}
+
+long orc_patch_list(const orc_params *P, const double *x, const double *Q, const int *pairs, long np,
+                    double max_ang, orc_patchint *out, long cap)
+{
+    const orc_model *M = P->model;
+    double max_dis = orc_max_check(M) + 1.;
+    long cnt = 0;
+    for (long q = 0; q < np; q++) {
+        int p1 = pairs[2 * q], p2 = pairs[2 * q + 1];
+        if (p2 < p1) { int t = p1; p1 = p2; p2 = t; }
+        double un[3];
+        double dis = sqrt(orc_distance_vector(P, x, p1, p2, un));
+        if (!(dis < max_dis)) continue;
+        un[0] /= dis; un[1] /= dis; un[2] /= dis;
+        int k1 = orc_type_of(M, p1), k2 = orc_type_of(M, p2);
+        int n1 = M->patches_per_type[k1], n2 = M->patches_per_type[k2];
+        int ps = orc_pot_start(M, k1, k2), o1 = orc_orient_start(M, k1), o2 = orc_orient_start(M, k2);
+        for (int a = 0; a < n1; a++)
+            for (int b = 0; b < n2; b++) {
+                double m1[3], m2[3];
+                orc_lab_patch(M->orient[o1 + a], Q + 9 * p1, m1);
+                orc_lab_patch(M->orient[o2 + b], Q + 9 * p2, m2);
+                double ai = -(m1[0] * un[0] + m1[1] * un[1] + m1[2] * un[2]);
+                double aj = (m2[0] * un[0] + m2[1] * un[1] + m2[2] * un[2]);
+                if ((ai - max_ang) + (aj - max_ang) > -0.4) {
+                    if (cnt < cap) {
+                        orc_patchint *e = out + cnt;
+                        e->p1 = p1; e->p2 = p2; e->potn = ps + a * n2 + b;
+                        e->wp1 = orc_patch_index(M, p1, k1, a);
+                        e->wp2 = orc_patch_index(M, p2, k2, b);
+                    }
+                    cnt++;
+                }
+            }
+    }
+    return cnt;
+}
+
+/* species of a patch index: SortingFunctionUniform / SortingFunctionNonUniform
+ * (Bindings/BindingModelTernary.h:6-30); BindingModelBinary's `index < div` (BindingModelBinary.cpp);
+ * a single species for BindingModelSingle */
+static int orc_species(const orc_binding *B, int idx)
+{
+    switch (B->rule) {
+    case 1: return idx < B->div1 ? 1 : 2;
+    case 2: return idx < B->div1 ? 1 : (idx < B->div2 ? 2 : 3);
+    case 3:
+        if (idx < B->div1) return 1;
+        if (idx < B->div2) return 2;
+        return ((idx - B->div2) % B->np == B->np - 1) ? 3 : 1;
+    default: return 1;
+    }
+}
+
+/* table rows: species pairs 11, 12, 13, 22, 23, 33 and sorted triples 111 ... 333 in lexicographic order
+ * (get_drate / get_trate, BindingModelTernary.cpp:489-520, 652-700) */
+static int orc_pair_row(int a, int b) { return a == 1 ? b - 1 : (a == 2 ? b + 1 : 5); }
+static int orc_triple_row(int a, int b, int c)
+{
+    static const int base[4] = {0, 0, 6, 9};   /* rows starting with species a */
+    if (a == 1) return b == 1 ? c - 1 : (b == 2 ? c + 1 : 5);
+    if (a == 2) return base[2] + (b == 2 ? c - 2 : 2);
+    return base[3];
+}
+
+/* AbstractBindingModel::doublet (BindingModelTernary.cpp:523-560; the Single / Binary forms are the
+ * same arithmetic on their own tables) */
+static int orc_doublet(const orc_binding *B, int before, int i1, int i2, double ran)
+{
+    int s1 = orc_species(B, i1), s2 = orc_species(B, i2);
+    if (s2 < s1) { int t = s1; s1 = s2; s2 = t; }
+    const double *rt = B->drate[orc_pair_row(s1, s2)];
+    int st = before ? 1 : 0;
+    double r1 = rt[st * 2 + 0], r2 = rt[st * 2 + 1];
+    double totalr = r1 + r2;
+    double rr = totalr * ran;
+    return !(rr < r1);
+}
+
+/* sort_triplet_and_save_permutation (Basic/basic.h:166-230): perm ids 0..5 = 123, 132, 312, 213, 231, 321 */
+static int orc_sort3(const int t[3], int s[3])
+{
+    int a = t[0], b = t[1], c = t[2];
+    if (a <= b) {
+        if (b <= c) { s[0] = a; s[1] = b; s[2] = c; return 0; }
+        if (a <= c) { s[0] = a; s[1] = c; s[2] = b; return 1; }
+        s[0] = c; s[1] = a; s[2] = b; return 2;
+    }
+    if (a <= c) { s[0] = b; s[1] = a; s[2] = c; return 3; }
+    if (b <= c) { s[0] = b; s[1] = c; s[2] = a; return 4; }
+    s[0] = c; s[1] = b; s[2] = a; return 5;
+}
+
+/* save_to_type / inverse_save_to_type (Basic/basic.h:373-470) as slot maps over (12, 23, 13):
+ * out[k] = in[map[perm][k]] */
+static const int ORC_SAVE[6][3] = {{0, 1, 2}, {2, 1, 0}, {1, 2, 0}, {0, 2, 1}, {1, 2, 0}, {1, 0, 2}};
+static const int ORC_UNSAVE[6][3] = {{0, 1, 2}, {2, 1, 0}, {1, 2, 0}, {0, 2, 1}, {2, 0, 1}, {1, 0, 2}};
+
+/* AbstractBindingModel::triplet (BindingModelTernary.cpp:791-870) -> out[0..2] = (a12, a23, a13) */
+static void orc_triplet(const orc_binding *B, const int b[3], const int c[3], int i1, int i2, int i3, double ran,
+                        int out[3])
+{
+    int sp[3] = {orc_species(B, i1), orc_species(B, i2), orc_species(B, i3)}, st[3];
+    int perm = orc_sort3(sp, st);
+    int tb[3], tc[3], ta[3];
+    for (int k = 0; k < 3; k++) { tb[k] = b[ORC_SAVE[perm][k]]; tc[k] = c[ORC_SAVE[perm][k]]; }
+    int state = tb[0] ? 0 : (tb[1] ? 1 : (tb[2] ? 2 : 3));
+    const double *rt = B->trate[orc_triple_row(st[0], st[1], st[2])];
+    double r1 = tc[0] * rt[state * 4 + 0];
+    double r2 = tc[1] * rt[state * 4 + 1];
+    double r3 = tc[2] * rt[state * 4 + 2];
+    double r4 = rt[state * 4 + 3];
+    double totalr = r1 + r2 + r3 + r4;
+    double rr = totalr * ran;
+    ta[0] = ta[1] = ta[2] = 0;
+    if (rr < r1) ta[0] = 1;
+    else if (rr >= r1 && rr < r1 + r2) ta[1] = 1;
+    else if (rr >= r1 + r2 && rr < r1 + r2 + r3) ta[2] = 1;
+    for (int k = 0; k < 3; k++) out[k] = ta[ORC_UNSAVE[perm][k]];
+}
+
+/* uniform [0, 1) for a binding decision (Philox stream of the GPU path): cluster root patch, draw, the
+ * decision's number inside its cluster */
+double orc_bind_uniform(uint64_t seed, uint32_t replica, uint64_t draw, uint32_t root, uint32_t iter)
+{
+    uint32_t ctr[4] = {root, (uint32_t)draw, (uint32_t)(draw >> 32), replica};
+    uint32_t key[2] = {(uint32_t)seed + 0x2545F491u * (iter + 1u), (uint32_t)(seed >> 32) ^ 0x6A09E667u};
+    uint32_t o[4];
+    orc_philox4x32_10(ctr, key, o);
+    uint64_t w = ((uint64_t)o[1] << 32) | o[0];
+    return (double)(w >> 11) * (1.0 / 9007199254740992.0);
+}
+
+typedef struct { int a, b; double scr; } orc_wedge;
+
+/* one bound pair: KernFrenkelOnePatch2::force_and_torque of the pair's potential
+ * (LangevinRforce.cpp:3960-4010) accumulated into F, T */
+static void orc_bound_force(const orc_params *P, const double *x, const double *Q, int wp1, int wp2, double *F,
+                            double *T)
+{
+    const orc_model *M = P->model;
+    int p1, p2, k1, k2, c1, c2;
+    orc_patch_owner(M, wp1, &p1, &k1, &c1);
+    orc_patch_owner(M, wp2, &p2, &k2, &c2);
+    if (p2 < p1) { int t = p1; p1 = p2; p2 = t; }
+    double un[3];
+    double dis = sqrt(orc_distance_vector(P, x, p1, p2, un));
+    /* GeneralPatch::which_potential (GeneralPatch.cpp:450-462) with the patch numbers of wp1, wp2 */
+    int potn = orc_pot_start(M, orc_type_of(M, p1), orc_type_of(M, p2)) + c1 * M->patches_per_type[k2] + c2;
+    un[0] /= dis; un[1] /= dis; un[2] /= dis;
+    int o1 = orc_orient_start(M, orc_type_of(M, p1)), o2 = orc_orient_start(M, orc_type_of(M, p2));
+    double o[9];
+    orc_kf2_force_torque(M->orient[o1 + c1], M->orient[o2 + c2], M->att[potn], M->dis[potn], M->thetam[potn], un,
+                         dis, Q + 9 * p1, Q + 9 * p2, o);
+    F[3 * p1 + 0] += o[0]; F[3 * p1 + 1] += o[1]; F[3 * p1 + 2] += o[2];
+    F[3 * p2 + 0] += -o[0]; F[3 * p2 + 1] += -o[1]; F[3 * p2 + 2] += -o[2];
+    T[3 * p1 + 0] += o[3]; T[3 * p1 + 1] += o[4]; T[3 * p1 + 2] += o[5];
+    T[3 * p2 + 0] += o[6]; T[3 * p2 + 1] += o[7]; T[3 * p2 + 2] += o[8];
+}
+
+/* ConnectedComponents (Bindings/GraphAlgorithms.cpp:487-551) of n nodes under edges e[0..ne): the
+ * depth-first order from each unvisited node in index order (DFUtilstore), neighbours in edge order.
+ * ind <- visit order, dem[0..ncomp] <- component boundaries; returns ncomp. */
+static int orc_dfs_components(int n, const orc_wedge *e, int ne, int *ind, int *dem)
+{
+    int *deg = (int *)calloc((size_t)n + 1, sizeof(int));
+    int *adj = (int *)malloc(sizeof(int) * (size_t)(2 * ne + 1));
+    int *fill = (int *)calloc((size_t)n + 1, sizeof(int));
+    for (int q = 0; q < ne; q++) { deg[e[q].a + 1]++; deg[e[q].b + 1]++; }
+    for (int i = 0; i < n; i++) deg[i + 1] += deg[i];
+    for (int q = 0; q < ne; q++) {   /* PairHistogram order: a's list gets b, b's list gets a */
+        adj[deg[e[q].a] + fill[e[q].a]++] = e[q].b;
+        adj[deg[e[q].b] + fill[e[q].b]++] = e[q].a;
+    }
+    int *seen = (int *)calloc((size_t)n + 1, sizeof(int));
+    int *stk = (int *)malloc(sizeof(int) * (size_t)(n + 1)), *pos = (int *)malloc(sizeof(int) * (size_t)(n + 1));
+    int it = 0, nc = 0;
+    dem[0] = 0;
+    for (int s = 0; s < n; s++) {
+        if (seen[s]) continue;
+        int top = 0;
+        stk[0] = s; pos[0] = 0; seen[s] = 1; ind[it++] = s;
+        while (top >= 0) {   /* recursive preorder, iteratively */
+            int v = stk[top];
+            if (pos[top] < deg[v + 1] - deg[v]) {
+                int w = adj[deg[v] + pos[top]++];
+                if (!seen[w]) { seen[w] = 1; ind[it++] = w; stk[++top] = w; pos[top] = 0; }
+            } else {
+                top--;
+            }
+        }
+        nc++;
+        dem[nc] = it;
+    }
+    free(deg); free(adj); free(fill); free(seen); free(stk); free(pos);
+    return nc;
+}
+
+static int orc_first_max(const orc_wedge *e, int ne)
+{
+    int m = 0;
+    for (int q = 1; q < ne; q++)
+        if (e[m].scr < e[q].scr) m = q;   /* std::max_element with mdpairwdCompareScore */
+    return m;
+}
+
+static void orc_push_pair(int **pairs, int *np, int *cap, int a, int b)
+{
+    if (*np == *cap) {
+        *cap = *cap ? 2 * *cap : 64;
+        *pairs = (int *)realloc(*pairs, sizeof(int) * 2 * (size_t)*cap);
+    }
+    (*pairs)[2 * *np] = a;
+    (*pairs)[2 * *np + 1] = b;
+    (*np)++;
+}
+
+/* the triplet's connectivity flags from the adjacency of its lowest member (LangevinRforce.cpp:3230-3280):
+ * nb1 = degree of m1, first = its first neighbour; returns 0 or -1 (the reference's error()) */
+static int orc_triplet_links(int nb1, int first, int nb2, int m2, int m3, int c[3])
+{
+    if (nb1 == 1) {
+        if (first == m2) { c[0] = 1; c[2] = 0; c[1] = 1; }
+        else if (first == m3) { c[2] = 1; c[0] = 0; c[1] = 1; }
+        else return -1;
+    } else if (nb1 == 2) {
+        c[0] = 1; c[2] = 1;
+        c[1] = nb2 == 1 ? 0 : 1;
+    } else {
+        return -1;
+    }
+    return 0;
+}
+
+static void orc_apply_triplet(const int a[3], int i1, int i2, int i3, int *boundto, unsigned char *isbound,
+                              int **pairs, int *np, int *cap)
+{
+    if (a[0]) {
+        boundto[i1] = i2; boundto[i2] = i1;
+        isbound[i1] = 1; isbound[i2] = 1; isbound[i3] = 0;
+        orc_push_pair(pairs, np, cap, i1, i2);
+    } else if (a[1]) {
+        boundto[i2] = i3; boundto[i3] = i2;
+        isbound[i1] = 0; isbound[i2] = 1; isbound[i3] = 1;
+        orc_push_pair(pairs, np, cap, i2, i3);
+    } else if (a[2]) {
+        boundto[i1] = i3; boundto[i3] = i1;
+        isbound[i1] = 1; isbound[i2] = 0; isbound[i3] = 1;
+        orc_push_pair(pairs, np, cap, i1, i3);
+    } else {
+        isbound[i1] = 0; isbound[i2] = 0; isbound[i3] = 0;
+    }
+}
+
+static void orc_apply_doublet(int aft, int i1, int i2, int *boundto, unsigned char *isbound, int **pairs, int *np,
+                              int *cap)
+{
+    if (aft) {
+        boundto[i1] = i2; boundto[i2] = i1;
+        isbound[i1] = 1; isbound[i2] = 1;
+        orc_push_pair(pairs, np, cap, i1, i2);
+    } else {
+        isbound[i1] = 0; isbound[i2] = 0;
+    }
+}
+
+static void orc_sort3_plain(int a, int b, int c, int s[3])
+{
+    int t[3] = {a, b, c};
+    orc_sort3(t, s);
+}
+
+int orc_bind_update(const orc_params *P, const double *x, const double *Q, const orc_patchint *list, long nl,
+                    const orc_binding *B, int rng, uint64_t seed, uint32_t replica, uint64_t draw, int *boundto,
+                    unsigned char *isbound, double *F, double *T)
+{
+    const orc_model *M = P->model;
+    const int np = orc_total_patches(M, P->n);
+    const double mk = orc_max_check(M);
+    int status = 0;
+
+    /* ---- candidate patch pairs -> edges with scores (LangevinRforce.cpp:2900-3090) */
+    orc_wedge *edges = (orc_wedge *)malloc(sizeof(orc_wedge) * (size_t)(nl + 1));
+    int ne = 0;
+    for (long q = 0; q < nl; q++) {
+        const orc_patchint *e = list + q;
+        double un[3];
+        double dis = orc_distance_vector(P, x, e->p1, e->p2, un);
+        if (!(dis < SQR(mk))) continue;
+        dis = sqrt(dis);
+        un[0] /= dis; un[1] /= dis; un[2] /= dis;
+        int wp1 = e->wp1, wp2 = e->wp2, potn = e->potn;
+        int k1 = orc_type_of(M, e->p1), k2 = orc_type_of(M, e->p2);
+        int ps = orc_pot_start(M, k1, k2), n2 = M->patches_per_type[k2];
+        int a = (potn - ps) / n2, b = (potn - ps) % n2;
+        double m1[3], m2[3];
+        orc_lab_patch(M->orient[orc_orient_start(M, k1) + a], Q + 9 * e->p1, m1);
+        orc_lab_patch(M->orient[orc_orient_start(M, k2) + b], Q + 9 * e->p2, m2);
+        double disp = 1.4 * M->dis[potn], thetam = M->thetam[potn], ctm = cos(thetam);
+        double ai = -(m1[0] * un[0] + m1[1] * un[1] + m1[2] * un[2]);
+        double aj = (m2[0] * un[0] + m2[1] * un[1] + m2[2] * un[2]);
+        int cond1 = boundto[wp1] == wp2 && boundto[wp2] == wp1;
+        int b1 = isbound[wp1] != 0, b2 = isbound[wp2] != 0;
+        double disp2;
+        if (b1 && b2 && cond1) disp2 = disp;
+        else if (b1 && b2 && !cond1) disp2 = 0.5 * disp;
+        else if (b1 != b2) disp2 = 0.7 * disp;
+        else disp2 = disp;
+        if (ai > ctm && aj > ctm && dis < disp2) {
+            double scr1 = 1 - (ai - cos(thetam));
+            double scr2 = 1 - (aj - cos(thetam));
+            double scr3 = 2 * (dis / disp2);
+            edges[ne].a = wp1; edges[ne].b = wp2; edges[ne].scr = scr1 + scr2 + scr3;
+            ne++;
+        }
+    }
+
+    /* ---- PairHistogramExtended (GraphAlgorithms.cpp:264-330): per patch, partners and scores in edge order */
+    int *start = (int *)calloc((size_t)np + 1, sizeof(int));
+    int *fill = (int *)calloc((size_t)np + 1, sizeof(int));
+    int *nbr = (int *)malloc(sizeof(int) * (size_t)(2 * ne + 1));
+    double *nsc = (double *)malloc(sizeof(double) * (size_t)(2 * ne + 1));
+    for (int q = 0; q < ne; q++) { start[edges[q].a + 1]++; start[edges[q].b + 1]++; }
+    for (int i = 0; i < np; i++) start[i + 1] += start[i];
+    for (int q = 0; q < ne; q++) {
+        int a = edges[q].a, b = edges[q].b;
+        nbr[start[a] + fill[a]] = b; nsc[start[a] + fill[a]++] = edges[q].scr;
+        nbr[start[b] + fill[b]] = a; nsc[start[b] + fill[b]++] = edges[q].scr;
+    }
+#define DEG(i) (start[(i) + 1] - start[(i)])
+
+    /* ---- a bond whose partner is no longer a candidate breaks (LangevinRforce.cpp:3110-3133) */
+    for (int i = 0; i < np; i++) {
+        if (!isbound[i]) continue;
+        int found = 0;
+        for (int k = start[i]; k < start[i + 1]; k++)
+            if (nbr[k] == boundto[i]) { found = 1; break; }
+        if (!found) isbound[i] = 0;
+    }
+
+    /* ---- ConnectedComponentsParallel_Old: each patch labelled by the smallest index of its component;
+     * SingleHistogram (GraphAlgorithms.cpp:2-48): members per label in increasing order */
+    int *lab = (int *)malloc(sizeof(int) * (size_t)(np + 1));
+    for (int i = 0; i < np; i++) lab[i] = i;
+    for (int q = 0; q < ne; q++) {
+        int a = orc_find(lab, edges[q].a), b = orc_find(lab, edges[q].b);
+        if (a < b) lab[b] = a;
+        else if (b < a) lab[a] = b;
+    }
+    for (int i = 0; i < np; i++) lab[i] = orc_find(lab, i);
+    int *ccs = (int *)calloc((size_t)np + 1, sizeof(int));
+    for (int i = 0; i < np; i++) ccs[lab[i]]++;
+    int *mstart = (int *)calloc((size_t)np + 1, sizeof(int));
+    for (int i = 0; i < np; i++) mstart[i + 1] = mstart[i] + ccs[i];
+    int *members = (int *)malloc(sizeof(int) * (size_t)(np + 1));
+    int *mfill = (int *)calloc((size_t)np + 1, sizeof(int));
+    for (int i = 0; i < np; i++) members[mstart[lab[i]] + mfill[lab[i]]++] = i;
+
+    /* ---- one random number per cluster of two or more (Generate_Random_Numbers_Needed,
+     * GraphAlgorithms.cpp:431-438) */
+    double *rands = (double *)calloc((size_t)np + 1, sizeof(double));
+    int maxc = 0;
+    for (int i = 0; i < np; i++) {
+        if (ccs[i] > maxc) maxc = ccs[i];
+        if (ccs[i] > 1)
+            rands[i] = rng == 1 ? (double)rand() / (double)RAND_MAX : orc_bind_uniform(seed, replica, draw, (uint32_t)i, 0);
+    }
+
+    int *bpairs = NULL, nbp = 0, bcap = 0;
+    int *large = (int *)malloc(sizeof(int) * (size_t)(np + 1));
+    int nlarge = 0;
+    /* ---- clusters of one, two and three patches (LangevinRforce.cpp:3160-3480) */
+    for (int i = 0; i < np && status == 0; i++) {
+        int sz = ccs[i];
+        const int *mb = members + mstart[i];
+        if (sz == 0) continue;
+        if (sz == 1) {
+            isbound[mb[0]] = 0;
+        } else if (sz == 2) {
+            int i1 = mb[0] < mb[1] ? mb[0] : mb[1], i2 = mb[0] < mb[1] ? mb[1] : mb[0];
+            int already = boundto[i1] == i2 && boundto[i2] == i1 && isbound[i1] && isbound[i2];
+            orc_apply_doublet(orc_doublet(B, already, i1, i2, rands[i]), i1, i2, boundto, isbound, &bpairs, &nbp, &bcap);
+        } else if (sz == 3) {
+            int s[3];
+            orc_sort3_plain(mb[0], mb[1], mb[2], s);
+            int i1 = s[0], i2 = s[1], i3 = s[2];
+            int bb[3] = {boundto[i1] == i2 && boundto[i2] == i1 && isbound[i1] && isbound[i2],
+                         boundto[i2] == i3 && boundto[i3] == i2 && isbound[i2] && isbound[i3],
+                         boundto[i1] == i3 && boundto[i3] == i1 && isbound[i1] && isbound[i3]};
+            int c[3] = {0, 0, 0};
+            if (orc_triplet_links(DEG(i1), DEG(i1) > 0 ? nbr[start[i1]] : -1, DEG(i2), i2, i3, c)) { status = -2; break; }
+            int a[3];
+            orc_triplet(B, bb, c, i1, i2, i3, rands[i], a);
+            orc_apply_triplet(a, i1, i2, i3, boundto, isbound, &bpairs, &nbp, &bcap);
+        } else {
+            large[nlarge++] = i;
+        }
+    }
+
+    /* ---- larger clusters: drop the highest-scoring edge until no component exceeds three patches,
+     * then decide the pieces (LangevinRforce.cpp:3560-3880) */
+    int ncols = maxc / 2 + 1;
+    double *rl = (double *)malloc(sizeof(double) * (size_t)(nlarge > 0 ? nlarge * ncols : 1));
+    if (rng == 1)
+        for (int q = 0; q < nlarge * ncols; q++) rl[q] = (double)rand() / (double)RAND_MAX;   /* generate_random_matrix */
+    for (int allc = 0; allc < nlarge && status == 0; allc++) {
+        int root = large[allc], m = ccs[root];
+        const int *u = members + mstart[root];   /* unique_indexes, increasing */
+        /* RecapitulateEdges (LangevinRforceUtil.cpp:508-572): local (a < b) edges in member / neighbour order */
+        int cap = 1;
+        for (int j = 0; j < m; j++) cap += DEG(u[j]);
+        orc_wedge *me = (orc_wedge *)malloc(sizeof(orc_wedge) * (size_t)cap);
+        int nme = 0;
+        for (int j = 0; j < m; j++)
+            for (int k = start[u[j]]; k < start[u[j] + 1]; k++) {
+                int f2 = 0;
+                while (f2 < m && u[f2] != nbr[k]) f2++;
+                int a = j < f2 ? j : f2, b = j < f2 ? f2 : j;
+                int dup = 0;
+                for (int l = 0; l < nme; l++)
+                    if (me[l].a == a && me[l].b == b) { dup = 1; break; }
+                if (!dup) { me[nme].a = a; me[nme].b = b; me[nme].scr = nsc[k]; nme++; }
+            }
+        int *ind = (int *)malloc(sizeof(int) * (size_t)m), *dem = (int *)malloc(sizeof(int) * (size_t)(m + 1));
+        int mx = orc_first_max(me, nme);
+        memmove(me + mx, me + mx + 1, sizeof(orc_wedge) * (size_t)(nme - mx - 1));
+        nme--;
+        int ncomp = orc_dfs_components(m, me, nme, ind, dem);
+        for (;;) {
+            int big = 0;
+            for (int q = 0; q < ncomp; q++)
+                if (dem[q + 1] - dem[q] > big) big = dem[q + 1] - dem[q];
+            if (big <= 3) break;
+            mx = orc_first_max(me, nme);
+            memmove(me + mx, me + mx + 1, sizeof(orc_wedge) * (size_t)(nme - mx - 1));
+            nme--;
+            ncomp = orc_dfs_components(m, me, nme, ind, dem);
+        }
+        /* PairHistogram of the remaining edges (degree <= 2 inside a piece) */
+        int *lens = (int *)calloc((size_t)m, sizeof(int)), *bx = (int *)malloc(sizeof(int) * 3 * (size_t)m);
+        for (int q = 0; q < nme; q++) {
+            bx[3 * me[q].a + lens[me[q].a]++] = me[q].b;
+            bx[3 * me[q].b + lens[me[q].b]++] = me[q].a;
+        }
+        for (int k1 = 0; k1 < m; k1++) {
+            if (!isbound[u[k1]]) continue;
+            int outside = 1;
+            for (int k = 0; k < lens[k1]; k++)
+                if (boundto[u[k1]] == u[bx[3 * k1 + k]]) { outside = 0; break; }
+            if (outside) isbound[u[k1]] = 0;
+        }
+        int it = 0;
+        for (int j = 0; j < ncomp && status == 0; j++) {
+            int sz = dem[j + 1] - dem[j];
+            double ran = 0;
+            if (sz == 2 || sz == 3)
+                ran = rng == 1 ? rl[allc * ncols + it] : orc_bind_uniform(seed, replica, draw, (uint32_t)root, (uint32_t)it);
+            if (sz == 1) {
+                isbound[u[ind[dem[j]]]] = 0;
+            } else if (sz == 2) {
+                int t1 = u[ind[dem[j]]], t2 = u[ind[dem[j] + 1]];
+                int i1 = t1 <= t2 ? t1 : t2, i2 = t1 <= t2 ? t2 : t1;
+                int already = boundto[i1] == i2 && boundto[i2] == i1 && isbound[i1] && isbound[i2];
+                orc_apply_doublet(orc_doublet(B, already, i1, i2, ran), i1, i2, boundto, isbound, &bpairs, &nbp, &bcap);
+                it++;
+            } else if (sz == 3) {
+                int ni[3], s[3];
+                orc_sort3_plain(ind[dem[j]], ind[dem[j] + 1], ind[dem[j] + 2], ni);
+                orc_sort3_plain(u[ni[0]], u[ni[1]], u[ni[2]], s);
+                int i1 = s[0], i2 = s[1], i3 = s[2];
+                int bb[3] = {boundto[i1] == i2 && boundto[i2] == i1 && isbound[i1] && isbound[i2],
+                             boundto[i2] == i3 && boundto[i3] == i2 && isbound[i2] && isbound[i3],
+                             boundto[i1] == i3 && boundto[i3] == i1 && isbound[i1] && isbound[i3]};
+                int c[3] = {0, 0, 0};
+                if (orc_triplet_links(lens[ni[0]], lens[ni[0]] > 0 ? bx[3 * ni[0]] : -1, lens[ni[1]], ni[1], ni[2], c)) {
+                    status = -2;
+                    break;
+                }
+                int a[3];
+                orc_triplet(B, bb, c, i1, i2, i3, ran, a);
+                orc_apply_triplet(a, i1, i2, i3, boundto, isbound, &bpairs, &nbp, &bcap);
+                it++;
+            } else {
+                status = -3;
+            }
+        }
+        free(me); free(ind); free(dem); free(lens); free(bx);
+    }
+#undef DEG
+
+    /* ---- forces of the bound pairs only, in the order they were made (LangevinRforce.cpp:3940-4030) */
+    if (status == 0)
+        for (int q = 0; q < nbp; q++) orc_bound_force(P, x, Q, bpairs[2 * q], bpairs[2 * q + 1], F, T);
+
+    free(edges); free(start); free(fill); free(nbr); free(nsc); free(lab); free(ccs); free(mstart); free(members);
+    free(mfill); free(rands); free(large); free(rl); free(bpairs);
+    return status;
+}
+
+static long orc_patch_list_alloc(const orc_params *P, const double *x, const double *Q, const int *pairs, long np,
+                                 double max_ang, orc_patchint **out)
+{
+    long n = orc_patch_list(P, x, Q, pairs, np, max_ang, NULL, 0);
+    *out = (orc_patchint *)malloc(sizeof(orc_patchint) * (size_t)(n > 0 ? n : 1));
+    orc_patch_list(P, x, Q, pairs, np, max_ang, *out, n);
+    return n;
+}
+
+int orc_run_singlebond(const orc_params *P, double *x, double *p, double *Lb, double *Q, double *Ft, double *Tt,
+                       int *boundto, unsigned char *isbound, const orc_binding *B, double max_ang, int nsteps, int i0,
+                       int ncell, double pair_cut, int pair_every, int patch_every, int init, uint64_t init_draw,
+                       int noise_mode, const double *noise, uint64_t seed, uint32_t replica, uint64_t draw0)
+{
+    int n = P->n, status = 0;
+    int *pairs = NULL;
+    orc_patchint *plist = NULL;
+    double *xi = (double *)calloc(6 * (size_t)(n > 0 ? n : 1), sizeof(double));
+    long np = orc_pairs_alloc(P, x, ncell, pair_cut, &pairs);
+    long nl = orc_patch_list_alloc(P, x, Q, pairs, np, max_ang, &plist);
+    if (init) {
+        orc_central_forces(P, x, pairs, np, Ft);
+        memset(Tt, 0, sizeof(double) * 3 * (size_t)n);
+        status |= orc_bind_update(P, x, Q, plist, nl, B, 0, seed, replica, init_draw, boundto, isbound, Ft, Tt);
+        if (noise_mode == 2) orc_philox_noise(n, seed, replica, init_draw, xi);
+        orc_langevin_forces(P, p, Lb, Q, xi, Ft, Tt);   /* Philox draw init_draw, or xi = 0 */
+    }
+    for (int s = 0; s < nsteps; s++) {
+        int i = i0 + s;
+        if (i > 0 && i % pair_every == 0 && s > 0) {
+            free(pairs);
+            np = orc_pairs_alloc(P, x, ncell, pair_cut, &pairs);
+        }
+        if (i > 0 && i % patch_every == 0) {
+            free(plist);
+            nl = orc_patch_list_alloc(P, x, Q, pairs, np, max_ang, &plist);
+        }
+        orc_halfkick(n, P->dt, p, Lb, Ft, Tt);
+        orc_drift(P, x, p);
+        orc_rotate(P, Lb, Q);
+        orc_central_forces(P, x, pairs, np, Ft);
+        memset(Tt, 0, sizeof(double) * 3 * (size_t)n);
+        status |= orc_bind_update(P, x, Q, plist, nl, B, 0, seed, replica, draw0 + (uint64_t)s, boundto, isbound, Ft, Tt);
+        const double *nz = xi;
+        if (noise_mode == 1) nz = noise + 6 * (size_t)n * (size_t)s;
+        else if (noise_mode == 2) orc_philox_noise(n, seed, replica, draw0 + (uint64_t)s, xi);
+        else memset(xi, 0, sizeof(double) * 6 * (size_t)n);
+        orc_langevin_forces(P, p, Lb, Q, nz, Ft, Tt);
+        orc_halfkick(n, P->dt, p, Lb, Ft, Tt);
+    }
+    free(pairs);
+    free(plist);
+    free(xi);
+    return status;
+}

@@ -136,6 +136,57 @@ int orc_run(const orc_params *P, double *x, double *p, double *Lb, double *Q, do
             int nsteps, int ncell, double rc, int rebuild, int noise_mode, const double *noise,
             uint64_t seed, uint32_t replica, uint64_t draw0, int check_skin);
 
+/* ---------------------------------------------------------------- single-bond-per-patch mode
+ * Condensate::run_singlebond (Condensate/Condensate.cpp:422-618). */
+
+/* Binding model in table form.  rule: species of a patch index -- 0: one species (BindingModelSingle),
+ * 1: index < div1 ? 1 : 2 (BindingModelBinary), 2: SortingFunctionUniform, 3: SortingFunctionNonUniform
+ * (Bindings/BindingModelTernary.h:6-30).  drate rows: species pairs 11, 12, 13, 22, 23, 33, each
+ * [before * 2 + 0] = rate to unbound, [before * 2 + 1] = rate to bound (doubr**).  trate rows: sorted
+ * species triples 111, 112, 113, 122, 123, 133, 222, 223, 233, 333, each [state * 4 + k] (tripr***). */
+typedef struct {
+    int rule;
+    int div1, div2, np;
+    double drate[6][4];
+    double trate[10][16];
+} orc_binding;
+
+/* patchint (LangevinR.cpp:1790-1800): one candidate patch pair */
+typedef struct { int p1, p2, potn, wp1, wp2; } orc_patchint;
+
+double orc_max_check(const orc_model *M);
+int orc_total_patches(const orc_model *M, int n);
+
+/* LangevinNVTR::calculate_patch_list(pairs, iny) (LangevinR.cpp:1702-1852).  max_ang = ComboPatch::max_ang
+ * (0.6, combopatch.h:15; GeneralPatch lowers it to the smallest cos(thetam), GeneralPatch.cpp:99).
+ * Returns the count (entries beyond cap are not written). */
+long orc_patch_list(const orc_params *P, const double *x, const double *Q, const int *pairs, long np,
+                    double max_ang, orc_patchint *out, long cap);
+
+/* uniform [0, 1) of the GPU path's binding decisions: Philox4x32-10 with counter (root, draw, replica),
+ * key (seed_lo + 0x2545F491 (iter + 1), seed_hi ^ 0x6A09E667), 53 bits of the first two words */
+double orc_bind_uniform(uint64_t seed, uint32_t replica, uint64_t draw, uint32_t root, uint32_t iter);
+
+/* LangevinNVTR::calculate_forces_and_torques3D_onlyone_nonlets (LangevinRforce.cpp:2874-4030) on the
+ * candidate list: edges, bond breaking, patch clusters, binding decisions, then the KF2 force and torque
+ * of every bound pair added to F, T.  boundto / isbound (total patches) are updated in place.
+ * rng 1: random numbers from the C library's rand() in the reference's order (Generate_Random_Numbers_Needed,
+ * then generate_random_matrix for the larger clusters); rng 0: orc_bind_uniform(seed, replica, draw, root
+ * patch of the cluster, decision number inside it).  Returns 0, or -2 / -3 where the reference calls error(). */
+int orc_bind_update(const orc_params *P, const double *x, const double *Q, const orc_patchint *list, long nl,
+                    const orc_binding *B, int rng, uint64_t seed, uint32_t replica, uint64_t draw, int *boundto,
+                    unsigned char *isbound, double *F, double *T);
+
+/* The run_singlebond loop (Condensate.cpp:422-560) on one system, nsteps from loop index i0:
+ * pairs within pair_cut rebuilt when i > 0 and i % pair_every == 0 (and at the start), the candidate
+ * list when i > 0 and i % patch_every == 0 (and at the start); F = central forces, T = 0, then
+ * orc_bind_update (rng 0, draw0 + s), noise (noise_mode as orc_run), half-kick.  With init, the
+ * initial pass before the loop runs first (F, T, bind update and noise of draw init_draw -> Ft, Tt). */
+int orc_run_singlebond(const orc_params *P, double *x, double *p, double *Lb, double *Q, double *Ft, double *Tt,
+                       int *boundto, unsigned char *isbound, const orc_binding *B, double max_ang, int nsteps, int i0,
+                       int ncell, double pair_cut, int pair_every, int patch_every, int init, uint64_t init_draw,
+                       int noise_mode, const double *noise, uint64_t seed, uint32_t replica, uint64_t draw0);
+
 #ifdef __cplusplus
 }
 #endif

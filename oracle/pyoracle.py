@@ -57,8 +57,53 @@ class OrcParams(C.Structure):
                 ("nbonds", C.c_long), ("bond_k", C.c_double), ("bond_r0", C.c_double)]
 
 
+class OrcBinding(C.Structure):
+    """orc_binding: species rule + doublet rows (11, 12, 13, 22, 23, 33) + triplet rows (111 ... 333)."""
+    _fields_ = [("rule", C.c_int), ("div1", C.c_int), ("div2", C.c_int), ("np", C.c_int),
+                ("drate", (C.c_double * 4) * 6), ("trate", (C.c_double * 16) * 10)]
+
+
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)
+_U8 = C.POINTER(C.c_ubyte)
+
+
+def binding(rule: int, drate, trate, div1: int = 0, div2: int = 0, np_: int = 1) -> OrcBinding:
+    b = OrcBinding()
+    b.rule, b.div1, b.div2, b.np = int(rule), int(div1), int(div2), int(np_)
+    d = np.asarray(drate, float).reshape(6, 4)
+    t = np.asarray(trate, float).reshape(10, 16)
+    for r in range(6):
+        for k in range(4):
+            b.drate[r][k] = float(d[r, k])
+    for r in range(10):
+        for k in range(16):
+            b.trate[r][k] = float(t[r, k])
+    return b
+
+
+def binding_single(on: float, off: float) -> OrcBinding:
+    """BindingModelSingle(on, off) (Bindings/BindingModelSingle.cpp): doublet rates (off, on) whatever the
+    state before; triplet rows per state (bound 12, 23, 13, none)."""
+    d = np.zeros((6, 4))
+    d[0] = [off, on, off, on]
+    t = np.zeros((10, 16))
+    x = (off / 3.) + 0.001
+    t[0] = [on, x, x, x, x, on, x, x, x, x, on, x, on / 3., on / 3., on / 3., off]
+    return binding(0, d, t)
+
+
+def binding_binary(div: int, raw_tables) -> OrcBinding:
+    """BindingModelBinary(div) from its rate vectors (doubr11/12/22, tripr111/112/122/222 in the rows of the
+    table form); its 122 and 222 triplets take the rate to none-bound from tripr111
+    (BindingModelBinary.cpp triplet)."""
+    raw = np.asarray(raw_tables, float)
+    d = raw[:24].reshape(6, 4).copy()
+    t = raw[24:].reshape(10, 16).copy()
+    for row in (3, 6):
+        for st in range(4):
+            t[row, 4 * st + 3] = t[0, 4 * st + 3]
+    return binding(1, d, t, div1=div)
 
 
 def _d(a):
@@ -98,6 +143,21 @@ def orc() -> C.CDLL:
         L.orc_observables.argtypes = [P, _D, _D, _I, C.c_long, _D]
         L.orc_neighbor_cells.restype = C.c_int
         L.orc_neighbor_cells.argtypes = [C.c_int, C.c_int, _I]
+        L.orc_max_check.restype = C.c_double
+        L.orc_max_check.argtypes = [C.POINTER(OrcModel)]
+        L.orc_total_patches.restype = C.c_int
+        L.orc_total_patches.argtypes = [C.POINTER(OrcModel), C.c_int]
+        L.orc_patch_list.restype = C.c_long
+        L.orc_patch_list.argtypes = [P, _D, _D, _I, C.c_long, C.c_double, _I, C.c_long]
+        L.orc_bind_uniform.restype = C.c_double
+        L.orc_bind_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32]
+        L.orc_bind_update.restype = C.c_int
+        L.orc_bind_update.argtypes = [P, _D, _D, _I, C.c_long, C.POINTER(OrcBinding), C.c_int, C.c_uint64,
+                                      C.c_uint32, C.c_uint64, _I, C.POINTER(C.c_ubyte), _D, _D]
+        L.orc_run_singlebond.restype = C.c_int
+        L.orc_run_singlebond.argtypes = [P, _D, _D, _D, _D, _D, _D, _I, C.POINTER(C.c_ubyte), C.POINTER(OrcBinding),
+                                         C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
+                                         C.c_int, C.c_uint64, C.c_int, _D, C.c_uint64, C.c_uint32, C.c_uint64]
         _orc = L
     return _orc
 
@@ -225,6 +285,63 @@ class System:
         return out
 
 
+    # ---- single-bond mode
+    def max_check(self) -> float:
+        return orc().orc_max_check(C.byref(self.model))
+
+    def total_patches(self) -> int:
+        return orc().orc_total_patches(C.byref(self.model), self.spec.n)
+
+    def default_max_ang(self) -> float:
+        """ComboPatch::max_ang of the GeneralPatch form: min(0.6, cos(thetam)) over the potentials."""
+        th = np.asarray(self.spec.model.params, float).reshape(-1, 3)[:, 2]
+        return float(min([0.6] + [math.cos(t) for t in th]))
+
+    def patch_list(self, x, Q, pairs, max_ang: float) -> np.ndarray:
+        """calculate_patch_list: (n, 5) rows (p1, p2, potn, wp1, wp2)."""
+        x = np.ascontiguousarray(x, float)
+        Q = np.ascontiguousarray(Q, float)
+        pr = np.ascontiguousarray(pairs, dtype=np.intc).reshape(-1, 2)
+        n = orc().orc_patch_list(C.byref(self.params), _d(x), _d(Q), pr.ctypes.data_as(_I), len(pr), float(max_ang),
+                                 None, 0)
+        out = np.empty((max(n, 1), 5), dtype=np.intc)
+        orc().orc_patch_list(C.byref(self.params), _d(x), _d(Q), pr.ctypes.data_as(_I), len(pr), float(max_ang),
+                             out.ctypes.data_as(_I), n)
+        return out[:n].copy()
+
+    def bind_update(self, x, Q, plist, bind: OrcBinding, boundto, isbound, rng: int = 0, seed: int = 0,
+                    replica: int = 0, draw: int = 0):
+        """onlyone_nonlets on a candidate list; boundto / isbound (int32 / uint8) are updated in place.
+        Returns (status, F, T) of the bound pairs alone."""
+        pl = np.ascontiguousarray(plist, dtype=np.intc).reshape(-1, 5)
+        assert boundto.dtype == np.intc and isbound.dtype == np.uint8
+        F = np.zeros((self.spec.n, 3))
+        T = np.zeros((self.spec.n, 3))
+        st = orc().orc_bind_update(C.byref(self.params), _d(np.ascontiguousarray(x, float)),
+                                   _d(np.ascontiguousarray(Q, float)), pl.ctypes.data_as(_I), len(pl), C.byref(bind),
+                                   int(rng), int(seed) & 0xFFFFFFFFFFFFFFFF, int(replica), int(draw),
+                                   boundto.ctypes.data_as(_I), isbound.ctypes.data_as(_U8), _d(F), _d(T))
+        return st, F, T
+
+    def run_singlebond(self, state: dict, bind: OrcBinding, nsteps: int, max_ang: float, i0: int = 0,
+                       pair_cut: float = 2.5, pair_every: int = 20, patch_every: int = 10, init: bool = False,
+                       init_draw: int = 0, noise_mode: int = 0, noise=None, seed: int = 0, replica: int = 0,
+                       draw0: int = 0) -> int:
+        """The run_singlebond loop on state (x, p, Lb, Q, Ft, Tt, boundto, isbound; modified in place)."""
+        ncell = max(1, int(math.floor(self.spec.box / pair_cut)))
+        return orc().orc_run_singlebond(
+            C.byref(self.params), _d(state["x"]), _d(state["p"]), _d(state["Lb"]), _d(state["Q"]), _d(state["Ft"]),
+            _d(state["Tt"]), state["boundto"].ctypes.data_as(_I), state["isbound"].ctypes.data_as(_U8),
+            C.byref(bind), float(max_ang), int(nsteps), int(i0), ncell, float(pair_cut), int(pair_every),
+            int(patch_every), int(bool(init)), int(init_draw), int(noise_mode),
+            _d(None if noise is None else np.ascontiguousarray(noise, float)), int(seed) & 0xFFFFFFFFFFFFFFFF,
+            int(replica), int(draw0))
+
+
+def bind_uniform(seed: int, replica: int, draw: int, root: int, it: int) -> float:
+    return orc().orc_bind_uniform(int(seed) & 0xFFFFFFFFFFFFFFFF, int(replica), int(draw), int(root), int(it))
+
+
 def philox(ctr, key) -> list:
     c = (C.c_uint32 * 4)(*ctr)
     k = (C.c_uint32 * 2)(*key)
@@ -271,6 +388,10 @@ def ref() -> C.CDLL | None:
         L.ref_forces_bonded.argtypes = [C.c_int, C.c_double, C.c_int, _D, _D, C.c_int, C.c_double, C.c_double,
                                         C.c_double, C.c_int, _I, _I, _D, _D, _I, C.c_long, C.c_double, C.c_double,
                                         _D, _D]
+        L.ref_singlebond.restype = C.c_long
+        L.ref_singlebond.argtypes = [C.c_int, C.c_double, C.c_int, _D, _D, C.c_int, C.c_double, C.c_int, C.c_double,
+                                     C.c_double, C.c_double, C.c_int, _I, _I, _D, _D, C.c_int, _D, _I, _U8, C.c_uint,
+                                     _D, _D, _I, C.c_long, _D, _D]
         _ref = L
     return _ref
 
@@ -282,3 +403,29 @@ def ref_model_args(model):
     orient = np.ascontiguousarray(np.asarray(model.orient, float).reshape(-1, 3))
     params = np.ascontiguousarray(np.asarray(model.params, float).reshape(-1, 3))
     return 2, 0.0, 0.0, 0.0, len(ppt), ppt, npt, orient, params
+
+
+def ref_singlebond(spec, x, Q, pair_cut: float, bm_kind: int, args, boundto, isbound, seed: int):
+    """The reference's calculate_patch_list + onlyone_nonlets (srand(seed) first) on a copy of the bind state.
+    Returns dict(F, T, boundto, isbound, plist, tables, max_ang, max_check)."""
+    L = ref()
+    n = int(spec.n)
+    _, att, dis, th, nt, ppt, npt, orient, params = ref_model_args(spec.model)
+    bt = np.ascontiguousarray(boundto, dtype=np.intc).copy()
+    ib = np.ascontiguousarray(isbound, dtype=np.uint8).copy()
+    F = np.empty((n, 3))
+    T = np.empty((n, 3))
+    cap = 16 * 16 * n + 64   # at most 16 patch pairs for each of the <= 16 n pairs within 2.5 sigma
+    plist = np.empty((cap, 5), dtype=np.intc)
+    tables = np.empty(184)
+    caps = np.empty(2)
+    a = np.ascontiguousarray(np.asarray(args, float).reshape(-1))
+    ncell = max(1, int(math.floor(float(spec.box) / pair_cut)))
+    npl = L.ref_singlebond(n, float(spec.box), int(bool(spec.periodic)), _d(np.ascontiguousarray(x, float)),
+                           _d(np.ascontiguousarray(Q, float)), ncell, float(pair_cut), 2, att, dis, th, nt,
+                           ppt.ctypes.data_as(_I), npt.ctypes.data_as(_I), _d(orient), _d(params), int(bm_kind), _d(a),
+                           bt.ctypes.data_as(_I), ib.ctypes.data_as(_U8), int(seed), _d(F), _d(T),
+                           plist.ctypes.data_as(_I), cap, _d(tables), _d(caps))
+    assert npl <= cap, "candidate list larger than the buffer"
+    return dict(F=F, T=T, boundto=bt, isbound=ib, plist=plist[:npl].copy(), tables=tables,
+                max_ang=float(caps[0]), max_check=float(caps[1]))

@@ -336,6 +336,120 @@ void ref_run(int n, double box, int periodic, double *x, double *p, double *Lb, 
     delete obj;
 }
 
+// One call of the single-bond force pass as Condensate::run_singlebond makes it (Condensate.cpp:430-470):
+// pairs = calculatepairs(boxes, pair_cut), opairs = calculate_patch_list(*pairs, *pots), runs_diff =
+// adjacency(opairs), then srand(seed) and calculate_forces_and_torques3D_onlyone_nonlets(opairs, runs_diff,
+// *pots, bbs, *bm, F, T) from F = T = 0.  Binding model bm_kind: 0 BindingModelSingle(args[0] on, args[1] off),
+// 1 BindingModelBinary(args[0] div) + setup_equilibrium(), 2 BindingModelTernary<SortingFunctionUniform>
+// (div1 args[0], div2 args[1]) + setup(args[2..16]), 3 BindingModelTernary<SortingFunctionNonUniform>
+// (div1, div2, np = args[0..2]) + setup(args[3..17]).  Outputs: boundto / isbound updated in place, F, T,
+// the candidate list (plist, 5 ints per entry, up to plist_cap; the count is returned), the model's rate
+// vectors in tables (doubr11, 12, 13, 22, 23, 33 then tripr111 ... 333, zero where the model has none) and
+// max_ang / max_check in caps[0..1].
+long ref_singlebond(int n, double box, int periodic, const double *x, const double *Q, int ncell, double pair_cut,
+                    int kind, double att, double dis, double thetam, int n_types, const int *ppt, const int *npt,
+                    const double *orient, const double *params, int bm_kind, const double *args, int *boundto,
+                    unsigned char *isbound, unsigned seed, double *F, double *T, int *plist, long plist_cap,
+                    double *tables, double *caps)
+{
+    vector<double> zeros3(3 * (size_t)n, 0.0);
+    LangevinNVTR *b = make_system(n, box, periodic, x, zeros3.data(), zeros3.data(), Q, 0.005, 1, 1, 1);
+    RefModelDesc d = {kind, att, dis, thetam, n_types, ppt, npt, orient, params};
+    ComboPatch *pots = make_model(d);
+    int ccc;
+    matrix<int> boxes = b->getgeo().generate_boxes_relationships(ncell, ccc);
+    matrix<int> *pairs = b->calculatepairs(boxes, pair_cut);
+    vector<patchint> opairs = b->calculate_patch_list(*pairs, *pots);
+    vector<int> runs_diff = adjacency(opairs);
+    int nh = pots->get_total_patches(n);
+    BinaryBindStore bbs;
+    vector1<bool> ib(nh);
+    vector1<int> bt(nh);
+    for (int i = 0; i < nh; i++) {
+        ib[i] = isbound[i] != 0;
+        bt[i] = boundto[i];
+    }
+    bbs.isbound = ib;
+    bbs.boundto = bt;
+    AbstractBindingModel *bm = nullptr;
+    vector<const vector1<double> *> dv(6, nullptr), tv(10, nullptr);
+    BindingModelBinary *bb = nullptr;
+    SortingFunctionUniform fu;
+    SortingFunctionNonUniform fn;
+    BindingModelTernary<SortingFunctionUniform> *tu = nullptr;
+    BindingModelTernary<SortingFunctionNonUniform> *tn = nullptr;
+    if (bm_kind == 0) {
+        bm = new BindingModelSingle(args[0], args[1]);
+    } else if (bm_kind == 1) {
+        bb = new BindingModelBinary((int)args[0]);
+        bb->setup_equilibrium();
+        bm = bb;
+        dv[0] = &bb->doubr11; dv[1] = &bb->doubr12; dv[3] = &bb->doubr22;
+        tv[0] = &bb->tripr111; tv[1] = &bb->tripr112; tv[3] = &bb->tripr122; tv[6] = &bb->tripr222;
+    } else if (bm_kind == 2) {
+        fu.div1 = (int)args[0];
+        fu.div2 = (int)args[1];
+        tu = new BindingModelTernary<SortingFunctionUniform>(fu);
+        tu->setup(args[2], args[3], args[4], args[5], args[6], args[7], args[8], args[9], args[10], args[11],
+                  args[12], args[13], args[14], args[15], args[16]);
+        bm = tu;
+    } else {
+        fn.div1 = (int)args[0];
+        fn.div2 = (int)args[1];
+        fn.np = (int)args[2];
+        tn = new BindingModelTernary<SortingFunctionNonUniform>(fn);
+        tn->setup(args[3], args[4], args[5], args[6], args[7], args[8], args[9], args[10], args[11], args[12],
+                  args[13], args[14], args[15], args[16], args[17]);
+        bm = tn;
+    }
+    if (tu || tn) {
+        auto fill = [&](auto *t) {
+            dv[0] = &t->doubr11; dv[1] = &t->doubr12; dv[2] = &t->doubr13;
+            dv[3] = &t->doubr22; dv[4] = &t->doubr23; dv[5] = &t->doubr33;
+            tv[0] = &t->tripr111; tv[1] = &t->tripr112; tv[2] = &t->tripr113; tv[3] = &t->tripr122;
+            tv[4] = &t->tripr123; tv[5] = &t->tripr133; tv[6] = &t->tripr222; tv[7] = &t->tripr223;
+            tv[8] = &t->tripr233; tv[9] = &t->tripr333;
+        };
+        if (tu) fill(tu);
+        else fill(tn);
+    }
+    if (tables) {
+        for (int r = 0; r < 6; r++)
+            for (int k = 0; k < 4; k++) tables[4 * r + k] = dv[r] && dv[r]->getsize() > k ? dv[r]->gpcons(k) : 0.0;
+        for (int r = 0; r < 10; r++)
+            for (int k = 0; k < 16; k++)
+                tables[24 + 16 * r + k] = tv[r] && tv[r]->getsize() > k ? tv[r]->gpcons(k) : 0.0;
+    }
+    if (caps) {
+        caps[0] = pots->max_ang;
+        caps[1] = pots->max_check;
+    }
+    long np = (long)opairs.size();
+    for (long q = 0; q < np && q < plist_cap; q++) {
+        plist[5 * q + 0] = opairs[q].particle_index1;
+        plist[5 * q + 1] = opairs[q].particle_index2;
+        plist[5 * q + 2] = opairs[q].potn;
+        plist[5 * q + 3] = opairs[q].patch_index1;
+        plist[5 * q + 4] = opairs[q].patch_index2;
+    }
+    matrix<double> Fm(n, 3), Tm(n, 3);
+    Fm.reset_parallel(0.0);
+    Tm.reset_parallel(0.0);
+    srand(seed);
+    b->calculate_forces_and_torques3D_onlyone_nonlets(opairs, runs_diff, *pots, bbs, *bm, Fm, Tm);
+    from_mat(Fm, F, n, 3);
+    from_mat(Tm, T, n, 3);
+    for (int i = 0; i < nh; i++) {
+        isbound[i] = bbs.isbound[i] ? 1 : 0;
+        boundto[i] = bbs.boundto[i];
+    }
+    delete bm;
+    delete pairs;
+    delete pots;
+    delete b;
+    return np;
+}
+
 // LangevinNVTR::genfullmat (LangevinR.cpp:392-461) for a single particle's body angular momentum.
 void ref_rotation_matrix(double dt, const double *L, double *R)
 {

@@ -145,6 +145,55 @@ def analysis_cases():
               f"components={len(np.unique(labels))} largest={np.bincount(labels).max()}")
 
 
+# binding models of the single-bond fixtures: (reference kind, args); the Ternary setups take six binding
+# strengths then nine asymmetries (BindingModelTernary.cpp:29-140)
+TERNARY_SETUP = [0.6, 0.5, 0.4, 0.55, 0.45, 0.35] + [0.1, -0.2, 0.3, 0.0, 0.15, -0.1, 0.2, -0.3, 0.05]
+SINGLEBOND_CASES = [
+    # (n, phi, cos thetam, periodic, seed, bm_kind, args)
+    (400, 0.15, 0.90, True, 11, 0, [1.0, 0.1]),
+    (300, 0.30, 0.70, True, 12, 0, [0.7, 0.5]),
+    (300, 0.30, 0.70, True, 13, 1, [600]),
+    (300, 0.30, 0.70, True, 14, 2, [400, 900] + TERNARY_SETUP),
+    (300, 0.30, 0.70, True, 15, 3, [300, 800, 3] + TERNARY_SETUP),
+    (300, 0.30, 0.75, False, 16, 0, [1.0, 0.2]),
+]
+
+
+def singlebond_cases():
+    """I. single-bond force pass: the reference's calculate_patch_list + onlyone_nonlets (srand(seed) first)
+    over three rounds from an unbound start: round 1 re-decides the round-0 bonds in place, round 2 after
+    new orientations (bonds break)."""
+    import hashlib
+    for k, (n, phi, cosm, per, seed, kind, args) in enumerate(SINGLEBOND_CASES):
+        box = box_for(n, phi)
+        spec = ReplicaSpec(n=n, box=box, model=PatchModelSpec.tetrahedral(n, 8.0, 1.2, math.acos(cosm)),
+                           periodic=per, seed=seed)
+        x = f32(random_positions(n, box, per, 0.9, 3000 + seed))
+        Qs = [f32(random_rotations(n, 4000 + seed))] * 2 + [f32(random_rotations(n, 5000 + seed))]
+        npatch = 4 * n
+        bt = np.zeros(npatch, dtype=np.intc)
+        ib = np.zeros(npatch, dtype=np.uint8)
+        rec = dict(x=x, Q=np.stack(Qs), bm_kind=kind, args=np.asarray(args, float), srand=seed)
+        outs = {key: [] for key in ("bt_in", "ib_in", "bt", "ib", "F", "T", "plist_sha", "plist_n")}
+        for rnd in range(3):
+            r = po.ref_singlebond(spec, x, Qs[rnd], 2.5, kind, args, bt, ib, seed + rnd)
+            pl = r["plist"][np.lexsort(r["plist"].T[::-1])]
+            outs["bt_in"].append(bt.copy())
+            outs["ib_in"].append(ib.copy())
+            outs["bt"].append(r["boundto"])
+            outs["ib"].append(r["isbound"])
+            outs["F"].append(r["F"])
+            outs["T"].append(r["T"])
+            outs["plist_sha"].append(hashlib.sha256(np.ascontiguousarray(pl, dtype=np.int32).tobytes()).hexdigest())
+            outs["plist_n"].append(len(pl))
+            bt, ib = r["boundto"].copy(), r["isbound"].copy()
+        rec.update({key: np.asarray(v) for key, v in outs.items()})
+        rec.update(tables=r["tables"], max_ang=r["max_ang"], max_check=r["max_check"])
+        np.savez_compressed(HERE / f"singlebond_{k}.npz", **rec, **spec_record(spec))
+        print(f"singlebond_{k}: n={n} phi={phi} cos={cosm} model={kind} candidates={outs['plist_n']} "
+              f"bound={[int(v.sum()) for v in outs['ib']]}")
+
+
 def ref_run(spec, st, nsteps, rc, rebuild, noise=None, init=True, noise0=None):
     R = po.ref()
     kind, att, dis, th, nt, ppt, npt, orient, params = po.ref_model_args(spec.model)
@@ -232,7 +281,8 @@ def spec_record(spec):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
-    ap.add_argument("--only", choices=["bonded", "frames", "analysis"], help="regenerate one group of fixtures only")
+    ap.add_argument("--only", choices=["bonded", "frames", "analysis", "singlebond"],
+                    help="regenerate one group of fixtures only")
     args = ap.parse_args()
     po.build_oracle()
     po.build_ref(args.reference)
@@ -245,6 +295,9 @@ def main():
         return
     if args.only == "analysis":
         analysis_cases()
+        return
+    if args.only == "singlebond":
+        singlebond_cases()
         return
 
     # ---- A. pair sets (MD::calculatepairs and calculatepairs_parallel)
@@ -334,6 +387,7 @@ def main():
     bonded_cases()
     frame_cases()
     analysis_cases()
+    singlebond_cases()
 
 
 if __name__ == "__main__":
