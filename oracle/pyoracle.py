@@ -286,6 +286,15 @@ class System:
 
 
     # ---- single-bond mode
+    def central_forces(self, x) -> np.ndarray:
+        """MD::calculateforces with the HSPotential (plus any fixed bonds): the central forces alone."""
+        x = np.ascontiguousarray(x, float)
+        rc = 1.12246 * float(self.spec.hs_sigma) * 1.01
+        pr = self.pairs(x, rc)
+        F = np.empty((self.spec.n, 3))
+        orc().orc_central_forces(C.byref(self.params), _d(x), pr.ctypes.data_as(_I), len(pr), _d(F))
+        return F
+
     def max_check(self) -> float:
         return orc().orc_max_check(C.byref(self.model))
 
