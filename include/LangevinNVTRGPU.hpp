@@ -46,6 +46,84 @@ void from_rows(const std::vector<double> &in, int n, int c, M &m) {
         for (int k = 0; k < c; k++) m(i, k) = in[(size_t)c * i + k];
 }
 
+// Binding models of the reference (MDBase/Bindings) in the C ABI's table form.  Templates, so this header
+// needs none of the reference's headers: any object with the reference's public members converts.
+// BindingModelSingle: on_rate, off_rate.
+template <class BMS>
+mtg_binding_model binding_single_from(const BMS &bm) {
+    mtg_binding_model m;
+    mtg_binding_single(&m, bm.on_rate, bm.off_rate);
+    return m;
+}
+
+template <class Vec>
+void copy_rates(const Vec &v, double *out, int count) {
+    for (int k = 0; k < count; k++) out[k] = k < v.getsize() ? v.gpcons(k) : 0.0;
+}
+
+// BindingModelBinary: div and its rate vectors; its 122 / 222 triplets take the rate to none-bound from
+// tripr111 (BindingModelBinary.cpp triplet)
+template <class BMB>
+mtg_binding_model binding_binary_from(const BMB &bm) {
+    mtg_binding_model m{};
+    m.species_rule = 1;
+    m.div1 = bm.div;
+    m.np = 1;
+    copy_rates(bm.doubr11, m.drate[0], 4);
+    copy_rates(bm.doubr12, m.drate[1], 4);
+    copy_rates(bm.doubr22, m.drate[3], 4);
+    copy_rates(bm.tripr111, m.trate[0], 16);
+    copy_rates(bm.tripr112, m.trate[1], 16);
+    copy_rates(bm.tripr122, m.trate[3], 16);
+    copy_rates(bm.tripr222, m.trate[6], 16);
+    for (int r : {3, 6})
+        for (int st = 0; st < 4; st++) m.trate[r][4 * st + 3] = m.trate[0][4 * st + 3];
+    return m;
+}
+
+template <class BMT>
+void ternary_rates(const BMT &bm, mtg_binding_model &m) {
+    copy_rates(bm.doubr11, m.drate[0], 4);
+    copy_rates(bm.doubr12, m.drate[1], 4);
+    copy_rates(bm.doubr13, m.drate[2], 4);
+    copy_rates(bm.doubr22, m.drate[3], 4);
+    copy_rates(bm.doubr23, m.drate[4], 4);
+    copy_rates(bm.doubr33, m.drate[5], 4);
+    copy_rates(bm.tripr111, m.trate[0], 16);
+    copy_rates(bm.tripr112, m.trate[1], 16);
+    copy_rates(bm.tripr113, m.trate[2], 16);
+    copy_rates(bm.tripr122, m.trate[3], 16);
+    copy_rates(bm.tripr123, m.trate[4], 16);
+    copy_rates(bm.tripr133, m.trate[5], 16);
+    copy_rates(bm.tripr222, m.trate[6], 16);
+    copy_rates(bm.tripr223, m.trate[7], 16);
+    copy_rates(bm.tripr233, m.trate[8], 16);
+    copy_rates(bm.tripr333, m.trate[9], 16);
+}
+
+// BindingModelTernary<SortingFunctionUniform> / <SortingFunctionNonUniform> (BindingModelTernary.h:6-30)
+template <class BMT>
+mtg_binding_model binding_ternary_uniform_from(const BMT &bm) {
+    mtg_binding_model m{};
+    m.species_rule = 2;
+    m.div1 = bm.func.div1;
+    m.div2 = bm.func.div2;
+    m.np = 1;
+    ternary_rates(bm, m);
+    return m;
+}
+
+template <class BMT>
+mtg_binding_model binding_ternary_nonuniform_from(const BMT &bm) {
+    mtg_binding_model m{};
+    m.species_rule = 3;
+    m.div1 = bm.func.div1;
+    m.div2 = bm.func.div2;
+    m.np = bm.func.np;
+    ternary_rates(bm, m);
+    return m;
+}
+
 }  // namespace mtg_adapter
 
 template <class Matrix>
@@ -117,6 +195,56 @@ class LangevinNVTRGPU {
             b[2 * (size_t)i + 1] = bonds(i, 1);
         }
         mtg_adapter::require_ok(h_, mtg_set_bonds(h_, nb ? b.data() : nullptr, nb, k, r0), "setbonds");
+    }
+
+    // Condensate::run_singlebond (Condensate.cpp:422-618): from now on each force pass keeps one bond per
+    // patch, decided by the binding model (mtg_adapter::binding_*_from converts the reference's models), and
+    // only bound patch pairs exert the Kern-Frenkel force.  The candidate list is rebuilt every patch_every
+    // steps from pairs closer than list_cut (run_singlebond: 10 steps, 2.5 sigma).
+    void setsinglebond(const mtg_binding_model &bm, int patch_every = 10, double list_cut = 2.5) {
+        if (!h_) create();
+        mtg_single_bond sb;
+        mtg_single_bond_defaults(&sb);
+        sb.model = bm;
+        sb.patch_every = patch_every;
+        sb.list_cut = list_cut;
+        mtg_adapter::require_ok(h_, mtg_set_single_bond(h_, &sb), "setsinglebond");
+    }
+
+    // BinaryBindStore (Bindings/BinaryBindStore.h): isbound / boundto of every patch, in and out; any
+    // vectors with operator[] and getsize() (e.g. vector1<bool>, vector1<int>)
+    template <class BoolVec, class IntVec>
+    void setbindings(BoolVec &isbound, IntVec &boundto) {
+        const int64_t np = mtg_num_patches(h_);
+        std::vector<int32_t> bt((size_t)np);
+        std::vector<uint8_t> ib((size_t)np);
+        for (int64_t i = 0; i < np; i++) {
+            bt[(size_t)i] = boundto[(int)i];
+            ib[(size_t)i] = isbound[(int)i] ? 1 : 0;
+        }
+        mtg_adapter::require_ok(h_, mtg_set_bind_state(h_, bt.data(), ib.data()), "setbindings");
+    }
+    template <class BoolVec, class IntVec>
+    void getbindings(BoolVec &isbound, IntVec &boundto) {
+        const int64_t np = mtg_num_patches(h_);
+        std::vector<int32_t> bt((size_t)np);
+        std::vector<uint8_t> ib((size_t)np);
+        mtg_adapter::require_ok(h_, mtg_get_bind_state(h_, bt.data(), ib.data()), "getbindings");
+        for (int64_t i = 0; i < np; i++) {
+            boundto[(int)i] = bt[(size_t)i];
+            isbound[(int)i] = ib[(size_t)i] != 0;
+        }
+    }
+
+    // LangevinNVTR::calculate_forces_and_torques3D_onlyone_nonlets (LangevinRforce.cpp:2874-4030) at the
+    // current state, with the candidate list rebuilt first: decides the bonds, then F = calculateforces(HS)
+    // + bound-pair forces and T = bound-pair torques, as run_singlebond's first call (Condensate.cpp:455-460)
+    void calculate_forces_and_torques3D_onlyone_nonlets(Matrix &F, Matrix &T) {
+        const int n = desc_.n;
+        std::vector<double> f((size_t)n * 3), t((size_t)n * 3);
+        mtg_adapter::require_ok(h_, mtg_bind_update(h_, f.data(), t.data()), "calculate_forces_and_torques3D_onlyone_nonlets");
+        mtg_adapter::from_rows(f, n, 3, F);
+        mtg_adapter::from_rows(t, n, 3, T);
     }
 
     // MD::calculatepairs_parallel(boxes, rc) -> pairs (i < j), P x 2, into any resizable int matrix

@@ -214,10 +214,12 @@ int64_t mtg_launch_count(const mtg_system *h);
 /* Instrumented steps: nsteps of mtg_step launched one kernel at a time (no graph) with CUDA events
  * around every launch on the handle's stream.  kernel_ms[k] receives the summed device time of
  * kernel k over the nsteps, for k = 0 scan_reduce, 1 scan_top, 2 scan_down, 3 scatter (reorder +
- * first half-step), 4 force (force/torque + Langevin epilogue + next binning).  With a neighbour skin:
- * 0 = rebuild decision + binning + scan_reduce, 1 scan_top, 2 scan_down, 3 scatter + copy-back (rebuild
- * steps) + in-place first half-step (other steps), 4 force.  Synchronising. */
-#define MTG_PROFILE_KERNELS 5
+ * first half-step), 4 force (force/torque + Langevin epilogue + next binning), and in single-bond mode
+ * 5 bind_candidates (the update's start + the candidate list when due), 6 bind_decide (edges, clusters,
+ * bond decisions).  With a neighbour skin: 0 = rebuild decision + binning + scan_reduce, 1 scan_top,
+ * 2 scan_down, 3 scatter + copy-back (rebuild steps) + in-place first half-step (other steps), 4 force.
+ * Synchronising. */
+#define MTG_PROFILE_KERNELS 7
 mtg_status mtg_step_profile(mtg_system *h, int nsteps, double *kernel_ms);
 
 /* With a neighbour skin: list rebuilds since mtg_create (each initial force pass and each step that

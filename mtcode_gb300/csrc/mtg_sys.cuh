@@ -1023,9 +1023,9 @@ struct Sys : SysBase {
         step(0, nullptr);  // initial forces / bins, as mtg_step would
         unsigned long long h[2] = {draw, draw};
         MTG_CUDA(cudaMemcpyAsync(d_draw, h, sizeof(h), cudaMemcpyHostToDevice, st));
-        cudaEvent_t ev[6];
+        cudaEvent_t ev[10];
         for (auto &e : ev) MTG_CUDA(cudaEventCreate(&e));
-        double acc[5] = {0, 0, 0, 0, 0};
+        double acc[MTG_PROFILE_KERNELS] = {};
         mtg::Tables<real> tb = tables();
         const int g = grid_for(ntot_, 256, occ_stream, sms);
         const int gf = grid_for(ntot_, 128, occ_force, sms);
@@ -1060,6 +1060,9 @@ struct Sys : SysBase {
         }
         for (int s = 0; s < nsteps && skin <= 0; s++) {
             const int b = cur;
+            MTG_CUDA(cudaEventRecord(ev[6], st));
+            if (single_bond) enqueue_bind_begin(b, 0, 1);
+            MTG_CUDA(cudaEventRecord(ev[7], st));
             MTG_CUDA(cudaEventRecord(ev[0], st));
             mtg::scan_reduce_kernel<<<nblk, mtg::kScanThreads, 0, st>>>(d_count, ncells, d_block);
             MTG_CUDA(cudaEventRecord(ev[1], st));
@@ -1068,23 +1071,30 @@ struct Sys : SysBase {
             mtg::scan_down_kernel<<<nblk, mtg::kScanThreads, 0, st>>>(d_count, ncells, d_block, d_start);
             MTG_CUDA(cudaEventRecord(ev[3], st));
             mtg::scatter_kernel<real, true><<<g, 256, 0, st>>>(tb, buf[b], buf[b ^ 1], d_bin, d_start, d_flags);
+            MTG_CUDA(cudaEventRecord(ev[8], st));
+            if (single_bond) enqueue_bind_decide(b ^ 1);
+            MTG_CUDA(cudaEventRecord(ev[9], st));
             MTG_CUDA(cudaEventRecord(ev[4], st));
             mtg::ForceArgs<real> a = force_args(b ^ 1, 1);
             launch_force<mtg::kModeStep>(a);
             MTG_CUDA(cudaEventRecord(ev[5], st));
             check_launch();
             MTG_CUDA(cudaEventSynchronize(ev[5]));
+            float ms = 0;
             for (int k = 0; k < 5; k++) {
-                float ms = 0;
-                MTG_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+                MTG_CUDA(cudaEventElapsedTime(&ms, ev[k == 3 ? 3 : k], k == 3 ? ev[8] : ev[k + 1]));
                 acc[k] += ms;
             }
+            MTG_CUDA(cudaEventElapsedTime(&ms, ev[6], ev[7]));
+            acc[5] += ms;
+            MTG_CUDA(cudaEventElapsedTime(&ms, ev[8], ev[9]));
+            acc[6] += ms;
             cur ^= 1;
-            nlaunch += 5;
+            nlaunch += 5 + (single_bond ? kBindLaunches : 0);
             draw += 1;
         }
         for (auto &e : ev) cudaEventDestroy(e);
-        for (int k = 0; k < 5; k++) kernel_ms[k] = acc[k];
+        for (int k = 0; k < MTG_PROFILE_KERNELS; k++) kernel_ms[k] = acc[k];
         cells_valid = true;
         bins_valid = true;
     }

@@ -25,6 +25,8 @@ def main() -> None:
     ap.add_argument("--kernel", choices=["pairs", "tiled", "per_particle"], default="pairs")
     ap.add_argument("--profile", action="store_true", help="also print per-kernel device times")
     ap.add_argument("--skin", type=float, default=0.0, help="neighbour skin (sigma); 0 rebuilds cells every step")
+    ap.add_argument("--single-bond", nargs=2, type=float, metavar=("ON", "OFF"), default=None,
+                    help="single-bond-per-patch mode (run_singlebond) with BindingModelSingle(ON, OFF)")
     args = ap.parse_args()
     if args.workload == "c4":
         W = workloads.patchy_c4(seed=args.seed, n_replicas=args.replicas)
@@ -38,6 +40,9 @@ def main() -> None:
         s.initialize(W.x, z, z, W.Q)
         if W.bonds is not None:
             s.set_bonds(W.bonds, W.bond_k, W.bond_r0)
+        if args.single_bond:
+            from .system import binding_single
+            s.set_single_bond(binding_single(*args.single_bond))
         s.init_forces()
         s.sync()
         t0 = time.perf_counter()
@@ -48,6 +53,8 @@ def main() -> None:
                f"{n * args.steps / dt:.3e} particle-steps/s"
         if args.skin > 0:
             line += f", {s.rebuilds} list builds"
+        if args.single_bond:
+            line += f", {int(s.get_bind_state()[1].sum())} bound patches"
         if args.profile:
             prof = s.step_profile(max(1, args.steps))
             line += " | " + " ".join(f"{k}={v / max(1, args.steps):.3f}ms" for k, v in prof.items())

@@ -62,4 +62,44 @@ void run_on_gpu(double l, int N, matrix<double> &dat, int runtime, TetrahedralPa
     obj.getorientation(orient);
 }
 
+// Condensate::run_singlebond's loop with the force pass on the GPU: the reference's binding models and
+// BinaryBindStore go through the adapter unchanged
+void run_singlebond_on_gpu(double l, int N, matrix<double> &dat, int runtime, TetrahedralPatch &pots) {
+    mtg_patch_model model;
+    mtg_model_tetrahedral(&model, pots.str, pots.dis, pots.ang);
+    LangevinNVTRGPU<matrix<double>> obj(l, true, N, model);
+    obj.sethardcore(3.0, 1.0);   // HSPotential wsa(3.0, size_mol) (Condensate.cpp:440)
+    BindingModelSingle single(1.0, 0.1);
+    BindingModelBinary binary(2 * N);
+    binary.setup_equilibrium();
+    SortingFunctionUniform fu;
+    fu.div1 = N;
+    fu.div2 = 2 * N;
+    BindingModelTernary<SortingFunctionUniform> ternary(fu);
+    SortingFunctionNonUniform fn;
+    fn.div1 = N;
+    fn.div2 = 2 * N;
+    fn.np = 3;
+    BindingModelTernary<SortingFunctionNonUniform> ternary2(fn);
+    mtg_binding_model tables[4] = {mtg_adapter::binding_single_from(single), mtg_adapter::binding_binary_from(binary),
+                                   mtg_adapter::binding_ternary_uniform_from(ternary),
+                                   mtg_adapter::binding_ternary_nonuniform_from(ternary2)};
+    obj.setsinglebond(tables[0]);
+    matrix<double> mom(N, 3), ang(N, 3), orient(N, 9);
+    for (int i = 0; i < N; i++) orient(i, 0) = orient(i, 4) = orient(i, 8) = 1.0;
+    obj.initialize(dat, mom, orient, ang);
+    BinaryBindStore bbs;
+    vector1<bool> isbound(4 * N);
+    vector1<int> boundto(4 * N);
+    bbs.isbound = isbound;
+    bbs.boundto = boundto;
+    obj.setbindings(bbs.isbound, bbs.boundto);
+    matrix<double> F(N, 3), T(N, 3);
+    obj.calculate_forces_and_torques3D_onlyone_nonlets(F, T);
+    obj.init_forces();
+    for (int i = 0; i < runtime; i++) obj.step(1);
+    obj.getbindings(bbs.isbound, bbs.boundto);
+    obj.getdat(dat);
+}
+
 int main() { return 0; }
