@@ -3,25 +3,20 @@
 // pairs exert the Kern-Frenkel force.
 //
 // Per step (all replicas in every launch):
-//   [begin]     one thread: this update's stamp, whether the candidate list is due (every patch_every steps)
-//   [candidates] one thread per particle, every patch_every steps (LangevinNVTR::calculate_patch_list,
-//               LangevinR.cpp:1702-1852): patch pairs of particle pairs closer than
-//               min(list cut, max_check + 1) whose cones pass (c_i - max_ang) + (c_j - max_ang) > -0.4.
-//               Entries hold particle ids and patch ids, so they outlive the re-sorting of every step.
-//   [edges]     one thread per candidate (LangevinRforce.cpp:2900-3090): the distance / cone / bind-state
-//               test; an edge goes into both patches' adjacency (stamped counters: no reset pass).
-//   [decide]    one thread per patch: no edge -> unbound; else a breadth-first walk of its component.  The
-//               component's smallest patch decides a cluster of two or three (doublet / triplet of the
-//               binding model, LangevinRforce.cpp:3160-3480); members of larger components queue for:
-//   [large]     one thread per queued patch; the smallest one runs the reference's reduction (drop the
-//               highest-scoring edge until no piece exceeds three patches, LangevinRforce.cpp:3560-3880)
-//               with its scratch in global memory.
-// The bound pairs' forces are added by the force epilogue (bound_patch_forces), from both ends.
-//
-// Exactness.  Every test that decides a bond is the reference's FP64 expression, evaluated with explicit
-// roundings in the reference's operation order on the stored coordinates, so the GPU and an FP64 CPU
-// evaluation of the same state take identical decisions.  In FP32 the tests first run in float; only a
-// value within a margin of its threshold (far above the float evaluation's error) is re-evaluated in FP64.
+//   [begin]    one thread: this update's stamp; whether the candidate list is due (every patch_every steps
+//              of the run_singlebond loop).  When it is, the scatter stores every particle's position and
+//              rotation at the start of the step (the snapshot the candidate list is evaluated on);
+//              otherwise particles carry their snapshot along.
+//   [edges]    inside the force pass's pair loop (bind_pair_edges in mtg_kernels.cuh): every patch pair
+//              that passes the current edge test and the candidate-list condition on the snapshot goes into
+//              both patches' adjacency (stamped counters, no reset pass).
+//   [decide]   one thread per patch: no edge -> unbound; else a breadth-first walk of its component.  The
+//              component's smallest patch decides a cluster of two or three (doublet / triplet of the
+//              binding model, LangevinRforce.cpp:3160-3480); members of larger components queue for:
+//   [large]    one thread per queued patch; the smallest one runs the reference's reduction (drop the
+//              highest-scoring edge until no piece exceeds three patches, LangevinRforce.cpp:3560-3880)
+//              with its scratch in global memory.
+// The bound pairs' forces are then added by the force epilogue (bound_patch_forces), from both ends.
 #pragma once
 
 #include <cooperative_groups.h>
@@ -30,11 +25,9 @@
 
 namespace mtg {
 
-constexpr int kAdjCap = 8;            // candidate partners of one patch in one update
 constexpr int kClusterCap = 128;      // patches of one cluster reduced by one thread
 constexpr int kClusterEdges = kClusterCap * kAdjCap / 2;
 constexpr int kLargeThreads = 64;     // block of the large-cluster kernel
-constexpr unsigned kFlagBind = 0x20u; // a capacity of this mode was exceeded (see MTG_FLAG_BIND)
 
 // binding model in table form: species rule of a patch index, doublet rows (species pairs 11, 12, 13, 22,
 // 23, 33; [before * 2 + 0] to unbound, + 1 to bound) and triplet rows (sorted triples 111 ... 333,
@@ -52,12 +45,10 @@ struct BindState {
     int nrep;
     int ptot;
     int patch_every;
-    int4 *plist;                  // candidates: (id1 < id2, patch of id1, patch of id2), global indices
-    long long plist_cap;
-    unsigned long long *ctr;      // [0] candidates [1] queued large-cluster patches [2] update stamp
-                                  // [3] steps of the run_singlebond loop so far [4] candidates due this update
+    unsigned long long *ctr;      // [1] queued large-cluster patches [2] update stamp [3] steps of the
+                                  // run_singlebond loop so far [4] candidate list due this update
     unsigned long long *deg;      // per patch: stamp << 32 | edges of this update
-    int2 *adj;                    // per patch kAdjCap: (partner patch, candidate << 2 | disp2 class)
+    int2 *adj;                    // per patch kAdjCap: (partner patch, disp2 class)
     int *boundto;                 // global patch indices
     unsigned char *isbound;
     int *large;                   // queued patches of clusters above three
@@ -69,196 +60,23 @@ struct BindState {
 
 namespace {
 
-// ------------------------------------------------------------------ FP64 tests in the reference's order
-// cube::distance_vector (geometry.h:277-294): un = x_a - x_b (minimum image), returns |un|^2
-__device__ __forceinline__ double exact_dist_vec(const BindRep &B, const double xa[3], const double xb[3], double un[3]) {
-    double temp = 0.0;
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        double as = __dsub_rn(xa[k], xb[k]);
-        if (B.periodic && __dmul_rn(as, as) > B.l2s) as = as >= 0.0 ? __dsub_rn(as, B.box) : __dadd_rn(as, B.box);
-        temp = __dadd_rn(temp, __dmul_rn(as, as));
-        un[k] = as;
-    }
-    return temp;
-}
-
-// Q^T n_b (LangevinRforce.cpp:2980-2985) then -(n . u) or (n . u)
-__device__ __forceinline__ double exact_cos(const double nb[3], const double q[9], const double u[3], bool negate) {
-    double n[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++)
-        n[k] = __dadd_rn(__dadd_rn(__dmul_rn(nb[0], q[k]), __dmul_rn(nb[1], q[3 + k])), __dmul_rn(nb[2], q[6 + k]));
-    const double d = __dadd_rn(__dadd_rn(__dmul_rn(n[0], u[0]), __dmul_rn(n[1], u[1])), __dmul_rn(n[2], u[2]));
-    return negate ? -d : d;
-}
-
-// position and rotation of a slot as doubles (exact conversions of the stored values)
-template <class real>
-__device__ __forceinline__ void load_state_d(const Buffers<real> &b, int s, double x[3], double q[9]) {
-    Payload<real> P;
-    P.load(b.pos, b.rota, b.rotb, s);
-#pragma unroll
-    for (int k = 0; k < 3; k++) x[k] = (double)P.v[k];
-#pragma unroll
-    for (int k = 0; k < 9; k++) q[k] = (double)P.v[3 + k];
-}
-
-// float value v against threshold t: +1 certainly above, -1 certainly below, 0 too close to tell
-__device__ __forceinline__ int side(double v, double t, double margin) {
-    return v > t + margin ? 1 : (v < t - margin ? -1 : 0);
-}
-
-// ------------------------------------------------------------------ candidate list
-__device__ __forceinline__ void plist_append(const BindState &S, int4 e) {
-    namespace cg = cooperative_groups;
-    cg::coalesced_group g = cg::coalesced_threads();
-    unsigned long long base = 0;
-    if (g.thread_rank() == 0) base = atomicAdd(S.ctr, (unsigned long long)g.size());
-    base = g.shfl(base, 0) + g.thread_rank();
-    if ((long long)base < S.plist_cap) S.plist[base] = e;
-    else atomicOr(S.flags, kFlagBind);
-}
-
-// cells of one axis within `reach` of cell c, each once (all cells when the grid is narrower than the stencil)
-__device__ __forceinline__ int axis_cells(int c, int nc, int reach, int periodic, int out[5]) {
-    int m = 0;
-    if (nc <= 2 * reach) {
-        for (int k = 0; k < nc && k < 5; k++) out[m++] = k;
-        return m;
-    }
-    for (int d = -reach; d <= reach; d++) {
-        int cc = c + d;
-        if (cc < 0 || cc >= nc) {
-            if (!periodic) continue;
-            cc = cc < 0 ? cc + nc : cc - nc;
-        }
-        out[m++] = cc;
-    }
-    return m;
-}
-
 __global__ void bind_begin_kernel(BindState S, int force, int advance) {
     if (threadIdx.x || blockIdx.x) return;
     const unsigned long long step = S.ctr[3];
-    const int due = force || (step > 0 && S.patch_every > 0 && step % (unsigned long long)S.patch_every == 0);
-    S.ctr[4] = due;
-    if (due) S.ctr[0] = 0;
+    S.ctr[4] = force || (step > 0 && S.patch_every > 0 && step % (unsigned long long)S.patch_every == 0);
     S.ctr[1] = 0;
     S.ctr[2] += 1;
     if (advance) S.ctr[3] = step + 1;
 }
 
-// LangevinNVTR::calculate_patch_list on the current (cell-sorted) buffers
+// the candidate list is due now, at the current positions (a pass that does not move particles)
 template <class real>
-__global__ void __launch_bounds__(256) bind_candidates_kernel(ForceArgs<real> a, BindState S) {
-    if (!S.ctr[4]) return;
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= a.tb.ntot) return;
-    const int r = find_replica(a.tb.rep_slot, a.tb.nrep, s);
-    const Replica<real> &R = a.tb.reps[r];
-    const Model<real> &M = a.tb.models[R.model];
-    const BindRep &B = S.reps[r];
-    const int id = a.buf.ident[s], li = id - R.off, ti = type_of<real>(M, li), na = M.np[ti];
-    if (na == 0) return;
-    Payload<real> Pi;
-    Pi.load(a.buf.pos, a.buf.rota, a.buf.rotb, s);
-    const int nc = R.nc;
-    int cx[5], cy[5], cz[5];
-    const int mx = axis_cells(axis_cell<real>(Pi.v[0], R.cell_scale, nc), nc, B.reach, R.periodic, cx);
-    const int my = axis_cells(axis_cell<real>(Pi.v[1], R.cell_scale, nc), nc, B.reach, R.periodic, cy);
-    const int mz = axis_cells(axis_cell<real>(Pi.v[2], R.cell_scale, nc), nc, B.reach, R.periodic, cz);
-    const double max_dis2 = B.max_dis * B.max_dis;
-    for (int iz = 0; iz < mz; iz++)
-        for (int iy = 0; iy < my; iy++)
-            for (int ix = 0; ix < mx; ix++) {
-                const int cell = R.cell_off + cx[ix] + nc * (cy[iy] + nc * cz[iz]);
-                const int j0 = __ldg(a.start + cell), j1 = __ldg(a.start + cell + 1);
-                for (int j = j0; j < j1; j++) {
-                    const int idj = __ldg(a.buf.ident + j);
-                    if (idj <= id) continue;   // each pair once, p1 < p2 (LangevinR.cpp:1722-1727)
-                    const int lj = idj - R.off, tj = type_of<real>(M, lj), nb = M.np[tj];
-                    if (nb == 0) continue;
-                    real xj, yj, zj;
-                    load_pos(a.buf.pos + 4 * (size_t)j, xj, yj, zj);
-                    const real dx = min_image<real>(Pi.v[0] - xj, R.box, R.l2s, R.periodic);
-                    const real dy = min_image<real>(Pi.v[1] - yj, R.box, R.l2s, R.periodic);
-                    const real dz = min_image<real>(Pi.v[2] - zj, R.box, R.l2s, R.periodic);
-                    const double d2f = (double)(dx * dx + dy * dy + dz * dz);
-                    // pair list (distance_less_than at the list cut) and dis < max_check + 1
-                    int in1 = side(d2f, B.list_cut2, 1e-5 * B.list_cut2), in2 = side(d2f, max_dis2, 1e-5 * max_dis2);
-                    if (in1 > 0 || in2 > 0) continue;
-                    double xa[3], qa[9], xb[3], qb[9], un[3];
-                    bool exact = std::is_same<real, double>::value || in1 == 0 || in2 == 0;
-                    double d2 = d2f, dis = 0;
-                    if (exact) {
-                        load_state_d<real>(a.buf, s, xa, qa);
-                        load_state_d<real>(a.buf, j, xb, qb);
-                        d2 = exact_dist_vec(B, xa, xb, un);
-                        if (!(d2 < B.list_cut2)) continue;
-                        dis = __dsqrt_rn(d2);
-                        if (!(dis < B.max_dis)) continue;
-                        un[0] = __ddiv_rn(un[0], dis); un[1] = __ddiv_rn(un[1], dis); un[2] = __ddiv_rn(un[2], dis);
-                    }
-                    // cones of every patch pair, float first where it is decisive
-                    real Qj[9];
-                    {
-                        Payload<real> Pj;
-                        Pj.load(a.buf.pos, a.buf.rota, a.buf.rotb, j);
-#pragma unroll
-                        for (int k = 0; k < 9; k++) Qj[k] = Pj.v[3 + k];
-                    }
-                    const real rr = sqrt(dx * dx + dy * dy + dz * dz);
-                    const real u[3] = {dx / rr, dy / rr, dz / rr};
-                    real wa[3], wb[3];
-#pragma unroll
-                    for (int k = 0; k < 3; k++) {
-                        wa[k] = Pi.v[3 + 3 * k] * u[0] + Pi.v[4 + 3 * k] * u[1] + Pi.v[5 + 3 * k] * u[2];
-                        wb[k] = Qj[3 * k] * u[0] + Qj[3 * k + 1] * u[1] + Qj[3 * k + 2] * u[2];
-                    }
-                    const int oa = M.ooff[ti], ob = M.ooff[tj];
-                    for (int ka = 0; ka < na; ka++) {
-                        const real *va = M.orient[oa + ka];
-                        const real ci = -(va[0] * wa[0] + va[1] * wa[1] + va[2] * wa[2]);
-                        for (int kb = 0; kb < nb; kb++) {
-                            const real *vb = M.orient[ob + kb];
-                            const real cj = vb[0] * wb[0] + vb[1] * wb[1] + vb[2] * wb[2];
-                            int pass = side(((double)ci - B.max_ang) + ((double)cj - B.max_ang), -0.4, 4e-5);
-                            if (exact || pass == 0) {
-                                if (!exact) {
-                                    load_state_d<real>(a.buf, s, xa, qa);
-                                    load_state_d<real>(a.buf, j, xb, qb);
-                                    d2 = exact_dist_vec(B, xa, xb, un);
-                                    dis = __dsqrt_rn(d2);
-                                    un[0] = __ddiv_rn(un[0], dis); un[1] = __ddiv_rn(un[1], dis); un[2] = __ddiv_rn(un[2], dis);
-                                    exact = true;
-                                }
-                                const double ei = exact_cos(B.orient[oa + ka], qa, un, true);
-                                const double ej = exact_cos(B.orient[ob + kb], qb, un, false);
-                                pass = __dadd_rn(__dsub_rn(ei, B.max_ang), __dsub_rn(ej, B.max_ang)) > -0.4 ? 1 : -1;
-                            }
-                            if (pass > 0)
-                                plist_append(S, make_int4(id, idj, patch_of<real>(B, M, li, ti, ka),
-                                                          patch_of<real>(B, M, lj, tj, kb)));
-                        }
-                    }
-                }
-            }
-}
-
-// ------------------------------------------------------------------ edges
-// slot of this update's adjacency for patch p (stamped counter: a stale stamp counts as zero edges)
-__device__ __forceinline__ int adj_take(unsigned long long *deg, int p, unsigned stamp, unsigned *flags) {
-    unsigned long long old = deg[p];
-    for (int it = 0; it < (1 << 20); it++) {
-        const unsigned cnt = (unsigned)(old >> 32) == stamp ? (unsigned)old : 0u;
-        const unsigned long long nw = ((unsigned long long)stamp << 32) | (unsigned long long)(cnt + 1u);
-        const unsigned long long prev = atomicCAS(deg + p, old, nw);
-        if (prev == old) return (int)cnt;
-        old = prev;
+__global__ void __launch_bounds__(256) bind_snapshot_kernel(int ntot, Buffers<real> b) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ntot; s += gridDim.x * blockDim.x) {
+        Payload<real> P;
+        P.load(b.pos, b.rota, b.rotb, s);
+        P.store(b.snap_a, b.snap_b, b.snap_c, s);
     }
-    atomicOr(flags, kFlagBind);
-    return kAdjCap;
 }
 
 __device__ __forceinline__ int adj_count(const unsigned long long *deg, int p, unsigned stamp) {
@@ -267,111 +85,30 @@ __device__ __forceinline__ int adj_count(const unsigned long long *deg, int p, u
     return c < kAdjCap ? c : kAdjCap;
 }
 
-// the reference's bind-state dependent range (LangevinRforce.cpp:3010-3030): class 0 disp, 1 0.5 disp,
-// 2 0.7 disp
-__device__ __forceinline__ double disp2_of(double disp, int cls) {
-    return cls == 1 ? __dmul_rn(0.5, disp) : (cls == 2 ? __dmul_rn(0.7, disp) : disp);
-}
-
-// FP64 edge test of one candidate; with score != null also its score (LangevinRforce.cpp:3040-3060)
-template <class real>
-__device__ __forceinline__ bool exact_edge(const BindRep &B, const Buffers<real> &b, int s1, int s2, int o1, int o2,
-                                           int potn, double disp2, double *score) {
-    double xa[3], qa[9], xb[3], qb[9], un[3];
-    load_state_d<real>(b, s1, xa, qa);
-    load_state_d<real>(b, s2, xb, qb);
-    double dis = exact_dist_vec(B, xa, xb, un);
-    if (!(dis < B.mk2)) return false;
-    dis = __dsqrt_rn(dis);
-    un[0] = __ddiv_rn(un[0], dis); un[1] = __ddiv_rn(un[1], dis); un[2] = __ddiv_rn(un[2], dis);
-    const double ai = exact_cos(B.orient[o1], qa, un, true), aj = exact_cos(B.orient[o2], qb, un, false);
-    const double ctm = B.ctm[potn];
-    if (!(ai > ctm && aj > ctm && dis < disp2)) return false;
-    if (score) {
-        const double scr1 = __dsub_rn(1.0, __dsub_rn(ai, ctm));
-        const double scr2 = __dsub_rn(1.0, __dsub_rn(aj, ctm));
-        const double scr3 = __dmul_rn(2.0, __ddiv_rn(dis, disp2));
-        *score = __dadd_rn(__dadd_rn(scr1, scr2), scr3);
-    }
-    return true;
-}
-
-// the candidate's particles, patch numbers and potential
-struct Cand {
-    int s1, s2, o1, o2, potn, r;
+// slots, patch-vector rows and potential of the patch pair (w1, w2), w1 of the lower particle index
+struct PatchPair {
+    int s1, s2, o1, o2, potn;
 };
 
 template <class real>
-__device__ __forceinline__ Cand cand_of(const ForceArgs<real> &a, const BindState &S, int4 e) {
-    Cand c;
-    c.r = find_replica(a.tb.rep_slot, a.tb.nrep, e.x);
-    const Replica<real> &R = a.tb.reps[c.r];
-    const Model<real> &M = a.tb.models[R.model];
-    const BindRep &B = S.reps[c.r];
+__device__ __forceinline__ PatchPair patch_pair_of(const ForceArgs<real> &a, const BindRep &B, const Model<real> &M,
+                                                   int off, int w1, int w2) {
     int l1, t1, k1, l2, t2, k2;
-    patch_owner<real>(B, M, e.z - B.patch_off, l1, t1, k1);
-    patch_owner<real>(B, M, e.w - B.patch_off, l2, t2, k2);
-    c.s1 = a.buf.slot_of[e.x];
-    c.s2 = a.buf.slot_of[e.y];
-    c.o1 = M.ooff[t1] + k1;
-    c.o2 = M.ooff[t2] + k2;
-    c.potn = M.pstart[t1][t2] + k1 * M.np[t2] + k2;
-    return c;
-}
-
-template <class real>
-__global__ void __launch_bounds__(256) bind_edge_kernel(ForceArgs<real> a, BindState S) {
-    const long long n = (long long)S.ctr[0] < S.plist_cap ? (long long)S.ctr[0] : S.plist_cap;
-    const unsigned stamp = (unsigned)S.ctr[2];
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        const int4 e = S.plist[q];
-        const Cand c = cand_of<real>(a, S, e);
-        const Replica<real> &R = a.tb.reps[c.r];
-        const Model<real> &M = a.tb.models[R.model];
-        const BindRep &B = S.reps[c.r];
-        const bool b1 = S.isbound[e.z] != 0, b2 = S.isbound[e.w] != 0;
-        const bool cond1 = S.boundto[e.z] == e.w && S.boundto[e.w] == e.z;
-        const int cls = (b1 && b2) ? (cond1 ? 0 : 1) : (b1 != b2 ? 2 : 0);
-        const double disp2 = disp2_of(B.disp[c.potn], cls);
-        bool edge;
-        if (std::is_same<real, double>::value) {
-            edge = exact_edge<real>(B, a.buf, c.s1, c.s2, c.o1, c.o2, c.potn, disp2, nullptr);
-        } else {
-            // float evaluation; anything within a margin of a threshold is decided in FP64
-            Payload<real> P1, P2;
-            P1.load(a.buf.pos, a.buf.rota, a.buf.rotb, c.s1);
-            P2.load(a.buf.pos, a.buf.rota, a.buf.rotb, c.s2);
-            const real dx = min_image<real>(P1.v[0] - P2.v[0], R.box, R.l2s, R.periodic);
-            const real dy = min_image<real>(P1.v[1] - P2.v[1], R.box, R.l2s, R.periodic);
-            const real dz = min_image<real>(P1.v[2] - P2.v[2], R.box, R.l2s, R.periodic);
-            const real r2 = dx * dx + dy * dy + dz * dz;
-            int t0 = side((double)r2, B.mk2, 1e-5 * B.mk2);
-            if (t0 > 0) continue;
-            const real rr = sqrt(r2);
-            const real u[3] = {dx / rr, dy / rr, dz / rr};
-            const real *v1 = M.orient[c.o1], *v2 = M.orient[c.o2];
-            real n1[3], n2[3];
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                n1[k] = v1[0] * P1.v[3 + k] + v1[1] * P1.v[6 + k] + v1[2] * P1.v[9 + k];
-                n2[k] = v2[0] * P2.v[3 + k] + v2[1] * P2.v[6 + k] + v2[2] * P2.v[9 + k];
-            }
-            const real ci = -(n1[0] * u[0] + n1[1] * u[1] + n1[2] * u[2]);
-            const real cj = n2[0] * u[0] + n2[1] * u[1] + n2[2] * u[2];
-            const int t1 = side((double)ci, B.ctm[c.potn], 2e-5), t2 = side((double)cj, B.ctm[c.potn], 2e-5);
-            const int t3 = side((double)rr, disp2, 1e-5 * disp2);
-            if (t1 < 0 || t2 < 0 || t3 > 0) continue;
-            if (t0 < 0 && t1 > 0 && t2 > 0 && t3 < 0) edge = true;
-            else edge = exact_edge<real>(B, a.buf, c.s1, c.s2, c.o1, c.o2, c.potn, disp2, nullptr);
-        }
-        if (!edge) continue;
-        const int k1 = adj_take(S.deg, e.z, stamp, S.flags), k2 = adj_take(S.deg, e.w, stamp, S.flags);
-        const int tag = (int)(q << 2) | cls;
-        if (k1 < kAdjCap) S.adj[(size_t)e.z * kAdjCap + k1] = make_int2(e.w, tag);
-        else atomicOr(S.flags, kFlagBind);
-        if (k2 < kAdjCap) S.adj[(size_t)e.w * kAdjCap + k2] = make_int2(e.z, tag);
-        else atomicOr(S.flags, kFlagBind);
+    patch_owner<real>(B, M, w1 - B.patch_off, l1, t1, k1);
+    patch_owner<real>(B, M, w2 - B.patch_off, l2, t2, k2);
+    if (l2 < l1) {
+        int t;
+        t = l1; l1 = l2; l2 = t;
+        t = t1; t1 = t2; t2 = t;
+        t = k1; k1 = k2; k2 = t;
     }
+    PatchPair pp;
+    pp.s1 = a.buf.slot_of[off + l1];
+    pp.s2 = a.buf.slot_of[off + l2];
+    pp.o1 = M.ooff[t1] + k1;
+    pp.o2 = M.ooff[t2] + k2;
+    pp.potn = M.pstart[t1][t2] + k1 * M.np[t2] + k2;
+    return pp;
 }
 
 // ------------------------------------------------------------------ binding models
@@ -618,6 +355,8 @@ __global__ void __launch_bounds__(kLargeThreads) bind_large_kernel(ForceArgs<rea
         }
         const int r = find_replica(S.patch_slot, S.nrep, p);
         const BindRep &B = S.reps[r];
+        const Replica<real> &R = a.tb.reps[r];
+        const Model<real> &M = a.tb.models[R.model];
         const BindModel &mod = *S.model;
         for (int t = 0; t < nm; t++) break_check(S, mem[t], adj_count(S.deg, mem[t], stamp));
         // local edges (a < b) with their FP64 scores, sorted by (a, b) (RecapitulateEdges,
@@ -630,9 +369,9 @@ __global__ void __launch_bounds__(kLargeThreads) bind_large_kernel(ForceArgs<rea
                 if (ad.x < v) continue;   // each edge from its lower patch
                 int f2 = 0;
                 while (f2 < nm && mem[f2] != ad.x) f2++;
-                const Cand c = cand_of<real>(a, S, S.plist[ad.y >> 2]);
+                const PatchPair c = patch_pair_of<real>(a, B, M, R.off, v, ad.x);
                 double scr = 0;
-                exact_edge<real>(B, a.buf, c.s1, c.s2, c.o1, c.o2, c.potn, disp2_of(B.disp[c.potn], ad.y & 3), &scr);
+                exact_edge<real>(B, a.buf, c.s1, c.s2, c.o1, c.o2, c.potn, disp2_of(B.disp[c.potn], ad.y), &scr);
                 int t = ne++;
                 while (t > 0 && (ea[t - 1] > j || (ea[t - 1] == j && eb[t - 1] > f2))) {
                     ea[t] = ea[t - 1]; eb[t] = eb[t - 1]; es[t] = es[t - 1];

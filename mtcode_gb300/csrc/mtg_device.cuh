@@ -47,6 +47,31 @@ struct Replica {
     real bond_r;               // ComboPatch::max_check
 };
 
+// ------------------------------------------------------------------ single-bond-per-patch mode, per replica
+// Patch numbering (GeneralPatch, GeneralPatch.cpp:285-320) and the constants of the bond tests.  The FP64
+// values are the reference's thresholds; the float pairs bracket them by a margin far above the error of
+// a float evaluation, so that a float value outside [lo, hi] decides like the FP64 test.
+struct BindRep {
+    int patch_off, npatch;
+    int pbase[kMaxTypes + 1];     // first local patch of each type; pbase[n_types] = patches of the replica
+    int periodic;
+    uint32_t seed_lo, seed_hi;
+    double box, l2s;              // cube::l, (l/2)^2
+    double orient[kMaxOrient][3]; // body-frame patch vectors
+    double ctm[kMaxPots];         // cos(thetam) of each potential
+    double disp[kMaxPots];        // interaction_distance = 1.4 dis (potentialtheta.h:416)
+    double mk2;                   // ComboPatch::max_check^2
+    double max_dis;               // max_check + 1 (calculate_patch_list)
+    double list_cut2;             // squared pair-list cut the candidates come from (run_singlebond: 2.5 sigma)
+    double max_ang;               // ComboPatch::max_ang
+    float ctm_lo[kMaxPots], ctm_hi[kMaxPots];   // cos(thetam) -+ 2e-5
+    float disp_f[kMaxPots];                     // interaction_distance in float
+    float mk2_lo, mk2_hi;                       // max_check^2 (1 -+ 1e-5)
+    float memb2_lo, memb2_hi;                   // min(list_cut^2, (max_check + 1)^2) (1 -+ 1e-5)
+    float ang_lo, ang_hi;                       // -0.4 -+ 4e-5 for (c_i - max_ang) + (c_j - max_ang)
+    float max_ang_f;
+};
+
 // ------------------------------------------------------------------ patch model (GeneralPatch form)
 template <class real>
 struct Model {

@@ -17,7 +17,8 @@
 namespace mtg {
 namespace {  // internal linkage: every translation unit keeps its own kernels
 
-enum ForceMode : int { kModeStep = 0, kModeInit = 1, kModeForces = 2, kModeObs = 3 };
+// kModeEdges: single-bond mode, the pass that only records this update's bond candidates (edges)
+enum ForceMode : int { kModeStep = 0, kModeInit = 1, kModeForces = 2, kModeObs = 3, kModeEdges = 4 };
 
 template <class real>
 struct Buffers {
@@ -29,6 +30,8 @@ struct Buffers {
                            // kept only when bonds are set)
     real *xref;            // skin lists: position of each slot at the last list build (4 reals), shared
     int *home_cell;        // skin lists: cell of each slot at the last list build, shared
+    real *snap_a, *snap_b, *snap_c;  // single-bond mode: position and rotation at the last candidate-list
+                                     // build, laid out like pos / rota / rotb and carried with the particle
 };
 
 // Skin-list state (int[4], device): [0] this step rebuilds, [1] a particle will have moved more than half
@@ -293,7 +296,8 @@ __device__ __forceinline__ void advance_particle(const Replica<real> &R, Payload
 template <class real, bool MOVE>
 __global__ void __launch_bounds__(256) scatter_kernel(Tables<real> tb, Buffers<real> in, Buffers<real> out,
                                                       const int2 *bin, const int *start, unsigned *flags,
-                                                      const int *gate = nullptr) {
+                                                      const int *gate = nullptr,
+                                                      const unsigned long long *snap_due = nullptr) {
     if (gated_off(gate, 1)) return;
     // every particle must have been binned exactly once; otherwise nothing is moved (latched error)
     if (__ldg(start + tb.ncells) != tb.ntot) {
@@ -312,6 +316,18 @@ __global__ void __launch_bounds__(256) scatter_kernel(Tables<real> tb, Buffers<r
         P.load(in.pos, in.rota, in.rotb, s);
         M.load(in.motion + (size_t)s * kRow);
         const int id = in.ident[s];
+        if (out.snap_a) {
+            // single-bond mode: the candidate list is built from the positions at the start of the step
+            // (calculate_patch_list before advancemom_halfstep, Condensate.cpp:464-475); otherwise the
+            // particle carries its snapshot along
+            if (snap_due && *snap_due) {
+                P.store(out.snap_a, out.snap_b, out.snap_c, d);
+            } else {
+                Payload<real> S;
+                S.load(in.snap_a, in.snap_b, in.snap_c, s);
+                S.store(out.snap_a, out.snap_b, out.snap_c, d);
+            }
+        }
         if (MOVE) {
             const int r = find_replica(tb.rep_slot, tb.nrep, s);
             const Replica<real> R = tb.reps[r];
@@ -410,23 +426,6 @@ __global__ void __launch_bounds__(256) copy_back_kernel(int ntot, Buffers<real> 
 
 // ------------------------------------------------------------------ force + Langevin epilogue
 
-// per replica: patch numbering (GeneralPatch, GeneralPatch.cpp:285-320) and the FP64 constants of the tests
-struct BindRep {
-    int patch_off, npatch;
-    int pbase[kMaxTypes + 1];     // first local patch of each type; pbase[n_types] = patches of the replica
-    int reach;                    // candidate stencil half-width in force-grid cells
-    int periodic;
-    uint32_t seed_lo, seed_hi;
-    double box, l2s;              // cube::l, (l/2)^2
-    double orient[kMaxOrient][3]; // body-frame patch vectors
-    double ctm[kMaxPots];         // cos(thetam) of each potential
-    double disp[kMaxPots];        // interaction_distance = 1.4 dis (potentialtheta.h:416)
-    double mk2;                   // ComboPatch::max_check^2
-    double max_dis;               // max_check + 1 (calculate_patch_list)
-    double list_cut2;             // squared pair-list cut the candidates come from (run_singlebond: 2.5 sigma)
-    double max_ang;               // ComboPatch::max_ang
-};
-
 // ------------------------------------------------------------------ patch numbering
 template <class real>
 __device__ __forceinline__ int patch_of(const BindRep &B, const Model<real> &M, int li, int t, int c) {
@@ -469,11 +468,225 @@ struct ForceArgs {
     int *skin_next;
     unsigned *list;
     int *list_n;
-    // single-bond-per-patch mode (null otherwise): patch numbering per replica, bond state by global patch
+    // single-bond-per-patch mode (null otherwise): patch numbering per replica, bond state by global patch;
+    // on a pass that decides bonds also this update's adjacency (stamped counters, kAdjCap partners per
+    // patch) and the update counters (stamp = bind_ctr[2])
     const BindRep *bind_reps;
     const unsigned char *bind_on;
     const int *bind_to;
+    unsigned long long *bind_deg;
+    int2 *bind_adj;
+    const unsigned long long *bind_ctr;
 };
+
+// ------------------------------------------------------------------ single-bond mode: bond candidates
+// The edges of LangevinNVTR::calculate_forces_and_torques3D_onlyone_nonlets (LangevinRforce.cpp:2900-3090):
+// a patch pair (p1 < p2) is an edge when it is on the candidate list of the last list build
+// (calculate_patch_list, LangevinR.cpp:1702-1852) and now |x1 - x2|^2 < max_check^2, both cones hold
+// (c_i, c_j > cos thetam) and |x1 - x2| < disp2, the bind-state dependent range.  The list itself is not
+// stored: every particle carries its position and rotation of the list build (the snapshot), and a patch
+// pair that passes the current test is checked against the list's condition on the snapshot.  Every test is
+// the reference's FP64 expression in its operation order; float evaluations decide only outside a margin.
+constexpr int kAdjCap = 8;            // candidate partners of one patch in one update
+constexpr unsigned kFlagBind = 0x20u; // a capacity of this mode was exceeded (MTG_FLAG_BIND)
+
+// cube::distance_vector (geometry.h:277-294): un = x_a - x_b (minimum image), returns |un|^2
+__device__ __forceinline__ double exact_dist_vec(const BindRep &B, const double xa[3], const double xb[3], double un[3]) {
+    double temp = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        double as = __dsub_rn(xa[k], xb[k]);
+        if (B.periodic && __dmul_rn(as, as) > B.l2s) as = as >= 0.0 ? __dsub_rn(as, B.box) : __dadd_rn(as, B.box);
+        temp = __dadd_rn(temp, __dmul_rn(as, as));
+        un[k] = as;
+    }
+    return temp;
+}
+
+// Q^T n_b (LangevinRforce.cpp:2980-2985) then -(n . u) or (n . u)
+__device__ __forceinline__ double exact_cos(const double nb[3], const double q[9], const double u[3], bool negate) {
+    double n[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        n[k] = __dadd_rn(__dadd_rn(__dmul_rn(nb[0], q[k]), __dmul_rn(nb[1], q[3 + k])), __dmul_rn(nb[2], q[6 + k]));
+    const double d = __dadd_rn(__dadd_rn(__dmul_rn(n[0], u[0]), __dmul_rn(n[1], u[1])), __dmul_rn(n[2], u[2]));
+    return negate ? -d : d;
+}
+
+// position and rotation of slot s of a (pos, rota, rotb)-shaped triple as doubles (exact conversions)
+template <class real>
+__device__ __forceinline__ void load_state_d(const real *pa, const real *pb, const real *pc, int s, double x[3],
+                                             double q[9]) {
+    Payload<real> P;
+    P.load(pa, pb, pc, s);
+#pragma unroll
+    for (int k = 0; k < 3; k++) x[k] = (double)P.v[k];
+#pragma unroll
+    for (int k = 0; k < 9; k++) q[k] = (double)P.v[3 + k];
+}
+
+// value against a bracketed threshold: +1 certainly above, -1 certainly below, 0 inside the margin
+template <class T>
+__device__ __forceinline__ int side_of(T v, float lo, float hi) {
+    return v > (T)hi ? 1 : (v < (T)lo ? -1 : 0);
+}
+
+// the reference's bind-state dependent range (LangevinRforce.cpp:3010-3030): class 0 disp (neither or both
+// bound to each other), 1 0.5 disp (both bound elsewhere), 2 0.7 disp (exactly one bound)
+__device__ __forceinline__ int range_class(const int *boundto, const unsigned char *isbound, int w1, int w2) {
+    const bool b1 = isbound[w1] != 0, b2 = isbound[w2] != 0;
+    const bool cond1 = boundto[w1] == w2 && boundto[w2] == w1;
+    return (b1 && b2) ? (cond1 ? 0 : 1) : (b1 != b2 ? 2 : 0);
+}
+__device__ __forceinline__ double disp2_of(double disp, int cls) {
+    return cls == 1 ? __dmul_rn(0.5, disp) : (cls == 2 ? __dmul_rn(0.7, disp) : disp);
+}
+
+// FP64 edge test of the current state; with score != null also the edge's score (LangevinRforce.cpp:3040-3060)
+template <class real>
+__device__ __noinline__ bool exact_edge(const BindRep &B, const Buffers<real> &b, int s1, int s2, int o1, int o2,
+                                        int potn, double disp2, double *score) {
+    double xa[3], qa[9], xb[3], qb[9], un[3];
+    load_state_d<real>(b.pos, b.rota, b.rotb, s1, xa, qa);
+    load_state_d<real>(b.pos, b.rota, b.rotb, s2, xb, qb);
+    double dis = exact_dist_vec(B, xa, xb, un);
+    if (!(dis < B.mk2)) return false;
+    dis = __dsqrt_rn(dis);
+    un[0] = __ddiv_rn(un[0], dis); un[1] = __ddiv_rn(un[1], dis); un[2] = __ddiv_rn(un[2], dis);
+    const double ai = exact_cos(B.orient[o1], qa, un, true), aj = exact_cos(B.orient[o2], qb, un, false);
+    const double ctm = B.ctm[potn];
+    if (!(ai > ctm && aj > ctm && dis < disp2)) return false;
+    if (score) {
+        const double scr1 = __dsub_rn(1.0, __dsub_rn(ai, ctm));
+        const double scr2 = __dsub_rn(1.0, __dsub_rn(aj, ctm));
+        const double scr3 = __dmul_rn(2.0, __ddiv_rn(dis, disp2));
+        *score = __dadd_rn(__dadd_rn(scr1, scr2), scr3);
+    }
+    return true;
+}
+
+// FP64 candidate-list condition on the snapshot: distance < the list cut and < max_check + 1, and
+// (c_i - max_ang) + (c_j - max_ang) > -0.4 (LangevinR.cpp:1722-1800)
+template <class real>
+__device__ __noinline__ bool exact_member(const BindRep &B, const Buffers<real> &b, int s1, int s2, int o1, int o2) {
+    double xa[3], qa[9], xb[3], qb[9], un[3];
+    load_state_d<real>(b.snap_a, b.snap_b, b.snap_c, s1, xa, qa);
+    load_state_d<real>(b.snap_a, b.snap_b, b.snap_c, s2, xb, qb);
+    const double d2 = exact_dist_vec(B, xa, xb, un);
+    if (!(d2 < B.list_cut2)) return false;
+    const double dis = __dsqrt_rn(d2);
+    if (!(dis < B.max_dis)) return false;
+    un[0] = __ddiv_rn(un[0], dis); un[1] = __ddiv_rn(un[1], dis); un[2] = __ddiv_rn(un[2], dis);
+    const double ai = exact_cos(B.orient[o1], qa, un, true), aj = exact_cos(B.orient[o2], qb, un, false);
+    return __dadd_rn(__dsub_rn(ai, B.max_ang), __dsub_rn(aj, B.max_ang)) > -0.4;
+}
+
+template <class real>
+__device__ __forceinline__ bool candidate(const BindRep &B, const Replica<real> &R, const Model<real> &M,
+                                          const Buffers<real> &b, int s1, int s2, int o1, int o2) {
+    if (std::is_same<real, double>::value) return exact_member<real>(B, b, s1, s2, o1, o2);
+    Payload<real> A, C;
+    A.load(b.snap_a, b.snap_b, b.snap_c, s1);
+    C.load(b.snap_a, b.snap_b, b.snap_c, s2);
+    const real dx = min_image<real>(A.v[0] - C.v[0], R.box, R.l2s, R.periodic);
+    const real dy = min_image<real>(A.v[1] - C.v[1], R.box, R.l2s, R.periodic);
+    const real dz = min_image<real>(A.v[2] - C.v[2], R.box, R.l2s, R.periodic);
+    const real r2 = dx * dx + dy * dy + dz * dz;
+    const int t = side_of<real>(r2, B.memb2_lo, B.memb2_hi);
+    if (t > 0) return false;
+    if (t == 0) return exact_member<real>(B, b, s1, s2, o1, o2);
+    const real rr = sqrt(r2), u[3] = {dx / rr, dy / rr, dz / rr};
+    const real *v1 = M.orient[o1], *v2 = M.orient[o2];
+    real ci = 0, cj = 0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        ci -= (v1[0] * A.v[3 + k] + v1[1] * A.v[6 + k] + v1[2] * A.v[9 + k]) * u[k];
+        cj += (v2[0] * C.v[3 + k] + v2[1] * C.v[6 + k] + v2[2] * C.v[9 + k]) * u[k];
+    }
+    const int w = side_of<real>((ci - (real)B.max_ang_f) + (cj - (real)B.max_ang_f), B.ang_lo, B.ang_hi);
+    return w == 0 ? exact_member<real>(B, b, s1, s2, o1, o2) : w > 0;
+}
+
+// slot of this update's adjacency for patch p (stamped counter: a stale stamp counts as zero edges)
+__device__ __forceinline__ int adj_take(unsigned long long *deg, int p, unsigned stamp, unsigned *flags) {
+    unsigned long long old = deg[p];
+    for (int it = 0; it < (1 << 20); it++) {
+        const unsigned cnt = (unsigned)(old >> 32) == stamp ? (unsigned)old : 0u;
+        const unsigned long long nw = ((unsigned long long)stamp << 32) | (unsigned long long)(cnt + 1u);
+        const unsigned long long prev = atomicCAS(deg + p, old, nw);
+        if (prev == old) return (int)cnt;
+        old = prev;
+    }
+    atomicOr(flags, kFlagBind);
+    return kAdjCap;
+}
+
+template <class real>
+__device__ __forceinline__ void add_edge_t(unsigned long long *deg, int2 *adj, unsigned *flags, int w1, int w2,
+                                           int cls, unsigned stamp) {
+    const int k1 = adj_take(deg, w1, stamp, flags), k2 = adj_take(deg, w2, stamp, flags);
+    if (k1 < kAdjCap) adj[(size_t)w1 * kAdjCap + k1] = make_int2(w2, cls);
+    else atomicOr(flags, kFlagBind);
+    if (k2 < kAdjCap) adj[(size_t)w2 * kAdjCap + k2] = make_int2(w1, cls);
+    else atomicOr(flags, kFlagBind);
+}
+
+// Every edge of the particle pair (s1, s2), s1 the lower particle index, d = x1 - x2 (minimum image) and
+// r2 = |d|^2 as the caller's pair loop computed them.  Called once per pair on a bond-deciding pass.
+template <class real>
+__device__ __noinline__ void bind_pair_edges(const ForceArgs<real> &a, const Replica<real> &R, const Model<real> &M,
+                                             int r, int s1, int s2, int li1, int li2, const real d[3], real r2) {
+    const BindRep &B = a.bind_reps[r];
+    const int t0 = side_of<real>(r2, B.mk2_lo, B.mk2_hi);
+    if (t0 > 0) return;
+    const int ty1 = type_of<real>(M, li1), ty2 = type_of<real>(M, li2), na = M.np[ty1], nb = M.np[ty2];
+    if (na == 0 || nb == 0) return;
+    const real rr = sqrt(r2), u[3] = {d[0] / rr, d[1] / rr, d[2] / rr};
+    Payload<real> P1;
+    P1.load(a.buf.pos, a.buf.rota, a.buf.rotb, s1);
+    real w1[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) w1[k] = P1.v[3 + 3 * k] * u[0] + P1.v[4 + 3 * k] * u[1] + P1.v[5 + 3 * k] * u[2];
+    // particle 1's cones first: most pairs have no patch of it near any cone
+    const real pre = (real)M.mincos[ty1][ty2] - (real)4e-5;
+    const int o1 = M.ooff[ty1], o2 = M.ooff[ty2];
+    real c1[kMaxOrient];
+    bool any = false;
+    for (int ka = 0; ka < na; ka++) {
+        const real *v = M.orient[o1 + ka];
+        c1[ka] = -(v[0] * w1[0] + v[1] * w1[1] + v[2] * w1[2]);
+        any |= c1[ka] > pre;
+    }
+    if (!any) return;
+    Payload<real> P2;
+    P2.load(a.buf.pos, a.buf.rota, a.buf.rotb, s2);
+    real w2[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) w2[k] = P2.v[3 + 3 * k] * u[0] + P2.v[4 + 3 * k] * u[1] + P2.v[5 + 3 * k] * u[2];
+    const unsigned stamp = (unsigned)a.bind_ctr[2];
+    const bool fp64 = std::is_same<real, double>::value;
+    const int ps = M.pstart[ty1][ty2];
+    for (int ka = 0; ka < na; ka++) {
+        if (!(c1[ka] > pre)) continue;
+        for (int kb = 0; kb < nb; kb++) {
+            const real *v = M.orient[o2 + kb];
+            const real c2 = v[0] * w2[0] + v[1] * w2[1] + v[2] * w2[2];
+            const int q = ps + ka * nb + kb;
+            const int e1 = side_of<real>(c1[ka], B.ctm_lo[q], B.ctm_hi[q]), e2 = side_of<real>(c2, B.ctm_lo[q], B.ctm_hi[q]);
+            if (e1 < 0 || e2 < 0) continue;
+            const int wp1 = patch_of<real>(B, M, li1, ty1, ka), wp2 = patch_of<real>(B, M, li2, ty2, kb);
+            const int cls = range_class(a.bind_to, a.bind_on, wp1, wp2);
+            const float dfl = cls == 1 ? 0.5f * B.disp_f[q] : (cls == 2 ? 0.7f * B.disp_f[q] : B.disp_f[q]);
+            const int e3 = side_of<real>(rr, dfl * (1.f - 1e-5f), dfl * (1.f + 1e-5f));
+            if (e3 > 0) continue;
+            const bool sure = !fp64 && t0 < 0 && e1 > 0 && e2 > 0 && e3 < 0;
+            if (!sure && !exact_edge<real>(B, a.buf, s1, s2, o1 + ka, o2 + kb, q, disp2_of(B.disp[q], cls), nullptr))
+                continue;
+            if (!candidate<real>(B, R, M, a.buf, s1, s2, o1 + ka, o2 + kb)) continue;
+            add_edge_t<real>(a.bind_deg, a.bind_adj, a.flags, wp1, wp2, cls, stamp);
+        }
+    }
+}
 
 // skin lists: flags the next step for a rebuild when slot s's next position (xn) is more than half the
 // skin away from where it was at the last build (minimum image)
@@ -663,6 +876,14 @@ __device__ __noinline__ void simple_particle(const ForceArgs<real> &a, int s) {
                         real dz2 = min_image<real>(zi - zj, R.box, R.l2s, R.periodic);
                         real r2 = dx * dx + dy2 * dy2 + dz2 * dz2;
                         if (!(r2 < range2)) continue;
+                        if (MODE == kModeEdges) {   // single-bond mode: this update's edges, each pair once
+                            const int idj = __ldg(a.buf.ident + j);
+                            if (idi < idj) {
+                                const real dd[3] = {dx, dy2, dz2};
+                                bind_pair_edges<real>(a, R, Mo, r, s, j, li, idj - R.off, dd, r2);
+                            }
+                            continue;
+                        }
                         const real rr = sqrt(r2);
                         if (r2 < R.rc2) npairs++;
                         // WCA core: same vector for both orientations of the pair
@@ -711,6 +932,7 @@ __device__ __noinline__ void simple_particle(const ForceArgs<real> &a, int s) {
                 }
             }
         }
+        if (MODE == kModeEdges) return;
         real ebond = real(0);
         if (a.bond_start && MODE != kModeObs) {
             real fb[3] = {real(0), real(0), real(0)};

@@ -168,7 +168,9 @@ __device__ __forceinline__ void fixed_add(long long *acc, float v) {
     if (v != 0.f) atomicAdd(reinterpret_cast<unsigned long long *>(acc), (unsigned long long)to_fixed(v));
 }
 
-// forces and torques of the listed pairs into acc (6 fixed-point sums per slot: F lab, T lab)
+// forces and torques of the listed pairs into acc (6 fixed-point sums per slot: F lab, T lab); with BIND
+// (single-bond mode, a bond-deciding pass) also this update's bond candidates of every pair
+template <bool BIND>
 __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<float> a, const int2 *pairs,
                                                                  const unsigned long long *npairs, long long cap,
                                                                  long long *acc) {
@@ -195,6 +197,16 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
             fa[0] = s_ * d[0];
             fa[1] = s_ * d[1];
             fa[2] = s_ * d[2];
+        }
+        if (BIND) {
+            const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
+            const Model<float> &M = a.tb.models[R.model];
+            if (ida < idb) {
+                bind_pair_edges<float>(a, R, M, r, sa, sb, ida - R.off, idb - R.off, d, r2);
+            } else {
+                const float dn[3] = {-d[0], -d[1], -d[2]};
+                bind_pair_edges<float>(a, R, M, r, sb, sa, idb - R.off, ida - R.off, dn, r2);
+            }
         }
         if (r2 < R.patch_r2) {
             const Model<float> &M = a.tb.models[R.model];

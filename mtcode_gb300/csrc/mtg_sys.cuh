@@ -250,8 +250,7 @@ struct Sys : SysBase {
     mtg::BindRep *d_brep = nullptr;
     mtg::BindModel *d_bmodel = nullptr;
     int *d_patch_slot = nullptr, *d_boundto = nullptr, *d_large = nullptr, *d_scratch = nullptr;
-    int4 *d_plist = nullptr;
-    long long plist_cap = 0;
+    int ncells_full = 0;                         // the force grid's cells outside single-bond mode
     unsigned long long *d_bctr = nullptr, *d_deg = nullptr;
     int2 *d_adj = nullptr;
     unsigned char *d_isbound = nullptr;
@@ -476,7 +475,7 @@ struct Sys : SysBase {
     }
 
     // ---------------------------------------------------------------- single-bond-per-patch mode
-    static constexpr int kBindLaunches = 5;   // begin, candidates, edges, decide, large
+    static constexpr int kBindLaunches = 4;   // begin (+ snapshot or edges-only pass), decide, large
 
     mtg::BindState bind_state() const {
         mtg::BindState S;
@@ -487,8 +486,6 @@ struct Sys : SysBase {
         S.nrep = nrep;
         S.ptot = ptot;
         S.patch_every = patch_every;
-        S.plist = d_plist;
-        S.plist_cap = plist_cap;
         S.ctr = d_bctr;
         S.deg = d_deg;
         S.adj = d_adj;
@@ -502,30 +499,32 @@ struct Sys : SysBase {
         return S;
     }
 
-    // this update's stamp and, when due (or forced), the candidate list from buffer b, whose cells the
-    // current cell starts describe
+    // this update's stamp and whether the candidate list is due; a forced list (a pass that does not move
+    // the particles) takes its snapshot from buffer b at once, a step's from the scatter
     void enqueue_bind_begin(int b, int force, int advance) {
-        const mtg::BindState S = bind_state();
-        mtg::bind_begin_kernel<<<1, 32, 0, st>>>(S, force, advance);
-        const int g = std::max(1, (ntot_ + 255) / 256);
-        mtg::bind_candidates_kernel<real><<<g, 256, 0, st>>>(force_args(b, 0), S);
+        mtg::bind_begin_kernel<<<1, 32, 0, st>>>(bind_state(), force, advance);
+        if (force) {
+            const int g = grid_for(ntot_, 256, occ_stream, sms);
+            mtg::bind_snapshot_kernel<real><<<g, 256, 0, st>>>(ntot_, buf[b]);
+        }
     }
 
-    // edges, clusters and bond decisions on buffer b (positions reached through slot_of)
-    void enqueue_bind_decide(int b) {
+    // clusters and bond decisions from this update's edges (positions reached through slot_of)
+    void enqueue_bind_decide(const mtg::ForceArgs<real> &a) {
         const mtg::BindState S = bind_state();
-        const mtg::ForceArgs<real> a = force_args(b, 0);
-        mtg::bind_edge_kernel<real><<<sms * 8, 256, 0, st>>>(a, S);
         mtg::bind_decide_kernel<<<std::max(1, (ptot + 255) / 256), 256, 0, st>>>(S);
         mtg::bind_large_kernel<real><<<scratch_threads / mtg::kLargeThreads, mtg::kLargeThreads, 0, st>>>(a, S);
     }
 
     void free_bind() {
         cudaFree(d_brep); cudaFree(d_bmodel); cudaFree(d_patch_slot); cudaFree(d_boundto); cudaFree(d_large);
-        cudaFree(d_scratch); cudaFree(d_plist); cudaFree(d_bctr); cudaFree(d_deg); cudaFree(d_adj);
-        cudaFree(d_isbound);
+        cudaFree(d_scratch); cudaFree(d_bctr); cudaFree(d_deg); cudaFree(d_adj); cudaFree(d_isbound);
         d_brep = nullptr; d_bmodel = nullptr; d_patch_slot = d_boundto = d_large = d_scratch = nullptr;
-        d_plist = nullptr; d_bctr = d_deg = nullptr; d_adj = nullptr; d_isbound = nullptr;
+        d_bctr = d_deg = nullptr; d_adj = nullptr; d_isbound = nullptr;
+        for (int b = 0; b < 2; b++) {
+            cudaFree(buf[b].snap_a); cudaFree(buf[b].snap_b); cudaFree(buf[b].snap_c);
+            buf[b].snap_a = buf[b].snap_b = buf[b].snap_c = nullptr;
+        }
     }
 
     void drop_graphs() {
@@ -555,8 +554,10 @@ struct Sys : SysBase {
             free_bind();
             single_bond = false;
             reps = reps_full;
+            ncells = ncells_full;
             MTG_CUDA(cudaMemcpy(d_reps, reps.data(), sizeof(mtg::Replica<real>) * nrep, cudaMemcpyHostToDevice));
             forces_ready = false;
+            cells_valid = bins_valid = false;
             return;
         }
         MTG_REQUIRE(skin <= 0, "mtg_set_single_bond: not available with a neighbour skin");
@@ -609,10 +610,20 @@ struct Sys : SysBase {
             B.max_dis = mc + 1.;
             B.list_cut2 = sb->list_cut * sb->list_cut;
             B.max_ang = std::isnan(sb->max_ang) ? ma : sb->max_ang;
-            const double side = d.box / reps[r].nc, range = std::min(sb->list_cut, mc + 1.);
-            B.reach = std::max(1, (int)std::ceil(range / side));
-            MTG_REQUIRE(B.reach <= 2 || reps[r].nc <= 4,
-                        "mtg_set_single_bond: the candidate range spans more than two force-grid cells");
+            for (int q = 0; q < npots; q++) {
+                B.ctm_lo[q] = (float)(B.ctm[q] - 2e-5);
+                B.ctm_hi[q] = (float)(B.ctm[q] + 2e-5);
+                B.disp_f[q] = (float)B.disp[q];
+            }
+            const double memb2 = std::min(B.list_cut2, B.max_dis * B.max_dis);
+            B.mk2_lo = (float)(B.mk2 * (1 - 1e-5));
+            B.mk2_hi = (float)(B.mk2 * (1 + 1e-5));
+            B.memb2_lo = (float)(memb2 * (1 - 1e-5));
+            B.memb2_hi = (float)(memb2 * (1 + 1e-5));
+            B.ang_lo = (float)(-0.4 - 4e-5);
+            B.ang_hi = (float)(-0.4 + 4e-5);
+            B.max_ang_f = (float)B.max_ang;
+            MTG_REQUIRE(reps_obs[r].nc >= 1, "mtg_set_single_bond: no cell grid");
             poff += base;
             MTG_REQUIRE(poff < (int64_t)INT32_MAX, "mtg_set_single_bond: too many patches");
             pslot.push_back((int)poff);
@@ -632,14 +643,18 @@ struct Sys : SysBase {
         patch_every = sb->patch_every;
         patch_slot = pslot;
         const size_t np = (size_t)std::max(ptot, 1);
-        plist_cap = std::min<long long>((1LL << 29) - 1, 64LL * std::max(ntot_, 1) + 1024);
         scratch_threads = std::max(1, sms) * 8;
         scratch_threads = (scratch_threads + mtg::kLargeThreads - 1) / mtg::kLargeThreads * mtg::kLargeThreads;
         MTG_CUDA(cudaMalloc(&d_brep, sizeof(mtg::BindRep) * nrep));
         MTG_CUDA(cudaMalloc(&d_bmodel, sizeof(mtg::BindModel)));
         MTG_CUDA(cudaMalloc(&d_patch_slot, sizeof(int) * (nrep + 1)));
-        MTG_CUDA(cudaMalloc(&d_plist, sizeof(int4) * (size_t)plist_cap));
         MTG_CUDA(cudaMalloc(&d_bctr, sizeof(unsigned long long) * 8));
+        const size_t nn = (size_t)std::max(ntot_, 1);
+        for (int b = 0; b < 2; b++) {
+            MTG_CUDA(cudaMalloc(&buf[b].snap_a, sizeof(real) * 4 * nn));
+            MTG_CUDA(cudaMalloc(&buf[b].snap_b, sizeof(real) * 4 * nn));
+            MTG_CUDA(cudaMalloc(&buf[b].snap_c, sizeof(real) * 4 * nn));
+        }
         MTG_CUDA(cudaMalloc(&d_deg, sizeof(unsigned long long) * np));
         MTG_CUDA(cudaMalloc(&d_adj, sizeof(int2) * mtg::kAdjCap * np));
         MTG_CUDA(cudaMalloc(&d_boundto, sizeof(int) * np));
@@ -654,18 +669,27 @@ struct Sys : SysBase {
         MTG_CUDA(cudaMemset(d_boundto, 0, sizeof(int) * np));
         MTG_CUDA(cudaMemset(d_isbound, 0, np));
         ensure_slot_of();
-        // the force pass keeps the WCA core only: no pair reaches the patch term, and the pair range
-        // shrinks to the WCA range (padded so that no rounding of r^2 against r drops a core pair)
-        if (!single_bond) reps_full = reps;
+        // the force pass keeps the WCA core and no patch term; its pair loop reaches max_check, where edges
+        // can form, on the grid of the observable pass (cells >= max(force range, max_check))
+        if (!single_bond) {
+            reps_full = reps;
+            ncells_full = ncells;
+        }
         reps = reps_full;
         for (int r = 0; r < nrep; r++) {
             const double hs = 1.12246 * desc[r].hs_sigma * (1 + 1e-6);
+            const double mk2 = br[(size_t)r].mk2 * (1 + 1e-5);
             reps[r].patch_r2 = (real)0;
-            reps[r].rc2 = (real)(hs * hs);
+            reps[r].rc2 = (real)std::max(hs * hs, mk2);
+            reps[r].nc = reps_obs[r].nc;
+            reps[r].cell_off = reps_obs[r].cell_off;
+            reps[r].cell_scale = reps_obs[r].cell_scale;
         }
+        ncells = ncells_obs;
         MTG_CUDA(cudaMemcpy(d_reps, reps.data(), sizeof(mtg::Replica<real>) * nrep, cudaMemcpyHostToDevice));
         single_bond = true;
         forces_ready = false;
+        cells_valid = bins_valid = false;
         MTG_CUDA(cudaStreamSynchronize(st));
     }
 
@@ -716,15 +740,13 @@ struct Sys : SysBase {
         if (!cells_valid) rebuild_cells(false);
         tick_draw();
         enqueue_bind_begin(cur, 1, 0);
-        enqueue_bind_decide(cur);
-        check_launch();
         nlaunch += kBindLaunches;
         size_t n = (size_t)ntot_;
         double *sF = d_stage, *sT = sF + 3 * n;
         mtg::ForceArgs<real> a = force_args(cur, 0);
         a.outF = sF;
         a.outT = sT;
-        launch_force<mtg::kModeForces>(a);
+        launch_force<mtg::kModeForces>(a, true);
         check_launch();
         nlaunch += 1;
         if (F) MTG_CUDA(cudaMemcpyAsync(F, sF, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
@@ -732,9 +754,23 @@ struct Sys : SysBase {
         MTG_CUDA(cudaStreamSynchronize(st));
     }
 
-    // force pass in the given mode: the FP32 tile kernel where it applies, else the per-particle kernel
+    // force pass in the given mode: the FP32 tile kernel where it applies, else the per-particle kernel.
+    // In single-bond mode a bond-deciding pass (bind) records this update's edges in its pair loop and runs
+    // the bond decisions before the forces of the bound pairs are summed (events: around the decisions).
     template <int MODE>
-    void launch_force(const mtg::ForceArgs<real> &a) {
+    void launch_force(const mtg::ForceArgs<real> &a0, bool bind = false, cudaEvent_t *bind_ev = nullptr) {
+        mtg::ForceArgs<real> a = a0;
+        bind = bind && single_bond;
+        if (bind) {
+            a.bind_deg = d_deg;
+            a.bind_adj = d_adj;
+            a.bind_ctr = d_bctr;
+        }
+        auto decide = [&]() {
+            if (bind_ev) MTG_CUDA(cudaEventRecord(bind_ev[0], st));
+            enqueue_bind_decide(a);
+            if (bind_ev) MTG_CUDA(cudaEventRecord(bind_ev[1], st));
+        };
         if constexpr (std::is_same<real, float>::value) {
             if (use_pipe && MODE != mtg::kModeObs && !a.outE) {
                 // with a skin the list is rebuilt only on rebuild steps (the gate); the force and epilogue
@@ -744,7 +780,12 @@ struct Sys : SysBase {
                 const int gb = (ntot_ + mtg::kPipeThreads - 1) / mtg::kPipeThreads;
                 mtg::pairfind_kernel<<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap,
                                                                                   skin > 0 ? 1 : 0, gate);
-                mtg::pairforce_kernel<<<sms * 16, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap, d_acc);
+                if (bind) {
+                    mtg::pairforce_kernel<true><<<sms * 16, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap, d_acc);
+                    decide();
+                } else {
+                    mtg::pairforce_kernel<false><<<sms * 16, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap, d_acc);
+                }
                 mtg::pair_epilogue_kernel<MODE><<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_acc);
                 return;
             }
@@ -755,6 +796,11 @@ struct Sys : SysBase {
             }
         }
         const int gf = grid_for(ntot_, 128, occ_force, sms);
+        if (bind) {   // the per-particle form: an edges-only pass, the decisions, then the force pass
+            mtg::force_kernel<real, mtg::kModeEdges><<<gf, 128, 0, st>>>(a);
+            decide();
+            a.bind_deg = nullptr;
+        }
         mtg::force_kernel<real, MODE><<<gf, 128, 0, st>>>(a);
     }
 
@@ -809,14 +855,14 @@ struct Sys : SysBase {
             return;
         }
         mtg::Tables<real> tb = tables();
-        if (single_bond) enqueue_bind_begin(b, 0, 1);   // candidates from the positions at the step's start
+        if (single_bond) enqueue_bind_begin(b, 0, 1);
         scan(ncells, true);
         const int g = grid_for(ntot_, 256, occ_stream, sms);
-        mtg::scatter_kernel<real, true><<<g, 256, 0, st>>>(tb, buf[b], buf[b ^ 1], d_bin, d_start, d_flags);
-        if (single_bond) enqueue_bind_decide(b ^ 1);
+        mtg::scatter_kernel<real, true><<<g, 256, 0, st>>>(tb, buf[b], buf[b ^ 1], d_bin, d_start, d_flags, nullptr,
+                                                           single_bond ? d_bctr + 4 : nullptr);
         mtg::ForceArgs<real> a = force_args(b ^ 1, 1);
         a.ext_noise = ext_noise;
-        launch_force<mtg::kModeStep>(a);
+        launch_force<mtg::kModeStep>(a, true);
         check_launch();
     }
 
@@ -899,12 +945,11 @@ struct Sys : SysBase {
         }
         if (single_bond) {   // run_singlebond's first onlyone_nonlets call (Condensate.cpp:455-460)
             enqueue_bind_begin(cur, 1, 0);
-            enqueue_bind_decide(cur);
             nlaunch += kBindLaunches;
         }
         mtg::ForceArgs<real> a = force_args(cur, 0);
         if (noise) a.ext_noise = upload_noise(noise);
-        launch_force<mtg::kModeInit>(a);
+        launch_force<mtg::kModeInit>(a, true);
         check_launch();
         nlaunch += 1;
         cells_valid = true;
@@ -1063,6 +1108,8 @@ struct Sys : SysBase {
             MTG_CUDA(cudaEventRecord(ev[6], st));
             if (single_bond) enqueue_bind_begin(b, 0, 1);
             MTG_CUDA(cudaEventRecord(ev[7], st));
+            MTG_CUDA(cudaEventRecord(ev[8], st));
+            MTG_CUDA(cudaEventRecord(ev[9], st));
             MTG_CUDA(cudaEventRecord(ev[0], st));
             mtg::scan_reduce_kernel<<<nblk, mtg::kScanThreads, 0, st>>>(d_count, ncells, d_block);
             MTG_CUDA(cudaEventRecord(ev[1], st));
@@ -1070,25 +1117,23 @@ struct Sys : SysBase {
             MTG_CUDA(cudaEventRecord(ev[2], st));
             mtg::scan_down_kernel<<<nblk, mtg::kScanThreads, 0, st>>>(d_count, ncells, d_block, d_start);
             MTG_CUDA(cudaEventRecord(ev[3], st));
-            mtg::scatter_kernel<real, true><<<g, 256, 0, st>>>(tb, buf[b], buf[b ^ 1], d_bin, d_start, d_flags);
-            MTG_CUDA(cudaEventRecord(ev[8], st));
-            if (single_bond) enqueue_bind_decide(b ^ 1);
-            MTG_CUDA(cudaEventRecord(ev[9], st));
+            mtg::scatter_kernel<real, true><<<g, 256, 0, st>>>(tb, buf[b], buf[b ^ 1], d_bin, d_start, d_flags,
+                                                               nullptr, single_bond ? d_bctr + 4 : nullptr);
             MTG_CUDA(cudaEventRecord(ev[4], st));
             mtg::ForceArgs<real> a = force_args(b ^ 1, 1);
-            launch_force<mtg::kModeStep>(a);
+            launch_force<mtg::kModeStep>(a, true, ev + 8);
             MTG_CUDA(cudaEventRecord(ev[5], st));
             check_launch();
             MTG_CUDA(cudaEventSynchronize(ev[5]));
-            float ms = 0;
+            float ms = 0, bind_ms = 0;
+            MTG_CUDA(cudaEventElapsedTime(&bind_ms, ev[8], ev[9]));
             for (int k = 0; k < 5; k++) {
-                MTG_CUDA(cudaEventElapsedTime(&ms, ev[k == 3 ? 3 : k], k == 3 ? ev[8] : ev[k + 1]));
-                acc[k] += ms;
+                MTG_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+                acc[k] += k == 4 ? ms - bind_ms : ms;
             }
             MTG_CUDA(cudaEventElapsedTime(&ms, ev[6], ev[7]));
             acc[5] += ms;
-            MTG_CUDA(cudaEventElapsedTime(&ms, ev[8], ev[9]));
-            acc[6] += ms;
+            acc[6] += bind_ms;
             cur ^= 1;
             nlaunch += 5 + (single_bond ? kBindLaunches : 0);
             draw += 1;
