@@ -277,7 +277,9 @@ __global__ void __launch_bounds__(256) bind_decide_kernel(BindState S) {
             }
         }
     }
-    if (nm > 3) {  // larger cluster: every member queues, the smallest decides
+    if (nm > 3) {  // larger cluster: its smallest patch decides; only patches below all their partners queue
+        for (int k = 0; k < d; k++)
+            if (S.adj[(size_t)p * kAdjCap + k].x < p) return;
         const unsigned long long at = atomicAdd(S.ctr + 1, 1ull);
         if ((long long)at < (long long)S.ptot) S.large[at] = p;
         return;
@@ -336,16 +338,17 @@ __global__ void __launch_bounds__(kLargeThreads) bind_large_kernel(ForceArgs<rea
                 bool seen = false;
                 for (int t = 0; t < nm && !seen; t++) seen = mem[t] == w;
                 if (seen) continue;
+                if (w < p) { lo = w; break; }   // not the smallest: another queued patch decides
                 if (nm == kClusterCap) { over = true; break; }
                 mem[nm++] = w;
-                lo = w < lo ? w : lo;
             }
+            if (lo != p) break;
         }
+        if (lo != p) continue;
         if (over) {
             atomicOr(S.flags, kFlagBind);
             continue;
         }
-        if (lo != p) continue;
         // members in increasing order (SingleHistogram, GraphAlgorithms.cpp:2-48)
         for (int i = 1; i < nm; i++) {
             const int v = mem[i];
@@ -371,7 +374,8 @@ __global__ void __launch_bounds__(kLargeThreads) bind_large_kernel(ForceArgs<rea
                 while (f2 < nm && mem[f2] != ad.x) f2++;
                 const PatchPair c = patch_pair_of<real>(a, B, M, R.off, v, ad.x);
                 double scr = 0;
-                exact_edge<real>(B, a.buf, c.s1, c.s2, c.o1, c.o2, c.potn, disp2_of(B.disp[c.potn], ad.y), &scr);
+                exact_edge<real>(B, a.buf.pos, a.buf.rota, a.buf.rotb, c.s1, c.s2, c.o1, c.o2, c.potn,
+                                 disp2_of(B.disp[c.potn], ad.y), &scr);
                 int t = ne++;
                 while (t > 0 && (ea[t - 1] > j || (ea[t - 1] == j && eb[t - 1] > f2))) {
                     ea[t] = ea[t - 1]; eb[t] = eb[t - 1]; es[t] = es[t - 1];

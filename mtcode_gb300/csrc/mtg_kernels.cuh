@@ -544,11 +544,11 @@ __device__ __forceinline__ double disp2_of(double disp, int cls) {
 
 // FP64 edge test of the current state; with score != null also the edge's score (LangevinRforce.cpp:3040-3060)
 template <class real>
-__device__ __noinline__ bool exact_edge(const BindRep &B, const Buffers<real> &b, int s1, int s2, int o1, int o2,
-                                        int potn, double disp2, double *score) {
+__device__ __noinline__ bool exact_edge(const BindRep &B, const real *pos, const real *rota, const real *rotb, int s1,
+                                        int s2, int o1, int o2, int potn, double disp2, double *score) {
     double xa[3], qa[9], xb[3], qb[9], un[3];
-    load_state_d<real>(b.pos, b.rota, b.rotb, s1, xa, qa);
-    load_state_d<real>(b.pos, b.rota, b.rotb, s2, xb, qb);
+    load_state_d<real>(pos, rota, rotb, s1, xa, qa);
+    load_state_d<real>(pos, rota, rotb, s2, xb, qb);
     double dis = exact_dist_vec(B, xa, xb, un);
     if (!(dis < B.mk2)) return false;
     dis = __dsqrt_rn(dis);
@@ -568,10 +568,11 @@ __device__ __noinline__ bool exact_edge(const BindRep &B, const Buffers<real> &b
 // FP64 candidate-list condition on the snapshot: distance < the list cut and < max_check + 1, and
 // (c_i - max_ang) + (c_j - max_ang) > -0.4 (LangevinR.cpp:1722-1800)
 template <class real>
-__device__ __noinline__ bool exact_member(const BindRep &B, const Buffers<real> &b, int s1, int s2, int o1, int o2) {
+__device__ __noinline__ bool exact_member(const BindRep &B, const real *sa, const real *sb, const real *sc, int s1,
+                                          int s2, int o1, int o2) {
     double xa[3], qa[9], xb[3], qb[9], un[3];
-    load_state_d<real>(b.snap_a, b.snap_b, b.snap_c, s1, xa, qa);
-    load_state_d<real>(b.snap_a, b.snap_b, b.snap_c, s2, xb, qb);
+    load_state_d<real>(sa, sb, sc, s1, xa, qa);
+    load_state_d<real>(sa, sb, sc, s2, xb, qb);
     const double d2 = exact_dist_vec(B, xa, xb, un);
     if (!(d2 < B.list_cut2)) return false;
     const double dis = __dsqrt_rn(d2);
@@ -583,18 +584,19 @@ __device__ __noinline__ bool exact_member(const BindRep &B, const Buffers<real> 
 
 template <class real>
 __device__ __forceinline__ bool candidate(const BindRep &B, const Replica<real> &R, const Model<real> &M,
-                                          const Buffers<real> &b, int s1, int s2, int o1, int o2) {
-    if (std::is_same<real, double>::value) return exact_member<real>(B, b, s1, s2, o1, o2);
+                                          const real *sa, const real *sb, const real *sc, int s1, int s2, int o1,
+                                          int o2) {
+    if (std::is_same<real, double>::value) return exact_member<real>(B, sa, sb, sc, s1, s2, o1, o2);
     Payload<real> A, C;
-    A.load(b.snap_a, b.snap_b, b.snap_c, s1);
-    C.load(b.snap_a, b.snap_b, b.snap_c, s2);
+    A.load(sa, sb, sc, s1);
+    C.load(sa, sb, sc, s2);
     const real dx = min_image<real>(A.v[0] - C.v[0], R.box, R.l2s, R.periodic);
     const real dy = min_image<real>(A.v[1] - C.v[1], R.box, R.l2s, R.periodic);
     const real dz = min_image<real>(A.v[2] - C.v[2], R.box, R.l2s, R.periodic);
     const real r2 = dx * dx + dy * dy + dz * dz;
     const int t = side_of<real>(r2, B.memb2_lo, B.memb2_hi);
     if (t > 0) return false;
-    if (t == 0) return exact_member<real>(B, b, s1, s2, o1, o2);
+    if (t == 0) return exact_member<real>(B, sa, sb, sc, s1, s2, o1, o2);
     const real rr = sqrt(r2), u[3] = {dx / rr, dy / rr, dz / rr};
     const real *v1 = M.orient[o1], *v2 = M.orient[o2];
     real ci = 0, cj = 0;
@@ -604,7 +606,7 @@ __device__ __forceinline__ bool candidate(const BindRep &B, const Replica<real> 
         cj += (v2[0] * C.v[3 + k] + v2[1] * C.v[6 + k] + v2[2] * C.v[9 + k]) * u[k];
     }
     const int w = side_of<real>((ci - (real)B.max_ang_f) + (cj - (real)B.max_ang_f), B.ang_lo, B.ang_hi);
-    return w == 0 ? exact_member<real>(B, b, s1, s2, o1, o2) : w > 0;
+    return w == 0 ? exact_member<real>(B, sa, sb, sc, s1, s2, o1, o2) : w > 0;
 }
 
 // slot of this update's adjacency for patch p (stamped counter: a stale stamp counts as zero edges)
@@ -634,7 +636,7 @@ __device__ __forceinline__ void add_edge_t(unsigned long long *deg, int2 *adj, u
 // Every edge of the particle pair (s1, s2), s1 the lower particle index, d = x1 - x2 (minimum image) and
 // r2 = |d|^2 as the caller's pair loop computed them.  Called once per pair on a bond-deciding pass.
 template <class real>
-__device__ __noinline__ void bind_pair_edges(const ForceArgs<real> &a, const Replica<real> &R, const Model<real> &M,
+__device__ __forceinline__ void bind_pair_edges(const ForceArgs<real> &a, const Replica<real> &R, const Model<real> &M,
                                              int r, int s1, int s2, int li1, int li2, const real d[3], real r2) {
     const BindRep &B = a.bind_reps[r];
     const int t0 = side_of<real>(r2, B.mk2_lo, B.mk2_hi);
@@ -680,9 +682,10 @@ __device__ __noinline__ void bind_pair_edges(const ForceArgs<real> &a, const Rep
             const int e3 = side_of<real>(rr, dfl * (1.f - 1e-5f), dfl * (1.f + 1e-5f));
             if (e3 > 0) continue;
             const bool sure = !fp64 && t0 < 0 && e1 > 0 && e2 > 0 && e3 < 0;
-            if (!sure && !exact_edge<real>(B, a.buf, s1, s2, o1 + ka, o2 + kb, q, disp2_of(B.disp[q], cls), nullptr))
+            if (!sure && !exact_edge<real>(B, a.buf.pos, a.buf.rota, a.buf.rotb, s1, s2, o1 + ka, o2 + kb, q,
+                                           disp2_of(B.disp[q], cls), nullptr))
                 continue;
-            if (!candidate<real>(B, R, M, a.buf, s1, s2, o1 + ka, o2 + kb)) continue;
+            if (!candidate<real>(B, R, M, a.buf.snap_a, a.buf.snap_b, a.buf.snap_c, s1, s2, o1 + ka, o2 + kb)) continue;
             add_edge_t<real>(a.bind_deg, a.bind_adj, a.flags, wp1, wp2, cls, stamp);
         }
     }

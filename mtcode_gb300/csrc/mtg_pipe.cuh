@@ -168,9 +168,7 @@ __device__ __forceinline__ void fixed_add(long long *acc, float v) {
     if (v != 0.f) atomicAdd(reinterpret_cast<unsigned long long *>(acc), (unsigned long long)to_fixed(v));
 }
 
-// forces and torques of the listed pairs into acc (6 fixed-point sums per slot: F lab, T lab); with BIND
-// (single-bond mode, a bond-deciding pass) also this update's bond candidates of every pair
-template <bool BIND>
+// forces and torques of the listed pairs into acc (6 fixed-point sums per slot: F lab, T lab)
 __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<float> a, const int2 *pairs,
                                                                  const unsigned long long *npairs, long long cap,
                                                                  long long *acc) {
@@ -197,16 +195,6 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
             fa[0] = s_ * d[0];
             fa[1] = s_ * d[1];
             fa[2] = s_ * d[2];
-        }
-        if (BIND) {
-            const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
-            const Model<float> &M = a.tb.models[R.model];
-            if (ida < idb) {
-                bind_pair_edges<float>(a, R, M, r, sa, sb, ida - R.off, idb - R.off, d, r2);
-            } else {
-                const float dn[3] = {-d[0], -d[1], -d[2]};
-                bind_pair_edges<float>(a, R, M, r, sb, sa, idb - R.off, ida - R.off, dn, r2);
-            }
         }
         if (r2 < R.patch_r2) {
             const Model<float> &M = a.tb.models[R.model];
@@ -262,6 +250,35 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
         }
     }
     if (big) atomicOr(a.flags, 2u);
+}
+
+// single-bond mode, a bond-deciding pass: this update's edges of every listed pair (each pair once, in its
+// canonical order: lower particle index first)
+__global__ void __launch_bounds__(kPipeThreads) bind_pairs_kernel(ForceArgs<float> a, const int2 *pairs,
+                                                                const unsigned long long *npairs, long long cap) {
+    const long long n = (long long)*npairs < cap ? (long long)*npairs : cap;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int2 pr = pairs[q];
+        const int sa = pr.x, sb = pr.y;
+        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, sa);
+        const Replica<float> &R = a.tb.reps[r];
+        float xa[4], xb[4];
+        load4(a.buf.pos + 4 * (size_t)sa, xa);
+        load4(a.buf.pos + 4 * (size_t)sb, xb);
+        const float d[3] = {min_image<float>(xa[0] - xb[0], R.box, R.l2s, R.periodic),
+                            min_image<float>(xa[1] - xb[1], R.box, R.l2s, R.periodic),
+                            min_image<float>(xa[2] - xb[2], R.box, R.l2s, R.periodic)};
+        const float r2 = sep_r2(d[0], d[1], d[2]);
+        if (!(r2 < R.rc2)) continue;
+        const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
+        const Model<float> &M = a.tb.models[R.model];
+        if (ida < idb) {
+            bind_pair_edges<float>(a, R, M, r, sa, sb, ida - R.off, idb - R.off, d, r2);
+        } else {
+            const float dn[3] = {-d[0], -d[1], -d[2]};
+            bind_pair_edges<float>(a, R, M, r, sb, sa, idb - R.off, ida - R.off, dn, r2);
+        }
+    }
 }
 
 // per particle: the summed force and torque (cleared for the next pass), bonds, then the mode's output

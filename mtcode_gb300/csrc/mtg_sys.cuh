@@ -780,11 +780,10 @@ struct Sys : SysBase {
                 const int gb = (ntot_ + mtg::kPipeThreads - 1) / mtg::kPipeThreads;
                 mtg::pairfind_kernel<<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap,
                                                                                   skin > 0 ? 1 : 0, gate);
+                mtg::pairforce_kernel<<<sms * 16, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap, d_acc);
                 if (bind) {
-                    mtg::pairforce_kernel<true><<<sms * 16, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap, d_acc);
+                    mtg::bind_pairs_kernel<<<sms * 8, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap);
                     decide();
-                } else {
-                    mtg::pairforce_kernel<false><<<sms * 16, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap, d_acc);
                 }
                 mtg::pair_epilogue_kernel<MODE><<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_acc);
                 return;
