@@ -633,6 +633,31 @@ __device__ __forceinline__ void add_edge_t(unsigned long long *deg, int2 *adj, u
     else atomicOr(flags, kFlagBind);
 }
 
+// One patch pair (patch ka of particle s1, kb of s2; s1 the lower particle index) with cosines c1, c2 and
+// distance rr from the caller's float geometry (t0: the max_check test's side): the edge test, the
+// candidate-list condition, and the edge into both patches' adjacency.
+template <class real>
+__device__ __forceinline__ void bind_patch_edge(const ForceArgs<real> &a, const BindRep &B, const Replica<real> &R,
+                                                const Model<real> &M, int s1, int s2, int li1, int li2, int ty1,
+                                                int ty2, int ka, int kb, real c1, real c2, real rr, int t0,
+                                                unsigned stamp) {
+    const int q = M.pstart[ty1][ty2] + ka * M.np[ty2] + kb;
+    const int e1 = side_of<real>(c1, B.ctm_lo[q], B.ctm_hi[q]), e2 = side_of<real>(c2, B.ctm_lo[q], B.ctm_hi[q]);
+    if (e1 < 0 || e2 < 0) return;
+    const int wp1 = patch_of<real>(B, M, li1, ty1, ka), wp2 = patch_of<real>(B, M, li2, ty2, kb);
+    const int cls = range_class(a.bind_to, a.bind_on, wp1, wp2);
+    const float dfl = cls == 1 ? 0.5f * B.disp_f[q] : (cls == 2 ? 0.7f * B.disp_f[q] : B.disp_f[q]);
+    const int e3 = side_of<real>(rr, dfl * (1.f - 1e-5f), dfl * (1.f + 1e-5f));
+    if (e3 > 0) return;
+    const int o1 = M.ooff[ty1] + ka, o2 = M.ooff[ty2] + kb;
+    const bool sure = !std::is_same<real, double>::value && t0 < 0 && e1 > 0 && e2 > 0 && e3 < 0;
+    if (!sure && !exact_edge<real>(B, a.buf.pos, a.buf.rota, a.buf.rotb, s1, s2, o1, o2, q, disp2_of(B.disp[q], cls),
+                                   nullptr))
+        return;
+    if (!candidate<real>(B, R, M, a.buf.snap_a, a.buf.snap_b, a.buf.snap_c, s1, s2, o1, o2)) return;
+    add_edge_t<real>(a.bind_deg, a.bind_adj, a.flags, wp1, wp2, cls, stamp);
+}
+
 // Every edge of the particle pair (s1, s2), s1 the lower particle index, d = x1 - x2 (minimum image) and
 // r2 = |d|^2 as the caller's pair loop computed them.  Called once per pair on a bond-deciding pass.
 template <class real>
@@ -666,27 +691,12 @@ __device__ __forceinline__ void bind_pair_edges(const ForceArgs<real> &a, const 
 #pragma unroll
     for (int k = 0; k < 3; k++) w2[k] = P2.v[3 + 3 * k] * u[0] + P2.v[4 + 3 * k] * u[1] + P2.v[5 + 3 * k] * u[2];
     const unsigned stamp = (unsigned)a.bind_ctr[2];
-    const bool fp64 = std::is_same<real, double>::value;
-    const int ps = M.pstart[ty1][ty2];
     for (int ka = 0; ka < na; ka++) {
         if (!(c1[ka] > pre)) continue;
         for (int kb = 0; kb < nb; kb++) {
             const real *v = M.orient[o2 + kb];
-            const real c2 = v[0] * w2[0] + v[1] * w2[1] + v[2] * w2[2];
-            const int q = ps + ka * nb + kb;
-            const int e1 = side_of<real>(c1[ka], B.ctm_lo[q], B.ctm_hi[q]), e2 = side_of<real>(c2, B.ctm_lo[q], B.ctm_hi[q]);
-            if (e1 < 0 || e2 < 0) continue;
-            const int wp1 = patch_of<real>(B, M, li1, ty1, ka), wp2 = patch_of<real>(B, M, li2, ty2, kb);
-            const int cls = range_class(a.bind_to, a.bind_on, wp1, wp2);
-            const float dfl = cls == 1 ? 0.5f * B.disp_f[q] : (cls == 2 ? 0.7f * B.disp_f[q] : B.disp_f[q]);
-            const int e3 = side_of<real>(rr, dfl * (1.f - 1e-5f), dfl * (1.f + 1e-5f));
-            if (e3 > 0) continue;
-            const bool sure = !fp64 && t0 < 0 && e1 > 0 && e2 > 0 && e3 < 0;
-            if (!sure && !exact_edge<real>(B, a.buf.pos, a.buf.rota, a.buf.rotb, s1, s2, o1 + ka, o2 + kb, q,
-                                           disp2_of(B.disp[q], cls), nullptr))
-                continue;
-            if (!candidate<real>(B, R, M, a.buf.snap_a, a.buf.snap_b, a.buf.snap_c, s1, s2, o1 + ka, o2 + kb)) continue;
-            add_edge_t<real>(a.bind_deg, a.bind_adj, a.flags, wp1, wp2, cls, stamp);
+            bind_patch_edge<real>(a, B, R, M, s1, s2, li1, li2, ty1, ty2, ka, kb, c1[ka], v[0] * w2[0] + v[1] * w2[1] + v[2] * w2[2],
+                                  rr, t0, stamp);
         }
     }
 }

@@ -252,31 +252,95 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
     if (big) atomicOr(a.flags, 2u);
 }
 
-// single-bond mode, a bond-deciding pass: this update's edges of every listed pair (each pair once, in its
-// canonical order: lower particle index first)
+// single-bond mode, a bond-deciding pass: this update's edges of every listed pair, each pair in its
+// canonical order (lower particle index first).  A warp takes 32 pairs; each lane tests whether both of its
+// particles have a patch near a cone (few pairs do), then the whole warp works through the pairs that
+// passed, one patch pair per lane.
 __global__ void __launch_bounds__(kPipeThreads) bind_pairs_kernel(ForceArgs<float> a, const int2 *pairs,
                                                                 const unsigned long long *npairs, long long cap) {
     const long long n = (long long)*npairs < cap ? (long long)*npairs : cap;
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        const int2 pr = pairs[q];
-        const int sa = pr.x, sb = pr.y;
-        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, sa);
-        const Replica<float> &R = a.tb.reps[r];
-        float xa[4], xb[4];
-        load4(a.buf.pos + 4 * (size_t)sa, xa);
-        load4(a.buf.pos + 4 * (size_t)sb, xb);
-        const float d[3] = {min_image<float>(xa[0] - xb[0], R.box, R.l2s, R.periodic),
-                            min_image<float>(xa[1] - xb[1], R.box, R.l2s, R.periodic),
-                            min_image<float>(xa[2] - xb[2], R.box, R.l2s, R.periodic)};
-        const float r2 = sep_r2(d[0], d[1], d[2]);
-        if (!(r2 < R.rc2)) continue;
-        const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
-        const Model<float> &M = a.tb.models[R.model];
-        if (ida < idb) {
-            bind_pair_edges<float>(a, R, M, r, sa, sb, ida - R.off, idb - R.off, d, r2);
-        } else {
-            const float dn[3] = {-d[0], -d[1], -d[2]};
-            bind_pair_edges<float>(a, R, M, r, sb, sa, idb - R.off, ida - R.off, dn, r2);
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const unsigned stamp = (unsigned)a.bind_ctr[2];
+    for (long long base = warp * 32; base < n; base += nwarps * 32) {
+        const long long q = base + lane;
+        bool pass = false;
+        int s1 = 0, s2 = 0, li1 = 0, li2 = 0, ty1 = 0, ty2 = 0, r = 0, t0 = 1;
+        float w1[3] = {0.f, 0.f, 0.f}, w2[3] = {0.f, 0.f, 0.f}, rr = 1.f;
+        if (q < n) {
+            const int2 pr = pairs[q];
+            r = find_replica(a.tb.rep_slot, a.tb.nrep, pr.x);
+            const Replica<float> &R = a.tb.reps[r];
+            const BindRep &B = a.bind_reps[r];
+            const Model<float> &M = a.tb.models[R.model];
+            float xa[4], xb[4];
+            load4(a.buf.pos + 4 * (size_t)pr.x, xa);
+            load4(a.buf.pos + 4 * (size_t)pr.y, xb);
+            float d[3] = {min_image<float>(xa[0] - xb[0], R.box, R.l2s, R.periodic),
+                          min_image<float>(xa[1] - xb[1], R.box, R.l2s, R.periodic),
+                          min_image<float>(xa[2] - xb[2], R.box, R.l2s, R.periodic)};
+            const float r2 = sep_r2(d[0], d[1], d[2]);
+            t0 = side_of<float>(r2, B.mk2_lo, B.mk2_hi);
+            const int ida = __ldg(a.buf.ident + pr.x), idb = __ldg(a.buf.ident + pr.y);
+            const bool a_first = ida < idb;
+            s1 = a_first ? pr.x : pr.y;
+            s2 = a_first ? pr.y : pr.x;
+            li1 = (a_first ? ida : idb) - R.off;
+            li2 = (a_first ? idb : ida) - R.off;
+            ty1 = type_of<float>(M, li1);
+            ty2 = type_of<float>(M, li2);
+            if (t0 <= 0 && M.np[ty1] > 0 && M.np[ty2] > 0) {
+                rr = sqrtf(r2);
+                const float sg = a_first ? 1.f : -1.f;
+                const float u[3] = {sg * d[0] / rr, sg * d[1] / rr, sg * d[2] / rr};
+                const float pre = M.mincos[ty1][ty2] - 4e-5f;
+                float Q[9];
+                load_q(a, s1, a_first ? xa[3] : xb[3], Q);
+#pragma unroll
+                for (int k = 0; k < 3; k++) w1[k] = Q[3 * k] * u[0] + Q[3 * k + 1] * u[1] + Q[3 * k + 2] * u[2];
+                bool any1 = false;
+                for (int k = 0; k < M.np[ty1]; k++) {
+                    const float *v = M.orient[M.ooff[ty1] + k];
+                    any1 |= -(v[0] * w1[0] + v[1] * w1[1] + v[2] * w1[2]) > pre;
+                }
+                if (any1) {
+                    load_q(a, s2, a_first ? xb[3] : xa[3], Q);
+#pragma unroll
+                    for (int k = 0; k < 3; k++) w2[k] = Q[3 * k] * u[0] + Q[3 * k + 1] * u[1] + Q[3 * k + 2] * u[2];
+                    for (int k = 0; k < M.np[ty2]; k++) {
+                        const float *v = M.orient[M.ooff[ty2] + k];
+                        pass |= v[0] * w2[0] + v[1] * w2[1] + v[2] * w2[2] > pre;
+                    }
+                }
+            }
+        }
+        unsigned m = __ballot_sync(0xffffffffu, pass);
+        while (m) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            const int p1 = __shfl_sync(0xffffffffu, s1, src), p2 = __shfl_sync(0xffffffffu, s2, src);
+            const int l1 = __shfl_sync(0xffffffffu, li1, src), l2 = __shfl_sync(0xffffffffu, li2, src);
+            const int y1 = __shfl_sync(0xffffffffu, ty1, src), y2 = __shfl_sync(0xffffffffu, ty2, src);
+            const int rp = __shfl_sync(0xffffffffu, r, src), tt = __shfl_sync(0xffffffffu, t0, src);
+            const float dist = __shfl_sync(0xffffffffu, rr, src);
+            float v1[3], v2[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                v1[k] = __shfl_sync(0xffffffffu, w1[k], src);
+                v2[k] = __shfl_sync(0xffffffffu, w2[k], src);
+            }
+            const Replica<float> &R = a.tb.reps[rp];
+            const BindRep &B = a.bind_reps[rp];
+            const Model<float> &M = a.tb.models[R.model];
+            const int na = M.np[y1], nb = M.np[y2];
+            for (int pp = lane; pp < na * nb; pp += 32) {
+                const int ka = pp / nb, kb = pp - ka * nb;
+                const float *va = M.orient[M.ooff[y1] + ka], *vb = M.orient[M.ooff[y2] + kb];
+                const float c1 = -(va[0] * v1[0] + va[1] * v1[1] + va[2] * v1[2]);
+                const float c2 = vb[0] * v2[0] + vb[1] * v2[1] + vb[2] * v2[2];
+                bind_patch_edge<float>(a, B, R, M, p1, p2, l1, l2, y1, y2, ka, kb, c1, c2, dist, tt, stamp);
+            }
         }
     }
 }
