@@ -47,11 +47,13 @@ struct BindState {
     int patch_every;
     unsigned long long *ctr;      // [1] queued large-cluster patches [2] update stamp [3] steps of the
                                   // run_singlebond loop so far [4] candidate list due this update
+                                  // [5] patches with an edge (touched) [6] pairs listed for the edge pass
     unsigned long long *deg;      // per patch: stamp << 32 | edges of this update
     int2 *adj;                    // per patch kAdjCap: (partner patch, disp2 class)
     int *boundto;                 // global patch indices
     unsigned char *isbound;
     int *large;                   // queued patches of clusters above three
+    int *touched;                 // patches with at least one edge in this update
     int *scratch;                 // large-cluster scratch, one block of kScratchInts per thread
     int scratch_threads;
     unsigned *flags;
@@ -65,6 +67,8 @@ __global__ void bind_begin_kernel(BindState S, int force, int advance) {
     const unsigned long long step = S.ctr[3];
     S.ctr[4] = force || (step > 0 && S.patch_every > 0 && step % (unsigned long long)S.patch_every == 0);
     S.ctr[1] = 0;
+    S.ctr[5] = 0;
+    S.ctr[6] = 0;
     S.ctr[2] += 1;
     if (advance) S.ctr[3] = step + 1;
 }
@@ -252,16 +256,17 @@ __device__ __forceinline__ void break_check(const BindState &S, int p, int d) {
     S.isbound[p] = 0;
 }
 
-// ------------------------------------------------------------------ clusters of up to three
-__global__ void __launch_bounds__(256) bind_decide_kernel(BindState S) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= S.ptot) return;
+// ------------------------------------------------------------------ clusters
+// a patch without an edge is a cluster of one: unbound (LangevinRforce.cpp:3110-3133, 3165-3170)
+__global__ void __launch_bounds__(256) bind_unbind_kernel(BindState S) {
     const unsigned stamp = (unsigned)S.ctr[2];
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < S.ptot; p += gridDim.x * blockDim.x)
+        if (S.isbound[p] && adj_count(S.deg, p, stamp) == 0) S.isbound[p] = 0;
+}
+
+// clusters of two or three: the walk from one patch with an edge
+__device__ __forceinline__ void decide_one(const BindState &S, int p, unsigned stamp) {
     const int d = adj_count(S.deg, p, stamp);
-    if (d == 0) {  // a cluster of one: unbound (LangevinRforce.cpp:3165-3170)
-        if (S.isbound[p]) S.isbound[p] = 0;
-        return;
-    }
     // breadth-first walk of p's component, stopped at a fourth member
     int m[4], nm = 1, lo = p;
     m[0] = p;
@@ -304,6 +309,13 @@ __global__ void __launch_bounds__(256) bind_decide_kernel(BindState S) {
         return;
     }
     apply_triplet(S, mod, B.patch_off, s[0], s[1], s[2], c, ran);
+}
+
+__global__ void __launch_bounds__(256) bind_decide_kernel(BindState S) {
+    const long long nt = (long long)S.ctr[5] < (long long)S.ptot ? (long long)S.ctr[5] : (long long)S.ptot;
+    const unsigned stamp = (unsigned)S.ctr[2];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += (long long)gridDim.x * blockDim.x)
+        decide_one(S, S.touched[i], stamp);
 }
 
 // ------------------------------------------------------------------ larger clusters

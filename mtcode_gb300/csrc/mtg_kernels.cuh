@@ -12,6 +12,8 @@
 //              the second half-kick, and the binning of the next step
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "mtg_device.cuh"
 
 namespace mtg {
@@ -476,7 +478,8 @@ struct ForceArgs {
     const int *bind_to;
     unsigned long long *bind_deg;
     int2 *bind_adj;
-    const unsigned long long *bind_ctr;
+    unsigned long long *bind_ctr;    // [2] stamp, [5] patches with an edge so far (bind_touched)
+    int *bind_touched;
 };
 
 // ------------------------------------------------------------------ single-bond mode: bond candidates
@@ -623,14 +626,25 @@ __device__ __forceinline__ int adj_take(unsigned long long *deg, int p, unsigned
     return kAdjCap;
 }
 
+// a patch's first edge of this update puts it on the touched list (the patches the decisions visit)
+__device__ __forceinline__ void touch(int *touched, unsigned long long *count, int p) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(count, (unsigned long long)g.size());
+    base = g.shfl(base, 0) + g.thread_rank();
+    touched[base] = p;   // at most one entry per patch: base < total patches
+}
+
 template <class real>
-__device__ __forceinline__ void add_edge_t(unsigned long long *deg, int2 *adj, unsigned *flags, int w1, int w2,
-                                           int cls, unsigned stamp) {
-    const int k1 = adj_take(deg, w1, stamp, flags), k2 = adj_take(deg, w2, stamp, flags);
-    if (k1 < kAdjCap) adj[(size_t)w1 * kAdjCap + k1] = make_int2(w2, cls);
-    else atomicOr(flags, kFlagBind);
-    if (k2 < kAdjCap) adj[(size_t)w2 * kAdjCap + k2] = make_int2(w1, cls);
-    else atomicOr(flags, kFlagBind);
+__device__ __forceinline__ void add_edge_t(const ForceArgs<real> &a, int w1, int w2, int cls, unsigned stamp) {
+    const int k1 = adj_take(a.bind_deg, w1, stamp, a.flags), k2 = adj_take(a.bind_deg, w2, stamp, a.flags);
+    if (k1 < kAdjCap) a.bind_adj[(size_t)w1 * kAdjCap + k1] = make_int2(w2, cls);
+    else atomicOr(a.flags, kFlagBind);
+    if (k2 < kAdjCap) a.bind_adj[(size_t)w2 * kAdjCap + k2] = make_int2(w1, cls);
+    else atomicOr(a.flags, kFlagBind);
+    if (k1 == 0) touch(a.bind_touched, a.bind_ctr + 5, w1);
+    if (k2 == 0) touch(a.bind_touched, a.bind_ctr + 5, w2);
 }
 
 // One patch pair (patch ka of particle s1, kb of s2; s1 the lower particle index) with cosines c1, c2 and
@@ -655,7 +669,7 @@ __device__ __forceinline__ void bind_patch_edge(const ForceArgs<real> &a, const 
                                    nullptr))
         return;
     if (!candidate<real>(B, R, M, a.buf.snap_a, a.buf.snap_b, a.buf.snap_c, s1, s2, o1, o2)) return;
-    add_edge_t<real>(a.bind_deg, a.bind_adj, a.flags, wp1, wp2, cls, stamp);
+    add_edge_t<real>(a, wp1, wp2, cls, stamp);
 }
 
 // Every edge of the particle pair (s1, s2), s1 the lower particle index, d = x1 - x2 (minimum image) and

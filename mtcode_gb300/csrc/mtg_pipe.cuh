@@ -168,10 +168,26 @@ __device__ __forceinline__ void fixed_add(long long *acc, float v) {
     if (v != 0.f) atomicAdd(reinterpret_cast<unsigned long long *>(acc), (unsigned long long)to_fixed(v));
 }
 
-// forces and torques of the listed pairs into acc (6 fixed-point sums per slot: F lab, T lab)
+// warp-aggregated append of one entry to a list with a 64-bit counter; false (and the flag) when full
+__device__ __forceinline__ void list_append(int2 *list, unsigned long long *count, long long cap, int2 e,
+                                            unsigned *flags) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(count, (unsigned long long)g.size());
+    base = g.shfl(base, 0) + g.thread_rank();
+    if ((long long)base < cap) list[base] = e;
+    else atomicOr(flags, kFlagBind);
+}
+
+// forces and torques of the listed pairs into acc (6 fixed-point sums per slot: F lab, T lab).  BIND
+// (single-bond mode, a bond-deciding pass): pairs where both particles have a patch near a cone along the
+// pair go, in canonical order (lower particle index first), to bind_list for bind_pairs_kernel.
+template <bool BIND>
 __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<float> a, const int2 *pairs,
                                                                  const unsigned long long *npairs, long long cap,
-                                                                 long long *acc) {
+                                                                 long long *acc, int2 *bind_list = nullptr,
+                                                                 unsigned long long *bind_n = nullptr) {
     const long long n = (long long)*npairs < cap ? (long long)*npairs : cap;
     bool big = false;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
@@ -195,6 +211,35 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
             fa[0] = s_ * d[0];
             fa[1] = s_ * d[1];
             fa[2] = s_ * d[2];
+        }
+        if (BIND) {
+            // along d = x_a - x_b: a's cosines are -(n_a . d) / r and b's (n_b . d) / r in either canonical order
+            const Model<float> &M = a.tb.models[R.model];
+            const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
+            const int ta = type_of<float>(M, ida - R.off), tb = type_of<float>(M, idb - R.off);
+            if (M.np[ta] > 0 && M.np[tb] > 0) {
+                const float inv = 1.f / sqrtf(r2), pre = M.mincos[ta][tb] - 4e-5f;
+                float Q[9], w[3];
+                load_q(a, sa, xa[3], Q);
+#pragma unroll
+                for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
+                bool any = false;
+                for (int k = 0; k < M.np[ta]; k++) {
+                    const float *v = M.orient[M.ooff[ta] + k];
+                    any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > pre;
+                }
+                if (any) {
+                    load_q(a, sb, xb[3], Q);
+#pragma unroll
+                    for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
+                    bool anyb = false;
+                    for (int k = 0; k < M.np[tb]; k++) {
+                        const float *v = M.orient[M.ooff[tb] + k];
+                        anyb |= v[0] * w[0] + v[1] * w[1] + v[2] * w[2] > pre;
+                    }
+                    if (anyb) list_append(bind_list, bind_n, cap, ida < idb ? make_int2(sa, sb) : make_int2(sb, sa), a.flags);
+                }
+            }
         }
         if (r2 < R.patch_r2) {
             const Model<float> &M = a.tb.models[R.model];
@@ -252,70 +297,52 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
     if (big) atomicOr(a.flags, 2u);
 }
 
-// single-bond mode, a bond-deciding pass: this update's edges of every listed pair, each pair in its
-// canonical order (lower particle index first).  A warp takes 32 pairs; each lane tests whether both of its
-// particles have a patch near a cone (few pairs do), then the whole warp works through the pairs that
-// passed, one patch pair per lane.
-__global__ void __launch_bounds__(kPipeThreads) bind_pairs_kernel(ForceArgs<float> a, const int2 *pairs,
-                                                                const unsigned long long *npairs, long long cap) {
-    const long long n = (long long)*npairs < cap ? (long long)*npairs : cap;
+// single-bond mode, a bond-deciding pass: this update's edges of the pairs pairforce_kernel<true> listed
+// (canonical order, both particles with a patch near a cone).  A warp takes 32 of them and works through
+// them one at a time, one patch pair per lane.
+__global__ void __launch_bounds__(kPipeThreads) bind_pairs_kernel(ForceArgs<float> a, const int2 *list,
+                                                                const unsigned long long *nlist, long long cap) {
+    const long long n = (long long)*nlist < cap ? (long long)*nlist : cap;
     const int lane = threadIdx.x & 31;
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     const unsigned stamp = (unsigned)a.bind_ctr[2];
     for (long long base = warp * 32; base < n; base += nwarps * 32) {
         const long long q = base + lane;
-        bool pass = false;
         int s1 = 0, s2 = 0, li1 = 0, li2 = 0, ty1 = 0, ty2 = 0, r = 0, t0 = 1;
         float w1[3] = {0.f, 0.f, 0.f}, w2[3] = {0.f, 0.f, 0.f}, rr = 1.f;
-        if (q < n) {
-            const int2 pr = pairs[q];
-            r = find_replica(a.tb.rep_slot, a.tb.nrep, pr.x);
+        const bool live = q < n;
+        if (live) {
+            const int2 pr = list[q];
+            s1 = pr.x;
+            s2 = pr.y;
+            r = find_replica(a.tb.rep_slot, a.tb.nrep, s1);
             const Replica<float> &R = a.tb.reps[r];
             const BindRep &B = a.bind_reps[r];
             const Model<float> &M = a.tb.models[R.model];
-            float xa[4], xb[4];
-            load4(a.buf.pos + 4 * (size_t)pr.x, xa);
-            load4(a.buf.pos + 4 * (size_t)pr.y, xb);
-            float d[3] = {min_image<float>(xa[0] - xb[0], R.box, R.l2s, R.periodic),
-                          min_image<float>(xa[1] - xb[1], R.box, R.l2s, R.periodic),
-                          min_image<float>(xa[2] - xb[2], R.box, R.l2s, R.periodic)};
+            float x1[4], x2[4];
+            load4(a.buf.pos + 4 * (size_t)s1, x1);
+            load4(a.buf.pos + 4 * (size_t)s2, x2);
+            const float d[3] = {min_image<float>(x1[0] - x2[0], R.box, R.l2s, R.periodic),
+                                min_image<float>(x1[1] - x2[1], R.box, R.l2s, R.periodic),
+                                min_image<float>(x1[2] - x2[2], R.box, R.l2s, R.periodic)};
             const float r2 = sep_r2(d[0], d[1], d[2]);
             t0 = side_of<float>(r2, B.mk2_lo, B.mk2_hi);
-            const int ida = __ldg(a.buf.ident + pr.x), idb = __ldg(a.buf.ident + pr.y);
-            const bool a_first = ida < idb;
-            s1 = a_first ? pr.x : pr.y;
-            s2 = a_first ? pr.y : pr.x;
-            li1 = (a_first ? ida : idb) - R.off;
-            li2 = (a_first ? idb : ida) - R.off;
+            li1 = __ldg(a.buf.ident + s1) - R.off;
+            li2 = __ldg(a.buf.ident + s2) - R.off;
             ty1 = type_of<float>(M, li1);
             ty2 = type_of<float>(M, li2);
-            if (t0 <= 0 && M.np[ty1] > 0 && M.np[ty2] > 0) {
-                rr = sqrtf(r2);
-                const float sg = a_first ? 1.f : -1.f;
-                const float u[3] = {sg * d[0] / rr, sg * d[1] / rr, sg * d[2] / rr};
-                const float pre = M.mincos[ty1][ty2] - 4e-5f;
-                float Q[9];
-                load_q(a, s1, a_first ? xa[3] : xb[3], Q);
+            rr = sqrtf(r2);
+            const float u[3] = {d[0] / rr, d[1] / rr, d[2] / rr};
+            float Q[9];
+            load_q(a, s1, x1[3], Q);
 #pragma unroll
-                for (int k = 0; k < 3; k++) w1[k] = Q[3 * k] * u[0] + Q[3 * k + 1] * u[1] + Q[3 * k + 2] * u[2];
-                bool any1 = false;
-                for (int k = 0; k < M.np[ty1]; k++) {
-                    const float *v = M.orient[M.ooff[ty1] + k];
-                    any1 |= -(v[0] * w1[0] + v[1] * w1[1] + v[2] * w1[2]) > pre;
-                }
-                if (any1) {
-                    load_q(a, s2, a_first ? xb[3] : xa[3], Q);
+            for (int k = 0; k < 3; k++) w1[k] = Q[3 * k] * u[0] + Q[3 * k + 1] * u[1] + Q[3 * k + 2] * u[2];
+            load_q(a, s2, x2[3], Q);
 #pragma unroll
-                    for (int k = 0; k < 3; k++) w2[k] = Q[3 * k] * u[0] + Q[3 * k + 1] * u[1] + Q[3 * k + 2] * u[2];
-                    for (int k = 0; k < M.np[ty2]; k++) {
-                        const float *v = M.orient[M.ooff[ty2] + k];
-                        pass |= v[0] * w2[0] + v[1] * w2[1] + v[2] * w2[2] > pre;
-                    }
-                }
-            }
+            for (int k = 0; k < 3; k++) w2[k] = Q[3 * k] * u[0] + Q[3 * k + 1] * u[1] + Q[3 * k + 2] * u[2];
         }
-        unsigned m = __ballot_sync(0xffffffffu, pass);
+        unsigned m = __ballot_sync(0xffffffffu, live && t0 <= 0);
         while (m) {
             const int src = __ffs(m) - 1;
             m &= m - 1;

@@ -250,6 +250,8 @@ struct Sys : SysBase {
     mtg::BindRep *d_brep = nullptr;
     mtg::BindModel *d_bmodel = nullptr;
     int *d_patch_slot = nullptr, *d_boundto = nullptr, *d_large = nullptr, *d_scratch = nullptr;
+    int *d_touched = nullptr;
+    int2 *d_bind_pairs = nullptr;   // pairs the FP32 pipeline lists for the edge pass
     int ncells_full = 0;                         // the force grid's cells outside single-bond mode
     unsigned long long *d_bctr = nullptr, *d_deg = nullptr;
     int2 *d_adj = nullptr;
@@ -475,7 +477,7 @@ struct Sys : SysBase {
     }
 
     // ---------------------------------------------------------------- single-bond-per-patch mode
-    static constexpr int kBindLaunches = 4;   // begin (+ snapshot or edges-only pass), decide, large
+    static constexpr int kBindLaunches = 5;   // begin (+ snapshot), edges, unbind, decide, large
 
     mtg::BindState bind_state() const {
         mtg::BindState S;
@@ -492,6 +494,7 @@ struct Sys : SysBase {
         S.boundto = d_boundto;
         S.isbound = d_isbound;
         S.large = d_large;
+        S.touched = d_touched;
         S.scratch = d_scratch;
         S.scratch_threads = scratch_threads;
         S.flags = d_flags;
@@ -512,13 +515,17 @@ struct Sys : SysBase {
     // clusters and bond decisions from this update's edges (positions reached through slot_of)
     void enqueue_bind_decide(const mtg::ForceArgs<real> &a) {
         const mtg::BindState S = bind_state();
-        mtg::bind_decide_kernel<<<std::max(1, (ptot + 255) / 256), 256, 0, st>>>(S);
+        mtg::bind_unbind_kernel<<<grid_for(ptot, 256, occ_stream, sms), 256, 0, st>>>(S);
+        mtg::bind_decide_kernel<<<grid_for(ptot, 256, 4, sms), 256, 0, st>>>(S);
         mtg::bind_large_kernel<real><<<scratch_threads / mtg::kLargeThreads, mtg::kLargeThreads, 0, st>>>(a, S);
     }
 
     void free_bind() {
         cudaFree(d_brep); cudaFree(d_bmodel); cudaFree(d_patch_slot); cudaFree(d_boundto); cudaFree(d_large);
         cudaFree(d_scratch); cudaFree(d_bctr); cudaFree(d_deg); cudaFree(d_adj); cudaFree(d_isbound);
+        cudaFree(d_touched); cudaFree(d_bind_pairs);
+        d_touched = nullptr;
+        d_bind_pairs = nullptr;
         d_brep = nullptr; d_bmodel = nullptr; d_patch_slot = d_boundto = d_large = d_scratch = nullptr;
         d_bctr = d_deg = nullptr; d_adj = nullptr; d_isbound = nullptr;
         for (int b = 0; b < 2; b++) {
@@ -660,6 +667,8 @@ struct Sys : SysBase {
         MTG_CUDA(cudaMalloc(&d_boundto, sizeof(int) * np));
         MTG_CUDA(cudaMalloc(&d_isbound, np));
         MTG_CUDA(cudaMalloc(&d_large, sizeof(int) * np));
+        MTG_CUDA(cudaMalloc(&d_touched, sizeof(int) * np));
+        if (use_pipe) MTG_CUDA(cudaMalloc(&d_bind_pairs, sizeof(int2) * (size_t)std::max<long long>(pair_cap, 1)));
         MTG_CUDA(cudaMalloc(&d_scratch, sizeof(int) * (size_t)mtg::kScratchInts * scratch_threads));
         MTG_CUDA(cudaMemcpy(d_brep, br.data(), sizeof(mtg::BindRep) * nrep, cudaMemcpyHostToDevice));
         MTG_CUDA(cudaMemcpy(d_bmodel, &hm, sizeof(hm), cudaMemcpyHostToDevice));
@@ -765,6 +774,7 @@ struct Sys : SysBase {
             a.bind_deg = d_deg;
             a.bind_adj = d_adj;
             a.bind_ctr = d_bctr;
+            a.bind_touched = d_touched;
         }
         auto decide = [&]() {
             if (bind_ev) MTG_CUDA(cudaEventRecord(bind_ev[0], st));
@@ -780,10 +790,13 @@ struct Sys : SysBase {
                 const int gb = (ntot_ + mtg::kPipeThreads - 1) / mtg::kPipeThreads;
                 mtg::pairfind_kernel<<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap,
                                                                                   skin > 0 ? 1 : 0, gate);
-                mtg::pairforce_kernel<<<sms * 16, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap, d_acc);
                 if (bind) {
-                    mtg::bind_pairs_kernel<<<sms * 8, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap);
+                    mtg::pairforce_kernel<true><<<sms * 16, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap,
+                                                                                      d_acc, d_bind_pairs, d_bctr + 6);
+                    mtg::bind_pairs_kernel<<<sms * 8, mtg::kPipeThreads, 0, st>>>(a, d_bind_pairs, d_bctr + 6, pair_cap);
                     decide();
+                } else {
+                    mtg::pairforce_kernel<false><<<sms * 16, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap, d_acc);
                 }
                 mtg::pair_epilogue_kernel<MODE><<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_acc);
                 return;
