@@ -53,7 +53,10 @@ struct BindState {
     int *boundto;                 // global patch indices
     unsigned char *isbound;
     int *large;                   // queued patches of clusters above three
-    int *touched;                 // patches with at least one edge in this update
+    int *touched;                 // patches with at least one edge in this update (kSegs segments of tcap)
+    long long tcap;
+    int2 *bound;                  // pairs bound by this update's decisions (kSegs segments of bcap), or null
+    long long bcap;
     int *scratch;                 // large-cluster scratch, one block of kScratchInts per thread
     int scratch_threads;
     unsigned *flags;
@@ -67,8 +70,7 @@ __global__ void bind_begin_kernel(BindState S, int force, int advance) {
     const unsigned long long step = S.ctr[3];
     S.ctr[4] = force || (step > 0 && S.patch_every > 0 && step % (unsigned long long)S.patch_every == 0);
     S.ctr[1] = 0;
-    S.ctr[5] = 0;
-    S.ctr[6] = 0;
+    for (int k = kSegPairs; k < kBindCounters; k++) S.ctr[k] = 0;
     S.ctr[2] += 1;
     if (advance) S.ctr[3] = step + 1;
 }
@@ -209,6 +211,7 @@ __device__ __forceinline__ void set_pair(const BindState &S, int i1, int i2) {
     S.boundto[i2] = i1;
     S.isbound[i1] = 1;
     S.isbound[i2] = 1;
+    if (S.bound) seg_append<int2>(S.bound, S.ctr + kSegBound, S.bcap, make_int2(i1, i2), S.flags);
 }
 
 __device__ __forceinline__ void apply_doublet(const BindState &S, const BindModel &m, int lo, int i1, int i2, double ran) {
@@ -312,10 +315,13 @@ __device__ __forceinline__ void decide_one(const BindState &S, int p, unsigned s
 }
 
 __global__ void __launch_bounds__(256) bind_decide_kernel(BindState S) {
-    const long long nt = (long long)S.ctr[5] < (long long)S.ptot ? (long long)S.ctr[5] : (long long)S.ptot;
     const unsigned stamp = (unsigned)S.ctr[2];
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += (long long)gridDim.x * blockDim.x)
-        decide_one(S, S.touched[i], stamp);
+    for (int seg = 0; seg < kSegs; seg++) {
+        const long long nt = min((long long)S.ctr[kSegTouched + seg], S.tcap);
+        const int *t = S.touched + (size_t)seg * (size_t)S.tcap;
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += (long long)gridDim.x * blockDim.x)
+            decide_one(S, t[i], stamp);
+    }
 }
 
 // ------------------------------------------------------------------ larger clusters

@@ -434,6 +434,17 @@ __device__ __forceinline__ int patch_of(const BindRep &B, const Model<real> &M, 
     return B.patch_off + B.pbase[t] + (li - (t ? M.ncum[t - 1] : 0)) * M.np[t] + c;
 }
 
+// replica of global patch wp (binary search over the replicas' first patches)
+__device__ __forceinline__ int patch_replica(const BindRep *reps, int nrep, int wp) {
+    int lo = 0, hi = nrep;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (reps[mid].patch_off <= wp) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 // GeneralPatch::which_particle: local particle, type and patch number of local patch lp
 template <class real>
 __device__ __forceinline__ void patch_owner(const BindRep &B, const Model<real> &M, int lp, int &li, int &t, int &c) {
@@ -478,8 +489,10 @@ struct ForceArgs {
     const int *bind_to;
     unsigned long long *bind_deg;
     int2 *bind_adj;
-    unsigned long long *bind_ctr;    // [2] stamp, [5] patches with an edge so far (bind_touched)
-    int *bind_touched;
+    unsigned long long *bind_ctr;    // [2] stamp; segment counters of the update's lists (kSegTouched, ...)
+    int *bind_touched;               // patches with an edge this update, kSegs segments of bind_tcap
+    long long bind_tcap;
+    int bind_listed;                 // bound-pair forces summed by a pair kernel, not by the epilogue
 };
 
 // ------------------------------------------------------------------ single-bond mode: bond candidates
@@ -626,14 +639,26 @@ __device__ __forceinline__ int adj_take(unsigned long long *deg, int p, unsigned
     return kAdjCap;
 }
 
-// a patch's first edge of this update puts it on the touched list (the patches the decisions visit)
-__device__ __forceinline__ void touch(int *touched, unsigned long long *count, int p) {
+// Lists built during a pass (pairs for the edge pass, touched patches, bound pairs) are split into kSegs
+// segments, each with its own counter, chosen by warp: appends from different warps rarely meet on one
+// address.  Segment k holds entries [k * cap, k * cap + count[k]).
+constexpr int kSegs = 64;
+constexpr int kSegPairs = 8;                   // bind_ctr offsets of the segment counters
+constexpr int kSegTouched = kSegPairs + kSegs;
+constexpr int kSegBound = kSegTouched + kSegs;
+constexpr int kBindCounters = kSegBound + kSegs;
+
+template <class T>
+__device__ __forceinline__ void seg_append(T *list, unsigned long long *counts, long long cap, const T &e,
+                                           unsigned *flags) {
     namespace cg = cooperative_groups;
     cg::coalesced_group g = cg::coalesced_threads();
+    const int k = (int)((blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) & (kSegs - 1));
     unsigned long long base = 0;
-    if (g.thread_rank() == 0) base = atomicAdd(count, (unsigned long long)g.size());
+    if (g.thread_rank() == 0) base = atomicAdd(counts + k, (unsigned long long)g.size());
     base = g.shfl(base, 0) + g.thread_rank();
-    touched[base] = p;   // at most one entry per patch: base < total patches
+    if ((long long)base < cap) list[(size_t)k * (size_t)cap + base] = e;
+    else atomicOr(flags, kFlagBind);
 }
 
 template <class real>
@@ -643,8 +668,8 @@ __device__ __forceinline__ void add_edge_t(const ForceArgs<real> &a, int w1, int
     else atomicOr(a.flags, kFlagBind);
     if (k2 < kAdjCap) a.bind_adj[(size_t)w2 * kAdjCap + k2] = make_int2(w1, cls);
     else atomicOr(a.flags, kFlagBind);
-    if (k1 == 0) touch(a.bind_touched, a.bind_ctr + 5, w1);
-    if (k2 == 0) touch(a.bind_touched, a.bind_ctr + 5, w2);
+    if (k1 == 0) seg_append<int>(a.bind_touched, a.bind_ctr + kSegTouched, a.bind_tcap, w1, a.flags);
+    if (k2 == 0) seg_append<int>(a.bind_touched, a.bind_ctr + kSegTouched, a.bind_tcap, w2, a.flags);
 }
 
 // One patch pair (patch ka of particle s1, kb of s2; s1 the lower particle index) with cosines c1, c2 and

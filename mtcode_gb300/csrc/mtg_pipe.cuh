@@ -168,18 +168,6 @@ __device__ __forceinline__ void fixed_add(long long *acc, float v) {
     if (v != 0.f) atomicAdd(reinterpret_cast<unsigned long long *>(acc), (unsigned long long)to_fixed(v));
 }
 
-// warp-aggregated append of one entry to a list with a 64-bit counter; false (and the flag) when full
-__device__ __forceinline__ void list_append(int2 *list, unsigned long long *count, long long cap, int2 e,
-                                            unsigned *flags) {
-    namespace cg = cooperative_groups;
-    cg::coalesced_group g = cg::coalesced_threads();
-    unsigned long long base = 0;
-    if (g.thread_rank() == 0) base = atomicAdd(count, (unsigned long long)g.size());
-    base = g.shfl(base, 0) + g.thread_rank();
-    if ((long long)base < cap) list[base] = e;
-    else atomicOr(flags, kFlagBind);
-}
-
 // forces and torques of the listed pairs into acc (6 fixed-point sums per slot: F lab, T lab).  BIND
 // (single-bond mode, a bond-deciding pass): pairs where both particles have a patch near a cone along the
 // pair go, in canonical order (lower particle index first), to bind_list for bind_pairs_kernel.
@@ -187,7 +175,7 @@ template <bool BIND>
 __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<float> a, const int2 *pairs,
                                                                  const unsigned long long *npairs, long long cap,
                                                                  long long *acc, int2 *bind_list = nullptr,
-                                                                 unsigned long long *bind_n = nullptr) {
+                                                                 long long bind_cap = 0) {
     const long long n = (long long)*npairs < cap ? (long long)*npairs : cap;
     bool big = false;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
@@ -237,7 +225,9 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
                         const float *v = M.orient[M.ooff[tb] + k];
                         anyb |= v[0] * w[0] + v[1] * w[1] + v[2] * w[2] > pre;
                     }
-                    if (anyb) list_append(bind_list, bind_n, cap, ida < idb ? make_int2(sa, sb) : make_int2(sb, sa), a.flags);
+                    if (anyb)
+                        seg_append<int2>(bind_list, a.bind_ctr + kSegPairs, bind_cap,
+                                         ida < idb ? make_int2(sa, sb) : make_int2(sb, sa), a.flags);
                 }
             }
         }
@@ -300,14 +290,15 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
 // single-bond mode, a bond-deciding pass: this update's edges of the pairs pairforce_kernel<true> listed
 // (canonical order, both particles with a patch near a cone).  A warp takes 32 of them and works through
 // them one at a time, one patch pair per lane.
-__global__ void __launch_bounds__(kPipeThreads) bind_pairs_kernel(ForceArgs<float> a, const int2 *list,
-                                                                const unsigned long long *nlist, long long cap) {
-    const long long n = (long long)*nlist < cap ? (long long)*nlist : cap;
+__global__ void __launch_bounds__(kPipeThreads) bind_pairs_kernel(ForceArgs<float> a, const int2 *list_all,
+                                                                long long cap) {
     const int lane = threadIdx.x & 31;
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     const unsigned stamp = (unsigned)a.bind_ctr[2];
-    for (long long base = warp * 32; base < n; base += nwarps * 32) {
+    for (int seg = 0; seg < kSegs; seg++)
+    for (long long base = warp * 32, n = min((long long)a.bind_ctr[kSegPairs + seg], cap); base < n; base += nwarps * 32) {
+        const int2 *list = list_all + (size_t)seg * (size_t)cap;
         const long long q = base + lane;
         int s1 = 0, s2 = 0, li1 = 0, li2 = 0, ty1 = 0, ty2 = 0, r = 0, t0 = 1;
         float w1[3] = {0.f, 0.f, 0.f}, w2[3] = {0.f, 0.f, 0.f}, rr = 1.f;
@@ -372,6 +363,63 @@ __global__ void __launch_bounds__(kPipeThreads) bind_pairs_kernel(ForceArgs<floa
     }
 }
 
+// single-bond mode, a bond-deciding pass: KernFrenkelOnePatch2::force_and_torque of every pair bound by this
+// update's decisions (LangevinRforce.cpp:3940-4030), one thread per pair, into the fixed-point sums of both
+// particles (the epilogue then leaves bound pairs alone)
+__global__ void __launch_bounds__(kPipeThreads) bound_pairs_kernel(ForceArgs<float> a, const int2 *list_all,
+                                                                 long long cap, long long *acc) {
+    for (int seg = 0; seg < kSegs; seg++) {
+        const long long n = min((long long)a.bind_ctr[kSegBound + seg], cap);
+        const int2 *list = list_all + (size_t)seg * (size_t)cap;
+        for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+            const int2 e = list[q];
+            const int rp = patch_replica(a.bind_reps, a.tb.nrep, e.x);
+            const Replica<float> &R = a.tb.reps[rp];
+            const BindRep &B = a.bind_reps[rp];
+            const Model<float> &M = a.tb.models[R.model];
+            int l1, t1, k1, l2, t2, k2;
+            patch_owner<float>(B, M, e.x - B.patch_off, l1, t1, k1);
+            patch_owner<float>(B, M, e.y - B.patch_off, l2, t2, k2);
+            if (l2 < l1) {
+                int t;
+                t = l1; l1 = l2; l2 = t;
+                t = t1; t1 = t2; t2 = t;
+                t = k1; k1 = k2; k2 = t;
+            }
+            const int s1 = a.buf.slot_of[R.off + l1], s2 = a.buf.slot_of[R.off + l2];
+            Payload<float> P1, P2;
+            P1.load(a.buf.pos, a.buf.rota, a.buf.rotb, s1);
+            P2.load(a.buf.pos, a.buf.rota, a.buf.rotb, s2);
+            const float dx = min_image<float>(P1.v[0] - P2.v[0], R.box, R.l2s, R.periodic);
+            const float dy = min_image<float>(P1.v[1] - P2.v[1], R.box, R.l2s, R.periodic);
+            const float dz = min_image<float>(P1.v[2] - P2.v[2], R.box, R.l2s, R.periodic);
+            const float rr = sqrtf(dx * dx + dy * dy + dz * dz);
+            const int qp = M.pstart[t1][t2] + k1 * M.np[t2] + k2;
+            if (rr > M.rmax[qp]) continue;
+            const float u[3] = {dx / rr, dy / rr, dz / rr};
+            const float *b1 = M.orient[M.ooff[t1] + k1], *b2 = M.orient[M.ooff[t2] + k2];
+            float n1[3], n2[3];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                n1[k] = b1[0] * P1.v[3 + k] + b1[1] * P1.v[6 + k] + b1[2] * P1.v[9 + k];
+                n2[k] = b2[0] * P2.v[3 + k] + b2[1] * P2.v[6 + k] + b2[2] * P2.v[9 + k];
+            }
+            const float ci = -(n1[0] * u[0] + n1[1] * u[1] + n1[2] * u[2]);
+            const float cj = n2[0] * u[0] + n2[1] * u[1] + n2[2] * u[2];
+            if (!(ci > M.costm[qp] && cj > M.costm[qp])) continue;
+            float f[3] = {0.f, 0.f, 0.f}, ta[3] = {0.f, 0.f, 0.f}, tb[3] = {0.f, 0.f, 0.f}, ee = 0.f;
+            kf2_pair<float>(M.att[qp], M.dis[qp], M.inv_dis[qp], M.kfac[qp], u, rr, n1, n2, ci, cj, f, ta, tb, ee);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                fixed_add(acc + 6 * (size_t)s1 + k, f[k]);
+                fixed_add(acc + 6 * (size_t)s2 + k, -f[k]);
+                fixed_add(acc + 6 * (size_t)s1 + 3 + k, ta[k]);
+                fixed_add(acc + 6 * (size_t)s2 + 3 + k, tb[k]);
+            }
+        }
+    }
+}
+
 // per particle: the summed force and torque (cleared for the next pass), bonds, then the mode's output
 template <int MODE>
 __global__ void __launch_bounds__(kPipeThreads) pair_epilogue_kernel(ForceArgs<float> a, long long *acc) {
@@ -397,7 +445,7 @@ __global__ void __launch_bounds__(kPipeThreads) pair_epilogue_kernel(ForceArgs<f
             bond_forces<float>(a, R, id, xi[0], xi[1], xi[2], F, eb, big);
             if (big) atomicOr(a.flags, 2u);
         }
-        if (a.bind_on) {
+        if (a.bind_on && !a.bind_listed) {
             Payload<float> P;
             P.load(a.buf.pos, a.buf.rota, a.buf.rotb, s);
             float eb = 0.f;

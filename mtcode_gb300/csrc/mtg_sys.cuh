@@ -252,6 +252,8 @@ struct Sys : SysBase {
     int *d_patch_slot = nullptr, *d_boundto = nullptr, *d_large = nullptr, *d_scratch = nullptr;
     int *d_touched = nullptr;
     int2 *d_bind_pairs = nullptr;   // pairs the FP32 pipeline lists for the edge pass
+    int2 *d_bound = nullptr;        // pairs bound by the decisions (FP32 pipeline)
+    long long tcap = 0, bcap = 0, lcap = 0;   // segment capacities: touched, bound, listed pairs
     int ncells_full = 0;                         // the force grid's cells outside single-bond mode
     unsigned long long *d_bctr = nullptr, *d_deg = nullptr;
     int2 *d_adj = nullptr;
@@ -477,7 +479,7 @@ struct Sys : SysBase {
     }
 
     // ---------------------------------------------------------------- single-bond-per-patch mode
-    static constexpr int kBindLaunches = 5;   // begin (+ snapshot), edges, unbind, decide, large
+    static constexpr int kBindLaunches = 6;   // begin (+ snapshot), edges, unbind, decide, large, bound pairs
 
     mtg::BindState bind_state() const {
         mtg::BindState S;
@@ -495,6 +497,9 @@ struct Sys : SysBase {
         S.isbound = d_isbound;
         S.large = d_large;
         S.touched = d_touched;
+        S.tcap = tcap;
+        S.bound = nullptr;
+        S.bcap = bcap;
         S.scratch = d_scratch;
         S.scratch_threads = scratch_threads;
         S.flags = d_flags;
@@ -513,8 +518,9 @@ struct Sys : SysBase {
     }
 
     // clusters and bond decisions from this update's edges (positions reached through slot_of)
-    void enqueue_bind_decide(const mtg::ForceArgs<real> &a) {
-        const mtg::BindState S = bind_state();
+    void enqueue_bind_decide(const mtg::ForceArgs<real> &a, bool listed) {
+        mtg::BindState S = bind_state();
+        if (listed) S.bound = d_bound;
         mtg::bind_unbind_kernel<<<grid_for(ptot, 256, occ_stream, sms), 256, 0, st>>>(S);
         mtg::bind_decide_kernel<<<grid_for(ptot, 256, 4, sms), 256, 0, st>>>(S);
         mtg::bind_large_kernel<real><<<scratch_threads / mtg::kLargeThreads, mtg::kLargeThreads, 0, st>>>(a, S);
@@ -523,9 +529,10 @@ struct Sys : SysBase {
     void free_bind() {
         cudaFree(d_brep); cudaFree(d_bmodel); cudaFree(d_patch_slot); cudaFree(d_boundto); cudaFree(d_large);
         cudaFree(d_scratch); cudaFree(d_bctr); cudaFree(d_deg); cudaFree(d_adj); cudaFree(d_isbound);
-        cudaFree(d_touched); cudaFree(d_bind_pairs);
+        cudaFree(d_touched); cudaFree(d_bind_pairs); cudaFree(d_bound);
         d_touched = nullptr;
         d_bind_pairs = nullptr;
+        d_bound = nullptr;
         d_brep = nullptr; d_bmodel = nullptr; d_patch_slot = d_boundto = d_large = d_scratch = nullptr;
         d_bctr = d_deg = nullptr; d_adj = nullptr; d_isbound = nullptr;
         for (int b = 0; b < 2; b++) {
@@ -655,7 +662,7 @@ struct Sys : SysBase {
         MTG_CUDA(cudaMalloc(&d_brep, sizeof(mtg::BindRep) * nrep));
         MTG_CUDA(cudaMalloc(&d_bmodel, sizeof(mtg::BindModel)));
         MTG_CUDA(cudaMalloc(&d_patch_slot, sizeof(int) * (nrep + 1)));
-        MTG_CUDA(cudaMalloc(&d_bctr, sizeof(unsigned long long) * 8));
+        MTG_CUDA(cudaMalloc(&d_bctr, sizeof(unsigned long long) * mtg::kBindCounters));
         const size_t nn = (size_t)std::max(ntot_, 1);
         for (int b = 0; b < 2; b++) {
             MTG_CUDA(cudaMalloc(&buf[b].snap_a, sizeof(real) * 4 * nn));
@@ -667,13 +674,21 @@ struct Sys : SysBase {
         MTG_CUDA(cudaMalloc(&d_boundto, sizeof(int) * np));
         MTG_CUDA(cudaMalloc(&d_isbound, np));
         MTG_CUDA(cudaMalloc(&d_large, sizeof(int) * np));
-        MTG_CUDA(cudaMalloc(&d_touched, sizeof(int) * np));
-        if (use_pipe) MTG_CUDA(cudaMalloc(&d_bind_pairs, sizeof(int2) * (size_t)std::max<long long>(pair_cap, 1)));
+        // segment capacities: twice the even share of each list's bound (the warp-chosen segments fill
+        // evenly), at least 1024 entries
+        tcap = std::max<long long>(1024, 2 * ((long long)np + mtg::kSegs - 1) / mtg::kSegs);
+        bcap = std::max<long long>(1024, 2 * ((long long)np / 2 + mtg::kSegs - 1) / mtg::kSegs);
+        lcap = std::max<long long>(1024, 2 * (pair_cap + mtg::kSegs - 1) / mtg::kSegs);
+        MTG_CUDA(cudaMalloc(&d_touched, sizeof(int) * (size_t)tcap * mtg::kSegs));
+        if (use_pipe) {
+            MTG_CUDA(cudaMalloc(&d_bind_pairs, sizeof(int2) * (size_t)lcap * mtg::kSegs));
+            MTG_CUDA(cudaMalloc(&d_bound, sizeof(int2) * (size_t)bcap * mtg::kSegs));
+        }
         MTG_CUDA(cudaMalloc(&d_scratch, sizeof(int) * (size_t)mtg::kScratchInts * scratch_threads));
         MTG_CUDA(cudaMemcpy(d_brep, br.data(), sizeof(mtg::BindRep) * nrep, cudaMemcpyHostToDevice));
         MTG_CUDA(cudaMemcpy(d_bmodel, &hm, sizeof(hm), cudaMemcpyHostToDevice));
         MTG_CUDA(cudaMemcpy(d_patch_slot, pslot.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice));
-        MTG_CUDA(cudaMemset(d_bctr, 0, sizeof(unsigned long long) * 8));
+        MTG_CUDA(cudaMemset(d_bctr, 0, sizeof(unsigned long long) * mtg::kBindCounters));
         MTG_CUDA(cudaMemset(d_deg, 0, sizeof(unsigned long long) * np));
         MTG_CUDA(cudaMemset(d_boundto, 0, sizeof(int) * np));
         MTG_CUDA(cudaMemset(d_isbound, 0, np));
@@ -770,15 +785,18 @@ struct Sys : SysBase {
     void launch_force(const mtg::ForceArgs<real> &a0, bool bind = false, cudaEvent_t *bind_ev = nullptr) {
         mtg::ForceArgs<real> a = a0;
         bind = bind && single_bond;
+        const bool listed = bind && use_pipe && MODE != mtg::kModeObs && !a.outE;
         if (bind) {
             a.bind_deg = d_deg;
             a.bind_adj = d_adj;
             a.bind_ctr = d_bctr;
             a.bind_touched = d_touched;
+            a.bind_tcap = tcap;
+            a.bind_listed = listed ? 1 : 0;
         }
         auto decide = [&]() {
             if (bind_ev) MTG_CUDA(cudaEventRecord(bind_ev[0], st));
-            enqueue_bind_decide(a);
+            enqueue_bind_decide(a, listed);
             if (bind_ev) MTG_CUDA(cudaEventRecord(bind_ev[1], st));
         };
         if constexpr (std::is_same<real, float>::value) {
@@ -792,9 +810,10 @@ struct Sys : SysBase {
                                                                                   skin > 0 ? 1 : 0, gate);
                 if (bind) {
                     mtg::pairforce_kernel<true><<<sms * 16, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap,
-                                                                                      d_acc, d_bind_pairs, d_bctr + 6);
-                    mtg::bind_pairs_kernel<<<sms * 8, mtg::kPipeThreads, 0, st>>>(a, d_bind_pairs, d_bctr + 6, pair_cap);
+                                                                                      d_acc, d_bind_pairs, lcap);
+                    mtg::bind_pairs_kernel<<<sms * 8, mtg::kPipeThreads, 0, st>>>(a, d_bind_pairs, lcap);
                     decide();
+                    mtg::bound_pairs_kernel<<<sms * 4, mtg::kPipeThreads, 0, st>>>(a, d_bound, bcap, d_acc);
                 } else {
                     mtg::pairforce_kernel<false><<<sms * 16, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap, d_acc);
                 }
