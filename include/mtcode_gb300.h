@@ -52,9 +52,13 @@ typedef enum { MTG_FP32 = 0, MTG_FP64 = 1 } mtg_precision;
 #define MTG_FLAG_TIMEOUT     0x4u   /* a bounded device wait expired (see MTG_ERR_TIMEOUT) */
 #define MTG_FLAG_OVERFLOW    0x8u   /* a tile's pair list overflowed: handled by the per-particle path */
 #define MTG_FLAG_BINNING     0x10u  /* the cell histogram disagreed with the particle count: step skipped */
-#define MTG_FLAG_BIND        0x20u  /* single-bond mode: the candidate list, a patch's candidate partners (8)
-                                       or a patch cluster (128 patches) outgrew its capacity, or a cluster
-                                       reached one of the reference's error() paths */
+#define MTG_FLAG_BIND        0x20u  /* single-bond mode: a capacity was exceeded or a cluster reached one of
+                                       the reference's error() paths; one of the reasons below is set too */
+#define MTG_BIND_WHY_ADJ     0x10000u  /* a patch had more than 8 candidate partners in one update */
+#define MTG_BIND_WHY_CLUSTER 0x20000u  /* a patch cluster had more than 128 patches */
+#define MTG_BIND_WHY_LIST    0x40000u  /* a list of the force pass (pairs, patches, bound pairs) was full */
+#define MTG_BIND_WHY_REF     0x80000u  /* a cluster reached one of the reference's error() paths */
+#define MTG_BIND_WHY_SPIN    0x100000u /* an atomic retry loop reached its bound */
 
 typedef struct mtg_system mtg_system;
 

@@ -66,6 +66,17 @@ struct mtg_system {
         }                                                     \
     } while (0)
 
+// the single-bond capacity that failed, from the reason bits latched with MTG_FLAG_BIND
+static std::string bind_failure(uint32_t f) {
+    std::string m = "single-bond mode:";
+    if (f & MTG_BIND_WHY_ADJ) m += " a patch had more than 8 candidate partners;";
+    if (f & MTG_BIND_WHY_CLUSTER) m += " a patch cluster exceeded 128 patches;";
+    if (f & MTG_BIND_WHY_LIST) m += " a list of the force pass was full;";
+    if (f & MTG_BIND_WHY_REF) m += " a cluster reached one of the reference's error() paths;";
+    if (f & MTG_BIND_WHY_SPIN) m += " an atomic retry loop reached its bound;";
+    return m;
+}
+
 extern "C" {
 
 int mtg_api_version(void) { return MTG_API_VERSION; }
@@ -293,9 +304,7 @@ mtg_status mtg_sync(mtg_system *h) {
         const uint32_t f = h->impl->flags();
         if (f & MTG_FLAG_TIMEOUT) throw Fail{MTG_ERR_TIMEOUT, "a bounded device wait expired"};
         if (f & MTG_FLAG_BINNING) throw Fail{MTG_ERR_STATE, "cell binning incomplete: a step was skipped"};
-        if (f & MTG_FLAG_BIND)
-            throw Fail{MTG_ERR_CAPACITY, "single-bond mode: a candidate list, candidate partners of a patch (8) or "
-                                         "a patch cluster (128) exceeded its capacity"};
+        if (f & MTG_FLAG_BIND) throw Fail{MTG_ERR_CAPACITY, bind_failure(f)};
         if (f & MTG_FLAG_NONFINITE) return MTG_ERR_NONFINITE;
     });
     return MTG_OK;
@@ -323,9 +332,8 @@ mtg_status mtg_get_bind_state(mtg_system *h, int32_t *boundto, uint8_t *isbound)
 mtg_status mtg_bind_update(mtg_system *h, double *F, double *T) {
     MTG_GUARD(h, {
         h->impl->bind_update(F, T);
-        if (h->impl->flags() & MTG_FLAG_BIND)
-            throw Fail{MTG_ERR_CAPACITY, "single-bond mode: a candidate list, candidate partners of a patch (8) or "
-                                         "a patch cluster (128) exceeded its capacity"};
+        const uint32_t f = h->impl->flags();
+        if (f & MTG_FLAG_BIND) throw Fail{MTG_ERR_CAPACITY, bind_failure(f)};
     });
     return MTG_OK;
 }

@@ -308,20 +308,18 @@ __device__ __forceinline__ void decide_one(const BindState &S, int p, unsigned s
     bool c[3];
     const int d1 = adj_count(S.deg, s[0], stamp);
     if (!triplet_links(d1, S.adj[(size_t)s[0] * kAdjCap].x, adj_count(S.deg, s[1], stamp), s[1], s[2], c)) {
-        atomicOr(S.flags, kFlagBind);
+        atomicOr(S.flags, kFlagBind | kBindWhyRef);
         return;
     }
     apply_triplet(S, mod, B.patch_off, s[0], s[1], s[2], c, ran);
 }
 
 __global__ void __launch_bounds__(256) bind_decide_kernel(BindState S) {
+    __shared__ long long segs[kSegs + 1];
+    seg_prefix(S.ctr + kSegTouched, S.tcap, segs);
     const unsigned stamp = (unsigned)S.ctr[2];
-    for (int seg = 0; seg < kSegs; seg++) {
-        const long long nt = min((long long)S.ctr[kSegTouched + seg], S.tcap);
-        const int *t = S.touched + (size_t)seg * (size_t)S.tcap;
-        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += (long long)gridDim.x * blockDim.x)
-            decide_one(S, t[i], stamp);
-    }
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < segs[kSegs]; i += (long long)gridDim.x * blockDim.x)
+        decide_one(S, S.touched[seg_slot(segs, S.tcap, i)], stamp);
 }
 
 // ------------------------------------------------------------------ larger clusters
@@ -364,7 +362,7 @@ __global__ void __launch_bounds__(kLargeThreads) bind_large_kernel(ForceArgs<rea
         }
         if (lo != p) continue;
         if (over) {
-            atomicOr(S.flags, kFlagBind);
+            atomicOr(S.flags, kFlagBind | kBindWhyCluster);
             continue;
         }
         // members in increasing order (SingleHistogram, GraphAlgorithms.cpp:2-48)
@@ -443,7 +441,7 @@ __global__ void __launch_bounds__(kLargeThreads) bind_large_kernel(ForceArgs<rea
             nbx[3 * eb[q] + lens[eb[q]]++] = ea[q];
         }
         if (bad) {
-            atomicOr(S.flags, kFlagBind);
+            atomicOr(S.flags, kFlagBind | kBindWhyRef);
             continue;
         }
         for (int v = 0; v < nm; v++) {
@@ -471,14 +469,14 @@ __global__ void __launch_bounds__(kLargeThreads) bind_large_kernel(ForceArgs<rea
             } else if (np_ == 3) {
                 bool c[3];
                 if (!triplet_links(lens[pm[0]], nbx[3 * pm[0]], lens[pm[1]], pm[1], pm[2], c)) {
-                    atomicOr(S.flags, kFlagBind);
+                    atomicOr(S.flags, kFlagBind | kBindWhyRef);
                     break;
                 }
                 apply_triplet(S, mod, B.patch_off, mem[pm[0]], mem[pm[1]], mem[pm[2]], c,
                               bind_uniform(B, r, S.draw[0], p - B.patch_off, it));
                 it++;
             } else {
-                atomicOr(S.flags, kFlagBind);
+                atomicOr(S.flags, kFlagBind | kBindWhyRef);
                 break;
             }
         }

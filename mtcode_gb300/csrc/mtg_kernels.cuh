@@ -504,7 +504,12 @@ struct ForceArgs {
 // pair that passes the current test is checked against the list's condition on the snapshot.  Every test is
 // the reference's FP64 expression in its operation order; float evaluations decide only outside a margin.
 constexpr int kAdjCap = 8;            // candidate partners of one patch in one update
-constexpr unsigned kFlagBind = 0x20u; // a capacity of this mode was exceeded (MTG_FLAG_BIND)
+constexpr unsigned kFlagBind = 0x20u; // a capacity of this mode was exceeded (MTG_FLAG_BIND), with one of:
+constexpr unsigned kBindWhyAdj = 1u << 16;      // a patch had more than kAdjCap candidate partners
+constexpr unsigned kBindWhyCluster = 1u << 17;  // a patch cluster exceeded the large-cluster capacity
+constexpr unsigned kBindWhyList = 1u << 18;     // a segment of a pass's list was full
+constexpr unsigned kBindWhyRef = 1u << 19;      // a cluster reached one of the reference's error() paths
+constexpr unsigned kBindWhySpin = 1u << 20;     // an atomic retry loop reached its bound
 
 // cube::distance_vector (geometry.h:277-294): un = x_a - x_b (minimum image), returns |un|^2
 __device__ __forceinline__ double exact_dist_vec(const BindRep &B, const double xa[3], const double xb[3], double un[3]) {
@@ -635,7 +640,7 @@ __device__ __forceinline__ int adj_take(unsigned long long *deg, int p, unsigned
         if (prev == old) return (int)cnt;
         old = prev;
     }
-    atomicOr(flags, kFlagBind);
+    atomicOr(flags, kFlagBind | kBindWhySpin);
     return kAdjCap;
 }
 
@@ -648,6 +653,31 @@ constexpr int kSegTouched = kSegPairs + kSegs;
 constexpr int kSegBound = kSegTouched + kSegs;
 constexpr int kBindCounters = kSegBound + kSegs;
 
+// A kernel that reads a segmented list first lays its segments end to end: seg_prefix (every thread of the
+// block, before any early exit) leaves the exclusive prefix of the segment lengths in shared memory, and
+// seg_slot maps an index below sh[kSegs] to its entry.
+__device__ __forceinline__ void seg_prefix(const unsigned long long *counts, long long cap, long long *sh) {
+    if (threadIdx.x == 0) {
+        long long t = 0;
+        for (int k = 0; k < kSegs; k++) {
+            sh[k] = t;
+            const long long c = (long long)counts[k];
+            t += c < cap ? c : cap;
+        }
+        sh[kSegs] = t;
+    }
+    __syncthreads();
+}
+__device__ __forceinline__ size_t seg_slot(const long long *sh, long long cap, long long i) {
+    int lo = 0, hi = kSegs;   // sh[lo] <= i < sh[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (sh[mid] <= i) lo = mid;
+        else hi = mid;
+    }
+    return (size_t)lo * (size_t)cap + (size_t)(i - sh[lo]);
+}
+
 template <class T>
 __device__ __forceinline__ void seg_append(T *list, unsigned long long *counts, long long cap, const T &e,
                                            unsigned *flags) {
@@ -658,16 +688,16 @@ __device__ __forceinline__ void seg_append(T *list, unsigned long long *counts, 
     if (g.thread_rank() == 0) base = atomicAdd(counts + k, (unsigned long long)g.size());
     base = g.shfl(base, 0) + g.thread_rank();
     if ((long long)base < cap) list[(size_t)k * (size_t)cap + base] = e;
-    else atomicOr(flags, kFlagBind);
+    else atomicOr(flags, kFlagBind | kBindWhyList);
 }
 
 template <class real>
 __device__ __forceinline__ void add_edge_t(const ForceArgs<real> &a, int w1, int w2, int cls, unsigned stamp) {
     const int k1 = adj_take(a.bind_deg, w1, stamp, a.flags), k2 = adj_take(a.bind_deg, w2, stamp, a.flags);
     if (k1 < kAdjCap) a.bind_adj[(size_t)w1 * kAdjCap + k1] = make_int2(w2, cls);
-    else atomicOr(a.flags, kFlagBind);
+    else atomicOr(a.flags, kFlagBind | kBindWhyAdj);
     if (k2 < kAdjCap) a.bind_adj[(size_t)w2 * kAdjCap + k2] = make_int2(w1, cls);
-    else atomicOr(a.flags, kFlagBind);
+    else atomicOr(a.flags, kFlagBind | kBindWhyAdj);
     if (k1 == 0) seg_append<int>(a.bind_touched, a.bind_ctr + kSegTouched, a.bind_tcap, w1, a.flags);
     if (k2 == 0) seg_append<int>(a.bind_touched, a.bind_ctr + kSegTouched, a.bind_tcap, w2, a.flags);
 }

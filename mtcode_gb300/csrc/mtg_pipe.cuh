@@ -292,19 +292,20 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
 // them one at a time, one patch pair per lane.
 __global__ void __launch_bounds__(kPipeThreads) bind_pairs_kernel(ForceArgs<float> a, const int2 *list_all,
                                                                 long long cap) {
+    __shared__ long long segs[kSegs + 1];
+    seg_prefix(a.bind_ctr + kSegPairs, cap, segs);
+    const long long n = segs[kSegs];
     const int lane = threadIdx.x & 31;
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     const unsigned stamp = (unsigned)a.bind_ctr[2];
-    for (int seg = 0; seg < kSegs; seg++)
-    for (long long base = warp * 32, n = min((long long)a.bind_ctr[kSegPairs + seg], cap); base < n; base += nwarps * 32) {
-        const int2 *list = list_all + (size_t)seg * (size_t)cap;
+    for (long long base = warp * 32; base < n; base += nwarps * 32) {
         const long long q = base + lane;
         int s1 = 0, s2 = 0, li1 = 0, li2 = 0, ty1 = 0, ty2 = 0, r = 0, t0 = 1;
         float w1[3] = {0.f, 0.f, 0.f}, w2[3] = {0.f, 0.f, 0.f}, rr = 1.f;
         const bool live = q < n;
         if (live) {
-            const int2 pr = list[q];
+            const int2 pr = list_all[seg_slot(segs, cap, q)];
             s1 = pr.x;
             s2 = pr.y;
             r = find_replica(a.tb.rep_slot, a.tb.nrep, s1);
@@ -368,11 +369,12 @@ __global__ void __launch_bounds__(kPipeThreads) bind_pairs_kernel(ForceArgs<floa
 // particles (the epilogue then leaves bound pairs alone)
 __global__ void __launch_bounds__(kPipeThreads) bound_pairs_kernel(ForceArgs<float> a, const int2 *list_all,
                                                                  long long cap, long long *acc) {
-    for (int seg = 0; seg < kSegs; seg++) {
-        const long long n = min((long long)a.bind_ctr[kSegBound + seg], cap);
-        const int2 *list = list_all + (size_t)seg * (size_t)cap;
+    __shared__ long long segs[kSegs + 1];
+    seg_prefix(a.bind_ctr + kSegBound, cap, segs);
+    const long long n = segs[kSegs];
+    {
         for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-            const int2 e = list[q];
+            const int2 e = list_all[seg_slot(segs, cap, q)];
             const int rp = patch_replica(a.bind_reps, a.tb.nrep, e.x);
             const Replica<float> &R = a.tb.reps[rp];
             const BindRep &B = a.bind_reps[rp];
