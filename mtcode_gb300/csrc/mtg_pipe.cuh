@@ -288,77 +288,52 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
 }
 
 // single-bond mode, a bond-deciding pass: this update's edges of the pairs pairforce_kernel<true> listed
-// (canonical order, both particles with a patch near a cone).  A warp takes 32 of them and works through
-// them one at a time, one patch pair per lane.
+// (canonical order, both particles with a patch near a cone), one pair per thread: every listed pair has
+// passed the cone pre-test, so the lanes of a warp run the patch-pair loop together and overlap the
+// bond-state, snapshot and adjacency accesses of their pairs.
 __global__ void __launch_bounds__(kPipeThreads) bind_pairs_kernel(ForceArgs<float> a, const int2 *list_all,
                                                                 long long cap) {
     __shared__ long long segs[kSegs + 1];
     seg_prefix(a.bind_ctr + kSegPairs, cap, segs);
     const long long n = segs[kSegs];
-    const int lane = threadIdx.x & 31;
-    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     const unsigned stamp = (unsigned)a.bind_ctr[2];
-    for (long long base = warp * 32; base < n; base += nwarps * 32) {
-        const long long q = base + lane;
-        int s1 = 0, s2 = 0, li1 = 0, li2 = 0, ty1 = 0, ty2 = 0, r = 0, t0 = 1;
-        float w1[3] = {0.f, 0.f, 0.f}, w2[3] = {0.f, 0.f, 0.f}, rr = 1.f;
-        const bool live = q < n;
-        if (live) {
-            const int2 pr = list_all[seg_slot(segs, cap, q)];
-            s1 = pr.x;
-            s2 = pr.y;
-            r = find_replica(a.tb.rep_slot, a.tb.nrep, s1);
-            const Replica<float> &R = a.tb.reps[r];
-            const BindRep &B = a.bind_reps[r];
-            const Model<float> &M = a.tb.models[R.model];
-            float x1[4], x2[4];
-            load4(a.buf.pos + 4 * (size_t)s1, x1);
-            load4(a.buf.pos + 4 * (size_t)s2, x2);
-            const float d[3] = {min_image<float>(x1[0] - x2[0], R.box, R.l2s, R.periodic),
-                                min_image<float>(x1[1] - x2[1], R.box, R.l2s, R.periodic),
-                                min_image<float>(x1[2] - x2[2], R.box, R.l2s, R.periodic)};
-            const float r2 = sep_r2(d[0], d[1], d[2]);
-            t0 = side_of<float>(r2, B.mk2_lo, B.mk2_hi);
-            li1 = __ldg(a.buf.ident + s1) - R.off;
-            li2 = __ldg(a.buf.ident + s2) - R.off;
-            ty1 = type_of<float>(M, li1);
-            ty2 = type_of<float>(M, li2);
-            rr = sqrtf(r2);
-            const float u[3] = {d[0] / rr, d[1] / rr, d[2] / rr};
-            float Q[9];
-            load_q(a, s1, x1[3], Q);
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int2 pr = list_all[seg_slot(segs, cap, q)];
+        const int s1 = pr.x, s2 = pr.y;
+        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, s1);
+        const Replica<float> &R = a.tb.reps[r];
+        const BindRep &B = a.bind_reps[r];
+        const Model<float> &M = a.tb.models[R.model];
+        float x1[4], x2[4];
+        load4(a.buf.pos + 4 * (size_t)s1, x1);
+        load4(a.buf.pos + 4 * (size_t)s2, x2);
+        const float d[3] = {min_image<float>(x1[0] - x2[0], R.box, R.l2s, R.periodic),
+                            min_image<float>(x1[1] - x2[1], R.box, R.l2s, R.periodic),
+                            min_image<float>(x1[2] - x2[2], R.box, R.l2s, R.periodic)};
+        const float r2 = sep_r2(d[0], d[1], d[2]);
+        const int t0 = side_of<float>(r2, B.mk2_lo, B.mk2_hi);
+        if (t0 > 0) continue;
+        const int li1 = __ldg(a.buf.ident + s1) - R.off, li2 = __ldg(a.buf.ident + s2) - R.off;
+        const int ty1 = type_of<float>(M, li1), ty2 = type_of<float>(M, li2);
+        const float rr = sqrtf(r2), u[3] = {d[0] / rr, d[1] / rr, d[2] / rr};
+        float Q[9], w1[3], w2[3];
+        load_q(a, s1, x1[3], Q);
 #pragma unroll
-            for (int k = 0; k < 3; k++) w1[k] = Q[3 * k] * u[0] + Q[3 * k + 1] * u[1] + Q[3 * k + 2] * u[2];
-            load_q(a, s2, x2[3], Q);
+        for (int k = 0; k < 3; k++) w1[k] = Q[3 * k] * u[0] + Q[3 * k + 1] * u[1] + Q[3 * k + 2] * u[2];
+        load_q(a, s2, x2[3], Q);
 #pragma unroll
-            for (int k = 0; k < 3; k++) w2[k] = Q[3 * k] * u[0] + Q[3 * k + 1] * u[1] + Q[3 * k + 2] * u[2];
-        }
-        unsigned m = __ballot_sync(0xffffffffu, live && t0 <= 0);
-        while (m) {
-            const int src = __ffs(m) - 1;
-            m &= m - 1;
-            const int p1 = __shfl_sync(0xffffffffu, s1, src), p2 = __shfl_sync(0xffffffffu, s2, src);
-            const int l1 = __shfl_sync(0xffffffffu, li1, src), l2 = __shfl_sync(0xffffffffu, li2, src);
-            const int y1 = __shfl_sync(0xffffffffu, ty1, src), y2 = __shfl_sync(0xffffffffu, ty2, src);
-            const int rp = __shfl_sync(0xffffffffu, r, src), tt = __shfl_sync(0xffffffffu, t0, src);
-            const float dist = __shfl_sync(0xffffffffu, rr, src);
-            float v1[3], v2[3];
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                v1[k] = __shfl_sync(0xffffffffu, w1[k], src);
-                v2[k] = __shfl_sync(0xffffffffu, w2[k], src);
-            }
-            const Replica<float> &R = a.tb.reps[rp];
-            const BindRep &B = a.bind_reps[rp];
-            const Model<float> &M = a.tb.models[R.model];
-            const int na = M.np[y1], nb = M.np[y2];
-            for (int pp = lane; pp < na * nb; pp += 32) {
-                const int ka = pp / nb, kb = pp - ka * nb;
-                const float *va = M.orient[M.ooff[y1] + ka], *vb = M.orient[M.ooff[y2] + kb];
-                const float c1 = -(va[0] * v1[0] + va[1] * v1[1] + va[2] * v1[2]);
-                const float c2 = vb[0] * v2[0] + vb[1] * v2[1] + vb[2] * v2[2];
-                bind_patch_edge<float>(a, B, R, M, p1, p2, l1, l2, y1, y2, ka, kb, c1, c2, dist, tt, stamp);
+        for (int k = 0; k < 3; k++) w2[k] = Q[3 * k] * u[0] + Q[3 * k + 1] * u[1] + Q[3 * k + 2] * u[2];
+        const float pre = M.mincos[ty1][ty2] - 4e-5f;
+        const int na = M.np[ty1], nb = M.np[ty2];
+        for (int ka = 0; ka < na; ka++) {
+            const float *va = M.orient[M.ooff[ty1] + ka];
+            const float c1 = -(va[0] * w1[0] + va[1] * w1[1] + va[2] * w1[2]);
+            if (!(c1 > pre)) continue;
+            for (int kb = 0; kb < nb; kb++) {
+                const float *vb = M.orient[M.ooff[ty2] + kb];
+                const float c2 = vb[0] * w2[0] + vb[1] * w2[1] + vb[2] * w2[2];
+                if (!(c2 > pre)) continue;
+                bind_patch_edge<float>(a, B, R, M, s1, s2, li1, li2, ty1, ty2, ka, kb, c1, c2, rr, t0, stamp);
             }
         }
     }
