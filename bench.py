@@ -41,6 +41,12 @@ BYTES_SCATTER = 8 + 4 + 48 + 48 + 4 + 24 + 48 + 24 + 4 + 24  # bin,start,row,row
 BYTES_SCAN_PER_CELL = 16
 
 
+def metric_of(args) -> str:
+    if args.single_bond:
+        return "particle-steps/s on 1 GB300, single-bond-per-patch step (run_singlebond), batched FP32"
+    return METRIC
+
+
 def peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -151,9 +157,10 @@ def make_workload(args, rank: int):
 
 
 # ---------------------------------------------------------------- CPU side (oracle port)
-def cpu_sample_rate(W, n_reps: int, steps: int, threads: int) -> dict:
+def cpu_sample_rate(W, n_reps: int, steps: int, threads: int, single_bond=None) -> dict:
     """Oracle port of the reference step on a bounded sample: the first n_reps replicas, `steps` steps
-    each, one replica per host thread (the reference's own scale-out is one process per system)."""
+    each, one replica per host thread (the reference's own scale-out is one process per system).  With
+    single_bond = (on, off): the run_singlebond loop with BindingModelSingle(on, off)."""
     from oracle import pyoracle as po
     po.orc()
     reps = W.replicas[:n_reps]
@@ -165,6 +172,17 @@ def cpu_sample_rate(W, n_reps: int, steps: int, threads: int) -> dict:
         a, b = offs[r], offs[r + 1]
         st = dict(x=np.ascontiguousarray(W.x[a:b]), p=np.zeros((spec.n, 3)), Lb=np.zeros((spec.n, 3)),
                   Q=np.ascontiguousarray(W.Q[a:b]))
+        if single_bond:
+            npatch = sysm.total_patches()
+            st.update(Ft=np.zeros((spec.n, 3)), Tt=np.zeros((spec.n, 3)),
+                      boundto=np.zeros(npatch, dtype=np.intc), isbound=np.zeros(npatch, dtype=np.uint8))
+            bind = po.binding_single(*single_bond)
+            sysm.run_singlebond(st, bind, 0, sysm.default_max_ang(), init=True, noise_mode=2, seed=spec.seed,
+                                replica=r, init_draw=0)
+            t0 = time.perf_counter()
+            sysm.run_singlebond(st, bind, steps, sysm.default_max_ang(), noise_mode=2, seed=spec.seed, replica=r,
+                                draw0=1)
+            return spec.n * steps, time.perf_counter() - t0
         st["Ft"], st["Tt"] = sysm.init_forces(st["x"], st["p"], st["Lb"], st["Q"])
         t0 = time.perf_counter()
         sysm.run(st, steps, noise_mode=2, seed=spec.seed, replica=r, draw0=1, check_skin=False)
@@ -178,7 +196,8 @@ def cpu_sample_rate(W, n_reps: int, steps: int, threads: int) -> dict:
     cpu_s = sum(r[1] for r in res)
     return {"value": ps / wall, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{len(reps)} of {len(W.replicas)} replicas ({ps // steps} particles) x {steps} steps, "
-                      f"one replica per thread, {cpu_s:.1f} s of CPU work"}
+                      f"one replica per thread, {cpu_s:.1f} s of CPU work"
+                      + (" (run_singlebond loop)" if single_bond else "")}
 
 
 def run_reference(args, rank, world):
@@ -191,12 +210,12 @@ def run_reference(args, rank, world):
     # each timed step advances a sample of 2 replicas per host thread by one step, in parallel
     n_reps = min(len(W.replicas), 2 * threads)
     steps = max(1, args.steps)
-    cpu_sample_rate(W, min(n_reps, threads), max(1, args.warmup), threads)  # untimed warm-up
+    cpu_sample_rate(W, min(n_reps, threads), max(1, args.warmup), threads, args.single_bond)  # untimed warm-up
     t0 = time.perf_counter()
-    cb = cpu_sample_rate(W, n_reps, steps, threads)
+    cb = cpu_sample_rate(W, n_reps, steps, threads, args.single_bond)
     elapsed = time.perf_counter() - t0
     value = cb["value"]
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+    line = {"metric": metric_of(args), "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
             "config": {"workload": f"{args.workload}: {len(W.replicas)} patchy replicas, {W.n_total} particles",
@@ -216,6 +235,9 @@ def run_gpu(args, rank, world, local):
     n = W.n_total
     z = np.zeros((n, 3))
     s = LangevinNVTRGPU(W.replicas, precision=args.precision, device=local)
+    if args.single_bond:
+        from mtcode_gb300.system import binding_single
+        s.set_single_bond(binding_single(*args.single_bond))
     s.initialize(W.x, z, z, W.Q)
     s.init_forces()
     s.step(max(args.warmup, 3))
@@ -273,18 +295,20 @@ def run_gpu(args, rank, world, local):
     cpu = None
     if rank == 0 and world == 1 and args.cpu_baseline:
         threads = os.cpu_count() or 1
-        cpu = cpu_sample_rate(W, min(len(W.replicas), args.cpu_replicas), args.cpu_steps, threads)
+        cpu = cpu_sample_rate(W, min(len(W.replicas), args.cpu_replicas), args.cpu_steps, threads, args.single_bond)
     s.close()
 
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        line = {"metric": metric_of(args), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "fp32" if args.precision == "fp32" else "f64",
                 "data": "synthetic (seeded)",
                 "config": {"workload": f"{args.workload}: {len(W.replicas)} patchy replicas, {n} particles per GPU",
                            "replicas": len(W.replicas), "particles_per_gpu": n, "precision": args.precision,
                            "l2": "inputs larger than L2 (state ~%d MB per GPU)" % (n * 250 // 2 ** 20),
-                           "parallelism": f"replicas x{world}"},
+                           "parallelism": f"replicas x{world}",
+                           "single_bond": (f"run_singlebond force pass, BindingModelSingle{tuple(args.single_bond)}"
+                                           if args.single_bond else None)},
                 "gpu_launches": launches, "clocks": clk.summary(), "roofline": roofline, "e2e": e2e,
                 "cpu_baseline": cpu, "plain_fp64": plain}
         print(json.dumps(line), flush=True)
@@ -332,6 +356,9 @@ def run_plain_fp64(W, args, device) -> dict:
         spec = W.replicas[r]
         a, b = offs[r], offs[r + 1]
         with LangevinNVTRGPU([spec], precision="fp64", device=device, track_displacement=False) as s:
+            if args.single_bond:
+                from mtcode_gb300.system import binding_single
+                s.set_single_bond(binding_single(*args.single_bond))
             z = np.zeros((spec.n, 3))
             s.initialize(W.x[a:b], z, z, W.Q[a:b])
             s.init_forces()
@@ -366,6 +393,9 @@ def main():
     ap.add_argument("--no-plain-fp64", dest="plain_fp64", action="store_false")
     ap.add_argument("--plain-replicas", type=int, default=16)
     ap.add_argument("--plain-steps", type=int, default=20)
+    ap.add_argument("--single-bond", nargs=2, type=float, metavar=("ON", "OFF"), default=None,
+                    help="time the single-bond-per-patch step (Condensate::run_singlebond's force pass) with "
+                         "BindingModelSingle(ON, OFF) instead of the full Kern-Frenkel step")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
