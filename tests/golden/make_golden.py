@@ -149,14 +149,30 @@ def analysis_cases():
 # strengths then nine asymmetries (BindingModelTernary.cpp:29-140)
 TERNARY_SETUP = [0.6, 0.5, 0.4, 0.55, 0.45, 0.35] + [0.1, -0.2, 0.3, 0.0, 0.15, -0.1, 0.2, -0.3, 0.05]
 SINGLEBOND_CASES = [
-    # (n, phi, cos thetam, periodic, seed, bm_kind, args)
+    # (n, phi, cos thetam, periodic, seed, bm_kind, args[, model]): tetrahedral unless a model is named
     (400, 0.15, 0.90, True, 11, 0, [1.0, 0.1]),
     (300, 0.30, 0.70, True, 12, 0, [0.7, 0.5]),
     (300, 0.30, 0.70, True, 13, 1, [600]),
     (300, 0.30, 0.70, True, 14, 2, [400, 900] + TERNARY_SETUP),
     (300, 0.30, 0.70, True, 15, 3, [300, 800, 3] + TERNARY_SETUP),
     (300, 0.30, 0.75, False, 16, 0, [1.0, 0.2]),
+    (300, 0.30, 0.70, True, 17, 2, [300, 700] + TERNARY_SETUP, "three_types"),
+    (300, 0.30, 0.75, True, 18, 1, [500], "tubulin"),
 ]
+
+
+def three_type_model(n: int, cosm: float) -> PatchModelSpec:
+    """GeneralPatch with three types, as the production drivers use: 4 tetrahedral patches (half the
+    particles), 2 polar patches (a third), crowders without patches; wider cones between unlike types."""
+    from mtcode_gb300.system import TETRA
+    n0, n1 = n // 2, n // 2 + n // 3
+    orient = np.vstack([TETRA, [[0, 0, 1.0], [0, 0, -1.0]]])
+    params = []
+    for (a, b), (att, dis, c) in {(0, 0): (8.0, 1.2, cosm), (0, 1): (6.0, 1.15, cosm - 0.05),
+                                  (1, 1): (7.0, 1.1, cosm + 0.05)}.items():
+        for _ in range([4, 2][a] * [4, 2][b]):
+            params.append([att, dis, math.acos(c)])
+    return PatchModelSpec([4, 2, 0], [n0, n1, n], orient, np.array(params))
 
 
 def singlebond_cases():
@@ -164,13 +180,20 @@ def singlebond_cases():
     over three rounds from an unbound start: round 1 re-decides the round-0 bonds in place, round 2 after
     new orientations (bonds break)."""
     import hashlib
-    for k, (n, phi, cosm, per, seed, kind, args) in enumerate(SINGLEBOND_CASES):
+    for k, case in enumerate(SINGLEBOND_CASES):
+        n, phi, cosm, per, seed, kind, args = case[:7]
+        model_name = case[7] if len(case) > 7 else "tetra"
         box = box_for(n, phi)
-        spec = ReplicaSpec(n=n, box=box, model=PatchModelSpec.tetrahedral(n, 8.0, 1.2, math.acos(cosm)),
-                           periodic=per, seed=seed)
+        if model_name == "three_types":
+            model = three_type_model(n, cosm)
+        elif model_name == "tubulin":
+            model = tubulin_model(n, cos_max=cosm)
+        else:
+            model = PatchModelSpec.tetrahedral(n, 8.0, 1.2, math.acos(cosm))
+        spec = ReplicaSpec(n=n, box=box, model=model, periodic=per, seed=seed)
         x = f32(random_positions(n, box, per, 0.9, 3000 + seed))
         Qs = [f32(random_rotations(n, 4000 + seed))] * 2 + [f32(random_rotations(n, 5000 + seed))]
-        npatch = 4 * n
+        npatch = po.System(spec).total_patches()
         bt = np.zeros(npatch, dtype=np.intc)
         ib = np.zeros(npatch, dtype=np.uint8)
         rec = dict(x=x, Q=np.stack(Qs), bm_kind=kind, args=np.asarray(args, float), srand=seed)
@@ -190,7 +213,7 @@ def singlebond_cases():
         rec.update({key: np.asarray(v) for key, v in outs.items()})
         rec.update(tables=r["tables"], max_ang=r["max_ang"], max_check=r["max_check"])
         np.savez_compressed(HERE / f"singlebond_{k}.npz", **rec, **spec_record(spec))
-        print(f"singlebond_{k}: n={n} phi={phi} cos={cosm} model={kind} candidates={outs['plist_n']} "
+        print(f"singlebond_{k}: {model_name} n={n} phi={phi} cos={cosm} binding={kind} candidates={outs['plist_n']} "
               f"bound={[int(v.sum()) for v in outs['ib']]}")
 
 

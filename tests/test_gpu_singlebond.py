@@ -51,7 +51,7 @@ def oracle_update(sysm, B, x, Q, bt, ib, draw, replica=0):
 
 
 @pytest.mark.parametrize("precision,kernel", CONFIGS)
-@pytest.mark.parametrize("k", range(6))
+@pytest.mark.parametrize("k", range(8))
 def test_bind_update_matches_oracle(k, precision, kernel):
     d = load(f"singlebond_{k}.npz")
     spec = spec_from(d)
@@ -60,7 +60,7 @@ def test_bind_update_matches_oracle(k, precision, kernel):
     z = np.zeros((spec.n, 3))
     with LangevinNVTRGPU([spec], precision=precision, force_kernel=kernel) as s:
         s.set_single_bond(gpu_model(d))
-        assert s.num_patches == 4 * spec.n and s.patch_offset(0) == 0
+        assert s.num_patches == sysm.total_patches() and s.patch_offset(0) == 0
         for rnd in range(3):
             Q = d["Q"][rnd]
             s.initialize(d["x"], z, z, Q)

@@ -19,7 +19,7 @@ from oracle import pyoracle as po
 from tests._util import load, spec_from
 
 EXACT = platform.machine() in ("x86_64", "AMD64")
-CASES = range(6)
+CASES = range(8)
 
 
 def close(a, b, rtol=1e-12):
@@ -55,7 +55,9 @@ def test_model_constants_match_reference(k):
     sysm = po.System(spec_from(d))
     assert sysm.max_check() == float(d["max_check"])
     assert sysm.default_max_ang() == float(d["max_ang"])
-    assert sysm.total_patches() == 4 * int(d["n"])
+    ppt, cnt = d["patches_per_type"], d["count_per_type"]
+    assert sysm.total_patches() == sum(int(ppt[k]) * (int(cnt[k]) - (int(cnt[k - 1]) if k else 0))
+                                       for k in range(len(ppt)))
 
 
 @pytest.mark.parametrize("k", CASES)
