@@ -39,6 +39,9 @@ UNIT = "particle-steps/s"
 BYTES_FORCE = 48 + 24 + 4 + 48 + 8 + 4          # own x,Q + p,L + id; write p,L,F~,T~ + bin + histogram
 BYTES_SCATTER = 8 + 4 + 48 + 48 + 4 + 24 + 48 + 24 + 4 + 24  # bin,start,row,row,id,disp -> row,p+L,id,disp
 BYTES_SCAN_PER_CELL = 16
+# measured DRAM bytes per particle and launch (ncu dram__bytes_read + dram__bytes_write on 160 replicas,
+# state larger than L2; profiles/step_dram_traffic_c4x160.md), scaled by the particle count
+TRAFFIC_PER_PARTICLE = {"force": 383.0, "scatter": 231.1}
 
 
 def metric_of(args) -> str:
@@ -274,8 +277,11 @@ def run_gpu(args, rank, world, local):
     pk = peaks()
     alg = bytes_per.get(dominant)
     achieved = alg / (per_launch[dominant] / 1e3) / 1e9 if alg else None
+    traffic = TRAFFIC_PER_PARTICLE.get(dominant) if not args.single_bond else None
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                "frac": (achieved / pk["hbm_gbs"]) if achieved else None, "traffic": None,
+                "frac": (achieved / pk["hbm_gbs"]) if achieved else None,
+                "traffic": traffic * n if traffic else None,
+                "traffic_source": "ncu DRAM bytes per particle at 160 replicas, scaled" if traffic else None,
                 "peak_source": pk["source"],
                 "kernel_ms_per_step": {k: round(v, 5) for k, v in per_launch.items()},
                 "share": {k: round(v / total_prof, 4) for k, v in prof.items()},
