@@ -1174,24 +1174,33 @@ __global__ void store_state_kernel(int ntot, Buffers<real> in, double *x, double
 
 // LangevinNVTR::measured_temperature sums (LangevinR.cpp:170-193): per replica sum p_k^2, sum L_k^2
 template <class real>
-__global__ void __launch_bounds__(256) temperature_kernel(Tables<real> tb, Buffers<real> in, double *out) {
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
+__global__ void __launch_bounds__(256) temperature_kernel(Tables<real> tb, Buffers<real> in, double *out, int chunk) {
+    // block b sums slots [b * chunk, (b + 1) * chunk): replicas are contiguous slot ranges, so a thread's
+    // slots almost always belong to one replica and it adds them up before one warp reduction
+    const int base = blockIdx.x * chunk;
+    const int end = min(base + chunk, tb.ntot);
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    int cur = -1;
+    for (int s = base + threadIdx.x; s < end; s += blockDim.x) {
         const int r = find_replica(tb.rep_slot, tb.nrep, s);
+        if (r != cur) {
+            if (cur >= 0)
+                for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)cur + k, acc[k]);
+            cur = r;
+            for (int k = 0; k < 6; k++) acc[k] = 0.0;
+        }
         Row<real> M;
         M.load(in.motion + (size_t)s * kRow);
-        double v[6];
-        for (int k = 0; k < 6; k++) v[k] = (double)M.v[k] * (double)M.v[k];
-        unsigned active = __activemask();
-        unsigned peers = __match_any_sync(active, r);
-        const int lane = threadIdx.x & 31;
-        if (peers == 0xffffffffu) {
-            for (int k = 0; k < 6; k++)
-                for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
-            if (lane == 0)
-                for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)r + k, v[k]);
-        } else {
-            for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)r + k, v[k]);
-        }
+        for (int k = 0; k < 6; k++) acc[k] += (double)M.v[k] * (double)M.v[k];
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, cur);
+    if (peers == 0xffffffffu) {
+        for (int k = 0; k < 6; k++)
+            for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], o);
+        if ((threadIdx.x & 31) == 0 && cur >= 0)
+            for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)cur + k, acc[k]);
+    } else if (cur >= 0) {
+        for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)cur + k, acc[k]);
     }
 }
 

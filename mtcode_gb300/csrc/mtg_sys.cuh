@@ -1208,8 +1208,9 @@ struct Sys : SysBase {
     void temperature(double *out) override {
         if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_temperature: no state has been set"};
         MTG_CUDA(cudaMemsetAsync(d_obs, 0, sizeof(double) * 6 * nrep, st));
-        const int g = grid_for(ntot_, 256, occ_stream, sms);
-        mtg::temperature_kernel<real><<<g, 256, 0, st>>>(tables(), buf[cur], d_obs);
+        const int chunk = 256 * 8;
+        mtg::temperature_kernel<real><<<std::max(1, (ntot_ + chunk - 1) / chunk), 256, 0, st>>>(tables(), buf[cur],
+                                                                                              d_obs, chunk);
         check_launch();
         nlaunch += 1;
         MTG_CUDA(cudaMemcpyAsync(out, d_obs, sizeof(double) * 6 * nrep, cudaMemcpyDeviceToHost, st));
