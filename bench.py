@@ -338,7 +338,7 @@ def run_e2e(s, W, args, stream, ev0, ev1) -> dict:
     for _ in range(k_e2e):
         s.step(1)
         temps[...] = s.measured_temperature()
-    st = s.get_state()
+    st = s.get_state(out)
     ev1.record(stream)
     ev1.synchronize()
     wall = time.perf_counter() - t0

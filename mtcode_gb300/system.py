@@ -153,9 +153,16 @@ class LangevinNVTRGPU:
         self._hold = arrs  # host memory must outlive the (staged) copies
         _check(self._h, _lib.lib().mtg_set_state(self._h, *[dptr(a) for a in arrs]))
 
-    def get_state(self) -> dict:
-        out = {k: np.empty((self.n, w)) for k, w in (("x", 3), ("p", 3), ("Lb", 3), ("Q", 9), ("Ft", 3), ("Tt", 3))}
-        _check(self._h, _lib.lib().mtg_get_state(self._h, *[dptr(out[k]) for k in ("x", "p", "Lb", "Q", "Ft", "Tt")]))
+    def get_state(self, out: dict | None = None) -> dict:
+        """The whole state (x, p, Lb, Q, F~, T~).  ``out``: caller arrays to fill (e.g. pinned host memory,
+        which the download then reaches by DMA); new arrays otherwise."""
+        shapes = (("x", 3), ("p", 3), ("Lb", 3), ("Q", 9), ("Ft", 3), ("Tt", 3))
+        if out is None:
+            out = {k: np.empty((self.n, w)) for k, w in shapes}
+        for k, w in shapes:
+            if out[k].size != self.n * w:
+                raise ValueError(f"out[{k!r}] holds {out[k].size} values, expected {self.n * w}")
+        _check(self._h, _lib.lib().mtg_get_state(self._h, *[dptr(out[k]) for k, _ in shapes]))
         return out
 
     def getdat(self) -> np.ndarray:
