@@ -680,7 +680,7 @@ __device__ __forceinline__ size_t seg_slot(const long long *sh, long long cap, l
 
 template <class T>
 __device__ __forceinline__ void seg_append(T *list, unsigned long long *counts, long long cap, const T &e,
-                                           unsigned *flags) {
+                                           unsigned *flags, unsigned full_flag = kFlagBind | kBindWhyList) {
     namespace cg = cooperative_groups;
     cg::coalesced_group g = cg::coalesced_threads();
     const int k = (int)((blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) & (kSegs - 1));
@@ -688,7 +688,7 @@ __device__ __forceinline__ void seg_append(T *list, unsigned long long *counts, 
     if (g.thread_rank() == 0) base = atomicAdd(counts + k, (unsigned long long)g.size());
     base = g.shfl(base, 0) + g.thread_rank();
     if ((long long)base < cap) list[(size_t)k * (size_t)cap + base] = e;
-    else atomicOr(flags, kFlagBind | kBindWhyList);
+    else atomicOr(flags, full_flag);
 }
 
 template <class real>

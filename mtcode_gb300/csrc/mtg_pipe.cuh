@@ -159,7 +159,10 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
     }
 }
 
-__global__ void pair_reset_kernel(unsigned long long *npairs, const int *gate) {
+// the pair list's length (on list-building steps) and the patch list's segment counters (every pass)
+__global__ void pair_reset_kernel(unsigned long long *npairs, const int *gate, unsigned long long *patch_counts) {
+    if (patch_counts && blockIdx.x == 0)
+        for (int k = threadIdx.x; k < kSegs; k += blockDim.x) patch_counts[k] = 0ull;
     if (gated_off(gate, 1)) return;
     if (threadIdx.x == 0 && blockIdx.x == 0) *npairs = 0ull;
 }
@@ -168,14 +171,23 @@ __device__ __forceinline__ void fixed_add(long long *acc, float v) {
     if (v != 0.f) atomicAdd(reinterpret_cast<unsigned long long *>(acc), (unsigned long long)to_fixed(v));
 }
 
-// forces and torques of the listed pairs into acc (6 fixed-point sums per slot: F lab, T lab).  BIND
-// (single-bond mode, a bond-deciding pass): pairs where both particles have a patch near a cone along the
-// pair go, in canonical order (lower particle index first), to bind_list for bind_pairs_kernel.
-template <bool BIND>
+// Forces and torques of the listed pairs into acc (6 fixed-point sums per slot: F lab, T lab).
+// KIND kPairFull: WCA core and Kern-Frenkel patch terms of every pair.
+// KIND kPairSplit: WCA core here; pairs where both particles have a patch near a cone go to `list` for
+//   patch_pairs_kernel, which evaluates their patch terms with every lane busy (the rest of the pairs
+//   never reach the patch code, so this kernel runs without the divergent, register-heavy branch).
+// KIND kPairBind (single-bond mode, a bond-deciding pass): WCA core here; pairs where both particles have
+//   a patch near a cone go, in canonical order (lower particle index first), to `list` for
+//   bind_pairs_kernel.
+enum PairKind : int { kPairFull = 0, kPairBind = 1, kPairSplit = 2 };
+
+template <int KIND>
 __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<float> a, const int2 *pairs,
                                                                  const unsigned long long *npairs, long long cap,
-                                                                 long long *acc, int2 *bind_list = nullptr,
-                                                                 long long bind_cap = 0) {
+                                                                 long long *acc, int2 *list = nullptr,
+                                                                 long long list_cap = 0,
+                                                                 unsigned long long *list_counts = nullptr) {
+    constexpr bool BIND = KIND == kPairBind;
     const long long n = (long long)*npairs < cap ? (long long)*npairs : cap;
     bool big = false;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
@@ -226,12 +238,49 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
                         anyb |= v[0] * w[0] + v[1] * w[1] + v[2] * w[2] > pre;
                     }
                     if (anyb)
-                        seg_append<int2>(bind_list, a.bind_ctr + kSegPairs, bind_cap,
+                        seg_append<int2>(list, a.bind_ctr + kSegPairs, list_cap,
                                          ida < idb ? make_int2(sa, sb) : make_int2(sb, sa), a.flags);
                 }
             }
         }
-        if (r2 < R.patch_r2) {
+        if (KIND == kPairSplit && r2 < R.patch_r2) {
+            // the one-sided tests of both particles along d = x_a - x_b (with the 1e-5 margin of the full
+            // kernel's own early test): a's cosines -(n . Qa d) / r, b's (n . Qb d) / r
+            const Model<float> &M = a.tb.models[R.model];
+            const int ida = __ldg(a.buf.ident + sa);
+            const int tya = M.n_types == 1 ? 0 : type_of<float>(M, ida - R.off);
+            if (M.np[tya] > 0) {
+                const float inv = 1.f / sqrtf(r2);
+                float Q[9], w[3];
+                load_q(a, sa, xa[3], Q);
+#pragma unroll
+                for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
+                const float mca = M.mincos_any[tya] - 1e-5f;
+                bool any = false;
+                for (int k = 0; k < M.np[tya]; k++) {
+                    const float *v = M.orient[M.ooff[tya] + k];
+                    any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > mca;
+                }
+                if (any) {
+                    const int idb = __ldg(a.buf.ident + sb);
+                    const int tyb = M.n_types == 1 ? 0 : type_of<float>(M, idb - R.off);
+                    if (M.np[tyb] > 0) {
+                        load_q(a, sb, xb[3], Q);
+#pragma unroll
+                        for (int k = 0; k < 3; k++)
+                            w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
+                        const float mcb = M.mincos_any[tyb] - 1e-5f;
+                        bool anyb = false;
+                        for (int k = 0; k < M.np[tyb]; k++) {
+                            const float *v = M.orient[M.ooff[tyb] + k];
+                            anyb |= v[0] * w[0] + v[1] * w[1] + v[2] * w[2] > mcb;
+                        }
+                        if (anyb) seg_append<int2>(list, list_counts, list_cap, pr, a.flags, 8u);
+                    }
+                }
+            }
+        }
+        if (KIND == kPairFull && r2 < R.patch_r2) {
             const Model<float> &M = a.tb.models[R.model];
             const int ida = __ldg(a.buf.ident + sa);
             const bool single = M.n_types == 1;
@@ -285,6 +334,50 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
         }
     }
     if (big) atomicOr(a.flags, 2u);
+}
+
+// the Kern-Frenkel terms of the pairs pairforce_kernel<kPairSplit> listed, one pair per thread, into the
+// fixed-point sums of both particles (the same evaluation as the full kernel's patch branch)
+__global__ void __launch_bounds__(kPipeThreads) patch_pairs_kernel(ForceArgs<float> a, const int2 *list_all,
+                                                                 long long cap, const unsigned long long *counts,
+                                                                 long long *acc) {
+    __shared__ long long segs[kSegs + 1];
+    seg_prefix(counts, cap, segs);
+    const long long n = segs[kSegs];
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int2 pr = list_all[seg_slot(segs, cap, q)];
+        const int sa = pr.x, sb = pr.y;
+        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, sa);
+        const Replica<float> &R = a.tb.reps[r];
+        const Model<float> &M = a.tb.models[R.model];
+        float xa[4], xb[4];
+        load4(a.buf.pos + 4 * (size_t)sa, xa);
+        load4(a.buf.pos + 4 * (size_t)sb, xb);
+        const float d[3] = {min_image<float>(xa[0] - xb[0], R.box, R.l2s, R.periodic),
+                            min_image<float>(xa[1] - xb[1], R.box, R.l2s, R.periodic),
+                            min_image<float>(xa[2] - xb[2], R.box, R.l2s, R.periodic)};
+        const float rr = sqrtf(sep_r2(d[0], d[1], d[2]));
+        const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
+        const bool single = M.n_types == 1;
+        const int tya = single ? 0 : type_of<float>(M, ida - R.off), tyb = single ? 0 : type_of<float>(M, idb - R.off);
+        float Qa[9], Qb[9];
+        load_q(a, sa, xa[3], Qa);
+        load_q(a, sb, xb[3], Qb);
+        const bool a_first = ida < idb;  // canonical order of the reference (p1 < p2)
+        const float sg = a_first ? 1.f : -1.f, inv = 1.f / rr;
+        const float u[3] = {sg * d[0] * inv, sg * d[1] * inv, sg * d[2] * inv};
+        float f[3] = {0.f, 0.f, 0.f}, t1[3] = {0.f, 0.f, 0.f}, t2[3] = {0.f, 0.f, 0.f}, e = 0.f;
+        int nbond = 0;
+        if (a_first) patch_pair<float>(M, tya, tyb, Qa, Qb, u, rr, R.bond_r, f, t1, t2, e, nbond);
+        else patch_pair<float>(M, tyb, tya, Qb, Qa, u, rr, R.bond_r, f, t1, t2, e, nbond);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            fixed_add(acc + 6 * (size_t)sa + k, sg * f[k]);
+            fixed_add(acc + 6 * (size_t)sb + k, -sg * f[k]);
+            fixed_add(acc + 6 * (size_t)sa + 3 + k, a_first ? t1[k] : t2[k]);
+            fixed_add(acc + 6 * (size_t)sb + 3 + k, a_first ? t2[k] : t1[k]);
+        }
+    }
 }
 
 // single-bond mode, a bond-deciding pass: this update's edges of the pairs pairforce_kernel<true> listed

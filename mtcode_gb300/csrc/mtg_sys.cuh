@@ -233,6 +233,10 @@ struct Sys : SysBase {
     unsigned long long *d_npairs = nullptr;
     long long *d_acc = nullptr;
     long long pair_cap = 0;
+    // pairs with a patch near a cone on both sides, for the patch-pair kernel (segmented list)
+    int2 *d_patch_list = nullptr;
+    unsigned long long *d_patch_ctr = nullptr;
+    long long patch_cap = 0;
     // skin lists (null without a skin): state flags, candidate lists and lengths, build positions / cells
     double skin = 0;
     int *d_skin = nullptr, *d_list_n = nullptr, *d_home_cell = nullptr;
@@ -355,6 +359,10 @@ struct Sys : SysBase {
                 MTG_CUDA(cudaMemset(d_npairs, 0, sizeof(unsigned long long)));
                 MTG_CUDA(cudaMalloc(&d_acc, sizeof(long long) * 6 * n));
                 MTG_CUDA(cudaMemset(d_acc, 0, sizeof(long long) * 6 * n));
+                patch_cap = std::max<long long>(1024, 2 * (pair_cap + mtg::kSegs - 1) / mtg::kSegs);
+                MTG_CUDA(cudaMalloc(&d_patch_list, sizeof(int2) * (size_t)patch_cap * mtg::kSegs));
+                MTG_CUDA(cudaMalloc(&d_patch_ctr, sizeof(unsigned long long) * mtg::kSegs));
+                MTG_CUDA(cudaMemset(d_patch_ctr, 0, sizeof(unsigned long long) * mtg::kSegs));
                 if (!d_home_cell) {
                     MTG_CUDA(cudaMalloc(&d_home_cell, sizeof(int) * n));
                     MTG_CUDA(cudaMemset(d_home_cell, 0, sizeof(int) * n));
@@ -397,7 +405,7 @@ struct Sys : SysBase {
         cudaFree(d_tiles);
         cudaFree(d_bond_start); cudaFree(d_bond_partner); cudaFree(d_slot_of);
         cudaFree(d_skin); cudaFree(d_list); cudaFree(d_list_n); cudaFree(d_home_cell); cudaFree(d_xref);
-        cudaFree(d_pairs); cudaFree(d_npairs); cudaFree(d_acc);
+        cudaFree(d_pairs); cudaFree(d_npairs); cudaFree(d_acc); cudaFree(d_patch_list); cudaFree(d_patch_ctr);
         free_bind();
         if (h_flags) cudaFreeHost(h_flags);
         if (st) cudaStreamDestroy(st);
@@ -804,18 +812,21 @@ struct Sys : SysBase {
                 // with a skin the list is rebuilt only on rebuild steps (the gate); the force and epilogue
                 // passes run every time
                 const int *gate = skin > 0 ? d_skin : nullptr;
-                mtg::pair_reset_kernel<<<1, 32, 0, st>>>(d_npairs, gate);
+                mtg::pair_reset_kernel<<<1, 64, 0, st>>>(d_npairs, gate, bind ? nullptr : d_patch_ctr);
                 const int gb = (ntot_ + mtg::kPipeThreads - 1) / mtg::kPipeThreads;
                 mtg::pairfind_kernel<<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap,
                                                                                   skin > 0 ? 1 : 0, gate);
                 if (bind) {
-                    mtg::pairforce_kernel<true><<<sms * 16, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap,
-                                                                                      d_acc, d_bind_pairs, lcap);
+                    mtg::pairforce_kernel<mtg::kPairBind><<<sms * 16, mtg::kPipeThreads, 0, st>>>(
+                        a, d_pairs, d_npairs, pair_cap, d_acc, d_bind_pairs, lcap);
                     mtg::bind_pairs_kernel<<<sms * 8, mtg::kPipeThreads, 0, st>>>(a, d_bind_pairs, lcap);
                     decide();
                     mtg::bound_pairs_kernel<<<sms * 4, mtg::kPipeThreads, 0, st>>>(a, d_bound, bcap, d_acc);
                 } else {
-                    mtg::pairforce_kernel<false><<<sms * 16, mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap, d_acc);
+                    mtg::pairforce_kernel<mtg::kPairSplit><<<sms * 16, mtg::kPipeThreads, 0, st>>>(
+                        a, d_pairs, d_npairs, pair_cap, d_acc, d_patch_list, patch_cap, d_patch_ctr);
+                    mtg::patch_pairs_kernel<<<sms * 8, mtg::kPipeThreads, 0, st>>>(a, d_patch_list, patch_cap, d_patch_ctr,
+                                                                                  d_acc);
                 }
                 mtg::pair_epilogue_kernel<MODE><<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_acc);
                 return;
