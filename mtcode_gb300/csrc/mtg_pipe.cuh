@@ -25,10 +25,6 @@ namespace {  // internal linkage
 constexpr int kPipeThreads = 256;
 constexpr int kPairBlockCap = 2048;    // pairs a pairfind block buffers in shared memory
 constexpr int kPairsPerParticle = 16;  // capacity of the pair list (unordered pairs per particle)
-// a listed pair's second slot carries this bit when the first particle has a patch near a cone along the
-// pair (pairfind's one-sided test; lists built for the current step only)
-constexpr int kConeMark = (int)0x80000000u;
-constexpr int kSlotMask = 0x7fffffff;
 
 // |d|^2 with explicit roundings (no contraction), so that pairfind and pairforce decide a pair at the
 // cutoff identically; with the image shift applied as (x_i - x_j) - s the separation is bit for bit the
@@ -77,19 +73,6 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
         const int cx = key % nc, cy = (key / nc) % nc, cz = key / (nc * nc);
         const float4 pi = __ldg(reinterpret_cast<const float4 *>(a.buf.pos) + s);
         const float L = R.box;
-        // On a list built for this very step (no skin), the own particle's one-sided cone test of every
-        // pair it lists within the patch range: its rotation is loaded once here, and pairforce_kernel
-        // then examines the patches of only the pairs marked kConeMark.
-        const Model<float> &M = a.tb.models[R.model];
-        int tys = 0;
-        bool cone = !range_list && R.patch_r2 > 0.f;
-        if (cone) {
-            tys = M.n_types == 1 ? 0 : type_of<float>(M, __ldg(a.buf.ident + s) - R.off);
-            cone = M.np[tys] > 0;
-        }
-        float Qs[9];
-        if (cone) load_q(a, s, pi.w, Qs);
-        const float mcs = M.mincos_any[tys] - 1e-5f;
         // Each unordered pair once.  With three or more cells per side: the forward half of the stencil
         // (rows (dy, dz) = (0, 0) [cells x, x + 1], (1, 0), (-1..1, 1) [cells x - 1 .. x + 1]) -- an offset
         // and its negative are distinct cells, so exactly one of the two particles' scans holds the
@@ -160,24 +143,8 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
                         dy2 = min_image<float>(pi.y - pj.y, R.box, R.l2s, R.periodic);
                         dz2 = min_image<float>(pi.z - pj.z, R.box, R.l2s, R.periodic);
                     }
-                    const float r2 = sep_r2(dx, dy2, dz2);
-                    if (r2 < range2) {
-                        int mark = 0;
-                        if (cone && r2 < R.patch_r2) {
-                            const float inv = 1.f / sqrtf(r2);
-                            float w[3];
-#pragma unroll
-                            for (int k = 0; k < 3; k++)
-                                w[k] = (Qs[3 * k] * dx + Qs[3 * k + 1] * dy2 + Qs[3 * k + 2] * dz2) * inv;
-                            bool any = false;
-                            for (int k = 0; k < M.np[tys]; k++) {
-                                const float *v = M.orient[M.ooff[tys] + k];
-                                any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > mcs;
-                            }
-                            mark = any ? kConeMark : 0;
-                        }
-                        block_pair_append(buf, &nb, make_int2(s, t | mark), pairs, npairs, cap, a.flags);
-                    }
+                    if (sep_r2(dx, dy2, dz2) < range2)
+                        block_pair_append(buf, &nb, make_int2(s, t), pairs, npairs, cap, a.flags);
                 }
             }
         }
@@ -224,9 +191,7 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
     const long long n = (long long)*npairs < cap ? (long long)*npairs : cap;
     bool big = false;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        const int2 pr0 = pairs[q];
-        const bool marked = (pr0.y & kConeMark) != 0;
-        const int2 pr = make_int2(pr0.x, pr0.y & kSlotMask);
+        const int2 pr = pairs[q];
         const int sa = pr.x, sb = pr.y;
         const int r = find_replica(a.tb.rep_slot, a.tb.nrep, sa);
         const Replica<float> &R = a.tb.reps[r];
@@ -278,31 +243,24 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
                 }
             }
         }
-        // with a list built for this step (no skin), pairfind has run a's one-sided test and marked the
-        // pairs that pass; a skin list is older than the orientations, so it is tested here
-        if (KIND == kPairSplit && r2 < R.patch_r2 && (marked || a.skin)) {
+        if (KIND == kPairSplit && r2 < R.patch_r2) {
             // the one-sided tests of both particles along d = x_a - x_b (with the 1e-5 margin of the full
             // kernel's own early test): a's cosines -(n . Qa d) / r, b's (n . Qb d) / r
             const Model<float> &M = a.tb.models[R.model];
-            const float inv = 1.f / sqrtf(r2);
-            float Q[9], w[3];
-            bool any = marked;
-            if (!marked) {
-                const int ida = __ldg(a.buf.ident + sa);
-                const int tya = M.n_types == 1 ? 0 : type_of<float>(M, ida - R.off);
-                if (M.np[tya] > 0) {
-                    load_q(a, sa, xa[3], Q);
+            const int ida = __ldg(a.buf.ident + sa);
+            const int tya = M.n_types == 1 ? 0 : type_of<float>(M, ida - R.off);
+            if (M.np[tya] > 0) {
+                const float inv = 1.f / sqrtf(r2);
+                float Q[9], w[3];
+                load_q(a, sa, xa[3], Q);
 #pragma unroll
-                    for (int k = 0; k < 3; k++)
-                        w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
-                    const float mca = M.mincos_any[tya] - 1e-5f;
-                    for (int k = 0; k < M.np[tya]; k++) {
-                        const float *v = M.orient[M.ooff[tya] + k];
-                        any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > mca;
-                    }
+                for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
+                const float mca = M.mincos_any[tya] - 1e-5f;
+                bool any = false;
+                for (int k = 0; k < M.np[tya]; k++) {
+                    const float *v = M.orient[M.ooff[tya] + k];
+                    any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > mca;
                 }
-            }
-            {
                 if (any) {
                     const int idb = __ldg(a.buf.ident + sb);
                     const int tyb = M.n_types == 1 ? 0 : type_of<float>(M, idb - R.off);
