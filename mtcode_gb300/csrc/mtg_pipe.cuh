@@ -172,14 +172,13 @@ __device__ __forceinline__ void fixed_add(long long *acc, float v) {
 }
 
 // Forces and torques of the listed pairs into acc (6 fixed-point sums per slot: F lab, T lab).
-// KIND kPairFull: WCA core and Kern-Frenkel patch terms of every pair.
 // KIND kPairSplit: WCA core here; pairs where both particles have a patch near a cone go to `list` for
 //   patch_pairs_kernel, which evaluates their patch terms with every lane busy (the rest of the pairs
 //   never reach the patch code, so this kernel runs without the divergent, register-heavy branch).
 // KIND kPairBind (single-bond mode, a bond-deciding pass): WCA core here; pairs where both particles have
 //   a patch near a cone go, in canonical order (lower particle index first), to `list` for
 //   bind_pairs_kernel.
-enum PairKind : int { kPairFull = 0, kPairBind = 1, kPairSplit = 2 };
+enum PairKind : int { kPairBind = 1, kPairSplit = 2 };
 
 template <int KIND>
 __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<float> a, const int2 *pairs,
@@ -204,7 +203,7 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
         const float r2 = sep_r2(d[0], d[1], d[2]);
         if (!(r2 < R.rc2)) continue;  // skin lists hold pairs up to the list range
         const float rr = sqrtf(r2);
-        float fa[3] = {0.f, 0.f, 0.f}, ta[3] = {0.f, 0.f, 0.f}, tb[3] = {0.f, 0.f, 0.f};
+        float fa[3] = {0.f, 0.f, 0.f};   // the WCA core; patch forces and torques come from the pair lists' kernels
         if (rr < R.hs_limit) {
             const float s_ = hs_force_over_r<float>(R, r2);
             big |= fabsf(s_ * rr) > 1e4f;
@@ -216,16 +215,16 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
             // along d = x_a - x_b: a's cosines are -(n_a . d) / r and b's (n_b . d) / r in either canonical order
             const Model<float> &M = a.tb.models[R.model];
             const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
-            const int ta = type_of<float>(M, ida - R.off), tb = type_of<float>(M, idb - R.off);
-            if (M.np[ta] > 0 && M.np[tb] > 0) {
-                const float inv = 1.f / sqrtf(r2), pre = M.mincos[ta][tb] - 4e-5f;
+            const int tya = type_of<float>(M, ida - R.off), tyb = type_of<float>(M, idb - R.off);
+            if (M.np[tya] > 0 && M.np[tyb] > 0) {
+                const float inv = 1.f / sqrtf(r2), pre = M.mincos[tya][tyb] - 4e-5f;
                 float Q[9], w[3];
                 load_q(a, sa, xa[3], Q);
 #pragma unroll
                 for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
                 bool any = false;
-                for (int k = 0; k < M.np[ta]; k++) {
-                    const float *v = M.orient[M.ooff[ta] + k];
+                for (int k = 0; k < M.np[tya]; k++) {
+                    const float *v = M.orient[M.ooff[tya] + k];
                     any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > pre;
                 }
                 if (any) {
@@ -233,8 +232,8 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
 #pragma unroll
                     for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
                     bool anyb = false;
-                    for (int k = 0; k < M.np[tb]; k++) {
-                        const float *v = M.orient[M.ooff[tb] + k];
+                    for (int k = 0; k < M.np[tyb]; k++) {
+                        const float *v = M.orient[M.ooff[tyb] + k];
                         anyb |= v[0] * w[0] + v[1] * w[1] + v[2] * w[2] > pre;
                     }
                     if (anyb)
@@ -280,57 +279,10 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
                 }
             }
         }
-        if (KIND == kPairFull && r2 < R.patch_r2) {
-            const Model<float> &M = a.tb.models[R.model];
-            const int ida = __ldg(a.buf.ident + sa);
-            const bool single = M.n_types == 1;
-            const int tya = single ? 0 : type_of<float>(M, ida - R.off);
-            float Qa[9];
-            bool any = M.np[tya] > 0;
-            if (any) {
-                // particle a's own cone test first: its cosines are -(n . Qa (d / r)) in either order of
-                // the pair (the ones patch_pair tests, up to rounding: the 1e-5 margin); most pairs have
-                // no patch of a in any cone and need neither b's orientation nor its type
-                load_q(a, sa, xa[3], Qa);
-                const float inv = 1.f / rr;
-                float w[3];
-#pragma unroll
-                for (int k = 0; k < 3; k++)
-                    w[k] = Qa[3 * k] * (d[0] * inv) + Qa[3 * k + 1] * (d[1] * inv) + Qa[3 * k + 2] * (d[2] * inv);
-                const float mca = M.mincos_any[tya] - 1e-5f;
-                const int oa = M.ooff[tya];
-                any = false;
-                for (int ia = 0; ia < M.np[tya]; ia++) {
-                    const float *v = M.orient[oa + ia];
-                    any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > mca;
-                }
-            }
-            const int idb = any ? __ldg(a.buf.ident + sb) : 0;
-            const int tyb = single || !any ? 0 : type_of<float>(M, idb - R.off);
-            if (any && M.np[tyb] > 0) {
-                float Qb[9];
-                load_q(a, sb, xb[3], Qb);
-                const bool a_first = ida < idb;  // canonical order of the reference (p1 < p2)
-                const float sg = a_first ? 1.f : -1.f, inv = 1.f / rr;
-                const float u[3] = {sg * d[0] * inv, sg * d[1] * inv, sg * d[2] * inv};
-                float f[3] = {0.f, 0.f, 0.f}, t1[3] = {0.f, 0.f, 0.f}, t2[3] = {0.f, 0.f, 0.f}, e = 0.f;
-                int nbond = 0;
-                if (a_first) patch_pair<float>(M, tya, tyb, Qa, Qb, u, rr, R.bond_r, f, t1, t2, e, nbond);
-                else patch_pair<float>(M, tyb, tya, Qb, Qa, u, rr, R.bond_r, f, t1, t2, e, nbond);
-#pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    fa[k] += sg * f[k];
-                    ta[k] = a_first ? t1[k] : t2[k];
-                    tb[k] = a_first ? t2[k] : t1[k];
-                }
-            }
-        }
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             fixed_add(acc + 6 * (size_t)sa + k, fa[k]);
             fixed_add(acc + 6 * (size_t)sb + k, -fa[k]);
-            fixed_add(acc + 6 * (size_t)sa + 3 + k, ta[k]);
-            fixed_add(acc + 6 * (size_t)sb + 3 + k, tb[k]);
         }
     }
     if (big) atomicOr(a.flags, 2u);
