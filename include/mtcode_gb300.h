@@ -219,7 +219,7 @@ int64_t mtg_launch_count(const mtg_system *h);
  * around every launch on the handle's stream.  kernel_ms[k] receives the summed device time of
  * kernel k over the nsteps, for k = 0 scan_reduce, 1 scan_top, 2 scan_down, 3 scatter (reorder +
  * first half-step), 4 force (force/torque + Langevin epilogue + next binning), and in single-bond mode
- * 5 bind_candidates (the update's start + the candidate list when due), 6 bind_decide (edges, clusters,
+ * 5 bind_begin (the update's start; the edges are part of the force pass), 6 bind_decide (clusters and
  * bond decisions).  With a neighbour skin: 0 = rebuild decision + binning + scan_reduce, 1 scan_top,
  * 2 scan_down, 3 scatter + copy-back (rebuild steps) + in-place first half-step (other steps), 4 force.
  * Synchronising. */

@@ -19,7 +19,7 @@ MTG_OBS_COUNT = 5
 MTG_PROFILE_KERNELS = 7
 MTG_NOALLOC_MAX_PARTICLES = 65536
 MTG_NOALLOC_MAX_CELLS = 65536
-PROFILE_KERNEL_NAMES = ("scan_reduce", "scan_top", "scan_down", "scatter", "force", "bind_candidates", "bind_decide")
+PROFILE_KERNEL_NAMES = ("scan_reduce", "scan_top", "scan_down", "scatter", "force", "bind_begin", "bind_decide")
 MTG_FP32 = 0
 MTG_FP64 = 1
 MTG_FLAG_NONFINITE = 0x1
