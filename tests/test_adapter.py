@@ -80,3 +80,63 @@ def test_condensate_loop_through_the_adapter_matches_oracle(tmp_path):
     assert sysm.run(st, steps, noise_mode=0) == 0
     for got, key in ((xf, "x"), (pf, "p"), (Qf, "Q"), (Lf, "Lb")):
         assert np.abs(got - st[key]).max() <= 1e-9 * max(1.0, np.abs(st[key]).max()), key
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_singlebond_driver_compiles_standalone():
+    compile_driver("singlebond_gpu.cpp", BUILD / "singlebond_gpu")
+
+
+@pytest.mark.gpu
+def test_singlebond_loop_through_the_adapter_matches_oracle(tmp_path):
+    """run_singlebond through the adapter (FP64, noise off): the first onlyone_nonlets pass (bond state,
+    forces, torques) and the bond state and configuration after init + 25 steps equal the oracle's."""
+    exe = compile_driver("singlebond_gpu.cpp", BUILD / "singlebond_gpu")
+    n, steps = 300, 25
+    spec = ReplicaSpec(n=n, box=box_for(n, 0.3), model=PatchModelSpec.tetrahedral(n, 8.0, 1.2, math.acos(0.7)),
+                       kT=0.0, seed=0)
+    x = random_positions(n, spec.box, True, 0.95, 31)
+    Q = random_rotations(n, 32)
+    inp = tmp_path / "in.bin"
+    with open(inp, "wb") as f:
+        np.array([n, _lib.MTG_FP64, steps], dtype=np.int32).tofile(f)
+        np.array([spec.box, spec.kT, spec.dt], dtype=np.float64).tofile(f)
+        x.tofile(f)
+        Q.tofile(f)
+    out = tmp_path / "out.bin"
+    proc = subprocess.run([str(exe), str(inp), str(out)], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
+                          timeout=300)
+    assert proc.returncode == 0, proc.stdout
+    raw = out.read_bytes()
+    np_ = 4 * n
+    F = np.frombuffer(raw, np.float64, 3 * n, 0).reshape(n, 3)
+    T = np.frombuffer(raw, np.float64, 3 * n, 24 * n).reshape(n, 3)
+    off = 48 * n
+    ib1 = np.frombuffer(raw, np.uint8, np_, off)
+    ib2 = np.frombuffer(raw, np.uint8, np_, off + np_)
+    off += 2 * np_
+    bt1 = np.frombuffer(raw, np.int32, np_, off)
+    bt2 = np.frombuffer(raw, np.int32, np_, off + 4 * np_)
+    off += 8 * np_
+    xf = np.frombuffer(raw, np.float64, 3 * n, off).reshape(n, 3)
+    Qf = np.frombuffer(raw, np.float64, 9 * n, off + 24 * n).reshape(n, 9)
+    sysm = po.System(spec)
+    bind = po.binding_single(0.7, 0.5)
+    ncell = max(1, int(math.floor(spec.box / 2.5)))
+    bt = np.zeros(np_, dtype=np.intc)
+    ib = np.zeros(np_, dtype=np.uint8)
+    st, Fb, Tb = sysm.bind_update(x, Q, sysm.patch_list(x, Q, sysm.pairs(x, 2.5, ncell), sysm.default_max_ang()),
+                                  bind, bt, ib, rng=0, seed=0, replica=0, draw=0)
+    assert st == 0 and ib.sum() > 0
+    assert np.array_equal(ib1, ib) and np.array_equal(bt1[ib == 1], bt[ib == 1])
+    Fo = sysm.central_forces(x) + Fb
+    assert np.linalg.norm(F - Fo) <= 1e-12 * np.linalg.norm(Fo)
+    assert np.linalg.norm(T - Tb) <= 1e-12 * np.linalg.norm(Tb)
+    state = dict(x=x.copy(), p=np.zeros((n, 3)), Lb=np.zeros((n, 3)), Q=Q.copy(), Ft=np.zeros((n, 3)),
+                 Tt=np.zeros((n, 3)), boundto=bt, isbound=ib)
+    assert sysm.run_singlebond(state, bind, steps, sysm.default_max_ang(), init=True, init_draw=1, seed=0,
+                               replica=0, draw0=2) == 0
+    assert np.array_equal(ib2, state["isbound"])
+    assert np.array_equal(bt2[ib2 == 1], state["boundto"][state["isbound"] == 1])
+    assert np.abs(xf - state["x"]).max() <= 1e-9 * max(1.0, np.abs(state["x"]).max())
+    assert np.abs(Qf - state["Q"]).max() <= 1e-9
