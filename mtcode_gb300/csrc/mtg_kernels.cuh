@@ -51,6 +51,8 @@ struct Tables {
     int nrep;
     int ntot;
     int ncells;
+    int uniform;   // every replica has the pair constants of replica 0 and one particle type: pair kernels
+                   // read replica 0 instead of searching the slot's replica
 };
 
 __device__ __forceinline__ int find_replica(const int *rep_slot, int nrep, int s) {

@@ -15,8 +15,6 @@
 // the force kernel drops the pairs beyond the force range each step.
 #pragma once
 
-#include <cooperative_groups.h>
-
 #include "mtg_tile.cuh"
 
 namespace mtg {
@@ -33,23 +31,43 @@ __device__ __forceinline__ float sep_r2(float dx, float dy, float dz) {
     return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
-__device__ __forceinline__ void block_pair_append(int2 *buf, int *nb, int2 p, int2 *pairs,
-                                                  unsigned long long *npairs, long long cap, unsigned *flags) {
-    // warp-aggregated: the lanes that found a pair in this iteration take consecutive buffer entries
-    cooperative_groups::coalesced_group g = cooperative_groups::coalesced_threads();
+// Appends the pairs (s, c0 + b) for every bit b of each lane's mask: one warp-wide scan of the counts and
+// one shared-memory atomic per warp take consecutive entries of the block buffer; entries past its end go
+// straight to the list.  Called by all 32 lanes of the warp.
+__device__ __forceinline__ void warp_pair_flush(int2 *buf, int *nb, int s, int c0, unsigned mask, int2 *pairs,
+                                                unsigned long long *npairs, long long cap, unsigned *flags) {
+    const unsigned full = 0xffffffffu;
+    if (!__ballot_sync(full, mask != 0u)) return;
+    const int lane = threadIdx.x & 31;
+    const int cnt = __popc(mask);
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(full, incl, o);
+        if (lane >= o) incl += v;
+    }
     int q = 0;
-    if (g.thread_rank() == 0) q = atomicAdd(nb, (int)g.size());
-    q = g.shfl(q, 0) + (int)g.thread_rank();
-    if (q < kPairBlockCap) {
-        buf[q] = p;
-    } else {  // the block buffer is full: straight to the list
-        const unsigned long long w = atomicAdd(npairs, 1ull);
-        if ((long long)w < cap) pairs[w] = p;
-        else atomicOr(flags, 8u);
+    if (lane == 31) q = atomicAdd(nb, incl);
+    q = __shfl_sync(full, q, 31) + incl - cnt;
+    while (mask) {
+        const int b = __ffs(mask) - 1;
+        mask &= mask - 1u;
+        const int2 p = make_int2(s, c0 + b);
+        if (q < kPairBlockCap) {
+            buf[q] = p;
+        } else {  // the block buffer is full
+            const unsigned long long w = atomicAdd(npairs, 1ull);
+            if ((long long)w < cap) pairs[w] = p;
+            else atomicOr(flags, 8u);
+        }
+        q++;
     }
 }
 
-// range2_list: use the replica's list range (skin lists) instead of its force range
+// range_list: use the replica's list range (skin lists) instead of its force range.
+// Each lane scans its particle's candidate segments in chunks of at most 32 slots and marks the hits of a
+// chunk in a bit mask; the warp then appends the marked pairs together (warp_pair_flush), so the candidate
+// loop itself carries no appends.  The chunk and segment loops are warp-uniform.
 __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float> a, int2 *pairs,
                                                                 unsigned long long *npairs, long long cap,
                                                                 int range_list, const int *gate) {
@@ -60,31 +78,34 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
     if (threadIdx.x == 0) nb = 0;
     __syncthreads();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < a.tb.ntot) {
-        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, s);
-        const Replica<float> &R = a.tb.reps[r];
-        const float range2 = range_list ? R.rc2_list : R.rc2;
-        const int nc = R.nc;
-        int key = a.buf.home_cell[s] - R.cell_off;
-        if (key < 0 || key >= nc * nc * nc) {
-            atomicOr(a.flags, 16u);
-            key = 0;
-        }
-        const int cx = key % nc, cy = (key / nc) % nc, cz = key / (nc * nc);
-        const float4 pi = __ldg(reinterpret_cast<const float4 *>(a.buf.pos) + s);
-        const float L = R.box;
-        // Each unordered pair once.  With three or more cells per side: the forward half of the stencil
-        // (rows (dy, dz) = (0, 0) [cells x, x + 1], (1, 0), (-1..1, 1) [cells x - 1 .. x + 1]) -- an offset
-        // and its negative are distinct cells, so exactly one of the two particles' scans holds the
-        // other -- and in the own cell only the later slots.  Smaller grids: every cell, later slots.
-        const bool small = nc < 3;
-        const int nrows = small ? 9 : 5;
-        for (int rr = 0; rr < nrows; rr++) {
+    const bool valid = s < a.tb.ntot;
+    int r = 0;
+    if (valid) r = find_replica(a.tb.rep_slot, a.tb.nrep, s);
+    const Replica<float> &R = a.tb.reps[r];
+    const float range2 = range_list ? R.rc2_list : R.rc2;
+    const int nc = R.nc;
+    int key = valid ? a.buf.home_cell[s] - R.cell_off : 0;
+    if (key < 0 || key >= nc * nc * nc) {
+        atomicOr(a.flags, 16u);
+        key = 0;
+    }
+    const int cx = key % nc, cy = (key / nc) % nc, cz = key / (nc * nc);
+    const float4 pi = valid ? __ldg(reinterpret_cast<const float4 *>(a.buf.pos) + s) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float L = R.box;
+    // Each unordered pair once.  With three or more cells per side: the forward half of the stencil
+    // (rows (dy, dz) = (0, 0) [cells x, x + 1], (1, 0), (-1..1, 1) [cells x - 1 .. x + 1]) -- an offset
+    // and its negative are distinct cells, so exactly one of the two particles' scans holds the
+    // other -- and in the own cell only the later slots.  Smaller grids: every cell, later slots.
+    const bool small = nc < 3;
+    const int nrows = !valid ? 0 : (small ? 9 : 5);
+    for (int rr = 0; rr < 9; rr++) {  // warp-uniform; rows past a lane's nrows are empty
+        int a0 = 0, a1 = 0, b0 = 0, b1 = 0;
+        float shz = 0.f, shy = 0.f, shb = 0.f;
+        if (rr < nrows) {
             int dy, dz;
             if (small) {
                 dy = rr % 3;
                 dz = rr / 3;
-                if (dy >= nc || dz >= nc) continue;
             } else {
                 dy = rr == 0 ? 0 : (rr == 1 ? 1 : rr - 3);
                 dz = rr <= 1 ? 0 : 1;
@@ -92,50 +113,52 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
             // pairfind runs right after a sort, so every particle lies in its cell: a neighbour cell
             // reached across a periodic face holds coordinates one box length away (image shift)
             int zz = small ? dz : cz + dz, yy = small ? dy : cy + dy;
-            float shz = 0.f, shy = 0.f;
+            bool skip = small && (dy >= nc || dz >= nc);
             if (zz >= nc) {
-                if (!R.periodic) continue;
+                skip |= !R.periodic;
                 shz = L;
                 zz -= nc;
             }
             if (yy < 0 || yy >= nc) {
-                if (!R.periodic) continue;
+                skip |= !R.periodic;
                 shy = yy < 0 ? -L : L;
                 yy = yy < 0 ? yy + nc : yy - nc;
             }
-            const int row = R.cell_off + nc * (yy + nc * zz);
-            // x cells of this row as at most two contiguous slot segments: [a0, a1) unshifted and one
-            // wrapped cell [b0, b1) (image shift shb)
-            int a0, a1, b0 = 0, b1 = 0;
-            float shb = 0.f;
-            if (small) {
-                a0 = __ldg(a.start + row);
-                a1 = __ldg(a.start + row + nc);
-            } else {
-                const int x0 = rr == 0 ? cx : cx - 1, x1 = cx + 1;  // the own row starts at the own cell
-                a0 = __ldg(a.start + row + (x0 < 0 ? 0 : x0));
-                a1 = __ldg(a.start + row + (x1 >= nc ? nc : x1 + 1));
-                if (R.periodic) {
-                    if (x0 < 0) {
-                        b0 = __ldg(a.start + row + nc - 1);
-                        b1 = __ldg(a.start + row + nc);
-                        shb = -L;
-                    } else if (x1 >= nc) {
-                        b0 = __ldg(a.start + row);
-                        b1 = __ldg(a.start + row + 1);
-                        shb = L;
+            if (!skip) {
+                const int row = R.cell_off + nc * (yy + nc * zz);
+                // x cells of this row as at most two contiguous slot segments: [a0, a1) unshifted and one
+                // wrapped cell [b0, b1) (image shift shb)
+                if (small) {
+                    a0 = __ldg(a.start + row);
+                    a1 = __ldg(a.start + row + nc);
+                } else {
+                    const int x0 = rr == 0 ? cx : cx - 1, x1 = cx + 1;  // the own row starts at the own cell
+                    a0 = __ldg(a.start + row + (x0 < 0 ? 0 : x0));
+                    a1 = __ldg(a.start + row + (x1 >= nc ? nc : x1 + 1));
+                    if (R.periodic) {
+                        if (x0 < 0) {
+                            b0 = __ldg(a.start + row + nc - 1);
+                            b1 = __ldg(a.start + row + nc);
+                            shb = -L;
+                        } else if (x1 >= nc) {
+                            b0 = __ldg(a.start + row);
+                            b1 = __ldg(a.start + row + 1);
+                            shb = L;
+                        }
                     }
                 }
-            }
-            const bool own = small || rr == 0;  // segments [a0, a1) that hold s's own cell
-            for (int seg = 0; seg < 2; seg++) {
-                int t0 = seg ? b0 : a0;
-                const int t1 = seg ? b1 : a1;
                 // only the own cell filters by slot; the wrapped cell of the own row is a forward
                 // neighbour whose slots may lie below s
-                if (own && seg == 0 && t0 <= s) t0 = s + 1;
-                const float shx = seg ? shb : 0.f;
-                for (int t = t0; t < t1; t++) {
+                if ((small || rr == 0) && a0 <= s) a0 = s + 1;
+            }
+        }
+        for (int seg = 0; seg < 2; seg++) {
+            const int t0 = seg ? b0 : a0, t1 = seg ? b1 : a1;
+            const float shx = seg ? shb : 0.f;
+            for (int c0 = t0; __any_sync(0xffffffffu, c0 < t1); c0 += 32) {
+                unsigned mask = 0u;
+                const int ce = t1 < c0 + 32 ? t1 : c0 + 32;
+                for (int t = c0; t < ce; t++) {
                     const float4 pj = __ldg(reinterpret_cast<const float4 *>(a.buf.pos) + t);
                     float dx = (pi.x - pj.x) - shx, dy2 = (pi.y - pj.y) - shy, dz2 = (pi.z - pj.z) - shz;
                     if (small) {  // tiny grids: no cell geometry to lean on
@@ -143,9 +166,9 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
                         dy2 = min_image<float>(pi.y - pj.y, R.box, R.l2s, R.periodic);
                         dz2 = min_image<float>(pi.z - pj.z, R.box, R.l2s, R.periodic);
                     }
-                    if (sep_r2(dx, dy2, dz2) < range2)
-                        block_pair_append(buf, &nb, make_int2(s, t), pairs, npairs, cap, a.flags);
+                    if (sep_r2(dx, dy2, dz2) < range2) mask |= 1u << (t - c0);
                 }
+                warp_pair_flush(buf, &nb, s, c0, mask, pairs, npairs, cap, a.flags);
             }
         }
     }
@@ -165,6 +188,38 @@ __global__ void pair_reset_kernel(unsigned long long *npairs, const int *gate, u
         for (int k = threadIdx.x; k < kSegs; k += blockDim.x) patch_counts[k] = 0ull;
     if (gated_off(gate, 1)) return;
     if (threadIdx.x == 0 && blockIdx.x == 0) *npairs = 0ull;
+}
+
+// Pairs a pair kernel lists go through a per-block staging buffer in shared memory (a shared-memory
+// atomic per appending warp) and reach their segmented list with one global atomic per block at the end
+// (segment blockIdx mod kSegs); entries past the buffer go straight to the list.
+constexpr int kBlockListCap = 1024;
+
+__device__ __forceinline__ void block_list_put(int2 *sbuf, int *sn, int2 e, int2 *list, unsigned long long *counts,
+                                               long long cap, unsigned *flags, unsigned full_flag) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    int q = 0;
+    if (g.thread_rank() == 0) q = atomicAdd(sn, (int)g.size());
+    q = g.shfl(q, 0) + (int)g.thread_rank();
+    if (q < kBlockListCap) sbuf[q] = e;
+    else seg_append<int2>(list, counts, cap, e, flags, full_flag);
+}
+
+// all threads of the block
+__device__ __forceinline__ void block_list_flush(const int2 *sbuf, const int *sn, unsigned long long *sbase,
+                                                 int2 *list, unsigned long long *counts, long long cap,
+                                                 unsigned *flags, unsigned full_flag) {
+    __syncthreads();
+    const int n = *sn < kBlockListCap ? *sn : kBlockListCap;
+    const int k = (int)(blockIdx.x & (kSegs - 1));
+    if (threadIdx.x == 0) *sbase = n ? atomicAdd(counts + k, (unsigned long long)n) : 0ull;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const unsigned long long w = *sbase + (unsigned long long)i;
+        if ((long long)w < cap) list[(size_t)k * (size_t)cap + w] = sbuf[i];
+        else atomicOr(flags, full_flag);
+    }
 }
 
 __device__ __forceinline__ void fixed_add(long long *acc, float v) {
@@ -187,12 +242,23 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
                                                                  long long list_cap = 0,
                                                                  unsigned long long *list_counts = nullptr) {
     constexpr bool BIND = KIND == kPairBind;
+    __shared__ int2 lbuf[kBlockListCap];
+    __shared__ int lnb;
+    __shared__ unsigned long long lbase;
+    if (threadIdx.x == 0) lnb = 0;
+    __syncthreads();
+    unsigned long long *const lcounts = BIND ? a.bind_ctr + kSegPairs : list_counts;
+    const unsigned lflag = BIND ? (kFlagBind | kBindWhyList) : 8u;
     const long long n = (long long)*npairs < cap ? (long long)*npairs : cap;
+    const long long stride = (long long)gridDim.x * blockDim.x;
     bool big = false;
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        const int2 pr = pairs[q];
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int2 next = q < n ? __ldcs(pairs + q) : make_int2(0, 0);
+    for (; q < n; q += stride) {
+        const int2 pr = next;  // the next iteration's entry is loaded one iteration ahead
+        if (q + stride < n) next = __ldcs(pairs + q + stride);
         const int sa = pr.x, sb = pr.y;
-        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, sa);
+        const int r = a.tb.uniform ? 0 : find_replica(a.tb.rep_slot, a.tb.nrep, sa);
         const Replica<float> &R = a.tb.reps[r];
         float xa[4], xb[4];
         load4(a.buf.pos + 4 * (size_t)sa, xa);
@@ -215,7 +281,8 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
             // along d = x_a - x_b: a's cosines are -(n_a . d) / r and b's (n_b . d) / r in either canonical order
             const Model<float> &M = a.tb.models[R.model];
             const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
-            const int tya = type_of<float>(M, ida - R.off), tyb = type_of<float>(M, idb - R.off);
+            const bool single = M.n_types == 1;
+            const int tya = single ? 0 : type_of<float>(M, ida - R.off), tyb = single ? 0 : type_of<float>(M, idb - R.off);
             if (M.np[tya] > 0 && M.np[tyb] > 0) {
                 const float inv = 1.f / sqrtf(r2), pre = M.mincos[tya][tyb] - 4e-5f;
                 float Q[9], w[3];
@@ -237,8 +304,8 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
                         anyb |= v[0] * w[0] + v[1] * w[1] + v[2] * w[2] > pre;
                     }
                     if (anyb)
-                        seg_append<int2>(list, a.bind_ctr + kSegPairs, list_cap,
-                                         ida < idb ? make_int2(sa, sb) : make_int2(sb, sa), a.flags);
+                        block_list_put(lbuf, &lnb, ida < idb ? make_int2(sa, sb) : make_int2(sb, sa), list, lcounts,
+                                       list_cap, a.flags, lflag);
                 }
             }
         }
@@ -274,7 +341,7 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
                             const float *v = M.orient[M.ooff[tyb] + k];
                             anyb |= v[0] * w[0] + v[1] * w[1] + v[2] * w[2] > mcb;
                         }
-                        if (anyb) seg_append<int2>(list, list_counts, list_cap, pr, a.flags, 8u);
+                        if (anyb) block_list_put(lbuf, &lnb, pr, list, lcounts, list_cap, a.flags, lflag);
                     }
                 }
             }
@@ -286,6 +353,7 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
         }
     }
     if (big) atomicOr(a.flags, 2u);
+    block_list_flush(lbuf, &lnb, &lbase, list, lcounts, list_cap, a.flags, lflag);
 }
 
 // the Kern-Frenkel terms of the pairs pairforce_kernel<kPairSplit> listed, one pair per thread, into the
@@ -299,7 +367,7 @@ __global__ void __launch_bounds__(kPipeThreads) patch_pairs_kernel(ForceArgs<flo
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
         const int2 pr = list_all[seg_slot(segs, cap, q)];
         const int sa = pr.x, sb = pr.y;
-        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, sa);
+        const int r = a.tb.uniform ? 0 : find_replica(a.tb.rep_slot, a.tb.nrep, sa);
         const Replica<float> &R = a.tb.reps[r];
         const Model<float> &M = a.tb.models[R.model];
         float xa[4], xb[4];
@@ -332,7 +400,7 @@ __global__ void __launch_bounds__(kPipeThreads) patch_pairs_kernel(ForceArgs<flo
     }
 }
 
-// single-bond mode, a bond-deciding pass: this update's edges of the pairs pairforce_kernel<true> listed
+// single-bond mode, a bond-deciding pass: this update's edges of the pairs pairforce_kernel<kPairBind> listed
 // (canonical order, both particles with a patch near a cone), one pair per thread: every listed pair has
 // passed the cone pre-test, so the lanes of a warp run the patch-pair loop together and overlap the
 // bond-state, snapshot and adjacency accesses of their pairs.

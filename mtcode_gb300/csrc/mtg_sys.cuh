@@ -203,6 +203,7 @@ struct Sys : SysBase {
     int ncells = 0, ncells_obs = 0, ncells_alloc = 0;
 
     mtg::Replica<real> *d_reps = nullptr, *d_reps_obs = nullptr;
+    int reps_uniform = 0, reps_obs_uniform = 0;   // see pair_uniform()
     mtg::Model<real> *d_models = nullptr;
     int *d_rep_slot = nullptr;
     mtg::Buffers<real> buf[2] = {};
@@ -300,7 +301,9 @@ struct Sys : SysBase {
         MTG_CUDA(cudaMalloc(&d_models, sizeof(mtg::Model<real>) * nrep));
         MTG_CUDA(cudaMalloc(&d_rep_slot, sizeof(int) * (nrep + 1)));
         MTG_CUDA(cudaMemcpy(d_reps, reps.data(), sizeof(mtg::Replica<real>) * nrep, cudaMemcpyHostToDevice));
+        reps_uniform = pair_uniform(reps);
         MTG_CUDA(cudaMemcpy(d_reps_obs, reps_obs.data(), sizeof(mtg::Replica<real>) * nrep, cudaMemcpyHostToDevice));
+        reps_obs_uniform = pair_uniform(reps_obs);
         MTG_CUDA(cudaMemcpy(d_models, models.data(), sizeof(mtg::Model<real>) * nrep, cudaMemcpyHostToDevice));
         MTG_CUDA(cudaMemcpy(d_rep_slot, rep_slot.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice));
 
@@ -419,7 +422,36 @@ struct Sys : SysBase {
         t.nrep = nrep;
         t.ntot = ntot_;
         t.ncells = obs ? ncells_obs : ncells;
+        t.uniform = obs ? reps_obs_uniform : reps_uniform;
         return t;
+    }
+
+    // 1 when every replica has replica 0's pair constants (box, boundary, ranges, HSPotential, patch range)
+    // and a model equal to replica 0's with one particle type: a pair's constants then do not depend on
+    // its replica (per-replica fields -- offsets, counts, seeds, cell grid -- are not compared)
+    int pair_uniform(const std::vector<mtg::Replica<real>> &rs) const {
+        if (rs.empty()) return 0;
+        const mtg::Replica<real> &a = rs[0];
+        const mtg::Model<real> &ma = models[a.model];
+        if (ma.n_types != 1) return 0;
+        auto same = [](const void *x, const void *y, size_t n) { return std::memcmp(x, y, n) == 0; };
+        for (const mtg::Replica<real> &b : rs) {
+            if (b.periodic != a.periodic || b.box != a.box || b.half_box != a.half_box || b.l2s != a.l2s ||
+                b.hs_limit != a.hs_limit || b.hs_4eps != a.hs_4eps || b.hs_s6 != a.hs_s6 || b.hs_s12 != a.hs_s12 ||
+                b.hs_eps != a.hs_eps || b.max_dist2 != a.max_dist2 || b.rc2 != a.rc2 || b.patch_r2 != a.patch_r2 ||
+                b.rc2_list != a.rc2_list || b.half_skin2 != a.half_skin2 || b.bond_r != a.bond_r)
+                return 0;
+            const mtg::Model<real> &mb = models[b.model];
+            if (mb.n_types != 1 || !same(mb.np, ma.np, sizeof ma.np) || !same(mb.ooff, ma.ooff, sizeof ma.ooff) ||
+                !same(mb.pstart, ma.pstart, sizeof ma.pstart) || !same(mb.orient, ma.orient, sizeof ma.orient) ||
+                !same(mb.att, ma.att, sizeof ma.att) || !same(mb.dis, ma.dis, sizeof ma.dis) ||
+                !same(mb.inv_dis, ma.inv_dis, sizeof ma.inv_dis) || !same(mb.rmax, ma.rmax, sizeof ma.rmax) ||
+                !same(mb.costm, ma.costm, sizeof ma.costm) || !same(mb.kfac, ma.kfac, sizeof ma.kfac) ||
+                !same(mb.mincos, ma.mincos, sizeof ma.mincos) ||
+                !same(mb.mincos_any, ma.mincos_any, sizeof ma.mincos_any))
+                return 0;
+        }
+        return 1;
     }
 
     int64_t ntot() const override { return ntot_; }
@@ -578,6 +610,8 @@ struct Sys : SysBase {
             reps = reps_full;
             ncells = ncells_full;
             MTG_CUDA(cudaMemcpy(d_reps, reps.data(), sizeof(mtg::Replica<real>) * nrep, cudaMemcpyHostToDevice));
+            reps_uniform = pair_uniform(reps);
+        reps_uniform = pair_uniform(reps);
             forces_ready = false;
             cells_valid = bins_valid = false;
             return;
@@ -719,6 +753,7 @@ struct Sys : SysBase {
         }
         ncells = ncells_obs;
         MTG_CUDA(cudaMemcpy(d_reps, reps.data(), sizeof(mtg::Replica<real>) * nrep, cudaMemcpyHostToDevice));
+        reps_uniform = pair_uniform(reps);
         single_bond = true;
         forces_ready = false;
         cells_valid = bins_valid = false;
