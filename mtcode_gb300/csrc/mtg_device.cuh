@@ -353,6 +353,73 @@ __device__ __forceinline__ int type_of(const Model<real> &M, int local) {
     return t;
 }
 
+// patch_pair for types with at most four patches each: the cosines stay in registers and the in-cone
+// potentials (i, j) are collected in a 16-bit mask (bit 4 i + j) and evaluated in ascending bit order,
+// which is patch_pair's loop order, so sums and counts are the same bit for bit.
+template <class real>
+__device__ __forceinline__ void patch_pair4(const Model<real> &M, int ta_, int tb_, const real *Qa, const real *Qb,
+                                            const real u[3], real r, real bond_r, real f[3], real tqa[3],
+                                            real tqb[3], real &e, int &bonds) {
+    const int na = M.np[ta_], nb = M.np[tb_];
+    real wa[3], wb[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        wa[k] = Qa[3 * k] * u[0] + Qa[3 * k + 1] * u[1] + Qa[3 * k + 2] * u[2];
+        wb[k] = Qb[3 * k] * u[0] + Qb[3 * k + 1] * u[1] + Qb[3 * k + 2] * u[2];
+    }
+    const real mc = M.mincos[ta_][tb_];
+    const int oa = M.ooff[ta_], ob = M.ooff[tb_];
+    real ca[4], cb[4];
+    unsigned ma = 0u, mb = 0u;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        ca[i] = real(0);
+        cb[i] = real(0);
+        if (i < na) {
+            const real *v = M.orient[oa + i];
+            ca[i] = -(v[0] * wa[0] + v[1] * wa[1] + v[2] * wa[2]);
+            if (ca[i] > mc) ma |= 1u << i;
+        }
+        if (i < nb) {
+            const real *v = M.orient[ob + i];
+            cb[i] = v[0] * wb[0] + v[1] * wb[1] + v[2] * wb[2];
+            if (cb[i] > mc) mb |= 1u << i;
+        }
+    }
+    if (!ma || !mb) return;
+    const int ps = M.pstart[ta_][tb_];
+    unsigned m = 0u;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        if (!((ma >> i) & 1u)) continue;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (j >= nb) continue;
+            const int q = ps + i * nb + j;
+            const real cm = M.costm[q];
+            if (!(ca[i] > cm && cb[j] > cm)) continue;
+            if (r < bond_r) bonds++;
+            if (!(r > M.rmax[q])) m |= 1u << (4 * i + j);
+        }
+    }
+    while (m) {
+        const int bit = __ffs(m) - 1;
+        m &= m - 1u;
+        const int i = bit >> 2, j = bit & 3;
+        const real ci = i == 0 ? ca[0] : (i == 1 ? ca[1] : (i == 2 ? ca[2] : ca[3]));
+        const real cj = j == 0 ? cb[0] : (j == 1 ? cb[1] : (j == 2 ? cb[2] : cb[3]));
+        const int q = ps + i * nb + j;
+        const real *b1 = M.orient[oa + i], *b2 = M.orient[ob + j];
+        real n1[3], n2[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            n1[k] = b1[0] * Qa[k] + b1[1] * Qa[3 + k] + b1[2] * Qa[6 + k];
+            n2[k] = b2[0] * Qb[k] + b2[1] * Qb[3 + k] + b2[2] * Qb[6 + k];
+        }
+        kf2_pair<real>(M.att[q], M.dis[q], M.inv_dis[q], M.kfac[q], u, r, n1, n2, ci, cj, f, tqa, tqb, e);
+    }
+}
+
 // All potentials of the canonical pair (a, b): Qa/Qb lab->body rows, u = (x_a - x_b)/r.
 // Returns the number of in-cone potentials; adds force on a, torques on a/b, energy, bonds.
 template <class real>
@@ -360,6 +427,10 @@ __device__ __forceinline__ void patch_pair(const Model<real> &M, int ta_, int tb
                                            const real u[3], real r, real bond_r, real f[3], real tqa[3],
                                            real tqb[3], real &e, int &bonds) {
     const int na = M.np[ta_], nb = M.np[tb_];
+    if (na <= 4 && nb <= 4) {
+        patch_pair4<real>(M, ta_, tb_, Qa, Qb, u, r, bond_r, f, tqa, tqb, e, bonds);
+        return;
+    }
     // body-frame images of u: c_i(patch) = -n_body . (Qa u), c_j = n_body . (Qb u)
     real wa[3], wb[3];
 #pragma unroll
