@@ -98,7 +98,8 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
     // other -- and in the own cell only the later slots.  Smaller grids: every cell, later slots.
     const bool small = nc < 3;
     const int nrows = !valid ? 0 : (small ? 9 : 5);
-    for (int rr = 0; rr < 9; rr++) {  // warp-uniform; rows past a lane's nrows are empty
+    const int nrows_warp = __any_sync(0xffffffffu, nrows == 9) ? 9 : 5;
+    for (int rr = 0; rr < nrows_warp; rr++) {  // warp-uniform; rows past a lane's nrows are empty
         int a0 = 0, a1 = 0, b0 = 0, b1 = 0;
         float shz = 0.f, shy = 0.f, shb = 0.f;
         if (rr < nrows) {
@@ -158,15 +159,24 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
             for (int c0 = t0; __any_sync(0xffffffffu, c0 < t1); c0 += 32) {
                 unsigned mask = 0u;
                 const int ce = t1 < c0 + 32 ? t1 : c0 + 32;
-                for (int t = c0; t < ce; t++) {
-                    const float4 pj = __ldg(reinterpret_cast<const float4 *>(a.buf.pos) + t);
-                    float dx = (pi.x - pj.x) - shx, dy2 = (pi.y - pj.y) - shy, dz2 = (pi.z - pj.z) - shz;
-                    if (small) {  // tiny grids: no cell geometry to lean on
-                        dx = min_image<float>(pi.x - pj.x, R.box, R.l2s, R.periodic);
-                        dy2 = min_image<float>(pi.y - pj.y, R.box, R.l2s, R.periodic);
-                        dz2 = min_image<float>(pi.z - pj.z, R.box, R.l2s, R.periodic);
+                // not unrolled: the lanes' trip counts differ, and an unrolled body keeps the short
+                // lanes idle for longer (measured slower)
+                if (!small) {
+#pragma unroll 1
+                    for (int t = c0; t < ce; t++) {
+                        const float4 pj = __ldg(reinterpret_cast<const float4 *>(a.buf.pos) + t);
+                        const float dx = (pi.x - pj.x) - shx, dy2 = (pi.y - pj.y) - shy, dz2 = (pi.z - pj.z) - shz;
+                        if (sep_r2(dx, dy2, dz2) < range2) mask |= 1u << (t - c0);
                     }
-                    if (sep_r2(dx, dy2, dz2) < range2) mask |= 1u << (t - c0);
+                } else {  // tiny grids: no cell geometry to lean on
+#pragma unroll 1
+                    for (int t = c0; t < ce; t++) {
+                        const float4 pj = __ldg(reinterpret_cast<const float4 *>(a.buf.pos) + t);
+                        const float dx = min_image<float>(pi.x - pj.x, R.box, R.l2s, R.periodic);
+                        const float dy2 = min_image<float>(pi.y - pj.y, R.box, R.l2s, R.periodic);
+                        const float dz2 = min_image<float>(pi.z - pj.z, R.box, R.l2s, R.periodic);
+                        if (sep_r2(dx, dy2, dz2) < range2) mask |= 1u << (t - c0);
+                    }
                 }
                 warp_pair_flush(buf, &nb, s, c0, mask, pairs, npairs, cap, a.flags);
             }
