@@ -156,14 +156,30 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_sums, int &
     return excl;
 }
 
+// A thread's kScanItems cells start at a multiple of 32 bytes of a cudaMalloc'd array: whole groups move as
+// two 16-byte words, the ragged end of the array element by element.
+static_assert(kScanItems == 8, "the scans move a thread's cells as two int4");
+__device__ __forceinline__ void scan_load8(const int *p, int base, int n, int v[8]) {
+    if (base + 8 <= n) {
+        const int4 x = *reinterpret_cast<const int4 *>(p + base), y = *reinterpret_cast<const int4 *>(p + base + 4);
+        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+        v[4] = y.x; v[5] = y.y; v[6] = y.z; v[7] = y.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; k++) v[k] = base + k < n ? p[base + k] : 0;
+    }
+}
+
 __global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const int *count, int n, int *block_sums,
                                                                    const int *gate = nullptr) {
     if (gated_off(gate, 1)) return;
     __shared__ int ws[33];
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int v[kScanItems];
+    scan_load8(count, base, n, v);
     int s = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; k++) s += (base + k < n) ? __ldg(count + base + k) : 0;
+    for (int k = 0; k < kScanItems; k++) s += v[k];
     int total;
     block_exclusive_scan(s, ws, total);
     if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
@@ -199,21 +215,31 @@ __global__ void __launch_bounds__(kScanThreads) scan_down_kernel(int *count, int
     __shared__ int ws[33];
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     int v[kScanItems];
+    scan_load8(count, base, n, v);
     int s = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; k++) {
-        v[k] = (base + k < n) ? count[base + k] : 0;
-        s += v[k];
-    }
+    for (int k = 0; k < kScanItems; k++) s += v[k];
     int total;
     int e = block_exclusive_scan(s, ws, total) + block_sums[blockIdx.x];
+    int o[kScanItems];
 #pragma unroll
     for (int k = 0; k < kScanItems; k++) {
-        if (base + k < n) {
-            start[base + k] = e;
-            count[base + k] = 0;  // ready for the next histogram
-        }
+        o[k] = e;
         e += v[k];
+    }
+    if (base + 8 <= n) {  // the counts are cleared for the next histogram
+        *reinterpret_cast<int4 *>(start + base) = make_int4(o[0], o[1], o[2], o[3]);
+        *reinterpret_cast<int4 *>(start + base + 4) = make_int4(o[4], o[5], o[6], o[7]);
+        *reinterpret_cast<int4 *>(count + base) = make_int4(0, 0, 0, 0);
+        *reinterpret_cast<int4 *>(count + base + 4) = make_int4(0, 0, 0, 0);
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            if (base + k < n) {
+                start[base + k] = o[k];
+                count[base + k] = 0;
+            }
+        }
     }
 }
 

@@ -413,9 +413,11 @@ __global__ void __launch_bounds__(kPipeThreads) patch_pairs_kernel(ForceArgs<flo
 // single-bond mode, a bond-deciding pass: this update's edges of the pairs pairforce_kernel<kPairBind> listed
 // (canonical order, both particles with a patch near a cone), one pair per thread: every listed pair has
 // passed the cone pre-test, so the lanes of a warp run the patch-pair loop together and overlap the
-// bond-state, snapshot and adjacency accesses of their pairs.
-__global__ void __launch_bounds__(kPipeThreads) bind_pairs_kernel(ForceArgs<float> a, const int2 *list_all,
-                                                                long long cap) {
+// bond-state, snapshot and adjacency accesses of their pairs.  Capped at 64 registers (four blocks per SM):
+// the kernel waits on dependent loads and atomics, and more resident warps hide more of that than the few
+// spills (rare branches) cost.
+__global__ void __launch_bounds__(kPipeThreads, 4) bind_pairs_kernel(ForceArgs<float> a, const int2 *list_all,
+                                                                   long long cap) {
     __shared__ long long segs[kSegs + 1];
     seg_prefix(a.bind_ctr + kSegPairs, cap, segs);
     const long long n = segs[kSegs];
