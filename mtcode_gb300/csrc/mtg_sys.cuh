@@ -219,6 +219,8 @@ struct Sys : SysBase {
     uint64_t draw = 0;
     bool have_state = false, cells_valid = false, bins_valid = false, forces_ready = false;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int graph_kernels[2] = {0, 0};   // kernel launches of one step (kernel nodes of its graph)
+    bool capturing = false;          // a step graph is being captured: its launches are counted per replay
     // fixed bonds (CSR by global index) and the id -> slot map the bond pass needs
     int *d_bond_start = nullptr, *d_bond_partner = nullptr, *d_slot_of = nullptr;
     int64_t nbonds = 0;
@@ -460,6 +462,10 @@ struct Sys : SysBase {
     int64_t launches() const override { return nlaunch; }
 
     void check_launch() { MTG_CUDA(cudaGetLastError()); }
+    // k kernels enqueued (outside a graph capture; a replayed step graph adds its own kernel count)
+    void counted(int k) {
+        if (!capturing) nlaunch += k;
+    }
 
     // counting sort of the current buffer by cell (no motion), result in the other buffer
     void rebuild_cells(bool obs) {
@@ -473,7 +479,7 @@ struct Sys : SysBase {
         mtg::scatter_kernel<real, false><<<g, 256, 0, st>>>(tb, buf[cur], buf[cur ^ 1], d_bin, d_start, d_flags);
         check_launch();
         cur ^= 1;
-        nlaunch += 5;
+        nlaunch += 2;  // bin and scatter (the scan counts its own)
         cells_valid = !obs;
         bins_valid = false;
     }
@@ -485,6 +491,7 @@ struct Sys : SysBase {
         mtg::scan_top_kernel<<<1, mtg::kScanThreads, 0, st>>>(d_block, nblk, d_start, n, d_draw, consume_draw ? 1 : 0);
         mtg::scan_down_kernel<<<nblk, mtg::kScanThreads, 0, st>>>(d_count, n, d_block, d_start);
         check_launch();
+        counted(3);
     }
 
     mtg::ForceArgs<real> force_args(int b, int do_kick) {
@@ -519,7 +526,6 @@ struct Sys : SysBase {
     }
 
     // ---------------------------------------------------------------- single-bond-per-patch mode
-    static constexpr int kBindLaunches = 6;   // begin (+ snapshot), edges, unbind, decide, large, bound pairs
 
     mtg::BindState bind_state() const {
         mtg::BindState S;
@@ -551,9 +557,11 @@ struct Sys : SysBase {
     // the particles) takes its snapshot from buffer b at once, a step's from the scatter
     void enqueue_bind_begin(int b, int force, int advance) {
         mtg::bind_begin_kernel<<<1, 32, 0, st>>>(bind_state(), force, advance);
+        counted(1);
         if (force) {
             const int g = grid_for(ntot_, 256, occ_stream, sms);
             mtg::bind_snapshot_kernel<real><<<g, 256, 0, st>>>(ntot_, buf[b]);
+            counted(1);
         }
     }
 
@@ -564,6 +572,7 @@ struct Sys : SysBase {
         mtg::bind_unbind_kernel<<<grid_for(ptot, 256, occ_stream, sms), 256, 0, st>>>(S);
         mtg::bind_decide_kernel<<<grid_for(ptot, 256, 4, sms), 256, 0, st>>>(S);
         mtg::bind_large_kernel<real><<<scratch_threads / mtg::kLargeThreads, mtg::kLargeThreads, 0, st>>>(a, S);
+        counted(3);
     }
 
     void free_bind() {
@@ -585,6 +594,7 @@ struct Sys : SysBase {
         for (int b = 0; b < 2; b++) {
             if (graph[b]) cudaGraphExecDestroy(graph[b]);
             graph[b] = nullptr;
+            graph_kernels[b] = 0;
         }
     }
 
@@ -807,7 +817,6 @@ struct Sys : SysBase {
         if (!cells_valid) rebuild_cells(false);
         tick_draw();
         enqueue_bind_begin(cur, 1, 0);
-        nlaunch += kBindLaunches;
         size_t n = (size_t)ntot_;
         double *sF = d_stage, *sT = sF + 3 * n;
         mtg::ForceArgs<real> a = force_args(cur, 0);
@@ -815,7 +824,6 @@ struct Sys : SysBase {
         a.outT = sT;
         launch_force<mtg::kModeForces>(a, true);
         check_launch();
-        nlaunch += 1;
         if (F) MTG_CUDA(cudaMemcpyAsync(F, sF, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
         if (T) MTG_CUDA(cudaMemcpyAsync(T, sT, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
         MTG_CUDA(cudaStreamSynchronize(st));
@@ -864,21 +872,25 @@ struct Sys : SysBase {
                                                                                   d_acc);
                 }
                 mtg::pair_epilogue_kernel<MODE><<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_acc);
+                counted(bind ? 6 : 5);  // (enqueue_bind_decide counts its own)
                 return;
             }
             if (use_tiles && MODE != mtg::kModeObs && !a.outE) {
                 const int g = std::max(1, std::min(ntiles, occ_tile * sms));  // persistent: one CTA per SM
                 mtg::tile_force_kernel<MODE><<<g, mtg::kTileThreads, tile_smem, st>>>(a, d_tiles, ntiles);
+                counted(1);
                 return;
             }
         }
         const int gf = grid_for(ntot_, 128, occ_force, sms);
         if (bind) {   // the per-particle form: an edges-only pass, the decisions, then the force pass
             mtg::force_kernel<real, mtg::kModeEdges><<<gf, 128, 0, st>>>(a);
+            counted(1);
             decide();
             a.bind_deg = nullptr;
         }
         mtg::force_kernel<real, MODE><<<gf, 128, 0, st>>>(a);
+        counted(1);
     }
 
     // a skin-list step on buffer b (which stays the buffer in use): the decision, then either the
@@ -896,6 +908,7 @@ struct Sys : SysBase {
         mtg::scatter_kernel<real, true><<<g, 256, 0, st>>>(tb, buf[b], buf[b ^ 1], d_bin, d_start, d_flags, d_skin);
         mtg::copy_back_kernel<real><<<g, 256, 0, st>>>(ntot_, buf[b ^ 1], buf[b], d_skin);
         mtg::integrate_kernel<real><<<g, 256, 0, st>>>(tb, buf[b], d_flags, d_skin);
+        counted(8);
         mtg::ForceArgs<real> a = force_args(b, 1);
         a.ext_noise = ext_noise;
         launch_force<mtg::kModeStep>(a);
@@ -937,6 +950,7 @@ struct Sys : SysBase {
         const int g = grid_for(ntot_, 256, occ_stream, sms);
         mtg::scatter_kernel<real, true><<<g, 256, 0, st>>>(tb, buf[b], buf[b ^ 1], d_bin, d_start, d_flags, nullptr,
                                                            single_bond ? d_bctr + 4 : nullptr);
+        counted(1);
         mtg::ForceArgs<real> a = force_args(b ^ 1, 1);
         a.ext_noise = ext_noise;
         launch_force<mtg::kModeStep>(a, true);
@@ -1022,13 +1036,11 @@ struct Sys : SysBase {
         }
         if (single_bond) {   // run_singlebond's first onlyone_nonlets call (Condensate.cpp:455-460)
             enqueue_bind_begin(cur, 1, 0);
-            nlaunch += kBindLaunches;
         }
         mtg::ForceArgs<real> a = force_args(cur, 0);
         if (noise) a.ext_noise = upload_noise(noise);
         launch_force<mtg::kModeInit>(a, true);
         check_launch();
-        nlaunch += 1;
         cells_valid = true;
         bins_valid = true;
         forces_ready = true;
@@ -1037,8 +1049,21 @@ struct Sys : SysBase {
     void build_graph(int b) {
         cudaGraph_t g;
         MTG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        capturing = true;
         enqueue_step(b, nullptr);
+        capturing = false;
         MTG_CUDA(cudaStreamEndCapture(st, &g));
+        size_t nn = 0;
+        MTG_CUDA(cudaGraphGetNodes(g, nullptr, &nn));
+        std::vector<cudaGraphNode_t> nodes(nn);
+        if (nn) MTG_CUDA(cudaGraphGetNodes(g, nodes.data(), &nn));
+        int k = 0;
+        for (cudaGraphNode_t nd : nodes) {
+            cudaGraphNodeType t;
+            MTG_CUDA(cudaGraphNodeGetType(nd, &t));
+            if (t == cudaGraphNodeTypeKernel) k++;
+        }
+        graph_kernels[b] = k;
         MTG_CUDA(cudaGraphInstantiate(&graph[b], g, 0));
         MTG_CUDA(cudaGraphDestroy(g));
     }
@@ -1122,7 +1147,6 @@ struct Sys : SysBase {
             for (int s = 0; s < nsteps; s++) {
                 enqueue_step(cur, upload_noise(noise + (size_t)s * 6 * n));
                 if (skin <= 0) cur ^= 1;  // a skin step leaves the state in the buffer it started in
-                nlaunch += (skin > 0 ? 9 : 5) + (single_bond ? kBindLaunches : 0);
                 draw += 1;
             }
             MTG_CUDA(cudaStreamSynchronize(st));
@@ -1130,8 +1154,8 @@ struct Sys : SysBase {
             for (int s = 0; s < nsteps; s++) {
                 if (!graph[cur]) build_graph(cur);
                 MTG_CUDA(cudaGraphLaunch(graph[cur], st));
+                nlaunch += graph_kernels[cur];
                 if (skin <= 0) cur ^= 1;
-                nlaunch += (skin > 0 ? 9 : 5) + (single_bond ? kBindLaunches : 0);
                 draw += 1;
             }
         }
@@ -1177,7 +1201,7 @@ struct Sys : SysBase {
                 MTG_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
                 acc[k] += ms;
             }
-            nlaunch += 9;
+            nlaunch += 8;  // the explicit kernels above (launch_force counts its own)
             draw += 1;
         }
         for (int s = 0; s < nsteps && skin <= 0; s++) {
@@ -1212,7 +1236,7 @@ struct Sys : SysBase {
             acc[5] += ms;
             acc[6] += bind_ms;
             cur ^= 1;
-            nlaunch += 5 + (single_bond ? kBindLaunches : 0);
+            nlaunch += 4;  // the scans and the scatter (launch_force and bind begin count their own)
             draw += 1;
         }
         for (auto &e : ev) cudaEventDestroy(e);
@@ -1244,7 +1268,6 @@ struct Sys : SysBase {
         a.outE = E ? sE : nullptr;
         launch_force<mtg::kModeForces>(a);
         check_launch();
-        nlaunch += 1;
         MTG_CUDA(cudaMemcpyAsync(F, sF, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
         MTG_CUDA(cudaMemcpyAsync(T, sT, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
         if (E) MTG_CUDA(cudaMemcpyAsync(E, sE, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
@@ -1281,7 +1304,6 @@ struct Sys : SysBase {
         std::vector<double> h(6 * (size_t)nrep);
         launch_force<mtg::kModeObs>(a);
         check_launch();
-        nlaunch += 1;
         MTG_CUDA(cudaMemcpyAsync(h.data(), d_obs, sizeof(double) * 6 * nrep, cudaMemcpyDeviceToHost, st));
         MTG_CUDA(cudaStreamSynchronize(st));
         for (int r = 0; r < nrep; r++)

@@ -125,3 +125,26 @@ def test_full_size_batch_newton_third_law_and_finiteness(kernel):
     for r, spec in enumerate(W.replicas):
         xr = st["x"][off[r]:off[r + 1]]
         assert (xr >= 0).all() and (xr <= spec.box).all()
+
+
+@pytest.mark.parametrize("kernel,single_bond,per_step", [("pairs", False, 9), ("tiled", False, 5),
+                                                         ("per_particle", False, 5), ("pairs", True, 14)])
+def test_launch_count_per_step(kernel, single_bond, per_step):
+    """mtg_launches counts every kernel a step replays: scans (3) + scatter + the force pass (pair pipeline:
+    reset, pairfind, pairforce, patch pairs, epilogue; single-bond mode: bind begin, the edge and bound-pair
+    passes and the three decision kernels instead of the patch pairs)."""
+    from mtcode_gb300.system import binding_single
+    W = small_batch(seed=6, n_replicas=4)
+    z = W.zeros3()
+    with LangevinNVTRGPU(W.replicas, force_kernel=kernel) as s:
+        s.initialize(W.x, z, z, W.Q)
+        if single_bond:
+            s.set_single_bond(binding_single(1.0, 0.1))
+        s.init_forces()
+        s.step(2)
+        s.sync()
+        l0 = s.launches
+        s.step(5)
+        s.sync()
+        assert s.launches - l0 == 5 * per_step
+        assert s.flags == 0
