@@ -35,13 +35,14 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "particle-steps/s on 1 GB300, batched FP32 vs plain FP64, force rel err <=1e-5"
 UNIT = "particle-steps/s"
-# algorithmic bytes per particle (FP32 rows of 48 B)
+# algorithmic bytes per particle (FP32 rows of 48 B): what a pass must read and write once per particle
 BYTES_FORCE = 48 + 24 + 4 + 48 + 8 + 4          # own x,Q + p,L + id; write p,L,F~,T~ + bin + histogram
 BYTES_SCATTER = 8 + 4 + 48 + 48 + 4 + 24 + 48 + 24 + 4 + 24  # bin,start,row,row,id,disp -> row,p+L,id,disp
 BYTES_SCAN_PER_CELL = 16
 # measured DRAM bytes per particle and launch (ncu dram__bytes_read + dram__bytes_write on 160 replicas,
-# state larger than L2; profiles/step_dram_traffic_c4x160.md), scaled by the particle count
-TRAFFIC_PER_PARTICLE = {"force": 383.0, "scatter": 231.1}
+# state larger than L2; profiles/step_dram_traffic_c4x160.md), scaled by the particle count.  Force pass:
+# pairfind + pairforce + patch pairs + epilogue.
+TRAFFIC_PER_PARTICLE = {"force": 422.0, "scatter": 233.1}
 
 
 def metric_of(args) -> str:
