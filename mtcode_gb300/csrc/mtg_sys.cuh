@@ -1049,9 +1049,14 @@ struct Sys : SysBase {
     void build_graph(int b) {
         cudaGraph_t g;
         MTG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        capturing = true;
-        enqueue_step(b, nullptr);
-        capturing = false;
+        {
+            struct Capturing {
+                bool &f;
+                explicit Capturing(bool &x) : f(x) { f = true; }
+                ~Capturing() { f = false; }
+            } guard(capturing);  // cleared on every exit, an exception included
+            enqueue_step(b, nullptr);
+        }
         MTG_CUDA(cudaStreamEndCapture(st, &g));
         size_t nn = 0;
         MTG_CUDA(cudaGraphGetNodes(g, nullptr, &nn));

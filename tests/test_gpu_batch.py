@@ -148,3 +148,32 @@ def test_launch_count_per_step(kernel, single_bond, per_step):
         s.sync()
         assert s.launches - l0 == 5 * per_step
         assert s.flags == 0
+
+
+def test_identical_replicas_in_batch_equal_each_alone():
+    """A batch whose replicas share every pair constant (same size, box, model) takes the pair kernels'
+    uniform form (no per-pair replica search); each replica still equals the same replica run alone."""
+    from mtcode_gb300.system import PatchModelSpec, ReplicaSpec, random_positions, random_rotations
+    n = 900
+    box = workloads.box_for(n, 0.15)
+    model = PatchModelSpec.tetrahedral(n, 8.0, 1.2, math.acos(0.9))
+    reps = [ReplicaSpec(n=n, box=box, model=model, kT=0.0, seed=40 + r) for r in range(3)]
+    xs = [random_positions(n, box, True, 0.95, 50 + r) for r in range(3)]
+    Qs = [random_rotations(n, 60 + r) for r in range(3)]
+    x, Q = np.concatenate(xs), np.concatenate(Qs)
+    z = np.zeros((3 * n, 3))
+    with LangevinNVTRGPU(reps, force_kernel="pairs") as s:
+        s.initialize(x, z, z, Q)
+        s.init_forces()
+        s.step(25)
+        batch = s.get_state()
+        assert s.flags == 0
+    for r in range(3):
+        zz = np.zeros((n, 3))
+        with LangevinNVTRGPU([reps[r]], force_kernel="pairs") as s1:
+            s1.initialize(xs[r], zz, zz, Qs[r])
+            s1.init_forces()
+            s1.step(25)
+            alone = s1.get_state()
+        for key in ("x", "p", "Lb", "Q"):
+            assert np.array_equal(batch[key][r * n:(r + 1) * n], alone[key]), (r, key)
