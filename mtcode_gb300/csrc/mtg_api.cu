@@ -269,8 +269,7 @@ mtg_status mtg_pairs(mtg_system *h, int replica, double rc, int32_t *pairs, int6
 mtg_status mtg_temperature(mtg_system *h, double *out) {
     MTG_GUARD(h, {
         if (!out) throw Fail{MTG_ERR_ARG, "mtg_temperature: null output"};
-        h->impl->temperature(out);
-        if (h->impl->flags() & MTG_FLAG_NONFINITE) return MTG_ERR_NONFINITE;
+        if (h->impl->temperature(out) & MTG_FLAG_NONFINITE) return MTG_ERR_NONFINITE;
     });
     return MTG_OK;
 }

@@ -55,6 +55,15 @@ struct Tables {
                    // read replica 0 instead of searching the slot's replica
 };
 
+// the device's noise-draw counter (draw used by the next pass, next draw), set from the host by value: a
+// kernel parameter, so the call neither waits for the stream nor needs a host buffer that outlives it
+__global__ void draw_set_kernel(unsigned long long *draw, unsigned long long now, unsigned long long next) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        draw[0] = now;
+        draw[1] = next;
+    }
+}
+
 __device__ __forceinline__ int find_replica(const int *rep_slot, int nrep, int s) {
     int lo = 0, hi = nrep;  // rep_slot[lo] <= s < rep_slot[hi]
     while (hi - lo > 1) {
@@ -1201,34 +1210,104 @@ __global__ void store_state_kernel(int ntot, Buffers<real> in, double *x, double
 }
 
 // LangevinNVTR::measured_temperature sums (LangevinR.cpp:170-193): per replica sum p_k^2, sum L_k^2
-template <class real>
-__global__ void __launch_bounds__(256) temperature_kernel(Tables<real> tb, Buffers<real> in, double *out, int chunk) {
-    // block b sums slots [b * chunk, (b + 1) * chunk): replicas are contiguous slot ranges, so a thread's
-    // slots almost always belong to one replica and it adds them up before one warp reduction
-    const int base = blockIdx.x * chunk;
-    const int end = min(base + chunk, tb.ntot);
-    double acc[6] = {0, 0, 0, 0, 0, 0};
-    int cur = -1;
-    for (int s = base + threadIdx.x; s < end; s += blockDim.x) {
-        const int r = find_replica(tb.rep_slot, tb.nrep, s);
-        if (r != cur) {
-            if (cur >= 0)
-                for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)cur + k, acc[k]);
-            cur = r;
-            for (int k = 0; k < 6; k++) acc[k] = 0.0;
-        }
-        Row<real> M;
-        M.load(in.motion + (size_t)s * kRow);
-        for (int k = 0; k < 6; k++) acc[k] += (double)M.v[k] * (double)M.v[k];
+// p and L of a motion row (its first six values)
+__device__ __forceinline__ void load_pl(const float *row, float v[6]) {
+    const float4 a = __ldg(reinterpret_cast<const float4 *>(row));
+    const float2 b = __ldg(reinterpret_cast<const float2 *>(row + 4));
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y;
+}
+__device__ __forceinline__ void load_pl(const double *row, double v[6]) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const double2 a = __ldg(reinterpret_cast<const double2 *>(row) + k);
+        v[2 * k] = a.x;
+        v[2 * k + 1] = a.y;
     }
+}
+
+// Sum of squares of a thread's values.  FP32 rows: each square is split exactly into two floats (product
+// and its rounding error, by FMA) and added with TwoSum, so the float pair (hi, lo) carries about 48 bits
+// and the result matches a double-precision sum of the squares to ~1e-14 relative without FP64 arithmetic
+// per particle.  FP64 rows: plain double arithmetic.
+template <class real> struct SqSum;
+template <> struct SqSum<float> {
+    float hi[6], lo[6];
+    __device__ __forceinline__ void clear() {
+#pragma unroll
+        for (int k = 0; k < 6; k++) hi[k] = lo[k] = 0.f;
+    }
+    __device__ __forceinline__ void add(const float v[6]) {
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            const float p = __fmul_rn(v[k], v[k]), pe = __fmaf_rn(v[k], v[k], -p);   // p + pe = v^2 exactly
+            const float s = __fadd_rn(hi[k], p), bb = __fsub_rn(s, hi[k]);
+            const float e = __fadd_rn(__fsub_rn(hi[k], __fsub_rn(s, bb)), __fsub_rn(p, bb));  // hi + p = s + e
+            hi[k] = s;
+            lo[k] = __fadd_rn(lo[k], __fadd_rn(e, pe));
+        }
+    }
+    __device__ __forceinline__ double get(int k) const { return (double)hi[k] + (double)lo[k]; }
+};
+template <> struct SqSum<double> {
+    double v_[6];
+    __device__ __forceinline__ void clear() {
+#pragma unroll
+        for (int k = 0; k < 6; k++) v_[k] = 0.0;
+    }
+    __device__ __forceinline__ void add(const double v[6]) {
+#pragma unroll
+        for (int k = 0; k < 6; k++) v_[k] += v[k] * v[k];
+    }
+    __device__ __forceinline__ double get(int k) const { return v_[k]; }
+};
+
+constexpr int kTempPerThread = 8;   // slots per thread: a block of 256 threads sums 2048 slots
+
+template <class real>
+__global__ void __launch_bounds__(256) temperature_kernel(Tables<real> tb, Buffers<real> in, double *out) {
+    // block b sums slots [b * 2048, (b + 1) * 2048): replicas are contiguous slot ranges, so a thread's
+    // slots almost always belong to one replica.  A thread loads all its rows first (independent loads in
+    // flight together), then walks the replica boundaries in slot order, adds its slots of a replica up,
+    // and the warp reduces before the atomics.
+    const int base = blockIdx.x * (kTempPerThread * blockDim.x) + threadIdx.x;
+    real v[kTempPerThread][6];
+#pragma unroll
+    for (int i = 0; i < kTempPerThread; i++) {
+        const int s = base + i * blockDim.x;
+        if (s < tb.ntot) {
+            load_pl(in.motion + (size_t)s * kRow, v[i]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 6; k++) v[i][k] = real(0);
+        }
+    }
+    SqSum<real> acc;
+    acc.clear();
+    int cur = -1, next_start = 0;
+#pragma unroll
+    for (int i = 0; i < kTempPerThread; i++) {
+        const int s = base + i * blockDim.x;
+        if (s >= tb.ntot) break;
+        if (s >= next_start) {  // a replica boundary (slots ascend)
+            if (cur >= 0)
+                for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)cur + k, acc.get(k));
+            cur = find_replica(tb.rep_slot, tb.nrep, s);
+            next_start = __ldg(tb.rep_slot + cur + 1);
+            acc.clear();
+        }
+        acc.add(v[i]);
+    }
+    double d[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) d[k] = acc.get(k);
     const unsigned peers = __match_any_sync(0xffffffffu, cur);
     if (peers == 0xffffffffu) {
         for (int k = 0; k < 6; k++)
-            for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], o);
+            for (int o = 16; o > 0; o >>= 1) d[k] += __shfl_down_sync(0xffffffffu, d[k], o);
         if ((threadIdx.x & 31) == 0 && cur >= 0)
-            for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)cur + k, acc[k]);
+            for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)cur + k, d[k]);
     } else if (cur >= 0) {
-        for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)cur + k, acc[k]);
+        for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)cur + k, d[k]);
     }
 }
 

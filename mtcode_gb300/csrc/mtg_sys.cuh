@@ -216,6 +216,7 @@ struct Sys : SysBase {
     double *d_noise = nullptr;   // ntot x 6 (external noise)
     double *d_obs = nullptr;     // nrep x 6
     unsigned *h_flags = nullptr; // pinned
+    double *h_obs = nullptr;     // pinned: the temperature read-back
     uint64_t draw = 0;
     bool have_state = false, cells_valid = false, bins_valid = false, forces_ready = false;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -413,6 +414,7 @@ struct Sys : SysBase {
         cudaFree(d_pairs); cudaFree(d_npairs); cudaFree(d_acc); cudaFree(d_patch_list); cudaFree(d_patch_ctr);
         free_bind();
         if (h_flags) cudaFreeHost(h_flags);
+        if (h_obs) cudaFreeHost(h_obs);
         if (st) cudaStreamDestroy(st);
     }
 
@@ -1011,11 +1013,16 @@ struct Sys : SysBase {
         MTG_CUDA(cudaStreamSynchronize(st));
     }
 
+    // the device draw counter <- (now, next)
+    void set_device_draw(unsigned long long now, unsigned long long next) {
+        mtg::draw_set_kernel<<<1, 32, 0, st>>>(d_draw, now, next);
+        check_launch();
+        counted(1);
+    }
+
     void tick_draw() {
         // draw[0] <- draw[1]++ for a pass that does not run the scan
-        unsigned long long h[2] = {draw, draw + 1};
-        MTG_CUDA(cudaMemcpyAsync(d_draw, h, sizeof(h), cudaMemcpyHostToDevice, st));
-        MTG_CUDA(cudaStreamSynchronize(st));
+        set_device_draw(draw, draw + 1);
         draw += 1;
     }
 
@@ -1145,8 +1152,7 @@ struct Sys : SysBase {
             bins_valid = true;
         }
         // the device draw counter follows the host one
-        unsigned long long h[2] = {draw, draw};
-        MTG_CUDA(cudaMemcpyAsync(d_draw, h, sizeof(h), cudaMemcpyHostToDevice, st));
+        set_device_draw(draw, draw);
         size_t n = (size_t)ntot_;
         if (noise) {
             for (int s = 0; s < nsteps; s++) {
@@ -1172,8 +1178,7 @@ struct Sys : SysBase {
         if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_step_profile: no state has been set"};
         MTG_REQUIRE(nsteps >= 1 && kernel_ms, "mtg_step_profile: nsteps >= 1 and an output are required");
         step(0, nullptr);  // initial forces / bins, as mtg_step would
-        unsigned long long h[2] = {draw, draw};
-        MTG_CUDA(cudaMemcpyAsync(d_draw, h, sizeof(h), cudaMemcpyHostToDevice, st));
+        set_device_draw(draw, draw);
         cudaEvent_t ev[10];
         for (auto &e : ev) MTG_CUDA(cudaEventCreate(&e));
         double acc[MTG_PROFILE_KERNELS] = {};
@@ -1279,16 +1284,20 @@ struct Sys : SysBase {
         MTG_CUDA(cudaStreamSynchronize(st));
     }
 
-    void temperature(double *out) override {
+    uint32_t temperature(double *out) override {
         if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_temperature: no state has been set"};
         MTG_CUDA(cudaMemsetAsync(d_obs, 0, sizeof(double) * 6 * nrep, st));
-        const int chunk = 256 * 8;
+        const int chunk = 256 * mtg::kTempPerThread;
         mtg::temperature_kernel<real><<<std::max(1, (ntot_ + chunk - 1) / chunk), 256, 0, st>>>(tables(), buf[cur],
-                                                                                              d_obs, chunk);
+                                                                                              d_obs);
         check_launch();
         nlaunch += 1;
-        MTG_CUDA(cudaMemcpyAsync(out, d_obs, sizeof(double) * 6 * nrep, cudaMemcpyDeviceToHost, st));
-        MTG_CUDA(cudaStreamSynchronize(st));
+        if (!h_obs) MTG_CUDA(cudaMallocHost(&h_obs, sizeof(double) * 6 * nrep));  // pinned: an asynchronous copy
+        MTG_CUDA(cudaMemcpyAsync(h_obs, d_obs, sizeof(double) * 6 * nrep, cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaMemcpyAsync(h_flags, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));  // one round trip for the sums and the flags
+        std::memcpy(out, h_obs, sizeof(double) * 6 * nrep);
+        const uint32_t fl = *h_flags;
         for (int r = 0; r < nrep; r++) {
             double n = (double)desc[r].n;
             for (int k = 0; k < 3; k++) {
@@ -1296,6 +1305,7 @@ struct Sys : SysBase {
                 out[6 * r + 3 + k] = out[6 * r + 3 + k] / (2. * desc[r].inertia) / n;
             }
         }
+        return fl;
     }
 
     void observables(double *out) override {

@@ -43,7 +43,7 @@ struct SysBase {
     virtual void clusters(int, double, int32_t *) = 0;
     virtual int64_t rebuilds() = 0;
     virtual mtg_status pairs(int, double, int32_t *, int64_t, int64_t *) = 0;
-    virtual void temperature(double *) = 0;
+    virtual uint32_t temperature(double *) = 0;   // returns the status flags, read with the result
     virtual void observables(double *) = 0;
     virtual void displacement(double *) = 0;
     virtual void set_draw(uint64_t) = 0;
