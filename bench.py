@@ -329,20 +329,22 @@ def run_e2e(s, W, args, stream, ev0, ev1) -> dict:
     pinned = {k: torch.empty(v.shape, dtype=torch.float64, pin_memory=True).numpy() for k, v in state.items()}
     for k in pinned:
         pinned[k][...] = state[k]
-    temps = torch.empty((R, 6), dtype=torch.float64, pin_memory=True).numpy()
     out = {k: torch.empty(v.shape, dtype=torch.float64, pin_memory=True).numpy() for k, v in state.items()}
     k_e2e = max(10, args.steps // 2)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     ev0.record(stream)
     s.initialize(pinned["x"], pinned["p"], pinned["Lb"], pinned["Q"], pinned["Ft"], pinned["Tt"])
-    for _ in range(k_e2e):
+    temps = np.empty((k_e2e, R, 6))
+    for i in range(k_e2e):  # Condensate::run: a step, then the temperature read back to the host
         s.step(1)
-        temps[...] = s.measured_temperature()
+        temps[i] = s.measured_temperature()
     st = s.get_state(out)
     ev1.record(stream)
     ev1.synchronize()
     wall = time.perf_counter() - t0
+    if temps.shape != (k_e2e, R, 6) or not np.isfinite(temps).all() or not np.isfinite(st["x"]).all():
+        raise RuntimeError("e2e: non-finite temperatures or state")
     h2d = n * (3 + 3 + 3 + 9 + 3 + 3) * 8
     d2h_state = n * (3 + 3 + 3 + 9 + 3 + 3) * 8
     return {"value": n * k_e2e / wall, "unit": UNIT, "h2d_bytes_per_step": h2d / k_e2e,

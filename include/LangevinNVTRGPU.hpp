@@ -270,6 +270,12 @@ class LangevinNVTRGPU {
         for (int k = 0; k < 6; k++) ret[k] = t[k];
     }
 
+    // nsteps of the loop body, each followed by measured_temperature of that step, with no host round trip
+    // between steps: out holds nsteps x n_replicas x 6 (step-major) when the call returns
+    void step_measured(int nsteps, double *out) {
+        mtg_adapter::require_ok(h_, mtg_step_temperatures(h_, nsteps, out), "step_measured");
+    }
+
     // getdat / getmom / getorientation / getangmom (LangevinR.h:190-196), into caller matrices
     void getdat(Matrix &x) { get(0, x); }
     void getmom(Matrix &p) { get(1, p); }

@@ -177,6 +177,12 @@ mtg_status mtg_pairs(mtg_system *h, int replica, double rc, int32_t *pairs, int6
  * (<p_k^2/2m>, <L_k^2/2I>, k = x,y,z).  out: n_replicas x 6. Synchronising. */
 mtg_status mtg_temperature(mtg_system *h, double *out);
 
+/* nsteps steps of mtg_step, each followed by mtg_temperature's per-replica sums of that step, as
+ * Condensate::run measures the temperature every step (Condensate.cpp:335-378).  Every step's sums are
+ * copied to pinned host memory as the step completes (an asynchronous copy per step, no host round trip
+ * between steps); the call synchronises once at the end.  out: nsteps x n_replicas x 6, step-major. */
+mtg_status mtg_step_temperatures(mtg_system *h, int nsteps, double *out);
+
 /* Per-replica FP64 observables at the current state, out: n_replicas x MTG_OBS_COUNT:
  *  [0] KF2 patch energy, [1] WCA energy (+eps shifted, r < 1.12246 sigma), [2] virial sum r.f,
  *  [3] bonded patch pairs (LangevinNVTR::calculate_bound_pairs criterion, LangevinR.cpp:1854-1998),

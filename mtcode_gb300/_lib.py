@@ -122,6 +122,7 @@ SIGNATURES = [
     ("mtg_clusters", C.c_int, [_H, C.c_int, C.c_double, _I32]),
     ("mtg_pairs", C.c_int, [_H, C.c_int, C.c_double, _I32, C.c_int64, C.POINTER(C.c_int64)]),
     ("mtg_temperature", C.c_int, [_H, _D]),
+    ("mtg_step_temperatures", C.c_int, [_H, C.c_int, _D]),
     ("mtg_observables", C.c_int, [_H, _D]),
     ("mtg_get_displacement", C.c_int, [_H, _D]),
     ("mtg_get_draw", C.c_uint64, [_H]),

@@ -274,6 +274,15 @@ mtg_status mtg_temperature(mtg_system *h, double *out) {
     return MTG_OK;
 }
 
+mtg_status mtg_step_temperatures(mtg_system *h, int nsteps, double *out) {
+    MTG_GUARD(h, {
+        if (nsteps < 0) throw Fail{MTG_ERR_ARG, "mtg_step_temperatures: nsteps must be >= 0"};
+        if (!out && nsteps > 0) throw Fail{MTG_ERR_ARG, "mtg_step_temperatures: null output"};
+        if (h->impl->step_temperatures(nsteps, out) & MTG_FLAG_NONFINITE) return MTG_ERR_NONFINITE;
+    });
+    return MTG_OK;
+}
+
 mtg_status mtg_observables(mtg_system *h, double *out) {
     MTG_GUARD(h, {
         if (!out) throw Fail{MTG_ERR_ARG, "mtg_observables: null output"};

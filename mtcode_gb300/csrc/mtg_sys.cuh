@@ -216,7 +216,8 @@ struct Sys : SysBase {
     double *d_noise = nullptr;   // ntot x 6 (external noise)
     double *d_obs = nullptr;     // nrep x 6
     unsigned *h_flags = nullptr; // pinned
-    double *h_obs = nullptr;     // pinned: the temperature read-back
+    double *h_obs = nullptr;     // pinned: temperature read-backs (one slot of 6 x nrep per step)
+    size_t h_obs_cap = 0;
     uint64_t draw = 0;
     bool have_state = false, cells_valid = false, bins_valid = false, forces_ready = false;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -1284,28 +1285,57 @@ struct Sys : SysBase {
         MTG_CUDA(cudaStreamSynchronize(st));
     }
 
-    uint32_t temperature(double *out) override {
-        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_temperature: no state has been set"};
+    // the per-replica sums of p^2 and L^2 at the current state into pinned host memory (asynchronous)
+    void enqueue_temperature(double *h_dst) {
         MTG_CUDA(cudaMemsetAsync(d_obs, 0, sizeof(double) * 6 * nrep, st));
         const int chunk = 256 * mtg::kTempPerThread;
         mtg::temperature_kernel<real><<<std::max(1, (ntot_ + chunk - 1) / chunk), 256, 0, st>>>(tables(), buf[cur],
                                                                                               d_obs);
         check_launch();
         nlaunch += 1;
-        if (!h_obs) MTG_CUDA(cudaMallocHost(&h_obs, sizeof(double) * 6 * nrep));  // pinned: an asynchronous copy
-        MTG_CUDA(cudaMemcpyAsync(h_obs, d_obs, sizeof(double) * 6 * nrep, cudaMemcpyDeviceToHost, st));
-        MTG_CUDA(cudaMemcpyAsync(h_flags, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-        MTG_CUDA(cudaStreamSynchronize(st));  // one round trip for the sums and the flags
-        std::memcpy(out, h_obs, sizeof(double) * 6 * nrep);
-        const uint32_t fl = *h_flags;
+        MTG_CUDA(cudaMemcpyAsync(h_dst, d_obs, sizeof(double) * 6 * nrep, cudaMemcpyDeviceToHost, st));
+    }
+    // sums -> <p_k^2/2m>, <L_k^2/2I> of each replica
+    void normalise_temperature(const double *sums, double *out) const {
         for (int r = 0; r < nrep; r++) {
             double n = (double)desc[r].n;
             for (int k = 0; k < 3; k++) {
-                out[6 * r + k] = out[6 * r + k] / (2. * desc[r].mass) / n;
-                out[6 * r + 3 + k] = out[6 * r + 3 + k] / (2. * desc[r].inertia) / n;
+                out[6 * r + k] = sums[6 * r + k] / (2. * desc[r].mass) / n;
+                out[6 * r + 3 + k] = sums[6 * r + 3 + k] / (2. * desc[r].inertia) / n;
             }
         }
-        return fl;
+    }
+    void ensure_obs_ring(size_t doubles) {
+        if (doubles <= h_obs_cap) return;
+        if (h_obs) cudaFreeHost(h_obs);
+        h_obs = nullptr;
+        h_obs_cap = 0;
+        MTG_CUDA(cudaMallocHost(&h_obs, sizeof(double) * doubles));  // pinned: asynchronous copies
+        h_obs_cap = doubles;
+    }
+
+    uint32_t temperature(double *out) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_temperature: no state has been set"};
+        ensure_obs_ring((size_t)6 * nrep);
+        enqueue_temperature(h_obs);
+        MTG_CUDA(cudaMemcpyAsync(h_flags, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));  // one round trip for the sums and the flags
+        normalise_temperature(h_obs, out);
+        return *h_flags;
+    }
+
+    uint32_t step_temperatures(int nsteps, double *out) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_step_temperatures: no state has been set"};
+        const size_t per = (size_t)6 * nrep;
+        ensure_obs_ring(per * (size_t)std::max(nsteps, 1));
+        for (int s = 0; s < nsteps; s++) {
+            step(1, nullptr);
+            enqueue_temperature(h_obs + per * (size_t)s);  // stream order: step s's copy precedes step s+1's sums
+        }
+        MTG_CUDA(cudaMemcpyAsync(h_flags, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+        for (int s = 0; s < nsteps; s++) normalise_temperature(h_obs + per * (size_t)s, out + per * (size_t)s);
+        return *h_flags;
     }
 
     void observables(double *out) override {

@@ -44,6 +44,7 @@ struct SysBase {
     virtual int64_t rebuilds() = 0;
     virtual mtg_status pairs(int, double, int32_t *, int64_t, int64_t *) = 0;
     virtual uint32_t temperature(double *) = 0;   // returns the status flags, read with the result
+    virtual uint32_t step_temperatures(int, double *) = 0;   // likewise
     virtual void observables(double *) = 0;
     virtual void displacement(double *) = 0;
     virtual void set_draw(uint64_t) = 0;

@@ -295,6 +295,13 @@ class LangevinNVTRGPU:
         _check(self._h, _lib.lib().mtg_temperature(self._h, dptr(out)))
         return out
 
+    def step_temperatures(self, nsteps: int) -> np.ndarray:
+        """nsteps steps, each followed by measured_temperature of that step: (nsteps, replicas, 6).  The
+        per-step sums reach pinned host memory as each step completes; one synchronisation at the end."""
+        out = np.empty((int(nsteps), len(self.replicas), 6))
+        _check(self._h, _lib.lib().mtg_step_temperatures(self._h, int(nsteps), dptr(out)))
+        return out
+
     def observables(self) -> np.ndarray:
         """Per replica: patch energy, WCA energy, virial, bonded patch pairs, pairs in range."""
         out = np.empty((len(self.replicas), _lib.MTG_OBS_COUNT))

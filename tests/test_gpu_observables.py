@@ -201,3 +201,61 @@ def test_patch_energy_statistics_match_oracle():
         m1, m2 = gpu[:, i].mean(), orc[:, i].mean()
         se = math.sqrt(gpu[:, i].var(ddof=1) / blocks + orc[:, i].var(ddof=1) / blocks)
         assert abs(m1 - m2) <= 4 * se + 0.02 * abs(m2), (name, m1, m2, se)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_step_temperatures_equal_the_step_by_step_read_back(precision):
+    """mtg_step_temperatures (per-step sums copied asynchronously, one synchronisation) gives, step by step,
+    what mtg_step(1) + mtg_temperature give, and leaves the same state (bit for bit in FP32; the temperature
+    sums meet in double-precision atomics, whose order moves the last bits)."""
+    spec = tetra_spec(600, 0.2)
+    x = random_positions(spec.n, spec.box, True, 0.95, 31)
+    Q = random_rotations(spec.n, 32)
+    z = np.zeros((spec.n, 3))
+    nsteps = 12
+    with LangevinNVTRGPU([spec, spec], precision=precision) as s:
+        s.initialize(np.concatenate([x, x]), np.concatenate([z, z]), np.concatenate([z, z]), np.concatenate([Q, Q]))
+        got = s.step_temperatures(nsteps)
+        st_got = s.get_state()
+    want = []
+    with LangevinNVTRGPU([spec, spec], precision=precision) as s:
+        s.initialize(np.concatenate([x, x]), np.concatenate([z, z]), np.concatenate([z, z]), np.concatenate([Q, Q]))
+        for _ in range(nsteps):
+            s.step(1)
+            want.append(s.measured_temperature())
+        st_want = s.get_state()
+    assert got.shape == (nsteps, 2, 6)
+    np.testing.assert_allclose(got, np.array(want), rtol=1e-12, atol=0)
+    for key in ("x", "p", "Lb", "Q"):
+        if precision == "fp32":  # fixed-point force sums: bit-reproducible
+            assert np.array_equal(st_got[key], st_want[key]), key
+        else:  # FP64 sums a particle's neighbours in slot order, and ranks within a cell come from atomics
+            np.testing.assert_allclose(st_got[key], st_want[key], rtol=1e-10, atol=1e-12, err_msg=key)
+    assert got[-1].min() > 0
+
+
+@pytest.mark.parametrize("precision,kernel", [("fp32", "pairs"), ("fp32", "tiled"), ("fp64", "pairs")])
+def test_temperature_after_steps_matches_oracle(precision, kernel):
+    """After steps, mtg_temperature / mtg_step_temperatures (the pair pipeline's epilogue sums where that
+    path runs, a reduction over the state otherwise) equal the oracle's temperature of the downloaded
+    momenta; replica sizes that are not multiples of 32 put replica boundaries inside warps."""
+    specs = [tetra_spec(n, 0.2) for n in (333, 517, 1000)]
+    xs = [random_positions(sp.n, sp.box, True, 0.95, 40 + r) for r, sp in enumerate(specs)]
+    Qs = [random_rotations(sp.n, 50 + r) for r, sp in enumerate(specs)]
+    off = np.concatenate([[0], np.cumsum([sp.n for sp in specs])])
+    z = np.zeros((off[-1], 3))
+    with LangevinNVTRGPU(specs, precision=precision, force_kernel=kernel) as s:
+        s.initialize(np.concatenate(xs), z, z, np.concatenate(Qs))
+        s.step(7)
+        got = s.measured_temperature()
+        st = s.get_state()
+        got2 = s.step_temperatures(3)
+        st2 = s.get_state()
+    for r, sp in enumerate(specs):
+        a, b = off[r], off[r + 1]
+        sysm = po.System(sp)
+        want = sysm.temperature(np.ascontiguousarray(st["p"][a:b]), np.ascontiguousarray(st["Lb"][a:b]))
+        np.testing.assert_allclose(got[r], want, rtol=1e-9, atol=0)
+        want2 = sysm.temperature(np.ascontiguousarray(st2["p"][a:b]), np.ascontiguousarray(st2["Lb"][a:b]))
+        np.testing.assert_allclose(got2[-1][r], want2, rtol=1e-9, atol=0)
+        assert want.min() > 0
