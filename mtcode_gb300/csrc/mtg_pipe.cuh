@@ -367,10 +367,11 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
 }
 
 // the Kern-Frenkel terms of the pairs pairforce_kernel<kPairSplit> listed, one pair per thread, into the
-// fixed-point sums of both particles (the same evaluation as the full kernel's patch branch)
-__global__ void __launch_bounds__(kPipeThreads) patch_pairs_kernel(ForceArgs<float> a, const int2 *list_all,
-                                                                 long long cap, const unsigned long long *counts,
-                                                                 long long *acc) {
+// fixed-point sums of both particles (the same evaluation as the full kernel's patch branch); capped at 64
+// registers (four blocks per SM), measured a little faster than its natural 80
+__global__ void __launch_bounds__(kPipeThreads, 4) patch_pairs_kernel(ForceArgs<float> a, const int2 *list_all,
+                                                                    long long cap, const unsigned long long *counts,
+                                                                    long long *acc) {
     __shared__ long long segs[kSegs + 1];
     seg_prefix(counts, cap, segs);
     const long long n = segs[kSegs];
