@@ -261,10 +261,25 @@ __device__ __forceinline__ void break_check(const BindState &S, int p, int d) {
 
 // ------------------------------------------------------------------ clusters
 // a patch without an edge is a cluster of one: unbound (LangevinRforce.cpp:3110-3133, 3165-3170)
+// A thread takes 16 patches: their bound flags as one 16-byte word (the array is a cudaMalloc'd base and
+// groups start at multiples of 16), then the adjacency counter of each bound one.
 __global__ void __launch_bounds__(256) bind_unbind_kernel(BindState S) {
     const unsigned stamp = (unsigned)S.ctr[2];
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < S.ptot; p += gridDim.x * blockDim.x)
-        if (S.isbound[p] && adj_count(S.deg, p, stamp) == 0) S.isbound[p] = 0;
+    const int ngroups = (S.ptot + 15) / 16;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += gridDim.x * blockDim.x) {
+        const int p0 = 16 * g;
+        if (p0 + 16 <= S.ptot) {
+            const uint4 v = *reinterpret_cast<const uint4 *>(S.isbound + p0);
+            if (!(v.x | v.y | v.z | v.w)) continue;
+            const unsigned w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int b = 0; b < 16; b++)
+                if (((w[b >> 2] >> (8 * (b & 3))) & 0xffu) && adj_count(S.deg, p0 + b, stamp) == 0) S.isbound[p0 + b] = 0;
+        } else {
+            for (int p = p0; p < S.ptot; p++)
+                if (S.isbound[p] && adj_count(S.deg, p, stamp) == 0) S.isbound[p] = 0;
+        }
+    }
 }
 
 // clusters of two or three: the walk from one patch with an edge

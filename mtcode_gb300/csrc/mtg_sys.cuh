@@ -572,7 +572,7 @@ struct Sys : SysBase {
     void enqueue_bind_decide(const mtg::ForceArgs<real> &a, bool listed) {
         mtg::BindState S = bind_state();
         if (listed) S.bound = d_bound;
-        mtg::bind_unbind_kernel<<<grid_for(ptot, 256, occ_stream, sms), 256, 0, st>>>(S);
+        mtg::bind_unbind_kernel<<<grid_for((ptot + 15) / 16, 256, occ_stream, sms), 256, 0, st>>>(S);  // 16 patches a thread
         mtg::bind_decide_kernel<<<grid_for(ptot, 256, 4, sms), 256, 0, st>>>(S);
         mtg::bind_large_kernel<real><<<scratch_threads / mtg::kLargeThreads, mtg::kLargeThreads, 0, st>>>(a, S);
         counted(3);
