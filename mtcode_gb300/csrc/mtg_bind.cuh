@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(256) bind_snapshot_kernel(int ntot, Buffers<re
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ntot; s += gridDim.x * blockDim.x) {
         Payload<real> P;
         P.load(b.pos, b.rota, b.rotb, s);
-        P.store(b.snap_a, b.snap_b, b.snap_c, s);
+        P.store(b.snap_a, b.snap_b, b.snap_c, b.ident[s]);   // by global index
     }
 }
 

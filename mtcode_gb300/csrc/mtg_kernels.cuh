@@ -33,7 +33,9 @@ struct Buffers {
     real *xref;            // skin lists: position of each slot at the last list build (4 reals), shared
     int *home_cell;        // skin lists: cell of each slot at the last list build, shared
     real *snap_a, *snap_b, *snap_c;  // single-bond mode: position and rotation at the last candidate-list
-                                     // build, laid out like pos / rota / rotb and carried with the particle
+                                     // build, laid out like pos / rota / rotb but indexed by the particle's
+                                     // global index (ident), so a re-sort leaves it in place; one set shared
+                                     // by both buffers
 };
 
 // Skin-list state (int[4], device): [0] this step rebuilds, [1] a particle will have moved more than half
@@ -359,13 +361,7 @@ __global__ void __launch_bounds__(256) scatter_kernel(Tables<real> tb, Buffers<r
             // single-bond mode: the candidate list is built from the positions at the start of the step
             // (calculate_patch_list before advancemom_halfstep, Condensate.cpp:464-475); otherwise the
             // particle carries its snapshot along
-            if (snap_due && *snap_due) {
-                P.store(out.snap_a, out.snap_b, out.snap_c, d);
-            } else {
-                Payload<real> S;
-                S.load(in.snap_a, in.snap_b, in.snap_c, s);
-                S.store(out.snap_a, out.snap_b, out.snap_c, d);
-            }
+            if (snap_due && *snap_due) P.store(out.snap_a, out.snap_b, out.snap_c, id);
         }
         if (MOVE) {
             const int r = find_replica(tb.rep_slot, tb.nrep, s);
@@ -623,8 +619,8 @@ __device__ __noinline__ bool exact_edge(const BindRep &B, const real *pos, const
     return true;
 }
 
-// FP64 candidate-list condition on the snapshot: distance < the list cut and < max_check + 1, and
-// (c_i - max_ang) + (c_j - max_ang) > -0.4 (LangevinR.cpp:1722-1800)
+// FP64 candidate-list condition on the snapshot (s1, s2: the particles' global indices): distance < the list
+// cut and < max_check + 1, and (c_i - max_ang) + (c_j - max_ang) > -0.4 (LangevinR.cpp:1722-1800)
 template <class real>
 __device__ __noinline__ bool exact_member(const BindRep &B, const real *sa, const real *sb, const real *sc, int s1,
                                           int s2, int o1, int o2) {
@@ -760,7 +756,8 @@ __device__ __forceinline__ void bind_patch_edge(const ForceArgs<real> &a, const 
     if (!sure && !exact_edge<real>(B, a.buf.pos, a.buf.rota, a.buf.rotb, s1, s2, o1, o2, q, disp2_of(B.disp[q], cls),
                                    nullptr))
         return;
-    if (!candidate<real>(B, R, M, a.buf.snap_a, a.buf.snap_b, a.buf.snap_c, s1, s2, o1, o2)) return;
+    if (!candidate<real>(B, R, M, a.buf.snap_a, a.buf.snap_b, a.buf.snap_c, li1 + R.off, li2 + R.off, o1, o2))
+        return;
     add_edge_t<real>(a, wp1, wp2, cls, stamp);
 }
 

@@ -587,10 +587,8 @@ struct Sys : SysBase {
         d_bound = nullptr;
         d_brep = nullptr; d_bmodel = nullptr; d_patch_slot = d_boundto = d_large = d_scratch = nullptr;
         d_bctr = d_deg = nullptr; d_adj = nullptr; d_isbound = nullptr;
-        for (int b = 0; b < 2; b++) {
-            cudaFree(buf[b].snap_a); cudaFree(buf[b].snap_b); cudaFree(buf[b].snap_c);
-            buf[b].snap_a = buf[b].snap_b = buf[b].snap_c = nullptr;
-        }
+        cudaFree(buf[0].snap_a); cudaFree(buf[0].snap_b); cudaFree(buf[0].snap_c);  // one set, shared
+        for (int b = 0; b < 2; b++) buf[b].snap_a = buf[b].snap_b = buf[b].snap_c = nullptr;
     }
 
     void drop_graphs() {
@@ -719,11 +717,13 @@ struct Sys : SysBase {
         MTG_CUDA(cudaMalloc(&d_patch_slot, sizeof(int) * (nrep + 1)));
         MTG_CUDA(cudaMalloc(&d_bctr, sizeof(unsigned long long) * mtg::kBindCounters));
         const size_t nn = (size_t)std::max(ntot_, 1);
-        for (int b = 0; b < 2; b++) {
-            MTG_CUDA(cudaMalloc(&buf[b].snap_a, sizeof(real) * 4 * nn));
-            MTG_CUDA(cudaMalloc(&buf[b].snap_b, sizeof(real) * 4 * nn));
-            MTG_CUDA(cudaMalloc(&buf[b].snap_c, sizeof(real) * 4 * nn));
-        }
+        // one snapshot set by global index, shared by both buffers
+        MTG_CUDA(cudaMalloc(&buf[0].snap_a, sizeof(real) * 4 * nn));
+        MTG_CUDA(cudaMalloc(&buf[0].snap_b, sizeof(real) * 4 * nn));
+        MTG_CUDA(cudaMalloc(&buf[0].snap_c, sizeof(real) * 4 * nn));
+        buf[1].snap_a = buf[0].snap_a;
+        buf[1].snap_b = buf[0].snap_b;
+        buf[1].snap_c = buf[0].snap_c;
         MTG_CUDA(cudaMalloc(&d_deg, sizeof(unsigned long long) * np));
         MTG_CUDA(cudaMalloc(&d_adj, sizeof(int2) * mtg::kAdjCap * np));
         MTG_CUDA(cudaMalloc(&d_boundto, sizeof(int) * np));
