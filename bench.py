@@ -39,10 +39,18 @@ UNIT = "particle-steps/s"
 BYTES_FORCE = 48 + 24 + 4 + 48 + 8 + 4          # own x,Q + p,L + id; write p,L,F~,T~ + bin + histogram
 BYTES_SCATTER = 8 + 4 + 48 + 48 + 4 + 24 + 48 + 24 + 4 + 24  # bin,start,row,row,id,disp -> row,p+L,id,disp
 BYTES_SCAN_PER_CELL = 16
+# the epilogue kernel alone: the force pass's own-particle traffic plus the read and clear of the 64-bit
+# fixed-point force/torque sums the pair kernels accumulate (48 + 48 B)
+BYTES_EPILOGUE = BYTES_FORCE + 96
 # measured DRAM bytes per particle and launch (ncu dram__bytes_read + dram__bytes_write on 160 replicas,
 # state larger than L2; profiles/step_dram_traffic_c4x160.md), scaled by the particle count.  Force pass:
 # pairfind + pairforce + patch pairs + epilogue.
 TRAFFIC_PER_PARTICLE = {"force": 422.0, "scatter": 233.1}
+# the end-to-end leg: a fixed number of steps, whatever --steps is
+E2E_STEPS = 100
+# CPU legs (reference arm and cpu_baseline): the same replica sample, processed largest first, one replica
+# per host thread at a time
+CPU_SAMPLE_REPLICAS = 128
 
 
 def metric_of(args) -> str:
@@ -153,18 +161,44 @@ def shard_replicas(n_replicas: int, rank: int, world: int) -> list:
     return list(range(start, start + per + (1 if rank < extra else 0)))
 
 
-def make_workload(args, rank: int):
+def make_workload(args, rank: int, gen=None):
+    """The bench workload; ``gen`` (the oracle's generators for the CPU legs) supplies the seeded inputs."""
     from mtcode_gb300 import workloads
     if args.workload == "c4":
-        return workloads.patchy_c4(seed=args.seed + rank, n_replicas=args.replicas)
-    return workloads.WORKLOADS[args.workload](seed=args.seed + rank)
+        return workloads.patchy_c4(seed=args.seed + rank, n_replicas=args.replicas, gen=gen)
+    return workloads.WORKLOADS[args.workload](seed=args.seed + rank, gen=gen)
 
 
 # ---------------------------------------------------------------- CPU side (oracle port)
+def cpu_info() -> dict:
+    """Host facts the CPU figures depend on: logical cores, CPU model, and the long double format (the
+    reference's angular factors run in long double; on aarch64 that is IEEE binary128 in software)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.split(":")[0].strip() == "Model name":
+                model = (model + " / " if model else "") + ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        try:
+            for ln in Path("/proc/cpuinfo").read_text().splitlines():
+                if ln.lower().startswith(("model name", "cpu part")):
+                    model = ln.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    nm = np.finfo(np.longdouble).nmant
+    ld = {112: "IEEE binary128 (software arithmetic)", 63: "x87 80-bit extended (hardware)",
+          52: "same as double"}.get(nm, f"{nm}-bit mantissa")
+    return {"nproc": os.cpu_count(), "cpu_model": model, "machine": os.uname().machine, "long_double": ld}
+
+
 def cpu_sample_rate(W, n_reps: int, steps: int, threads: int, single_bond=None) -> dict:
     """Oracle port of the reference step on a bounded sample: the first n_reps replicas, `steps` steps
-    each, one replica per host thread (the reference's own scale-out is one process per system).  With
-    single_bond = (on, off): the run_singlebond loop with BindingModelSingle(on, off)."""
+    each, one replica per host thread (the reference's own scale-out is one process per system), largest
+    replica first.  With single_bond = (on, off): the run_singlebond loop with BindingModelSingle(on, off)."""
     from oracle import pyoracle as po
     po.orc()
     reps = W.replicas[:n_reps]
@@ -192,38 +226,51 @@ def cpu_sample_rate(W, n_reps: int, steps: int, threads: int, single_bond=None) 
         sysm.run(st, steps, noise_mode=2, seed=spec.seed, replica=r, draw0=1, check_skin=False)
         return spec.n * steps, time.perf_counter() - t0
 
+    order = sorted(range(len(reps)), key=lambda r: -reps[r].n)   # longest first: balanced threads
     t0 = time.perf_counter()
     with ThreadPoolExecutor(max_workers=threads) as ex:
-        res = list(ex.map(one, range(len(reps))))
+        res = list(ex.map(one, order))
     wall = time.perf_counter() - t0
     ps = sum(r[0] for r in res)
     cpu_s = sum(r[1] for r in res)
     return {"value": ps / wall, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{len(reps)} of {len(W.replicas)} replicas ({ps // steps} particles) x {steps} steps, "
-                      f"one replica per thread, {cpu_s:.1f} s of CPU work"
+            "sample": f"{len(reps)} of {len(W.replicas)} replicas ({ps // steps} particles) x {steps} steps from the "
+                      f"seeded start, one replica per thread (largest first), {cpu_s:.1f} s of CPU work"
                       + (" (run_singlebond loop)" if single_bond else "")}
+
+
+def cpu_baseline_line(W, steps: int, single_bond=None) -> dict:
+    """cpu_baseline: the sample on every host thread, plus a 1-thread figure on its first 4 replicas."""
+    threads = os.cpu_count() or 1
+    cb = cpu_sample_rate(W, min(len(W.replicas), CPU_SAMPLE_REPLICAS), steps, threads, single_bond)
+    one = cpu_sample_rate(W, min(len(W.replicas), 16), 3, 1, single_bond)
+    cb["one_thread"] = {"value": one["value"], "sample": one["sample"]}
+    cb.update(cpu_info())
+    cb["note"] = ("oracle port of the reference step (FP64, long double angular factors like the reference), "
+                  "timed instead of the reference's own build, whose sources do not travel to the GPU host")
+    return cb
 
 
 def run_reference(args, rank, world):
     """Reference arm: the oracle port of the reference's CPU step (the reference's own build cannot travel
-    to the GPU host), all host threads, each step a bounded sample of the same workload."""
+    to the GPU host), all host threads, on the same replica sample as the cpu_baseline leg.  The workload is
+    built with the oracle's generators: nothing of the product library is loaded."""
     if rank != 0:
         return
-    W = make_workload(args, 0)
+    from oracle import pyoracle as po
+    W = make_workload(args, 0, gen=po.Generators)
     threads = os.cpu_count() or 1
-    # each timed step advances a sample of 2 replicas per host thread by one step, in parallel
-    n_reps = min(len(W.replicas), 2 * threads)
+    cpu_sample_rate(W, min(len(W.replicas), threads), max(1, args.warmup), threads, args.single_bond)  # warm-up
     steps = max(1, args.steps)
-    cpu_sample_rate(W, min(n_reps, threads), max(1, args.warmup), threads, args.single_bond)  # untimed warm-up
     t0 = time.perf_counter()
-    cb = cpu_sample_rate(W, n_reps, steps, threads, args.single_bond)
+    cb = cpu_baseline_line(W, steps, args.single_bond)
     elapsed = time.perf_counter() - t0
     value = cb["value"]
     line = {"metric": metric_of(args), "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
             "config": {"workload": f"{args.workload}: {len(W.replicas)} patchy replicas, {W.n_total} particles",
-                       "sample": cb["sample"]},
+                       "sample": cb["sample"], "state_age_steps": 0},
             "cpu_baseline": cb,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -244,6 +291,8 @@ def run_gpu(args, rank, world, local):
         s.set_single_bond(binding_single(*args.single_bond))
     s.initialize(W.x, z, z, W.Q)
     s.init_forces()
+    # untimed equilibration: the timed steps see the bonded steady state, not the random start
+    s.step(args.equilibrate)
     s.step(max(args.warmup, 3))
     s.sync()
     stream = torch.cuda.ExternalStream(s.stream, device=torch.device("cuda", local))
@@ -270,8 +319,13 @@ def run_gpu(args, rank, world, local):
     # ---- per-kernel device times (instrumented steps, same stream) -> roofline of the dominant kernel
     prof_steps = max(5, min(50, args.steps // 4))
     prof = s.step_profile(prof_steps)
+    # slots of the step's passes; the pipeline's per-kernel slots split the force pass
+    passes = ["scan_reduce", "scan_top", "scan_down", "scatter", "force"]
+    if args.single_bond:
+        passes += ["bind_begin", "bind_decide"]
+    sub = {k: prof[k] / prof_steps for k in ("pairfind", "pairforce", "patch_pairs", "epilogue") if prof.get(k, 0) > 0}
+    prof = {k: prof[k] for k in passes}
     total_prof = sum(prof.values())
-    ncells = None
     per_launch = {k: v / prof_steps for k, v in prof.items()}
     dominant = max(per_launch, key=per_launch.get)
     bytes_per = {"force": BYTES_FORCE * n, "scatter": BYTES_SCATTER * n}
@@ -287,10 +341,17 @@ def run_gpu(args, rank, world, local):
                 "kernel_ms_per_step": {k: round(v, 5) for k, v in per_launch.items()},
                 "share": {k: round(v / total_prof, 4) for k, v in prof.items()},
                 "algorithmic_bytes_per_particle": {"force": BYTES_FORCE, "scatter": BYTES_SCATTER}}
+    if sub:
+        roofline["force_kernels_ms_per_step"] = {k: round(v, 5) for k, v in sub.items()}
     if "scatter" in per_launch:
         a2 = BYTES_SCATTER * n / (per_launch["scatter"] / 1e3) / 1e9
         roofline["scatter_gbs"] = a2
         roofline["scatter_frac"] = a2 / pk["hbm_gbs"]
+    if "epilogue" in sub:
+        a3 = BYTES_EPILOGUE * n / (sub["epilogue"] / 1e3) / 1e9
+        roofline["epilogue_gbs"] = a3
+        roofline["epilogue_frac"] = a3 / pk["hbm_gbs"]
+        roofline["epilogue_bytes_per_particle"] = BYTES_EPILOGUE
 
     # ---- end to end through the C ABI with host buffers
     e2e = run_e2e(s, W, args, stream, ev0, ev1)
@@ -300,10 +361,9 @@ def run_gpu(args, rank, world, local):
     plain = run_plain_fp64(W, args, local) if args.plain_fp64 and rank == 0 else None
 
     cpu = None
-    if rank == 0 and world == 1 and args.cpu_baseline:
-        threads = os.cpu_count() or 1
-        cpu = cpu_sample_rate(W, min(len(W.replicas), args.cpu_replicas), args.cpu_steps, threads, args.single_bond)
     s.close()
+    if rank == 0 and world == 1 and args.cpu_baseline:
+        cpu = cpu_baseline_line(W, args.cpu_steps, args.single_bond)
 
     if rank == 0:
         line = {"metric": metric_of(args), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -314,6 +374,7 @@ def run_gpu(args, rank, world, local):
                            "replicas": len(W.replicas), "particles_per_gpu": n, "precision": args.precision,
                            "l2": "inputs larger than L2 (state ~%d MB per GPU)" % (n * 250 // 2 ** 20),
                            "parallelism": f"replicas x{world}",
+                           "state_age_steps": args.equilibrate + max(args.warmup, 3),
                            "single_bond": (f"run_singlebond force pass, BindingModelSingle{tuple(args.single_bond)}"
                                            if args.single_bond else None)},
                 "gpu_launches": launches, "clocks": clk.summary(), "roofline": roofline, "e2e": e2e,
@@ -330,7 +391,7 @@ def run_e2e(s, W, args, stream, ev0, ev1) -> dict:
     for k in pinned:
         pinned[k][...] = state[k]
     out = {k: torch.empty(v.shape, dtype=torch.float64, pin_memory=True).numpy() for k, v in state.items()}
-    k_e2e = max(10, args.steps // 2)
+    k_e2e = E2E_STEPS
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     ev0.record(stream)
@@ -397,8 +458,9 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--cpu-replicas", type=int, default=128)
-    ap.add_argument("--cpu-steps", type=int, default=5)
+    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--equilibrate", type=int, default=2000,
+                    help="untimed steps before the timed region (the bonded steady state)")
     ap.add_argument("--no-plain-fp64", dest="plain_fp64", action="store_false")
     ap.add_argument("--plain-replicas", type=int, default=16)
     ap.add_argument("--plain-steps", type=int, default=20)

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define MTG_API_VERSION 3
+#define MTG_API_VERSION 4
 
 typedef enum {
     MTG_OK = 0,
@@ -230,8 +230,10 @@ int64_t mtg_launch_count(const mtg_system *h);
  * 5 bind_begin (the update's start; the edges are part of the force pass), 6 bind_decide (clusters and
  * bond decisions).  With a neighbour skin: 0 = rebuild decision + binning + scan_reduce, 1 scan_top,
  * 2 scan_down, 3 scatter + copy-back (rebuild steps) + in-place first half-step (other steps), 4 force.
- * Synchronising. */
-#define MTG_PROFILE_KERNELS 7
+ * With the FP32 pair pipeline, 7..10 split slot 4 by kernel: 7 pair reset + pairfind, 8 pairforce,
+ * 9 patch pairs (single-bond mode: edges + bound pairs, without slot 6's decisions), 10 epilogue; zero
+ * otherwise.  Slots 5 and 6 are zero outside single-bond mode.  Synchronising. */
+#define MTG_PROFILE_KERNELS 11
 mtg_status mtg_step_profile(mtg_system *h, int nsteps, double *kernel_ms);
 
 /* With a neighbour skin: list rebuilds since mtg_create (each initial force pass and each step that
@@ -323,9 +325,11 @@ mtg_status mtg_bind_update(mtg_system *h, double *F, double *T);
  * Scratch lives in one fixed array inside the library (a file-scope device array, held by every GPU
  * that loads the library until the process exits), which limits a call to
  * n <= MTG_NOALLOC_MAX_PARTICLES and (floor(box / rc))^3 <= MTG_NOALLOC_MAX_CELLS; larger calls return
- * MTG_ERR_ARG without touching the device.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) and should come before any stream capture.  Every call shares the one
- * array: calls that overlap on the GPU (different streams, or host threads sharing a device) race. */
+ * MTG_ERR_ARG without touching the device.  The array takes 1,836,544 bytes of device memory.  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress) and should come before any
+ * stream capture; the address is kept, so do not call this across cudaDeviceReset of that device.  Every
+ * call shares the one array: calls that overlap on the GPU (different streams, or host threads sharing a
+ * device) race. */
 #define MTG_NOALLOC_MAX_PARTICLES 65536
 #define MTG_NOALLOC_MAX_CELLS 65536
 mtg_status mtg_pairs_noalloc(const double *x_dev, int n, double box, int periodic, double rc, int32_t *pairs_dev,

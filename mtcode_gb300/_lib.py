@@ -16,10 +16,11 @@ MTG_MAX_TYPES = 4
 MTG_MAX_ORIENT = 16
 MTG_MAX_POTS = 64
 MTG_OBS_COUNT = 5
-MTG_PROFILE_KERNELS = 7
+MTG_PROFILE_KERNELS = 11
 MTG_NOALLOC_MAX_PARTICLES = 65536
 MTG_NOALLOC_MAX_CELLS = 65536
-PROFILE_KERNEL_NAMES = ("scan_reduce", "scan_top", "scan_down", "scatter", "force", "bind_begin", "bind_decide")
+PROFILE_KERNEL_NAMES = ("scan_reduce", "scan_top", "scan_down", "scatter", "force", "bind_begin", "bind_decide",
+                        "pairfind", "pairforce", "patch_pairs", "epilogue")
 MTG_FP32 = 0
 MTG_FP64 = 1
 MTG_FLAG_NONFINITE = 0x1

@@ -10,7 +10,9 @@
 // Host code cannot use the array's symbol as a device address (on the host it names a stand-in
 // object), so on the first call on each device this file asks the runtime for the array's device
 // address with cudaGetSymbolAddress, with that device current, and passes the address to the
-// kernels.  That first call should therefore come before any stream capture.
+// kernels.  That first call should therefore come before any stream capture.  The address is kept for
+// the life of the process, so the library must not be used across cudaDeviceReset on that device (the
+// reset unloads the module that holds the array).
 //
 // All calls share the one scratch area and it keeps the last call's contents: each call clears the
 // parts that must start at zero, and calls whose work overlaps on the GPU (different streams, or
@@ -43,6 +45,8 @@ constexpr size_t kOffPcnt = kOffMembers + align256(sizeof(int) * kNoAllocMaxPart
 constexpr size_t kOffPoff = kOffPcnt + align256(sizeof(int) * (kNoAllocMaxParticles + 1));
 constexpr size_t kOffPartBlk = kOffPoff + align256(sizeof(int) * (kNoAllocMaxParticles + 1));
 constexpr size_t kNoAllocScratchBytes = kOffPartBlk + align256(sizeof(int) * kNoAllocMaxBlocks);
+// 1,836,544 bytes with 4096-entry scan tiles: the figure the documentation quotes
+static_assert(kNoAllocScratchBytes == 1836544, "the documented scratch size no longer matches the layout");
 
 __device__ __align__(256) static unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 

@@ -143,6 +143,18 @@ inline int cells_per_side(double box, double range) {
     return std::max(1, nc);
 }
 
+// Cells per side of an analysis grid (pair export, g(r), clusters) for a cut rc: side >= rc, so the
+// 27-cell stencil holds every pair closer than rc.  The count is capped (in 64-bit arithmetic) at the
+// smaller of 512 and about twice the cube root of n: cells only grow beyond rc, which keeps the pair set
+// exact, and nc^3 and every cell key stay far inside int even for a tiny rc.
+inline int analysis_cells(double box, double rc, int n) {
+    const double f = std::floor(box / (rc * (1 + 1e-12)));
+    int64_t nc = !(f >= 1) ? 1 : (f > 512 ? 512 : (int64_t)f);
+    int64_t cap = 2;
+    while (cap * cap * cap < 8 * (int64_t)std::max(n, 1) && cap < 512) cap++;
+    return (int)std::max<int64_t>(1, std::min(nc, cap));
+}
+
 inline int grid_for(int64_t n, int block, int per_sm, int sms) {
     int64_t need = (n + block - 1) / block;
     int64_t cap = (int64_t)per_sm * sms;
@@ -228,6 +240,7 @@ struct Sys : SysBase {
     int64_t nbonds = 0;
     double bond_k = 0, bond_r0 = 0;
     int64_t nlaunch = 0;
+    cudaEvent_t *prof_ev = nullptr;  // set by step_profile: events around the pair pipeline's kernels
     // FP32 tile kernel
     bool use_tiles = false;
     int4 *d_tiles = nullptr;
@@ -858,23 +871,32 @@ struct Sys : SysBase {
                 // with a skin the list is rebuilt only on rebuild steps (the gate); the force and epilogue
                 // passes run every time
                 const int *gate = skin > 0 ? d_skin : nullptr;
+                auto mark = [&](int k) {
+                    if (prof_ev) MTG_CUDA(cudaEventRecord(prof_ev[k], st));
+                };
+                mark(0);
                 mtg::pair_reset_kernel<<<1, 64, 0, st>>>(d_npairs, gate, bind ? nullptr : d_patch_ctr);
                 const int gb = (ntot_ + mtg::kPipeThreads - 1) / mtg::kPipeThreads;
                 mtg::pairfind_kernel<<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap,
                                                                                   skin > 0 ? 1 : 0, gate);
+                mark(1);
                 if (bind) {
                     mtg::pairforce_kernel<mtg::kPairBind><<<sms * 16, mtg::kPipeThreads, 0, st>>>(
                         a, d_pairs, d_npairs, pair_cap, d_acc, d_bind_pairs, lcap);
+                    mark(2);
                     mtg::bind_pairs_kernel<<<sms * 8, mtg::kPipeThreads, 0, st>>>(a, d_bind_pairs, lcap);
                     decide();
                     mtg::bound_pairs_kernel<<<sms * 4, mtg::kPipeThreads, 0, st>>>(a, d_bound, bcap, d_acc);
                 } else {
                     mtg::pairforce_kernel<mtg::kPairSplit><<<sms * 16, mtg::kPipeThreads, 0, st>>>(
                         a, d_pairs, d_npairs, pair_cap, d_acc, d_patch_list, patch_cap, d_patch_ctr);
+                    mark(2);
                     mtg::patch_pairs_kernel<<<sms * 8, mtg::kPipeThreads, 0, st>>>(a, d_patch_list, patch_cap, d_patch_ctr,
                                                                                   d_acc);
                 }
+                mark(3);
                 mtg::pair_epilogue_kernel<MODE><<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_acc);
+                mark(4);
                 counted(bind ? 6 : 5);  // (enqueue_bind_decide counts its own)
                 return;
             }
@@ -1180,8 +1202,25 @@ struct Sys : SysBase {
         MTG_REQUIRE(nsteps >= 1 && kernel_ms, "mtg_step_profile: nsteps >= 1 and an output are required");
         step(0, nullptr);  // initial forces / bins, as mtg_step would
         set_device_draw(draw, draw);
-        cudaEvent_t ev[10];
+        cudaEvent_t ev[10], pev[5];
         for (auto &e : ev) MTG_CUDA(cudaEventCreate(&e));
+        for (auto &e : pev) MTG_CUDA(cudaEventCreate(&e));
+        struct Restore {
+            cudaEvent_t *&p;
+            ~Restore() { p = nullptr; }
+        } restore{prof_ev};
+        const bool piped = use_pipe;
+        if (piped) prof_ev = pev;
+        // the pipeline's sub-kernel times of one force pass (pair reset + pairfind, pairforce, patch-pair or
+        // edge/bound-pair kernels, epilogue); the decisions between them are slot 6
+        auto pipe_times = [&](double *acc, float bind_ms) {
+            if (!piped) return;
+            for (int k = 0; k < 4; k++) {
+                float ms = 0;
+                MTG_CUDA(cudaEventElapsedTime(&ms, pev[k], pev[k + 1]));
+                acc[7 + k] += k == 2 ? ms - bind_ms : ms;
+            }
+        };
         double acc[MTG_PROFILE_KERNELS] = {};
         mtg::Tables<real> tb = tables();
         const int g = grid_for(ntot_, 256, occ_stream, sms);
@@ -1212,6 +1251,7 @@ struct Sys : SysBase {
                 MTG_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
                 acc[k] += ms;
             }
+            pipe_times(acc, 0.f);
             nlaunch += 8;  // the explicit kernels above (launch_force counts its own)
             draw += 1;
         }
@@ -1246,11 +1286,13 @@ struct Sys : SysBase {
             MTG_CUDA(cudaEventElapsedTime(&ms, ev[6], ev[7]));
             acc[5] += ms;
             acc[6] += bind_ms;
+            pipe_times(acc, bind_ms);
             cur ^= 1;
             nlaunch += 4;  // the scans and the scatter (launch_force and bind begin count their own)
             draw += 1;
         }
         for (auto &e : ev) cudaEventDestroy(e);
+        for (auto &e : pev) cudaEventDestroy(e);
         for (int k = 0; k < MTG_PROFILE_KERNELS; k++) kernel_ms[k] = acc[k];
         cells_valid = true;
         bins_valid = true;
@@ -1362,8 +1404,8 @@ struct Sys : SysBase {
         MTG_REQUIRE(replica >= 0 && replica < nrep, "mtg_pairs: replica out of range");
         MTG_REQUIRE(rc > 0 && npairs, "mtg_pairs: rc must be positive and npairs non-null");
         const mtg_replica_desc &d = desc[replica];
-        int nc = std::max(1, (int)std::floor(d.box / (rc * (1 + 1e-12))));
-        int ncell = nc * nc * nc;
+        const int nc = analysis_cells(d.box, rc, d.n);
+        const int ncell = nc * nc * nc;
         int n = d.n;
         int off = rep_slot[replica];
         // device scratch: bins, counts, starts, members, per-particle pair counts, offsets, pairs
@@ -1401,12 +1443,18 @@ struct Sys : SysBase {
             MTG_CUDA(cudaMemcpyAsync(hc.data(), pcnt, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
             MTG_CUDA(cudaStreamSynchronize(st));
             int64_t total = 0;
+            for (int i = 0; i < n; i++) total += hc[i];
+            *npairs = total;
+            // the per-particle offsets and the write kernel index pairs with int
+            if (out && total <= cap && total > (int64_t)INT32_MAX)   // (the handler below frees the scratch)
+                throw Fail{MTG_ERR_CAPACITY, "mtg_pairs: " + std::to_string(total) +
+                                                 " pairs exceed the 2^31 - 1 this call can write"};
+            total = 0;
             for (int i = 0; i < n; i++) {
                 ho[i] = (int)total;
                 total += hc[i];
             }
             ho[n] = (int)total;
-            *npairs = total;
             if (total > cap || !out) {
                 cleanup();
                 return total > cap ? MTG_ERR_CAPACITY : MTG_OK;
@@ -1448,7 +1496,7 @@ struct Sys : SysBase {
 
     void bin_replica(int replica, double rc, ReplicaCells &c) {
         const mtg_replica_desc &d = desc[replica];
-        const int nc = std::max(1, (int)std::floor(d.box / (rc * (1 + 1e-12))));
+        const int nc = analysis_cells(d.box, rc, d.n);
         c.ncell = nc * nc * nc;
         const int n = d.n;
         size_t nn = (size_t)std::max(n, 1);

@@ -4,6 +4,10 @@ Every workload uses L = (N pi / 6 / phi)^(1/3), a uniform start with non-overlap
 uniform random rotations (the LangevinNVTR::initialize construction, LangevinR.cpp:239-267), zero momenta
 and zero angular momenta.  No public dataset is involved; everything is generated from the seed.
 
+Every builder takes ``gen``, the source of the seeded positions, rotations and chains: the product
+library's generators by default, or any object with the same three functions and outputs (the CPU
+baselines pass the oracle's, so that they load nothing from the product library).
+
   patchy_c1   N=4,096 tetrahedral (depth 8, range 1.2, cos 0.90), phi 0.10, kT 1, dt 0.005
   patchy_c2   N=65,536 "tubulin-like": poles (depth 10) + laterals at +-65 deg (depth 6), range 1.15,
               cos 0.92, phi 0.20 (pole-lateral cross depth: 0)
@@ -23,7 +27,8 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .system import PatchModelSpec, ReplicaSpec, random_chains, random_positions, random_rotations
+from . import system as _system
+from .system import PatchModelSpec, ReplicaSpec
 
 
 @dataclass
@@ -48,11 +53,12 @@ def box_for(n: int, phi: float) -> float:
     return (n * math.pi / 6.0 / phi) ** (1.0 / 3.0)
 
 
-def _state(replicas, seed: int, min_dist: float = 0.9):
+def _state(replicas, seed: int, min_dist: float = 0.9, gen=None):
+    gen = gen or _system
     xs, qs = [], []
     for r, rep in enumerate(replicas):
-        xs.append(random_positions(rep.n, rep.box, rep.periodic, min_dist, seed * 1000003 + 2 * r))
-        qs.append(random_rotations(rep.n, seed * 1000003 + 2 * r + 1))
+        xs.append(gen.random_positions(rep.n, rep.box, rep.periodic, min_dist, seed * 1000003 + 2 * r))
+        qs.append(gen.random_rotations(rep.n, seed * 1000003 + 2 * r + 1))
     return np.concatenate(xs), np.concatenate(qs)
 
 
@@ -77,24 +83,24 @@ def crowded_model(n_patchy: int, n_total: int, depth: float = 7.0, dis: float = 
     return PatchModelSpec([4, 0], [n_patchy, n_total], TETRA.copy(), np.tile([depth, dis, th], (16, 1)))
 
 
-def patchy_c1(seed: int = 0, n: int = 4096, phi: float = 0.10, kT: float = 1.0) -> Workload:
+def patchy_c1(seed: int = 0, n: int = 4096, phi: float = 0.10, kT: float = 1.0, gen=None) -> Workload:
     box = box_for(n, phi)
     rep = ReplicaSpec(n=n, box=box, model=PatchModelSpec.tetrahedral(n, 8.0, 1.2, math.acos(0.90)), kT=kT,
                       seed=seed)
-    x, Q = _state([rep], seed)
+    x, Q = _state([rep], seed, gen=gen)
     return Workload("patchy_c1", [rep], x, Q)
 
 
-def patchy_c2(seed: int = 0, n: int = 65536, phi: float = 0.20) -> Workload:
+def patchy_c2(seed: int = 0, n: int = 65536, phi: float = 0.20, gen=None) -> Workload:
     rep = ReplicaSpec(n=n, box=box_for(n, phi), model=tubulin_model(n), seed=seed)
-    x, Q = _state([rep], seed)
+    x, Q = _state([rep], seed, gen=gen)
     return Workload("patchy_c2", [rep], x, Q)
 
 
-def patchy_c3(seed: int = 0, n: int = 1048576, phi: float = 0.25) -> Workload:
+def patchy_c3(seed: int = 0, n: int = 1048576, phi: float = 0.25, gen=None) -> Workload:
     n_patchy = n // 4
     rep = ReplicaSpec(n=n, box=box_for(n, phi), model=crowded_model(n_patchy, n), seed=seed)
-    x, Q = _state([rep], seed)
+    x, Q = _state([rep], seed, gen=gen)
     return Workload("patchy_c3", [rep], x, Q)
 
 
@@ -104,7 +110,7 @@ def c4_sizes(n_replicas: int = 512, n_min: int = 1024, n_max: int = 32768, seed:
 
 
 def patchy_c4(seed: int = 0, n_replicas: int = 512, n_min: int = 1024, n_max: int = 32768,
-              phi: float = 0.15) -> Workload:
+              phi: float = 0.15, gen=None) -> Workload:
     rng = np.random.default_rng(seed + 7)
     sizes = c4_sizes(n_replicas, n_min, n_max, seed)
     reps = []
@@ -115,7 +121,7 @@ def patchy_c4(seed: int = 0, n_replicas: int = 512, n_min: int = 1024, n_max: in
         reps.append(ReplicaSpec(n=n, box=box_for(n, phi),
                                 model=PatchModelSpec.tetrahedral(n, depth, 1.2, math.acos(0.90)), kT=kT,
                                 seed=(seed << 20) + r))
-    x, Q = _state(reps, seed)
+    x, Q = _state(reps, seed, gen=gen)
     return Workload("patchy_c4", reps, x, Q)
 
 
@@ -126,10 +132,10 @@ def bead_model(n_patchy: int, n: int, depth: float = 8.0, dis: float = 1.2, cos_
                           np.tile([depth, dis, th], (4, 1)).astype(float))
 
 
-def chain_replica(n_chains: int, beads: int, box: float, every: int, seed: int, periodic: bool = True):
+def chain_replica(n_chains: int, beads: int, box: float, every: int, seed: int, periodic: bool = True, gen=None):
     """Random-walk chains with every `every`-th bead patchy, renumbered patchy-first.
     Returns (x, bonds, n_patchy) in the new numbering."""
-    xc = random_chains(n_chains, beads, box, periodic, 1.0, 0.9, seed)
+    xc = (gen or _system).random_chains(n_chains, beads, box, periodic, 1.0, 0.9, seed)
     n = n_chains * beads
     idx = np.arange(n)
     patchy = (idx % beads) % every == 0
@@ -142,14 +148,15 @@ def chain_replica(n_chains: int, beads: int, box: float, every: int, seed: int, 
 
 
 def polymer_c5(seed: int = 0, n_replicas: int = 64, n_chains: int = 2621, beads: int = 100, phi: float = 0.10,
-               every: int = 10, k: float = 100.0, r0: float = 1.0, dt: float = 0.002, kT: float = 1.0) -> Workload:
+               every: int = 10, k: float = 100.0, r0: float = 1.0, dt: float = 0.002, kT: float = 1.0,
+               gen=None) -> Workload:
     from concurrent.futures import ThreadPoolExecutor
     n = n_chains * beads
     box = box_for(n, phi)
     reps = []
 
     def one(r):
-        return chain_replica(n_chains, beads, box, every, seed * 1000003 + 2 * r)
+        return chain_replica(n_chains, beads, box, every, seed * 1000003 + 2 * r, gen=gen)
 
     with ThreadPoolExecutor(max_workers=16) as ex:
         parts = list(ex.map(one, range(n_replicas)))
@@ -157,7 +164,7 @@ def polymer_c5(seed: int = 0, n_replicas: int = 64, n_chains: int = 2621, beads:
     for r, (x, b, n_patchy) in enumerate(parts):
         reps.append(ReplicaSpec(n=n, box=box, model=bead_model(n_patchy, n), kT=kT, dt=dt, seed=(seed << 20) + r))
         xs.append(x)
-        qs.append(random_rotations(n, seed * 1000003 + 2 * r + 1))
+        qs.append((gen or _system).random_rotations(n, seed * 1000003 + 2 * r + 1))
         bs.append(b + r * n)
     return Workload("polymer_c5", reps, np.concatenate(xs), np.concatenate(qs), np.concatenate(bs), k, r0)
 

@@ -1294,3 +1294,229 @@ int orc_run_singlebond(const orc_params *P, double *x, double *p, double *Lb, do
     free(xi);
     return status;
 }
+
+/* ---------------------------------------------------------------- seeded synthetic inputs */
+
+/* splitmix64 (Steele, Lea, Flood, "Fast splittable pseudorandom number generators", OOPSLA 2014) */
+static uint64_t orc_splitmix(uint64_t *s)
+{
+    uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+/* [0, 1) from the top 53 bits */
+static double orc_unit(uint64_t *s) { return (double)(orc_splitmix(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+/* accepted particles hashed by cell: head per cell, next per particle */
+typedef struct {
+    int nc;
+    double scale;
+    int *head, *next;
+} orc_hash;
+
+static int orc_hash_init(orc_hash *h, double box, double min_dist, int cap_nc, long n)
+{
+    int nc = min_dist > 0 ? (int)floor(box / min_dist) : 1;
+    if (nc < 1) nc = 1;
+    if (nc > cap_nc) nc = cap_nc;
+    h->nc = nc;
+    h->scale = nc / box;
+    size_t ncell = (size_t)nc * nc * nc;
+    h->head = (int *)malloc(sizeof(int) * ncell);
+    h->next = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    if (!h->head || !h->next) return -1;
+    for (size_t c = 0; c < ncell; c++) h->head[c] = -1;
+    for (long i = 0; i < (n > 0 ? n : 1); i++) h->next[i] = -1;
+    return 0;
+}
+
+static void orc_hash_free(orc_hash *h)
+{
+    free(h->head);
+    free(h->next);
+}
+
+static int orc_hash_cell(const orc_hash *h, const double c[3], int clamp_low)
+{
+    int ci[3];
+    for (int k = 0; k < 3; k++) {
+        ci[k] = (int)(c[k] * h->scale);
+        if (ci[k] >= h->nc) ci[k] = h->nc - 1;
+        if (clamp_low && ci[k] < 0) ci[k] = 0;
+    }
+    return ci[0] + h->nc * (ci[1] + h->nc * ci[2]);
+}
+
+/* 1 if no accepted particle of the 27 surrounding cells is closer than sqrt(md2) (minimum image) */
+static int orc_hash_free_at(const orc_hash *h, const double *x, const double c[3], int cell, double box, int periodic,
+                            double md2)
+{
+    const int nc = h->nc;
+    const int ci[3] = {cell % nc, (cell / nc) % nc, cell / (nc * nc)};
+    const int lo = nc >= 3 ? -1 : 0, hi = nc >= 2 ? 1 : 0;
+    for (int dz = lo; dz <= hi; dz++)
+        for (int dy = lo; dy <= hi; dy++)
+            for (int dx = lo; dx <= hi; dx++) {
+                int a = ci[0] + dx, b = ci[1] + dy, e = ci[2] + dz;
+                if (!periodic && (a < 0 || a >= nc || b < 0 || b >= nc || e < 0 || e >= nc)) continue;
+                a = (a + nc) % nc;
+                b = (b + nc) % nc;
+                e = (e + nc) % nc;
+                for (int j = h->head[(size_t)a + nc * ((size_t)b + (size_t)nc * e)]; j >= 0; j = h->next[j]) {
+                    double d2 = 0;
+                    for (int k = 0; k < 3; k++) {
+                        double d = c[k] - x[3 * (size_t)j + k];
+                        if (periodic) d -= box * nearbyint(d / box);
+                        d2 += d * d;
+                    }
+                    if (d2 < md2) return 0;
+                }
+            }
+    return 1;
+}
+
+int orc_random_positions(int n, double box, int periodic, double min_dist, uint64_t seed, double *x)
+{
+    if (n < 0 || box <= 0 || min_dist < 0 || !x) return -1;
+    uint64_t s = seed ^ 0x5DEECE66Dull;
+    orc_hash h;
+    if (orc_hash_init(&h, box, min_dist, 512, n) != 0) {
+        orc_hash_free(&h);
+        return -1;
+    }
+    const double md2 = min_dist * min_dist;
+    long long attempts = 0, limit = 1000LL * (long long)(n > 0 ? n : 1);
+    int placed = 0;
+    while (placed < n) {
+        if (++attempts > limit) {
+            orc_hash_free(&h);
+            return -1;
+        }
+        double c[3];
+        c[0] = orc_unit(&s) * box;   /* one statement each: the draws are taken x, y, z */
+        c[1] = orc_unit(&s) * box;
+        c[2] = orc_unit(&s) * box;
+        const int cell = orc_hash_cell(&h, c, 0);
+        if (!orc_hash_free_at(&h, x, c, cell, box, periodic, md2)) continue;
+        for (int k = 0; k < 3; k++) x[3 * (size_t)placed + k] = c[k];
+        h.next[placed] = h.head[cell];
+        h.head[cell] = placed;
+        placed++;
+    }
+    orc_hash_free(&h);
+    return 0;
+}
+
+void orc_random_rotations(int n, uint64_t seed, double *Q)
+{
+    uint64_t s = seed ^ 0xA0761D6478BD642Full;
+    const double two_pi = 6.283185307179586476925286766559;
+    for (int i = 0; i < n; i++) {
+        double x1 = orc_unit(&s);
+        double x2 = orc_unit(&s);
+        double x3 = orc_unit(&s);
+        /* v uniform on the sphere's upper half from (x2, x3), a Householder reflection of a rotation about
+         * z by 2 pi x1: the construction of LangevinR.cpp:239-267 */
+        double v[3] = {cos(two_pi * x2) * sqrt(x3), sin(two_pi * x2) * sqrt(x3), sqrt(1. - x3)};
+        double c = cos(two_pi * x1), sn = sin(two_pi * x1);
+        double Rz[3][3] = {{c, sn, 0}, {-sn, c, 0}, {0, 0, 1}};
+        double *q = Q + 9 * (size_t)i;
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) {
+                double acc = 0;
+                for (int k = 0; k < 3; k++) acc += (2 * v[a] * v[k] - (a == k ? 1.0 : 0.0)) * Rz[k][b];
+                q[3 * a + b] = acc;
+            }
+    }
+}
+
+int orc_random_chains(int n_chains, int beads, double box, int periodic, double step, double min_dist,
+                      uint64_t seed, double *x)
+{
+    if (n_chains < 0 || beads < 1 || box <= 0 || step <= 0 || min_dist < 0 || min_dist >= step || !x) return -1;
+    const long long n = (long long)n_chains * beads;
+    if (n > 2147483647LL) return -1;
+    uint64_t s = seed ^ 0x2545F4914F6CDD1Dull;
+    orc_hash h;
+    int *cell_of = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    if (!cell_of || orc_hash_init(&h, box, min_dist, 1024, (long)n) != 0) {
+        free(cell_of);
+        return -1;
+    }
+    const double md2 = min_dist * min_dist;
+    int status = 0;
+    for (int ch = 0; ch < n_chains && status == 0; ch++) {
+        const int i0 = ch * beads;
+        int done = 0;
+        for (int restart = 0; restart < 1000 && !done; restart++) {
+            int placed = 0;
+            for (int tries = 0; tries < 10000 && placed == 0; tries++) {
+                double c[3];
+                c[0] = orc_unit(&s) * box;
+                c[1] = orc_unit(&s) * box;
+                c[2] = orc_unit(&s) * box;
+                const int cell = orc_hash_cell(&h, c, 1);
+                if (orc_hash_free_at(&h, x, c, cell, box, periodic, md2)) {
+                    for (int k = 0; k < 3; k++) x[3 * (size_t)i0 + k] = c[k];
+                    cell_of[i0] = cell;
+                    h.next[i0] = h.head[cell];
+                    h.head[cell] = i0;
+                    placed = 1;
+                }
+            }
+            if (!placed) {
+                status = -1;
+                break;
+            }
+            while (placed < beads) {
+                int ok = 0;
+                for (int tries = 0; tries < 200 && !ok; tries++) {
+                    double v[3], r2 = 0;
+                    do {
+                        r2 = 0;
+                        for (int k = 0; k < 3; k++) {
+                            v[k] = 2.0 * orc_unit(&s) - 1.0;
+                            r2 += v[k] * v[k];
+                        }
+                    } while (r2 > 1.0 || r2 < 1e-6);
+                    const double inv = step / sqrt(r2);
+                    double c[3];
+                    int inside = 1;
+                    for (int k = 0; k < 3; k++) {
+                        c[k] = x[3 * (size_t)(i0 + placed - 1) + k] + v[k] * inv;
+                        if (periodic) {
+                            if (c[k] < 0) c[k] += box;
+                            else if (c[k] >= box) c[k] -= box;
+                        } else if (c[k] < 0 || c[k] >= box) {
+                            inside = 0;
+                        }
+                    }
+                    if (!inside) continue;
+                    const int cell = orc_hash_cell(&h, c, 1);
+                    if (orc_hash_free_at(&h, x, c, cell, box, periodic, md2)) {
+                        const int i = i0 + placed;
+                        for (int k = 0; k < 3; k++) x[3 * (size_t)i + k] = c[k];
+                        cell_of[i] = cell;
+                        h.next[i] = h.head[cell];
+                        h.head[cell] = i;
+                        ok = 1;
+                    }
+                }
+                if (!ok) break;
+                placed++;
+            }
+            if (placed == beads) {
+                done = 1;
+            } else {
+                /* stuck: unlink this chain's beads (the most recent insertions head their cells) */
+                for (int i = i0 + placed - 1; i >= i0; i--) h.head[cell_of[i]] = h.next[i];
+            }
+        }
+        if (!done && status == 0) status = -1;
+    }
+    orc_hash_free(&h);
+    free(cell_of);
+    return status;
+}

@@ -187,6 +187,19 @@ int orc_run_singlebond(const orc_params *P, double *x, double *p, double *Lb, do
                        int ncell, double pair_cut, int pair_every, int patch_every, int init, uint64_t init_draw,
                        int noise_mode, const double *noise, uint64_t seed, uint32_t replica, uint64_t draw0);
 
+/* ---------------------------------------------------------------- seeded synthetic inputs
+ * The test and benchmark inputs, generated here as well so that the CPU baselines need nothing from the
+ * product library.  They are the same algorithms, draw for draw, as the library's mtg_random_positions /
+ * mtg_random_rotations / mtg_random_chains (tests/test_oracle_generators.py checks the outputs are
+ * identical): splitmix64 uniforms; random sequential addition with a cell hash at side >= min_dist;
+ * uniform rotations by the construction of LangevinNVTR::initialize (LangevinR.cpp:239-267); self-avoiding
+ * random-walk chains with directions from cube rejection.  Return 0, or -1 where the library returns
+ * MTG_ERR_ARG. */
+int orc_random_positions(int n, double box, int periodic, double min_dist, uint64_t seed, double *x);
+void orc_random_rotations(int n, uint64_t seed, double *Q);
+int orc_random_chains(int n_chains, int beads, double box, int periodic, double step, double min_dist,
+                      uint64_t seed, double *x);
+
 #ifdef __cplusplus
 }
 #endif

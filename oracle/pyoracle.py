@@ -33,9 +33,16 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_SO
 
 
-def build_ref(reference_root: str | Path = "/root/reference") -> Path | None:
+def reference_root() -> Path:
+    """Where the reference checkout (the directory that holds Code/) is looked for: the directory named by
+    the MTCODE_REFERENCE environment variable, else a directory ``reference`` beside this repository."""
+    env = os.environ.get("MTCODE_REFERENCE")
+    return Path(env) if env else HERE.parent.parent / "reference"
+
+
+def build_ref(reference_root_dir: str | Path | None = None) -> Path | None:
     """Compile the reference's own routines through ref_driver.cpp (only where the sources exist)."""
-    root = Path(reference_root)
+    root = Path(reference_root_dir) if reference_root_dir is not None else reference_root()
     if not (root / "Code").is_dir():
         return None
     subprocess.run(["sh", str(HERE / "build_ref.sh"), str(root)], check=True)
@@ -158,8 +165,42 @@ def orc() -> C.CDLL:
         L.orc_run_singlebond.argtypes = [P, _D, _D, _D, _D, _D, _D, _I, C.POINTER(C.c_ubyte), C.POINTER(OrcBinding),
                                          C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
                                          C.c_int, C.c_uint64, C.c_int, _D, C.c_uint64, C.c_uint32, C.c_uint64]
+        L.orc_random_positions.restype = C.c_int
+        L.orc_random_positions.argtypes = [C.c_int, C.c_double, C.c_int, C.c_double, C.c_uint64, _D]
+        L.orc_random_rotations.argtypes = [C.c_int, C.c_uint64, _D]
+        L.orc_random_chains.restype = C.c_int
+        L.orc_random_chains.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double, C.c_uint64, _D]
         _orc = L
     return _orc
+
+
+class Generators:
+    """The seeded synthetic inputs (positions, rotations, chains) computed by the oracle library, with the
+    signatures of mtcode_gb300.system's generators: the CPU baselines build their workloads from these, so
+    that they load nothing from the product library.  Outputs are identical to the product's generators."""
+
+    @staticmethod
+    def random_positions(n: int, box: float, periodic: bool = True, min_dist: float = 0.9, seed: int = 0) -> np.ndarray:
+        x = np.empty((n, 3))
+        if orc().orc_random_positions(int(n), float(box), int(bool(periodic)), float(min_dist),
+                                      int(seed) & 0xFFFFFFFFFFFFFFFF, _d(x)) != 0:
+            raise ValueError(f"could not place {n} particles at min_dist {min_dist} in a box of {box}")
+        return x
+
+    @staticmethod
+    def random_rotations(n: int, seed: int = 0) -> np.ndarray:
+        Q = np.empty((n, 9))
+        orc().orc_random_rotations(int(n), int(seed) & 0xFFFFFFFFFFFFFFFF, _d(Q))
+        return Q
+
+    @staticmethod
+    def random_chains(n_chains: int, beads: int, box: float, periodic: bool = True, step: float = 1.0,
+                      min_dist: float = 0.9, seed: int = 0) -> np.ndarray:
+        x = np.empty((n_chains * beads, 3))
+        if orc().orc_random_chains(int(n_chains), int(beads), float(box), int(bool(periodic)), float(step),
+                                   float(min_dist), int(seed) & 0xFFFFFFFFFFFFFFFF, _d(x)) != 0:
+            raise ValueError(f"could not place {n_chains} chains of {beads} beads in a box of {box}")
+        return x
 
 
 class System:

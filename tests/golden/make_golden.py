@@ -1,7 +1,7 @@
 """Generates the golden fixtures in this directory by running the REFERENCE's own routines
 (osmanovicdino/mtcode, compiled by oracle/build_ref.sh into oracle/_ref/libmtref.so) on seeded inputs.
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py [--reference <reference checkout, the directory holding Code/>]
 
 Inputs are rounded to float32-representable doubles so that the FP32 GPU path, the FP64 GPU path,
 the oracle and the reference all start from bit-identical coordinates.  Force cases are re-seeded
@@ -303,7 +303,8 @@ def spec_record(spec):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=None,
+                    help="reference checkout (default: MTCODE_REFERENCE, else ../reference beside this repository)")
     ap.add_argument("--only", choices=["bonded", "frames", "analysis", "singlebond"],
                     help="regenerate one group of fixtures only")
     args = ap.parse_args()

@@ -20,7 +20,7 @@ from tests._util import sorted_pairs
 
 ROOT = Path(__file__).resolve().parents[1]
 BUILD = ROOT / "mtcode_gb300" / "_build"
-REF = Path("/root/reference/Code")
+REF = po.reference_root() / "Code"
 
 
 def compile_driver(src: str, out: Path, extra=()) -> Path:
