@@ -1,5 +1,7 @@
-// mtg_pipe.cuh -- the FP32 force pass as a pair pipeline: three high-occupancy kernels, no shared-memory
-// tiles.
+// mtg_pipe.cuh -- the force pass as a pair pipeline: high-occupancy kernels, no shared-memory tiles.
+// FP32 (the batched path) and FP64 (the plain single-system path) share the kernels; they differ in the
+// per-particle sums (FP32: 64-bit fixed point, order-independent; FP64: double atomics) and in the
+// single-bond kernels, which are FP32 only.
 //
 //   pairfind   one thread per particle (slot s): every candidate t > s of the 27 cells around s's cell
 //              within the range (the force range, or with a neighbour skin the list range) is one
@@ -27,8 +29,27 @@ constexpr int kPairsPerParticle = 16;  // capacity of the pair list (unordered p
 // |d|^2 with explicit roundings (no contraction), so that pairfind and pairforce decide a pair at the
 // cutoff identically; with the image shift applied as (x_i - x_j) - s the separation is bit for bit the
 // minimum image's
-__device__ __forceinline__ float sep_r2(float dx, float dy, float dz) {
-    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+template <class real>
+__device__ __forceinline__ real sep_r2(real dx, real dy, real dz) {
+    return add_rn(add_rn(mul_rn(dx, dx), mul_rn(dy, dy)), mul_rn(dz, dz));
+}
+
+__device__ __forceinline__ float sqrt_r(float v) { return sqrtf(v); }
+__device__ __forceinline__ double sqrt_r(double v) { return sqrt(v); }
+
+// the per-slot force/torque sums of the pair kernels: FP32 in 64-bit fixed point (integer atomics commute,
+// so the sums do not depend on the order of the pairs), FP64 in doubles (hardware double atomics; the
+// order changes the last bits only)
+template <class real> struct PairAcc { using type = long long; };
+template <> struct PairAcc<double> { using type = double; };
+
+// orientation rows of a slot for the FP64 pipeline (the FP32 form sits beside the tile kernel)
+__device__ __forceinline__ void load_q(const ForceArgs<double> &a, int slot, double q8, double Q[9]) {
+    double b[4], c[4];
+    load4(a.buf.rota + 4 * (size_t)slot, b);
+    load4(a.buf.rotb + 4 * (size_t)slot, c);
+    Q[0] = b[0]; Q[1] = b[1]; Q[2] = b[2]; Q[3] = b[3];
+    Q[4] = c[0]; Q[5] = c[1]; Q[6] = c[2]; Q[7] = c[3]; Q[8] = q8;
 }
 
 // Appends the pairs (s, c0 + b) for every bit b of each lane's mask: one warp-wide scan of the counts and
@@ -68,7 +89,8 @@ __device__ __forceinline__ void warp_pair_flush(int2 *buf, int *nb, int s, int c
 // Each lane scans its particle's candidate segments in chunks of at most 32 slots and marks the hits of a
 // chunk in a bit mask; the warp then appends the marked pairs together (warp_pair_flush), so the candidate
 // loop itself carries no appends.  The chunk and segment loops are warp-uniform.
-__global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float> a, int2 *pairs,
+template <class real>
+__global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<real> a, int2 *pairs,
                                                                 unsigned long long *npairs, long long cap,
                                                                 int range_list, const int *gate) {
     if (gated_off(gate, 1)) return;
@@ -81,8 +103,8 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
     const bool valid = s < a.tb.ntot;
     int r = 0;
     if (valid) r = find_replica(a.tb.rep_slot, a.tb.nrep, s);
-    const Replica<float> &R = a.tb.reps[r];
-    const float range2 = range_list ? R.rc2_list : R.rc2;
+    const Replica<real> &R = a.tb.reps[r];
+    const real range2 = range_list ? R.rc2_list : R.rc2;
     const int nc = R.nc;
     int key = valid ? a.buf.home_cell[s] - R.cell_off : 0;
     if (key < 0 || key >= nc * nc * nc) {
@@ -90,8 +112,9 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
         key = 0;
     }
     const int cx = key % nc, cy = (key / nc) % nc, cz = key / (nc * nc);
-    const float4 pi = valid ? __ldg(reinterpret_cast<const float4 *>(a.buf.pos) + s) : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float L = R.box;
+    real pi[3] = {real(0), real(0), real(0)};
+    if (valid) load_pos(a.buf.pos + 4 * (size_t)s, pi[0], pi[1], pi[2]);
+    const real L = R.box;
     // Each unordered pair once.  With three or more cells per side: the forward half of the stencil
     // (rows (dy, dz) = (0, 0) [cells x, x + 1], (1, 0), (-1..1, 1) [cells x - 1 .. x + 1]) -- an offset
     // and its negative are distinct cells, so exactly one of the two particles' scans holds the
@@ -101,7 +124,7 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
     const int nrows_warp = __any_sync(0xffffffffu, nrows == 9) ? 9 : 5;
     for (int rr = 0; rr < nrows_warp; rr++) {  // warp-uniform; rows past a lane's nrows are empty
         int a0 = 0, a1 = 0, b0 = 0, b1 = 0;
-        float shz = 0.f, shy = 0.f, shb = 0.f;
+        real shz = real(0), shy = real(0), shb = real(0);
         if (rr < nrows) {
             int dy, dz;
             if (small) {
@@ -155,7 +178,7 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
         }
         for (int seg = 0; seg < 2; seg++) {
             const int t0 = seg ? b0 : a0, t1 = seg ? b1 : a1;
-            const float shx = seg ? shb : 0.f;
+            const real shx = seg ? shb : real(0);
             for (int c0 = t0; __any_sync(0xffffffffu, c0 < t1); c0 += 32) {
                 unsigned mask = 0u;
                 const int ce = t1 < c0 + 32 ? t1 : c0 + 32;
@@ -164,18 +187,20 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<float>
                 if (!small) {
 #pragma unroll 1
                     for (int t = c0; t < ce; t++) {
-                        const float4 pj = __ldg(reinterpret_cast<const float4 *>(a.buf.pos) + t);
-                        const float dx = (pi.x - pj.x) - shx, dy2 = (pi.y - pj.y) - shy, dz2 = (pi.z - pj.z) - shz;
-                        if (sep_r2(dx, dy2, dz2) < range2) mask |= 1u << (t - c0);
+                        real pj[3];
+                        load_pos(a.buf.pos + 4 * (size_t)t, pj[0], pj[1], pj[2]);
+                        const real dx = (pi[0] - pj[0]) - shx, dy2 = (pi[1] - pj[1]) - shy, dz2 = (pi[2] - pj[2]) - shz;
+                        if (sep_r2<real>(dx, dy2, dz2) < range2) mask |= 1u << (t - c0);
                     }
                 } else {  // tiny grids: no cell geometry to lean on
 #pragma unroll 1
                     for (int t = c0; t < ce; t++) {
-                        const float4 pj = __ldg(reinterpret_cast<const float4 *>(a.buf.pos) + t);
-                        const float dx = min_image<float>(pi.x - pj.x, R.box, R.l2s, R.periodic);
-                        const float dy2 = min_image<float>(pi.y - pj.y, R.box, R.l2s, R.periodic);
-                        const float dz2 = min_image<float>(pi.z - pj.z, R.box, R.l2s, R.periodic);
-                        if (sep_r2(dx, dy2, dz2) < range2) mask |= 1u << (t - c0);
+                        real pj[3];
+                        load_pos(a.buf.pos + 4 * (size_t)t, pj[0], pj[1], pj[2]);
+                        const real dx = min_image<real>(pi[0] - pj[0], R.box, R.l2s, R.periodic);
+                        const real dy2 = min_image<real>(pi[1] - pj[1], R.box, R.l2s, R.periodic);
+                        const real dz2 = min_image<real>(pi[2] - pj[2], R.box, R.l2s, R.periodic);
+                        if (sep_r2<real>(dx, dy2, dz2) < range2) mask |= 1u << (t - c0);
                     }
                 }
                 warp_pair_flush(buf, &nb, s, c0, mask, pairs, npairs, cap, a.flags);
@@ -235,6 +260,9 @@ __device__ __forceinline__ void block_list_flush(const int2 *sbuf, const int *sn
 __device__ __forceinline__ void fixed_add(long long *acc, float v) {
     if (v != 0.f) atomicAdd(reinterpret_cast<unsigned long long *>(acc), (unsigned long long)to_fixed(v));
 }
+__device__ __forceinline__ void fixed_add(double *acc, double v) {
+    if (v != 0.0) atomicAdd(acc, v);
+}
 
 // Forces and torques of the listed pairs into acc (6 fixed-point sums per slot: F lab, T lab).
 // KIND kPairSplit: WCA core here; pairs where both particles have a patch near a cone go to `list` for
@@ -245,11 +273,11 @@ __device__ __forceinline__ void fixed_add(long long *acc, float v) {
 //   bind_pairs_kernel.
 enum PairKind : int { kPairBind = 1, kPairSplit = 2 };
 
-template <int KIND>
-__global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<float> a, const int2 *pairs,
+template <class real, int KIND>
+__global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<real> a, const int2 *pairs,
                                                                  const unsigned long long *npairs, long long cap,
-                                                                 long long *acc, int2 *list = nullptr,
-                                                                 long long list_cap = 0,
+                                                                 typename PairAcc<real>::type *acc,
+                                                                 int2 *list = nullptr, long long list_cap = 0,
                                                                  unsigned long long *list_counts = nullptr) {
     constexpr bool BIND = KIND == kPairBind;
     __shared__ int2 lbuf[kBlockListCap];
@@ -269,39 +297,39 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
         if (q + stride < n) next = __ldcs(pairs + q + stride);
         const int sa = pr.x, sb = pr.y;
         const int r = a.tb.uniform ? 0 : find_replica(a.tb.rep_slot, a.tb.nrep, sa);
-        const Replica<float> &R = a.tb.reps[r];
-        float xa[4], xb[4];
+        const Replica<real> &R = a.tb.reps[r];
+        real xa[4], xb[4];
         load4(a.buf.pos + 4 * (size_t)sa, xa);
         load4(a.buf.pos + 4 * (size_t)sb, xb);
-        const float d[3] = {min_image<float>(xa[0] - xb[0], R.box, R.l2s, R.periodic),
-                            min_image<float>(xa[1] - xb[1], R.box, R.l2s, R.periodic),
-                            min_image<float>(xa[2] - xb[2], R.box, R.l2s, R.periodic)};
-        const float r2 = sep_r2(d[0], d[1], d[2]);
+        const real d[3] = {min_image<real>(xa[0] - xb[0], R.box, R.l2s, R.periodic),
+                           min_image<real>(xa[1] - xb[1], R.box, R.l2s, R.periodic),
+                           min_image<real>(xa[2] - xb[2], R.box, R.l2s, R.periodic)};
+        const real r2 = sep_r2<real>(d[0], d[1], d[2]);
         if (!(r2 < R.rc2)) continue;  // skin lists hold pairs up to the list range
-        const float rr = sqrtf(r2);
-        float fa[3] = {0.f, 0.f, 0.f};   // the WCA core; patch forces and torques come from the pair lists' kernels
+        const real rr = sqrt_r(r2);
+        real fa[3] = {real(0), real(0), real(0)};   // the WCA core; patch terms come from the pair lists' kernels
         if (rr < R.hs_limit) {
-            const float s_ = hs_force_over_r<float>(R, r2);
-            big |= fabsf(s_ * rr) > 1e4f;
+            const real s_ = hs_force_over_r<real>(R, r2);
+            big |= fabs(s_ * rr) > real(1e4);
             fa[0] = s_ * d[0];
             fa[1] = s_ * d[1];
             fa[2] = s_ * d[2];
         }
         if (BIND) {
             // along d = x_a - x_b: a's cosines are -(n_a . d) / r and b's (n_b . d) / r in either canonical order
-            const Model<float> &M = a.tb.models[R.model];
+            const Model<real> &M = a.tb.models[R.model];
             const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
             const bool single = M.n_types == 1;
-            const int tya = single ? 0 : type_of<float>(M, ida - R.off), tyb = single ? 0 : type_of<float>(M, idb - R.off);
+            const int tya = single ? 0 : type_of<real>(M, ida - R.off), tyb = single ? 0 : type_of<real>(M, idb - R.off);
             if (M.np[tya] > 0 && M.np[tyb] > 0) {
-                const float inv = 1.f / sqrtf(r2), pre = M.mincos[tya][tyb] - 4e-5f;
-                float Q[9], w[3];
+                const real inv = real(1) / sqrt_r(r2), pre = M.mincos[tya][tyb] - real(4e-5);
+                real Q[9], w[3];
                 load_q(a, sa, xa[3], Q);
 #pragma unroll
                 for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
                 bool any = false;
                 for (int k = 0; k < M.np[tya]; k++) {
-                    const float *v = M.orient[M.ooff[tya] + k];
+                    const real *v = M.orient[M.ooff[tya] + k];
                     any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > pre;
                 }
                 if (any) {
@@ -310,7 +338,7 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
                     for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
                     bool anyb = false;
                     for (int k = 0; k < M.np[tyb]; k++) {
-                        const float *v = M.orient[M.ooff[tyb] + k];
+                        const real *v = M.orient[M.ooff[tyb] + k];
                         anyb |= v[0] * w[0] + v[1] * w[1] + v[2] * w[2] > pre;
                     }
                     if (anyb)
@@ -322,33 +350,33 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
         if (KIND == kPairSplit && r2 < R.patch_r2) {
             // the one-sided tests of both particles along d = x_a - x_b (with the 1e-5 margin of the full
             // kernel's own early test): a's cosines -(n . Qa d) / r, b's (n . Qb d) / r
-            const Model<float> &M = a.tb.models[R.model];
+            const Model<real> &M = a.tb.models[R.model];
             const int ida = __ldg(a.buf.ident + sa);
-            const int tya = M.n_types == 1 ? 0 : type_of<float>(M, ida - R.off);
+            const int tya = M.n_types == 1 ? 0 : type_of<real>(M, ida - R.off);
             if (M.np[tya] > 0) {
-                const float inv = 1.f / sqrtf(r2);
-                float Q[9], w[3];
+                const real inv = real(1) / sqrt_r(r2);
+                real Q[9], w[3];
                 load_q(a, sa, xa[3], Q);
 #pragma unroll
                 for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
-                const float mca = M.mincos_any[tya] - 1e-5f;
+                const real mca = M.mincos_any[tya] - real(1e-5);
                 bool any = false;
                 for (int k = 0; k < M.np[tya]; k++) {
-                    const float *v = M.orient[M.ooff[tya] + k];
+                    const real *v = M.orient[M.ooff[tya] + k];
                     any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > mca;
                 }
                 if (any) {
                     const int idb = __ldg(a.buf.ident + sb);
-                    const int tyb = M.n_types == 1 ? 0 : type_of<float>(M, idb - R.off);
+                    const int tyb = M.n_types == 1 ? 0 : type_of<real>(M, idb - R.off);
                     if (M.np[tyb] > 0) {
                         load_q(a, sb, xb[3], Q);
 #pragma unroll
                         for (int k = 0; k < 3; k++)
                             w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
-                        const float mcb = M.mincos_any[tyb] - 1e-5f;
+                        const real mcb = M.mincos_any[tyb] - real(1e-5);
                         bool anyb = false;
                         for (int k = 0; k < M.np[tyb]; k++) {
-                            const float *v = M.orient[M.ooff[tyb] + k];
+                            const real *v = M.orient[M.ooff[tyb] + k];
                             anyb |= v[0] * w[0] + v[1] * w[1] + v[2] * w[2] > mcb;
                         }
                         if (anyb) block_list_put(lbuf, &lnb, pr, list, lcounts, list_cap, a.flags, lflag);
@@ -369,9 +397,10 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<fl
 // the Kern-Frenkel terms of the pairs pairforce_kernel<kPairSplit> listed, one pair per thread, into the
 // fixed-point sums of both particles (the same evaluation as the full kernel's patch branch); capped at 64
 // registers (four blocks per SM), measured a little faster than its natural 80
-__global__ void __launch_bounds__(kPipeThreads, 4) patch_pairs_kernel(ForceArgs<float> a, const int2 *list_all,
+template <class real>
+__global__ void __launch_bounds__(kPipeThreads, 4) patch_pairs_kernel(ForceArgs<real> a, const int2 *list_all,
                                                                     long long cap, const unsigned long long *counts,
-                                                                    long long *acc) {
+                                                                    typename PairAcc<real>::type *acc) {
     __shared__ long long segs[kSegs + 1];
     seg_prefix(counts, cap, segs);
     const long long n = segs[kSegs];
@@ -379,28 +408,29 @@ __global__ void __launch_bounds__(kPipeThreads, 4) patch_pairs_kernel(ForceArgs<
         const int2 pr = list_all[seg_slot(segs, cap, q)];
         const int sa = pr.x, sb = pr.y;
         const int r = a.tb.uniform ? 0 : find_replica(a.tb.rep_slot, a.tb.nrep, sa);
-        const Replica<float> &R = a.tb.reps[r];
-        const Model<float> &M = a.tb.models[R.model];
-        float xa[4], xb[4];
+        const Replica<real> &R = a.tb.reps[r];
+        const Model<real> &M = a.tb.models[R.model];
+        real xa[4], xb[4];
         load4(a.buf.pos + 4 * (size_t)sa, xa);
         load4(a.buf.pos + 4 * (size_t)sb, xb);
-        const float d[3] = {min_image<float>(xa[0] - xb[0], R.box, R.l2s, R.periodic),
-                            min_image<float>(xa[1] - xb[1], R.box, R.l2s, R.periodic),
-                            min_image<float>(xa[2] - xb[2], R.box, R.l2s, R.periodic)};
-        const float rr = sqrtf(sep_r2(d[0], d[1], d[2]));
+        const real d[3] = {min_image<real>(xa[0] - xb[0], R.box, R.l2s, R.periodic),
+                           min_image<real>(xa[1] - xb[1], R.box, R.l2s, R.periodic),
+                           min_image<real>(xa[2] - xb[2], R.box, R.l2s, R.periodic)};
+        const real rr = sqrt_r(sep_r2<real>(d[0], d[1], d[2]));
         const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
         const bool single = M.n_types == 1;
-        const int tya = single ? 0 : type_of<float>(M, ida - R.off), tyb = single ? 0 : type_of<float>(M, idb - R.off);
-        float Qa[9], Qb[9];
+        const int tya = single ? 0 : type_of<real>(M, ida - R.off), tyb = single ? 0 : type_of<real>(M, idb - R.off);
+        real Qa[9], Qb[9];
         load_q(a, sa, xa[3], Qa);
         load_q(a, sb, xb[3], Qb);
         const bool a_first = ida < idb;  // canonical order of the reference (p1 < p2)
-        const float sg = a_first ? 1.f : -1.f, inv = 1.f / rr;
-        const float u[3] = {sg * d[0] * inv, sg * d[1] * inv, sg * d[2] * inv};
-        float f[3] = {0.f, 0.f, 0.f}, t1[3] = {0.f, 0.f, 0.f}, t2[3] = {0.f, 0.f, 0.f}, e = 0.f;
+        const real sg = a_first ? real(1) : real(-1), inv = real(1) / rr;
+        const real u[3] = {sg * d[0] * inv, sg * d[1] * inv, sg * d[2] * inv};
+        real f[3] = {real(0), real(0), real(0)}, t1[3] = {real(0), real(0), real(0)},
+             t2[3] = {real(0), real(0), real(0)}, e = real(0);
         int nbond = 0;
-        if (a_first) patch_pair<float>(M, tya, tyb, Qa, Qb, u, rr, R.bond_r, f, t1, t2, e, nbond);
-        else patch_pair<float>(M, tyb, tya, Qb, Qa, u, rr, R.bond_r, f, t1, t2, e, nbond);
+        if (a_first) patch_pair<real>(M, tya, tyb, Qa, Qb, u, rr, R.bond_r, f, t1, t2, e, nbond);
+        else patch_pair<real>(M, tyb, tya, Qb, Qa, u, rr, R.bond_r, f, t1, t2, e, nbond);
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             fixed_add(acc + 6 * (size_t)sa + k, sg * f[k]);
@@ -524,35 +554,51 @@ __global__ void __launch_bounds__(kPipeThreads) bound_pairs_kernel(ForceArgs<flo
 }
 
 // per particle: the summed force and torque (cleared for the next pass), bonds, then the mode's output
-template <int MODE>
-__global__ void __launch_bounds__(kPipeThreads) pair_epilogue_kernel(ForceArgs<float> a, long long *acc) {
+// the six sums of a slot (F lab, T lab), read and cleared for the next pass: 48 B, 16-byte aligned
+__device__ __forceinline__ void take_sums(long long *acc, size_t s, float F[3], float T[3]) {
+    longlong2 *as = reinterpret_cast<longlong2 *>(acc + 6 * s);
+    const longlong2 s0 = as[0], s1 = as[1], s2 = as[2];
+    F[0] = from_fixed(s0.x); F[1] = from_fixed(s0.y); F[2] = from_fixed(s1.x);
+    T[0] = from_fixed(s1.y); T[1] = from_fixed(s2.x); T[2] = from_fixed(s2.y);
+    const longlong2 zero = make_longlong2(0, 0);
+    as[0] = zero;
+    as[1] = zero;
+    as[2] = zero;
+}
+__device__ __forceinline__ void take_sums(double *acc, size_t s, double F[3], double T[3]) {
+    double2 *as = reinterpret_cast<double2 *>(acc + 6 * s);
+    const double2 s0 = as[0], s1 = as[1], s2 = as[2];
+    F[0] = s0.x; F[1] = s0.y; F[2] = s1.x;
+    T[0] = s1.y; T[1] = s2.x; T[2] = s2.y;
+    const double2 zero = make_double2(0.0, 0.0);
+    as[0] = zero;
+    as[1] = zero;
+    as[2] = zero;
+}
+
+template <class real, int MODE>
+__global__ void __launch_bounds__(kPipeThreads) pair_epilogue_kernel(ForceArgs<real> a, typename PairAcc<real>::type *acc) {
     {
         const int s = blockIdx.x * blockDim.x + threadIdx.x;  // one particle per thread: many loads in flight
         if (s >= a.tb.ntot) return;
         const int r = find_replica(a.tb.rep_slot, a.tb.nrep, s);
-        const Replica<float> &R = a.tb.reps[r];
-        longlong2 *as = reinterpret_cast<longlong2 *>(acc + 6 * (size_t)s);  // 48 B per slot: 16-byte aligned
-        const longlong2 s0 = as[0], s1 = as[1], s2 = as[2];
-        float F[3] = {from_fixed(s0.x), from_fixed(s0.y), from_fixed(s1.x)};
-        float T[3] = {from_fixed(s1.y), from_fixed(s2.x), from_fixed(s2.y)};
-        const longlong2 zero = make_longlong2(0, 0);
-        as[0] = zero;
-        as[1] = zero;
-        as[2] = zero;
+        const Replica<real> &R = a.tb.reps[r];
+        real F[3], T[3];
+        take_sums(acc, (size_t)s, F, T);
         const int id = a.buf.ident[s];
-        float xi[4];
+        real xi[4];
         load4(a.buf.pos + 4 * (size_t)s, xi);
         if (a.bond_start) {
-            float eb = 0.f;
+            real eb = real(0);
             bool big = false;
-            bond_forces<float>(a, R, id, xi[0], xi[1], xi[2], F, eb, big);
+            bond_forces<real>(a, R, id, xi[0], xi[1], xi[2], F, eb, big);
             if (big) atomicOr(a.flags, 2u);
         }
         if (a.bind_on && !a.bind_listed) {
-            Payload<float> P;
+            Payload<real> P;
             P.load(a.buf.pos, a.buf.rota, a.buf.rotb, s);
-            float eb = 0.f;
-            bound_patch_forces<float>(a, R, a.tb.models[R.model], r, id, P.v, F, T, eb);
+            real eb = real(0);
+            bound_patch_forces<real>(a, R, a.tb.models[R.model], r, id, P.v, F, T, eb);
         }
         if (MODE == kModeForces) {
 #pragma unroll
@@ -561,9 +607,9 @@ __global__ void __launch_bounds__(kPipeThreads) pair_epilogue_kernel(ForceArgs<f
                 a.outT[3 * (size_t)id + k] = T[k];
             }
         } else {
-            float Qi[9];
+            real Qi[9];
             load_q(a, s, xi[3], Qi);
-            langevin_epilogue(a, R, r, s, id, F, T, Qi, xi[0], xi[1], xi[2]);
+            langevin_epilogue<real>(a, R, r, s, id, F, T, Qi, xi[0], xi[1], xi[2]);
         }
     }
 }

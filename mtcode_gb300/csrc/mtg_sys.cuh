@@ -245,11 +245,12 @@ struct Sys : SysBase {
     bool use_tiles = false;
     int4 *d_tiles = nullptr;
     int ntiles = 0, occ_tile = 1;
-    // FP32 pair pipeline (force_kernel 2): pair list, its length, fixed-point force/torque sums per slot
+    // pair pipeline (force_kernel 0): pair list, its length, force/torque sums per slot (FP32: fixed point)
     bool use_pipe = false;
     int2 *d_pairs = nullptr;
     unsigned long long *d_npairs = nullptr;
-    long long *d_acc = nullptr;
+    using acc_t = typename mtg::PairAcc<real>::type;
+    acc_t *d_acc = nullptr;
     long long pair_cap = 0;
     // pairs with a patch near a cone on both sides, for the patch-pair kernel (segmented list)
     int2 *d_patch_list = nullptr;
@@ -369,26 +370,29 @@ struct Sys : SysBase {
         occ_force = std::max(occ, 1);
         MTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mtg::scatter_kernel<real, true>, 256, 0));
         occ_stream = std::max(occ, 1);
-        if constexpr (std::is_same<real, float>::value) {
-            use_pipe = cfg.force_kernel == 0;
-            use_tiles = cfg.force_kernel == 2;
-            if (use_pipe) {
-                pair_cap = (long long)mtg::kPairsPerParticle * (long long)n;
-                MTG_CUDA(cudaMalloc(&d_pairs, sizeof(int2) * (size_t)pair_cap));
-                MTG_CUDA(cudaMalloc(&d_npairs, sizeof(unsigned long long)));
-                MTG_CUDA(cudaMemset(d_npairs, 0, sizeof(unsigned long long)));
-                MTG_CUDA(cudaMalloc(&d_acc, sizeof(long long) * 6 * n));
-                MTG_CUDA(cudaMemset(d_acc, 0, sizeof(long long) * 6 * n));
-                patch_cap = std::max<long long>(1024, 2 * (pair_cap + mtg::kSegs - 1) / mtg::kSegs);
-                MTG_CUDA(cudaMalloc(&d_patch_list, sizeof(int2) * (size_t)patch_cap * mtg::kSegs));
-                MTG_CUDA(cudaMalloc(&d_patch_ctr, sizeof(unsigned long long) * mtg::kSegs));
-                MTG_CUDA(cudaMemset(d_patch_ctr, 0, sizeof(unsigned long long) * mtg::kSegs));
-                if (!d_home_cell) {
-                    MTG_CUDA(cudaMalloc(&d_home_cell, sizeof(int) * n));
-                    MTG_CUDA(cudaMemset(d_home_cell, 0, sizeof(int) * n));
-                    buf[0].home_cell = buf[1].home_cell = d_home_cell;
-                }
+        MTG_REQUIRE(cfg.force_kernel >= 0 && cfg.force_kernel <= 2, "mtg_create: force_kernel must be 0, 1 or 2");
+        MTG_REQUIRE((cfg.force_kernel != 2 || std::is_same<real, float>::value),
+                    "mtg_create: the tiled force kernel (force_kernel 2) is FP32 only");
+        use_pipe = cfg.force_kernel == 0;
+        if (use_pipe) {
+            pair_cap = (long long)mtg::kPairsPerParticle * (long long)n;
+            MTG_CUDA(cudaMalloc(&d_pairs, sizeof(int2) * (size_t)pair_cap));
+            MTG_CUDA(cudaMalloc(&d_npairs, sizeof(unsigned long long)));
+            MTG_CUDA(cudaMemset(d_npairs, 0, sizeof(unsigned long long)));
+            MTG_CUDA(cudaMalloc(&d_acc, sizeof(acc_t) * 6 * n));
+            MTG_CUDA(cudaMemset(d_acc, 0, sizeof(acc_t) * 6 * n));
+            patch_cap = std::max<long long>(1024, 2 * (pair_cap + mtg::kSegs - 1) / mtg::kSegs);
+            MTG_CUDA(cudaMalloc(&d_patch_list, sizeof(int2) * (size_t)patch_cap * mtg::kSegs));
+            MTG_CUDA(cudaMalloc(&d_patch_ctr, sizeof(unsigned long long) * mtg::kSegs));
+            MTG_CUDA(cudaMemset(d_patch_ctr, 0, sizeof(unsigned long long) * mtg::kSegs));
+            if (!d_home_cell) {
+                MTG_CUDA(cudaMalloc(&d_home_cell, sizeof(int) * n));
+                MTG_CUDA(cudaMemset(d_home_cell, 0, sizeof(int) * n));
+                buf[0].home_cell = buf[1].home_cell = d_home_cell;
             }
+        }
+        if constexpr (std::is_same<real, float>::value) {
+            use_tiles = cfg.force_kernel == 2;
             if (use_tiles) {
                 std::vector<int4> tiles;
                 for (int r = 0; r < nrep; r++)
@@ -852,7 +856,10 @@ struct Sys : SysBase {
     void launch_force(const mtg::ForceArgs<real> &a0, bool bind = false, cudaEvent_t *bind_ev = nullptr) {
         mtg::ForceArgs<real> a = a0;
         bind = bind && single_bond;
-        const bool listed = bind && use_pipe && MODE != mtg::kModeObs && !a.outE;
+        // the FP64 pipeline has no single-bond kernels: FP64 single-bond passes run per particle
+        const bool piped = use_pipe && MODE != mtg::kModeObs && !a.outE &&
+                           (std::is_same<real, float>::value || !single_bond);
+        const bool listed = bind && piped;
         if (bind) {
             a.bind_deg = d_deg;
             a.bind_adj = d_adj;
@@ -866,40 +873,45 @@ struct Sys : SysBase {
             enqueue_bind_decide(a, listed);
             if (bind_ev) MTG_CUDA(cudaEventRecord(bind_ev[1], st));
         };
-        if constexpr (std::is_same<real, float>::value) {
-            if (use_pipe && MODE != mtg::kModeObs && !a.outE) {
-                // with a skin the list is rebuilt only on rebuild steps (the gate); the force and epilogue
-                // passes run every time
-                const int *gate = skin > 0 ? d_skin : nullptr;
-                auto mark = [&](int k) {
-                    if (prof_ev) MTG_CUDA(cudaEventRecord(prof_ev[k], st));
-                };
-                mark(0);
-                mtg::pair_reset_kernel<<<1, 64, 0, st>>>(d_npairs, gate, bind ? nullptr : d_patch_ctr);
-                const int gb = (ntot_ + mtg::kPipeThreads - 1) / mtg::kPipeThreads;
-                mtg::pairfind_kernel<<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap,
-                                                                                  skin > 0 ? 1 : 0, gate);
-                mark(1);
+        if (piped) {
+            // with a skin the list is rebuilt only on rebuild steps (the gate); the force and epilogue
+            // passes run every time
+            const int *gate = skin > 0 ? d_skin : nullptr;
+            auto mark = [&](int k) {
+                if (prof_ev) MTG_CUDA(cudaEventRecord(prof_ev[k], st));
+            };
+            mark(0);
+            mtg::pair_reset_kernel<<<1, 64, 0, st>>>(d_npairs, gate, bind ? nullptr : d_patch_ctr);
+            const int gb = (ntot_ + mtg::kPipeThreads - 1) / mtg::kPipeThreads;
+            mtg::pairfind_kernel<real><<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap,
+                                                                                    skin > 0 ? 1 : 0, gate);
+            mark(1);
+            bool bind_pass = false;
+            if constexpr (std::is_same<real, float>::value) {
                 if (bind) {
-                    mtg::pairforce_kernel<mtg::kPairBind><<<sms * 16, mtg::kPipeThreads, 0, st>>>(
+                    bind_pass = true;
+                    mtg::pairforce_kernel<float, mtg::kPairBind><<<sms * 16, mtg::kPipeThreads, 0, st>>>(
                         a, d_pairs, d_npairs, pair_cap, d_acc, d_bind_pairs, lcap);
                     mark(2);
                     mtg::bind_pairs_kernel<<<sms * 8, mtg::kPipeThreads, 0, st>>>(a, d_bind_pairs, lcap);
                     decide();
                     mtg::bound_pairs_kernel<<<sms * 4, mtg::kPipeThreads, 0, st>>>(a, d_bound, bcap, d_acc);
-                } else {
-                    mtg::pairforce_kernel<mtg::kPairSplit><<<sms * 16, mtg::kPipeThreads, 0, st>>>(
-                        a, d_pairs, d_npairs, pair_cap, d_acc, d_patch_list, patch_cap, d_patch_ctr);
-                    mark(2);
-                    mtg::patch_pairs_kernel<<<sms * 8, mtg::kPipeThreads, 0, st>>>(a, d_patch_list, patch_cap, d_patch_ctr,
-                                                                                  d_acc);
                 }
-                mark(3);
-                mtg::pair_epilogue_kernel<MODE><<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_acc);
-                mark(4);
-                counted(bind ? 6 : 5);  // (enqueue_bind_decide counts its own)
-                return;
             }
+            if (!bind_pass) {
+                mtg::pairforce_kernel<real, mtg::kPairSplit><<<sms * 16, mtg::kPipeThreads, 0, st>>>(
+                    a, d_pairs, d_npairs, pair_cap, d_acc, d_patch_list, patch_cap, d_patch_ctr);
+                mark(2);
+                mtg::patch_pairs_kernel<real><<<sms * 8, mtg::kPipeThreads, 0, st>>>(a, d_patch_list, patch_cap,
+                                                                                   d_patch_ctr, d_acc);
+            }
+            mark(3);
+            mtg::pair_epilogue_kernel<real, MODE><<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_acc);
+            mark(4);
+            counted(bind_pass ? 6 : 5);  // (enqueue_bind_decide counts its own)
+            return;
+        }
+        if constexpr (std::is_same<real, float>::value) {
             if (use_tiles && MODE != mtg::kModeObs && !a.outE) {
                 const int g = std::max(1, std::min(ntiles, occ_tile * sms));  // persistent: one CTA per SM
                 mtg::tile_force_kernel<MODE><<<g, mtg::kTileThreads, tile_smem, st>>>(a, d_tiles, ntiles);
@@ -1209,7 +1221,7 @@ struct Sys : SysBase {
             cudaEvent_t *&p;
             ~Restore() { p = nullptr; }
         } restore{prof_ev};
-        const bool piped = use_pipe;
+        const bool piped = use_pipe && (std::is_same<real, float>::value || !single_bond);  // as launch_force
         if (piped) prof_ev = pev;
         // the pipeline's sub-kernel times of one force pass (pair reset + pairfind, pairforce, patch-pair or
         // edge/bound-pair kernels, epilogue); the decisions between them are slot 6

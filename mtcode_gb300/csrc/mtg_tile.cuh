@@ -149,21 +149,22 @@ __device__ __forceinline__ float acc_get(unsigned long long a) { return from_fix
 
 // the Langevin epilogue shared with the simple kernel (create_forces_and_torques_sphere + half-kick +
 // binning of the next step); F, T are the lab-frame force and torque of slot s
-__device__ __forceinline__ void langevin_epilogue(const ForceArgs<float> &a, const Replica<float> &R, int r, int s, int id,
-                                                  const float F[3], const float T[3], const float Qi[9], float xi,
-                                                  float yi, float zi) {
-    Row<float> Mv;
+template <class real>
+__device__ __forceinline__ void langevin_epilogue(const ForceArgs<real> &a, const Replica<real> &R, int r, int s, int id,
+                                                  const real F[3], const real T[3], const real Qi[9], real xi,
+                                                  real yi, real zi) {
+    Row<real> Mv;
     Mv.load(a.buf.motion + (size_t)s * kRow);
-    float p[3] = {Mv.v[0], Mv.v[1], Mv.v[2]}, L[3] = {Mv.v[3], Mv.v[4], Mv.v[5]};
-    float xi6[6];
+    real p[3] = {Mv.v[0], Mv.v[1], Mv.v[2]}, L[3] = {Mv.v[3], Mv.v[4], Mv.v[5]};
+    real xi6[6];
     const int li = id - R.off;
     if (a.ext_noise) {
 #pragma unroll
-        for (int k = 0; k < 6; k++) xi6[k] = (float)a.ext_noise[6 * (size_t)id + k];
+        for (int k = 0; k < 6; k++) xi6[k] = (real)a.ext_noise[6 * (size_t)id + k];
     } else {
-        philox_noise6<float>((uint32_t)li, (uint32_t)r, a.draw[0], R.seed_lo, R.seed_hi, xi6);
+        philox_noise6<real>((uint32_t)li, (uint32_t)r, a.draw[0], R.seed_lo, R.seed_hi, xi6);
     }
-    float pb[3], fb[3], Ft[3], Tt[3];
+    real pb[3], fb[3], Ft[3], Tt[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) pb[k] = Qi[3 * k] * p[0] + Qi[3 * k + 1] * p[1] + Qi[3 * k + 2] * p[2];
 #pragma unroll
@@ -188,16 +189,16 @@ __device__ __forceinline__ void langevin_epilogue(const ForceArgs<float> &a, con
     Mv.v[6] = Ft[0]; Mv.v[7] = Ft[1]; Mv.v[8] = Ft[2];
     Mv.v[9] = Tt[0]; Mv.v[10] = Tt[1]; Mv.v[11] = Tt[2];
     Mv.store(a.buf.motion + (size_t)s * kRow);
-    float xn[3] = {xi, yi, zi}, pn[3] = {p[0], p[1], p[2]};
-    drift_position<float>(R, xn, pn, Ft);
+    real xn[3] = {xi, yi, zi}, pn[3] = {p[0], p[1], p[2]};
+    drift_position<real>(R, xn, pn, Ft);
     if (!(isfinite(xn[0]) && isfinite(xn[1]) && isfinite(xn[2]))) {
         atomicOr(a.flags, 1u);
-        xn[0] = xn[1] = xn[2] = 0.f;
+        xn[0] = xn[1] = xn[2] = real(0);
     }
     if (a.skin) {
-        skin_check<float>(a, R, s, xn);
+        skin_check<real>(a, R, s, xn);
     } else {
-        const int key = cell_of<float>(R, xn[0], xn[1], xn[2]);
+        const int key = cell_of<real>(R, xn[0], xn[1], xn[2]);
         const int rank = aggregated_rank(a.count, key);
         a.bin[s] = make_int2(key, rank);
     }
@@ -844,7 +845,7 @@ __device__ void consume_staged_unit(const ForceArgs<float> &a, const StageBuf &B
             const float4 pi = B.pos[myk];
             float Qi[9];
             home_q(W, lane, pi.w, Qi);
-            langevin_epilogue(a, R, g.rep, s, W.h_id[lane], F, T, Qi, pi.x, pi.y, pi.z);
+            langevin_epilogue<float>(a, R, g.rep, s, W.h_id[lane], F, T, Qi, pi.x, pi.y, pi.z);
         }
     }
     __syncwarp();

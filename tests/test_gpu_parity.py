@@ -26,13 +26,19 @@ from oracle import pyoracle as po
 from tests._util import force_errors, load, sorted_pairs, spec_from
 
 pytestmark = pytest.mark.gpu
-PRECISIONS = ["fp32", "fp64", "fp32-tiled"]  # fp32: the default pair pipeline; fp32-tiled: the tile kernel
+# fp32 / fp64: the default pair pipeline in each precision; fp32-tiled: the tile kernel; fp64-pp: the FP64
+# one-thread-per-particle kernel
+PRECISIONS = ["fp32", "fp64", "fp32-tiled", "fp64-pp"]
 
 
 def make(spec, x, Q, precision, p=None, Lb=None, Ft=None, Tt=None):
     n = spec.n
-    s = (LangevinNVTRGPU([spec], precision="fp32", force_kernel="tiled") if precision == "fp32-tiled"
-         else LangevinNVTRGPU([spec], precision=precision))
+    if precision == "fp32-tiled":
+        s = LangevinNVTRGPU([spec], precision="fp32", force_kernel="tiled")
+    elif precision == "fp64-pp":
+        s = LangevinNVTRGPU([spec], precision="fp64", force_kernel="per_particle")
+    else:
+        s = LangevinNVTRGPU([spec], precision=precision)
     z = np.zeros((n, 3))
     s.initialize(x, z if p is None else p, z if Lb is None else Lb, Q, Ft, Tt)
     return s
@@ -61,7 +67,7 @@ def test_forces_and_torques(k, precision):
 
 def check_errors(a, b, precision, flipped_ok=0.0):
     e = force_errors(a, b)
-    rms_tol, max_tol = (1e-12, 1e-11) if precision == "fp64" else (1e-5, 1e-4)
+    rms_tol, max_tol = (1e-12, 1e-11) if precision.startswith("fp64") else (1e-5, 1e-4)
     assert e["rms"] <= rms_tol, e
     if flipped_ok == 0.0:
         assert e["max"] <= max_tol, e
@@ -134,12 +140,12 @@ def test_trajectories_100_steps(k, precision):
     d = load(f"traj_{k}.npz")
     st = _run_gpu(d, precision)
     noise_free = str(d["noise_mode"]) == "off"
-    spread = fp32_shadow_error(d, int(d["nsteps"]), float(d["rc"])) if (noise_free and precision != "fp64") else None
+    spread = fp32_shadow_error(d, int(d["nsteps"]), float(d["rc"])) if (noise_free and not precision.startswith("fp64")) else None
     for key in ("x", "p", "Lb", "Q", "Ft", "Tt"):
         ref = d["final_" + key]
         scale = max(1.0, float(np.abs(ref).max()))
         err = float(np.abs(st[key] - ref).max())
-        if precision == "fp64":
+        if precision.startswith("fp64"):
             assert err <= 1e-9 * scale, (key, err)
         else:
             tol = 2e-4 if key == "x" else 1e-3 * scale
@@ -157,11 +163,11 @@ def test_two_particle_torque_cases(k, precision):
         s.init_forces()
         s.step(int(d["nsteps"]))
         st = s.get_state()
-    spread = fp32_shadow_error(d, int(d["nsteps"]), float(d["rc"])) if precision != "fp64" else None
+    spread = fp32_shadow_error(d, int(d["nsteps"]), float(d["rc"])) if not precision.startswith("fp64") else None
     for key in ("x", "Q", "p", "Lb"):
         ref = d["final_" + key]
         err = float(np.abs(st[key] - ref).max())
-        if precision == "fp64":
+        if precision.startswith("fp64"):
             assert err <= 1e-10 * max(1.0, float(np.abs(ref).max())), (key, err)
         else:
             tol = max(2e-5, 20 * spread[key])
@@ -190,6 +196,6 @@ def test_philox_noise_matches_oracle(precision):
     # F~ = Q^T (Rt xi): solve instead of multiplying by Q (the rounded Q is not exactly orthogonal)
     xi_t = np.linalg.solve(np.transpose(Qm, (0, 2, 1)), st["Ft"][..., None])[..., 0] / Rt
     xi_r = st["Tt"] / Rr
-    tol = 1e-12 if precision == "fp64" else 2e-6
+    tol = 1e-12 if precision.startswith("fp64") else 2e-6
     assert np.abs(xi_t - xi[:, :3]).max() <= tol
     assert np.abs(xi_r - xi[:, 3:]).max() <= tol
