@@ -124,6 +124,48 @@ mtg_binding_model binding_ternary_nonuniform_from(const BMT &bm) {
     return m;
 }
 
+// Patch models of the reference (MDBase/Potentials/ComboPatch) in the C ABI's GeneralPatch form, read from
+// the objects' public members, so a driver passes its own ComboPatch instead of filling arrays by hand.
+// TetrahedralPatch(str, dis, ang) (TetrahedralPatch.cpp:4-44)
+template <class TP>
+mtg_patch_model model_from_tetrahedral(const TP &tp) {
+    mtg_patch_model m;
+    mtg_model_tetrahedral(&m, tp.str, tp.dis, tp.ang);
+    return m;
+}
+// BivalentPatch(str, dis, ang) (BivalentPatch.cpp:4-34)
+template <class BP>
+mtg_patch_model model_from_bivalent(const BP &bp) {
+    mtg_patch_model m;
+    mtg_model_bivalent(&m, bp.str, bp.dis, bp.ang);
+    return m;
+}
+// GeneralPatch (GeneralPatch.cpp:7-121): no_types, no_patches_per_type[], num_per_type[] (cumulative), the
+// orient rows (patch unit vectors, types contiguous) and the params rows (att, dis, thetam) per potential, in
+// the order GeneralPatch enumerates potential_bundle -- the C ABI's own order, so the rows copy unchanged
+template <class GP>
+mtg_patch_model model_from_general(GP &gp) {
+    mtg_patch_model m{};
+    if (gp.no_types < 1 || gp.no_types > MTG_MAX_TYPES)
+        throw std::runtime_error("model_from_general: " + std::to_string(gp.no_types) + " particle types (1 to " +
+                                 std::to_string(MTG_MAX_TYPES) + " supported)");
+    m.n_types = gp.no_types;
+    int norient = 0;
+    for (int k = 0; k < gp.no_types; k++) {
+        m.patches_per_type[k] = gp.no_patches_per_type[k];
+        m.count_per_type[k] = gp.num_per_type[k];
+        norient += gp.no_patches_per_type[k];
+    }
+    const int npots = gp.params.getnrows();
+    if (norient > MTG_MAX_ORIENT || npots > MTG_MAX_POTS)
+        throw std::runtime_error("model_from_general: more patch vectors or potentials than the C ABI holds");
+    for (int i = 0; i < norient; i++)
+        for (int c = 0; c < 3; c++) m.orient[i][c] = gp.orient(i, c);
+    for (int q = 0; q < npots; q++)
+        for (int c = 0; c < 3; c++) m.params[q][c] = gp.params(q, c);
+    return m;
+}
+
 }  // namespace mtg_adapter
 
 template <class Matrix>
@@ -182,6 +224,100 @@ class LangevinNVTRGPU {
         mtg_adapter::from_rows(f, n, 3, F);
         mtg_adapter::from_rows(t, n, 3, T);
     }
+
+    // ---- the loop body one method at a time, with the reference's signatures (Condensate.cpp:335-378):
+    //   advancemom_halfstep(F, T); advance_pos(); rotate(); F = calculateforces(pairs, HS); T = 0;
+    //   calculate_forces_and_torques3D(pairs, patches, F, T); create_forces_and_torques_sphere(F, T, R);
+    //   advancemom_halfstep(F, T);
+    // Pair lists and potentials are accepted for the signatures' sake: the GPU's own cell list finds every pair
+    // within the force range (the pair set of any caller list that covers that range), and the potentials are
+    // the handle's (sethardcore, and the patch model given at construction).
+
+    // MD::calculatepairs_parallel(boxlist, rc) (MD.h:83): a new P x 2 matrix of the pairs (i < j) closer than rc,
+    // which the caller deletes (Condensate.cpp:348-349)
+    template <class IntMatrix>
+    IntMatrix *calculatepairs_parallel(IntMatrix &boxlist, double rc) {
+        (void)boxlist;
+        int64_t np = 0;
+        mtg_status st = mtg_pairs(h_, 0, rc, nullptr, 0, &np);
+        if (st != MTG_OK && st != MTG_ERR_CAPACITY) mtg_adapter::require_ok(h_, st, "calculatepairs_parallel");
+        std::vector<int32_t> buf((size_t)(np > 0 ? np : 1) * 2);
+        mtg_adapter::require_ok(h_, mtg_pairs(h_, 0, rc, buf.data(), np, &np), "calculatepairs_parallel");
+        IntMatrix *out = new IntMatrix((int)np, 2);
+        for (int64_t i = 0; i < np; i++) {
+            (*out)((int)i, 0) = buf[2 * i];
+            (*out)((int)i, 1) = buf[2 * i + 1];
+        }
+        return out;
+    }
+
+    // MD::calculateforces(pairs, HSPotential) (MD.h:110): the WCA core forces (plus any setbonds bonds)
+    template <class IntMatrix, class Potential>
+    Matrix calculateforces(IntMatrix &pairs, Potential &pot) {
+        (void)pairs;
+        (void)pot;
+        const int n = desc_.n;
+        std::vector<double> f((size_t)n * 3);
+        mtg_adapter::require_ok(h_, mtg_calculateforces(h_, f.data()), "calculateforces");
+        Matrix F(n, 3);
+        mtg_adapter::from_rows(f, n, 3, F);
+        return F;
+    }
+
+    // LangevinNVTR::calculate_forces_and_torques3D(pairs, ComboPatch, F, T) (LangevinR.h:247): ADDS the patch
+    // forces to F and the lab-frame torques to T
+    template <class IntMatrix, class Combo>
+    void calculate_forces_and_torques3D(IntMatrix &pairs, Combo &patches, Matrix &F, Matrix &T) {
+        (void)pairs;
+        (void)patches;
+        const int n = desc_.n;
+        std::vector<double> f, t;
+        mtg_adapter::to_rows(F, n, 3, f);
+        mtg_adapter::to_rows(T, n, 3, t);
+        mtg_adapter::require_ok(h_, mtg_calculate_forces_and_torques3D(h_, f.data(), t.data()),
+                                "calculate_forces_and_torques3D");
+        mtg_adapter::from_rows(f, n, 3, F);
+        mtg_adapter::from_rows(t, n, 3, T);
+    }
+
+    // LangevinNVTR::create_forces_and_torques_sphere(F, T, R) (LangevinR.h:244): F (lab), T (lab) in; F~ (lab)
+    // and T~ (body) out, with the caller's n x 6 noise R
+    template <class RMatrix>
+    void create_forces_and_torques_sphere(Matrix &F, Matrix &T, RMatrix &R) {
+        const int n = desc_.n;
+        std::vector<double> f, t, r;
+        mtg_adapter::to_rows(F, n, 3, f);
+        mtg_adapter::to_rows(T, n, 3, t);
+        mtg_adapter::to_rows(R, n, 6, r);
+        mtg_adapter::require_ok(h_, mtg_create_forces_and_torques_sphere(h_, f.data(), t.data(), r.data()),
+                                "create_forces_and_torques_sphere");
+        mtg_adapter::from_rows(f, n, 3, F);
+        mtg_adapter::from_rows(t, n, 3, T);
+    }
+    // the same with the handle's counter-based Philox noise in place of R
+    void create_forces_and_torques_sphere(Matrix &F, Matrix &T) {
+        const int n = desc_.n;
+        std::vector<double> f, t;
+        mtg_adapter::to_rows(F, n, 3, f);
+        mtg_adapter::to_rows(T, n, 3, t);
+        mtg_adapter::require_ok(h_, mtg_create_forces_and_torques_sphere(h_, f.data(), t.data(), nullptr),
+                                "create_forces_and_torques_sphere");
+        mtg_adapter::from_rows(f, n, 3, F);
+        mtg_adapter::from_rows(t, n, 3, T);
+    }
+
+    // LangevinNVTR::advancemom_halfstep(F, T) (LangevinR.h:259): F lab, T body
+    void advancemom_halfstep(Matrix &F, Matrix &T) {
+        const int n = desc_.n;
+        std::vector<double> f, t;
+        mtg_adapter::to_rows(F, n, 3, f);
+        mtg_adapter::to_rows(T, n, 3, t);
+        mtg_adapter::require_ok(h_, mtg_advancemom_halfstep(h_, f.data(), t.data()), "advancemom_halfstep");
+    }
+
+    // LangevinNVT::advance_pos() (Langevin.h:57) and LangevinNVTR::rotate() (LangevinR.h:233)
+    void advance_pos() { mtg_adapter::require_ok(h_, mtg_advance_pos(h_), "advance_pos"); }
+    void rotate() { mtg_adapter::require_ok(h_, mtg_rotate(h_), "rotate"); }
 
     // the bonded term of the polymer drivers: F += MD::calculateforces(bonds, HarmonicPotential(k, r0))
     // (mainActivePolymer.cpp:390-402) on every force pass; bonds is any B x 2 int matrix (e.g. matrix<int>)

@@ -102,10 +102,11 @@ typedef struct {
     const mtg_replica_desc *replicas;
     int device;                        /* CUDA device ordinal */
     int track_displacement;            /* 1: keep FP64 unwrapped-displacement accumulators */
-    int force_kernel;                  /* FP32 only: 0 = pair pipeline (default: pair list, one thread per
-                                              pair, fixed-point atomics on both particles, per-particle
-                                              epilogue), 1 = one thread per particle (the form the FP64
-                                              path uses), 2 = tiled shared-memory kernel */
+    int force_kernel;                  /* 0 = pair pipeline (default, both precisions: pair list, one thread
+                                              per pair, per-particle epilogue; FP32 sums in order-independent
+                                              fixed point, FP64 sums by double atomics), 1 = one thread per
+                                              particle, 2 = tiled shared-memory kernel (FP32 only; an FP64
+                                              handle asking for it gets MTG_ERR_ARG) */
     double neighbor_skin;              /* 0 (default): the cell list is rebuilt every step.  > 0: Verlet
                                           skin (sigma): cells and per-particle candidate lists are built at
                                           force range + skin and reused until some particle has moved more
@@ -158,6 +159,33 @@ mtg_status mtg_step_noise(mtg_system *h, int nsteps, const double *noise);
  * T = the lab-frame torques of LangevinNVTR::calculate_forces_and_torques3D (LangevinR.cpp:911-1047).
  * energy (nullable): per-particle potential energy, half of every pair energy (WCA + KF2). */
 mtg_status mtg_forces(mtg_system *h, double *F, double *T, double *energy);
+
+/* The loop body one phase at a time, for a driver that keeps Condensate::run's loop (Condensate.cpp:335-378)
+ * and swaps its calls one by one.  Host arrays hold all replicas by global index (n x 3 doubles unless
+ * stated); each call runs on the handle's state, synchronises, and matches the fused mtg_step's arithmetic.
+ * The force calls take no pair list: the handle's cell list finds every pair within the force range, which is
+ * the pair set of a caller's list that covers that range.
+ *
+ * MD::calculateforces(pairs, HSPotential) (MD.cpp:1684-1764): F = the WCA core forces (plus the harmonic
+ * bonds of mtg_set_bonds), overwritten. */
+mtg_status mtg_calculateforces(mtg_system *h, double *F);
+/* LangevinNVTR::calculate_forces_and_torques3D(pairs, ComboPatch, F, T) (LangevinR.cpp:911-1047): ADDS the
+ * Kern-Frenkel patch forces to F and the lab-frame torques to T, as the reference does (in single-bond mode:
+ * the bound pairs' forces and torques). */
+mtg_status mtg_calculate_forces_and_torques3D(mtg_system *h, double *F, double *T);
+/* LangevinNVTR::create_forces_and_torques_sphere(F, T, R) (LangevinR.cpp:474-592): F (lab) and T (lab) in,
+ * F~ = F + friction + noise (lab) and T~ (BODY frame) out, in place.  R: n x 6 noise (matrix2.cpp:1807-1821),
+ * or NULL for the handle's Philox noise of the next draw.  F~ and T~ also become the handle's carried
+ * forces, which mtg_step's first half-kick uses. */
+mtg_status mtg_create_forces_and_torques_sphere(mtg_system *h, double *F, double *T, const double *R);
+/* LangevinNVTR::advancemom_halfstep(F, T) (LangevinR.cpp:327-347): p += dt/2 F (F lab), L += dt/2 T (T body). */
+mtg_status mtg_advancemom_halfstep(mtg_system *h, const double *F, const double *T);
+/* LangevinNVT::advance_pos() (Langevin.cpp:205-222): x += (dt/m) p, then wrap (periodic) or reflect with p
+ * negated (walls), cube::correct_position_and_momentum (geometry.h:403-446). */
+mtg_status mtg_advance_pos(mtg_system *h);
+/* LangevinNVTR::rotate() (LangevinR.cpp:594-695): the free-rotor propagator genfullmat (:392-461) applied to
+ * L (L <- R L) and the orientation (Q <- R^T Q). */
+mtg_status mtg_rotate(mtg_system *h);
 
 /* Fixed bonds with HarmonicPotential(k, r0) (MDBase/Potentials/potential.h:265-297): from now on every
  * force pass adds MD::calculateforces(bonds, pot) (MD.cpp:1684-1764), f = -k (r - r0) along the

@@ -114,6 +114,12 @@ SIGNATURES = [
     ("mtg_init_forces", C.c_int, [_H]),
     ("mtg_init_forces_noise", C.c_int, [_H, _D]),
     ("mtg_step_profile", C.c_int, [_H, C.c_int, _D]),
+    ("mtg_calculateforces", C.c_int, [_H, _D]),
+    ("mtg_calculate_forces_and_torques3D", C.c_int, [_H, _D, _D]),
+    ("mtg_create_forces_and_torques_sphere", C.c_int, [_H, _D, _D, _D]),
+    ("mtg_advancemom_halfstep", C.c_int, [_H, _D, _D]),
+    ("mtg_advance_pos", C.c_int, [_H]),
+    ("mtg_rotate", C.c_int, [_H]),
     ("mtg_step", C.c_int, [_H, C.c_int]),
     ("mtg_step_noise", C.c_int, [_H, C.c_int, _D]),
     ("mtg_forces", C.c_int, [_H, _D, _D, _D]),

@@ -337,6 +337,48 @@ mtg_status mtg_get_bind_state(mtg_system *h, int32_t *boundto, uint8_t *isbound)
     return MTG_OK;
 }
 
+// ---- the step's phases one at a time (host arrays by global index, all replicas)
+
+mtg_status mtg_calculateforces(mtg_system *h, double *F) {
+    MTG_GUARD(h, h->impl->phase_forces(1, F, nullptr));
+    return MTG_OK;
+}
+
+mtg_status mtg_calculate_forces_and_torques3D(mtg_system *h, double *F, double *T) {
+    MTG_GUARD(h, {
+        MTG_REQUIRE(F && T, "mtg_calculate_forces_and_torques3D: F and T are required");
+        const size_t n = (size_t)h->impl->ntot();
+        std::vector<double> pf(3 * n), pt(3 * n);
+        h->impl->phase_forces(2, pf.data(), pt.data());
+        // the reference adds the patch terms to the caller's F and T (LangevinR.cpp:1015-1030)
+        for (size_t i = 0; i < 3 * n; i++) {
+            F[i] += pf[i];
+            T[i] += pt[i];
+        }
+    });
+    return MTG_OK;
+}
+
+mtg_status mtg_create_forces_and_torques_sphere(mtg_system *h, double *F, double *T, const double *R) {
+    MTG_GUARD(h, h->impl->phase_langevin(F, T, R));
+    return MTG_OK;
+}
+
+mtg_status mtg_advancemom_halfstep(mtg_system *h, const double *F, const double *T) {
+    MTG_GUARD(h, h->impl->phase_halfkick(F, T));
+    return MTG_OK;
+}
+
+mtg_status mtg_advance_pos(mtg_system *h) {
+    MTG_GUARD(h, h->impl->phase_drift());
+    return MTG_OK;
+}
+
+mtg_status mtg_rotate(mtg_system *h) {
+    MTG_GUARD(h, h->impl->phase_rotate());
+    return MTG_OK;
+}
+
 mtg_status mtg_bind_update(mtg_system *h, double *F, double *T) {
     MTG_GUARD(h, {
         h->impl->bind_update(F, T);

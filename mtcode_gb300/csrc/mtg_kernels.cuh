@@ -504,6 +504,9 @@ struct ForceArgs {
     double *outF, *outT, *outE;      // mode forces: by global index
     double *obs;                     // mode obs: n_rep x 5
     int do_kick;                     // second half-kick (step) or not (init)
+    int parts;                       // terms summed: bit 0 central (WCA core + harmonic bonds), bit 1 patch
+                                     // (Kern-Frenkel force + torque, bound-pair forces); 3 for every pass
+                                     // but the per-phase force calls
     // fixed bonds, by global index (CSR: partners of i are bond_partner[bond_start[i] .. bond_start[i+1]));
     // null when the system has none.  HarmonicPotential(bond_k, bond_r0).
     const int *bond_start, *bond_partner;
@@ -1004,14 +1007,14 @@ __device__ __noinline__ void simple_particle(const ForceArgs<real> &a, int s) {
                         if (r2 < R.rc2) npairs++;
                         // WCA core: same vector for both orientations of the pair
                         real fi[3] = {0, 0, 0};
-                        if (rr < R.hs_limit) {
+                        if (rr < R.hs_limit && (a.parts & 1)) {
                             real s_ = hs_force_over_r<real>(R, r2);
                             big |= fabs(s_ * rr) > real(1e4);
                             fi[0] = s_ * dx; fi[1] = s_ * dy2; fi[2] = s_ * dz2;
                             ewca += real(0.5) * wca_energy<real>(R, r2);
                         }
                         real ti_[3] = {0, 0, 0};
-                        if (r2 < R.patch_r2 || MODE == kModeObs) {
+                        if ((a.parts & 2) && (r2 < R.patch_r2 || MODE == kModeObs)) {
                             const int idj = __ldg(a.buf.ident + j);
                             const int tj = single_type ? 0 : type_of<real>(Mo, idj - R.off);
                             if (Mo.np[ti] > 0 && Mo.np[tj] > 0) {
@@ -1050,12 +1053,12 @@ __device__ __noinline__ void simple_particle(const ForceArgs<real> &a, int s) {
         }
         if (MODE == kModeEdges) return;
         real ebond = real(0);
-        if (a.bond_start && MODE != kModeObs) {
+        if (a.bond_start && MODE != kModeObs && (a.parts & 1)) {
             real fb[3] = {real(0), real(0), real(0)};
             bond_forces<real>(a, R, idi, xi, yi, zi, fb, ebond, big);
             F.add(fb[0], fb[1], fb[2]);
         }
-        if (a.bind_on && MODE != kModeObs) {
+        if (a.bind_on && MODE != kModeObs && (a.parts & 2)) {
             real fb[3] = {real(0), real(0), real(0)}, tb[3] = {real(0), real(0), real(0)};
             bound_patch_forces<real>(a, R, Mo, r, idi, P.v, fb, tb, epatch);
             F.add(fb[0], fb[1], fb[2]);
@@ -1305,6 +1308,137 @@ __global__ void __launch_bounds__(256) temperature_kernel(Tables<real> tb, Buffe
             for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)cur + k, d[k]);
     } else if (cur >= 0) {
         for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)cur + k, d[k]);
+    }
+}
+
+
+// ------------------------------------------------------------------ the step's phases one at a time
+// The reference's loop body calls advancemom_halfstep, advance_pos, rotate, the force routines and
+// create_forces_and_torques_sphere separately (Condensate.cpp:335-378).  These kernels run one phase on the
+// handle's state (every slot) with the caller's forces, torques and noise given by global index, in the same
+// arithmetic as the fused step, so a driver can swap its loop body method by method.
+
+// LangevinNVTR::advancemom_halfstep(F, T) (LangevinR.cpp:327-347): p += dt/2 F (lab), L_body += dt/2 T (body)
+template <class real>
+__global__ void phase_halfkick_kernel(Tables<real> tb, Buffers<real> b, const double *F, const double *T) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
+        const Replica<real> &R = tb.reps[find_replica(tb.rep_slot, tb.nrep, s)];
+        const size_t id = (size_t)b.ident[s];
+        Row<real> M;
+        M.load(b.motion + (size_t)s * kRow);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            M.v[k] = add_rn(M.v[k], mul_rn(R.half_dt, (real)F[3 * id + k]));
+            M.v[3 + k] = M.v[3 + k] + R.half_dt * (real)T[3 * id + k];
+        }
+        M.store(b.motion + (size_t)s * kRow);
+    }
+}
+
+// LangevinNVT::advance_pos (Langevin.cpp:205-222): x += dt/m p, then cube::correct_position_and_momentum
+// (wrap, or reflect and negate p at a wall, geometry.h:403-446); the FP64 displacement follows the drift
+template <class real>
+__global__ void phase_drift_kernel(Tables<real> tb, Buffers<real> b, unsigned *flags) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
+        const Replica<real> &R = tb.reps[find_replica(tb.rep_slot, tb.nrep, s)];
+        Row<real> M;
+        M.load(b.motion + (size_t)s * kRow);
+        real x[4];
+        load4(b.pos + 4 * (size_t)s, x);
+        real step[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            step[k] = mul_rn(R.c1, M.v[k]);
+            x[k] = add_rn(x[k], step[k]);
+            wrap_coord<real>(x[k], M.v[k], R.box, R.periodic);
+        }
+        if (!(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]))) atomicOr(flags, 1u);
+        store4(b.pos + 4 * (size_t)s, x[0], x[1], x[2], x[3]);
+        M.store(b.motion + (size_t)s * kRow);
+        if (b.dx) {
+            b.dx[s] += (double)step[0];
+            b.dy[s] += (double)step[1];
+            b.dz[s] += (double)step[2];
+        }
+    }
+}
+
+// LangevinNVTR::rotate() (LangevinR.cpp:594-695): the free-rotor propagator of genfullmat, L <- R L, Q <- R^T Q
+template <class real>
+__global__ void phase_rotate_kernel(Tables<real> tb, Buffers<real> b) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
+        const Replica<real> &R = tb.reps[find_replica(tb.rep_slot, tb.nrep, s)];
+        Payload<real> P;
+        Row<real> M;
+        P.load(b.pos, b.rota, b.rotb, s);
+        M.load(b.motion + (size_t)s * kRow);
+        const real L[3] = {M.v[3], M.v[4], M.v[5]};
+        real Rm[9];
+        free_rotor<real>(R.dt, R.inertia, L, Rm);
+#pragma unroll
+        for (int a = 0; a < 3; a++) M.v[3 + a] = L[0] * Rm[3 * a] + L[1] * Rm[3 * a + 1] + L[2] * Rm[3 * a + 2];
+        real Q[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) Q[k] = P.v[3 + k];
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) P.v[3 + 3 * a + c] = Q[c] * Rm[a] + Q[3 + c] * Rm[3 + a] + Q[6 + c] * Rm[6 + a];
+        P.store(b.pos, b.rota, b.rotb, s);
+        M.store(b.motion + (size_t)s * kRow);
+    }
+}
+
+// LangevinNVTR::create_forces_and_torques_sphere(F, T, R) (LangevinR.cpp:474-592): friction and noise added to
+// the caller's lab-frame F and T; out: F~ (lab) and T~ (body) by global index, also kept as the carried F~/T~
+// of the state.  noise: the caller's R (ntot x 6 by global index), or null for the handle's Philox draw.
+template <class real>
+__global__ void phase_langevin_kernel(Tables<real> tb, Buffers<real> b, const double *F, const double *T,
+                                      const double *noise, const unsigned long long *draw, double *outF,
+                                      double *outT, unsigned *flags) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
+        const int r = find_replica(tb.rep_slot, tb.nrep, s);
+        const Replica<real> &R = tb.reps[r];
+        const int id = b.ident[s];
+        Payload<real> P;
+        Row<real> M;
+        P.load(b.pos, b.rota, b.rotb, s);
+        M.load(b.motion + (size_t)s * kRow);
+        const real *Qi = P.v + 3;
+        real xi6[6];
+        if (noise) {
+#pragma unroll
+            for (int k = 0; k < 6; k++) xi6[k] = (real)noise[6 * (size_t)id + k];
+        } else {
+            philox_noise6<real>((uint32_t)(id - R.off), (uint32_t)r, draw[0], R.seed_lo, R.seed_hi, xi6);
+        }
+        real Fl[3], Tl[3], pb[3], fb[3], Ft[3], Tt[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            Fl[k] = (real)F[3 * (size_t)id + k];
+            Tl[k] = (real)T[3 * (size_t)id + k];
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) pb[k] = Qi[3 * k] * M.v[0] + Qi[3 * k + 1] * M.v[1] + Qi[3 * k + 2] * M.v[2];
+#pragma unroll
+        for (int k = 0; k < 3; k++) fb[k] = R.fric_t * pb[k] + R.Rt * xi6[k];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            Ft[k] = Fl[k] + fb[0] * Qi[k] + fb[1] * Qi[3 + k] + fb[2] * Qi[6 + k];
+            Tt[k] = R.fric_r * M.v[3 + k] + R.Rr * xi6[3 + k] + Tl[0] * Qi[3 * k] + Tl[1] * Qi[3 * k + 1] +
+                    Tl[2] * Qi[3 * k + 2];
+        }
+        if (!(isfinite(Ft[0]) && isfinite(Ft[1]) && isfinite(Ft[2]) && isfinite(Tt[0]) && isfinite(Tt[1]) &&
+              isfinite(Tt[2])))
+            atomicOr(flags, 1u);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            M.v[6 + k] = Ft[k];
+            M.v[9 + k] = Tt[k];
+            outF[3 * (size_t)id + k] = (double)Ft[k];
+            outT[3 * (size_t)id + k] = (double)Tt[k];
+        }
+        M.store(b.motion + (size_t)s * kRow);
     }
 }
 

@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<re
         if (!(r2 < R.rc2)) continue;  // skin lists hold pairs up to the list range
         const real rr = sqrt_r(r2);
         real fa[3] = {real(0), real(0), real(0)};   // the WCA core; patch terms come from the pair lists' kernels
-        if (rr < R.hs_limit) {
+        if (rr < R.hs_limit && (a.parts & 1)) {
             const real s_ = hs_force_over_r<real>(R, r2);
             big |= fabs(s_ * rr) > real(1e4);
             fa[0] = s_ * d[0];
@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<re
                 }
             }
         }
-        if (KIND == kPairSplit && r2 < R.patch_r2) {
+        if (KIND == kPairSplit && (a.parts & 2) && r2 < R.patch_r2) {
             // the one-sided tests of both particles along d = x_a - x_b (with the 1e-5 margin of the full
             // kernel's own early test): a's cosines -(n . Qa d) / r, b's (n . Qb d) / r
             const Model<real> &M = a.tb.models[R.model];
@@ -588,13 +588,13 @@ __global__ void __launch_bounds__(kPipeThreads) pair_epilogue_kernel(ForceArgs<r
         const int id = a.buf.ident[s];
         real xi[4];
         load4(a.buf.pos + 4 * (size_t)s, xi);
-        if (a.bond_start) {
+        if (a.bond_start && (a.parts & 1)) {
             real eb = real(0);
             bool big = false;
             bond_forces<real>(a, R, id, xi[0], xi[1], xi[2], F, eb, big);
             if (big) atomicOr(a.flags, 2u);
         }
-        if (a.bind_on && !a.bind_listed) {
+        if (a.bind_on && !a.bind_listed && (a.parts & 2)) {
             Payload<real> P;
             P.load(a.buf.pos, a.buf.rota, a.buf.rotb, s);
             real eb = real(0);

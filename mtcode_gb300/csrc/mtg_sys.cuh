@@ -525,6 +525,7 @@ struct Sys : SysBase {
         a.flags = d_flags;
         a.draw = d_draw;
         a.do_kick = do_kick;
+        a.parts = 3;
         if (skin > 0) {
             a.skin = d_skin;
             a.skin_next = d_skin + 1;
@@ -912,7 +913,7 @@ struct Sys : SysBase {
             return;
         }
         if constexpr (std::is_same<real, float>::value) {
-            if (use_tiles && MODE != mtg::kModeObs && !a.outE) {
+            if (use_tiles && MODE != mtg::kModeObs && !a.outE && a.parts == 3) {
                 const int g = std::max(1, std::min(ntiles, occ_tile * sms));  // persistent: one CTA per SM
                 mtg::tile_force_kernel<MODE><<<g, mtg::kTileThreads, tile_smem, st>>>(a, d_tiles, ntiles);
                 counted(1);
@@ -1313,18 +1314,8 @@ struct Sys : SysBase {
     void forces(double *F, double *T, double *E) override {
         if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_forces: no state has been set"};
         MTG_REQUIRE(F && T, "mtg_forces: F and T are required");
-        if (skin > 0) {
-            // the lists are valid for the current positions as long as the sort they were built on is
-            if (!cells_valid) {
-                rebuild_cells(false);
-                set_skin(1, -1, -1);
-                count_rebuild();
-            } else {
-                set_skin(0, -1, -1);
-            }
-        } else if (!cells_valid) {
-            rebuild_cells(false);
-        }
+        // with a skin the lists are valid for the current positions as long as the sort they were built on is
+        ensure_cells();
         size_t n = (size_t)ntot_;
         double *sF = d_stage, *sT = sF + 3 * n, *sE = sT + 3 * n;
         mtg::ForceArgs<real> a = force_args(cur, 0);
@@ -1336,6 +1327,101 @@ struct Sys : SysBase {
         MTG_CUDA(cudaMemcpyAsync(F, sF, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
         MTG_CUDA(cudaMemcpyAsync(T, sT, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
         if (E) MTG_CUDA(cudaMemcpyAsync(E, sE, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+    }
+
+    // ---------------------------------------------------------------- the step's phases one at a time
+
+    // the cell list of the current positions (a phase that moved the particles invalidated it)
+    void ensure_cells() {
+        if (skin > 0) {
+            if (!cells_valid) {
+                rebuild_cells(false);
+                set_skin(1, -1, -1);
+                count_rebuild();
+            } else {
+                set_skin(0, -1, -1);
+            }
+        } else if (!cells_valid) {
+            rebuild_cells(false);
+        }
+    }
+
+    // parts 1: MD::calculateforces(pairs, HSPotential) (+ harmonic bonds) into F; parts 2: the patch forces and
+    // lab torques of calculate_forces_and_torques3D (bound pairs only in single-bond mode) into F and T
+    void phase_forces(int parts, double *F, double *T) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_phase_forces: no state has been set"};
+        MTG_REQUIRE(parts == 1 || parts == 2, "mtg_phase_forces: parts must be 1 (central) or 2 (patch)");
+        MTG_REQUIRE(F && (parts == 1 || T), "mtg_phase_forces: F (and T for the patch part) are required");
+        ensure_cells();
+        size_t n = (size_t)ntot_;
+        double *sF = d_stage, *sT = sF + 3 * n;
+        mtg::ForceArgs<real> a = force_args(cur, 0);
+        a.outF = sF;
+        a.outT = sT;
+        a.parts = parts;
+        launch_force<mtg::kModeForces>(a);
+        check_launch();
+        MTG_CUDA(cudaMemcpyAsync(F, sF, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        if (T) MTG_CUDA(cudaMemcpyAsync(T, sT, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+    }
+
+    // create_forces_and_torques_sphere(F, T, R): F (lab) and T (lab) in, F~ (lab) and T~ (body) out, in place
+    void phase_langevin(double *F, double *T, const double *noise) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_phase_langevin: no state has been set"};
+        MTG_REQUIRE(F && T, "mtg_phase_langevin: F and T are required");
+        size_t n = (size_t)ntot_;
+        double *sF = d_stage, *sT = sF + 3 * n, *sN = sT + 3 * n, *oF = sN + 6 * n, *oT = oF + 3 * n;
+        MTG_CUDA(cudaMemcpyAsync(sF, F, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+        MTG_CUDA(cudaMemcpyAsync(sT, T, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+        if (noise) MTG_CUDA(cudaMemcpyAsync(sN, noise, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, st));
+        else tick_draw();
+        const int g = grid_for(ntot_, 256, occ_stream, sms);
+        mtg::phase_langevin_kernel<real><<<g, 256, 0, st>>>(tables(), buf[cur], sF, sT, noise ? sN : nullptr, d_draw,
+                                                           oF, oT, d_flags);
+        check_launch();
+        nlaunch += 1;
+        MTG_CUDA(cudaMemcpyAsync(F, oF, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaMemcpyAsync(T, oT, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        MTG_CUDA(cudaStreamSynchronize(st));
+        forces_ready = true;
+    }
+
+    // advancemom_halfstep(F lab, T body)
+    void phase_halfkick(const double *F, const double *T) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_phase_halfkick: no state has been set"};
+        MTG_REQUIRE(F && T, "mtg_phase_halfkick: F and T are required");
+        size_t n = (size_t)ntot_;
+        double *sF = d_stage, *sT = sF + 3 * n;
+        MTG_CUDA(cudaMemcpyAsync(sF, F, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+        MTG_CUDA(cudaMemcpyAsync(sT, T, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+        const int g = grid_for(ntot_, 256, occ_stream, sms);
+        mtg::phase_halfkick_kernel<real><<<g, 256, 0, st>>>(tables(), buf[cur], sF, sT);
+        check_launch();
+        nlaunch += 1;
+        MTG_CUDA(cudaStreamSynchronize(st));
+        bins_valid = false;   // the next step's binning came from the old momenta
+    }
+
+    // LangevinNVT::advance_pos
+    void phase_drift() override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_phase_advance_pos: no state has been set"};
+        const int g = grid_for(ntot_, 256, occ_stream, sms);
+        mtg::phase_drift_kernel<real><<<g, 256, 0, st>>>(tables(), buf[cur], d_flags);
+        check_launch();
+        nlaunch += 1;
+        MTG_CUDA(cudaStreamSynchronize(st));
+        cells_valid = bins_valid = false;   // particles left their cells
+    }
+
+    // LangevinNVTR::rotate()
+    void phase_rotate() override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_phase_rotate: no state has been set"};
+        const int g = grid_for(ntot_, 256, occ_stream, sms);
+        mtg::phase_rotate_kernel<real><<<g, 256, 0, st>>>(tables(), buf[cur]);
+        check_launch();
+        nlaunch += 1;
         MTG_CUDA(cudaStreamSynchronize(st));
     }
 

@@ -92,6 +92,12 @@ class ReplicaSpec:
         return d
 
 
+def _inplace(a: np.ndarray) -> np.ndarray:
+    if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous and a.flags.writeable):
+        raise TypeError("an in-place argument must be a writeable C-contiguous float64 array")
+    return a
+
+
 def _check(h, status: int) -> None:
     if status != 0:
         msg = _lib.lib().mtg_last_error(h)
@@ -276,6 +282,34 @@ class LangevinNVTRGPU:
         E = np.empty(self.n) if with_energy else None
         _check(self._h, _lib.lib().mtg_forces(self._h, dptr(F), dptr(T), dptr(E)))
         return (F, T, E) if with_energy else (F, T)
+
+    # ---- the loop body one phase at a time (Condensate.cpp:335-378), arrays by global index
+    def calculateforces(self) -> np.ndarray:
+        """MD::calculateforces(pairs, HSPotential): the WCA core forces (+ harmonic bonds)."""
+        F = np.empty((self.n, 3))
+        _check(self._h, _lib.lib().mtg_calculateforces(self._h, dptr(F)))
+        return F
+
+    def add_patch_forces_and_torques(self, F: np.ndarray, T: np.ndarray) -> None:
+        """calculate_forces_and_torques3D(pairs, ComboPatch, F, T): adds the patch forces to F and the lab
+        torques to T, in place (C-contiguous float64 n x 3 arrays)."""
+        _check(self._h, _lib.lib().mtg_calculate_forces_and_torques3D(self._h, dptr(_inplace(F)), dptr(_inplace(T))))
+
+    def create_forces_and_torques_sphere(self, F: np.ndarray, T: np.ndarray, R: np.ndarray | None = None) -> None:
+        """F (lab), T (lab) -> F~ (lab), T~ (body) in place; R: n x 6 noise, or None for Philox."""
+        Rp = None if R is None else dptr(np.ascontiguousarray(R, dtype=np.float64))
+        _check(self._h, _lib.lib().mtg_create_forces_and_torques_sphere(self._h, dptr(_inplace(F)), dptr(_inplace(T)),
+                                                                         Rp))
+
+    def advancemom_halfstep(self, F: np.ndarray, T: np.ndarray) -> None:
+        _check(self._h, _lib.lib().mtg_advancemom_halfstep(self._h, dptr(np.ascontiguousarray(F, dtype=np.float64)),
+                                                           dptr(np.ascontiguousarray(T, dtype=np.float64))))
+
+    def advance_pos(self) -> None:
+        _check(self._h, _lib.lib().mtg_advance_pos(self._h))
+
+    def rotate(self) -> None:
+        _check(self._h, _lib.lib().mtg_rotate(self._h))
 
     def calculatepairs_parallel(self, rc: float, replica: int = 0) -> np.ndarray:
         """MD::calculatepairs_parallel: sorted (i < j) pairs of one replica within rc."""

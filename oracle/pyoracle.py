@@ -165,6 +165,10 @@ def orc() -> C.CDLL:
         L.orc_run_singlebond.argtypes = [P, _D, _D, _D, _D, _D, _D, _I, C.POINTER(C.c_ubyte), C.POINTER(OrcBinding),
                                          C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
                                          C.c_int, C.c_uint64, C.c_int, _D, C.c_uint64, C.c_uint32, C.c_uint64]
+        L.orc_langevin_forces.argtypes = [P, _D, _D, _D, _D, _D, _D]
+        L.orc_halfkick.argtypes = [C.c_int, C.c_double, _D, _D, _D, _D]
+        L.orc_drift.argtypes = [P, _D, _D]
+        L.orc_rotate.argtypes = [P, _D, _D]
         L.orc_random_positions.restype = C.c_int
         L.orc_random_positions.argtypes = [C.c_int, C.c_double, C.c_int, C.c_double, C.c_uint64, _D]
         L.orc_random_rotations.argtypes = [C.c_int, C.c_uint64, _D]
@@ -325,6 +329,26 @@ class System:
                               _d(np.ascontiguousarray(Q, float)), pr.ctypes.data_as(_I), len(pr), _d(out))
         return out
 
+
+    # ---- the loop body's phases one at a time (arrays modified in place)
+    def patch_forces(self, x, Q, F, T) -> None:
+        """calculate_forces_and_torques3D: adds the patch forces and lab torques of every pair in range."""
+        pr = self.pairs(x, self.force_range * 1.05)
+        orc().orc_patch_forces(C.byref(self.params), _d(np.ascontiguousarray(x, float)),
+                               _d(np.ascontiguousarray(Q, float)), pr.ctypes.data_as(_I), len(pr), _d(F), _d(T))
+
+    def langevin_forces(self, p, Lb, Q, noise, F, T) -> None:
+        """create_forces_and_torques_sphere: F (lab), T (lab) -> F~ (lab), T~ (body), in place."""
+        orc().orc_langevin_forces(C.byref(self.params), _d(p), _d(Lb), _d(Q), _d(noise), _d(F), _d(T))
+
+    def halfkick(self, p, Lb, F, T) -> None:
+        orc().orc_halfkick(int(self.spec.n), float(self.spec.dt), _d(p), _d(Lb), _d(F), _d(T))
+
+    def drift(self, x, p) -> None:
+        orc().orc_drift(C.byref(self.params), _d(x), _d(p))
+
+    def rotate(self, Lb, Q) -> None:
+        orc().orc_rotate(C.byref(self.params), _d(Lb), _d(Q))
 
     # ---- single-bond mode
     def central_forces(self, x) -> np.ndarray:

@@ -29,6 +29,7 @@ using namespace std;
 #include "Condensate/Condensate.h"
 
 #include "LangevinNVTRGPU.hpp"
+#include "LangevinNVTRGPU_reference.hpp"
 
 // Condensate::run's loop with the step on the GPU; the reference's TetrahedralPatch parameters feed
 // the GeneralPatch-form model of the C ABI
@@ -100,6 +101,71 @@ void run_singlebond_on_gpu(double l, int N, matrix<double> &dat, int runtime, Te
     for (int i = 0; i < runtime; i++) obj.step(1);
     obj.getbindings(bbs.isbound, bbs.boundto);
     obj.getdat(dat);
+}
+
+// Condensate::run's own loop body (Condensate.cpp:288-378) with the integrator object swapped for the subclass of
+// LangevinNVTR: every call keeps the reference's signature and argument types
+void condensate_loop_with_the_subclass(double l, matrix<double> &dat, int runtime, ComboPatch *pots) {
+    vector1<bool> pb(3, true);
+    cube geo(l, pb, 3);
+    mtg_dropin::LangevinNVTRGPU b(geo, *pots);
+    b.setdt(0.005);
+    b.setkT(1.0);
+    b.setgamma(1.0);
+    b.setgammar(1.0);
+    const int NN = dat.getNsafe();
+    matrix<double> mom(NN, 3), ang(NN, 3), orient(NN, 9);
+    for (int i = 0; i < NN; i++) orient(i, 0) = orient(i, 4) = orient(i, 8) = 1.0;
+    b.initialize(dat, mom, orient, ang);
+    int ccc;
+    matrix<int> boxes = b.getgeo().generate_boxes_relationships(10, ccc);
+    matrix<int> *pairs = b.calculatepairs_parallel(boxes, 3.5);
+    HSPotential wsa(3.0, 1.0);
+    matrix<double> F(NN, 3), T(NN, 3), RT(NN, 6), zeromatrix(NN, 3);
+    F = b.calculateforces(*pairs, wsa);
+    b.calculate_forces_and_torques3D(*pairs, *pots, F, T);
+    generate_uniform_random_matrix(RT);
+    b.create_forces_and_torques_sphere(F, T, RT);
+    vector1<double> meas(6);
+    for (int i = 0; i < runtime; i++) {
+        b.measured_temperature(meas);
+        b.advancemom_halfstep(F, T);
+        b.advance_pos();
+        b.rotate();
+        F = b.calculateforces(*pairs, wsa);
+        T = zeromatrix;
+        b.calculate_forces_and_torques3D(*pairs, *pots, F, T);
+        generate_uniform_random_matrix(RT);
+        b.create_forces_and_torques_sphere(F, T, RT);
+        b.advancemom_halfstep(F, T);
+    }
+    delete pairs;
+    dat = b.getdat();
+}
+
+// the reference's own patch objects converted to the C ABI's model, without hand-filled arrays
+void patch_models(int N) {
+    TetrahedralPatch tp(8.0, 1.2, acos(0.9));
+    BivalentPatch bp(8.0, 1.2, acos(0.9));
+    vector1<int> ppt(1), npt(1);
+    ppt[0] = 4;
+    npt[0] = N;
+    matrix<double> params(16, 3), orient(4, 3);
+    for (int q = 0; q < 16; q++) {
+        params(q, 0) = 10.0;
+        params(q, 1) = 1.15;
+        params(q, 2) = acos(0.92);
+    }
+    orient(0, 2) = 1.0;
+    orient(1, 2) = -1.0;
+    orient(2, 0) = 1.0;
+    orient(3, 0) = -1.0;
+    GeneralPatch gp(ppt, npt, params, orient);
+    mtg_patch_model m[3] = {mtg_adapter::model_from_tetrahedral(tp), mtg_adapter::model_from_bivalent(bp),
+                            mtg_adapter::model_from_general(gp)};
+    (void)m;
+    mtg_patch_model d = mtg_dropin::patch_model_of(gp, N);
+    (void)d;
 }
 
 int main() { return 0; }

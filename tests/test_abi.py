@@ -17,7 +17,7 @@ HEADER = Path(__file__).resolve().parents[1] / "include" / "mtcode_gb300.h"
 def declared_functions():
     text = HEADER.read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(mtg_[a-z0-9_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(mtg_[A-Za-z0-9_]+)\s*\(", text)))
 
 
 def test_library_exports_every_declared_symbol():

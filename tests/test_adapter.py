@@ -83,6 +83,11 @@ def test_condensate_loop_through_the_adapter_matches_oracle(tmp_path):
 
 
 @pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_per_phase_driver_compiles_standalone():
+    compile_driver("phases_gpu.cpp", BUILD / "phases_gpu")
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
 def test_singlebond_driver_compiles_standalone():
     compile_driver("singlebond_gpu.cpp", BUILD / "singlebond_gpu")
 

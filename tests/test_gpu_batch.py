@@ -1,6 +1,6 @@
 """GPU tests of the batched path: many uneven replicas in one handle.
 
-  forces of every replica of a batch vs the oracle (both FP32 force kernels, and FP64);
+  forces of every replica of a batch vs the oracle (the three FP32 force kernels, and both FP64 ones);
   a replica advanced inside a batch equals the same replica advanced alone (noise off);
   FP32 steps are bit-for-bit reproducible run to run (fixed-point force sums + counter-based noise);
   at the full batched size, Newton's third law holds exactly (the fixed-point pair sums cancel).
@@ -33,7 +33,7 @@ def offsets(W):
 
 
 @pytest.mark.parametrize("precision,kernel", [("fp32", "tiled"), ("fp32", "per_particle"), ("fp32", "pairs"),
-                                              ("fp64", "tiled")])
+                                              ("fp64", "pairs"), ("fp64", "per_particle")])
 def test_batched_forces_vs_oracle(precision, kernel):
     W = small_batch(phi=0.3)
     z = W.zeros3()

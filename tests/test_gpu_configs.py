@@ -1,0 +1,204 @@
+"""Parity at every benchmark configuration's stated size: the CUDA path (through the C ABI) against the
+FP64 oracle on the same seeded inputs.
+
+  C1  4,096 tetrahedral patchy particles, phi 0.10: forces at the start and after 200 steps, and a 100-step
+      trajectory with live Philox noise (the oracle draws the same Philox numbers)
+  C2  65,536 tubulin-like particles (poles + laterals), phi 0.20: the full system
+  C3  1,048,576 particles, 1:3 tetrahedral : WCA crowders, phi 0.25: the full system
+  C4  the full 512-replica batch (5,158,422 particles) in one handle: 8 replicas sampled across the size range
+  C5  one 262,100-bead replica of the bonded-polymer configuration (harmonic bonds + WCA + patches)
+
+Error measures (those of test_gpu_parity.py):
+  force / torque   relative RMS error ||F - F_ref|| / ||F_ref|| over all compared particles, and the worst
+                   particle |F_i - F_ref,i| / rms|F_ref|
+  energy           relative error of each replica's KF2 patch energy and WCA energy (mtg_observables, FP64
+                   reductions) against the oracle's; bonded patch pairs within 0.1% (FP32) / 1 pair (FP64)
+Tolerances: FP32 force and torque RMS <= 1e-5 (the stated force-error target), worst particle <= 1e-4 of the
+RMS; energies <= 1e-5.  FP64: RMS <= 1e-12, worst <= 1e-11, energies <= 1e-11.
+Trajectories (C1, 100 steps, live noise): FP64 within 1e-9 of the state's scale; FP32 within 2e-4 RMS and
+2e-3 worst on positions (single-precision rounding amplified by the stiff WCA core).
+
+With MTG_CONFIG_ERRORS=<path> the measured errors are also written there as JSON (the per-configuration error
+table).
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from mtcode_gb300 import LangevinNVTRGPU, workloads
+from oracle import pyoracle as po
+from tests._util import force_errors
+
+pytestmark = pytest.mark.gpu
+
+RECORDS: list = []
+
+
+@pytest.fixture(scope="module", autouse=True)
+def error_table():
+    yield
+    path = os.environ.get("MTG_CONFIG_ERRORS")
+    if path and RECORDS:
+        with open(path, "w") as f:
+            json.dump(RECORDS, f, indent=1)
+
+
+def f32(a):
+    return np.asarray(a, np.float32).astype(np.float64)
+
+
+def tolerances(precision):
+    return (1e-12, 1e-11, 1e-11) if precision == "fp64" else (1e-5, 1e-4, 1e-5)
+
+
+def compare(config, precision, state, F, T, Fo, To, obs=None, obs_o=None):
+    """Checks and records the errors of one force evaluation (obs: GPU observables rows, obs_o: oracle's)."""
+    rms_tol, max_tol, e_tol = tolerances(precision)
+    ef, et = force_errors(F, Fo), force_errors(T, To)
+    rec = {"config": config, "precision": precision, "state": state, "particles": int(len(Fo)),
+           "force_rms": ef["rms"], "force_worst": ef["max"], "torque_rms": et["rms"], "torque_worst": et["max"]}
+    if obs is not None:
+        obs, obs_o = np.atleast_2d(obs), np.atleast_2d(obs_o)
+        pe = np.abs(obs[:, 0] - obs_o[:, 0]) / np.maximum(np.abs(obs_o[:, 0]), 1e-300)
+        we = np.abs(obs[:, 1] - obs_o[:, 1]) / np.maximum(np.abs(obs_o[:, 1]), 1e-300)
+        rec.update(patch_energy_rel=float(pe.max()), wca_energy_rel=float(we.max()),
+                   bonds=int(obs_o[:, 3].sum()), bonds_diff=int(np.abs(obs[:, 3] - obs_o[:, 3]).max()))
+    RECORDS.append(rec)
+    assert ef["rms"] <= rms_tol and et["rms"] <= rms_tol, rec
+    assert ef["max"] <= max_tol and et["max"] <= max_tol, rec
+    if obs is not None:
+        assert rec["patch_energy_rel"] <= e_tol and rec["wca_energy_rel"] <= e_tol, rec
+        bond_tol = np.maximum(1, 1e-3 * obs_o[:, 3]) if precision == "fp32" else 1
+        assert np.all(np.abs(obs[:, 3] - obs_o[:, 3]) <= bond_tol), rec
+
+
+def oracle_forces(spec, x, Q, bonds=None, k=0.0, r0=0.0):
+    sysm = po.System(spec)
+    if bonds is not None:
+        sysm.set_bonds(bonds, k, r0)
+    F, T = sysm.forces(x, Q)
+    return sysm, F, T
+
+
+def single_system(W, precision, steps, config, bonds=None):
+    """Forces (and energies) of a one-replica workload at its seeded start and after `steps` steps."""
+    spec = W.replicas[0]
+    n = spec.n
+    x0, Q0 = (f32(W.x), f32(W.Q)) if precision == "fp32" else (W.x, W.Q)
+    z = np.zeros((n, 3))
+    with LangevinNVTRGPU([spec], precision=precision) as s:
+        s.initialize(x0, z, z, Q0)
+        if bonds is not None:
+            s.set_bonds(bonds, W.bond_k, W.bond_r0)
+        for label, adv in (("start", 0), (f"after {steps} steps", steps)):
+            if adv:
+                s.init_forces()
+                s.step(adv)
+            st = s.get_state()
+            F, T = s.calculate_forces_and_torques3D()
+            obs = s.observables()[0]
+            sysm, Fo, To = oracle_forces(spec, st["x"], st["Q"], bonds, W.bond_k, W.bond_r0)
+            obs_o = sysm.observables(st["x"], st["Q"])
+            compare(config, precision, label, F, T, Fo, To, obs, obs_o)
+        assert s.flags == 0
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_c1_forces_at_size(precision):
+    single_system(workloads.patchy_c1(seed=1), precision, 200, "C1")
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_c1_trajectory_with_live_noise(precision):
+    """100 steps of the Condensate::run loop with Philox noise; the oracle draws the same numbers."""
+    W = workloads.patchy_c1(seed=2)
+    spec = W.replicas[0]
+    n, nsteps = spec.n, 100
+    x0, Q0 = (f32(W.x), f32(W.Q)) if precision == "fp32" else (W.x.copy(), W.Q.copy())
+    z = np.zeros((n, 3))
+    with LangevinNVTRGPU([spec], precision=precision) as s:
+        s.initialize(x0, z, z, Q0)
+        s.init_forces()
+        s.step(nsteps)
+        got = s.get_state()
+    sysm = po.System(spec)
+    st = dict(x=x0.copy(), p=z.copy(), Lb=z.copy(), Q=Q0.copy())
+    st["Ft"], st["Tt"] = sysm.init_forces(st["x"], st["p"], st["Lb"], st["Q"],
+                                          noise=po.philox_noise(n, spec.seed, 0, 0))
+    assert sysm.run(st, nsteps, noise_mode=2, seed=spec.seed, replica=0, draw0=1, check_skin=False) == 0
+    dev = {}
+    for key in ("x", "p", "Lb", "Q"):
+        d = got[key] - st[key]
+        if key == "x":
+            d -= spec.box * np.round(d / spec.box)
+        dev[key] = {"max": float(np.abs(d).max()), "rms": float(np.sqrt((d ** 2).mean())),
+                    "scale": float(max(1.0, np.abs(st[key]).max()))}
+    RECORDS.append({"config": "C1", "precision": precision, "state": f"{nsteps}-step trajectory, live noise",
+                    "particles": n, "trajectory_deviation": dev})
+    if precision == "fp64":
+        for key, v in dev.items():
+            assert v["max"] <= 1e-9 * v["scale"], (key, v)
+    else:
+        assert dev["x"]["rms"] <= 2e-4 and dev["x"]["max"] <= 2e-3, dev
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_c2_tubulin_full_system(precision):
+    single_system(workloads.patchy_c2(seed=1), precision, 100, "C2")
+
+
+def test_c3_crowded_condensate_full_system_fp32():
+    single_system(workloads.patchy_c3(seed=1), "fp32", 50, "C3")
+
+
+def test_c3_crowded_condensate_full_system_fp64():
+    W = workloads.patchy_c3(seed=1)
+    spec = W.replicas[0]
+    z = np.zeros((spec.n, 3))
+    with LangevinNVTRGPU([spec], precision="fp64") as s:
+        s.initialize(W.x, z, z, W.Q)
+        F, T = s.calculate_forces_and_torques3D()
+        obs = s.observables()[0]
+    sysm, Fo, To = oracle_forces(spec, W.x, W.Q)
+    compare("C3", "fp64", "start", F, T, Fo, To, obs, sysm.observables(W.x, W.Q))
+
+
+def test_c4_full_batch_sampled_replicas():
+    """The whole 512-replica batch in one FP32 handle; eight replicas across the size range against the
+    oracle, at the seeded start and after 200 steps."""
+    W = workloads.patchy_c4(seed=0)
+    sizes = np.array([r.n for r in W.replicas])
+    order = np.argsort(sizes)
+    pick = sorted({int(order[0]), int(order[-1]), *[int(order[int(q * (len(order) - 1))]) for q in
+                                                     (0.15, 0.3, 0.45, 0.6, 0.75, 0.9)]})
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    z = W.zeros3()
+    with LangevinNVTRGPU(W.replicas, precision="fp32") as s:
+        s.initialize(f32(W.x), z, z, f32(W.Q))
+        for label, adv in (("start", 0), ("after 200 steps", 200)):
+            if adv:
+                s.init_forces()
+                s.step(adv)
+            st = s.get_state()
+            F, T = s.calculate_forces_and_torques3D()
+            obs = s.observables()
+            Fs, Ts, Fos, Tos, ob, obo = [], [], [], [], [], []
+            for r in pick:
+                a, b = offs[r], offs[r + 1]
+                sysm, Fo, To = oracle_forces(W.replicas[r], st["x"][a:b], st["Q"][a:b])
+                Fs.append(F[a:b]); Ts.append(T[a:b]); Fos.append(Fo); Tos.append(To)
+                ob.append(obs[r]); obo.append(sysm.observables(st["x"][a:b], st["Q"][a:b]))
+            compare("C4 (8 of 512 replicas)", "fp32", label, np.concatenate(Fs), np.concatenate(Ts),
+                    np.concatenate(Fos), np.concatenate(Tos), np.array(ob), np.array(obo))
+        assert s.flags == 0
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_c5_bonded_polymer_replica(precision):
+    W = workloads.polymer_c5(seed=1, n_replicas=1)
+    single_system(W, precision, 50, "C5 (1 of 64 replicas)", bonds=W.bonds)
