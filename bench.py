@@ -293,6 +293,9 @@ def run_gpu(args, rank, world, local):
     s.init_forces()
     # untimed equilibration: the timed steps see the bonded steady state, not the random start
     s.step(args.equilibrate)
+    # launch shapes of the pair pipeline: the autotuner (or this device's cached choice for this workload)
+    from mtcode_gb300 import tuning
+    tune = tuning.tuned(s, f"{args.workload}|single_bond={args.single_bond}", device=local) if args.tune else None
     s.step(max(args.warmup, 3))
     s.sync()
     stream = torch.cuda.ExternalStream(s.stream, device=torch.device("cuda", local))
@@ -361,6 +364,7 @@ def run_gpu(args, rank, world, local):
     plain = run_plain_fp64(args, local) if args.plain_fp64 and rank == 0 else None
 
     cpu = None
+    s_launch = s.launch_config
     s.close()
     if rank == 0 and world == 1 and args.cpu_baseline:
         cpu = cpu_baseline_line(W, args.cpu_steps, args.single_bond)
@@ -377,6 +381,8 @@ def run_gpu(args, rank, world, local):
                            "state_age_steps": args.equilibrate + max(args.warmup, 3),
                            "single_bond": (f"run_singlebond force pass, BindingModelSingle{tuple(args.single_bond)}"
                                            if args.single_bond else None)},
+                "launch_config": s_launch, "tuning": ({k: v for k, v in tune.items() if k != "launch_config"}
+                                                        if tune else "defaults (--no-tune)"),
                 "gpu_launches": launches, "clocks": clk.summary(), "roofline": roofline, "e2e": e2e,
                 "cpu_baseline": cpu, "plain_fp64": plain}
         print(json.dumps(line), flush=True)
@@ -464,6 +470,8 @@ def main():
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--no-tune", dest="tune", action="store_false",
+                    help="keep the default launch shapes instead of the autotuner's")
     ap.add_argument("--equilibrate", type=int, default=2000,
                     help="untimed steps before the timed region (the bonded steady state)")
     ap.add_argument("--no-plain-fp64", dest="plain_fp64", action="store_false")

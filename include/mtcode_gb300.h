@@ -232,6 +232,31 @@ mtg_status mtg_gr(mtg_system *h, int replica, double rmax, double dr, int64_t *h
  * 672-800) converges to.  Synchronising. */
 mtg_status mtg_clusters(mtg_system *h, int replica, double cut, int32_t *labels);
 
+/* Launch shapes of the pair pipeline (force_kernel 0).  Every shape computes the same FP32 forces bit for bit
+ * (the sums are fixed point), so the shapes only change speed.  The reference has no counterpart: its one
+ * tuning knob is the pair-list rebuild interval (Condensate.cpp:344-350). */
+typedef struct {
+    int pairfind_threads;          /* pair finding, one thread per particle: 128, 256 (default) or 512 */
+    int pairforce_blocks_per_sm;   /* grid of the grid-stride pair-force kernel, blocks of 256 per SM: 1..64 (16) */
+    int patch_blocks_per_sm;       /* grid of the patch-pair (single-bond: edge) kernel per SM: 1..64 (8) */
+    int epilogue_threads;          /* per-particle epilogue: 128, 256 (default) or 512 */
+} mtg_launch_config;
+mtg_status mtg_get_launch_config(mtg_system *h, mtg_launch_config *out);
+/* Sets the shapes; the step graphs are captured again at the next step. */
+mtg_status mtg_set_launch_config(mtg_system *h, const mtg_launch_config *cfg);
+/* Autotuner: coordinate descent over the shapes above (two sweeps), each candidate timed with CUDA events on
+ * steps_per_trial steps of the current state -- the trials are real steps and advance the simulation (about
+ * 20 x steps_per_trial steps in all).  The fastest shape stays set and is returned with its time per step.
+ * A handle without the pair pipeline returns its time per step and the unchanged shapes.  Synchronising. */
+mtg_status mtg_autotune(mtg_system *h, int steps_per_trial, mtg_launch_config *best, double *ms_per_step);
+
+/* Bound on the device loops of mtg_clusters that wait on other threads' progress (each union-find parent walk
+ * and the compare-and-swap retries of one hook): at most `limit` iterations.  0 (the default) restores their
+ * own bound, n + 1, which always suffices.  A loop that reaches its bound stops and latches MTG_FLAG_TIMEOUT,
+ * its kernel returns normally, and mtg_clusters reports MTG_ERR_TIMEOUT; the handle stays usable.  (The tile
+ * kernel's pipeline waits keep their own fixed bound.) */
+mtg_status mtg_set_wait_limit(mtg_system *h, int64_t limit);
+
 /* FP64 unwrapped displacement accumulated since the last mtg_set_state (total particles x 3). */
 mtg_status mtg_get_displacement(mtg_system *h, double *disp);
 

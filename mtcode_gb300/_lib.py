@@ -43,6 +43,14 @@ class PatchModel(C.Structure):
     ]
 
 
+class LaunchConfig(C.Structure):
+    _fields_ = [("pairfind_threads", C.c_int), ("pairforce_blocks_per_sm", C.c_int),
+                ("patch_blocks_per_sm", C.c_int), ("epilogue_threads", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {name: int(getattr(self, name)) for name, _ in self._fields_}
+
+
 class ReplicaDesc(C.Structure):
     _fields_ = [
         ("n", C.c_int),
@@ -120,6 +128,10 @@ SIGNATURES = [
     ("mtg_advancemom_halfstep", C.c_int, [_H, _D, _D]),
     ("mtg_advance_pos", C.c_int, [_H]),
     ("mtg_rotate", C.c_int, [_H]),
+    ("mtg_set_wait_limit", C.c_int, [_H, C.c_int64]),
+    ("mtg_get_launch_config", C.c_int, [_H, C.POINTER(LaunchConfig)]),
+    ("mtg_set_launch_config", C.c_int, [_H, C.POINTER(LaunchConfig)]),
+    ("mtg_autotune", C.c_int, [_H, C.c_int, C.POINTER(LaunchConfig), C.POINTER(C.c_double)]),
     ("mtg_step", C.c_int, [_H, C.c_int]),
     ("mtg_step_noise", C.c_int, [_H, C.c_int, _D]),
     ("mtg_forces", C.c_int, [_H, _D, _D, _D]),

@@ -374,6 +374,40 @@ mtg_status mtg_advance_pos(mtg_system *h) {
     return MTG_OK;
 }
 
+mtg_status mtg_set_wait_limit(mtg_system *h, int64_t limit) {
+    MTG_GUARD(h, {
+        MTG_REQUIRE(limit >= 0, "mtg_set_wait_limit: limit must be >= 0");
+        h->impl->set_wait_limit(limit);
+    });
+    return MTG_OK;
+}
+
+mtg_status mtg_get_launch_config(mtg_system *h, mtg_launch_config *out) {
+    MTG_GUARD(h, {
+        MTG_REQUIRE(out, "mtg_get_launch_config: out is required");
+        h->impl->get_launch_config(out);
+    });
+    return MTG_OK;
+}
+
+mtg_status mtg_set_launch_config(mtg_system *h, const mtg_launch_config *cfg) {
+    MTG_GUARD(h, {
+        MTG_REQUIRE(cfg, "mtg_set_launch_config: cfg is required");
+        h->impl->set_launch_config(cfg);
+    });
+    return MTG_OK;
+}
+
+mtg_status mtg_autotune(mtg_system *h, int steps_per_trial, mtg_launch_config *best, double *ms_per_step) {
+    MTG_GUARD(h, {
+        MTG_REQUIRE(best && ms_per_step, "mtg_autotune: best and ms_per_step are required");
+        h->impl->autotune(steps_per_trial, best, ms_per_step);
+        const uint32_t f = h->impl->flags();
+        if (f & MTG_FLAG_NONFINITE) throw Fail{MTG_ERR_NONFINITE, "mtg_autotune: non-finite state during the trials"};
+    });
+    return MTG_OK;
+}
+
 mtg_status mtg_rotate(mtg_system *h) {
     MTG_GUARD(h, h->impl->phase_rotate());
     return MTG_OK;

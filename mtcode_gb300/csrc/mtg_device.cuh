@@ -218,6 +218,27 @@ __device__ __forceinline__ real min_image(real dx, real l, real l2s, int periodi
     return dx;
 }
 
+// The minimum-image separation x_a - x_b by the same rule.  FP64 forms it as the reference does, (x_a - x_b) -+ l.
+// FP32 forms the corrected separation as (x_a - l) - x_b or x_a - (x_b - l): the coordinate next to the far face
+// lies in [l/2, l], so its difference with l is exact (Sterbenz), and the separation carries one rounding of its
+// own size -- (x_a - x_b) -+ l would carry one of the box length's (4e-6 at l = 130, 3e-6 relative at r = 1.5).
+template <class real>
+__device__ __forceinline__ real min_image_sep(real xa, real xb, real l, real l2s, int periodic) {
+    real dx = xa - xb;
+    if (periodic && dx * dx > l2s) {
+        if constexpr (sizeof(real) == 4) dx = dx >= real(0) ? (xa - l) - xb : xa - (xb - l);
+        else dx = dx >= real(0) ? dx - l : dx + l;
+    }
+    return dx;
+}
+// x_a - x_b for a partner reached across a periodic face with image shift sh (+l, -l or 0), in the arithmetic of
+// min_image_sep (both give the same bits for the same pair)
+template <class real>
+__device__ __forceinline__ real shifted_sep(real xa, real xb, real sh) {
+    if constexpr (sizeof(real) == 4) return sh > real(0) ? (xa - sh) - xb : (sh < real(0) ? xa - (xb + sh) : xa - xb);
+    else return (xa - xb) - sh;
+}
+
 // ------------------------------------------------------------------ Philox4x32-10
 // Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3" (SC'11).
 __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
@@ -261,10 +282,12 @@ template <class real> struct Acc3;
 // so it can differ from a correctly rounded conversion by one unit in the last place; it is a fixed
 // function of the sum, which is what order independence needs.
 __device__ __forceinline__ long long to_fixed(float v) {
-    const float h = floorf(v);
-    const int hi = __float2int_rz(h);
-    const unsigned lo = __float2uint_rn((v - h) * 4294967296.0f);
-    return (long long)(((unsigned long long)(long long)hi << 32) + (unsigned long long)lo);
+    const float a = fabsf(v);
+    const float h = floorf(a);                                      // exact
+    const unsigned hi = __float2uint_rz(h);
+    const unsigned lo = __float2uint_rn((a - h) * 4294967296.0f);   // a - h exact, < 1 - 2^-24: fits
+    const long long m = (long long)(((unsigned long long)hi << 32) + (unsigned long long)lo);
+    return v < 0.f ? -m : m;
 }
 __device__ __forceinline__ float from_fixed(long long a) {
     const int hi = (int)(a >> 32);
@@ -298,6 +321,62 @@ __device__ __forceinline__ real hs_force_over_r(const Replica<real> &R, real r2)
     real inv2 = real(1) / r2;
     real s6 = R.hs_s6 * inv2 * inv2 * inv2;  // (sigma/r)^6
     return R.hs_4eps * inv2 * (real(12) * s6 * s6 - real(6) * s6);
+}
+
+// ---- float-float arithmetic (Dekker; Knuth's two-sum; the product error from an FMA), for the FP32 WCA core.
+// Every operation is an explicit round-to-nearest intrinsic, so no contraction changes the error terms.
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ FF ff_two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ FF ff_fast_sum(float a, float b) {   // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    const FF s = ff_two_sum(a.hi, b.hi);
+    return ff_fast_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+    const FF p = ff_two_prod(a.hi, b.hi);
+    return ff_fast_sum(p.hi, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, p.lo)));
+}
+__device__ __forceinline__ FF ff_mul(FF a, float b) {
+    const FF p = ff_two_prod(a.hi, b);
+    return ff_fast_sum(p.hi, __fmaf_rn(a.lo, b, p.lo));
+}
+// 1 / a: the rounded reciprocal of a.hi and one Newton correction with the residual 1 - a r0 kept exactly
+__device__ __forceinline__ FF ff_rcp(FF a) {
+    const float r0 = __frcp_rn(a.hi);
+    const FF p = ff_two_prod(a.hi, r0);
+    const float e = __fmaf_rn(-a.lo, r0, __fsub_rn(__fsub_rn(1.0f, p.hi), p.lo));   // 1 - p.hi is exact
+    return ff_fast_sum(r0, __fmul_rn(r0, e));
+}
+
+// The WCA core force of one pair in FP32 as float-float components: force = hi + lo per axis, from the exact
+// separation d (x_a - x_b).  |d|^2, 1/|d|^2, the powers and the force law run in float-float, so the pair force
+// carries about 1e-12 relative error instead of single precision's ~1e-7: the net force of a particle whose pair
+// forces of tens of eps/sigma cancel stays accurate (the sums are fixed point, 2^-32).  Same law as
+// hs_force_over_r: 4 eps (12 s^12/r^14 - 6 s^6/r^8) times d.
+__device__ __forceinline__ void hs_force_ff(const Replica<float> &R, const float d[3], float hi[3], float lo[3]) {
+    const FF r2 = ff_add(ff_add(ff_two_prod(d[0], d[0]), ff_two_prod(d[1], d[1])), ff_two_prod(d[2], d[2]));
+    const FF inv = ff_rcp(r2);
+    const FF s6 = ff_mul(ff_mul(ff_mul(inv, inv), inv), R.hs_s6);                      // (sigma / r)^6
+    const FF t = ff_add(ff_mul(ff_mul(s6, s6), 12.0f), ff_mul(s6, -6.0f));           // 12 s^12 - 6 s^6
+    const FF g = ff_mul(ff_mul(inv, t), R.hs_4eps);                                  // force / r
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const FF v = ff_mul(g, d[k]);
+        hi[k] = v.hi;
+        lo[k] = v.lo;
+    }
 }
 
 // shifted WCA energy used for the energy observable

@@ -55,6 +55,7 @@ struct Tables {
     int ncells;
     int uniform;   // every replica has the pair constants of replica 0 and one particle type: pair kernels
                    // read replica 0 instead of searching the slot's replica
+    const unsigned short *slot_rep;   // replica of every slot (slot ranges are fixed), or null: binary search
 };
 
 // the device's noise-draw counter (draw used by the next pass, next draw), set from the host by value: a
@@ -74,6 +75,12 @@ __device__ __forceinline__ int find_replica(const int *rep_slot, int nrep, int s
         else hi = mid;
     }
     return lo;
+}
+
+// the replica of slot s: one 2-byte load where the per-slot table exists (fewer than 65,536 replicas)
+template <class real>
+__device__ __forceinline__ int replica_of(const Tables<real> &tb, int s) {
+    return tb.slot_rep ? (int)__ldg(tb.slot_rep + s) : replica_of(tb, s);
 }
 
 // cell id of a position inside replica R (cube::assign_box with cells of the force grid)
@@ -114,7 +121,7 @@ __global__ void __launch_bounds__(256) bin_kernel(Tables<real> tb, Buffers<real>
                                                   unsigned *flags, const int *gate = nullptr) {
     if (gated_off(gate, 1)) return;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
-        const int r = find_replica(tb.rep_slot, tb.nrep, s);
+        const int r = replica_of(tb, s);
         const Replica<real> R = tb.reps[r];
         real x[3];
         load_pos(in.pos + 4 * (size_t)s, x[0], x[1], x[2]);
@@ -364,7 +371,7 @@ __global__ void __launch_bounds__(256) scatter_kernel(Tables<real> tb, Buffers<r
             if (snap_due && *snap_due) P.store(out.snap_a, out.snap_b, out.snap_c, id);
         }
         if (MOVE) {
-            const int r = find_replica(tb.rep_slot, tb.nrep, s);
+            const int r = replica_of(tb, s);
             const Replica<real> R = tb.reps[r];
             real step[3];
             advance_particle<real>(R, P, M, step, flags);
@@ -424,7 +431,7 @@ __global__ void __launch_bounds__(256) integrate_kernel(Tables<real> tb, Buffers
         Row<real> M;
         P.load(b.pos, b.rota, b.rotb, s);
         M.load(b.motion + (size_t)s * kRow);
-        const int r = find_replica(tb.rep_slot, tb.nrep, s);
+        const int r = replica_of(tb, s);
         const Replica<real> R = tb.reps[r];
         real step[3];
         advance_particle<real>(R, P, M, step, flags);
@@ -647,9 +654,9 @@ __device__ __forceinline__ bool candidate(const BindRep &B, const Replica<real> 
     Payload<real> A, C;
     A.load(sa, sb, sc, s1);
     C.load(sa, sb, sc, s2);
-    const real dx = min_image<real>(A.v[0] - C.v[0], R.box, R.l2s, R.periodic);
-    const real dy = min_image<real>(A.v[1] - C.v[1], R.box, R.l2s, R.periodic);
-    const real dz = min_image<real>(A.v[2] - C.v[2], R.box, R.l2s, R.periodic);
+    const real dx = min_image_sep<real>(A.v[0], C.v[0], R.box, R.l2s, R.periodic);
+    const real dy = min_image_sep<real>(A.v[1], C.v[1], R.box, R.l2s, R.periodic);
+    const real dz = min_image_sep<real>(A.v[2], C.v[2], R.box, R.l2s, R.periodic);
     const real r2 = dx * dx + dy * dy + dz * dz;
     const int t = side_of<real>(r2, B.memb2_lo, B.memb2_hi);
     if (t > 0) return false;
@@ -813,9 +820,9 @@ template <class real>
 __device__ __forceinline__ void skin_check(const ForceArgs<real> &a, const Replica<real> &R, int s, const real xn[3]) {
     real xr, yr, zr;
     load_pos(a.buf.xref + 4 * (size_t)s, xr, yr, zr);
-    const real dx = min_image<real>(xn[0] - xr, R.box, R.l2s, R.periodic);
-    const real dy = min_image<real>(xn[1] - yr, R.box, R.l2s, R.periodic);
-    const real dz = min_image<real>(xn[2] - zr, R.box, R.l2s, R.periodic);
+    const real dx = min_image_sep<real>(xn[0], xr, R.box, R.l2s, R.periodic);
+    const real dy = min_image_sep<real>(xn[1], yr, R.box, R.l2s, R.periodic);
+    const real dz = min_image_sep<real>(xn[2], zr, R.box, R.l2s, R.periodic);
     if (!(dx * dx + dy * dy + dz * dz <= R.half_skin2)) *a.skin_next = 1;
 }
 
@@ -832,9 +839,9 @@ __device__ __forceinline__ void bond_forces(const ForceArgs<real> &a, const Repl
         const int j = __ldg(a.buf.slot_of + __ldg(a.bond_partner + b));
         real xj, yj, zj;
         load_pos(a.buf.pos + 4 * (size_t)j, xj, yj, zj);
-        const real dx = min_image<real>(xi - xj, R.box, R.l2s, R.periodic);
-        const real dy = min_image<real>(yi - yj, R.box, R.l2s, R.periodic);
-        const real dz = min_image<real>(zi - zj, R.box, R.l2s, R.periodic);
+        const real dx = min_image_sep<real>(xi, xj, R.box, R.l2s, R.periodic);
+        const real dy = min_image_sep<real>(yi, yj, R.box, R.l2s, R.periodic);
+        const real dz = min_image_sep<real>(zi, zj, R.box, R.l2s, R.periodic);
         const real r = sqrt(dx * dx + dy * dy + dz * dz);
         const real f1 = -a.bond_k * (r - a.bond_r0);
         big |= fabs(f1) > real(1e4);
@@ -868,9 +875,9 @@ __device__ __forceinline__ void bound_patch_forces(const ForceArgs<real> &a, con
         const bool i_first = li < lj;
         const real *P1 = i_first ? Pi : Pj.v, *P2 = i_first ? Pj.v : Pi;
         const int t1 = i_first ? ti : tj, t2 = i_first ? tj : ti, c1 = i_first ? ka : kb, c2 = i_first ? kb : ka;
-        const real dx = min_image<real>(P1[0] - P2[0], R.box, R.l2s, R.periodic);
-        const real dy = min_image<real>(P1[1] - P2[1], R.box, R.l2s, R.periodic);
-        const real dz = min_image<real>(P1[2] - P2[2], R.box, R.l2s, R.periodic);
+        const real dx = min_image_sep<real>(P1[0], P2[0], R.box, R.l2s, R.periodic);
+        const real dy = min_image_sep<real>(P1[1], P2[1], R.box, R.l2s, R.periodic);
+        const real dz = min_image_sep<real>(P1[2], P2[2], R.box, R.l2s, R.periodic);
         const real rr = sqrt(dx * dx + dy * dy + dz * dz);
         const int q = M.pstart[t1][t2] + c1 * M.np[t2] + c2;
         if (rr > M.rmax[q]) continue;   // interaction_distance (potentialtheta.h:522)
@@ -903,7 +910,7 @@ template <class real, int MODE>
 __device__ __noinline__ void simple_particle(const ForceArgs<real> &a, int s) {
     const Tables<real> &tb = a.tb;
     {
-        const int r = find_replica(tb.rep_slot, tb.nrep, s);
+        const int r = replica_of(tb, s);
         const Replica<real> &R = tb.reps[r];
         const Model<real> &Mo = tb.models[R.model];
         Payload<real> P;
@@ -990,9 +997,9 @@ __device__ __noinline__ void simple_particle(const ForceArgs<real> &a, int s) {
                         if (j == s) continue;
                         real xj, yj, zj;
                         load_pos(a.buf.pos + 4 * (size_t)j, xj, yj, zj);
-                        real dx = min_image<real>(xi - xj, R.box, R.l2s, R.periodic);
-                        real dy2 = min_image<real>(yi - yj, R.box, R.l2s, R.periodic);
-                        real dz2 = min_image<real>(zi - zj, R.box, R.l2s, R.periodic);
+                        real dx = min_image_sep<real>(xi, xj, R.box, R.l2s, R.periodic);
+                        real dy2 = min_image_sep<real>(yi, yj, R.box, R.l2s, R.periodic);
+                        real dz2 = min_image_sep<real>(zi, zj, R.box, R.l2s, R.periodic);
                         real r2 = dx * dx + dy2 * dy2 + dz2 * dz2;
                         if (!(r2 < range2)) continue;
                         if (MODE == kModeEdges) {   // single-bond mode: this update's edges, each pair once
@@ -1291,7 +1298,7 @@ __global__ void __launch_bounds__(256) temperature_kernel(Tables<real> tb, Buffe
         if (s >= next_start) {  // a replica boundary (slots ascend)
             if (cur >= 0)
                 for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)cur + k, acc.get(k));
-            cur = find_replica(tb.rep_slot, tb.nrep, s);
+            cur = replica_of(tb, s);
             next_start = __ldg(tb.rep_slot + cur + 1);
             acc.clear();
         }
@@ -1322,7 +1329,7 @@ __global__ void __launch_bounds__(256) temperature_kernel(Tables<real> tb, Buffe
 template <class real>
 __global__ void phase_halfkick_kernel(Tables<real> tb, Buffers<real> b, const double *F, const double *T) {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
-        const Replica<real> &R = tb.reps[find_replica(tb.rep_slot, tb.nrep, s)];
+        const Replica<real> &R = tb.reps[replica_of(tb, s)];
         const size_t id = (size_t)b.ident[s];
         Row<real> M;
         M.load(b.motion + (size_t)s * kRow);
@@ -1340,7 +1347,7 @@ __global__ void phase_halfkick_kernel(Tables<real> tb, Buffers<real> b, const do
 template <class real>
 __global__ void phase_drift_kernel(Tables<real> tb, Buffers<real> b, unsigned *flags) {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
-        const Replica<real> &R = tb.reps[find_replica(tb.rep_slot, tb.nrep, s)];
+        const Replica<real> &R = tb.reps[replica_of(tb, s)];
         Row<real> M;
         M.load(b.motion + (size_t)s * kRow);
         real x[4];
@@ -1367,7 +1374,7 @@ __global__ void phase_drift_kernel(Tables<real> tb, Buffers<real> b, unsigned *f
 template <class real>
 __global__ void phase_rotate_kernel(Tables<real> tb, Buffers<real> b) {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
-        const Replica<real> &R = tb.reps[find_replica(tb.rep_slot, tb.nrep, s)];
+        const Replica<real> &R = tb.reps[replica_of(tb, s)];
         Payload<real> P;
         Row<real> M;
         P.load(b.pos, b.rota, b.rotb, s);
@@ -1397,7 +1404,7 @@ __global__ void phase_langevin_kernel(Tables<real> tb, Buffers<real> b, const do
                                       const double *noise, const unsigned long long *draw, double *outF,
                                       double *outT, unsigned *flags) {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < tb.ntot; s += gridDim.x * blockDim.x) {
-        const int r = find_replica(tb.rep_slot, tb.nrep, s);
+        const int r = replica_of(tb, s);
         const Replica<real> &R = tb.reps[r];
         const int id = b.ident[s];
         Payload<real> P;

@@ -202,33 +202,39 @@ __global__ void uf_init_kernel(int n, int *parent) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) parent[i] = i;
 }
 
+// limit: the bound on every parent walk and on the compare-and-swap retries of one hook, which wait on the
+// progress of other threads' hooks (n + 1 always suffices; a smaller caller limit may give up early).  A loop
+// that reaches it stops, latches MTG_FLAG_TIMEOUT and the kernel returns normally.
 template <class real>
 __global__ void uf_hook_kernel(PairGrid g, Buffers<real> in, const int *start, const int *members, int *parent,
-                               unsigned *flags) {
+                               unsigned *flags, int limit) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
         const int s = g.off + i;
         const int li = in.ident[s] - g.off;
         bool ok = true;
         pair_visit<real>(g, in, start, members, s, li, [&](int lj) {
             int u = li, v = lj;
-            for (int it = 0; it <= g.n && ok; it++) {
-                u = uf_find(parent, u, g.n + 1, ok);
-                v = uf_find(parent, v, g.n + 1, ok);
-                if (u == v) break;
+            bool done = false;
+            for (int it = 0; it < limit && ok; it++) {
+                u = uf_find(parent, u, limit, ok);
+                v = uf_find(parent, v, limit, ok);
+                if (!ok) break;
+                if (u == v) { done = true; break; }
                 if (u < v) { const int t = u; u = v; v = t; }
                 const int old = atomicCAS(parent + u, u, v);
-                if (old == u) break;
+                if (old == u) { done = true; break; }
                 u = old;
             }
+            if (!done) ok = false;
         });
         if (!ok) atomicOr(flags, 4u);
     }
 }
 
-__global__ void uf_label_kernel(int n, const int *parent, int32_t *labels, unsigned *flags) {
+__global__ void uf_label_kernel(int n, const int *parent, int32_t *labels, unsigned *flags, int limit) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         bool ok = true;
-        labels[i] = uf_find(parent, i, n + 1, ok);
+        labels[i] = uf_find(parent, i, limit, ok);
         if (!ok) atomicOr(flags, 4u);
     }
 }

@@ -22,13 +22,13 @@
 namespace mtg {
 namespace {  // internal linkage
 
-constexpr int kPipeThreads = 256;
-constexpr int kPairBlockCap = 2048;    // pairs a pairfind block buffers in shared memory
+constexpr int kPipeThreads = 256;      // block size of the grid-stride pair kernels; pairfind and the epilogue
+                                       // take theirs from the launch configuration (128, 256 or 512)
+constexpr int kPairsPerThread = 8;     // pairs a pairfind block buffers in shared memory, per thread
 constexpr int kPairsPerParticle = 16;  // capacity of the pair list (unordered pairs per particle)
 
 // |d|^2 with explicit roundings (no contraction), so that pairfind and pairforce decide a pair at the
-// cutoff identically; with the image shift applied as (x_i - x_j) - s the separation is bit for bit the
-// minimum image's
+// cutoff identically; with the image shift applied by shifted_sep the separation is bit for bit min_image_sep's
 template <class real>
 __device__ __forceinline__ real sep_r2(real dx, real dy, real dz) {
     return add_rn(add_rn(mul_rn(dx, dx), mul_rn(dy, dy)), mul_rn(dz, dz));
@@ -55,8 +55,9 @@ __device__ __forceinline__ void load_q(const ForceArgs<double> &a, int slot, dou
 // Appends the pairs (s, c0 + b) for every bit b of each lane's mask: one warp-wide scan of the counts and
 // one shared-memory atomic per warp take consecutive entries of the block buffer; entries past its end go
 // straight to the list.  Called by all 32 lanes of the warp.
-__device__ __forceinline__ void warp_pair_flush(int2 *buf, int *nb, int s, int c0, unsigned mask, int2 *pairs,
-                                                unsigned long long *npairs, long long cap, unsigned *flags) {
+__device__ __forceinline__ void warp_pair_flush(int2 *buf, int buf_cap, int *nb, int s, int c0, unsigned mask,
+                                                int2 *pairs, unsigned long long *npairs, long long cap,
+                                                unsigned *flags) {
     const unsigned full = 0xffffffffu;
     if (!__ballot_sync(full, mask != 0u)) return;
     const int lane = threadIdx.x & 31;
@@ -74,7 +75,7 @@ __device__ __forceinline__ void warp_pair_flush(int2 *buf, int *nb, int s, int c
         const int b = __ffs(mask) - 1;
         mask &= mask - 1u;
         const int2 p = make_int2(s, c0 + b);
-        if (q < kPairBlockCap) {
+        if (q < buf_cap) {
             buf[q] = p;
         } else {  // the block buffer is full
             const unsigned long long w = atomicAdd(npairs, 1ull);
@@ -89,12 +90,13 @@ __device__ __forceinline__ void warp_pair_flush(int2 *buf, int *nb, int s, int c
 // Each lane scans its particle's candidate segments in chunks of at most 32 slots and marks the hits of a
 // chunk in a bit mask; the warp then appends the marked pairs together (warp_pair_flush), so the candidate
 // loop itself carries no appends.  The chunk and segment loops are warp-uniform.
-template <class real>
-__global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<real> a, int2 *pairs,
-                                                                unsigned long long *npairs, long long cap,
-                                                                int range_list, const int *gate) {
+template <class real, int THREADS>
+__global__ void __launch_bounds__(THREADS) pairfind_kernel(ForceArgs<real> a, int2 *pairs,
+                                                           unsigned long long *npairs, long long cap,
+                                                           int range_list, const int *gate) {
     if (gated_off(gate, 1)) return;
-    __shared__ int2 buf[kPairBlockCap];
+    constexpr int kBufCap = kPairsPerThread * THREADS;
+    __shared__ int2 buf[kBufCap];
     __shared__ int nb;
     __shared__ unsigned long long base;
     if (threadIdx.x == 0) nb = 0;
@@ -102,7 +104,7 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<real> 
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = s < a.tb.ntot;
     int r = 0;
-    if (valid) r = find_replica(a.tb.rep_slot, a.tb.nrep, s);
+    if (valid) r = replica_of(a.tb, s);
     const Replica<real> &R = a.tb.reps[r];
     const real range2 = range_list ? R.rc2_list : R.rc2;
     const int nc = R.nc;
@@ -135,7 +137,8 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<real> 
                 dz = rr <= 1 ? 0 : 1;
             }
             // pairfind runs right after a sort, so every particle lies in its cell: a neighbour cell
-            // reached across a periodic face holds coordinates one box length away (image shift)
+            // reached across a periodic face holds coordinates one box length away (image shift, applied in
+            // the arithmetic of min_image_sep, so pairforce sees the same separation bit for bit)
             int zz = small ? dz : cz + dz, yy = small ? dy : cy + dy;
             bool skip = small && (dy >= nc || dz >= nc);
             if (zz >= nc) {
@@ -189,7 +192,8 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<real> 
                     for (int t = c0; t < ce; t++) {
                         real pj[3];
                         load_pos(a.buf.pos + 4 * (size_t)t, pj[0], pj[1], pj[2]);
-                        const real dx = (pi[0] - pj[0]) - shx, dy2 = (pi[1] - pj[1]) - shy, dz2 = (pi[2] - pj[2]) - shz;
+                        const real dx = shifted_sep<real>(pi[0], pj[0], shx), dy2 = shifted_sep<real>(pi[1], pj[1], shy),
+                                   dz2 = shifted_sep<real>(pi[2], pj[2], shz);
                         if (sep_r2<real>(dx, dy2, dz2) < range2) mask |= 1u << (t - c0);
                     }
                 } else {  // tiny grids: no cell geometry to lean on
@@ -197,18 +201,18 @@ __global__ void __launch_bounds__(kPipeThreads) pairfind_kernel(ForceArgs<real> 
                     for (int t = c0; t < ce; t++) {
                         real pj[3];
                         load_pos(a.buf.pos + 4 * (size_t)t, pj[0], pj[1], pj[2]);
-                        const real dx = min_image<real>(pi[0] - pj[0], R.box, R.l2s, R.periodic);
-                        const real dy2 = min_image<real>(pi[1] - pj[1], R.box, R.l2s, R.periodic);
-                        const real dz2 = min_image<real>(pi[2] - pj[2], R.box, R.l2s, R.periodic);
+                        const real dx = min_image_sep<real>(pi[0], pj[0], R.box, R.l2s, R.periodic);
+                        const real dy2 = min_image_sep<real>(pi[1], pj[1], R.box, R.l2s, R.periodic);
+                        const real dz2 = min_image_sep<real>(pi[2], pj[2], R.box, R.l2s, R.periodic);
                         if (sep_r2<real>(dx, dy2, dz2) < range2) mask |= 1u << (t - c0);
                     }
                 }
-                warp_pair_flush(buf, &nb, s, c0, mask, pairs, npairs, cap, a.flags);
+                warp_pair_flush(buf, kBufCap, &nb, s, c0, mask, pairs, npairs, cap, a.flags);
             }
         }
     }
     __syncthreads();
-    const int n = nb < kPairBlockCap ? nb : kPairBlockCap;
+    const int n = nb < kBufCap ? nb : kBufCap;
     if (threadIdx.x == 0) base = n ? atomicAdd(npairs, (unsigned long long)n) : 0ull;
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -263,6 +267,13 @@ __device__ __forceinline__ void fixed_add(long long *acc, float v) {
 __device__ __forceinline__ void fixed_add(double *acc, double v) {
     if (v != 0.0) atomicAdd(acc, v);
 }
+// a term already in the sum's representation (FP32: fixed point; FP64: double)
+__device__ __forceinline__ void acc_add_raw(long long *acc, long long v) {
+    if (v != 0) atomicAdd(reinterpret_cast<unsigned long long *>(acc), (unsigned long long)v);
+}
+__device__ __forceinline__ void acc_add_raw(double *acc, double v) {
+    if (v != 0.0) atomicAdd(acc, v);
+}
 
 // Forces and torques of the listed pairs into acc (6 fixed-point sums per slot: F lab, T lab).
 // KIND kPairSplit: WCA core here; pairs where both particles have a patch near a cone go to `list` for
@@ -296,24 +307,34 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<re
         const int2 pr = next;  // the next iteration's entry is loaded one iteration ahead
         if (q + stride < n) next = __ldcs(pairs + q + stride);
         const int sa = pr.x, sb = pr.y;
-        const int r = a.tb.uniform ? 0 : find_replica(a.tb.rep_slot, a.tb.nrep, sa);
+        const int r = a.tb.uniform ? 0 : replica_of(a.tb, sa);
         const Replica<real> &R = a.tb.reps[r];
         real xa[4], xb[4];
         load4(a.buf.pos + 4 * (size_t)sa, xa);
         load4(a.buf.pos + 4 * (size_t)sb, xb);
-        const real d[3] = {min_image<real>(xa[0] - xb[0], R.box, R.l2s, R.periodic),
-                           min_image<real>(xa[1] - xb[1], R.box, R.l2s, R.periodic),
-                           min_image<real>(xa[2] - xb[2], R.box, R.l2s, R.periodic)};
+        const real d[3] = {min_image_sep<real>(xa[0], xb[0], R.box, R.l2s, R.periodic),
+                           min_image_sep<real>(xa[1], xb[1], R.box, R.l2s, R.periodic),
+                           min_image_sep<real>(xa[2], xb[2], R.box, R.l2s, R.periodic)};
         const real r2 = sep_r2<real>(d[0], d[1], d[2]);
         if (!(r2 < R.rc2)) continue;  // skin lists hold pairs up to the list range
         const real rr = sqrt_r(r2);
-        real fa[3] = {real(0), real(0), real(0)};   // the WCA core; patch terms come from the pair lists' kernels
+        // the WCA core (patch terms come from the pair lists' kernels): FP32 as exact-ish float-float components
+        // summed in fixed point, FP64 in double
+        typename PairAcc<real>::type fa[3] = {0, 0, 0};
         if (rr < R.hs_limit && (a.parts & 1)) {
-            const real s_ = hs_force_over_r<real>(R, r2);
-            big |= fabs(s_ * rr) > real(1e4);
-            fa[0] = s_ * d[0];
-            fa[1] = s_ * d[1];
-            fa[2] = s_ * d[2];
+            if constexpr (sizeof(real) == 4) {
+                float hi[3], lo[3];
+                hs_force_ff(R, d, hi, lo);
+                big |= hi[0] * hi[0] + hi[1] * hi[1] + hi[2] * hi[2] > 1e8f;   // |f| > 1e4
+#pragma unroll
+                for (int k = 0; k < 3; k++) fa[k] = to_fixed(hi[k]) + to_fixed(lo[k]);
+            } else {
+                const real s_ = hs_force_over_r<real>(R, r2);
+                big |= fabs(s_ * rr) > real(1e4);
+                fa[0] = s_ * d[0];
+                fa[1] = s_ * d[1];
+                fa[2] = s_ * d[2];
+            }
         }
         if (BIND) {
             // along d = x_a - x_b: a's cosines are -(n_a . d) / r and b's (n_b . d) / r in either canonical order
@@ -386,8 +407,8 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<re
         }
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            fixed_add(acc + 6 * (size_t)sa + k, fa[k]);
-            fixed_add(acc + 6 * (size_t)sb + k, -fa[k]);
+            acc_add_raw(acc + 6 * (size_t)sa + k, fa[k]);
+            acc_add_raw(acc + 6 * (size_t)sb + k, -fa[k]);
         }
     }
     if (big) atomicOr(a.flags, 2u);
@@ -407,15 +428,15 @@ __global__ void __launch_bounds__(kPipeThreads, 4) patch_pairs_kernel(ForceArgs<
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
         const int2 pr = list_all[seg_slot(segs, cap, q)];
         const int sa = pr.x, sb = pr.y;
-        const int r = a.tb.uniform ? 0 : find_replica(a.tb.rep_slot, a.tb.nrep, sa);
+        const int r = a.tb.uniform ? 0 : replica_of(a.tb, sa);
         const Replica<real> &R = a.tb.reps[r];
         const Model<real> &M = a.tb.models[R.model];
         real xa[4], xb[4];
         load4(a.buf.pos + 4 * (size_t)sa, xa);
         load4(a.buf.pos + 4 * (size_t)sb, xb);
-        const real d[3] = {min_image<real>(xa[0] - xb[0], R.box, R.l2s, R.periodic),
-                           min_image<real>(xa[1] - xb[1], R.box, R.l2s, R.periodic),
-                           min_image<real>(xa[2] - xb[2], R.box, R.l2s, R.periodic)};
+        const real d[3] = {min_image_sep<real>(xa[0], xb[0], R.box, R.l2s, R.periodic),
+                           min_image_sep<real>(xa[1], xb[1], R.box, R.l2s, R.periodic),
+                           min_image_sep<real>(xa[2], xb[2], R.box, R.l2s, R.periodic)};
         const real rr = sqrt_r(sep_r2<real>(d[0], d[1], d[2]));
         const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
         const bool single = M.n_types == 1;
@@ -456,16 +477,16 @@ __global__ void __launch_bounds__(kPipeThreads, 4) bind_pairs_kernel(ForceArgs<f
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
         const int2 pr = list_all[seg_slot(segs, cap, q)];
         const int s1 = pr.x, s2 = pr.y;
-        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, s1);
+        const int r = replica_of(a.tb, s1);
         const Replica<float> &R = a.tb.reps[r];
         const BindRep &B = a.bind_reps[r];
         const Model<float> &M = a.tb.models[R.model];
         float x1[4], x2[4];
         load4(a.buf.pos + 4 * (size_t)s1, x1);
         load4(a.buf.pos + 4 * (size_t)s2, x2);
-        const float d[3] = {min_image<float>(x1[0] - x2[0], R.box, R.l2s, R.periodic),
-                            min_image<float>(x1[1] - x2[1], R.box, R.l2s, R.periodic),
-                            min_image<float>(x1[2] - x2[2], R.box, R.l2s, R.periodic)};
+        const float d[3] = {min_image_sep<float>(x1[0], x2[0], R.box, R.l2s, R.periodic),
+                            min_image_sep<float>(x1[1], x2[1], R.box, R.l2s, R.periodic),
+                            min_image_sep<float>(x1[2], x2[2], R.box, R.l2s, R.periodic)};
         const float r2 = sep_r2(d[0], d[1], d[2]);
         const int t0 = side_of<float>(r2, B.mk2_lo, B.mk2_hi);
         if (t0 > 0) continue;
@@ -523,9 +544,9 @@ __global__ void __launch_bounds__(kPipeThreads) bound_pairs_kernel(ForceArgs<flo
             Payload<float> P1, P2;
             P1.load(a.buf.pos, a.buf.rota, a.buf.rotb, s1);
             P2.load(a.buf.pos, a.buf.rota, a.buf.rotb, s2);
-            const float dx = min_image<float>(P1.v[0] - P2.v[0], R.box, R.l2s, R.periodic);
-            const float dy = min_image<float>(P1.v[1] - P2.v[1], R.box, R.l2s, R.periodic);
-            const float dz = min_image<float>(P1.v[2] - P2.v[2], R.box, R.l2s, R.periodic);
+            const float dx = min_image_sep<float>(P1.v[0], P2.v[0], R.box, R.l2s, R.periodic);
+            const float dy = min_image_sep<float>(P1.v[1], P2.v[1], R.box, R.l2s, R.periodic);
+            const float dz = min_image_sep<float>(P1.v[2], P2.v[2], R.box, R.l2s, R.periodic);
             const float rr = sqrtf(dx * dx + dy * dy + dz * dz);
             const int qp = M.pstart[t1][t2] + k1 * M.np[t2] + k2;
             if (rr > M.rmax[qp]) continue;
@@ -576,12 +597,12 @@ __device__ __forceinline__ void take_sums(double *acc, size_t s, double F[3], do
     as[2] = zero;
 }
 
-template <class real, int MODE>
-__global__ void __launch_bounds__(kPipeThreads) pair_epilogue_kernel(ForceArgs<real> a, typename PairAcc<real>::type *acc) {
+template <class real, int MODE, int THREADS>
+__global__ void __launch_bounds__(THREADS) pair_epilogue_kernel(ForceArgs<real> a, typename PairAcc<real>::type *acc) {
     {
         const int s = blockIdx.x * blockDim.x + threadIdx.x;  // one particle per thread: many loads in flight
         if (s >= a.tb.ntot) return;
-        const int r = find_replica(a.tb.rep_slot, a.tb.nrep, s);
+        const int r = replica_of(a.tb, s);
         const Replica<real> &R = a.tb.reps[r];
         real F[3], T[3];
         take_sums(acc, (size_t)s, F, T);

@@ -218,6 +218,7 @@ struct Sys : SysBase {
     int reps_uniform = 0, reps_obs_uniform = 0;   // see pair_uniform()
     mtg::Model<real> *d_models = nullptr;
     int *d_rep_slot = nullptr;
+    unsigned short *d_slot_rep = nullptr;   // replica of every slot (fewer than 65,536 replicas)
     mtg::Buffers<real> buf[2] = {};
     int cur = 0;
     int2 *d_bin = nullptr;
@@ -241,6 +242,10 @@ struct Sys : SysBase {
     double bond_k = 0, bond_r0 = 0;
     int64_t nlaunch = 0;
     cudaEvent_t *prof_ev = nullptr;  // set by step_profile: events around the pair pipeline's kernels
+    int64_t wait_limit = 0;          // mtg_set_wait_limit: 0 = each bounded loop's own bound
+    // launch shapes of the pair pipeline (mtg_set_launch_config / mtg_autotune); every shape gives the same
+    // FP32 results bit for bit (fixed-point sums), so the tuner may time them on the live state
+    mtg_launch_config lc = {256, 16, 8, 256};
     // FP32 tile kernel
     bool use_tiles = false;
     int4 *d_tiles = nullptr;
@@ -324,6 +329,13 @@ struct Sys : SysBase {
         reps_obs_uniform = pair_uniform(reps_obs);
         MTG_CUDA(cudaMemcpy(d_models, models.data(), sizeof(mtg::Model<real>) * nrep, cudaMemcpyHostToDevice));
         MTG_CUDA(cudaMemcpy(d_rep_slot, rep_slot.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice));
+        if (nrep < 65536) {
+            std::vector<unsigned short> sr((size_t)std::max(ntot_, 1), 0);
+            for (int r = 0; r < nrep; r++)
+                for (int i = rep_slot[r]; i < rep_slot[r + 1]; i++) sr[(size_t)i] = (unsigned short)r;
+            MTG_CUDA(cudaMalloc(&d_slot_rep, sizeof(unsigned short) * sr.size()));
+            MTG_CUDA(cudaMemcpy(d_slot_rep, sr.data(), sizeof(unsigned short) * sr.size(), cudaMemcpyHostToDevice));
+        }
 
         for (int b = 0; b < 2; b++) {
             MTG_CUDA(cudaMalloc(&buf[b].pos, sizeof(real) * 4 * n));
@@ -423,7 +435,7 @@ struct Sys : SysBase {
             cudaFree(buf[b].pos); cudaFree(buf[b].rota); cudaFree(buf[b].rotb); cudaFree(buf[b].motion); cudaFree(buf[b].ident);
             cudaFree(buf[b].dx); cudaFree(buf[b].dy); cudaFree(buf[b].dz);
         }
-        cudaFree(d_reps); cudaFree(d_reps_obs); cudaFree(d_models); cudaFree(d_rep_slot);
+        cudaFree(d_reps); cudaFree(d_reps_obs); cudaFree(d_models); cudaFree(d_rep_slot); cudaFree(d_slot_rep);
         cudaFree(d_bin); cudaFree(d_count); cudaFree(d_start); cudaFree(d_block);
         cudaFree(d_flags); cudaFree(d_draw); cudaFree(d_stage); cudaFree(d_noise); cudaFree(d_obs);
         cudaFree(d_tiles);
@@ -445,6 +457,7 @@ struct Sys : SysBase {
         t.ntot = ntot_;
         t.ncells = obs ? ncells_obs : ncells;
         t.uniform = obs ? reps_obs_uniform : reps_uniform;
+        t.slot_rep = d_slot_rep;
         return t;
     }
 
@@ -883,31 +896,43 @@ struct Sys : SysBase {
             };
             mark(0);
             mtg::pair_reset_kernel<<<1, 64, 0, st>>>(d_npairs, gate, bind ? nullptr : d_patch_ctr);
-            const int gb = (ntot_ + mtg::kPipeThreads - 1) / mtg::kPipeThreads;
-            mtg::pairfind_kernel<real><<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_pairs, d_npairs, pair_cap,
-                                                                                    skin > 0 ? 1 : 0, gate);
+            {
+                const int t = lc.pairfind_threads, gb = std::max(1, (ntot_ + t - 1) / t), rl = skin > 0 ? 1 : 0;
+                if (t == 128)
+                    mtg::pairfind_kernel<real, 128><<<gb, 128, 0, st>>>(a, d_pairs, d_npairs, pair_cap, rl, gate);
+                else if (t == 512)
+                    mtg::pairfind_kernel<real, 512><<<gb, 512, 0, st>>>(a, d_pairs, d_npairs, pair_cap, rl, gate);
+                else
+                    mtg::pairfind_kernel<real, 256><<<gb, 256, 0, st>>>(a, d_pairs, d_npairs, pair_cap, rl, gate);
+            }
             mark(1);
+            const int g_force = sms * lc.pairforce_blocks_per_sm, g_patch = sms * lc.patch_blocks_per_sm;
             bool bind_pass = false;
             if constexpr (std::is_same<real, float>::value) {
                 if (bind) {
                     bind_pass = true;
-                    mtg::pairforce_kernel<float, mtg::kPairBind><<<sms * 16, mtg::kPipeThreads, 0, st>>>(
+                    mtg::pairforce_kernel<float, mtg::kPairBind><<<g_force, mtg::kPipeThreads, 0, st>>>(
                         a, d_pairs, d_npairs, pair_cap, d_acc, d_bind_pairs, lcap);
                     mark(2);
-                    mtg::bind_pairs_kernel<<<sms * 8, mtg::kPipeThreads, 0, st>>>(a, d_bind_pairs, lcap);
+                    mtg::bind_pairs_kernel<<<g_patch, mtg::kPipeThreads, 0, st>>>(a, d_bind_pairs, lcap);
                     decide();
                     mtg::bound_pairs_kernel<<<sms * 4, mtg::kPipeThreads, 0, st>>>(a, d_bound, bcap, d_acc);
                 }
             }
             if (!bind_pass) {
-                mtg::pairforce_kernel<real, mtg::kPairSplit><<<sms * 16, mtg::kPipeThreads, 0, st>>>(
+                mtg::pairforce_kernel<real, mtg::kPairSplit><<<g_force, mtg::kPipeThreads, 0, st>>>(
                     a, d_pairs, d_npairs, pair_cap, d_acc, d_patch_list, patch_cap, d_patch_ctr);
                 mark(2);
-                mtg::patch_pairs_kernel<real><<<sms * 8, mtg::kPipeThreads, 0, st>>>(a, d_patch_list, patch_cap,
+                mtg::patch_pairs_kernel<real><<<g_patch, mtg::kPipeThreads, 0, st>>>(a, d_patch_list, patch_cap,
                                                                                    d_patch_ctr, d_acc);
             }
             mark(3);
-            mtg::pair_epilogue_kernel<real, MODE><<<std::max(gb, 1), mtg::kPipeThreads, 0, st>>>(a, d_acc);
+            {
+                const int t = lc.epilogue_threads, ge = std::max(1, (ntot_ + t - 1) / t);
+                if (t == 128) mtg::pair_epilogue_kernel<real, MODE, 128><<<ge, 128, 0, st>>>(a, d_acc);
+                else if (t == 512) mtg::pair_epilogue_kernel<real, MODE, 512><<<ge, 512, 0, st>>>(a, d_acc);
+                else mtg::pair_epilogue_kernel<real, MODE, 256><<<ge, 256, 0, st>>>(a, d_acc);
+            }
             mark(4);
             counted(bind_pass ? 6 : 5);  // (enqueue_bind_decide counts its own)
             return;
@@ -1663,9 +1688,10 @@ struct Sys : SysBase {
         MTG_CUDA(cudaMalloc(&dl, sizeof(int32_t) * (size_t)n));
         std::unique_ptr<void, void (*)(void *)> g2(dl, [](void *q) { cudaFree(q); });
         const int g = grid_for(n, 256, occ_stream, sms);
+        const int limit = wait_limit > 0 ? (int)std::min<int64_t>(wait_limit, (int64_t)n + 1) : n + 1;
         mtg::uf_init_kernel<<<g, 256, 0, st>>>(n, parent);
-        mtg::uf_hook_kernel<real><<<g, 256, 0, st>>>(c.grid, buf[cur], c.start, c.mem, parent, d_flags);
-        mtg::uf_label_kernel<<<g, 256, 0, st>>>(n, parent, dl, d_flags);
+        mtg::uf_hook_kernel<real><<<g, 256, 0, st>>>(c.grid, buf[cur], c.start, c.mem, parent, d_flags, limit);
+        mtg::uf_label_kernel<<<g, 256, 0, st>>>(n, parent, dl, d_flags, limit);
         check_launch();
         nlaunch += 3;
         MTG_CUDA(cudaMemcpyAsync(labels, dl, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, st));
@@ -1673,6 +1699,79 @@ struct Sys : SysBase {
         if (flags() & MTG_FLAG_TIMEOUT) throw Fail{MTG_ERR_TIMEOUT, "mtg_clusters: a union-find walk exceeded its bound"};
     }
 
+    void set_wait_limit(int64_t v) override { wait_limit = v; }
+
+    static bool valid_threads(int t) { return t == 128 || t == 256 || t == 512; }
+    void get_launch_config(mtg_launch_config *out) const override { *out = lc; }
+    void set_launch_config(const mtg_launch_config *c) override {
+        MTG_REQUIRE(valid_threads(c->pairfind_threads) && valid_threads(c->epilogue_threads),
+                    "mtg_set_launch_config: pairfind_threads and epilogue_threads must be 128, 256 or 512");
+        MTG_REQUIRE(c->pairforce_blocks_per_sm >= 1 && c->pairforce_blocks_per_sm <= 64 &&
+                        c->patch_blocks_per_sm >= 1 && c->patch_blocks_per_sm <= 64,
+                    "mtg_set_launch_config: blocks per SM must lie in [1, 64]");
+        MTG_CUDA(cudaStreamSynchronize(st));
+        lc = *c;
+        drop_graphs();   // the step graphs captured the old shapes
+    }
+
+    // ms per step of `n` graph-replayed steps (one untimed step first captures the graph)
+    double time_steps(int n) {
+        step(1, nullptr);
+        cudaEvent_t e0, e1;
+        MTG_CUDA(cudaEventCreate(&e0));
+        MTG_CUDA(cudaEventCreate(&e1));
+        MTG_CUDA(cudaEventRecord(e0, st));
+        step(n, nullptr);
+        MTG_CUDA(cudaEventRecord(e1, st));
+        MTG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        MTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return (double)ms / n;
+    }
+
+    // Coordinate descent over the pipeline's launch shapes, two sweeps, each candidate timed on `trial` steps
+    // of the live state (the steps advance the simulation like any others); the fastest shape stays set.
+    void autotune(int trial, mtg_launch_config *best, double *best_ms) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_autotune: no state has been set"};
+        MTG_REQUIRE(trial >= 1, "mtg_autotune: steps_per_trial must be >= 1");
+        if (!use_pipe) {   // only the pair pipeline has tunable shapes
+            *best = lc;
+            *best_ms = time_steps(trial);
+            return;
+        }
+        static const int threads[] = {128, 256, 512};
+        static const int force_bps[] = {4, 8, 12, 16, 24, 32};
+        static const int patch_bps[] = {2, 4, 8, 16, 24};
+        mtg_launch_config cur = lc;
+        double cur_ms = time_steps(trial);
+        using Field = int mtg_launch_config::*;
+        auto try_field = [&](Field f, const int *vals, int nv) {
+            const int first = cur.*f;
+            for (int i = 0; i < nv; i++) {
+                if (vals[i] == first) continue;
+                mtg_launch_config c = cur;
+                c.*f = vals[i];
+                set_launch_config(&c);
+                const double ms = time_steps(trial);
+                if (ms < cur_ms) {
+                    cur_ms = ms;
+                    cur.*f = vals[i];
+                }
+            }
+            set_launch_config(&cur);
+        };
+        for (int sweep = 0; sweep < 2; sweep++) {
+            try_field(&mtg_launch_config::pairforce_blocks_per_sm, force_bps, 6);
+            try_field(&mtg_launch_config::patch_blocks_per_sm, patch_bps, 5);
+            try_field(&mtg_launch_config::pairfind_threads, threads, 3);
+            try_field(&mtg_launch_config::epilogue_threads, threads, 3);
+        }
+        set_launch_config(&cur);
+        *best = cur;
+        *best_ms = time_steps(trial);   // the chosen shape, timed once more
+    }
     void set_draw(uint64_t d) override { draw = d; }
     uint64_t get_draw() const override { return draw; }
 

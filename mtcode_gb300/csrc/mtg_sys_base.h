@@ -66,6 +66,10 @@ struct SysBase {
     virtual void phase_halfkick(const double *, const double *) = 0;
     virtual void phase_drift() = 0;
     virtual void phase_rotate() = 0;
+    virtual void set_wait_limit(int64_t) = 0;
+    virtual void get_launch_config(mtg_launch_config *) const = 0;
+    virtual void set_launch_config(const mtg_launch_config *) = 0;
+    virtual void autotune(int, mtg_launch_config *, double *) = 0;
 };
 
 

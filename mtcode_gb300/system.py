@@ -311,6 +311,29 @@ class LangevinNVTRGPU:
     def rotate(self) -> None:
         _check(self._h, _lib.lib().mtg_rotate(self._h))
 
+    @property
+    def launch_config(self) -> dict:
+        """The pair pipeline's launch shapes (mtg_get_launch_config)."""
+        c = _lib.LaunchConfig()
+        _check(self._h, _lib.lib().mtg_get_launch_config(self._h, C.byref(c)))
+        return c.as_dict()
+
+    @launch_config.setter
+    def launch_config(self, cfg: dict) -> None:
+        c = _lib.LaunchConfig(**{k: int(v) for k, v in cfg.items()})
+        _check(self._h, _lib.lib().mtg_set_launch_config(self._h, C.byref(c)))
+
+    def autotune(self, steps_per_trial: int = 5) -> tuple:
+        """mtg_autotune: returns (chosen launch shapes, ms per step with them); the trials advance the state."""
+        c = _lib.LaunchConfig()
+        ms = C.c_double()
+        _check(self._h, _lib.lib().mtg_autotune(self._h, int(steps_per_trial), C.byref(c), C.byref(ms)))
+        return c.as_dict(), float(ms.value)
+
+    def set_wait_limit(self, limit: int) -> None:
+        """Bound (iterations) on mtg_clusters' waiting loops; 0 restores their own bound."""
+        _check(self._h, _lib.lib().mtg_set_wait_limit(self._h, int(limit)))
+
     def calculatepairs_parallel(self, rc: float, replica: int = 0) -> np.ndarray:
         """MD::calculatepairs_parallel: sorted (i < j) pairs of one replica within rc."""
         L = _lib.lib()
