@@ -45,7 +45,7 @@ class PatchModel(C.Structure):
 
 class LaunchConfig(C.Structure):
     _fields_ = [("pairfind_threads", C.c_int), ("pairforce_blocks_per_sm", C.c_int),
-                ("patch_blocks_per_sm", C.c_int), ("epilogue_threads", C.c_int)]
+                ("patch_blocks_per_sm", C.c_int), ("epilogue_threads", C.c_int), ("fused_pairs", C.c_int)]
 
     def as_dict(self) -> dict:
         return {name: int(getattr(self, name)) for name, _ in self._fields_}

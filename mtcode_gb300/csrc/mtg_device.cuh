@@ -33,6 +33,7 @@ struct Replica {
     int model;        // index into the model table
     uint32_t seed_lo, seed_hi;
     real box, half_box, l2s;   // cube::l, l/2, (l/2)^2
+    real box_lo;               // FP32: l - (float)l, the part of the double box length a float drops (0 in FP64)
     real cell_scale;           // nc / box  (cube::assign_box: n * x / l)
     real dt, half_dt, c1;      // dt, dt/2, dt/m
     real fric_t, fric_r;       // -gamma/m, -gammar/I
@@ -219,14 +220,16 @@ __device__ __forceinline__ real min_image(real dx, real l, real l2s, int periodi
 }
 
 // The minimum-image separation x_a - x_b by the same rule.  FP64 forms it as the reference does, (x_a - x_b) -+ l.
-// FP32 forms the corrected separation as (x_a - l) - x_b or x_a - (x_b - l): the coordinate next to the far face
-// lies in [l/2, l], so its difference with l is exact (Sterbenz), and the separation carries one rounding of its
-// own size -- (x_a - x_b) -+ l would carry one of the box length's (4e-6 at l = 130, 3e-6 relative at r = 1.5).
+// FP32 forms the corrected separation as ((x_a - l) - x_b) - l_lo or (x_a - (x_b - l)) + l_lo, l + l_lo being
+// the double box length: the coordinate next to the far face lies in [l/2, l], so its difference with l is exact
+// (Sterbenz), and the separation carries one rounding of its own size and the box length to double precision --
+// (x_a - x_b) -+ (float)l would carry a rounding of the box length's size and the float box's own error (each up
+// to 4e-6 at l = 130: 3e-6 relative at r = 1.5, 4e-5 in a WCA force).
 template <class real>
-__device__ __forceinline__ real min_image_sep(real xa, real xb, real l, real l2s, int periodic) {
+__device__ __forceinline__ real min_image_sep(real xa, real xb, real l, real l_lo, real l2s, int periodic) {
     real dx = xa - xb;
     if (periodic && dx * dx > l2s) {
-        if constexpr (sizeof(real) == 4) dx = dx >= real(0) ? (xa - l) - xb : xa - (xb - l);
+        if constexpr (sizeof(real) == 4) dx = dx >= real(0) ? ((xa - l) - xb) - l_lo : (xa - (xb - l)) + l_lo;
         else dx = dx >= real(0) ? dx - l : dx + l;
     }
     return dx;
@@ -234,8 +237,9 @@ __device__ __forceinline__ real min_image_sep(real xa, real xb, real l, real l2s
 // x_a - x_b for a partner reached across a periodic face with image shift sh (+l, -l or 0), in the arithmetic of
 // min_image_sep (both give the same bits for the same pair)
 template <class real>
-__device__ __forceinline__ real shifted_sep(real xa, real xb, real sh) {
-    if constexpr (sizeof(real) == 4) return sh > real(0) ? (xa - sh) - xb : (sh < real(0) ? xa - (xb + sh) : xa - xb);
+__device__ __forceinline__ real shifted_sep(real xa, real xb, real sh, real l_lo) {
+    if constexpr (sizeof(real) == 4)
+        return sh > real(0) ? ((xa - sh) - xb) - l_lo : (sh < real(0) ? (xa - (xb + sh)) + l_lo : xa - xb);
     else return (xa - xb) - sh;
 }
 

@@ -654,9 +654,9 @@ __device__ __forceinline__ bool candidate(const BindRep &B, const Replica<real> 
     Payload<real> A, C;
     A.load(sa, sb, sc, s1);
     C.load(sa, sb, sc, s2);
-    const real dx = min_image_sep<real>(A.v[0], C.v[0], R.box, R.l2s, R.periodic);
-    const real dy = min_image_sep<real>(A.v[1], C.v[1], R.box, R.l2s, R.periodic);
-    const real dz = min_image_sep<real>(A.v[2], C.v[2], R.box, R.l2s, R.periodic);
+    const real dx = min_image_sep<real>(A.v[0], C.v[0], R.box, R.box_lo, R.l2s, R.periodic);
+    const real dy = min_image_sep<real>(A.v[1], C.v[1], R.box, R.box_lo, R.l2s, R.periodic);
+    const real dz = min_image_sep<real>(A.v[2], C.v[2], R.box, R.box_lo, R.l2s, R.periodic);
     const real r2 = dx * dx + dy * dy + dz * dz;
     const int t = side_of<real>(r2, B.memb2_lo, B.memb2_hi);
     if (t > 0) return false;
@@ -820,9 +820,9 @@ template <class real>
 __device__ __forceinline__ void skin_check(const ForceArgs<real> &a, const Replica<real> &R, int s, const real xn[3]) {
     real xr, yr, zr;
     load_pos(a.buf.xref + 4 * (size_t)s, xr, yr, zr);
-    const real dx = min_image_sep<real>(xn[0], xr, R.box, R.l2s, R.periodic);
-    const real dy = min_image_sep<real>(xn[1], yr, R.box, R.l2s, R.periodic);
-    const real dz = min_image_sep<real>(xn[2], zr, R.box, R.l2s, R.periodic);
+    const real dx = min_image_sep<real>(xn[0], xr, R.box, R.box_lo, R.l2s, R.periodic);
+    const real dy = min_image_sep<real>(xn[1], yr, R.box, R.box_lo, R.l2s, R.periodic);
+    const real dz = min_image_sep<real>(xn[2], zr, R.box, R.box_lo, R.l2s, R.periodic);
     if (!(dx * dx + dy * dy + dz * dz <= R.half_skin2)) *a.skin_next = 1;
 }
 
@@ -839,9 +839,9 @@ __device__ __forceinline__ void bond_forces(const ForceArgs<real> &a, const Repl
         const int j = __ldg(a.buf.slot_of + __ldg(a.bond_partner + b));
         real xj, yj, zj;
         load_pos(a.buf.pos + 4 * (size_t)j, xj, yj, zj);
-        const real dx = min_image_sep<real>(xi, xj, R.box, R.l2s, R.periodic);
-        const real dy = min_image_sep<real>(yi, yj, R.box, R.l2s, R.periodic);
-        const real dz = min_image_sep<real>(zi, zj, R.box, R.l2s, R.periodic);
+        const real dx = min_image_sep<real>(xi, xj, R.box, R.box_lo, R.l2s, R.periodic);
+        const real dy = min_image_sep<real>(yi, yj, R.box, R.box_lo, R.l2s, R.periodic);
+        const real dz = min_image_sep<real>(zi, zj, R.box, R.box_lo, R.l2s, R.periodic);
         const real r = sqrt(dx * dx + dy * dy + dz * dz);
         const real f1 = -a.bond_k * (r - a.bond_r0);
         big |= fabs(f1) > real(1e4);
@@ -875,9 +875,9 @@ __device__ __forceinline__ void bound_patch_forces(const ForceArgs<real> &a, con
         const bool i_first = li < lj;
         const real *P1 = i_first ? Pi : Pj.v, *P2 = i_first ? Pj.v : Pi;
         const int t1 = i_first ? ti : tj, t2 = i_first ? tj : ti, c1 = i_first ? ka : kb, c2 = i_first ? kb : ka;
-        const real dx = min_image_sep<real>(P1[0], P2[0], R.box, R.l2s, R.periodic);
-        const real dy = min_image_sep<real>(P1[1], P2[1], R.box, R.l2s, R.periodic);
-        const real dz = min_image_sep<real>(P1[2], P2[2], R.box, R.l2s, R.periodic);
+        const real dx = min_image_sep<real>(P1[0], P2[0], R.box, R.box_lo, R.l2s, R.periodic);
+        const real dy = min_image_sep<real>(P1[1], P2[1], R.box, R.box_lo, R.l2s, R.periodic);
+        const real dz = min_image_sep<real>(P1[2], P2[2], R.box, R.box_lo, R.l2s, R.periodic);
         const real rr = sqrt(dx * dx + dy * dy + dz * dz);
         const int q = M.pstart[t1][t2] + c1 * M.np[t2] + c2;
         if (rr > M.rmax[q]) continue;   // interaction_distance (potentialtheta.h:522)
@@ -997,9 +997,9 @@ __device__ __noinline__ void simple_particle(const ForceArgs<real> &a, int s) {
                         if (j == s) continue;
                         real xj, yj, zj;
                         load_pos(a.buf.pos + 4 * (size_t)j, xj, yj, zj);
-                        real dx = min_image_sep<real>(xi, xj, R.box, R.l2s, R.periodic);
-                        real dy2 = min_image_sep<real>(yi, yj, R.box, R.l2s, R.periodic);
-                        real dz2 = min_image_sep<real>(zi, zj, R.box, R.l2s, R.periodic);
+                        real dx = min_image_sep<real>(xi, xj, R.box, R.box_lo, R.l2s, R.periodic);
+                        real dy2 = min_image_sep<real>(yi, yj, R.box, R.box_lo, R.l2s, R.periodic);
+                        real dz2 = min_image_sep<real>(zi, zj, R.box, R.box_lo, R.l2s, R.periodic);
                         real r2 = dx * dx + dy2 * dy2 + dz2 * dz2;
                         if (!(r2 < range2)) continue;
                         if (MODE == kModeEdges) {   // single-bond mode: this update's edges, each pair once

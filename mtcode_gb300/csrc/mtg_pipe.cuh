@@ -86,20 +86,237 @@ __device__ __forceinline__ void warp_pair_flush(int2 *buf, int buf_cap, int *nb,
     }
 }
 
+// the pair list's length (on list-building steps) and the patch list's segment counters (every pass)
+__global__ void pair_reset_kernel(unsigned long long *npairs, const int *gate, unsigned long long *patch_counts) {
+    if (patch_counts && blockIdx.x == 0)
+        for (int k = threadIdx.x; k < kSegs; k += blockDim.x) patch_counts[k] = 0ull;
+    if (gated_off(gate, 1)) return;
+    if (threadIdx.x == 0 && blockIdx.x == 0) *npairs = 0ull;
+}
+
+// Pairs a pair kernel lists go through a per-block staging buffer in shared memory (a shared-memory
+// atomic per appending warp) and reach their segmented list with one global atomic per block at the end
+// (segment blockIdx mod kSegs); entries past the buffer go straight to the list.
+constexpr int kBlockListCap = 1024;
+
+__device__ __forceinline__ void block_list_put(int2 *sbuf, int *sn, int2 e, int2 *list, unsigned long long *counts,
+                                               long long cap, unsigned *flags, unsigned full_flag) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    int q = 0;
+    if (g.thread_rank() == 0) q = atomicAdd(sn, (int)g.size());
+    q = g.shfl(q, 0) + (int)g.thread_rank();
+    if (q < kBlockListCap) sbuf[q] = e;
+    else seg_append<int2>(list, counts, cap, e, flags, full_flag);
+}
+
+// all threads of the block
+__device__ __forceinline__ void block_list_flush(const int2 *sbuf, const int *sn, unsigned long long *sbase,
+                                                 int2 *list, unsigned long long *counts, long long cap,
+                                                 unsigned *flags, unsigned full_flag) {
+    __syncthreads();
+    const int n = *sn < kBlockListCap ? *sn : kBlockListCap;
+    const int k = (int)(blockIdx.x & (kSegs - 1));
+    if (threadIdx.x == 0) *sbase = n ? atomicAdd(counts + k, (unsigned long long)n) : 0ull;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const unsigned long long w = *sbase + (unsigned long long)i;
+        if ((long long)w < cap) list[(size_t)k * (size_t)cap + w] = sbuf[i];
+        else atomicOr(flags, full_flag);
+    }
+}
+
+__device__ __forceinline__ void fixed_add(long long *acc, float v) {
+    if (v != 0.f) atomicAdd(reinterpret_cast<unsigned long long *>(acc), (unsigned long long)to_fixed(v));
+}
+__device__ __forceinline__ void fixed_add(double *acc, double v) {
+    if (v != 0.0) atomicAdd(acc, v);
+}
+// a term already in the sum's representation (FP32: fixed point; FP64: double)
+__device__ __forceinline__ void acc_add_raw(long long *acc, long long v) {
+    if (v != 0) atomicAdd(reinterpret_cast<unsigned long long *>(acc), (unsigned long long)v);
+}
+__device__ __forceinline__ void acc_add_raw(double *acc, double v) {
+    if (v != 0.0) atomicAdd(acc, v);
+}
+
+// Forces and torques of the listed pairs into acc (6 fixed-point sums per slot: F lab, T lab).
+// KIND kPairSplit: WCA core here; pairs where both particles have a patch near a cone go to `list` for
+//   patch_pairs_kernel, which evaluates their patch terms with every lane busy (the rest of the pairs
+//   never reach the patch code, so this kernel runs without the divergent, register-heavy branch).
+// KIND kPairBind (single-bond mode, a bond-deciding pass): WCA core here; pairs where both particles have
+//   a patch near a cone go, in canonical order (lower particle index first), to `list` for
+//   bind_pairs_kernel.
+enum PairKind : int { kPairBind = 1, kPairSplit = 2 };
+
+// One listed pair (sa, sb): the WCA core into acc (both particles), and -- KIND kPairSplit -- the pair onto
+// `list` when both particles have a patch near a cone, or -- KIND kPairBind -- onto `list` in canonical order
+// when both do (single-bond mode).  List entries are staged in the block's lbuf (block_list_put).
+template <class real, int KIND>
+__device__ __forceinline__ void pair_core(const ForceArgs<real> &a, int sa, int sb, typename PairAcc<real>::type *acc,
+                                          int2 *lbuf, int *lnb, int2 *list, long long list_cap,
+                                          unsigned long long *lcounts, unsigned lflag, bool &big) {
+    constexpr bool BIND = KIND == kPairBind;
+    const int r = a.tb.uniform ? 0 : replica_of(a.tb, sa);
+    const Replica<real> &R = a.tb.reps[r];
+    real xa[4], xb[4];
+    load4(a.buf.pos + 4 * (size_t)sa, xa);
+    load4(a.buf.pos + 4 * (size_t)sb, xb);
+    const real d[3] = {min_image_sep<real>(xa[0], xb[0], R.box, R.box_lo, R.l2s, R.periodic),
+                       min_image_sep<real>(xa[1], xb[1], R.box, R.box_lo, R.l2s, R.periodic),
+                       min_image_sep<real>(xa[2], xb[2], R.box, R.box_lo, R.l2s, R.periodic)};
+    const real r2 = sep_r2<real>(d[0], d[1], d[2]);
+    if (!(r2 < R.rc2)) return;  // skin lists hold pairs up to the list range
+    const real rr = sqrt_r(r2);
+    // the WCA core (patch terms come from the pair lists' kernels): FP32 as exact-ish float-float components
+    // summed in fixed point, FP64 in double
+    typename PairAcc<real>::type fa[3] = {0, 0, 0};
+    if (rr < R.hs_limit && (a.parts & 1)) {
+        if constexpr (sizeof(real) == 4) {
+            float hi[3], lo[3];
+            hs_force_ff(R, d, hi, lo);
+            big |= hi[0] * hi[0] + hi[1] * hi[1] + hi[2] * hi[2] > 1e8f;   // |f| > 1e4
+#pragma unroll
+            for (int k = 0; k < 3; k++) fa[k] = to_fixed(hi[k]) + to_fixed(lo[k]);
+        } else {
+            const real s_ = hs_force_over_r<real>(R, r2);
+            big |= fabs(s_ * rr) > real(1e4);
+            fa[0] = s_ * d[0];
+            fa[1] = s_ * d[1];
+            fa[2] = s_ * d[2];
+        }
+    }
+    if (BIND) {
+        // along d = x_a - x_b: a's cosines are -(n_a . d) / r and b's (n_b . d) / r in either canonical order
+        const Model<real> &M = a.tb.models[R.model];
+        const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
+        const bool single = M.n_types == 1;
+        const int tya = single ? 0 : type_of<real>(M, ida - R.off), tyb = single ? 0 : type_of<real>(M, idb - R.off);
+        if (M.np[tya] > 0 && M.np[tyb] > 0) {
+            const real inv = real(1) / sqrt_r(r2), pre = M.mincos[tya][tyb] - real(4e-5);
+            real Q[9], w[3];
+            load_q(a, sa, xa[3], Q);
+#pragma unroll
+            for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
+            bool any = false;
+            for (int k = 0; k < M.np[tya]; k++) {
+                const real *v = M.orient[M.ooff[tya] + k];
+                any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > pre;
+            }
+            if (any) {
+                load_q(a, sb, xb[3], Q);
+#pragma unroll
+                for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
+                bool anyb = false;
+                for (int k = 0; k < M.np[tyb]; k++) {
+                    const real *v = M.orient[M.ooff[tyb] + k];
+                    anyb |= v[0] * w[0] + v[1] * w[1] + v[2] * w[2] > pre;
+                }
+                if (anyb)
+                    block_list_put(lbuf, lnb, ida < idb ? make_int2(sa, sb) : make_int2(sb, sa), list, lcounts,
+                                   list_cap, a.flags, lflag);
+            }
+        }
+    }
+    if (KIND == kPairSplit && (a.parts & 2) && r2 < R.patch_r2) {
+        // the one-sided tests of both particles along d = x_a - x_b (with the 1e-5 margin of the full
+        // kernel's own early test): a's cosines -(n . Qa d) / r, b's (n . Qb d) / r
+        const Model<real> &M = a.tb.models[R.model];
+        const int ida = __ldg(a.buf.ident + sa);
+        const int tya = M.n_types == 1 ? 0 : type_of<real>(M, ida - R.off);
+        if (M.np[tya] > 0) {
+            const real inv = real(1) / sqrt_r(r2);
+            real Q[9], w[3];
+            load_q(a, sa, xa[3], Q);
+#pragma unroll
+            for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
+            const real mca = M.mincos_any[tya] - real(1e-5);
+            bool any = false;
+            for (int k = 0; k < M.np[tya]; k++) {
+                const real *v = M.orient[M.ooff[tya] + k];
+                any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > mca;
+            }
+            if (any) {
+                const int idb = __ldg(a.buf.ident + sb);
+                const int tyb = M.n_types == 1 ? 0 : type_of<real>(M, idb - R.off);
+                if (M.np[tyb] > 0) {
+                    load_q(a, sb, xb[3], Q);
+#pragma unroll
+                    for (int k = 0; k < 3; k++)
+                        w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
+                    const real mcb = M.mincos_any[tyb] - real(1e-5);
+                    bool anyb = false;
+                    for (int k = 0; k < M.np[tyb]; k++) {
+                        const real *v = M.orient[M.ooff[tyb] + k];
+                        anyb |= v[0] * w[0] + v[1] * w[1] + v[2] * w[2] > mcb;
+                    }
+                    if (anyb) block_list_put(lbuf, lnb, make_int2(sa, sb), list, lcounts, list_cap, a.flags, lflag);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        acc_add_raw(acc + 6 * (size_t)sa + k, fa[k]);
+        acc_add_raw(acc + 6 * (size_t)sb + k, -fa[k]);
+    }
+}
+
+template <class real, int KIND>
+__global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<real> a, const int2 *pairs,
+                                                                 const unsigned long long *npairs, long long cap,
+                                                                 typename PairAcc<real>::type *acc,
+                                                                 int2 *list = nullptr, long long list_cap = 0,
+                                                                 unsigned long long *list_counts = nullptr) {
+    constexpr bool BIND = KIND == kPairBind;
+    __shared__ int2 lbuf[kBlockListCap];
+    __shared__ int lnb;
+    __shared__ unsigned long long lbase;
+    if (threadIdx.x == 0) lnb = 0;
+    __syncthreads();
+    unsigned long long *const lcounts = BIND ? a.bind_ctr + kSegPairs : list_counts;
+    const unsigned lflag = BIND ? (kFlagBind | kBindWhyList) : 8u;
+    const long long n = (long long)*npairs < cap ? (long long)*npairs : cap;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    bool big = false;
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int2 next = q < n ? __ldcs(pairs + q) : make_int2(0, 0);
+    for (; q < n; q += stride) {
+        const int2 pr = next;  // the next iteration's entry is loaded one iteration ahead
+        if (q + stride < n) next = __ldcs(pairs + q + stride);
+        pair_core<real, KIND>(a, pr.x, pr.y, acc, lbuf, &lnb, list, list_cap, lcounts, lflag, big);
+    }
+    if (big) atomicOr(a.flags, 2u);
+    block_list_flush(lbuf, &lnb, &lbase, list, lcounts, list_cap, a.flags, lflag);
+}
+
 // range_list: use the replica's list range (skin lists) instead of its force range.
 // Each lane scans its particle's candidate segments in chunks of at most 32 slots and marks the hits of a
 // chunk in a bit mask; the warp then appends the marked pairs together (warp_pair_flush), so the candidate
 // loop itself carries no appends.  The chunk and segment loops are warp-uniform.
-template <class real, int THREADS>
+//
+// FUSED (no list reuse: every step rebuilds): the block's pairs do not go to the list at all.  After the scan
+// the whole block takes the buffered pairs, several per thread with every lane busy, through pair_core (WCA core,
+// cone pre-test, patch list) while their positions are still in L1; only pairs beyond the block buffer reach the
+// HBM list, for pairforce_kernel.
+template <class real, int THREADS, bool FUSED>
 __global__ void __launch_bounds__(THREADS) pairfind_kernel(ForceArgs<real> a, int2 *pairs,
                                                            unsigned long long *npairs, long long cap,
-                                                           int range_list, const int *gate) {
+                                                           int range_list, const int *gate,
+                                                           typename PairAcc<real>::type *acc = nullptr,
+                                                           int2 *list = nullptr, long long list_cap = 0,
+                                                           unsigned long long *list_counts = nullptr) {
     if (gated_off(gate, 1)) return;
     constexpr int kBufCap = kPairsPerThread * THREADS;
+    constexpr int kLBuf = FUSED ? kBlockListCap : 1;
     __shared__ int2 buf[kBufCap];
-    __shared__ int nb;
-    __shared__ unsigned long long base;
-    if (threadIdx.x == 0) nb = 0;
+    __shared__ int2 lbuf[kLBuf];
+    __shared__ int nb, lnb;
+    __shared__ unsigned long long base, lbase;
+    if (threadIdx.x == 0) {
+        nb = 0;
+        lnb = 0;
+    }
     __syncthreads();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = s < a.tb.ntot;
@@ -192,8 +409,9 @@ __global__ void __launch_bounds__(THREADS) pairfind_kernel(ForceArgs<real> a, in
                     for (int t = c0; t < ce; t++) {
                         real pj[3];
                         load_pos(a.buf.pos + 4 * (size_t)t, pj[0], pj[1], pj[2]);
-                        const real dx = shifted_sep<real>(pi[0], pj[0], shx), dy2 = shifted_sep<real>(pi[1], pj[1], shy),
-                                   dz2 = shifted_sep<real>(pi[2], pj[2], shz);
+                        const real dx = shifted_sep<real>(pi[0], pj[0], shx, R.box_lo),
+                                   dy2 = shifted_sep<real>(pi[1], pj[1], shy, R.box_lo),
+                                   dz2 = shifted_sep<real>(pi[2], pj[2], shz, R.box_lo);
                         if (sep_r2<real>(dx, dy2, dz2) < range2) mask |= 1u << (t - c0);
                     }
                 } else {  // tiny grids: no cell geometry to lean on
@@ -201,9 +419,9 @@ __global__ void __launch_bounds__(THREADS) pairfind_kernel(ForceArgs<real> a, in
                     for (int t = c0; t < ce; t++) {
                         real pj[3];
                         load_pos(a.buf.pos + 4 * (size_t)t, pj[0], pj[1], pj[2]);
-                        const real dx = min_image_sep<real>(pi[0], pj[0], R.box, R.l2s, R.periodic);
-                        const real dy2 = min_image_sep<real>(pi[1], pj[1], R.box, R.l2s, R.periodic);
-                        const real dz2 = min_image_sep<real>(pi[2], pj[2], R.box, R.l2s, R.periodic);
+                        const real dx = min_image_sep<real>(pi[0], pj[0], R.box, R.box_lo, R.l2s, R.periodic);
+                        const real dy2 = min_image_sep<real>(pi[1], pj[1], R.box, R.box_lo, R.l2s, R.periodic);
+                        const real dz2 = min_image_sep<real>(pi[2], pj[2], R.box, R.box_lo, R.l2s, R.periodic);
                         if (sep_r2<real>(dx, dy2, dz2) < range2) mask |= 1u << (t - c0);
                     }
                 }
@@ -213,206 +431,20 @@ __global__ void __launch_bounds__(THREADS) pairfind_kernel(ForceArgs<real> a, in
     }
     __syncthreads();
     const int n = nb < kBufCap ? nb : kBufCap;
+    if constexpr (FUSED) {
+        bool big = false;
+        for (int i = threadIdx.x; i < n; i += THREADS)
+            pair_core<real, kPairSplit>(a, buf[i].x, buf[i].y, acc, lbuf, &lnb, list, list_cap, list_counts, 8u, big);
+        if (big) atomicOr(a.flags, 2u);
+        block_list_flush(lbuf, &lnb, &lbase, list, list_counts, list_cap, a.flags, 8u);
+        return;
+    }
     if (threadIdx.x == 0) base = n ? atomicAdd(npairs, (unsigned long long)n) : 0ull;
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         if ((long long)(base + i) < cap) pairs[base + i] = buf[i];
         else atomicOr(a.flags, 8u);
     }
-}
-
-// the pair list's length (on list-building steps) and the patch list's segment counters (every pass)
-__global__ void pair_reset_kernel(unsigned long long *npairs, const int *gate, unsigned long long *patch_counts) {
-    if (patch_counts && blockIdx.x == 0)
-        for (int k = threadIdx.x; k < kSegs; k += blockDim.x) patch_counts[k] = 0ull;
-    if (gated_off(gate, 1)) return;
-    if (threadIdx.x == 0 && blockIdx.x == 0) *npairs = 0ull;
-}
-
-// Pairs a pair kernel lists go through a per-block staging buffer in shared memory (a shared-memory
-// atomic per appending warp) and reach their segmented list with one global atomic per block at the end
-// (segment blockIdx mod kSegs); entries past the buffer go straight to the list.
-constexpr int kBlockListCap = 1024;
-
-__device__ __forceinline__ void block_list_put(int2 *sbuf, int *sn, int2 e, int2 *list, unsigned long long *counts,
-                                               long long cap, unsigned *flags, unsigned full_flag) {
-    namespace cg = cooperative_groups;
-    cg::coalesced_group g = cg::coalesced_threads();
-    int q = 0;
-    if (g.thread_rank() == 0) q = atomicAdd(sn, (int)g.size());
-    q = g.shfl(q, 0) + (int)g.thread_rank();
-    if (q < kBlockListCap) sbuf[q] = e;
-    else seg_append<int2>(list, counts, cap, e, flags, full_flag);
-}
-
-// all threads of the block
-__device__ __forceinline__ void block_list_flush(const int2 *sbuf, const int *sn, unsigned long long *sbase,
-                                                 int2 *list, unsigned long long *counts, long long cap,
-                                                 unsigned *flags, unsigned full_flag) {
-    __syncthreads();
-    const int n = *sn < kBlockListCap ? *sn : kBlockListCap;
-    const int k = (int)(blockIdx.x & (kSegs - 1));
-    if (threadIdx.x == 0) *sbase = n ? atomicAdd(counts + k, (unsigned long long)n) : 0ull;
-    __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const unsigned long long w = *sbase + (unsigned long long)i;
-        if ((long long)w < cap) list[(size_t)k * (size_t)cap + w] = sbuf[i];
-        else atomicOr(flags, full_flag);
-    }
-}
-
-__device__ __forceinline__ void fixed_add(long long *acc, float v) {
-    if (v != 0.f) atomicAdd(reinterpret_cast<unsigned long long *>(acc), (unsigned long long)to_fixed(v));
-}
-__device__ __forceinline__ void fixed_add(double *acc, double v) {
-    if (v != 0.0) atomicAdd(acc, v);
-}
-// a term already in the sum's representation (FP32: fixed point; FP64: double)
-__device__ __forceinline__ void acc_add_raw(long long *acc, long long v) {
-    if (v != 0) atomicAdd(reinterpret_cast<unsigned long long *>(acc), (unsigned long long)v);
-}
-__device__ __forceinline__ void acc_add_raw(double *acc, double v) {
-    if (v != 0.0) atomicAdd(acc, v);
-}
-
-// Forces and torques of the listed pairs into acc (6 fixed-point sums per slot: F lab, T lab).
-// KIND kPairSplit: WCA core here; pairs where both particles have a patch near a cone go to `list` for
-//   patch_pairs_kernel, which evaluates their patch terms with every lane busy (the rest of the pairs
-//   never reach the patch code, so this kernel runs without the divergent, register-heavy branch).
-// KIND kPairBind (single-bond mode, a bond-deciding pass): WCA core here; pairs where both particles have
-//   a patch near a cone go, in canonical order (lower particle index first), to `list` for
-//   bind_pairs_kernel.
-enum PairKind : int { kPairBind = 1, kPairSplit = 2 };
-
-template <class real, int KIND>
-__global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<real> a, const int2 *pairs,
-                                                                 const unsigned long long *npairs, long long cap,
-                                                                 typename PairAcc<real>::type *acc,
-                                                                 int2 *list = nullptr, long long list_cap = 0,
-                                                                 unsigned long long *list_counts = nullptr) {
-    constexpr bool BIND = KIND == kPairBind;
-    __shared__ int2 lbuf[kBlockListCap];
-    __shared__ int lnb;
-    __shared__ unsigned long long lbase;
-    if (threadIdx.x == 0) lnb = 0;
-    __syncthreads();
-    unsigned long long *const lcounts = BIND ? a.bind_ctr + kSegPairs : list_counts;
-    const unsigned lflag = BIND ? (kFlagBind | kBindWhyList) : 8u;
-    const long long n = (long long)*npairs < cap ? (long long)*npairs : cap;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    bool big = false;
-    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int2 next = q < n ? __ldcs(pairs + q) : make_int2(0, 0);
-    for (; q < n; q += stride) {
-        const int2 pr = next;  // the next iteration's entry is loaded one iteration ahead
-        if (q + stride < n) next = __ldcs(pairs + q + stride);
-        const int sa = pr.x, sb = pr.y;
-        const int r = a.tb.uniform ? 0 : replica_of(a.tb, sa);
-        const Replica<real> &R = a.tb.reps[r];
-        real xa[4], xb[4];
-        load4(a.buf.pos + 4 * (size_t)sa, xa);
-        load4(a.buf.pos + 4 * (size_t)sb, xb);
-        const real d[3] = {min_image_sep<real>(xa[0], xb[0], R.box, R.l2s, R.periodic),
-                           min_image_sep<real>(xa[1], xb[1], R.box, R.l2s, R.periodic),
-                           min_image_sep<real>(xa[2], xb[2], R.box, R.l2s, R.periodic)};
-        const real r2 = sep_r2<real>(d[0], d[1], d[2]);
-        if (!(r2 < R.rc2)) continue;  // skin lists hold pairs up to the list range
-        const real rr = sqrt_r(r2);
-        // the WCA core (patch terms come from the pair lists' kernels): FP32 as exact-ish float-float components
-        // summed in fixed point, FP64 in double
-        typename PairAcc<real>::type fa[3] = {0, 0, 0};
-        if (rr < R.hs_limit && (a.parts & 1)) {
-            if constexpr (sizeof(real) == 4) {
-                float hi[3], lo[3];
-                hs_force_ff(R, d, hi, lo);
-                big |= hi[0] * hi[0] + hi[1] * hi[1] + hi[2] * hi[2] > 1e8f;   // |f| > 1e4
-#pragma unroll
-                for (int k = 0; k < 3; k++) fa[k] = to_fixed(hi[k]) + to_fixed(lo[k]);
-            } else {
-                const real s_ = hs_force_over_r<real>(R, r2);
-                big |= fabs(s_ * rr) > real(1e4);
-                fa[0] = s_ * d[0];
-                fa[1] = s_ * d[1];
-                fa[2] = s_ * d[2];
-            }
-        }
-        if (BIND) {
-            // along d = x_a - x_b: a's cosines are -(n_a . d) / r and b's (n_b . d) / r in either canonical order
-            const Model<real> &M = a.tb.models[R.model];
-            const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
-            const bool single = M.n_types == 1;
-            const int tya = single ? 0 : type_of<real>(M, ida - R.off), tyb = single ? 0 : type_of<real>(M, idb - R.off);
-            if (M.np[tya] > 0 && M.np[tyb] > 0) {
-                const real inv = real(1) / sqrt_r(r2), pre = M.mincos[tya][tyb] - real(4e-5);
-                real Q[9], w[3];
-                load_q(a, sa, xa[3], Q);
-#pragma unroll
-                for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
-                bool any = false;
-                for (int k = 0; k < M.np[tya]; k++) {
-                    const real *v = M.orient[M.ooff[tya] + k];
-                    any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > pre;
-                }
-                if (any) {
-                    load_q(a, sb, xb[3], Q);
-#pragma unroll
-                    for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
-                    bool anyb = false;
-                    for (int k = 0; k < M.np[tyb]; k++) {
-                        const real *v = M.orient[M.ooff[tyb] + k];
-                        anyb |= v[0] * w[0] + v[1] * w[1] + v[2] * w[2] > pre;
-                    }
-                    if (anyb)
-                        block_list_put(lbuf, &lnb, ida < idb ? make_int2(sa, sb) : make_int2(sb, sa), list, lcounts,
-                                       list_cap, a.flags, lflag);
-                }
-            }
-        }
-        if (KIND == kPairSplit && (a.parts & 2) && r2 < R.patch_r2) {
-            // the one-sided tests of both particles along d = x_a - x_b (with the 1e-5 margin of the full
-            // kernel's own early test): a's cosines -(n . Qa d) / r, b's (n . Qb d) / r
-            const Model<real> &M = a.tb.models[R.model];
-            const int ida = __ldg(a.buf.ident + sa);
-            const int tya = M.n_types == 1 ? 0 : type_of<real>(M, ida - R.off);
-            if (M.np[tya] > 0) {
-                const real inv = real(1) / sqrt_r(r2);
-                real Q[9], w[3];
-                load_q(a, sa, xa[3], Q);
-#pragma unroll
-                for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
-                const real mca = M.mincos_any[tya] - real(1e-5);
-                bool any = false;
-                for (int k = 0; k < M.np[tya]; k++) {
-                    const real *v = M.orient[M.ooff[tya] + k];
-                    any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > mca;
-                }
-                if (any) {
-                    const int idb = __ldg(a.buf.ident + sb);
-                    const int tyb = M.n_types == 1 ? 0 : type_of<real>(M, idb - R.off);
-                    if (M.np[tyb] > 0) {
-                        load_q(a, sb, xb[3], Q);
-#pragma unroll
-                        for (int k = 0; k < 3; k++)
-                            w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
-                        const real mcb = M.mincos_any[tyb] - real(1e-5);
-                        bool anyb = false;
-                        for (int k = 0; k < M.np[tyb]; k++) {
-                            const real *v = M.orient[M.ooff[tyb] + k];
-                            anyb |= v[0] * w[0] + v[1] * w[1] + v[2] * w[2] > mcb;
-                        }
-                        if (anyb) block_list_put(lbuf, &lnb, pr, list, lcounts, list_cap, a.flags, lflag);
-                    }
-                }
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            acc_add_raw(acc + 6 * (size_t)sa + k, fa[k]);
-            acc_add_raw(acc + 6 * (size_t)sb + k, -fa[k]);
-        }
-    }
-    if (big) atomicOr(a.flags, 2u);
-    block_list_flush(lbuf, &lnb, &lbase, list, lcounts, list_cap, a.flags, lflag);
 }
 
 // the Kern-Frenkel terms of the pairs pairforce_kernel<kPairSplit> listed, one pair per thread, into the
@@ -434,9 +466,9 @@ __global__ void __launch_bounds__(kPipeThreads, 4) patch_pairs_kernel(ForceArgs<
         real xa[4], xb[4];
         load4(a.buf.pos + 4 * (size_t)sa, xa);
         load4(a.buf.pos + 4 * (size_t)sb, xb);
-        const real d[3] = {min_image_sep<real>(xa[0], xb[0], R.box, R.l2s, R.periodic),
-                           min_image_sep<real>(xa[1], xb[1], R.box, R.l2s, R.periodic),
-                           min_image_sep<real>(xa[2], xb[2], R.box, R.l2s, R.periodic)};
+        const real d[3] = {min_image_sep<real>(xa[0], xb[0], R.box, R.box_lo, R.l2s, R.periodic),
+                           min_image_sep<real>(xa[1], xb[1], R.box, R.box_lo, R.l2s, R.periodic),
+                           min_image_sep<real>(xa[2], xb[2], R.box, R.box_lo, R.l2s, R.periodic)};
         const real rr = sqrt_r(sep_r2<real>(d[0], d[1], d[2]));
         const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
         const bool single = M.n_types == 1;
@@ -484,9 +516,9 @@ __global__ void __launch_bounds__(kPipeThreads, 4) bind_pairs_kernel(ForceArgs<f
         float x1[4], x2[4];
         load4(a.buf.pos + 4 * (size_t)s1, x1);
         load4(a.buf.pos + 4 * (size_t)s2, x2);
-        const float d[3] = {min_image_sep<float>(x1[0], x2[0], R.box, R.l2s, R.periodic),
-                            min_image_sep<float>(x1[1], x2[1], R.box, R.l2s, R.periodic),
-                            min_image_sep<float>(x1[2], x2[2], R.box, R.l2s, R.periodic)};
+        const float d[3] = {min_image_sep<float>(x1[0], x2[0], R.box, R.box_lo, R.l2s, R.periodic),
+                            min_image_sep<float>(x1[1], x2[1], R.box, R.box_lo, R.l2s, R.periodic),
+                            min_image_sep<float>(x1[2], x2[2], R.box, R.box_lo, R.l2s, R.periodic)};
         const float r2 = sep_r2(d[0], d[1], d[2]);
         const int t0 = side_of<float>(r2, B.mk2_lo, B.mk2_hi);
         if (t0 > 0) continue;
@@ -544,9 +576,9 @@ __global__ void __launch_bounds__(kPipeThreads) bound_pairs_kernel(ForceArgs<flo
             Payload<float> P1, P2;
             P1.load(a.buf.pos, a.buf.rota, a.buf.rotb, s1);
             P2.load(a.buf.pos, a.buf.rota, a.buf.rotb, s2);
-            const float dx = min_image_sep<float>(P1.v[0], P2.v[0], R.box, R.l2s, R.periodic);
-            const float dy = min_image_sep<float>(P1.v[1], P2.v[1], R.box, R.l2s, R.periodic);
-            const float dz = min_image_sep<float>(P1.v[2], P2.v[2], R.box, R.l2s, R.periodic);
+            const float dx = min_image_sep<float>(P1.v[0], P2.v[0], R.box, R.box_lo, R.l2s, R.periodic);
+            const float dy = min_image_sep<float>(P1.v[1], P2.v[1], R.box, R.box_lo, R.l2s, R.periodic);
+            const float dz = min_image_sep<float>(P1.v[2], P2.v[2], R.box, R.box_lo, R.l2s, R.periodic);
             const float rr = sqrtf(dx * dx + dy * dy + dz * dz);
             const int qp = M.pstart[t1][t2] + k1 * M.np[t2] + k2;
             if (rr > M.rmax[qp]) continue;

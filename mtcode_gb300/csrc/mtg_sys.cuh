@@ -110,6 +110,7 @@ mtg::Replica<real> make_replica(const mtg_replica_desc &d, int off, int cell_off
     R.seed_lo = (uint32_t)d.seed;
     R.seed_hi = (uint32_t)(d.seed >> 32);
     R.box = (real)d.box;
+    R.box_lo = (real)(d.box - (double)R.box);
     R.half_box = (real)(d.box * 0.5);
     R.l2s = (real)((d.box / 2.) * (d.box / 2.));
     R.cell_scale = (real)((double)nc / d.box);
@@ -245,7 +246,7 @@ struct Sys : SysBase {
     int64_t wait_limit = 0;          // mtg_set_wait_limit: 0 = each bounded loop's own bound
     // launch shapes of the pair pipeline (mtg_set_launch_config / mtg_autotune); every shape gives the same
     // FP32 results bit for bit (fixed-point sums), so the tuner may time them on the live state
-    mtg_launch_config lc = {256, 16, 8, 256};
+    mtg_launch_config lc = {256, 16, 8, 256, 1};
     // FP32 tile kernel
     bool use_tiles = false;
     int4 *d_tiles = nullptr;
@@ -471,7 +472,8 @@ struct Sys : SysBase {
         if (ma.n_types != 1) return 0;
         auto same = [](const void *x, const void *y, size_t n) { return std::memcmp(x, y, n) == 0; };
         for (const mtg::Replica<real> &b : rs) {
-            if (b.periodic != a.periodic || b.box != a.box || b.half_box != a.half_box || b.l2s != a.l2s ||
+            if (b.periodic != a.periodic || b.box != a.box || b.box_lo != a.box_lo || b.half_box != a.half_box ||
+                b.l2s != a.l2s ||
                 b.hs_limit != a.hs_limit || b.hs_4eps != a.hs_4eps || b.hs_s6 != a.hs_s6 || b.hs_s12 != a.hs_s12 ||
                 b.hs_eps != a.hs_eps || b.max_dist2 != a.max_dist2 || b.rc2 != a.rc2 || b.patch_r2 != a.patch_r2 ||
                 b.rc2_list != a.rc2_list || b.half_skin2 != a.half_skin2 || b.bond_r != a.bond_r)
@@ -896,14 +898,22 @@ struct Sys : SysBase {
             };
             mark(0);
             mtg::pair_reset_kernel<<<1, 64, 0, st>>>(d_npairs, gate, bind ? nullptr : d_patch_ctr);
+            // fused pair finding + WCA / pre-test (no list reuse, not a bond-deciding pass): the pair kernel then
+            // only takes the pairs beyond the blocks' buffers
+            const bool fused = lc.fused_pairs && skin <= 0 && !bind;
             {
                 const int t = lc.pairfind_threads, gb = std::max(1, (ntot_ + t - 1) / t), rl = skin > 0 ? 1 : 0;
-                if (t == 128)
-                    mtg::pairfind_kernel<real, 128><<<gb, 128, 0, st>>>(a, d_pairs, d_npairs, pair_cap, rl, gate);
-                else if (t == 512)
-                    mtg::pairfind_kernel<real, 512><<<gb, 512, 0, st>>>(a, d_pairs, d_npairs, pair_cap, rl, gate);
-                else
-                    mtg::pairfind_kernel<real, 256><<<gb, 256, 0, st>>>(a, d_pairs, d_npairs, pair_cap, rl, gate);
+                auto find = [&](auto threads, auto fuse) {
+                    constexpr int T = decltype(threads)::value;
+                    constexpr bool FU = decltype(fuse)::value;
+                    mtg::pairfind_kernel<real, T, FU><<<gb, T, 0, st>>>(a, d_pairs, d_npairs, pair_cap, rl, gate, d_acc,
+                                                                        d_patch_list, patch_cap, d_patch_ctr);
+                };
+                using F1 = std::true_type;
+                using F0 = std::false_type;
+                if (t == 128) fused ? find(std::integral_constant<int, 128>{}, F1{}) : find(std::integral_constant<int, 128>{}, F0{});
+                else if (t == 512) fused ? find(std::integral_constant<int, 512>{}, F1{}) : find(std::integral_constant<int, 512>{}, F0{});
+                else fused ? find(std::integral_constant<int, 256>{}, F1{}) : find(std::integral_constant<int, 256>{}, F0{});
             }
             mark(1);
             const int g_force = sms * lc.pairforce_blocks_per_sm, g_patch = sms * lc.patch_blocks_per_sm;
@@ -1709,14 +1719,15 @@ struct Sys : SysBase {
         MTG_REQUIRE(c->pairforce_blocks_per_sm >= 1 && c->pairforce_blocks_per_sm <= 64 &&
                         c->patch_blocks_per_sm >= 1 && c->patch_blocks_per_sm <= 64,
                     "mtg_set_launch_config: blocks per SM must lie in [1, 64]");
+        MTG_REQUIRE(c->fused_pairs == 0 || c->fused_pairs == 1, "mtg_set_launch_config: fused_pairs must be 0 or 1");
         MTG_CUDA(cudaStreamSynchronize(st));
         lc = *c;
         drop_graphs();   // the step graphs captured the old shapes
     }
 
-    // ms per step of `n` graph-replayed steps (one untimed step first captures the graph)
+    // ms per step of `n` graph-replayed steps (two untimed steps first capture the graphs of both buffer parities)
     double time_steps(int n) {
-        step(1, nullptr);
+        step(2, nullptr);
         cudaEvent_t e0, e1;
         MTG_CUDA(cudaEventCreate(&e0));
         MTG_CUDA(cudaEventCreate(&e1));
@@ -1742,6 +1753,7 @@ struct Sys : SysBase {
             return;
         }
         static const int threads[] = {128, 256, 512};
+        static const int onoff[] = {0, 1};
         static const int force_bps[] = {4, 8, 12, 16, 24, 32};
         static const int patch_bps[] = {2, 4, 8, 16, 24};
         mtg_launch_config cur = lc;
@@ -1767,6 +1779,7 @@ struct Sys : SysBase {
             try_field(&mtg_launch_config::patch_blocks_per_sm, patch_bps, 5);
             try_field(&mtg_launch_config::pairfind_threads, threads, 3);
             try_field(&mtg_launch_config::epilogue_threads, threads, 3);
+            try_field(&mtg_launch_config::fused_pairs, onoff, 2);
         }
         set_launch_config(&cur);
         *best = cur;

@@ -249,9 +249,9 @@ __device__ __forceinline__ void pair_sep(const Replica<float> &R, const StageBuf
                                          float4 &pi, float4 &pj, float d[3]) {
     pi = B.pos[W.h_k[pair_h(e)]];
     pj = B.pos[pair_k(e)];
-    d[0] = min_image_sep<float>(pi.x, pj.x, R.box, R.l2s, R.periodic);
-    d[1] = min_image_sep<float>(pi.y, pj.y, R.box, R.l2s, R.periodic);
-    d[2] = min_image_sep<float>(pi.z, pj.z, R.box, R.l2s, R.periodic);
+    d[0] = min_image_sep<float>(pi.x, pj.x, R.box, R.box_lo, R.l2s, R.periodic);
+    d[1] = min_image_sep<float>(pi.y, pj.y, R.box, R.box_lo, R.l2s, R.periodic);
+    d[2] = min_image_sep<float>(pi.z, pj.z, R.box, R.box_lo, R.l2s, R.periodic);
 }
 
 // phase 2a body: WCA core of pair entry e, then the home particle's own cone test from data in shared
@@ -681,9 +681,9 @@ __device__ __forceinline__ int scan_cells(const ForceArgs<float> &a, const Repli
                         float ddx, ddy, ddz;
                         if (KIND == kScanStale) {
                             // positions have moved since the cells were built: plain minimum image
-                            ddx = min_image_sep<float>(pi.x, pj[u].x, R.box, R.l2s, R.periodic);
-                            ddy = min_image_sep<float>(pi.y, pj[u].y, R.box, R.l2s, R.periodic);
-                            ddz = min_image_sep<float>(pi.z, pj[u].z, R.box, R.l2s, R.periodic);
+                            ddx = min_image_sep<float>(pi.x, pj[u].x, R.box, R.box_lo, R.l2s, R.periodic);
+                            ddy = min_image_sep<float>(pi.y, pj[u].y, R.box, R.box_lo, R.l2s, R.periodic);
+                            ddz = min_image_sep<float>(pi.z, pj[u].z, R.box, R.box_lo, R.l2s, R.periodic);
                         } else {
                             const float shx = t < lena ? 0.f : shw;
                             ddx = (pi.x - pj[u].x) - shx;
@@ -730,9 +730,9 @@ __device__ __forceinline__ int scan_list(const ForceArgs<float> &a, const Replic
         for (int u = 0; u < 4; u++) pj[u] = B.pos[t0 + u < cnt ? (int)(e[u] & 2047u) : myk];
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            const float ddx = min_image_sep<float>(pi.x, pj[u].x, R.box, R.l2s, R.periodic);
-            const float ddy = min_image_sep<float>(pi.y, pj[u].y, R.box, R.l2s, R.periodic);
-            const float ddz = min_image_sep<float>(pi.z, pj[u].z, R.box, R.l2s, R.periodic);
+            const float ddx = min_image_sep<float>(pi.x, pj[u].x, R.box, R.box_lo, R.l2s, R.periodic);
+            const float ddy = min_image_sep<float>(pi.y, pj[u].y, R.box, R.box_lo, R.l2s, R.periodic);
+            const float ddz = min_image_sep<float>(pi.z, pj[u].z, R.box, R.box_lo, R.l2s, R.periodic);
             const bool hit = t0 + u < cnt && ddx * ddx + ddy * ddy + ddz * ddz < R.rc2;
             const unsigned m = __ballot_sync(0xffffffffu, hit);
             if (hit) {

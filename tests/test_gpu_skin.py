@@ -75,15 +75,18 @@ def test_fp32_bonded_crowded_and_walled_systems_with_a_skin(kernel):
     assert rebuilds > 1
 
 
-def test_fp64_trajectory_with_a_skin():
+@pytest.mark.parametrize("kernel", ["pairs", "per_particle"])
+def test_fp64_trajectory_with_a_skin(kernel):
+    """FP64 sums a particle's pair terms in the order the pairs are found (double atomics in the pair pipeline),
+    which the lists change: the two runs agree to rounding, amplified over 50 steps."""
     spec = tetra(1500, 0.25, seed=5)
     x = random_positions(spec.n, spec.box, True, 0.95, 6)
     Q = random_rotations(spec.n, 7)
-    exact, _ = run([spec], x, Q, 50, precision="fp64")
-    listed, rebuilds = run([spec], x, Q, 50, precision="fp64", skin=0.4)
+    exact, _ = run([spec], x, Q, 50, precision="fp64", kernel=kernel)
+    listed, rebuilds = run([spec], x, Q, 50, precision="fp64", skin=0.4, kernel=kernel)
     for key in ("x", "p", "Lb", "Q"):
         scale = max(1.0, np.abs(exact[0][key]).max())
-        assert np.abs(listed[0][key] - exact[0][key]).max() <= 1e-12 * scale, key
+        assert np.abs(listed[0][key] - exact[0][key]).max() <= 1e-10 * scale, key
     assert rebuilds >= 1
 
 

@@ -12,9 +12,14 @@ from mtcode_gb300 import tuning
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [{"pairfind_threads": 256, "pairforce_blocks_per_sm": 16, "patch_blocks_per_sm": 8, "epilogue_threads": 256},
-          {"pairfind_threads": 128, "pairforce_blocks_per_sm": 4, "patch_blocks_per_sm": 2, "epilogue_threads": 512},
-          {"pairfind_threads": 512, "pairforce_blocks_per_sm": 32, "patch_blocks_per_sm": 24, "epilogue_threads": 128}]
+SHAPES = [{"pairfind_threads": 256, "pairforce_blocks_per_sm": 16, "patch_blocks_per_sm": 8, "epilogue_threads": 256,
+           "fused_pairs": 1},
+          {"pairfind_threads": 256, "pairforce_blocks_per_sm": 16, "patch_blocks_per_sm": 8, "epilogue_threads": 256,
+           "fused_pairs": 0},
+          {"pairfind_threads": 128, "pairforce_blocks_per_sm": 4, "patch_blocks_per_sm": 2, "epilogue_threads": 512,
+           "fused_pairs": 1},
+          {"pairfind_threads": 512, "pairforce_blocks_per_sm": 32, "patch_blocks_per_sm": 24, "epilogue_threads": 128,
+           "fused_pairs": 0}]
 
 
 def run(W, shape, steps=30):
@@ -51,6 +56,7 @@ def test_autotune_and_cache(tmp_path):
         cfg = got["launch_config"]
         assert cfg["pairfind_threads"] in (128, 256, 512) and cfg["epilogue_threads"] in (128, 256, 512)
         assert 1 <= cfg["pairforce_blocks_per_sm"] <= 64 and 1 <= cfg["patch_blocks_per_sm"] <= 64
+        assert cfg["fused_pairs"] in (0, 1)
         assert s.launch_config == cfg
         s.step(3)
         assert np.isfinite(s.get_state()["x"]).all() and s.flags == 0
