@@ -44,6 +44,8 @@ struct Replica {
     real rc2;                  // squared force range (max of HS range and patch range)
     real patch_r2;             // squared range of any patch force: min(max_dist2, (1.4 dis_max)^2)
     real rc2_list;             // skin lists: squared list range (force range + skin, padded for rounding)
+    real rc2_find, rc2_list_find;   // pair finding's ranges: rc2 / rc2_list widened by the rounding of its cheaper
+                                    // separation, (x_a - x_b) - shift; the pair kernels keep the exact test
     real half_skin2;           // skin lists: (skin / 2)^2, the displacement that forces a rebuild
     real bond_r;               // ComboPatch::max_check
 };
@@ -233,14 +235,6 @@ __device__ __forceinline__ real min_image_sep(real xa, real xb, real l, real l_l
         else dx = dx >= real(0) ? dx - l : dx + l;
     }
     return dx;
-}
-// x_a - x_b for a partner reached across a periodic face with image shift sh (+l, -l or 0), in the arithmetic of
-// min_image_sep (both give the same bits for the same pair)
-template <class real>
-__device__ __forceinline__ real shifted_sep(real xa, real xb, real sh, real l_lo) {
-    if constexpr (sizeof(real) == 4)
-        return sh > real(0) ? ((xa - sh) - xb) - l_lo : (sh < real(0) ? (xa - (xb + sh)) + l_lo : xa - xb);
-    else return (xa - xb) - sh;
 }
 
 // ------------------------------------------------------------------ Philox4x32-10

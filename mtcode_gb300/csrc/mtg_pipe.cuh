@@ -27,8 +27,9 @@ constexpr int kPipeThreads = 256;      // block size of the grid-stride pair ker
 constexpr int kPairsPerThread = 8;     // pairs a pairfind block buffers in shared memory, per thread
 constexpr int kPairsPerParticle = 16;  // capacity of the pair list (unordered pairs per particle)
 
-// |d|^2 with explicit roundings (no contraction), so that pairfind and pairforce decide a pair at the
-// cutoff identically; with the image shift applied by shifted_sep the separation is bit for bit min_image_sep's
+// |d|^2 with explicit roundings (no contraction).  Pair finding tests a cheaper separation against a range widened
+// by its rounding (rc2_find), so it finds a superset of the pairs; the pair kernels decide each pair with the
+// exact separation (min_image_sep) and drop the rest, so every path takes the same pair set.
 template <class real>
 __device__ __forceinline__ real sep_r2(real dx, real dy, real dz) {
     return add_rn(add_rn(mul_rn(dx, dx), mul_rn(dy, dy)), mul_rn(dz, dz));
@@ -323,7 +324,7 @@ __global__ void __launch_bounds__(THREADS) pairfind_kernel(ForceArgs<real> a, in
     int r = 0;
     if (valid) r = replica_of(a.tb, s);
     const Replica<real> &R = a.tb.reps[r];
-    const real range2 = range_list ? R.rc2_list : R.rc2;
+    const real range2 = range_list ? R.rc2_list_find : R.rc2_find;   // a superset: the pair kernels re-test
     const int nc = R.nc;
     int key = valid ? a.buf.home_cell[s] - R.cell_off : 0;
     if (key < 0 || key >= nc * nc * nc) {
@@ -354,8 +355,7 @@ __global__ void __launch_bounds__(THREADS) pairfind_kernel(ForceArgs<real> a, in
                 dz = rr <= 1 ? 0 : 1;
             }
             // pairfind runs right after a sort, so every particle lies in its cell: a neighbour cell
-            // reached across a periodic face holds coordinates one box length away (image shift, applied in
-            // the arithmetic of min_image_sep, so pairforce sees the same separation bit for bit)
+            // reached across a periodic face holds coordinates one box length away (image shift)
             int zz = small ? dz : cz + dz, yy = small ? dy : cy + dy;
             bool skip = small && (dy >= nc || dz >= nc);
             if (zz >= nc) {
@@ -409,9 +409,7 @@ __global__ void __launch_bounds__(THREADS) pairfind_kernel(ForceArgs<real> a, in
                     for (int t = c0; t < ce; t++) {
                         real pj[3];
                         load_pos(a.buf.pos + 4 * (size_t)t, pj[0], pj[1], pj[2]);
-                        const real dx = shifted_sep<real>(pi[0], pj[0], shx, R.box_lo),
-                                   dy2 = shifted_sep<real>(pi[1], pj[1], shy, R.box_lo),
-                                   dz2 = shifted_sep<real>(pi[2], pj[2], shz, R.box_lo);
+                        const real dx = (pi[0] - pj[0]) - shx, dy2 = (pi[1] - pj[1]) - shy, dz2 = (pi[2] - pj[2]) - shz;
                         if (sep_r2<real>(dx, dy2, dz2) < range2) mask |= 1u << (t - c0);
                     }
                 } else {  // tiny grids: no cell geometry to lean on

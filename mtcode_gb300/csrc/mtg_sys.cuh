@@ -134,6 +134,13 @@ mtg::Replica<real> make_replica(const mtg_replica_desc &d, int off, int cell_off
     R.bond_r = (real)g.bond_r;
     const double rl = list_range(g.rc, skin);
     R.rc2_list = (real)(rl * rl);
+    // pair finding forms a shifted separation as (x_a - x_b) - shift, which may differ from the pair kernels'
+    // min_image_sep by a rounding at the box length's scale plus the float box's own error; it takes every
+    // pair within the range widened by that slack, and the pair kernels drop the extra ones with the exact test
+    const double ulp_box = std::ldexp(1.0, std::ilogb(std::max(d.box, 1.0)) - 23);
+    const double slack = 2.0 * ulp_box + std::fabs(d.box - (double)(float)d.box) + 1e-6;
+    R.rc2_find = (real)((g.rc + slack) * (g.rc + slack) * (1 + 1e-6));
+    R.rc2_list_find = (real)((rl + slack) * (rl + slack) * (1 + 1e-6));
     R.half_skin2 = (real)(0.25 * skin * skin);
     return R;
 }
@@ -476,7 +483,8 @@ struct Sys : SysBase {
                 b.l2s != a.l2s ||
                 b.hs_limit != a.hs_limit || b.hs_4eps != a.hs_4eps || b.hs_s6 != a.hs_s6 || b.hs_s12 != a.hs_s12 ||
                 b.hs_eps != a.hs_eps || b.max_dist2 != a.max_dist2 || b.rc2 != a.rc2 || b.patch_r2 != a.patch_r2 ||
-                b.rc2_list != a.rc2_list || b.half_skin2 != a.half_skin2 || b.bond_r != a.bond_r)
+                b.rc2_list != a.rc2_list || b.rc2_find != a.rc2_find || b.rc2_list_find != a.rc2_list_find ||
+                b.half_skin2 != a.half_skin2 || b.bond_r != a.bond_r)
                 return 0;
             const mtg::Model<real> &mb = models[b.model];
             if (mb.n_types != 1 || !same(mb.np, ma.np, sizeof ma.np) || !same(mb.ooff, ma.ooff, sizeof ma.ooff) ||

@@ -27,6 +27,10 @@ def main() -> None:
     ap.add_argument("--skin", type=float, default=0.0, help="neighbour skin (sigma); 0 rebuilds cells every step")
     ap.add_argument("--single-bond", nargs=2, type=float, metavar=("ON", "OFF"), default=None,
                     help="single-bond-per-patch mode (run_singlebond) with BindingModelSingle(ON, OFF)")
+    ap.add_argument("--launch", default=None,
+                    help="pair-pipeline launch shapes as pairfind_threads,pairforce_blocks_per_sm,"
+                         "patch_blocks_per_sm,epilogue_threads,fused_pairs (default: the library's)")
+    ap.add_argument("--tune", action="store_true", help="run the launch-shape autotuner before timing")
     args = ap.parse_args()
     if args.workload == "c4":
         W = workloads.patchy_c4(seed=args.seed, n_replicas=args.replicas)
@@ -43,7 +47,14 @@ def main() -> None:
         if args.single_bond:
             from .system import binding_single
             s.set_single_bond(binding_single(*args.single_bond))
+        if args.launch:
+            keys = ("pairfind_threads", "pairforce_blocks_per_sm", "patch_blocks_per_sm", "epilogue_threads",
+                    "fused_pairs")
+            s.launch_config = dict(zip(keys, (int(v) for v in args.launch.split(","))))
         s.init_forces()
+        if args.tune:
+            cfg, ms = s.autotune(5)
+            print(f"autotune: {cfg} at {ms:.3f} ms/step", flush=True)
         s.sync()
         t0 = time.perf_counter()
         s.step(args.steps)
