@@ -80,7 +80,7 @@ __device__ __forceinline__ int find_replica(const int *rep_slot, int nrep, int s
 // the replica of slot s: one 2-byte load where the per-slot table exists (fewer than 65,536 replicas)
 template <class real>
 __device__ __forceinline__ int replica_of(const Tables<real> &tb, int s) {
-    return tb.slot_rep ? (int)__ldg(tb.slot_rep + s) : replica_of(tb, s);
+    return tb.slot_rep ? (int)__ldg(tb.slot_rep + s) : find_replica(tb.rep_slot, tb.nrep, s);
 }
 
 // cell id of a position inside replica R (cube::assign_box with cells of the force grid)

@@ -178,3 +178,30 @@ def test_identical_replicas_in_batch_equal_each_alone():
             alone = s1.get_state()
         for key in ("x", "p", "Lb", "Q"):
             assert np.array_equal(batch[key][r * n:(r + 1) * n], alone[key]), (r, key)
+
+
+def test_more_replicas_than_the_slot_table_holds():
+    """65,537 replicas: past the 2-byte per-slot replica table (65,536 replicas), every kernel finds a slot's
+    replica by binary search over the replica offsets; forces of sampled replicas against the oracle, then steps."""
+    from mtcode_gb300.system import PatchModelSpec, ReplicaSpec, random_positions, random_rotations
+    from mtcode_gb300.workloads import box_for
+    n_rep, n = 65537, 4
+    box = box_for(n, 0.1)
+    model = PatchModelSpec.tetrahedral(n, 8.0, 1.2, math.acos(0.9))
+    reps = [ReplicaSpec(n=n, box=box, model=model, kT=1.0, seed=r) for r in range(n_rep)]
+    x = np.concatenate([random_positions(n, box, True, 0.9, 10 + r) for r in range(n_rep)])
+    x = x.astype(np.float32).astype(np.float64)
+    Q = random_rotations(n * n_rep, 3).astype(np.float32).astype(np.float64)
+    z = np.zeros((n * n_rep, 3))
+    with LangevinNVTRGPU(reps, precision="fp32") as s:
+        s.initialize(x, z, z, Q)
+        F, T = s.calculate_forces_and_torques3D()
+        for r in (0, 1, 32768, 65535, 65536):
+            a, b = r * n, (r + 1) * n
+            Fo, To = po.System(reps[r]).forces(x[a:b], Q[a:b])
+            assert np.abs(F[a:b] - Fo).max() <= 1e-5 * max(1.0, np.abs(Fo).max()), r
+            assert np.abs(T[a:b] - To).max() <= 1e-5 * max(1.0, np.abs(To).max()), r
+        s.init_forces()
+        s.step(5)
+        st = s.get_state()
+        assert np.isfinite(st["x"]).all() and s.flags == 0
