@@ -95,6 +95,16 @@ inline ReplicaGeometry geometry_of(const mtg_replica_desc &d) {
 // rounding of the displacement test can never lose a pair
 inline double list_range(double rc, double skin) { return skin > 0 ? rc + skin + 1e-3 : rc; }
 
+// Pair finding forms a shifted separation as (x_a - x_b) - shift, which may differ from the pair kernels'
+// min_image_sep by a rounding at the box length's scale plus the float box's own error; it takes every pair
+// within the range widened by that slack (squared here), and the pair kernels drop the extra ones with the
+// exact test.
+inline double find_range2(double range, double box) {
+    const double ulp_box = std::ldexp(1.0, std::ilogb(std::max(box, 1.0)) - 23);
+    const double slack = 2.0 * ulp_box + std::fabs(box - (double)(float)box) + 1e-6;
+    return (range + slack) * (range + slack) * (1 + 1e-6);
+}
+
 template <class real>
 mtg::Replica<real> make_replica(const mtg_replica_desc &d, int off, int cell_off, int nc, int model,
                                 double skin = 0.0) {
@@ -134,13 +144,8 @@ mtg::Replica<real> make_replica(const mtg_replica_desc &d, int off, int cell_off
     R.bond_r = (real)g.bond_r;
     const double rl = list_range(g.rc, skin);
     R.rc2_list = (real)(rl * rl);
-    // pair finding forms a shifted separation as (x_a - x_b) - shift, which may differ from the pair kernels'
-    // min_image_sep by a rounding at the box length's scale plus the float box's own error; it takes every
-    // pair within the range widened by that slack, and the pair kernels drop the extra ones with the exact test
-    const double ulp_box = std::ldexp(1.0, std::ilogb(std::max(d.box, 1.0)) - 23);
-    const double slack = 2.0 * ulp_box + std::fabs(d.box - (double)(float)d.box) + 1e-6;
-    R.rc2_find = (real)((g.rc + slack) * (g.rc + slack) * (1 + 1e-6));
-    R.rc2_list_find = (real)((rl + slack) * (rl + slack) * (1 + 1e-6));
+    R.rc2_find = (real)find_range2(g.rc, d.box);
+    R.rc2_list_find = (real)find_range2(rl, d.box);
     R.half_skin2 = (real)(0.25 * skin * skin);
     return R;
 }
@@ -801,6 +806,7 @@ struct Sys : SysBase {
             const double mk2 = br[(size_t)r].mk2 * (1 + 1e-5);
             reps[r].patch_r2 = (real)0;
             reps[r].rc2 = (real)std::max(hs * hs, mk2);
+            reps[r].rc2_find = (real)find_range2(std::sqrt(std::max(hs * hs, mk2)), desc[r].box);
             reps[r].nc = reps_obs[r].nc;
             reps[r].cell_off = reps_obs[r].cell_off;
             reps[r].cell_scale = reps_obs[r].cell_scale;
