@@ -29,6 +29,8 @@ struct Replica {
     int off;          // first slot / global particle index
     int cell_off;     // first global cell
     int nc;           // cells per side of the force grid
+    uint32_t nc_mul;  // n / nc = umulhi(n, nc_mul) >> nc_sh for 0 <= n < nc^3 (nc_magic)
+    int nc_sh;
     int periodic;
     int model;        // index into the model table
     uint32_t seed_lo, seed_hi;
@@ -49,6 +51,12 @@ struct Replica {
     real half_skin2;           // skin lists: (skin / 2)^2, the displacement that forces a rebuild
     real bond_r;               // ComboPatch::max_check
 };
+
+// n / nc for a cell key 0 <= n < nc^3 of replica R's force grid, without an integer division
+template <class real>
+__device__ __forceinline__ int div_nc(const Replica<real> &R, int n) {
+    return (int)(__umulhi((unsigned)n, R.nc_mul) >> R.nc_sh);
+}
 
 // ------------------------------------------------------------------ single-bond-per-patch mode, per replica
 // Patch numbering (GeneralPatch, GeneralPatch.cpp:285-320) and the constants of the bond tests.  The FP64

@@ -53,37 +53,59 @@ __device__ __forceinline__ void load_q(const ForceArgs<double> &a, int slot, dou
     Q[4] = c[0]; Q[5] = c[1]; Q[6] = c[2]; Q[7] = c[3]; Q[8] = q8;
 }
 
-// Appends the pairs (s, c0 + b) for every bit b of each lane's mask: one warp-wide scan of the counts and
-// one shared-memory atomic per warp take consecutive entries of the block buffer; entries past its end go
-// straight to the list.  Called by all 32 lanes of the warp.
-__device__ __forceinline__ void warp_pair_flush(int2 *buf, int buf_cap, int *nb, int s, int c0, unsigned mask,
-                                                int2 *pairs, unsigned long long *npairs, long long cap,
-                                                unsigned *flags) {
-    const unsigned full = 0xffffffffu;
-    if (!__ballot_sync(full, mask != 0u)) return;
-    const int lane = threadIdx.x & 31;
-    const int cnt = __popc(mask);
-    int incl = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(full, incl, o);
-        if (lane >= o) incl += v;
-    }
-    int q = 0;
-    if (lane == 31) q = atomicAdd(nb, incl);
-    q = __shfl_sync(full, q, 31) + incl - cnt;
-    while (mask) {
-        const int b = __ffs(mask) - 1;
-        mask &= mask - 1u;
-        const int2 p = make_int2(s, c0 + b);
-        if (q < buf_cap) {
-            buf[q] = p;
-        } else {  // the block buffer is full
-            const unsigned long long w = atomicAdd(npairs, 1ull);
-            if ((long long)w < cap) pairs[w] = p;
-            else atomicOr(flags, 8u);
+// The squared separation pair finding tests: fused multiply-adds, rounded differently from sep_r2 by at most a
+// few units in the last place, which the relative widening of the finding range (1e-6) covers.
+__device__ __forceinline__ float find_r2(float dx, float dy, float dz) { return fmaf(dx, dx, fmaf(dy, dy, dz * dz)); }
+__device__ __forceinline__ double find_r2(double dx, double dy, double dz) { return fma(dx, dx, fma(dy, dy, dz * dz)); }
+
+// Pair finding keeps each warp's pairs in its own part of the block's shared-memory buffer.
+constexpr int kWarpPairs = kPairsPerThread * 32;
+
+// Appends the pairs (s, c0 + b) for every bit b of each lane's mask to the warp's part of the buffer: per round
+// one ballot, and every lane with a bit left writes its lowest at the warp's count plus the number of lower
+// lanes writing in that round.  `cnt` (the same in every lane) counts the warp's pairs; entries past the part
+// go straight to the list, where the pair-force kernel takes them.  Called by all 32 lanes.
+__device__ __forceinline__ void warp_append(int2 *part, int &cnt, int s, int c0, unsigned mask, int2 *pairs,
+                                            unsigned long long *npairs, long long cap, unsigned *flags) {
+    const unsigned lower = (1u << (threadIdx.x & 31)) - 1u;
+    for (;;) {
+        const unsigned bal = __ballot_sync(0xffffffffu, mask != 0u);
+        if (bal == 0u) break;
+        if (mask) {
+            const int b = __ffs(mask) - 1;
+            mask &= mask - 1u;
+            const int q = cnt + __popc(bal & lower);
+            const int2 p = make_int2(s, c0 + b);
+            if (q < kWarpPairs) {
+                part[q] = p;
+            } else {
+                const unsigned long long w = atomicAdd(npairs, 1ull);
+                if ((long long)w < cap) pairs[w] = p;
+                else atomicOr(flags, 8u);
+            }
         }
-        q++;
+        cnt += __popc(bal);
+    }
+}
+
+// The candidates [t0, t1) of one lane, tested against the lane's position minus the segment's image shift
+// (qx, qy, qz), in chunks of at most 32 slots whose hits are marked in a bit mask and appended by the warp
+// together (the chunk loop is warp-uniform; the candidate loop is not unrolled: the lanes' trip counts differ,
+// and an unrolled body keeps the short lanes idle for longer).
+template <class real>
+__device__ __forceinline__ void scan_segment(const real *pos, int t0, int t1, real qx, real qy, real qz, real range2,
+                                             int2 *part, int &cnt, int s, int2 *pairs, unsigned long long *npairs,
+                                             long long cap, unsigned *flags) {
+    for (int c0 = t0; __any_sync(0xffffffffu, c0 < t1); c0 += 32) {
+        unsigned mask = 0u;
+        const int ce = t1 < c0 + 32 ? t1 : c0 + 32;
+#pragma unroll 1
+        for (int t = c0; t < ce; t++) {
+            real pj[3];
+            load_pos(pos + 4 * (size_t)t, pj[0], pj[1], pj[2]);
+            if (find_r2(qx - pj[0], qy - pj[1], qz - pj[2]) < range2) mask |= 1u << (t - c0);
+        }
+        warp_append(part, cnt, s, c0, mask, pairs, npairs, cap, flags);
     }
 }
 
@@ -153,12 +175,13 @@ enum PairKind : int { kPairBind = 1, kPairSplit = 2 };
 // One listed pair (sa, sb): the WCA core into acc (both particles), and -- KIND kPairSplit -- the pair onto
 // `list` when both particles have a patch near a cone, or -- KIND kPairBind -- onto `list` in canonical order
 // when both do (single-bond mode).  List entries are staged in the block's lbuf (block_list_put).
+// rhint >= 0: sa's replica, known to the caller.
 template <class real, int KIND>
 __device__ __forceinline__ void pair_core(const ForceArgs<real> &a, int sa, int sb, typename PairAcc<real>::type *acc,
                                           int2 *lbuf, int *lnb, int2 *list, long long list_cap,
-                                          unsigned long long *lcounts, unsigned lflag, bool &big) {
+                                          unsigned long long *lcounts, unsigned lflag, bool &big, int rhint = -1) {
     constexpr bool BIND = KIND == kPairBind;
-    const int r = a.tb.uniform ? 0 : replica_of(a.tb, sa);
+    const int r = rhint >= 0 ? rhint : (a.tb.uniform ? 0 : replica_of(a.tb, sa));
     const Replica<real> &R = a.tb.reps[r];
     real xa[4], xb[4];
     load4(a.buf.pos + 4 * (size_t)sa, xa);
@@ -292,33 +315,41 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<re
 }
 
 // range_list: use the replica's list range (skin lists) instead of its force range.
-// Each lane scans its particle's candidate segments in chunks of at most 32 slots and marks the hits of a
-// chunk in a bit mask; the warp then appends the marked pairs together (warp_pair_flush), so the candidate
-// loop itself carries no appends.  The chunk and segment loops are warp-uniform.
+// Each lane scans its particle's candidate segments (scan_segment): chunks of at most 32 slots whose hits are
+// marked in a bit mask and appended by the warp together to its own part of the block buffer (warp_append), so
+// the candidate loop carries no appends and no shared-memory atomics.  Warps whose lanes all sit in grids of
+// three or more cells per side take the five rows of the forward half-stencil unrolled (row offsets and image
+// shifts known at compile time, the shifts taken out of the candidate loop); warps with a lane in a smaller grid
+// take the general row loop.
 //
-// FUSED (no list reuse: every step rebuilds): the block's pairs do not go to the list at all.  After the scan
-// the whole block takes the buffered pairs, several per thread with every lane busy, through pair_core (WCA core,
-// cone pre-test, patch list) while their positions are still in L1; only pairs beyond the block buffer reach the
-// HBM list, for pairforce_kernel.
+// FUSED (no list reuse: every step rebuilds): the pairs do not go to the list at all.  After its scan each
+// warp takes its own buffered pairs, one per lane, through pair_core (WCA core, cone pre-test, patch list)
+// while their positions are still in L1; only pairs beyond a warp's part reach the HBM list, for
+// pairforce_kernel.
+// FP32 register budgets: the fused form at 48 (five 256-thread blocks per SM; its natural 64 allow four,
+// measured 8% slower), the search alone at 40 (six blocks).  FP64 keeps its natural count (no spills).
 template <class real, int THREADS, bool FUSED>
-__global__ void __launch_bounds__(THREADS) pairfind_kernel(ForceArgs<real> a, int2 *pairs,
+__global__ void __launch_bounds__(THREADS, sizeof(real) == 4 ? (FUSED ? 1280 : 1536) / THREADS : 1)
+    pairfind_kernel(ForceArgs<real> a, int2 *pairs,
                                                            unsigned long long *npairs, long long cap,
                                                            int range_list, const int *gate,
                                                            typename PairAcc<real>::type *acc = nullptr,
                                                            int2 *list = nullptr, long long list_cap = 0,
                                                            unsigned long long *list_counts = nullptr) {
     if (gated_off(gate, 1)) return;
-    constexpr int kBufCap = kPairsPerThread * THREADS;
     constexpr int kLBuf = FUSED ? kBlockListCap : 1;
-    __shared__ int2 buf[kBufCap];
+    __shared__ int2 buf[kWarpPairs * (THREADS / 32)];
     __shared__ int2 lbuf[kLBuf];
-    __shared__ int nb, lnb;
-    __shared__ unsigned long long base, lbase;
-    if (threadIdx.x == 0) {
-        nb = 0;
-        lnb = 0;
+    __shared__ int lnb;
+    __shared__ unsigned long long lbase;
+    if constexpr (FUSED) {
+        if (threadIdx.x == 0) lnb = 0;
+        __syncthreads();
     }
-    __syncthreads();
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int2 *const part = buf + kWarpPairs * (threadIdx.x >> 5);
+    int cnt = 0;   // the warp's pairs (the same in every lane)
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = s < a.tb.ntot;
     int r = 0;
@@ -331,116 +362,175 @@ __global__ void __launch_bounds__(THREADS) pairfind_kernel(ForceArgs<real> a, in
         atomicOr(a.flags, 16u);
         key = 0;
     }
-    const int cx = key % nc, cy = (key / nc) % nc, cz = key / (nc * nc);
+    const int q1 = div_nc(R, key), cz = div_nc(R, q1);
+    const int cx = key - q1 * nc, cy = q1 - cz * nc;
     real pi[3] = {real(0), real(0), real(0)};
     if (valid) load_pos(a.buf.pos + 4 * (size_t)s, pi[0], pi[1], pi[2]);
     const real L = R.box;
+    const int periodic = R.periodic;
     // Each unordered pair once.  With three or more cells per side: the forward half of the stencil
     // (rows (dy, dz) = (0, 0) [cells x, x + 1], (1, 0), (-1..1, 1) [cells x - 1 .. x + 1]) -- an offset
     // and its negative are distinct cells, so exactly one of the two particles' scans holds the
     // other -- and in the own cell only the later slots.  Smaller grids: every cell, later slots.
+    // pairfind runs right after a sort, so every particle lies in its cell: a neighbour cell reached across a
+    // periodic face holds coordinates one box length away (image shift).
     const bool small = nc < 3;
-    const int nrows = !valid ? 0 : (small ? 9 : 5);
-    const int nrows_warp = __any_sync(0xffffffffu, nrows == 9) ? 9 : 5;
-    for (int rr = 0; rr < nrows_warp; rr++) {  // warp-uniform; rows past a lane's nrows are empty
-        int a0 = 0, a1 = 0, b0 = 0, b1 = 0;
-        real shz = real(0), shy = real(0), shb = real(0);
-        if (rr < nrows) {
-            int dy, dz;
-            if (small) {
-                dy = rr % 3;
-                dz = rr / 3;
-            } else {
-                dy = rr == 0 ? 0 : (rr == 1 ? 1 : rr - 3);
-                dz = rr <= 1 ? 0 : 1;
-            }
-            // pairfind runs right after a sort, so every particle lies in its cell: a neighbour cell
-            // reached across a periodic face holds coordinates one box length away (image shift)
-            int zz = small ? dz : cz + dz, yy = small ? dy : cy + dy;
-            bool skip = small && (dy >= nc || dz >= nc);
-            if (zz >= nc) {
-                skip |= !R.periodic;
+    if (!__any_sync(full, valid && small)) {
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+            const int dy = k == 0 ? 0 : (k == 1 ? 1 : k - 3), dz = k <= 1 ? 0 : 1;
+            int zz = cz + dz, yy = cy + dy;
+            real shz = real(0), shy = real(0), shb = real(0);
+            bool skip = !valid;
+            if (dz > 0 && zz >= nc) {
+                skip |= !periodic;
                 shz = L;
                 zz -= nc;
             }
-            if (yy < 0 || yy >= nc) {
-                skip |= !R.periodic;
-                shy = yy < 0 ? -L : L;
-                yy = yy < 0 ? yy + nc : yy - nc;
+            if (dy < 0 && yy < 0) {
+                skip |= !periodic;
+                shy = -L;
+                yy += nc;
+            } else if (dy > 0 && yy >= nc) {
+                skip |= !periodic;
+                shy = L;
+                yy -= nc;
             }
+            // the x cells of the row as at most two contiguous slot segments: [a0, a1) unshifted and one
+            // wrapped cell [b0, b1) (image shift shb)
+            int a0 = 0, a1 = 0, b0 = 0, b1 = 0;
             if (!skip) {
                 const int row = R.cell_off + nc * (yy + nc * zz);
-                // x cells of this row as at most two contiguous slot segments: [a0, a1) unshifted and one
-                // wrapped cell [b0, b1) (image shift shb)
+                const int x0 = k == 0 ? cx : cx - 1, x1 = cx + 1;  // the own row starts at the own cell
+                a0 = __ldg(a.start + row + (x0 < 0 ? 0 : x0));
+                a1 = __ldg(a.start + row + (x1 >= nc ? nc : x1 + 1));
+                if (periodic) {
+                    if (x0 < 0) {
+                        b0 = __ldg(a.start + row + nc - 1);
+                        b1 = __ldg(a.start + row + nc);
+                        shb = -L;
+                    } else if (x1 >= nc) {
+                        b0 = __ldg(a.start + row);
+                        b1 = __ldg(a.start + row + 1);
+                        shb = L;
+                    }
+                }
+                // only the own cell filters by slot; the wrapped cell of the own row is a forward neighbour
+                // whose slots may lie below s
+                if (k == 0 && a0 <= s) a0 = s + 1;
+            }
+            const real qy = pi[1] - shy, qz = pi[2] - shz;
+            scan_segment<real>(a.buf.pos, a0, a1, pi[0], qy, qz, range2, part, cnt, s, pairs, npairs, cap, a.flags);
+            scan_segment<real>(a.buf.pos, b0, b1, pi[0] - shb, qy, qz, range2, part, cnt, s, pairs, npairs, cap,
+                               a.flags);
+        }
+    } else {
+        const int nrows = !valid ? 0 : (small ? 9 : 5);
+        const int nrows_warp = __any_sync(full, nrows == 9) ? 9 : 5;
+        for (int rr = 0; rr < nrows_warp; rr++) {  // warp-uniform; rows past a lane's nrows are empty
+            int a0 = 0, a1 = 0, b0 = 0, b1 = 0;
+            real shz = real(0), shy = real(0), shb = real(0);
+            if (rr < nrows) {
+                int dy, dz;
                 if (small) {
-                    a0 = __ldg(a.start + row);
-                    a1 = __ldg(a.start + row + nc);
+                    dy = rr % 3;
+                    dz = rr / 3;
                 } else {
-                    const int x0 = rr == 0 ? cx : cx - 1, x1 = cx + 1;  // the own row starts at the own cell
-                    a0 = __ldg(a.start + row + (x0 < 0 ? 0 : x0));
-                    a1 = __ldg(a.start + row + (x1 >= nc ? nc : x1 + 1));
-                    if (R.periodic) {
-                        if (x0 < 0) {
-                            b0 = __ldg(a.start + row + nc - 1);
-                            b1 = __ldg(a.start + row + nc);
-                            shb = -L;
-                        } else if (x1 >= nc) {
-                            b0 = __ldg(a.start + row);
-                            b1 = __ldg(a.start + row + 1);
-                            shb = L;
+                    dy = rr == 0 ? 0 : (rr == 1 ? 1 : rr - 3);
+                    dz = rr <= 1 ? 0 : 1;
+                }
+                int zz = small ? dz : cz + dz, yy = small ? dy : cy + dy;
+                bool skip = small && (dy >= nc || dz >= nc);
+                if (zz >= nc) {
+                    skip |= !periodic;
+                    shz = L;
+                    zz -= nc;
+                }
+                if (yy < 0 || yy >= nc) {
+                    skip |= !periodic;
+                    shy = yy < 0 ? -L : L;
+                    yy = yy < 0 ? yy + nc : yy - nc;
+                }
+                if (!skip) {
+                    const int row = R.cell_off + nc * (yy + nc * zz);
+                    if (small) {
+                        a0 = __ldg(a.start + row);
+                        a1 = __ldg(a.start + row + nc);
+                    } else {
+                        const int x0 = rr == 0 ? cx : cx - 1, x1 = cx + 1;
+                        a0 = __ldg(a.start + row + (x0 < 0 ? 0 : x0));
+                        a1 = __ldg(a.start + row + (x1 >= nc ? nc : x1 + 1));
+                        if (periodic) {
+                            if (x0 < 0) {
+                                b0 = __ldg(a.start + row + nc - 1);
+                                b1 = __ldg(a.start + row + nc);
+                                shb = -L;
+                            } else if (x1 >= nc) {
+                                b0 = __ldg(a.start + row);
+                                b1 = __ldg(a.start + row + 1);
+                                shb = L;
+                            }
                         }
                     }
+                    if ((small || rr == 0) && a0 <= s) a0 = s + 1;
                 }
-                // only the own cell filters by slot; the wrapped cell of the own row is a forward
-                // neighbour whose slots may lie below s
-                if ((small || rr == 0) && a0 <= s) a0 = s + 1;
             }
-        }
-        for (int seg = 0; seg < 2; seg++) {
-            const int t0 = seg ? b0 : a0, t1 = seg ? b1 : a1;
-            const real shx = seg ? shb : real(0);
-            for (int c0 = t0; __any_sync(0xffffffffu, c0 < t1); c0 += 32) {
-                unsigned mask = 0u;
-                const int ce = t1 < c0 + 32 ? t1 : c0 + 32;
-                // not unrolled: the lanes' trip counts differ, and an unrolled body keeps the short
-                // lanes idle for longer (measured slower)
-                if (!small) {
+            for (int seg = 0; seg < 2; seg++) {
+                const int t0 = seg ? b0 : a0, t1 = seg ? b1 : a1;
+                for (int c0 = t0; __any_sync(full, c0 < t1); c0 += 32) {
+                    unsigned mask = 0u;
+                    const int ce = t1 < c0 + 32 ? t1 : c0 + 32;
 #pragma unroll 1
                     for (int t = c0; t < ce; t++) {
                         real pj[3];
                         load_pos(a.buf.pos + 4 * (size_t)t, pj[0], pj[1], pj[2]);
-                        const real dx = (pi[0] - pj[0]) - shx, dy2 = (pi[1] - pj[1]) - shy, dz2 = (pi[2] - pj[2]) - shz;
-                        if (sep_r2<real>(dx, dy2, dz2) < range2) mask |= 1u << (t - c0);
+                        real dx, dy2, dz2;
+                        if (small) {   // tiny grids: no cell geometry to lean on
+                            dx = min_image_sep<real>(pi[0], pj[0], R.box, R.box_lo, R.l2s, periodic);
+                            dy2 = min_image_sep<real>(pi[1], pj[1], R.box, R.box_lo, R.l2s, periodic);
+                            dz2 = min_image_sep<real>(pi[2], pj[2], R.box, R.box_lo, R.l2s, periodic);
+                        } else {
+                            dx = (pi[0] - (seg ? shb : real(0))) - pj[0];
+                            dy2 = (pi[1] - shy) - pj[1];
+                            dz2 = (pi[2] - shz) - pj[2];
+                        }
+                        if (find_r2(dx, dy2, dz2) < range2) mask |= 1u << (t - c0);
                     }
-                } else {  // tiny grids: no cell geometry to lean on
-#pragma unroll 1
-                    for (int t = c0; t < ce; t++) {
-                        real pj[3];
-                        load_pos(a.buf.pos + 4 * (size_t)t, pj[0], pj[1], pj[2]);
-                        const real dx = min_image_sep<real>(pi[0], pj[0], R.box, R.box_lo, R.l2s, R.periodic);
-                        const real dy2 = min_image_sep<real>(pi[1], pj[1], R.box, R.box_lo, R.l2s, R.periodic);
-                        const real dz2 = min_image_sep<real>(pi[2], pj[2], R.box, R.box_lo, R.l2s, R.periodic);
-                        if (sep_r2<real>(dx, dy2, dz2) < range2) mask |= 1u << (t - c0);
-                    }
+                    warp_append(part, cnt, s, c0, mask, pairs, npairs, cap, a.flags);
                 }
-                warp_pair_flush(buf, kBufCap, &nb, s, c0, mask, pairs, npairs, cap, a.flags);
             }
         }
     }
-    __syncthreads();
-    const int n = nb < kBufCap ? nb : kBufCap;
+    __syncwarp();
+    const int n = cnt < kWarpPairs ? cnt : kWarpPairs;
     if constexpr (FUSED) {
+        // the warp's pairs (s, t) have s among its own slots: when those lie in one replica, so do all of them
+        const int r0 = __shfl_sync(full, r, 0);
+        const int rhint = __all_sync(full, !valid || r == r0) && __shfl_sync(full, valid, 0) ? r0 : -1;
         bool big = false;
-        for (int i = threadIdx.x; i < n; i += THREADS)
-            pair_core<real, kPairSplit>(a, buf[i].x, buf[i].y, acc, lbuf, &lnb, list, list_cap, list_counts, 8u, big);
+        for (int i = lane; i < n; i += 32)
+            pair_core<real, kPairSplit>(a, part[i].x, part[i].y, acc, lbuf, &lnb, list, list_cap, list_counts, 8u, big,
+                                        rhint);
         if (big) atomicOr(a.flags, 2u);
         block_list_flush(lbuf, &lnb, &lbase, list, list_counts, list_cap, a.flags, 8u);
         return;
     }
-    if (threadIdx.x == 0) base = n ? atomicAdd(npairs, (unsigned long long)n) : 0ull;
+    // one list reservation per block (a single counter serves the whole grid): the warps' counts, then each
+    // warp copies its part after the parts of the warps before it
+    __shared__ int wcount[THREADS / 32];
+    if (lane == 0) wcount[threadIdx.x >> 5] = n;
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        if ((long long)(base + i) < cap) pairs[base + i] = buf[i];
+    if (threadIdx.x == 0) {
+        int tot = 0;
+        for (int w = 0; w < THREADS / 32; w++) tot += wcount[w];
+        lbase = tot ? atomicAdd(npairs, (unsigned long long)tot) : 0ull;
+    }
+    int before = 0;
+    for (int w = 0; w < (int)(threadIdx.x >> 5); w++) before += wcount[w];
+    __syncthreads();
+    const unsigned long long base = lbase + (unsigned long long)before;
+    for (int i = lane; i < n; i += 32) {
+        if ((long long)(base + i) < cap) pairs[base + i] = part[i];
         else atomicOr(a.flags, 8u);
     }
 }

@@ -105,6 +105,23 @@ inline double find_range2(double range, double box) {
     return (range + slack) * (range + slack) * (1 + 1e-6);
 }
 
+// Division by a cell count without an integer divide: n / nc = floor(n m / 2^(32+k)) with k the largest
+// integer such that 2^k < nc and m = ceil(2^(32+k) / nc) < 2^32.  With m = 2^(32+k) / nc + e (0 <= e < 1), the
+// product overshoots n / nc by n e / 2^(32+k) < 1 / nc whenever n nc < 2^(32+k), which cannot carry it past the
+// next integer; since 2^(k+1) >= nc, that holds for every n < nc^3 while nc^3 <= 2^31 (nc <= 1290; cell keys
+// are ints).  nc = 1: every key is 0, m = 0.
+inline void nc_magic(int nc, uint32_t &mul, int &sh) {
+    if (nc <= 1) {
+        mul = 0;
+        sh = 0;
+        return;
+    }
+    int k = 0;
+    while ((2ll << k) < nc) k++;
+    mul = (uint32_t)(((1ull << (32 + k)) + (uint64_t)nc - 1) / (uint64_t)nc);
+    sh = k;
+}
+
 template <class real>
 mtg::Replica<real> make_replica(const mtg_replica_desc &d, int off, int cell_off, int nc, int model,
                                 double skin = 0.0) {
@@ -115,6 +132,7 @@ mtg::Replica<real> make_replica(const mtg_replica_desc &d, int off, int cell_off
     R.off = off;
     R.cell_off = cell_off;
     R.nc = nc;
+    nc_magic(nc, R.nc_mul, R.nc_sh);
     R.periodic = d.periodic ? 1 : 0;
     R.model = model;
     R.seed_lo = (uint32_t)d.seed;
@@ -150,10 +168,11 @@ mtg::Replica<real> make_replica(const mtg_replica_desc &d, int off, int cell_off
     return R;
 }
 
-// cells per side so that side >= range (with room for rounding of the cell assignment)
+// cells per side so that side >= range (with room for rounding of the cell assignment), at most 1,024: cells
+// only grow beyond the range, which keeps every pair, and nc^3 keys stay within nc_magic's exact range
 inline int cells_per_side(double box, double range) {
-    int nc = (int)std::floor(box / (range * 1.0001));
-    return std::max(1, nc);
+    const double f = std::floor(box / (range * 1.0001));
+    return !(f >= 1) ? 1 : (f > 1024 ? 1024 : (int)f);
 }
 
 // Cells per side of an analysis grid (pair export, g(r), clusters) for a cut rc: side >= rc, so the
@@ -808,6 +827,8 @@ struct Sys : SysBase {
             reps[r].rc2 = (real)std::max(hs * hs, mk2);
             reps[r].rc2_find = (real)find_range2(std::sqrt(std::max(hs * hs, mk2)), desc[r].box);
             reps[r].nc = reps_obs[r].nc;
+            reps[r].nc_mul = reps_obs[r].nc_mul;
+            reps[r].nc_sh = reps_obs[r].nc_sh;
             reps[r].cell_off = reps_obs[r].cell_off;
             reps[r].cell_scale = reps_obs[r].cell_scale;
         }
