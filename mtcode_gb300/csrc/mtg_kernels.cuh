@@ -1254,6 +1254,21 @@ template <> struct SqSum<float> {
         }
     }
     __device__ __forceinline__ double get(int k) const { return (double)hi[k] + (double)lo[k]; }
+    // the sums of all 32 lanes into lane 0, as float pairs (TwoSum of the high parts, low parts added): the
+    // warp's reduction stays off the FP64 pipe, which on this part runs at a small fraction of the FP32 rate
+    __device__ __forceinline__ void warp_reduce() {
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float oh = __shfl_down_sync(0xffffffffu, hi[k], o), ol = __shfl_down_sync(0xffffffffu, lo[k], o);
+                const float s = __fadd_rn(hi[k], oh), bb = __fsub_rn(s, hi[k]);
+                const float e = __fadd_rn(__fsub_rn(hi[k], __fsub_rn(s, bb)), __fsub_rn(oh, bb));
+                hi[k] = s;
+                lo[k] = __fadd_rn(lo[k], __fadd_rn(ol, e));
+            }
+        }
+    }
 };
 template <> struct SqSum<double> {
     double v_[6];
@@ -1266,6 +1281,11 @@ template <> struct SqSum<double> {
         for (int k = 0; k < 6; k++) v_[k] += v[k] * v[k];
     }
     __device__ __forceinline__ double get(int k) const { return v_[k]; }
+    __device__ __forceinline__ void warp_reduce() {
+#pragma unroll
+        for (int k = 0; k < 6; k++)
+            for (int o = 16; o > 0; o >>= 1) v_[k] += __shfl_down_sync(0xffffffffu, v_[k], o);
+    }
 };
 
 constexpr int kTempPerThread = 8;   // slots per thread: a block of 256 threads sums 2048 slots
@@ -1304,17 +1324,13 @@ __global__ void __launch_bounds__(256) temperature_kernel(Tables<real> tb, Buffe
         }
         acc.add(v[i]);
     }
-    double d[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) d[k] = acc.get(k);
     const unsigned peers = __match_any_sync(0xffffffffu, cur);
     if (peers == 0xffffffffu) {
-        for (int k = 0; k < 6; k++)
-            for (int o = 16; o > 0; o >>= 1) d[k] += __shfl_down_sync(0xffffffffu, d[k], o);
+        acc.warp_reduce();
         if ((threadIdx.x & 31) == 0 && cur >= 0)
-            for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)cur + k, d[k]);
+            for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)cur + k, acc.get(k));
     } else if (cur >= 0) {
-        for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)cur + k, d[k]);
+        for (int k = 0; k < 6; k++) atomicAdd(out + 6 * (size_t)cur + k, acc.get(k));
     }
 }
 
