@@ -398,14 +398,17 @@ def run_e2e(s, W, args, stream, ev0, ev1) -> dict:
         pinned[k][...] = state[k]
     out = {k: torch.empty(v.shape, dtype=torch.float64, pin_memory=True).numpy() for k, v in state.items()}
     k_e2e = E2E_STEPS
+    ev_up, ev_down = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     ev0.record(stream)
     s.initialize(pinned["x"], pinned["p"], pinned["Lb"], pinned["Q"], pinned["Ft"], pinned["Tt"])
+    ev_up.record(stream)
     temps = np.empty((k_e2e, R, 6))
     for i in range(k_e2e):  # Condensate::run: a step, then the temperature read back to the host
         s.step(1)
         temps[i] = s.measured_temperature()
+    ev_down.record(stream)
     st = s.get_state(out)
     ev1.record(stream)
     ev1.synchronize()
@@ -416,6 +419,8 @@ def run_e2e(s, W, args, stream, ev0, ev1) -> dict:
     d2h_state = n * (3 + 3 + 3 + 9 + 3 + 3) * 8
     return {"value": n * k_e2e / wall, "unit": UNIT, "h2d_bytes_per_step": h2d / k_e2e,
             "d2h_bytes_per_step": R * 6 * 8 + d2h_state / k_e2e, "steps": k_e2e,
+            "upload_ms": ev0.elapsed_time(ev_up), "download_ms": ev_down.elapsed_time(ev1),
+            "steps_ms_per_step": ev_up.elapsed_time(ev_down) / k_e2e, "wall_ms": 1e3 * wall,
             "what": "mtg_set_state (host FP64 state) + per step: mtg_step(1) + mtg_temperature (read-back) "
                     "+ mtg_get_state at the end"}
 

@@ -1189,6 +1189,32 @@ __global__ void slot_map_kernel(int ntot, const int *ident, int *slot_of) {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ntot; s += gridDim.x * blockDim.x) slot_of[ident[s]] = s;
 }
 
+// slot order -> host order doubles by global index i, from the slot map (slot_of[i]): the rows are gathered
+// and the doubles written in order, so every warp writes contiguous bytes (the slot-order form scatters its
+// 24-byte rows across the whole array)
+template <class real>
+__global__ void gather_state_kernel(int ntot, Buffers<real> in, const int *slot_of, double *x, double *p, double *Lb,
+                                    double *Q, double *Ft, double *Tt) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ntot; i += gridDim.x * blockDim.x) {
+        const size_t s = (size_t)__ldg(slot_of + i), ii = (size_t)i;
+        Payload<real> P;
+        Row<real> M;
+        P.load(in.pos, in.rota, in.rotb, s);
+        M.load(in.motion + s * kRow);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            if (x) x[3 * ii + k] = (double)P.v[k];
+            if (p) p[3 * ii + k] = (double)M.v[k];
+            if (Lb) Lb[3 * ii + k] = (double)M.v[3 + k];
+            if (Ft) Ft[3 * ii + k] = (double)M.v[6 + k];
+            if (Tt) Tt[3 * ii + k] = (double)M.v[9 + k];
+        }
+        if (Q)
+#pragma unroll
+            for (int k = 0; k < 9; k++) Q[9 * ii + k] = (double)P.v[3 + k];
+    }
+}
+
 // slot order -> host order doubles; which: bit0 x, bit1 p, bit2 Lb, bit3 Q, bit4 Ft, bit5 Tt, bit6 disp
 template <class real>
 __global__ void store_state_kernel(int ntot, Buffers<real> in, double *x, double *p, double *Lb, double *Q, double *Ft,

@@ -270,6 +270,7 @@ struct Sys : SysBase {
     bool capturing = false;          // a step graph is being captured: its launches are counted per replay
     // fixed bonds (CSR by global index) and the id -> slot map the bond pass needs
     int *d_bond_start = nullptr, *d_bond_partner = nullptr, *d_slot_of = nullptr;
+    int *d_gather_map = nullptr;   // slot of each global index, built by get_state when d_slot_of is not kept
     int64_t nbonds = 0;
     double bond_k = 0, bond_r0 = 0;
     int64_t nlaunch = 0;
@@ -471,7 +472,7 @@ struct Sys : SysBase {
         cudaFree(d_bin); cudaFree(d_count); cudaFree(d_start); cudaFree(d_block);
         cudaFree(d_flags); cudaFree(d_draw); cudaFree(d_stage); cudaFree(d_noise); cudaFree(d_obs);
         cudaFree(d_tiles);
-        cudaFree(d_bond_start); cudaFree(d_bond_partner); cudaFree(d_slot_of);
+        cudaFree(d_bond_start); cudaFree(d_bond_partner); cudaFree(d_slot_of); cudaFree(d_gather_map);
         cudaFree(d_skin); cudaFree(d_list); cudaFree(d_list_n); cudaFree(d_home_cell); cudaFree(d_xref);
         cudaFree(d_pairs); cudaFree(d_npairs); cudaFree(d_acc); cudaFree(d_patch_list); cudaFree(d_patch_ctr);
         free_bind();
@@ -1091,9 +1092,19 @@ struct Sys : SysBase {
         size_t n = (size_t)ntot_;
         double *sx = d_stage, *sp = sx + 3 * n, *sl = sp + 3 * n, *sq = sl + 3 * n, *sf = sq + 9 * n, *stt = sf + 3 * n;
         const int g = grid_for(ntot_, 256, occ_stream, sms);
-        mtg::store_state_kernel<real><<<g, 256, 0, st>>>(ntot_, buf[cur], x ? sx : nullptr, p ? sp : nullptr,
-                                                         Lb ? sl : nullptr, Q ? sq : nullptr, Ft ? sf : nullptr,
-                                                         Tt ? stt : nullptr, nullptr);
+        // the slot of every global index: the maintained map when there is one (bonds, single-bond mode),
+        // else a map built here into scratch kept for later calls
+        const int *map = d_slot_of;
+        if (!map) {
+            if (!d_gather_map) MTG_CUDA(cudaMalloc(&d_gather_map, sizeof(int) * (size_t)std::max(ntot_, 1)));
+            mtg::slot_map_kernel<<<g, 256, 0, st>>>(ntot_, buf[cur].ident, d_gather_map);
+            check_launch();
+            nlaunch += 1;
+            map = d_gather_map;
+        }
+        mtg::gather_state_kernel<real><<<g, 256, 0, st>>>(ntot_, buf[cur], map, x ? sx : nullptr, p ? sp : nullptr,
+                                                          Lb ? sl : nullptr, Q ? sq : nullptr, Ft ? sf : nullptr,
+                                                          Tt ? stt : nullptr);
         check_launch();
         nlaunch += 1;
         if (x) MTG_CUDA(cudaMemcpyAsync(x, sx, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
