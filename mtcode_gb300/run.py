@@ -3,7 +3,9 @@
     python -m mtcode_gb300.run --workload c4 --replicas 48 --steps 4 [--precision fp32] [--profile]
 
 Used for quick timing and as the target of profiler captures (it launches the same kernels as the
-benchmark, on a workload of the chosen size).
+benchmark, on a workload of the chosen size).  ``--save-state F`` writes the state after the timed steps to F
+(.npz) and ``--load-state F`` starts from it instead of the seeded start, so a capture of a few launches can
+see an aged (bonded) state without running the steps that aged it.
 """
 from __future__ import annotations
 
@@ -31,6 +33,8 @@ def main() -> None:
                     help="pair-pipeline launch shapes as pairfind_threads,pairforce_blocks_per_sm,"
                          "patch_blocks_per_sm,epilogue_threads,fused_pairs (default: the library's)")
     ap.add_argument("--tune", action="store_true", help="run the launch-shape autotuner before timing")
+    ap.add_argument("--save-state", default=None, help="write the final state (x, p, Lb, Q, Ft, Tt) to this .npz")
+    ap.add_argument("--load-state", default=None, help="start from a state written by --save-state")
     args = ap.parse_args()
     if args.workload == "c4":
         W = workloads.patchy_c4(seed=args.seed, n_replicas=args.replicas)
@@ -41,7 +45,11 @@ def main() -> None:
     n = W.n_total
     z = np.zeros((n, 3))
     with LangevinNVTRGPU(W.replicas, precision=args.precision, force_kernel=args.kernel, neighbor_skin=args.skin) as s:
-        s.initialize(W.x, z, z, W.Q)
+        if args.load_state:
+            st = np.load(args.load_state)
+            s.initialize(st["x"], st["p"], st["Lb"], st["Q"], st["Ft"], st["Tt"])
+        else:
+            s.initialize(W.x, z, z, W.Q)
         if W.bonds is not None:
             s.set_bonds(W.bonds, W.bond_k, W.bond_r0)
         if args.single_bond:
@@ -70,6 +78,8 @@ def main() -> None:
             prof = s.step_profile(max(1, args.steps))
             line += " | " + " ".join(f"{k}={v / max(1, args.steps):.3f}ms" for k, v in prof.items())
         print(line, flush=True)
+        if args.save_state:
+            np.savez(args.save_state, **s.get_state())
 
 
 if __name__ == "__main__":
