@@ -372,6 +372,18 @@ class LangevinNVTRGPU {
         }
     }
 
+    // LangevinNVTR::setup_random_binding(pairs, divs, iny, bo, bm) (LangevinRforceUtil.cpp:749-1010), as
+    // run_singlebond calls it before its loop (Condensate.cpp:478-484): the candidate list of the current state
+    // (the device's own, from every pair within the list cut: the caller's pairs and divs are not read), the
+    // edges that can bind, taken in a random order, each binding two unbound patches; bo (a BinaryBindStore or
+    // anything with isbound / boundto members) receives the bond state.  The order is seeded (mtg_setup_random_binding)
+    // where the reference draws it from std::random_device.
+    template <class Pairs, class Divs, class Patches, class BindStore, class BindingModel>
+    void setup_random_binding(Pairs &, Divs &, Patches &, BindStore &bo, BindingModel &, uint64_t seed = 0) {
+        mtg_adapter::require_ok(h_, mtg_setup_random_binding(h_, seed), "setup_random_binding");
+        getbindings(bo.isbound, bo.boundto);
+    }
+
     // LangevinNVTR::calculate_forces_and_torques3D_onlyone_nonlets (LangevinRforce.cpp:2874-4030) at the
     // current state, with the candidate list rebuilt first: decides the bonds, then F = calculateforces(HS)
     // + bound-pair forces and T = bound-pair torques, as run_singlebond's first call (Condensate.cpp:455-460)

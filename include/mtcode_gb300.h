@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define MTG_API_VERSION 4
+#define MTG_API_VERSION 5
 
 typedef enum {
     MTG_OK = 0,
@@ -368,6 +368,15 @@ mtg_status mtg_get_bind_state(mtg_system *h, int32_t *boundto, uint8_t *isbound)
  * (+ harmonic bonds) + bound-pair forces and T = bound-pair torques (lab), either nullable.  The state
  * does not move.  Synchronising. */
 mtg_status mtg_bind_update(mtg_system *h, double *F, double *T);
+/* LangevinNVTR::setup_random_binding(pairs, divs, iny, bo, bm) (MDBase/Rotational/LangevinRforceUtil.cpp:749-1010,
+ * called by run_singlebond before its loop, Condensate.cpp:484): the candidate list of the current state, every
+ * candidate that passes the edge test as an edge with score scr1 + scr2 + scr3 - log(1e-10 + calculate_score),
+ * and the edges taken in a random order, each binding both patches when both are unbound and its score is below
+ * 4.  The reference draws the order from std::random_device; here it is ascending Philox4x32-10 priority of the
+ * replica-local patch pair (counter (lower patch, higher patch, replica, 0x53455455), key seed), ties by the
+ * lower then the higher patch -- reproducible for a seed.  Bonds already in the state stay.  The state does not
+ * move; the next force pass recomputes the forces.  Synchronising. */
+mtg_status mtg_setup_random_binding(mtg_system *h, uint64_t seed);
 
 /* Neighbour-pair build that allocates no device memory.  It has no counterpart in the reference.
  * It is for callers that cannot allocate device memory when they need the pair list: code that runs

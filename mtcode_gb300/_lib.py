@@ -171,6 +171,7 @@ SIGNATURES = [
     ("mtg_set_bind_state", C.c_int, [_H, _I32, _U8]),
     ("mtg_get_bind_state", C.c_int, [_H, _I32, _U8]),
     ("mtg_bind_update", C.c_int, [_H, _D, _D]),
+    ("mtg_setup_random_binding", C.c_int, [_H, C.c_uint64]),
 ]
 
 _lib = None

@@ -422,6 +422,15 @@ mtg_status mtg_bind_update(mtg_system *h, double *F, double *T) {
     return MTG_OK;
 }
 
+mtg_status mtg_setup_random_binding(mtg_system *h, uint64_t seed) {
+    MTG_GUARD(h, {
+        h->impl->setup_random_binding(seed);
+        const uint32_t f = h->impl->flags();
+        if (f & MTG_FLAG_BIND) throw Fail{MTG_ERR_CAPACITY, bind_failure(f)};
+    });
+    return MTG_OK;
+}
+
 uint32_t mtg_flags(mtg_system *h) {
     if (!h) return 0;
     try {

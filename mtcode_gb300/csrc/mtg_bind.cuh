@@ -498,6 +498,112 @@ __global__ void __launch_bounds__(kLargeThreads) bind_large_kernel(ForceArgs<rea
     }
 }
 
+// ------------------------------------------------------------------ random initial binding
+// LangevinNVTR::setup_random_binding (LangevinRforceUtil.cpp:749-1010): every candidate patch pair that passes
+// this update's edge test is an edge with score scr1 + scr2 + scr3 + scr4, scr4 = -log(1e-10 + the binding
+// model's calculate_score); the edges are shuffled and taken in that order, each binding its two patches when
+// both are unbound and its score is below 4.  The reference shuffles with std::random_device; here the order is
+// ascending (Philox priority of the replica-local patch pair, lower patch, higher patch), seeded, so the result
+// is reproducible and the oracle's greedy walk in the same order matches it.  Taking edges in a fixed order is
+// the greedy matching of that order, which rounds of mutual choices reach on the GPU: every unbound patch picks
+// its first live edge, and an edge both ends picked binds (the first live edge of the whole replica always is
+// one, so every round binds, and the edges bound are the ones the greedy walk binds).
+
+// -log(1e-10 + calculate_score(wp1, wp2, before)) per doublet row and prior state, computed on the host
+struct SetupScores {
+    double scr4[6][2];
+};
+
+// the doublet row calculate_score reads for (wp1 of the lower particle, wp2): BindingModelSingle one row;
+// BindingModelBinary 11 if both are below div, 12 if only wp1 is, else 22 (BindingModelBinary.cpp:194-230);
+// BindingModelTernary the sorted species pair (BindingModelTernary.cpp:596-640)
+__device__ __forceinline__ int score_row(const BindModel &m, int i1, int i2) {
+    if (m.rule == 0) return 0;
+    if (m.rule == 1) return (i1 < m.div1 && i2 < m.div1) ? 0 : (i1 < m.div1 ? 1 : 3);
+    int s1 = species(m, i1), s2 = species(m, i2);
+    if (s2 < s1) { const int t = s1; s1 = s2; s2 = t; }
+    return pair_row(s1, s2);
+}
+
+__device__ __forceinline__ uint32_t setup_priority(uint64_t seed, uint32_t replica, uint32_t lo, uint32_t hi) {
+    return philox4x32_10(make_uint4(lo, hi, replica, 0x53455455u), make_uint2((uint32_t)seed, (uint32_t)(seed >> 32))).x;
+}
+
+// per adjacency entry of this update: whether the edge can bind (edge test and score below 4) and its priority
+template <class real>
+__global__ void __launch_bounds__(256) setup_edges_kernel(ForceArgs<real> a, BindState S, SetupScores sc,
+                                                          uint64_t seed, uint32_t *prio, unsigned char *ok) {
+    const unsigned stamp = (unsigned)S.ctr[2];
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < S.ptot; p += gridDim.x * blockDim.x) {
+        const int dp = adj_count(S.deg, p, stamp);
+        if (!dp) continue;
+        const int r = find_replica(S.patch_slot, S.nrep, p);
+        const BindRep &B = S.reps[r];
+        const Replica<real> &R = a.tb.reps[r];
+        const Model<real> &M = a.tb.models[R.model];
+        for (int k = 0; k < dp; k++) {
+            const int2 ad = S.adj[(size_t)p * kAdjCap + k];
+            const int q = ad.x;
+            const PatchPair c = patch_pair_of<real>(a, B, M, R.off, p, q);
+            double scr = 0;
+            bool e = exact_edge<real>(B, a.buf.pos, a.buf.rota, a.buf.rotb, c.s1, c.s2, c.o1, c.o2, c.potn,
+                                      disp2_of(B.disp[c.potn], ad.y), &scr);
+            // wp1 is the patch of the lower particle index (the candidate list's order)
+            int l1, t1, k1, l2, t2, k2;
+            patch_owner<real>(B, M, p - B.patch_off, l1, t1, k1);
+            patch_owner<real>(B, M, q - B.patch_off, l2, t2, k2);
+            const int wp1 = (l1 < l2 ? p : q) - B.patch_off, wp2 = (l1 < l2 ? q : p) - B.patch_off;
+            const bool before = S.isbound[p] && S.isbound[q] && S.boundto[p] == q && S.boundto[q] == p;
+            e = e && __dadd_rn(scr, sc.scr4[score_row(*S.model, wp1, wp2)][before ? 1 : 0]) < 4.0;
+            const int lo = (p < q ? p : q) - B.patch_off, hi = (p < q ? q : p) - B.patch_off;
+            ok[(size_t)p * kAdjCap + k] = e ? 1 : 0;
+            prio[(size_t)p * kAdjCap + k] = setup_priority(seed, (uint32_t)r, (uint32_t)lo, (uint32_t)hi);
+        }
+    }
+}
+
+// one round, first half: every unbound patch's first live edge (to an unbound patch), in (priority, lower
+// patch, higher patch) order
+__global__ void __launch_bounds__(256) setup_choose_kernel(BindState S, const uint32_t *prio, const unsigned char *ok,
+                                                           int *best) {
+    const unsigned stamp = (unsigned)S.ctr[2];
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < S.ptot; p += gridDim.x * blockDim.x) {
+        int b = -1;
+        uint32_t bp = 0u;
+        int blo = 0, bhi = 0;
+        if (!S.isbound[p]) {
+            const int dp = adj_count(S.deg, p, stamp);
+            for (int k = 0; k < dp; k++) {
+                const size_t e = (size_t)p * kAdjCap + k;
+                const int q = S.adj[e].x;
+                if (!ok[e] || S.isbound[q]) continue;
+                const uint32_t pr = prio[e];
+                const int lo = p < q ? p : q, hi = p < q ? q : p;
+                if (b < 0 || pr < bp || (pr == bp && (lo < blo || (lo == blo && hi < bhi)))) {
+                    b = q;
+                    bp = pr;
+                    blo = lo;
+                    bhi = hi;
+                }
+            }
+        }
+        best[p] = b;
+    }
+}
+
+// second half: an edge both of whose ends chose it binds; `bound` counts this round's bonds
+__global__ void __launch_bounds__(256) setup_commit_kernel(BindState S, const int *best, unsigned long long *bound) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < S.ptot; p += gridDim.x * blockDim.x) {
+        const int q = best[p];
+        if (q <= p || best[q] != p) continue;
+        S.isbound[p] = 1;
+        S.isbound[q] = 1;
+        S.boundto[p] = q;
+        S.boundto[q] = p;
+        atomicAdd(bound, 1ull);
+    }
+}
+
 }  // namespace
 
 }  // namespace mtg

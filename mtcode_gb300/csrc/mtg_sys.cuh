@@ -307,6 +307,7 @@ struct Sys : SysBase {
     bool single_bond = false;
     int ptot = 0, patch_every = 10, scratch_threads = 0;
     std::vector<int> patch_slot;
+    mtg::BindModel bind_model_h;   // the binding model's tables (host copy)
     std::vector<mtg::Replica<real>> reps_full;   // replica constants with the full patch force
     mtg::BindRep *d_brep = nullptr;
     mtg::BindModel *d_bmodel = nullptr;
@@ -808,6 +809,7 @@ struct Sys : SysBase {
         MTG_CUDA(cudaMalloc(&d_scratch, sizeof(int) * (size_t)mtg::kScratchInts * scratch_threads));
         MTG_CUDA(cudaMemcpy(d_brep, br.data(), sizeof(mtg::BindRep) * nrep, cudaMemcpyHostToDevice));
         MTG_CUDA(cudaMemcpy(d_bmodel, &hm, sizeof(hm), cudaMemcpyHostToDevice));
+        bind_model_h = hm;
         MTG_CUDA(cudaMemcpy(d_patch_slot, pslot.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice));
         MTG_CUDA(cudaMemset(d_bctr, 0, sizeof(unsigned long long) * mtg::kBindCounters));
         MTG_CUDA(cudaMemset(d_deg, 0, sizeof(unsigned long long) * np));
@@ -881,6 +883,83 @@ struct Sys : SysBase {
                 if (ib) ib[o + i] = b[(size_t)(o + i)];
             }
         }
+    }
+
+    // -log(1e-10 + calculate_score(wp1, wp2, before)) of every doublet row: BindingModelSingle returns
+    // off_rate when the pair is bound to each other, else on_rate (BindingModelSingle.cpp:25-36; its table
+    // holds them as [0] = [2] = off, [1] = [3] = on); BindingModelBinary the table's [3] / [0]
+    // (BindingModelBinary.cpp:194-230); BindingModelTernary [before * 2 + 1] (BindingModelTernary.cpp:596-640)
+    mtg::SetupScores setup_scores() const {
+        mtg::SetupScores sc;
+        const mtg::BindModel &m = bind_model_h;
+        for (int row = 0; row < 6; row++)
+            for (int before = 0; before < 2; before++) {
+                const double *rt = m.drate[m.rule == 0 ? 0 : row];
+                const double score = m.rule == 0 ? (before ? rt[2] : rt[1])
+                                                 : (m.rule == 1 ? (before ? rt[3] : rt[0]) : rt[before * 2 + 1]);
+                sc.scr4[row][before] = -std::log(1e-10 + score);
+            }
+        return sc;
+    }
+
+    // LangevinNVTR::setup_random_binding (LangevinRforceUtil.cpp:749-1010) with a seeded order (mtg_bind.cuh):
+    // this update's edges at the current state (candidate list rebuilt), then rounds of mutual choices until
+    // a round binds nothing
+    void setup_random_binding(uint64_t seed) override {
+        if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_setup_random_binding: no state has been set"};
+        MTG_REQUIRE(single_bond, "mtg_setup_random_binding: the handle is not in single-bond mode");
+        if (!cells_valid) rebuild_cells(false);
+        enqueue_bind_begin(cur, 1, 0);
+        mtg::ForceArgs<real> a = force_args(cur, 0);
+        a.bind_deg = d_deg;
+        a.bind_adj = d_adj;
+        a.bind_ctr = d_bctr;
+        a.bind_touched = d_touched;
+        a.bind_tcap = tcap;
+        a.bind_listed = 0;
+        mtg::force_kernel<real, mtg::kModeEdges><<<grid_for(ntot_, 128, occ_force, sms), 128, 0, st>>>(a);
+        check_launch();
+        counted(1);
+        const size_t np = (size_t)std::max(ptot, 1);
+        uint32_t *d_prio = nullptr;
+        unsigned char *d_ok = nullptr;
+        int *d_best = nullptr;
+        unsigned long long *d_cnt = nullptr;
+        auto release = [&]() {
+            cudaFree(d_prio);
+            cudaFree(d_ok);
+            cudaFree(d_best);
+            cudaFree(d_cnt);
+        };
+        try {
+            MTG_CUDA(cudaMalloc(&d_prio, sizeof(uint32_t) * mtg::kAdjCap * np));
+            MTG_CUDA(cudaMalloc(&d_ok, mtg::kAdjCap * np));
+            MTG_CUDA(cudaMalloc(&d_best, sizeof(int) * np));
+            MTG_CUDA(cudaMalloc(&d_cnt, sizeof(unsigned long long)));
+            const mtg::BindState S = bind_state();
+            const int g = grid_for(ptot, 256, occ_stream, sms);
+            mtg::setup_edges_kernel<real><<<g, 256, 0, st>>>(a, S, setup_scores(), seed, d_prio, d_ok);
+            check_launch();
+            counted(1);
+            bool done = false;
+            for (int round = 0; round < 4096 && !done; round++) {   // every round binds at least one edge
+                MTG_CUDA(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long), st));
+                mtg::setup_choose_kernel<<<g, 256, 0, st>>>(S, d_prio, d_ok, d_best);
+                mtg::setup_commit_kernel<<<g, 256, 0, st>>>(S, d_best, d_cnt);
+                check_launch();
+                counted(2);
+                unsigned long long bound = 0;
+                MTG_CUDA(cudaMemcpyAsync(&bound, d_cnt, sizeof(bound), cudaMemcpyDeviceToHost, st));
+                MTG_CUDA(cudaStreamSynchronize(st));
+                done = bound == 0;
+            }
+            if (!done) throw Fail{MTG_ERR_TIMEOUT, "mtg_setup_random_binding: the matching did not finish in 4096 rounds"};
+        } catch (...) {
+            release();
+            throw;
+        }
+        release();
+        forces_ready = false;
     }
 
     void bind_update(double *F, double *T) override {

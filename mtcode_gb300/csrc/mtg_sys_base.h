@@ -61,6 +61,7 @@ struct SysBase {
     virtual void set_bind_state(const int32_t *, const uint8_t *) = 0;
     virtual void get_bind_state(int32_t *, uint8_t *) = 0;
     virtual void bind_update(double *, double *) = 0;
+    virtual void setup_random_binding(uint64_t seed) = 0;
     virtual void phase_forces(int, double *, double *) = 0;
     virtual void phase_langevin(double *, double *, const double *) = 0;
     virtual void phase_halfkick(const double *, const double *) = 0;

@@ -275,6 +275,11 @@ class LangevinNVTRGPU:
         _check(self._h, _lib.lib().mtg_bind_update(self._h, dptr(F), dptr(T)))
         return F, T
 
+    def setup_random_binding(self, seed: int = 0) -> None:
+        """LangevinNVTR::setup_random_binding at the current state: the candidate edges that can bind, taken in
+        a seeded random order, each binding two unbound patches (mtg_setup_random_binding)."""
+        _check(self._h, _lib.lib().mtg_setup_random_binding(self._h, int(seed) & 0xFFFFFFFFFFFFFFFF))
+
     def calculate_forces_and_torques3D(self, with_energy: bool = False):
         """MD::calculateforces(HSPotential) + LangevinNVTR::calculate_forces_and_torques3D: F, T (lab)."""
         F = np.empty((self.n, 3))

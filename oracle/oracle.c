@@ -1239,6 +1239,124 @@ int orc_bind_update(const orc_params *P, const double *x, const double *Q, const
     return status;
 }
 
+/* calculate_score(i1, i2, before) of the binding model in table form: BindingModelSingle off_rate if the pair
+ * is bound to each other, else on_rate (BindingModelSingle.cpp:25-36; the table holds [0] = [2] = off,
+ * [1] = [3] = on); BindingModelBinary doubr11 if both indices are below div, doubr12 if only i1 is, else doubr22,
+ * entry [before * 2 + 1] if bound, [before * 2 + 0] if not (BindingModelBinary.cpp:194-230);
+ * BindingModelTernary the sorted species pair's [before * 2 + 1] (BindingModelTernary.cpp:596-640) */
+static double orc_calculate_score(const orc_binding *B, int i1, int i2, int before)
+{
+    if (B->rule == 0) return before ? B->drate[0][2] : B->drate[0][1];
+    if (B->rule == 1) {
+        int row = (i1 < B->div1 && i2 < B->div1) ? 0 : (i1 < B->div1 ? 1 : 3);
+        return B->drate[row][before * 2 + (before ? 1 : 0)];
+    }
+    int s1 = orc_species(B, i1), s2 = orc_species(B, i2);
+    if (s2 < s1) { int t = s1; s1 = s2; s2 = t; }
+    return B->drate[orc_pair_row(s1, s2)][before * 2 + 1];
+}
+
+/* one edge of setup_random_binding: its patches, score and place in the seeded order */
+typedef struct { int a, b; double scr; uint32_t prio; int lo, hi; } orc_sedge;
+
+static int orc_sedge_cmp(const void *x, const void *y)
+{
+    const orc_sedge *e = (const orc_sedge *)x, *f = (const orc_sedge *)y;
+    if (e->prio != f->prio) return e->prio < f->prio ? -1 : 1;
+    if (e->lo != f->lo) return e->lo < f->lo ? -1 : 1;
+    return e->hi < f->hi ? -1 : (e->hi > f->hi ? 1 : 0);
+}
+
+uint32_t orc_setup_priority(uint64_t seed, uint32_t replica, uint32_t lo, uint32_t hi)
+{
+    uint32_t ctr[4] = {lo, hi, replica, 0x53455455u};
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    uint32_t o[4];
+    orc_philox4x32_10(ctr, key, o);
+    return o[0];
+}
+
+/* the edges of setup_random_binding and their scores (LangevinRforceUtil.cpp:781-930): the edge test of the
+ * bond update, score scr1 + scr2 + scr3 + scr4; returns the count */
+static long orc_setup_edge_list(const orc_params *P, const double *x, const double *Q, const orc_patchint *list,
+                                long nl, const orc_binding *B, uint64_t seed, uint32_t replica, const int *boundto,
+                                const unsigned char *isbound, orc_sedge *edges)
+{
+    const orc_model *M = P->model;
+    const double mk = orc_max_check(M);
+    long ne = 0;
+    for (long q = 0; q < nl; q++) {
+        const orc_patchint *e = list + q;
+        double un[3];
+        double dis = orc_distance_vector(P, x, e->p1, e->p2, un);
+        if (!(dis < SQR(mk))) continue;
+        dis = sqrt(dis);
+        un[0] /= dis; un[1] /= dis; un[2] /= dis;
+        int wp1 = e->wp1, wp2 = e->wp2, potn = e->potn;
+        int k1 = orc_type_of(M, e->p1), k2 = orc_type_of(M, e->p2);
+        int ps = orc_pot_start(M, k1, k2), n2 = M->patches_per_type[k2];
+        int a = (potn - ps) / n2, b = (potn - ps) % n2;
+        double m1[3], m2[3];
+        orc_lab_patch(M->orient[orc_orient_start(M, k1) + a], Q + 9 * e->p1, m1);
+        orc_lab_patch(M->orient[orc_orient_start(M, k2) + b], Q + 9 * e->p2, m2);
+        double disp = 1.4 * M->dis[potn], thetam = M->thetam[potn], ctm = cos(thetam);
+        double ai = -(m1[0] * un[0] + m1[1] * un[1] + m1[2] * un[2]);
+        double aj = (m2[0] * un[0] + m2[1] * un[1] + m2[2] * un[2]);
+        int cond1 = boundto[wp1] == wp2 && boundto[wp2] == wp1;
+        int b1 = isbound[wp1] != 0, b2 = isbound[wp2] != 0;
+        double disp2;
+        if (b1 && b2 && cond1) disp2 = disp;
+        else if (b1 && b2 && !cond1) disp2 = 0.5 * disp;
+        else if (b1 != b2) disp2 = 0.7 * disp;
+        else disp2 = disp;
+        if (ai > ctm && aj > ctm && dis < disp2) {
+            double scr1 = 1 - (ai - cos(thetam));
+            double scr2 = 1 - (aj - cos(thetam));
+            double scr3 = 2 * (dis / disp2);
+            double scr4 = -log(1E-10 + orc_calculate_score(B, wp1, wp2, b1 && b2 && cond1));
+            orc_sedge *s = edges + ne++;
+            s->a = wp1; s->b = wp2; s->scr = scr1 + scr2 + scr3 + scr4;
+            s->lo = wp1 < wp2 ? wp1 : wp2; s->hi = wp1 < wp2 ? wp2 : wp1;
+            s->prio = orc_setup_priority(seed, replica, (uint32_t)s->lo, (uint32_t)s->hi);
+        }
+    }
+    return ne;
+}
+
+long orc_setup_edges(const orc_params *P, const double *x, const double *Q, const orc_patchint *list, long nl,
+                     const orc_binding *B, const int *boundto, const unsigned char *isbound, int *ab, double *scr)
+{
+    orc_sedge *edges = (orc_sedge *)malloc(sizeof(orc_sedge) * (size_t)(nl + 1));
+    long ne = orc_setup_edge_list(P, x, Q, list, nl, B, 0, 0, boundto, isbound, edges);
+    for (long i = 0; i < ne; i++) {
+        ab[2 * i] = edges[i].a;
+        ab[2 * i + 1] = edges[i].b;
+        scr[i] = edges[i].scr;
+    }
+    free(edges);
+    return ne;
+}
+
+int orc_setup_random_binding(const orc_params *P, const double *x, const double *Q, const orc_patchint *list, long nl,
+                             const orc_binding *B, uint64_t seed, uint32_t replica, int *boundto,
+                             unsigned char *isbound)
+{
+    orc_sedge *edges = (orc_sedge *)malloc(sizeof(orc_sedge) * (size_t)(nl + 1));
+    long ne = orc_setup_edge_list(P, x, Q, list, nl, B, seed, replica, boundto, isbound, edges);
+    /* the reference's std::shuffle of the edges, here the seeded order; then the greedy walk
+     * (LangevinRforceUtil.cpp:985-1005) */
+    qsort(edges, (size_t)ne, sizeof(orc_sedge), orc_sedge_cmp);
+    for (long i = 0; i < ne; i++) {
+        int wp1 = edges[i].a, wp2 = edges[i].b;
+        if (!isbound[wp1] && !isbound[wp2] && edges[i].scr < 4.) {
+            isbound[wp1] = 1; isbound[wp2] = 1;
+            boundto[wp1] = wp2; boundto[wp2] = wp1;
+        }
+    }
+    free(edges);
+    return 0;
+}
+
 static long orc_patch_list_alloc(const orc_params *P, const double *x, const double *Q, const int *pairs, long np,
                                  double max_ang, orc_patchint **out)
 {

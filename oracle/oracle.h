@@ -177,6 +177,19 @@ int orc_bind_update(const orc_params *P, const double *x, const double *Q, const
                     const orc_binding *B, int rng, uint64_t seed, uint32_t replica, uint64_t draw, int *boundto,
                     unsigned char *isbound, double *F, double *T);
 
+/* LangevinNVTR::setup_random_binding(pairs, divs, iny, bo, bm) (LangevinRforceUtil.cpp:749-1010) on the
+ * candidate list: edges as the bond update's edge test finds them, score scr1 + scr2 + scr3 - log(1e-10 +
+ * calculate_score), then the greedy walk that binds two unbound patches when the score is below 4.  The
+ * reference walks the edges in a std::random_device shuffle; here in ascending (orc_setup_priority(seed,
+ * replica, lower patch, higher patch), lower patch, higher patch), the library's seeded order. */
+uint32_t orc_setup_priority(uint64_t seed, uint32_t replica, uint32_t lo, uint32_t hi);
+/* its edges (wp1, wp2 pairs into ab, 2 per edge) with their scores; returns the count (at most nl) */
+long orc_setup_edges(const orc_params *P, const double *x, const double *Q, const orc_patchint *list, long nl,
+                     const orc_binding *B, const int *boundto, const unsigned char *isbound, int *ab, double *scr);
+int orc_setup_random_binding(const orc_params *P, const double *x, const double *Q, const orc_patchint *list, long nl,
+                             const orc_binding *B, uint64_t seed, uint32_t replica, int *boundto,
+                             unsigned char *isbound);
+
 /* The run_singlebond loop (Condensate.cpp:422-560) on one system, nsteps from loop index i0:
  * pairs within pair_cut rebuilt when i > 0 and i % pair_every == 0 (and at the start), the candidate
  * list when i > 0 and i % patch_every == 0 (and at the start); F = central forces, T = 0, then

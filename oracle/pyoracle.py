@@ -161,6 +161,14 @@ def orc() -> C.CDLL:
         L.orc_bind_update.restype = C.c_int
         L.orc_bind_update.argtypes = [P, _D, _D, _I, C.c_long, C.POINTER(OrcBinding), C.c_int, C.c_uint64,
                                       C.c_uint32, C.c_uint64, _I, C.POINTER(C.c_ubyte), _D, _D]
+        L.orc_setup_priority.restype = C.c_uint32
+        L.orc_setup_priority.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32]
+        L.orc_setup_edges.restype = C.c_long
+        L.orc_setup_edges.argtypes = [P, _D, _D, _I, C.c_long, C.POINTER(OrcBinding), _I, C.POINTER(C.c_ubyte), _I,
+                                      _D]
+        L.orc_setup_random_binding.restype = C.c_int
+        L.orc_setup_random_binding.argtypes = [P, _D, _D, _I, C.c_long, C.POINTER(OrcBinding), C.c_uint64,
+                                               C.c_uint32, _I, C.POINTER(C.c_ubyte)]
         L.orc_run_singlebond.restype = C.c_int
         L.orc_run_singlebond.argtypes = [P, _D, _D, _D, _D, _D, _D, _I, C.POINTER(C.c_ubyte), C.POINTER(OrcBinding),
                                          C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
@@ -397,6 +405,29 @@ class System:
                                    boundto.ctypes.data_as(_I), isbound.ctypes.data_as(_U8), _d(F), _d(T))
         return st, F, T
 
+    def setup_random_binding(self, x, Q, plist, bind: OrcBinding, boundto, isbound, seed: int = 0,
+                             replica: int = 0) -> int:
+        """setup_random_binding on a candidate list in the library's seeded order; boundto / isbound (int32 /
+        uint8) are updated in place."""
+        pl = np.ascontiguousarray(plist, dtype=np.intc).reshape(-1, 5)
+        assert boundto.dtype == np.intc and isbound.dtype == np.uint8
+        return orc().orc_setup_random_binding(
+            C.byref(self.params), _d(np.ascontiguousarray(x, float)), _d(np.ascontiguousarray(Q, float)),
+            pl.ctypes.data_as(_I), len(pl), C.byref(bind), int(seed) & 0xFFFFFFFFFFFFFFFF, int(replica),
+            boundto.ctypes.data_as(_I), isbound.ctypes.data_as(_U8))
+
+    def setup_edges(self, x, Q, plist, bind: OrcBinding, boundto, isbound):
+        """setup_random_binding's edges: (m, 2) patch pairs (wp1, wp2) and their scores (m,)."""
+        pl = np.ascontiguousarray(plist, dtype=np.intc).reshape(-1, 5)
+        bt = np.ascontiguousarray(boundto, dtype=np.intc)
+        ib = np.ascontiguousarray(isbound, dtype=np.uint8)
+        ab = np.empty((max(len(pl), 1), 2), dtype=np.intc)
+        scr = np.empty(max(len(pl), 1))
+        m = orc().orc_setup_edges(C.byref(self.params), _d(np.ascontiguousarray(x, float)),
+                                  _d(np.ascontiguousarray(Q, float)), pl.ctypes.data_as(_I), len(pl), C.byref(bind),
+                                  bt.ctypes.data_as(_I), ib.ctypes.data_as(_U8), ab.ctypes.data_as(_I), _d(scr))
+        return ab[:m].copy(), scr[:m].copy()
+
     def run_singlebond(self, state: dict, bind: OrcBinding, nsteps: int, max_ang: float, i0: int = 0,
                        pair_cut: float = 2.5, pair_every: int = 20, patch_every: int = 10, init: bool = False,
                        init_draw: int = 0, noise_mode: int = 0, noise=None, seed: int = 0, replica: int = 0,
@@ -466,6 +497,10 @@ def ref() -> C.CDLL | None:
         L.ref_singlebond.argtypes = [C.c_int, C.c_double, C.c_int, _D, _D, C.c_int, C.c_double, C.c_int, C.c_double,
                                      C.c_double, C.c_double, C.c_int, _I, _I, _D, _D, C.c_int, _D, _I, _U8, C.c_uint,
                                      _D, _D, _I, C.c_long, _D, _D]
+        L.ref_setup_random_binding.restype = C.c_long
+        L.ref_setup_random_binding.argtypes = [C.c_int, C.c_double, C.c_int, _D, _D, C.c_int, C.c_double, C.c_int,
+                                               C.c_double, C.c_double, C.c_double, C.c_int, _I, _I, _D, _D, C.c_int,
+                                               _D, _I, _U8, _I, C.c_long]
         _ref = L
     return _ref
 
@@ -477,6 +512,27 @@ def ref_model_args(model):
     orient = np.ascontiguousarray(np.asarray(model.orient, float).reshape(-1, 3))
     params = np.ascontiguousarray(np.asarray(model.params, float).reshape(-1, 3))
     return 2, 0.0, 0.0, 0.0, len(ppt), ppt, npt, orient, params
+
+
+def ref_setup_random_binding(spec, x, Q, pair_cut: float, bm_kind: int, args, boundto, isbound):
+    """The reference's calculate_patch_list + setup_random_binding (std::random_device order) on a copy of the bind
+    state.  Returns (boundto, isbound)."""
+    L = ref()
+    n = int(spec.n)
+    _, att, dis, th, nt, ppt, npt, orient, params = ref_model_args(spec.model)
+    bt = np.ascontiguousarray(boundto, dtype=np.intc).copy()
+    ib = np.ascontiguousarray(isbound, dtype=np.uint8).copy()
+    cap = 16 * 16 * n + 64
+    plist = np.empty((cap, 5), dtype=np.intc)
+    a = np.ascontiguousarray(np.asarray(args, float).reshape(-1))
+    ncell = max(1, int(math.floor(float(spec.box) / pair_cut)))
+    npl = L.ref_setup_random_binding(n, float(spec.box), int(bool(spec.periodic)), _d(np.ascontiguousarray(x, float)),
+                                     _d(np.ascontiguousarray(Q, float)), ncell, float(pair_cut), 2, att, dis, th, nt,
+                                     ppt.ctypes.data_as(_I), npt.ctypes.data_as(_I), _d(orient), _d(params),
+                                     int(bm_kind), _d(a), bt.ctypes.data_as(_I), ib.ctypes.data_as(_U8),
+                                     plist.ctypes.data_as(_I), cap)
+    assert npl <= cap, "candidate list larger than the buffer"
+    return bt, ib
 
 
 def ref_singlebond(spec, x, Q, pair_cut: float, bm_kind: int, args, boundto, isbound, seed: int):

@@ -346,11 +346,40 @@ void ref_run(int n, double box, int periodic, double *x, double *p, double *Lb, 
 // the candidate list (plist, 5 ints per entry, up to plist_cap; the count is returned), the model's rate
 // vectors in tables (doubr11, 12, 13, 22, 23, 33 then tripr111 ... 333, zero where the model has none) and
 // max_ang / max_check in caps[0..1].
+static long singlebond_call(int n, double box, int periodic, const double *x, const double *Q, int ncell,
+                            double pair_cut, int kind, double att, double dis, double thetam, int n_types,
+                            const int *ppt, const int *npt, const double *orient, const double *params, int bm_kind,
+                            const double *args, int *boundto, unsigned char *isbound, unsigned seed, double *F,
+                            double *T, int *plist, long plist_cap, double *tables, double *caps, int setup);
+
 long ref_singlebond(int n, double box, int periodic, const double *x, const double *Q, int ncell, double pair_cut,
                     int kind, double att, double dis, double thetam, int n_types, const int *ppt, const int *npt,
                     const double *orient, const double *params, int bm_kind, const double *args, int *boundto,
                     unsigned char *isbound, unsigned seed, double *F, double *T, int *plist, long plist_cap,
                     double *tables, double *caps)
+{
+    return singlebond_call(n, box, periodic, x, Q, ncell, pair_cut, kind, att, dis, thetam, n_types, ppt, npt, orient,
+                           params, bm_kind, args, boundto, isbound, seed, F, T, plist, plist_cap, tables, caps, 0);
+}
+
+// LangevinNVTR::setup_random_binding(opairs, runs_diff, *pots, bbs, *bm) (LangevinRforceUtil.cpp:749-1010) on the
+// same candidate list as ref_singlebond builds (Condensate.cpp:478-484); its edge order comes from
+// std::random_device, so the result is one random draw of the reference's.  boundto / isbound updated in place.
+long ref_setup_random_binding(int n, double box, int periodic, const double *x, const double *Q, int ncell,
+                              double pair_cut, int kind, double att, double dis, double thetam, int n_types,
+                              const int *ppt, const int *npt, const double *orient, const double *params, int bm_kind,
+                              const double *args, int *boundto, unsigned char *isbound, int *plist, long plist_cap)
+{
+    return singlebond_call(n, box, periodic, x, Q, ncell, pair_cut, kind, att, dis, thetam, n_types, ppt, npt, orient,
+                           params, bm_kind, args, boundto, isbound, 0u, nullptr, nullptr, plist, plist_cap, nullptr,
+                           nullptr, 1);
+}
+
+static long singlebond_call(int n, double box, int periodic, const double *x, const double *Q, int ncell,
+                            double pair_cut, int kind, double att, double dis, double thetam, int n_types,
+                            const int *ppt, const int *npt, const double *orient, const double *params, int bm_kind,
+                            const double *args, int *boundto, unsigned char *isbound, unsigned seed, double *F,
+                            double *T, int *plist, long plist_cap, double *tables, double *caps, int setup)
 {
     vector<double> zeros3(3 * (size_t)n, 0.0);
     LangevinNVTR *b = make_system(n, box, periodic, x, zeros3.data(), zeros3.data(), Q, 0.005, 1, 1, 1);
@@ -432,13 +461,17 @@ long ref_singlebond(int n, double box, int periodic, const double *x, const doub
         plist[5 * q + 3] = opairs[q].patch_index1;
         plist[5 * q + 4] = opairs[q].patch_index2;
     }
-    matrix<double> Fm(n, 3), Tm(n, 3);
-    Fm.reset_parallel(0.0);
-    Tm.reset_parallel(0.0);
-    srand(seed);
-    b->calculate_forces_and_torques3D_onlyone_nonlets(opairs, runs_diff, *pots, bbs, *bm, Fm, Tm);
-    from_mat(Fm, F, n, 3);
-    from_mat(Tm, T, n, 3);
+    if (setup) {
+        b->setup_random_binding(opairs, runs_diff, *pots, bbs, *bm);
+    } else {
+        matrix<double> Fm(n, 3), Tm(n, 3);
+        Fm.reset_parallel(0.0);
+        Tm.reset_parallel(0.0);
+        srand(seed);
+        b->calculate_forces_and_torques3D_onlyone_nonlets(opairs, runs_diff, *pots, bbs, *bm, Fm, Tm);
+        from_mat(Fm, F, n, 3);
+        from_mat(Tm, T, n, 3);
+    }
     for (int i = 0; i < nh; i++) {
         isbound[i] = bbs.isbound[i] ? 1 : 0;
         boundto[i] = bbs.boundto[i];

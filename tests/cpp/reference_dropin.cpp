@@ -95,6 +95,10 @@ void run_singlebond_on_gpu(double l, int N, matrix<double> &dat, int runtime, Te
     bbs.isbound = isbound;
     bbs.boundto = boundto;
     obj.setbindings(bbs.isbound, bbs.boundto);
+    // run_singlebond's random initial binding (Condensate.cpp:478-484), with its argument types
+    vector<patchint> opairs;
+    vector<int> runs_diff;
+    obj.setup_random_binding(opairs, runs_diff, pots, bbs, single, 7);
     matrix<double> F(N, 3), T(N, 3);
     obj.calculate_forces_and_torques3D_onlyone_nonlets(F, T);
     obj.init_forces();

@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_api_version_and_status_strings():
     L = _lib.lib()
-    assert L.mtg_api_version() == 4
+    assert L.mtg_api_version() == 5
     assert L.mtg_status_string(0) == b"ok"
     assert L.mtg_status_string(5) == b"non-finite state on the device"
 
