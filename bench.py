@@ -42,10 +42,11 @@ BYTES_SCAN_PER_CELL = 16
 # the epilogue kernel alone: the force pass's own-particle traffic plus the read and clear of the 64-bit
 # fixed-point force/torque sums the pair kernels accumulate (48 + 48 B)
 BYTES_EPILOGUE = BYTES_FORCE + 96
-# measured DRAM bytes per particle and launch (ncu dram__bytes_read + dram__bytes_write on 160 replicas,
-# state larger than L2; profiles/step_dram_traffic_c4x160.md), scaled by the particle count.  Force pass:
-# pairfind + pairforce + patch pairs + epilogue.
-TRAFFIC_PER_PARTICLE = {"force": 422.0, "scatter": 233.1}
+# measured DRAM bytes per particle and launch (ncu dram__bytes_read + dram__bytes_write, one kernel per
+# capture, 160 replicas aged 2,000 steps, state larger than L2; profiles/step_dram_traffic_c4x160_aged.md),
+# scaled by the particle count.  Force pass: fused pair finding 113.5 + patch pairs 113.0 + epilogue 227.0 (the
+# pair-force kernel has no pairs to take).
+TRAFFIC_PER_PARTICLE = {"force": 453.5, "scatter": 233.1}
 # the end-to-end leg: a fixed number of steps, whatever --steps is
 E2E_STEPS = 100
 # CPU legs (reference arm and cpu_baseline): the same replica sample, processed largest first, one replica
@@ -339,7 +340,7 @@ def run_gpu(args, rank, world, local):
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": (achieved / pk["hbm_gbs"]) if achieved else None,
                 "traffic": traffic * n if traffic else None,
-                "traffic_source": "ncu DRAM bytes per particle at 160 replicas, scaled" if traffic else None,
+                "traffic_source": "ncu DRAM bytes per particle at 160 replicas (bonded state), scaled" if traffic else None,
                 "peak_source": pk["source"],
                 "kernel_ms_per_step": {k: round(v, 5) for k, v in per_launch.items()},
                 "share": {k: round(v / total_prof, 4) for k, v in prof.items()},
