@@ -8,8 +8,9 @@ FP32 state with FP64 reductions, cell list rebuilt every step, one CUDA-graph la
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mtcode|reference]
 
 One JSON line on rank 0.  ``value``: particle-steps/s of the device-resident step (all ranks);
-``e2e``: the same metric through the C ABI with host buffers (state upload, per-step temperature
-read-back as Condensate::run does, final state download) inside the timed region.  ``roofline``: the
+``e2e``: the same metric through the C ABI with host buffers (state upload, every step's temperature
+read back to pinned host memory as Condensate::run measures it every step, final state download) inside the
+timed region; ``e2e.per_step_sync`` repeats it with a synchronous read after each step.  ``roofline``: the
 dominant kernel's algorithmic bytes / its CUDA-event time against the measured HBM copy bandwidth.
 ``cpu_baseline``: the oracle (CPU restatement of the reference step) on a bounded sample, all host cores.
 Multi-GPU: replicas only -- each rank runs its own full replica set (weak scaling), no collective on the
@@ -360,6 +361,9 @@ def run_gpu(args, rank, world, local):
     # ---- end to end through the C ABI with host buffers
     e2e = run_e2e(s, W, args, stream, ev0, ev1)
     e2e["value"] = dist_max(world, -e2e["value"]) * -1 if world > 1 else e2e["value"]
+    # the same with a synchronous temperature read after every step, for comparison
+    sync = run_e2e(s, W, args, stream, ev0, ev1, batched=False)
+    e2e["per_step_sync"] = {k: sync[k] for k in ("value", "upload_ms", "steps_ms_per_step", "download_ms", "what")}
 
     # ---- plain FP64 single-system path on a sample of the same replicas
     plain = run_plain_fp64(args, local) if args.plain_fp64 and rank == 0 else None
@@ -389,7 +393,12 @@ def run_gpu(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
-def run_e2e(s, W, args, stream, ev0, ev1) -> dict:
+def run_e2e(s, W, args, stream, ev0, ev1, batched: bool = True) -> dict:
+    """The metric through the C ABI with host buffers: the FP64 state uploaded from pinned memory, a fixed number
+    of steps each followed by its temperature read back to the host (Condensate::run measures it every step), the
+    state downloaded into pinned memory.  batched: mtg_step_temperatures (every step's sums reach pinned host
+    memory as that step completes, one synchronisation at the end); else mtg_step(1) + mtg_temperature per step
+    (a synchronisation after every step)."""
     import torch
     n = W.n_total
     R = len(W.replicas)
@@ -405,10 +414,13 @@ def run_e2e(s, W, args, stream, ev0, ev1) -> dict:
     ev0.record(stream)
     s.initialize(pinned["x"], pinned["p"], pinned["Lb"], pinned["Q"], pinned["Ft"], pinned["Tt"])
     ev_up.record(stream)
-    temps = np.empty((k_e2e, R, 6))
-    for i in range(k_e2e):  # Condensate::run: a step, then the temperature read back to the host
-        s.step(1)
-        temps[i] = s.measured_temperature()
+    if batched:
+        temps = s.step_temperatures(k_e2e)
+    else:
+        temps = np.empty((k_e2e, R, 6))
+        for i in range(k_e2e):
+            s.step(1)
+            temps[i] = s.measured_temperature()
     ev_down.record(stream)
     st = s.get_state(out)
     ev1.record(stream)
@@ -418,12 +430,14 @@ def run_e2e(s, W, args, stream, ev0, ev1) -> dict:
         raise RuntimeError("e2e: non-finite temperatures or state")
     h2d = n * (3 + 3 + 3 + 9 + 3 + 3) * 8
     d2h_state = n * (3 + 3 + 3 + 9 + 3 + 3) * 8
+    what = ("mtg_set_state (host FP64 state) + mtg_step_temperatures (each step's temperatures to pinned host "
+            "memory as the step completes) + mtg_get_state at the end" if batched else
+            "mtg_set_state (host FP64 state) + per step: mtg_step(1) + mtg_temperature (synchronous read-back) "
+            "+ mtg_get_state at the end")
     return {"value": n * k_e2e / wall, "unit": UNIT, "h2d_bytes_per_step": h2d / k_e2e,
             "d2h_bytes_per_step": R * 6 * 8 + d2h_state / k_e2e, "steps": k_e2e,
             "upload_ms": ev0.elapsed_time(ev_up), "download_ms": ev_down.elapsed_time(ev1),
-            "steps_ms_per_step": ev_up.elapsed_time(ev_down) / k_e2e, "wall_ms": 1e3 * wall,
-            "what": "mtg_set_state (host FP64 state) + per step: mtg_step(1) + mtg_temperature (read-back) "
-                    "+ mtg_get_state at the end"}
+            "steps_ms_per_step": ev_up.elapsed_time(ev_down) / k_e2e, "wall_ms": 1e3 * wall, "what": what}
 
 
 def run_plain_fp64(args, device) -> dict:
