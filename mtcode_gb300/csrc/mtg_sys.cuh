@@ -1031,7 +1031,9 @@ struct Sys : SysBase {
                 else fused ? find(std::integral_constant<int, 256>{}, F1{}) : find(std::integral_constant<int, 256>{}, F0{});
             }
             mark(1);
-            const int g_force = sms * lc.pairforce_blocks_per_sm, g_patch = sms * lc.patch_blocks_per_sm;
+            // after fused pair finding the pair-force kernel only takes the pairs beyond the warps' buffers
+            // (normally none): one block per SM, so that its launch and exit cost little
+            const int g_force = fused ? sms : sms * lc.pairforce_blocks_per_sm, g_patch = sms * lc.patch_blocks_per_sm;
             bool bind_pass = false;
             if constexpr (std::is_same<real, float>::value) {
                 if (bind) {
