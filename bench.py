@@ -359,7 +359,11 @@ def run_gpu(args, rank, world, local):
         roofline["epilogue_bytes_per_particle"] = BYTES_EPILOGUE
 
     # ---- end to end through the C ABI with host buffers
-    e2e = run_e2e(s, W, args, stream, ev0, ev1)
+    # three repetitions, the median reported (the one-time host copies of ~1 GB each way vary with the shared
+    # host's load: 5-6 ms each when it is quiet, several times that at times); all three are in the line
+    reps = sorted((run_e2e(s, W, args, stream, ev0, ev1) for _ in range(3)), key=lambda e: e["value"])
+    e2e = dict(reps[1])
+    e2e["repetitions"] = [{k: r[k] for k in ("value", "upload_ms", "steps_ms_per_step", "download_ms")} for r in reps]
     e2e["value"] = dist_max(world, -e2e["value"]) * -1 if world > 1 else e2e["value"]
     # the same with a synchronous temperature read after every step, for comparison
     sync = run_e2e(s, W, args, stream, ev0, ev1, batched=False)
