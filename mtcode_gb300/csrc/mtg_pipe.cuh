@@ -314,6 +314,42 @@ __global__ void __launch_bounds__(kPipeThreads, 4) pairforce_kernel(ForceArgs<re
     block_list_flush(lbuf, &lnb, &lbase, list, lcounts, list_cap, a.flags, lflag);
 }
 
+// the Kern-Frenkel terms of one listed pair (sa, sb) into both particles' sums: the full kernel's patch branch
+template <class real>
+__device__ __forceinline__ void patch_terms(const ForceArgs<real> &a, int sa, int sb, typename PairAcc<real>::type *acc) {
+    const int r = a.tb.uniform ? 0 : replica_of(a.tb, sa);
+    const Replica<real> &R = a.tb.reps[r];
+    const Model<real> &M = a.tb.models[R.model];
+    real xa[4], xb[4];
+    load4(a.buf.pos + 4 * (size_t)sa, xa);
+    load4(a.buf.pos + 4 * (size_t)sb, xb);
+    const real d[3] = {min_image_sep<real>(xa[0], xb[0], R.box, R.box_lo, R.l2s, R.periodic),
+                       min_image_sep<real>(xa[1], xb[1], R.box, R.box_lo, R.l2s, R.periodic),
+                       min_image_sep<real>(xa[2], xb[2], R.box, R.box_lo, R.l2s, R.periodic)};
+    const real rr = sqrt_r(sep_r2<real>(d[0], d[1], d[2]));
+    const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
+    const bool single = M.n_types == 1;
+    const int tya = single ? 0 : type_of<real>(M, ida - R.off), tyb = single ? 0 : type_of<real>(M, idb - R.off);
+    real Qa[9], Qb[9];
+    load_q(a, sa, xa[3], Qa);
+    load_q(a, sb, xb[3], Qb);
+    const bool a_first = ida < idb;  // canonical order of the reference (p1 < p2)
+    const real sg = a_first ? real(1) : real(-1), inv = real(1) / rr;
+    const real u[3] = {sg * d[0] * inv, sg * d[1] * inv, sg * d[2] * inv};
+    real f[3] = {real(0), real(0), real(0)}, t1[3] = {real(0), real(0), real(0)},
+         t2[3] = {real(0), real(0), real(0)}, e = real(0);
+    int nbond = 0;
+    if (a_first) patch_pair<real>(M, tya, tyb, Qa, Qb, u, rr, R.bond_r, f, t1, t2, e, nbond);
+    else patch_pair<real>(M, tyb, tya, Qb, Qa, u, rr, R.bond_r, f, t1, t2, e, nbond);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        fixed_add(acc + 6 * (size_t)sa + k, sg * f[k]);
+        fixed_add(acc + 6 * (size_t)sb + k, -sg * f[k]);
+        fixed_add(acc + 6 * (size_t)sa + 3 + k, a_first ? t1[k] : t2[k]);
+        fixed_add(acc + 6 * (size_t)sb + 3 + k, a_first ? t2[k] : t1[k]);
+    }
+}
+
 // range_list: use the replica's list range (skin lists) instead of its force range.
 // Each lane scans its particle's candidate segments (scan_segment): chunks of at most 32 slots whose hits are
 // marked in a bit mask and appended by the warp together to its own part of the block buffer (warp_append), so
@@ -547,38 +583,7 @@ __global__ void __launch_bounds__(kPipeThreads, 4) patch_pairs_kernel(ForceArgs<
     const long long n = segs[kSegs];
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
         const int2 pr = list_all[seg_slot(segs, cap, q)];
-        const int sa = pr.x, sb = pr.y;
-        const int r = a.tb.uniform ? 0 : replica_of(a.tb, sa);
-        const Replica<real> &R = a.tb.reps[r];
-        const Model<real> &M = a.tb.models[R.model];
-        real xa[4], xb[4];
-        load4(a.buf.pos + 4 * (size_t)sa, xa);
-        load4(a.buf.pos + 4 * (size_t)sb, xb);
-        const real d[3] = {min_image_sep<real>(xa[0], xb[0], R.box, R.box_lo, R.l2s, R.periodic),
-                           min_image_sep<real>(xa[1], xb[1], R.box, R.box_lo, R.l2s, R.periodic),
-                           min_image_sep<real>(xa[2], xb[2], R.box, R.box_lo, R.l2s, R.periodic)};
-        const real rr = sqrt_r(sep_r2<real>(d[0], d[1], d[2]));
-        const int ida = __ldg(a.buf.ident + sa), idb = __ldg(a.buf.ident + sb);
-        const bool single = M.n_types == 1;
-        const int tya = single ? 0 : type_of<real>(M, ida - R.off), tyb = single ? 0 : type_of<real>(M, idb - R.off);
-        real Qa[9], Qb[9];
-        load_q(a, sa, xa[3], Qa);
-        load_q(a, sb, xb[3], Qb);
-        const bool a_first = ida < idb;  // canonical order of the reference (p1 < p2)
-        const real sg = a_first ? real(1) : real(-1), inv = real(1) / rr;
-        const real u[3] = {sg * d[0] * inv, sg * d[1] * inv, sg * d[2] * inv};
-        real f[3] = {real(0), real(0), real(0)}, t1[3] = {real(0), real(0), real(0)},
-             t2[3] = {real(0), real(0), real(0)}, e = real(0);
-        int nbond = 0;
-        if (a_first) patch_pair<real>(M, tya, tyb, Qa, Qb, u, rr, R.bond_r, f, t1, t2, e, nbond);
-        else patch_pair<real>(M, tyb, tya, Qb, Qa, u, rr, R.bond_r, f, t1, t2, e, nbond);
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            fixed_add(acc + 6 * (size_t)sa + k, sg * f[k]);
-            fixed_add(acc + 6 * (size_t)sb + k, -sg * f[k]);
-            fixed_add(acc + 6 * (size_t)sa + 3 + k, a_first ? t1[k] : t2[k]);
-            fixed_add(acc + 6 * (size_t)sb + 3 + k, a_first ? t2[k] : t1[k]);
-        }
+        patch_terms<real>(a, pr.x, pr.y, acc);
     }
 }
 
