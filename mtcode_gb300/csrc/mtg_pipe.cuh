@@ -358,13 +358,14 @@ __device__ __forceinline__ void patch_terms(const ForceArgs<real> &a, int sa, in
 // shifts known at compile time, the shifts taken out of the candidate loop); warps with a lane in a smaller grid
 // take the general row loop.
 //
-// FUSED (no list reuse: every step rebuilds): the pairs do not go to the list at all.  After its scan each
+// STAGE kPairSplit or kPairBind (no list reuse: every step rebuilds): the pairs do not go to the list at all
+// (FUSED).  After its scan each
 // warp takes its own buffered pairs, one per lane, through pair_core (WCA core, cone pre-test, patch list)
 // while their positions are still in L1; only pairs beyond a warp's part reach the HBM list, for
 // pairforce_kernel.
 // FP32 register budgets: the fused form at 48 (five 256-thread blocks per SM; its natural 64 allow four,
 // measured 8% slower), the search alone at 40 (six blocks).  FP64 keeps its natural count (no spills).
-template <class real, int THREADS, bool FUSED>
+template <class real, int THREADS, int STAGE, bool FUSED = STAGE != 0>
 __global__ void __launch_bounds__(THREADS, sizeof(real) == 4 ? (FUSED ? 1280 : 1536) / THREADS : 1)
     pairfind_kernel(ForceArgs<real> a, int2 *pairs,
                                                            unsigned long long *npairs, long long cap,
@@ -543,12 +544,15 @@ __global__ void __launch_bounds__(THREADS, sizeof(real) == 4 ? (FUSED ? 1280 : 1
         // the warp's pairs (s, t) have s among its own slots: when those lie in one replica, so do all of them
         const int r0 = __shfl_sync(full, r, 0);
         const int rhint = __all_sync(full, !valid || r == r0) && __shfl_sync(full, valid, 0) ? r0 : -1;
+        // kPairBind (single-bond mode, a bond-deciding pass): the listed pairs go to the bond pass's segments
+        unsigned long long *const lcounts = STAGE == kPairBind ? a.bind_ctr + kSegPairs : list_counts;
+        const unsigned lflag = STAGE == kPairBind ? (kFlagBind | kBindWhyList) : 8u;
         bool big = false;
         for (int i = lane; i < n; i += 32)
-            pair_core<real, kPairSplit>(a, part[i].x, part[i].y, acc, lbuf, &lnb, list, list_cap, list_counts, 8u, big,
-                                        rhint);
+            pair_core<real, STAGE == kPairBind ? kPairBind : kPairSplit>(a, part[i].x, part[i].y, acc, lbuf, &lnb,
+                                                                           list, list_cap, lcounts, lflag, big, rhint);
         if (big) atomicOr(a.flags, 2u);
-        block_list_flush(lbuf, &lnb, &lbase, list, list_counts, list_cap, a.flags, 8u);
+        block_list_flush(lbuf, &lnb, &lbase, list, lcounts, list_cap, a.flags, lflag);
         return;
     }
     // one list reservation per block (a single counter serves the whole grid): the warps' counts, then each

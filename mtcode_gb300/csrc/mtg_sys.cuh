@@ -1013,22 +1013,39 @@ struct Sys : SysBase {
             };
             mark(0);
             mtg::pair_reset_kernel<<<1, 64, 0, st>>>(d_npairs, gate, bind ? nullptr : d_patch_ctr);
-            // fused pair finding + WCA / pre-test (no list reuse, not a bond-deciding pass): the pair kernel then
-            // only takes the pairs beyond the blocks' buffers
-            const bool fused = lc.fused_pairs && skin <= 0 && !bind;
+            // fused pair finding + WCA / pre-test (no list reuse): the pair kernel then only takes the pairs beyond
+            // the warps' buffers.  A bond-deciding pass (FP32) fuses its own pair stage, which lists the bond
+            // pass's candidate pairs.
+            const bool fused = lc.fused_pairs && skin <= 0;
             {
                 const int t = lc.pairfind_threads, gb = std::max(1, (ntot_ + t - 1) / t), rl = skin > 0 ? 1 : 0;
-                auto find = [&](auto threads, auto fuse) {
+                auto find = [&](auto threads, auto stage) {
                     constexpr int T = decltype(threads)::value;
-                    constexpr bool FU = decltype(fuse)::value;
-                    mtg::pairfind_kernel<real, T, FU><<<gb, T, 0, st>>>(a, d_pairs, d_npairs, pair_cap, rl, gate, d_acc,
-                                                                        d_patch_list, patch_cap, d_patch_ctr);
+                    constexpr int SG = decltype(stage)::value;
+                    if constexpr (SG == mtg::kPairBind)
+                        mtg::pairfind_kernel<real, T, SG><<<gb, T, 0, st>>>(a, d_pairs, d_npairs, pair_cap, rl, gate,
+                                                                            d_acc, d_bind_pairs, lcap, nullptr);
+                    else
+                        mtg::pairfind_kernel<real, T, SG><<<gb, T, 0, st>>>(a, d_pairs, d_npairs, pair_cap, rl, gate,
+                                                                            d_acc, d_patch_list, patch_cap, d_patch_ctr);
                 };
-                using F1 = std::true_type;
-                using F0 = std::false_type;
-                if (t == 128) fused ? find(std::integral_constant<int, 128>{}, F1{}) : find(std::integral_constant<int, 128>{}, F0{});
-                else if (t == 512) fused ? find(std::integral_constant<int, 512>{}, F1{}) : find(std::integral_constant<int, 512>{}, F0{});
-                else fused ? find(std::integral_constant<int, 256>{}, F1{}) : find(std::integral_constant<int, 256>{}, F0{});
+                auto with_stage = [&](auto threads) {
+                    using S0 = std::integral_constant<int, 0>;
+                    using SP = std::integral_constant<int, mtg::kPairSplit>;
+                    if (!fused) {
+                        find(threads, S0{});
+                    } else if (bind) {
+                        if constexpr (std::is_same<real, float>::value)
+                            find(threads, std::integral_constant<int, mtg::kPairBind>{});
+                        else
+                            find(threads, S0{});   // (not reached: FP64 bond-deciding passes are not piped)
+                    } else {
+                        find(threads, SP{});
+                    }
+                };
+                if (t == 128) with_stage(std::integral_constant<int, 128>{});
+                else if (t == 512) with_stage(std::integral_constant<int, 512>{});
+                else with_stage(std::integral_constant<int, 256>{});
             }
             mark(1);
             // after fused pair finding the pair-force kernel only takes the pairs beyond the warps' buffers
