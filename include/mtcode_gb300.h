@@ -241,8 +241,9 @@ typedef struct {
     int patch_blocks_per_sm;       /* grid of the patch-pair (single-bond: edge) kernel per SM: 1..64 (8) */
     int epilogue_threads;          /* per-particle epilogue: 128, 256 (default) or 512 */
     int fused_pairs;               /* 1 (default): pair finding also evaluates the WCA core and the cone pre-test
-                                      of the pairs it finds, in the same block, and writes no pair list (steps
-                                      without a neighbour skin); 0: separate pair list and pair-force kernel */
+                                      of the pairs it finds, in the same kernel, and writes no pair list (steps
+                                      without a neighbour skin; in single-bond mode also the bond pass's pair
+                                      stage); 0: separate pair list and pair-force kernel */
 } mtg_launch_config;
 mtg_status mtg_get_launch_config(mtg_system *h, mtg_launch_config *out);
 /* Sets the shapes; the step graphs are captured again at the next step. */

@@ -172,6 +172,28 @@ __device__ __forceinline__ void acc_add_raw(double *acc, double v) {
 //   bind_pairs_kernel.
 enum PairKind : int { kPairBind = 1, kPairSplit = 2 };
 
+// whether a patch of type ty has sign (n . w) above mc: up to four patches unrolled, their loads issued together
+template <class real>
+__device__ __forceinline__ bool cone_any(const Model<real> &M, int ty, const real w[3], real mc, real sign) {
+    const int np = M.np[ty], o = M.ooff[ty];
+    bool any = false;
+    if (np <= 4) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (k < np) {
+                const real *v = M.orient[o + k];
+                any |= sign * (v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > mc;
+            }
+        }
+        return any;
+    }
+    for (int k = 0; k < np; k++) {
+        const real *v = M.orient[o + k];
+        any |= sign * (v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > mc;
+    }
+    return any;
+}
+
 // One listed pair (sa, sb): the WCA core into acc (both particles), and -- KIND kPairSplit -- the pair onto
 // `list` when both particles have a patch near a cone, or -- KIND kPairBind -- onto `list` in canonical order
 // when both do (single-bond mode).  List entries are staged in the block's lbuf (block_list_put).
@@ -222,21 +244,11 @@ __device__ __forceinline__ void pair_core(const ForceArgs<real> &a, int sa, int 
             load_q(a, sa, xa[3], Q);
 #pragma unroll
             for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
-            bool any = false;
-            for (int k = 0; k < M.np[tya]; k++) {
-                const real *v = M.orient[M.ooff[tya] + k];
-                any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > pre;
-            }
-            if (any) {
+            if (cone_any<real>(M, tya, w, pre, real(-1))) {
                 load_q(a, sb, xb[3], Q);
 #pragma unroll
                 for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
-                bool anyb = false;
-                for (int k = 0; k < M.np[tyb]; k++) {
-                    const real *v = M.orient[M.ooff[tyb] + k];
-                    anyb |= v[0] * w[0] + v[1] * w[1] + v[2] * w[2] > pre;
-                }
-                if (anyb)
+                if (cone_any<real>(M, tyb, w, pre, real(1)))
                     block_list_put(lbuf, lnb, ida < idb ? make_int2(sa, sb) : make_int2(sb, sa), list, lcounts,
                                    list_cap, a.flags, lflag);
             }
@@ -254,12 +266,7 @@ __device__ __forceinline__ void pair_core(const ForceArgs<real> &a, int sa, int 
             load_q(a, sa, xa[3], Q);
 #pragma unroll
             for (int k = 0; k < 3; k++) w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
-            const real mca = M.mincos_any[tya] - real(1e-5);
-            bool any = false;
-            for (int k = 0; k < M.np[tya]; k++) {
-                const real *v = M.orient[M.ooff[tya] + k];
-                any |= -(v[0] * w[0] + v[1] * w[1] + v[2] * w[2]) > mca;
-            }
+            const bool any = cone_any<real>(M, tya, w, M.mincos_any[tya] - real(1e-5), real(-1));
             if (any) {
                 const int idb = __ldg(a.buf.ident + sb);
                 const int tyb = M.n_types == 1 ? 0 : type_of<real>(M, idb - R.off);
@@ -268,12 +275,7 @@ __device__ __forceinline__ void pair_core(const ForceArgs<real> &a, int sa, int 
 #pragma unroll
                     for (int k = 0; k < 3; k++)
                         w[k] = (Q[3 * k] * d[0] + Q[3 * k + 1] * d[1] + Q[3 * k + 2] * d[2]) * inv;
-                    const real mcb = M.mincos_any[tyb] - real(1e-5);
-                    bool anyb = false;
-                    for (int k = 0; k < M.np[tyb]; k++) {
-                        const real *v = M.orient[M.ooff[tyb] + k];
-                        anyb |= v[0] * w[0] + v[1] * w[1] + v[2] * w[2] > mcb;
-                    }
+                    const bool anyb = cone_any<real>(M, tyb, w, M.mincos_any[tyb] - real(1e-5), real(1));
                     if (anyb) block_list_put(lbuf, lnb, make_int2(sa, sb), list, lcounts, list_cap, a.flags, lflag);
                 }
             }
