@@ -49,7 +49,7 @@ BYTES_EPILOGUE = BYTES_FORCE + 96
 # pair-force kernel has no pairs to take).
 TRAFFIC_PER_PARTICLE = {"force": 453.5, "scatter": 233.1}
 # the end-to-end leg: a fixed number of steps, whatever --steps is
-E2E_STEPS = 100
+E2E_STEPS = 1000   # Condensate::run uploads once per run of 10^4 steps; a tenth of that per e2e leg
 # CPU legs (reference arm and cpu_baseline): the same replica sample, processed largest first, one replica
 # per host thread at a time
 CPU_SAMPLE_REPLICAS = 128
