@@ -4,8 +4,8 @@
 
 Used for quick timing and as the target of profiler captures (it launches the same kernels as the
 benchmark, on a workload of the chosen size).  ``--save-state F`` writes the state after the timed steps to F
-(.npz) and ``--load-state F`` starts from it instead of the seeded start, so a capture of a few launches can
-see an aged (bonded) state without running the steps that aged it.
+(.npz; in single-bond mode with the bond state) and ``--load-state F`` starts from it instead of the seeded
+start, so a capture of a few launches can see an aged (bonded) state without running the steps that aged it.
 """
 from __future__ import annotations
 
@@ -55,6 +55,8 @@ def main() -> None:
         if args.single_bond:
             from .system import binding_single
             s.set_single_bond(binding_single(*args.single_bond))
+            if args.load_state and "boundto" in st:
+                s.set_bind_state(st["boundto"], st["isbound"])
         if args.launch:
             keys = ("pairfind_threads", "pairforce_blocks_per_sm", "patch_blocks_per_sm", "epilogue_threads",
                     "fused_pairs")
@@ -79,7 +81,10 @@ def main() -> None:
             line += " | " + " ".join(f"{k}={v / max(1, args.steps):.3f}ms" for k, v in prof.items())
         print(line, flush=True)
         if args.save_state:
-            np.savez(args.save_state, **s.get_state())
+            state = s.get_state()
+            if args.single_bond:   # the bond state too
+                state["boundto"], state["isbound"] = s.get_bind_state()
+            np.savez(args.save_state, **state)
 
 
 if __name__ == "__main__":
