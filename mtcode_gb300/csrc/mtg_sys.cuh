@@ -813,7 +813,12 @@ struct Sys : SysBase {
         MTG_CUDA(cudaMemcpy(d_patch_slot, pslot.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice));
         MTG_CUDA(cudaMemset(d_bctr, 0, sizeof(unsigned long long) * mtg::kBindCounters));
         MTG_CUDA(cudaMemset(d_deg, 0, sizeof(unsigned long long) * np));
-        MTG_CUDA(cudaMemset(d_boundto, 0, sizeof(int) * np));
+        {   // BinaryBindStore starts zeroed (boundto 0 in replica-local numbering: the replica's first patch)
+            std::vector<int> g0(np, 0);
+            for (int r = 0; r < nrep; r++)
+                for (int i = pslot[(size_t)r]; i < pslot[(size_t)r + 1]; i++) g0[(size_t)i] = pslot[(size_t)r];
+            MTG_CUDA(cudaMemcpy(d_boundto, g0.data(), sizeof(int) * np, cudaMemcpyHostToDevice));
+        }
         MTG_CUDA(cudaMemset(d_isbound, 0, np));
         ensure_slot_of();
         // the force pass keeps the WCA core and no patch term; its pair loop reaches max_check, where edges

@@ -88,3 +88,25 @@ def test_setup_random_binding_batch_and_run(precision):
         assert s.flags == 0
         st = s.get_state()
         assert np.isfinite(st["x"]).all()
+
+
+def test_bond_state_starts_zeroed_and_round_trips():
+    """A BinaryBindStore starts zeroed (boundto 0 in each replica's own numbering), and a bond state read back
+    from the device can be set again, after steps too (unbound patches keep a partner of their own replica)."""
+    ds = [load(f"singlebond_{k}.npz") for k in (1, 3)]
+    specs = [spec_from(d) for d in ds]
+    n = sum(sp.n for sp in specs)
+    z = np.zeros((n, 3))
+    with LangevinNVTRGPU(specs, precision="fp32") as s:
+        s.set_single_bond(gpu_model(ds[0]))
+        s.initialize(np.concatenate([d["x"] for d in ds]), z, z, np.concatenate([d["Q"][0] for d in ds]))
+        bt, ib = s.get_bind_state()
+        assert not ib.any() and not bt.any()
+        s.set_bind_state(bt, ib)
+        s.setup_random_binding(3)
+        s.init_forces()
+        s.step(15)
+        bt, ib = s.get_bind_state()
+        assert ib.any()
+        s.set_bind_state(bt, ib)   # every entry a patch of its replica
+        assert s.flags == 0
