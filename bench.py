@@ -45,9 +45,9 @@ BYTES_SCAN_PER_CELL = 16
 BYTES_EPILOGUE = BYTES_FORCE + 96
 # measured DRAM bytes per particle and launch (ncu dram__bytes_read + dram__bytes_write, one kernel per
 # capture, 160 replicas aged 2,000 steps, state larger than L2; profiles/step_dram_traffic_c4x160_aged.md),
-# scaled by the particle count.  Force pass: fused pair finding 113.5 + patch pairs 113.0 + epilogue 227.0 (the
-# pair-force kernel has no pairs to take).
-TRAFFIC_PER_PARTICLE = {"force": 453.5, "scatter": 233.1}
+# scaled by the particle count.  Force pass: fused pair finding 113.6 + patch pairs 113.0 + epilogue 227.0 (the
+# pair-force kernel has no pairs to take).  Scatter: 235.2.
+TRAFFIC_PER_PARTICLE = {"force": 453.6, "scatter": 235.2}
 # the end-to-end leg: a fixed number of steps, whatever --steps is
 E2E_STEPS = 1000   # Condensate::run uploads once per run of 10^4 steps; a tenth of that per e2e leg
 # CPU legs (reference arm and cpu_baseline): the same replica sample, processed largest first, one replica
