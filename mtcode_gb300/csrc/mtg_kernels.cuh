@@ -535,6 +535,8 @@ struct ForceArgs {
     unsigned long long *bind_ctr;    // [2] stamp; segment counters of the update's lists (kSegTouched, ...)
     int *bind_touched;               // patches with an edge this update, kSegs segments of bind_tcap
     long long bind_tcap;
+    int2 *bind_recheck;              // patch pairs for the FP64 tests (float edge pass), kSegs segments of bind_rcap
+    long long bind_rcap;
     int bind_listed;                 // bound-pair forces summed by a pair kernel, not by the epilogue
 };
 
@@ -597,9 +599,8 @@ __device__ __forceinline__ int side_of(T v, float lo, float hi) {
 
 // the reference's bind-state dependent range (LangevinRforce.cpp:3010-3030): class 0 disp (neither or both
 // bound to each other), 1 0.5 disp (both bound elsewhere), 2 0.7 disp (exactly one bound)
-__device__ __forceinline__ int range_class(const int *boundto, const unsigned char *isbound, int w1, int w2) {
-    const bool b1 = isbound[w1] != 0, b2 = isbound[w2] != 0;
-    const bool cond1 = boundto[w1] == w2 && boundto[w2] == w1;
+__device__ __forceinline__ int range_class(bool b1, bool b2, int boundto1, int boundto2, int w1, int w2) {
+    const bool cond1 = boundto1 == w2 && boundto2 == w1;
     return (b1 && b2) ? (cond1 ? 0 : 1) : (b1 != b2 ? 2 : 0);
 }
 __device__ __forceinline__ double disp2_of(double disp, int cls) {
@@ -646,21 +647,17 @@ __device__ __noinline__ bool exact_member(const BindRep &B, const real *sa, cons
     return __dadd_rn(__dsub_rn(ai, B.max_ang), __dsub_rn(aj, B.max_ang)) > -0.4;
 }
 
+// the candidate-list condition in float on snapshot rows A and C (the particles of patch rows o1, o2): 1 member,
+// -1 not, 0 within a margin of a threshold (the FP64 test, exact_member, decides)
 template <class real>
-__device__ __forceinline__ bool candidate(const BindRep &B, const Replica<real> &R, const Model<real> &M,
-                                          const real *sa, const real *sb, const real *sc, int s1, int s2, int o1,
-                                          int o2) {
-    if (std::is_same<real, double>::value) return exact_member<real>(B, sa, sb, sc, s1, s2, o1, o2);
-    Payload<real> A, C;
-    A.load(sa, sb, sc, s1);
-    C.load(sa, sb, sc, s2);
+__device__ __forceinline__ int candidate_side(const BindRep &B, const Replica<real> &R, const Model<real> &M,
+                                              const Payload<real> &A, const Payload<real> &C, int o1, int o2) {
     const real dx = min_image_sep<real>(A.v[0], C.v[0], R.box, R.box_lo, R.l2s, R.periodic);
     const real dy = min_image_sep<real>(A.v[1], C.v[1], R.box, R.box_lo, R.l2s, R.periodic);
     const real dz = min_image_sep<real>(A.v[2], C.v[2], R.box, R.box_lo, R.l2s, R.periodic);
     const real r2 = dx * dx + dy * dy + dz * dz;
     const int t = side_of<real>(r2, B.memb2_lo, B.memb2_hi);
-    if (t > 0) return false;
-    if (t == 0) return exact_member<real>(B, sa, sb, sc, s1, s2, o1, o2);
+    if (t != -1) return t > 0 ? -1 : 0;
     const real rr = sqrt(r2), u[3] = {dx / rr, dy / rr, dz / rr};
     const real *v1 = M.orient[o1], *v2 = M.orient[o2];
     real ci = 0, cj = 0;
@@ -669,11 +666,24 @@ __device__ __forceinline__ bool candidate(const BindRep &B, const Replica<real> 
         ci -= (v1[0] * A.v[3 + k] + v1[1] * A.v[6 + k] + v1[2] * A.v[9 + k]) * u[k];
         cj += (v2[0] * C.v[3 + k] + v2[1] * C.v[6 + k] + v2[2] * C.v[9 + k]) * u[k];
     }
-    const int w = side_of<real>((ci - (real)B.max_ang_f) + (cj - (real)B.max_ang_f), B.ang_lo, B.ang_hi);
+    return side_of<real>((ci - (real)B.max_ang_f) + (cj - (real)B.max_ang_f), B.ang_lo, B.ang_hi);
+}
+
+template <class real>
+__device__ __forceinline__ bool candidate(const BindRep &B, const Replica<real> &R, const Model<real> &M,
+                                          const real *sa, const real *sb, const real *sc, int s1, int s2, int o1,
+                                          int o2) {
+    if (std::is_same<real, double>::value) return exact_member<real>(B, sa, sb, sc, s1, s2, o1, o2);
+    Payload<real> A, C;
+    A.load(sa, sb, sc, s1);
+    C.load(sa, sb, sc, s2);
+    const int w = candidate_side<real>(B, R, M, A, C, o1, o2);
     return w == 0 ? exact_member<real>(B, sa, sb, sc, s1, s2, o1, o2) : w > 0;
 }
 
-// slot of this update's adjacency for patch p (stamped counter: a stale stamp counts as zero edges)
+// slot of this update's adjacency for patch p (stamped counter: a stale stamp counts as zero edges).  A max of
+// (stamp << 32) followed by an add would take the slot without the load, but the two atomics on one address
+// measured far slower than the load and the compare-and-swap.
 __device__ __forceinline__ int adj_take(unsigned long long *deg, int p, unsigned stamp, unsigned *flags) {
     unsigned long long old = deg[p];
     for (int it = 0; it < (1 << 20); it++) {
@@ -694,7 +704,8 @@ constexpr int kSegs = 64;
 constexpr int kSegPairs = 8;                   // bind_ctr offsets of the segment counters
 constexpr int kSegTouched = kSegPairs + kSegs;
 constexpr int kSegBound = kSegTouched + kSegs;
-constexpr int kBindCounters = kSegBound + kSegs;
+constexpr int kSegRecheck = kSegBound + kSegs;
+constexpr int kBindCounters = kSegRecheck + kSegs;
 
 // A kernel that reads a segmented list first lays its segments end to end: seg_prefix (every thread of the
 // block, before any early exit) leaves the exclusive prefix of the segment lengths in shared memory, and
@@ -757,7 +768,7 @@ __device__ __forceinline__ void bind_patch_edge(const ForceArgs<real> &a, const 
     const int e1 = side_of<real>(c1, B.ctm_lo[q], B.ctm_hi[q]), e2 = side_of<real>(c2, B.ctm_lo[q], B.ctm_hi[q]);
     if (e1 < 0 || e2 < 0) return;
     const int wp1 = patch_of<real>(B, M, li1, ty1, ka), wp2 = patch_of<real>(B, M, li2, ty2, kb);
-    const int cls = range_class(a.bind_to, a.bind_on, wp1, wp2);
+    const int cls = range_class(a.bind_on[wp1] != 0, a.bind_on[wp2] != 0, a.bind_to[wp1], a.bind_to[wp2], wp1, wp2);
     const float dfl = cls == 1 ? 0.5f * B.disp_f[q] : (cls == 2 ? 0.7f * B.disp_f[q] : B.disp_f[q]);
     const int e3 = side_of<real>(rr, dfl * (1.f - 1e-5f), dfl * (1.f + 1e-5f));
     if (e3 > 0) return;
@@ -769,6 +780,35 @@ __device__ __forceinline__ void bind_patch_edge(const ForceArgs<real> &a, const 
     if (!candidate<real>(B, R, M, a.buf.snap_a, a.buf.snap_b, a.buf.snap_c, li1 + R.off, li2 + R.off, o1, o2))
         return;
     add_edge_t<real>(a, wp1, wp2, cls, stamp);
+}
+
+// bind_patch_edge in float only, for the listed edge pass (bind_pairs_kernel): the same decision where every
+// float test is clear of its margin; a patch pair with a float test within a margin goes to the recheck list
+// (wp1 of particle s1, wp2 of s2) for bind_recheck_kernel, which repeats it with the FP64 tests.  With no FP64
+// code and no call the pass keeps its values in registers.  Both patches' bond states and both snapshot rows
+// are read before any of them is used, so a patch pair waits on memory once for all of them (reading the
+// adjacency counters there too, for compare-and-swaps issued together, measured a little slower).
+__device__ __forceinline__ void bind_patch_edge_f(const ForceArgs<float> &a, const BindRep &B, const Replica<float> &R,
+                                                  const Model<float> &M, int li1, int li2, int ty1, int ty2, int ka,
+                                                  int kb, float c1, float c2, float rr, int t0, unsigned stamp) {
+    const int q = M.pstart[ty1][ty2] + ka * M.np[ty2] + kb;
+    const int e1 = side_of<float>(c1, B.ctm_lo[q], B.ctm_hi[q]), e2 = side_of<float>(c2, B.ctm_lo[q], B.ctm_hi[q]);
+    if (e1 < 0 || e2 < 0) return;
+    const int wp1 = patch_of<float>(B, M, li1, ty1, ka), wp2 = patch_of<float>(B, M, li2, ty2, kb);
+    const bool b1 = a.bind_on[wp1] != 0, b2 = a.bind_on[wp2] != 0;
+    const int bt1 = a.bind_to[wp1], bt2 = a.bind_to[wp2];
+    Payload<float> A, C;
+    A.load(a.buf.snap_a, a.buf.snap_b, a.buf.snap_c, li1 + R.off);
+    C.load(a.buf.snap_a, a.buf.snap_b, a.buf.snap_c, li2 + R.off);
+    const int cls = range_class(b1, b2, bt1, bt2, wp1, wp2);
+    const float dfl = cls == 1 ? 0.5f * B.disp_f[q] : (cls == 2 ? 0.7f * B.disp_f[q] : B.disp_f[q]);
+    const int e3 = side_of<float>(rr, dfl * (1.f - 1e-5f), dfl * (1.f + 1e-5f));
+    if (e3 > 0) return;
+    const int w = (t0 < 0 && e1 > 0 && e2 > 0 && e3 < 0)
+                      ? candidate_side<float>(B, R, M, A, C, M.ooff[ty1] + ka, M.ooff[ty2] + kb) : 0;
+    if (w < 0) return;
+    if (w == 0) seg_append<int2>(a.bind_recheck, a.bind_ctr + kSegRecheck, a.bind_rcap, make_int2(wp1, wp2), a.flags);
+    else add_edge_t<float>(a, wp1, wp2, cls, stamp);
 }
 
 // Every edge of the particle pair (s1, s2), s1 the lower particle index, d = x1 - x2 (minimum image) and

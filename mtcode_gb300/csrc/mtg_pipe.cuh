@@ -594,11 +594,11 @@ __global__ void __launch_bounds__(kPipeThreads, 4) patch_pairs_kernel(ForceArgs<
 }
 
 // single-bond mode, a bond-deciding pass: this update's edges of the pairs pairforce_kernel<kPairBind> listed
-// (canonical order, both particles with a patch near a cone), one pair per thread: every listed pair has
-// passed the cone pre-test, so the lanes of a warp run the patch-pair loop together and overlap the
-// bond-state, snapshot and adjacency accesses of their pairs.  Capped at 64 registers (four blocks per SM):
-// the kernel waits on dependent loads and atomics, and more resident warps hide more of that than the few
-// spills (rare branches) cost.
+// (canonical order, both particles with a patch near a cone), one pair per thread, in float
+// (bind_patch_edge_f; bind_recheck_kernel takes the patch pairs within a margin): every listed pair has passed
+// the cone pre-test, so the lanes of a warp run the patch-pair loop together and overlap the bond-state,
+// snapshot and adjacency accesses of their pairs.  Four blocks per SM (64 registers): the kernel waits on
+// dependent loads and atomics, and more resident warps hide more of that.
 __global__ void __launch_bounds__(kPipeThreads, 4) bind_pairs_kernel(ForceArgs<float> a, const int2 *list_all,
                                                                    long long cap) {
     __shared__ long long segs[kSegs + 1];
@@ -612,7 +612,78 @@ __global__ void __launch_bounds__(kPipeThreads, 4) bind_pairs_kernel(ForceArgs<f
         const Replica<float> &R = a.tb.reps[r];
         const BindRep &B = a.bind_reps[r];
         const Model<float> &M = a.tb.models[R.model];
-        float x1[4], x2[4];
+        // both particles' rows and indices are read before any is used: the pair waits on memory once
+        float x1[4], x2[4], Q1[9], Q2[9];
+        load4(a.buf.pos + 4 * (size_t)s1, x1);
+        load4(a.buf.pos + 4 * (size_t)s2, x2);
+        load_q(a, s1, 0.f, Q1);
+        load_q(a, s2, 0.f, Q2);
+        const int id1 = __ldg(a.buf.ident + s1), id2 = __ldg(a.buf.ident + s2);
+        Q1[8] = x1[3];
+        Q2[8] = x2[3];
+        const float d[3] = {min_image_sep<float>(x1[0], x2[0], R.box, R.box_lo, R.l2s, R.periodic),
+                            min_image_sep<float>(x1[1], x2[1], R.box, R.box_lo, R.l2s, R.periodic),
+                            min_image_sep<float>(x1[2], x2[2], R.box, R.box_lo, R.l2s, R.periodic)};
+        const float r2 = sep_r2(d[0], d[1], d[2]);
+        const int t0 = side_of<float>(r2, B.mk2_lo, B.mk2_hi);
+        if (t0 > 0) continue;
+        const int li1 = id1 - R.off, li2 = id2 - R.off;
+        const int ty1 = type_of<float>(M, li1), ty2 = type_of<float>(M, li2);
+        const float rr = sqrtf(r2), u[3] = {d[0] / rr, d[1] / rr, d[2] / rr};
+        float w1[3], w2[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            w1[k] = Q1[3 * k] * u[0] + Q1[3 * k + 1] * u[1] + Q1[3 * k + 2] * u[2];
+            w2[k] = Q2[3 * k] * u[0] + Q2[3 * k + 1] * u[1] + Q2[3 * k + 2] * u[2];
+        }
+        const float pre = M.mincos[ty1][ty2] - 4e-5f;
+        // the patches of each particle near a cone, as masks; the combinations are then taken in mask order,
+        // so that every lane of a warp handles its first combination in the same round (usually the only one)
+        // and the warp waits on the edge's memory accesses once, not once per combination some lane has
+        const int na = M.np[ty1], nb = M.np[ty2];
+        unsigned m1 = 0u, m2 = 0u;
+        for (int k = 0; k < na; k++) {
+            const float *v = M.orient[M.ooff[ty1] + k];
+            if (-(v[0] * w1[0] + v[1] * w1[1] + v[2] * w1[2]) > pre) m1 |= 1u << k;
+        }
+        for (int k = 0; k < nb; k++) {
+            const float *v = M.orient[M.ooff[ty2] + k];
+            if (v[0] * w2[0] + v[1] * w2[1] + v[2] * w2[2] > pre) m2 |= 1u << k;
+        }
+        if (!m2) m1 = 0u;
+        for (; m1; m1 &= m1 - 1u) {
+            const int ka = __ffs(m1) - 1;
+            const float *va = M.orient[M.ooff[ty1] + ka];
+            const float c1 = -(va[0] * w1[0] + va[1] * w1[1] + va[2] * w1[2]);
+            for (unsigned mb = m2; mb; mb &= mb - 1u) {
+                const int kb = __ffs(mb) - 1;
+                const float *vb = M.orient[M.ooff[ty2] + kb];
+                const float c2 = vb[0] * w2[0] + vb[1] * w2[1] + vb[2] * w2[2];
+                bind_patch_edge_f(a, B, R, M, li1, li2, ty1, ty2, ka, kb, c1, c2, rr, t0, stamp);
+            }
+        }
+    }
+}
+
+// single-bond mode, after bind_pairs_kernel: the patch pairs whose float tests fell within a margin, one per
+// thread, through bind_patch_edge (the FP64 edge and candidate tests where the float ones are not clear).  The
+// list holds a few pairs per ten thousand edges tested.
+__global__ void __launch_bounds__(kPipeThreads) bind_recheck_kernel(ForceArgs<float> a) {
+    __shared__ long long segs[kSegs + 1];
+    seg_prefix(a.bind_ctr + kSegRecheck, a.bind_rcap, segs);
+    const long long n = segs[kSegs];
+    const unsigned stamp = (unsigned)a.bind_ctr[2];
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int2 e = a.bind_recheck[seg_slot(segs, a.bind_rcap, q)];
+        const int r = patch_replica(a.bind_reps, a.tb.nrep, e.x);
+        const Replica<float> &R = a.tb.reps[r];
+        const BindRep &B = a.bind_reps[r];
+        const Model<float> &M = a.tb.models[R.model];
+        int li1, ty1, ka, li2, ty2, kb;
+        patch_owner<float>(B, M, e.x - B.patch_off, li1, ty1, ka);
+        patch_owner<float>(B, M, e.y - B.patch_off, li2, ty2, kb);
+        const int s1 = a.buf.slot_of[R.off + li1], s2 = a.buf.slot_of[R.off + li2];
+        float x1[4], x2[4], Q[9], w1[3], w2[3];
         load4(a.buf.pos + 4 * (size_t)s1, x1);
         load4(a.buf.pos + 4 * (size_t)s2, x2);
         const float d[3] = {min_image_sep<float>(x1[0], x2[0], R.box, R.box_lo, R.l2s, R.periodic),
@@ -620,30 +691,17 @@ __global__ void __launch_bounds__(kPipeThreads, 4) bind_pairs_kernel(ForceArgs<f
                             min_image_sep<float>(x1[2], x2[2], R.box, R.box_lo, R.l2s, R.periodic)};
         const float r2 = sep_r2(d[0], d[1], d[2]);
         const int t0 = side_of<float>(r2, B.mk2_lo, B.mk2_hi);
-        if (t0 > 0) continue;
-        const int li1 = __ldg(a.buf.ident + s1) - R.off, li2 = __ldg(a.buf.ident + s2) - R.off;
-        const int ty1 = type_of<float>(M, li1), ty2 = type_of<float>(M, li2);
         const float rr = sqrtf(r2), u[3] = {d[0] / rr, d[1] / rr, d[2] / rr};
-        float Q[9], w1[3], w2[3];
         load_q(a, s1, x1[3], Q);
 #pragma unroll
         for (int k = 0; k < 3; k++) w1[k] = Q[3 * k] * u[0] + Q[3 * k + 1] * u[1] + Q[3 * k + 2] * u[2];
         load_q(a, s2, x2[3], Q);
 #pragma unroll
         for (int k = 0; k < 3; k++) w2[k] = Q[3 * k] * u[0] + Q[3 * k + 1] * u[1] + Q[3 * k + 2] * u[2];
-        const float pre = M.mincos[ty1][ty2] - 4e-5f;
-        const int na = M.np[ty1], nb = M.np[ty2];
-        for (int ka = 0; ka < na; ka++) {
-            const float *va = M.orient[M.ooff[ty1] + ka];
-            const float c1 = -(va[0] * w1[0] + va[1] * w1[1] + va[2] * w1[2]);
-            if (!(c1 > pre)) continue;
-            for (int kb = 0; kb < nb; kb++) {
-                const float *vb = M.orient[M.ooff[ty2] + kb];
-                const float c2 = vb[0] * w2[0] + vb[1] * w2[1] + vb[2] * w2[2];
-                if (!(c2 > pre)) continue;
-                bind_patch_edge<float>(a, B, R, M, s1, s2, li1, li2, ty1, ty2, ka, kb, c1, c2, rr, t0, stamp);
-            }
-        }
+        const float *va = M.orient[M.ooff[ty1] + ka], *vb = M.orient[M.ooff[ty2] + kb];
+        const float c1 = -(va[0] * w1[0] + va[1] * w1[1] + va[2] * w1[2]);
+        const float c2 = vb[0] * w2[0] + vb[1] * w2[1] + vb[2] * w2[2];
+        bind_patch_edge<float>(a, B, R, M, s1, s2, li1, li2, ty1, ty2, ka, kb, c1, c2, rr, t0, stamp);
     }
 }
 

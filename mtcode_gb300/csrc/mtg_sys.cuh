@@ -316,6 +316,8 @@ struct Sys : SysBase {
     int2 *d_bind_pairs = nullptr;   // pairs the FP32 pipeline lists for the edge pass
     int2 *d_bound = nullptr;        // pairs bound by the decisions (FP32 pipeline)
     long long tcap = 0, bcap = 0, lcap = 0;   // segment capacities: touched, bound, listed pairs
+    int2 *d_recheck = nullptr;                 // patch pairs for the FP64 tests of the float edge pass
+    long long rcap = 0;
     int ncells_full = 0;                         // the force grid's cells outside single-bond mode
     unsigned long long *d_bctr = nullptr, *d_deg = nullptr;
     int2 *d_adj = nullptr;
@@ -648,7 +650,8 @@ struct Sys : SysBase {
     void free_bind() {
         cudaFree(d_brep); cudaFree(d_bmodel); cudaFree(d_patch_slot); cudaFree(d_boundto); cudaFree(d_large);
         cudaFree(d_scratch); cudaFree(d_bctr); cudaFree(d_deg); cudaFree(d_adj); cudaFree(d_isbound);
-        cudaFree(d_touched); cudaFree(d_bind_pairs); cudaFree(d_bound);
+        cudaFree(d_touched); cudaFree(d_bind_pairs); cudaFree(d_bound); cudaFree(d_recheck);
+        d_recheck = nullptr;
         d_touched = nullptr;
         d_bind_pairs = nullptr;
         d_bound = nullptr;
@@ -804,6 +807,10 @@ struct Sys : SysBase {
         MTG_CUDA(cudaMalloc(&d_touched, sizeof(int) * (size_t)tcap * mtg::kSegs));
         if (use_pipe) {
             MTG_CUDA(cudaMalloc(&d_bind_pairs, sizeof(int2) * (size_t)lcap * mtg::kSegs));
+            // patch pairs within a margin of a float threshold: a few per ten thousand tested; room for one
+            // per 16 patches
+            rcap = std::max<long long>(1024, ((long long)np / 16 + mtg::kSegs - 1) / mtg::kSegs);
+            MTG_CUDA(cudaMalloc(&d_recheck, sizeof(int2) * (size_t)rcap * mtg::kSegs));
             MTG_CUDA(cudaMalloc(&d_bound, sizeof(int2) * (size_t)bcap * mtg::kSegs));
         }
         MTG_CUDA(cudaMalloc(&d_scratch, sizeof(int) * (size_t)mtg::kScratchInts * scratch_threads));
@@ -1002,6 +1009,8 @@ struct Sys : SysBase {
             a.bind_ctr = d_bctr;
             a.bind_touched = d_touched;
             a.bind_tcap = tcap;
+            a.bind_recheck = d_recheck;
+            a.bind_rcap = rcap;
             a.bind_listed = listed ? 1 : 0;
         }
         auto decide = [&]() {
@@ -1064,6 +1073,7 @@ struct Sys : SysBase {
                         a, d_pairs, d_npairs, pair_cap, d_acc, d_bind_pairs, lcap);
                     mark(2);
                     mtg::bind_pairs_kernel<<<g_patch, mtg::kPipeThreads, 0, st>>>(a, d_bind_pairs, lcap);
+                    mtg::bind_recheck_kernel<<<sms, mtg::kPipeThreads, 0, st>>>(a);
                     decide();
                     mtg::bound_pairs_kernel<<<sms * 4, mtg::kPipeThreads, 0, st>>>(a, d_bound, bcap, d_acc);
                 }
@@ -1083,7 +1093,7 @@ struct Sys : SysBase {
                 else mtg::pair_epilogue_kernel<real, MODE, 256><<<ge, 256, 0, st>>>(a, d_acc);
             }
             mark(4);
-            counted(bind_pass ? 6 : 5);  // (enqueue_bind_decide counts its own)
+            counted(bind_pass ? 7 : 5);  // (enqueue_bind_decide counts its own)
             return;
         }
         if constexpr (std::is_same<real, float>::value) {
