@@ -128,11 +128,12 @@ def test_full_size_batch_newton_third_law_and_finiteness(kernel):
 
 
 @pytest.mark.parametrize("kernel,single_bond,per_step", [("pairs", False, 9), ("tiled", False, 5),
-                                                         ("per_particle", False, 5), ("pairs", True, 14)])
+                                                         ("per_particle", False, 5), ("pairs", True, 15)])
 def test_launch_count_per_step(kernel, single_bond, per_step):
     """mtg_launches counts every kernel a step replays: scans (3) + scatter + the force pass (pair pipeline:
-    reset, pairfind, pairforce, patch pairs, epilogue; single-bond mode: bind begin, the edge and bound-pair
-    passes and the three decision kernels instead of the patch pairs), plus one launch per mtg_step call
+    reset, pairfind, pairforce, patch pairs, epilogue; single-bond mode: bind begin, the edge pass, its FP64
+    recheck, the three decision kernels and the bound-pair pass instead of the patch pairs), plus one launch
+    per mtg_step call
     that sets the device's noise-draw counter."""
     from mtcode_gb300.system import binding_single
     W = small_batch(seed=6, n_replicas=4)
