@@ -285,6 +285,11 @@ __global__ void __launch_bounds__(256) bind_unbind_kernel(BindState S) {
 // clusters of two or three: the walk from one patch with an edge
 __device__ __forceinline__ void decide_one(const BindState &S, int p, unsigned stamp) {
     const int d = adj_count(S.deg, p, stamp);
+    // a patch with a partner below it is not its component's smallest patch, so it decides nothing (a cluster
+    // of two or three is decided by its smallest patch, a larger one queued by a patch below all its partners):
+    // it leaves before the walk
+    for (int k = 0; k < d; k++)
+        if (S.adj[(size_t)p * kAdjCap + k].x < p) return;
     // breadth-first walk of p's component, stopped at a fourth member
     int m[4], nm = 1, lo = p;
     m[0] = p;
@@ -300,9 +305,7 @@ __device__ __forceinline__ void decide_one(const BindState &S, int p, unsigned s
             }
         }
     }
-    if (nm > 3) {  // larger cluster: its smallest patch decides; only patches below all their partners queue
-        for (int k = 0; k < d; k++)
-            if (S.adj[(size_t)p * kAdjCap + k].x < p) return;
+    if (nm > 3) {  // larger cluster: its smallest patch decides; patches below all their partners (p) queue
         const unsigned long long at = atomicAdd(S.ctr + 1, 1ull);
         if ((long long)at < (long long)S.ptot) S.large[at] = p;
         return;
