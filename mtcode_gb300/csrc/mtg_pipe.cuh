@@ -667,7 +667,7 @@ __global__ void __launch_bounds__(kPipeThreads, 4) bind_pairs_kernel(ForceArgs<f
 
 // single-bond mode, after bind_pairs_kernel: the patch pairs whose float tests fell within a margin, one per
 // thread, through bind_patch_edge (the FP64 edge and candidate tests where the float ones are not clear).  The
-// list holds a few pairs per ten thousand edges tested.
+// margins are a few 1e-5 wide, so the list is short: of the order of one patch pair per thousand tested.
 __global__ void __launch_bounds__(kPipeThreads) bind_recheck_kernel(ForceArgs<float> a) {
     __shared__ long long segs[kSegs + 1];
     seg_prefix(a.bind_ctr + kSegRecheck, a.bind_rcap, segs);

@@ -807,8 +807,8 @@ struct Sys : SysBase {
         MTG_CUDA(cudaMalloc(&d_touched, sizeof(int) * (size_t)tcap * mtg::kSegs));
         if (use_pipe) {
             MTG_CUDA(cudaMalloc(&d_bind_pairs, sizeof(int2) * (size_t)lcap * mtg::kSegs));
-            // patch pairs within a margin of a float threshold: a few per ten thousand tested; room for one
-            // per 16 patches
+            // patch pairs within a margin of a float threshold (margins a few 1e-5 wide: of the order of one
+            // per thousand tested); room for one per 16 patches, and a full segment latches MTG_FLAG_BIND
             rcap = std::max<long long>(1024, ((long long)np / 16 + mtg::kSegs - 1) / mtg::kSegs);
             MTG_CUDA(cudaMalloc(&d_recheck, sizeof(int2) * (size_t)rcap * mtg::kSegs));
             MTG_CUDA(cudaMalloc(&d_bound, sizeof(int2) * (size_t)bcap * mtg::kSegs));
