@@ -290,6 +290,25 @@ __device__ __forceinline__ void decide_one(const BindState &S, int p, unsigned s
     // it leaves before the walk
     for (int k = 0; k < d; k++)
         if (S.adj[(size_t)p * kAdjCap + k].x < p) return;
+    if (d == 1) {
+        // the common cluster, a doublet: p's one partner w has p as its one partner.  Both bond states are read
+        // with w's degree, so the decision waits on memory once after p's own row.  The bond-breaking checks
+        // of the general path leave no trace here: the decision writes both bound flags, and "already bound"
+        // needs the two bound to each other, which no check breaks
+        const int w = S.adj[(size_t)p * kAdjCap].x;
+        const int dw = adj_count(S.deg, w, stamp);
+        const bool bp = S.isbound[p] != 0, bw = S.isbound[w] != 0;
+        const int btp = S.boundto[p], btw = S.boundto[w];
+        const int r = find_replica(S.patch_slot, S.nrep, p);
+        if (dw == 1) {
+            const BindRep &B = S.reps[r];
+            const double ran = bind_uniform(B, r, S.draw[0], p - B.patch_off, 0);
+            const bool already = bp && bw && btp == w && btw == p;
+            if (doublet(*S.model, already, p - B.patch_off, w - B.patch_off, ran)) set_pair(S, p, w);
+            else S.isbound[p] = S.isbound[w] = 0;
+            return;
+        }
+    }
     // breadth-first walk of p's component, stopped at a fourth member
     int m[4], nm = 1, lo = p;
     m[0] = p;
