@@ -434,8 +434,8 @@ def run_e2e(s, W, args, stream, ev0, ev1, batched: bool = True) -> dict:
         raise RuntimeError("e2e: non-finite temperatures or state")
     h2d = n * (3 + 3 + 3 + 9 + 3 + 3) * 8
     d2h_state = n * (3 + 3 + 3 + 9 + 3 + 3) * 8
-    what = ("mtg_set_state (host FP64 state) + mtg_step_temperatures (each step's temperatures to pinned host "
-            "memory as the step completes) + mtg_get_state at the end" if batched else
+    what = ("mtg_set_state (host FP64 state) + mtg_step_temperatures (each step's temperatures summed on the "
+            "device and read back to pinned host memory) + mtg_get_state at the end" if batched else
             "mtg_set_state (host FP64 state) + per step: mtg_step(1) + mtg_temperature (synchronous read-back) "
             "+ mtg_get_state at the end")
     return {"value": n * k_e2e / wall, "unit": UNIT, "h2d_bytes_per_step": h2d / k_e2e,

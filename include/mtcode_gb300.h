@@ -206,11 +206,11 @@ mtg_status mtg_pairs(mtg_system *h, int replica, double rc, int32_t *pairs, int6
 mtg_status mtg_temperature(mtg_system *h, double *out);
 
 /* nsteps steps of mtg_step, each followed by mtg_temperature's per-replica sums of that step, as
- * Condensate::run measures the temperature every step (Condensate.cpp:335-378).  Every step's sums are
- * copied to pinned host memory as the step completes (an asynchronous copy per step, no host round trip
- * between steps); the call synchronises once at the end.  out: nsteps x n_replicas x 6, step-major.
- * The copies land in a pinned staging buffer of the same size (kept for later calls): for long runs,
- * call it in blocks of steps.  A failed pinned allocation returns MTG_ERR_CUDA. */
+ * Condensate::run measures the temperature every step (Condensate.cpp:335-378).  Every step's sums stay
+ * on the device (a ring of at most 32 MB) and are copied to pinned host memory once per chunk of steps (no
+ * host round trip between steps); the call synchronises once at the end.  out: nsteps x n_replicas x 6,
+ * step-major.  The copies land in a pinned staging buffer of the same size (kept for later calls): for
+ * long runs, call it in blocks of steps.  A failed allocation returns MTG_ERR_CUDA. */
 mtg_status mtg_step_temperatures(mtg_system *h, int nsteps, double *out);
 
 /* Per-replica FP64 observables at the current state, out: n_replicas x MTG_OBS_COUNT:

@@ -263,6 +263,8 @@ struct Sys : SysBase {
     unsigned *h_flags = nullptr; // pinned
     double *h_obs = nullptr;     // pinned: temperature read-backs (one slot of 6 x nrep per step)
     size_t h_obs_cap = 0;
+    double *d_tring = nullptr;   // device ring of per-step temperature sums (mtg_step_temperatures)
+    size_t d_tring_cap = 0;
     uint64_t draw = 0;
     bool have_state = false, cells_valid = false, bins_valid = false, forces_ready = false;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -474,6 +476,7 @@ struct Sys : SysBase {
         cudaFree(d_reps); cudaFree(d_reps_obs); cudaFree(d_models); cudaFree(d_rep_slot); cudaFree(d_slot_rep);
         cudaFree(d_bin); cudaFree(d_count); cudaFree(d_start); cudaFree(d_block);
         cudaFree(d_flags); cudaFree(d_draw); cudaFree(d_stage); cudaFree(d_noise); cudaFree(d_obs);
+        cudaFree(d_tring);
         cudaFree(d_tiles);
         cudaFree(d_bond_start); cudaFree(d_bond_partner); cudaFree(d_slot_of); cudaFree(d_gather_map);
         cudaFree(d_skin); cudaFree(d_list); cudaFree(d_list_n); cudaFree(d_home_cell); cudaFree(d_xref);
@@ -1392,13 +1395,7 @@ struct Sys : SysBase {
             }
             MTG_CUDA(cudaStreamSynchronize(st));
         } else {
-            for (int s = 0; s < nsteps; s++) {
-                if (!graph[cur]) build_graph(cur);
-                MTG_CUDA(cudaGraphLaunch(graph[cur], st));
-                nlaunch += graph_kernels[cur];
-                if (skin <= 0) cur ^= 1;
-                draw += 1;
-            }
+            for (int s = 0; s < nsteps; s++) replay_step();
         }
         cells_valid = true;
         bins_valid = true;
@@ -1619,14 +1616,18 @@ struct Sys : SysBase {
         MTG_CUDA(cudaStreamSynchronize(st));
     }
 
-    // the per-replica sums of p^2 and L^2 at the current state into pinned host memory (asynchronous)
-    void enqueue_temperature(double *h_dst) {
-        MTG_CUDA(cudaMemsetAsync(d_obs, 0, sizeof(double) * 6 * nrep, st));
+    // the per-replica sums of p^2 and L^2 at the current state, added to d_dst (6 x nrep doubles, zeroed)
+    void enqueue_temperature_sums(double *d_dst) {
         const int chunk = 256 * mtg::kTempPerThread;
         mtg::temperature_kernel<real><<<std::max(1, (ntot_ + chunk - 1) / chunk), 256, 0, st>>>(tables(), buf[cur],
-                                                                                              d_obs);
+                                                                                              d_dst);
         check_launch();
         nlaunch += 1;
+    }
+    // the same sums into pinned host memory (asynchronous)
+    void enqueue_temperature(double *h_dst) {
+        MTG_CUDA(cudaMemsetAsync(d_obs, 0, sizeof(double) * 6 * nrep, st));
+        enqueue_temperature_sums(d_obs);
         MTG_CUDA(cudaMemcpyAsync(h_dst, d_obs, sizeof(double) * 6 * nrep, cudaMemcpyDeviceToHost, st));
     }
     // sums -> <p_k^2/2m>, <L_k^2/2I> of each replica
@@ -1658,13 +1659,45 @@ struct Sys : SysBase {
         return *h_flags;
     }
 
+    // one more step of the captured step graph, after a step() call has set the device draw counter
+    void replay_step() {
+        if (!graph[cur]) build_graph(cur);
+        MTG_CUDA(cudaGraphLaunch(graph[cur], st));
+        nlaunch += graph_kernels[cur];
+        if (skin <= 0) cur ^= 1;
+        draw += 1;
+    }
+
+    // Every step's sums go to a device ring, zeroed once and copied back once per chunk of steps (at most
+    // 32 MB of sums), so that a step adds only the reduction kernel to its graph; the caller sees the same
+    // values, since the call returns after its last copy.
     uint32_t step_temperatures(int nsteps, double *out) override {
         if (!have_state) throw Fail{MTG_ERR_STATE, "mtg_step_temperatures: no state has been set"};
         const size_t per = (size_t)6 * nrep;
         ensure_obs_ring(per * (size_t)std::max(nsteps, 1));
-        for (int s = 0; s < nsteps; s++) {
-            step(1, nullptr);
-            enqueue_temperature(h_obs + per * (size_t)s);  // stream order: step s's copy precedes step s+1's sums
+        const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)std::max(nsteps, 1),
+                                                                    (32u << 20) / (sizeof(double) * per)));
+        if (nsteps > 0 && d_tring_cap < per * (size_t)chunk) {
+            cudaFree(d_tring);
+            d_tring = nullptr;
+            d_tring_cap = 0;
+            MTG_CUDA(cudaMalloc(&d_tring, sizeof(double) * per * (size_t)chunk));
+            d_tring_cap = per * (size_t)chunk;
+        }
+        for (int s0 = 0; s0 < nsteps; s0 += chunk) {
+            const int ns = std::min(chunk, nsteps - s0);
+            MTG_CUDA(cudaMemsetAsync(d_tring, 0, sizeof(double) * per * (size_t)ns, st));
+            for (int s = 0; s < ns; s++) {
+                if (s0 + s == 0) step(1, nullptr);   // forces, bins and the device draw counter, then one step
+                else replay_step();
+                enqueue_temperature_sums(d_tring + per * (size_t)s);
+            }
+            MTG_CUDA(cudaMemcpyAsync(h_obs + per * (size_t)s0, d_tring, sizeof(double) * per * (size_t)ns,
+                                     cudaMemcpyDeviceToHost, st));
+        }
+        if (nsteps > 0) {
+            cells_valid = true;
+            bins_valid = true;
         }
         MTG_CUDA(cudaMemcpyAsync(h_flags, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
         MTG_CUDA(cudaStreamSynchronize(st));

@@ -359,7 +359,8 @@ class LangevinNVTRGPU:
 
     def step_temperatures(self, nsteps: int) -> np.ndarray:
         """nsteps steps, each followed by measured_temperature of that step: (nsteps, replicas, 6).  The
-        per-step sums reach pinned host memory as each step completes; one synchronisation at the end."""
+        per-step sums stay on the device and reach pinned host memory once per chunk of steps; one
+        synchronisation at the end."""
         out = np.empty((int(nsteps), len(self.replicas), 6))
         _check(self._h, _lib.lib().mtg_step_temperatures(self._h, int(nsteps), dptr(out)))
         return out

@@ -234,6 +234,28 @@ def test_step_temperatures_equal_the_step_by_step_read_back(precision):
     assert got[-1].min() > 0
 
 
+def test_step_temperatures_across_ring_chunks():
+    """The per-step sums of mtg_step_temperatures wait in a device ring of at most 32 MB, copied back once per
+    chunk of steps: 3,000 replicas (144 KB of sums a step, 233 steps a chunk) over 250 steps cross a chunk
+    boundary, and every step still equals mtg_step(1) + mtg_temperature."""
+    nrep, n, nsteps = 3000, 12, 250
+    specs = [tetra_spec(n, 0.2) for _ in range(nrep)]
+    x = np.concatenate([random_positions(n, specs[0].box, True, 0.95, 100 + r) for r in range(nrep)])
+    Q = np.concatenate([random_rotations(n, 200 + r) for r in range(nrep)])
+    z = np.zeros((nrep * n, 3))
+    with LangevinNVTRGPU(specs) as s:
+        s.initialize(x, z, z, Q)
+        got = s.step_temperatures(nsteps)
+    want = []
+    with LangevinNVTRGPU(specs) as s:
+        s.initialize(x, z, z, Q)
+        for _ in range(nsteps):
+            s.step(1)
+            want.append(s.measured_temperature())
+    assert got.shape == (nsteps, nrep, 6)
+    np.testing.assert_allclose(got, np.array(want), rtol=1e-12, atol=0)
+
+
 @pytest.mark.parametrize("precision,kernel", [("fp32", "pairs"), ("fp32", "tiled"), ("fp64", "pairs")])
 def test_temperature_after_steps_matches_oracle(precision, kernel):
     """After steps, mtg_temperature / mtg_step_temperatures (the pair pipeline's epilogue sums where that
