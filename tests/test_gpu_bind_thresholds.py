@@ -140,3 +140,35 @@ def test_bond_decisions_at_thresholds_match_oracle(seed, precision, kernel):
             assert s.flags == 0
             formed += int(sum(io[16 * g] and bo[16 * g] == 16 * g + 4 for g in range(GROUPS)))   # A0-B0
     assert formed > 0   # some A0-B0 bonds form, so a wrong edge decision would show
+
+
+@pytest.mark.gpu
+def test_bond_decisions_at_thresholds_batched():
+    """Three threshold systems in one FP32 handle (pair pipeline): the recheck kernel finds each listed patch
+    pair's replica from its global patch index; every replica's bond state equals the oracle's update of that
+    replica (its own Philox stream)."""
+    from mtcode_gb300 import LangevinNVTRGPU
+    from mtcode_gb300.system import binding_single
+    from tests.test_gpu_singlebond import oracle_update
+
+    cases = [build(seed, "fp32") for seed in (21, 22, 23)]
+    specs = [c[0] for c in cases]
+    x = np.concatenate([c[1] for c in cases])
+    Q = np.concatenate([c[2] for c in cases])
+    bt0 = np.concatenate([c[3] for c in cases])   # replica-local partner indices
+    ib0 = np.concatenate([c[4] for c in cases])
+    z = np.zeros((len(x), 3))
+    B = po.binding_single(1.0, 0.1)
+    with LangevinNVTRGPU(specs, precision="fp32", force_kernel="pairs") as s:
+        s.set_single_bond(binding_single(1.0, 0.1))
+        s.initialize(x, z, z, Q)
+        s.set_bind_state(bt0, ib0)
+        draw = s.draw
+        s.bind_update()
+        bt, ib = s.get_bind_state()
+        assert s.flags == 0
+        for r, (spec, xr, Qr, btr, ibr, _) in enumerate(cases):
+            o, npatch = s.patch_offset(r), 4 * spec.n
+            bo, io, _, _ = oracle_update(po.System(spec), B, xr, Qr, btr, ibr, draw, replica=r)
+            assert np.array_equal(ib[o:o + npatch], io), f"replica {r}"
+            assert np.array_equal(bt[o:o + npatch][io == 1], bo[io == 1]), f"replica {r}"
