@@ -198,40 +198,62 @@ __device__ __forceinline__ bool cone_any(const Model<real> &M, int ty, const rea
 // `list` when both particles have a patch near a cone, or -- KIND kPairBind -- onto `list` in canonical order
 // when both do (single-bond mode).  List entries are staged in the block's lbuf (block_list_put).
 // rhint >= 0: sa's replica, known to the caller.
+// The WCA core of the pair (sa, sb) into both particles' sums: FP32 as exact-ish float-float components summed
+// in fixed point, FP64 in double.
+template <class real>
+__device__ __forceinline__ void wca_core(const ForceArgs<real> &a, const Replica<real> &R, int sa, int sb,
+                                         const real d[3], real r2, typename PairAcc<real>::type *acc, bool &big) {
+    typename PairAcc<real>::type fa[3] = {0, 0, 0};
+    if constexpr (sizeof(real) == 4) {
+        float hi[3], lo[3];
+        hs_force_ff(R, d, hi, lo);
+        big |= hi[0] * hi[0] + hi[1] * hi[1] + hi[2] * hi[2] > 1e8f;   // |f| > 1e4
+#pragma unroll
+        for (int k = 0; k < 3; k++) fa[k] = to_fixed(hi[k]) + to_fixed(lo[k]);
+    } else {
+        const real s_ = hs_force_over_r<real>(R, r2);
+        big |= fabs(s_ * sqrt_r(r2)) > real(1e4);
+        fa[0] = s_ * d[0];
+        fa[1] = s_ * d[1];
+        fa[2] = s_ * d[2];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        acc_add_raw(acc + 6 * (size_t)sa + k, fa[k]);
+        acc_add_raw(acc + 6 * (size_t)sb + k, -fa[k]);
+    }
+}
+
+// the separation of the pair (sa, sb) in replica R: d = x_a - x_b (minimum image), returns |d|^2
+template <class real>
+__device__ __forceinline__ real pair_sep(const ForceArgs<real> &a, const Replica<real> &R, int sa, int sb, real d[3],
+                                         real xa[4], real xb[4]) {
+    load4(a.buf.pos + 4 * (size_t)sa, xa);
+    load4(a.buf.pos + 4 * (size_t)sb, xb);
+    d[0] = min_image_sep<real>(xa[0], xb[0], R.box, R.box_lo, R.l2s, R.periodic);
+    d[1] = min_image_sep<real>(xa[1], xb[1], R.box, R.box_lo, R.l2s, R.periodic);
+    d[2] = min_image_sep<real>(xa[2], xb[2], R.box, R.box_lo, R.l2s, R.periodic);
+    return sep_r2<real>(d[0], d[1], d[2]);
+}
+
+// wca: null evaluates the WCA core here; else *wca tells whether the pair needs it, for the caller to
+// evaluate later (wca_core)
 template <class real, int KIND>
 __device__ __forceinline__ void pair_core(const ForceArgs<real> &a, int sa, int sb, typename PairAcc<real>::type *acc,
                                           int2 *lbuf, int *lnb, int2 *list, long long list_cap,
-                                          unsigned long long *lcounts, unsigned lflag, bool &big, int rhint = -1) {
+                                          unsigned long long *lcounts, unsigned lflag, bool &big, int rhint = -1,
+                                          bool *wca = nullptr) {
     constexpr bool BIND = KIND == kPairBind;
     const int r = rhint >= 0 ? rhint : (a.tb.uniform ? 0 : replica_of(a.tb, sa));
     const Replica<real> &R = a.tb.reps[r];
-    real xa[4], xb[4];
-    load4(a.buf.pos + 4 * (size_t)sa, xa);
-    load4(a.buf.pos + 4 * (size_t)sb, xb);
-    const real d[3] = {min_image_sep<real>(xa[0], xb[0], R.box, R.box_lo, R.l2s, R.periodic),
-                       min_image_sep<real>(xa[1], xb[1], R.box, R.box_lo, R.l2s, R.periodic),
-                       min_image_sep<real>(xa[2], xb[2], R.box, R.box_lo, R.l2s, R.periodic)};
-    const real r2 = sep_r2<real>(d[0], d[1], d[2]);
+    real xa[4], xb[4], d[3];
+    const real r2 = pair_sep<real>(a, R, sa, sb, d, xa, xb);
     if (!(r2 < R.rc2)) return;  // skin lists hold pairs up to the list range
     const real rr = sqrt_r(r2);
-    // the WCA core (patch terms come from the pair lists' kernels): FP32 as exact-ish float-float components
-    // summed in fixed point, FP64 in double
-    typename PairAcc<real>::type fa[3] = {0, 0, 0};
-    if (rr < R.hs_limit && (a.parts & 1)) {
-        if constexpr (sizeof(real) == 4) {
-            float hi[3], lo[3];
-            hs_force_ff(R, d, hi, lo);
-            big |= hi[0] * hi[0] + hi[1] * hi[1] + hi[2] * hi[2] > 1e8f;   // |f| > 1e4
-#pragma unroll
-            for (int k = 0; k < 3; k++) fa[k] = to_fixed(hi[k]) + to_fixed(lo[k]);
-        } else {
-            const real s_ = hs_force_over_r<real>(R, r2);
-            big |= fabs(s_ * rr) > real(1e4);
-            fa[0] = s_ * d[0];
-            fa[1] = s_ * d[1];
-            fa[2] = s_ * d[2];
-        }
-    }
+    // the WCA core (patch terms come from the pair lists' kernels)
+    const bool core = rr < R.hs_limit && (a.parts & 1);
+    if (wca) *wca = core;
+    else if (core) wca_core<real>(a, R, sa, sb, d, r2, acc, big);
     if (BIND) {
         // along d = x_a - x_b: a's cosines are -(n_a . d) / r and b's (n_b . d) / r in either canonical order
         const Model<real> &M = a.tb.models[R.model];
@@ -280,11 +302,6 @@ __device__ __forceinline__ void pair_core(const ForceArgs<real> &a, int sa, int 
                 }
             }
         }
-    }
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        acc_add_raw(acc + 6 * (size_t)sa + k, fa[k]);
-        acc_add_raw(acc + 6 * (size_t)sb + k, -fa[k]);
     }
 }
 
@@ -550,9 +567,42 @@ __global__ void __launch_bounds__(THREADS, sizeof(real) == 4 ? (FUSED ? 1280 : 1
         unsigned long long *const lcounts = STAGE == kPairBind ? a.bind_ctr + kSegPairs : list_counts;
         const unsigned lflag = STAGE == kPairBind ? (kFlagBind | kBindWhyList) : 8u;
         bool big = false;
-        for (int i = lane; i < n; i += 32)
-            pair_core<real, STAGE == kPairBind ? kPairBind : kPairSplit>(a, part[i].x, part[i].y, acc, lbuf, &lnb,
-                                                                           list, list_cap, lcounts, lflag, big, rhint);
+        constexpr int K = STAGE == kPairBind ? kPairBind : kPairSplit;
+        if constexpr (sizeof(real) == 4 && K == kPairBind) {
+            // FP32 bond-deciding passes (pairs out to max_check): the pairs inside the WCA range (about one in
+            // eight) are taken out first and their float-float core evaluated afterwards with every lane on one,
+            // instead of by the few lanes of each round that have one while the rest wait: 2.04 -> 2.02 ms a
+            // step.  (In the force pass, whose pairs reach only the force range, it measured 0.5% slower.)  They
+            // are compacted into the front of the warp's own part: a round's entries are in registers before
+            // the __syncwarp, and the writes stay below the round's end.
+            int nw = 0;
+            for (int base = 0; base < n; base += 32) {
+                const int i = base + lane;
+                int2 pr = make_int2(0, 0);
+                bool w = false;
+                if (i < n) {
+                    pr = part[i];
+                    pair_core<real, K>(a, pr.x, pr.y, acc, lbuf, &lnb, list, list_cap, lcounts, lflag, big, rhint,
+                                       &w);
+                }
+                const unsigned m = __ballot_sync(full, w);
+                __syncwarp();
+                if (w) part[nw + __popc(m & ((1u << lane) - 1u))] = pr;
+                nw += __popc(m);
+                __syncwarp();
+            }
+            for (int j = lane; j < nw; j += 32) {
+                const int2 pr = part[j];
+                const int r1 = rhint >= 0 ? rhint : (a.tb.uniform ? 0 : replica_of(a.tb, pr.x));
+                const Replica<real> &R = a.tb.reps[r1];
+                real xa[4], xb[4], d[3];
+                const real r2 = pair_sep<real>(a, R, pr.x, pr.y, d, xa, xb);
+                wca_core<real>(a, R, pr.x, pr.y, d, r2, acc, big);
+            }
+        } else {
+            for (int i = lane; i < n; i += 32)
+                pair_core<real, K>(a, part[i].x, part[i].y, acc, lbuf, &lnb, list, list_cap, lcounts, lflag, big, rhint);
+        }
         if (big) atomicOr(a.flags, 2u);
         block_list_flush(lbuf, &lnb, &lbase, list, lcounts, list_cap, a.flags, lflag);
         return;
