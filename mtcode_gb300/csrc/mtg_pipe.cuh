@@ -358,8 +358,15 @@ __device__ __forceinline__ void patch_terms(const ForceArgs<real> &a, int sa, in
     real f[3] = {real(0), real(0), real(0)}, t1[3] = {real(0), real(0), real(0)},
          t2[3] = {real(0), real(0), real(0)}, e = real(0);
     int nbond = 0;
-    if (a_first) patch_pair<real>(M, tya, tyb, Qa, Qb, u, rr, R.bond_r, f, t1, t2, e, nbond);
-    else patch_pair<real>(M, tyb, tya, Qb, Qa, u, rr, R.bond_r, f, t1, t2, e, nbond);
+    // the canonical first particle's rows and type by selects, not by a branch around two copies of the patch
+    // code (each copy ran with the half of the lanes whose pairs had that order)
+    real Q1[9], Q2[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        Q1[k] = a_first ? Qa[k] : Qb[k];
+        Q2[k] = a_first ? Qb[k] : Qa[k];
+    }
+    patch_pair<real>(M, a_first ? tya : tyb, a_first ? tyb : tya, Q1, Q2, u, rr, R.bond_r, f, t1, t2, e, nbond);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         fixed_add(acc + 6 * (size_t)sa + k, sg * f[k]);
